@@ -1,0 +1,316 @@
+#!/usr/bin/env python3
+"""Benchmark of the PanSim per-timestep agent loop on GB300.
+
+Metric: agent-steps/s on the 2M-agent workload (2,000,000 agents, 500,000
+non-home locations plus homes, dt = 10 min, FP32 infectiousness, uint32
+location ids, seeded synthetic population).  One bench step = one simulated
+day: the midnight phases (progression, statistics, daily plan) and the 144
+timesteps of movement -> regrouping -> infection, launched as one CUDA graph.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Under torchrun every rank runs its own replica of the workload (replicas only:
+the path does not shard a single population), value = all ranks' agent-steps
+/ the slowest rank's time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_AGENTS = 2_000_000
+N_OTHER_LOCS = 500_000
+METRIC = "agent-steps/s at 2M agents"
+UNIT = "agent-steps/s"
+# algorithmic bytes per step (per agent, per location) of the whole step,
+# 32*N + 20*L, and of each kernel of the step
+STEP_BYTES = (32, 20)
+KERNEL_BYTES = {"movement": (20, 4), "scan": (0, 30), "scatter_draw": (22, 0)}
+KERNEL_NAMES = ["movement", "scan", "scatter_draw"]
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def committed_traffic():
+    """dram bytes per launch of the dominant kernel from the committed ncu summary, or None."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(p) as f:
+            return json.load(f)
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    def __init__(self, gpu_index):
+        self.f = tempfile.NamedTemporaryFile(prefix="clocks_", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(gpu_index), "--query-gpu=" + q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except Exception:
+                self.p.kill()
+        self.f.close()
+        rows = []
+        try:
+            for line in open(self.f.name):
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        except Exception:
+            pass
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for n, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def make_snapshot(rank):
+    from pansim_gb300 import synth
+    return synth.make_snapshot(N_AGENTS, N_OTHER_LOCS, seed=1 + rank, model_seed=0x5EED0000, pop_seed=0x5EED0002)
+
+
+def pinned_copy(snap):
+    """Snapshot whose mutable arrays live in pinned host memory (torch.pin_memory)."""
+    import torch
+    from pansim_gb300.snapshot import AGENT_MUTABLE, LOC_MUTABLE
+    s = snap.copy()
+    pins = []
+
+    def pin(a):
+        t = torch.empty(max(a.nbytes, 1), dtype=torch.uint8, pin_memory=True)
+        v = t.numpy()[: a.nbytes].view(a.dtype).reshape(a.shape)
+        v[...] = a
+        pins.append(t)
+        return v
+
+    for k in AGENT_MUTABLE:
+        s.agents[k] = pin(s.agents[k])
+    for k in LOC_MUTABLE:
+        s.locs[k] = pin(s.locs[k])
+    s._pins = pins
+    return s
+
+
+def mutable_bytes(snap):
+    from pansim_gb300.snapshot import AGENT_MUTABLE, LOC_MUTABLE
+    return sum(snap.agents[k].nbytes for k in AGENT_MUTABLE) + sum(snap.locs[k].nbytes for k in LOC_MUTABLE)
+
+
+def cpu_baseline(snap, steps=24):
+    """The oracle port, single thread, on `steps` timesteps of the same workload."""
+    from oracle import binding as ob
+    s = snap.copy()
+    o = ob.Oracle(s)
+    o.midnight(0)
+    t0 = time.perf_counter()
+    for t in range(steps):
+        o.step(t)
+    dt = time.perf_counter() - t0
+    o.close()
+    return {"value": s.n_agents * steps / dt, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": "%d timesteps from midnight of day 0 of the 2M-agent workload (oracle port, 1 thread)" % steps,
+            "seconds": round(dt, 3)}
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return 0
+    from oracle import binding as ob
+    snap = make_snapshot(0)
+    o = ob.Oracle(snap)
+    o.midnight(0)
+    per_step_ts = 6  # timesteps per bench step: a bounded sample of a day
+    t = 0
+    for _ in range(args.warmup):
+        for _ in range(per_step_ts):
+            o.step(t)
+            t += 1
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for _ in range(per_step_ts):
+            o.step(t)
+            t += 1
+    dt = time.perf_counter() - t0
+    value = snap.n_agents * per_step_ts * args.steps / dt
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt * 1000 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "2M agents, 500k non-home locations, dt 10 min", "agents": snap.n_agents,
+                       "locations": snap.n_locations, "timesteps_per_step": per_step_ts},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
+                             "sample": "%d timesteps per step of the 2M-agent workload, oracle port" % per_step_ts},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=7)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, ws, rank)
+
+    import numpy as np
+    import torch
+    from pansim_gb300 import native
+
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    snap = make_snapshot(rank)
+    host_snap = snap.copy() if (rank == 0 and not args.no_cpu_baseline) else None
+    g = native.GpuSim(snap, device=local)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    ext = torch.cuda.ExternalStream(g.stream())
+    day = 0
+    for _ in range(args.warmup):
+        g.run_day(day)
+        day += 1
+    # per-kernel timing (roofline): CUDA events around each kernel on the library's stream
+    kt = []
+    t_probe = day * 144
+    for j in range(12):
+        kt.append(g.time_step_kernels(t_probe + j))
+    kms = np.mean(np.array(kt[2:]), axis=0)
+    g.run_day(day)  # resynchronise the day
+    day += 1
+    sampler = ClockSampler(local)
+    launches0 = g.launch_count()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    total_ms = 0.0
+    for _ in range(args.steps):
+        flush.fill_(1.0)  # L2 flush between timed days (buffer 2x L2)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        g.run_day(day)
+        e1.record(ext)
+        e1.synchronize()
+        total_ms += e0.elapsed_time(e1)
+        day += 1
+    torch.cuda.synchronize()
+    launches = g.launch_count() - launches0
+    clocks = sampler.stop()
+    t_max = total_ms
+    if dist:
+        tt = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max = float(tt.item())
+    agent_steps = snap.n_agents * 144 * args.steps * ws
+    value = agent_steps / (t_max / 1000.0)
+
+    # end to end through the C ABI with pinned host buffers: per step, the
+    # full mutable state host->device, one day, the full state device->host
+    e2e = None
+    if rank == 0 and args.e2e_steps > 0:
+        g.download()  # current state into snap
+        ps = pinned_copy(snap)
+        ge = native.GpuSim(ps, device=local)
+        ge.run_day(day)
+        nb = mutable_bytes(ps)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for j in range(args.e2e_steps):
+            ge.upload()
+            ge.run_day(day + 1 + j)
+            ge.download()
+        te = time.perf_counter() - t0
+        e2e = {"value": ps.n_agents * 144 * args.e2e_steps / te, "unit": UNIT,
+               "h2d_bytes_per_step": nb, "d2h_bytes_per_step": nb}
+        ge.close()
+
+    if rank == 0:
+        peak, peak_kind = peaks()
+        N, L = snap.n_agents, snap.n_locations
+        kern = {}
+        for name, ms in zip(KERNEL_NAMES, kms):
+            bn, bl = KERNEL_BYTES[name]
+            b = bn * N + bl * L
+            kern[name] = {"ms": float(ms), "alg_bytes": b, "gbs": b / (ms * 1e-3) / 1e9}
+        step_ms = float(np.sum(kms))
+        step_bytes = STEP_BYTES[0] * N + STEP_BYTES[1] * L
+        dom = max(kern, key=lambda k: kern[k]["ms"])
+        tr = committed_traffic()
+        traffic = None
+        if tr and dom in tr:
+            traffic = tr[dom]
+        ach = step_bytes / (step_ms * 1e-3) / 1e9
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "2M agents, 500k non-home locations (+homes), dt 10 min, 1 day per step",
+                       "agents": N, "locations": L, "timesteps_per_step": 144,
+                       "l2": "flushed between timed steps (256 MiB write)", "parallelism": "replicas" if ws > 1 else "1 gpu"},
+            "roofline": {"bound": "hbm", "kernel": "step (movement+scan+scatter_draw)", "achieved": ach, "peak": peak,
+                         "unit": "GB/s", "frac": ach / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "alg_bytes_per_launch": step_bytes, "launch_ms": step_ms, "dominant": dom,
+                         "per_kernel": kern},
+            "clocks": clocks, "gpu_launches": int(launches), "e2e": e2e,
+        }
+        if host_snap is not None:
+            line["cpu_baseline"] = cpu_baseline(host_snap)
+        print(json.dumps(line))
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

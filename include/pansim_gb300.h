@@ -1,0 +1,282 @@
+/*
+ * pansim_gb300 — C ABI of the GB300-native PanSim per-timestep agent loop.
+ *
+ * The library replaces the reference's per-step and per-day device work
+ * (khbence/pansim):
+ *   movement        RealMovement::movement        include/policies/movementPolicies.h:1625-1751
+ *                   RealMovementOps::doMovement   include/policies/movementPolicies.h:263-1041
+ *   regrouping      Util::updatePerLocationAgentLists  src/tools/util.cpp:55-108
+ *   infection       BasicInfection::infectionsAtLocations include/policies/infectionPolicies.h:481-588
+ *                   LocationsList::infectAgents   include/locationList.h:233-310
+ *   progression     Simulation::updateAgents      include/simulation.h:425-471
+ *                   DynamicPPState::update        src/agentData/dynamicPPState.cpp:246-303
+ *   daily plan      RealMovement::planLocations   include/policies/movementPolicies.h:1428-1622
+ *   testing         DetailedTesting::performTests include/policies/testingPolicies.h:370-475
+ *   statistics      Simulation::refreshAndPrintStatistics include/simulation.h:473-665
+ *   step loop       Simulation::runSimulation     include/simulation.h:899-926
+ *
+ * Every entry point returns 0 on success and a negative psim_status on
+ * failure; psim_last_error() gives a message.  Only plain pointers, sizes and
+ * POD structs cross the boundary.  Host pointers in psim_snapshot are read by
+ * psim_upload and written by psim_download; device memory is owned by the
+ * context.  All work of a context is issued on its own CUDA stream.
+ */
+#ifndef PANSIM_GB300_H
+#define PANSIM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PSIM_MAX_STRAINS 7   /* MAX_STRAINS, include/datatypes.h:17 */
+#define PSIM_MAX_BANDS 16
+#define PSIM_NO_LOCATION 0xFFFFFFFFu
+
+typedef enum psim_status {
+    PSIM_OK = 0,
+    PSIM_ERR_ARG = -1,        /* invalid argument or inconsistent snapshot */
+    PSIM_ERR_CUDA = -2,       /* a CUDA call failed */
+    PSIM_ERR_ALLOC = -3,      /* device allocation failed */
+    PSIM_ERR_RANGE = -4,      /* out-of-range index found in the snapshot */
+    PSIM_ERR_DEVICE = -5,     /* a kernel reported an error (bounded wait expired) */
+    PSIM_ERR_STATE = -6       /* call out of order (e.g. step before upload) */
+} psim_status;
+
+/* Model tables (immutable during a run).  Progression tables follow
+ * MultiBadMatrix (src/tools/progressionMatrices/multiBadMatrix.cpp:43-83) and
+ * LengthOfState (src/tools/progressionMatrices/basicLengthAbstract.cpp:31-53). */
+typedef struct psim_model {
+    uint32_t n_states;
+    uint32_t n_variants;            /* active strains, <= PSIM_MAX_STRAINS */
+    uint32_t n_prog;                /* progression tables (age band x pre-condition) */
+    uint32_t n_agent_types;
+    uint32_t n_trans;               /* total transition entries */
+    uint32_t n_events;              /* total schedule events */
+    uint32_t first_infected_state;  /* DynamicPPState::gotInfected */
+    uint32_t noncovid_dead_state;
+    uint32_t dead_state;            /* first state with WB == D */
+    uint32_t pad0;
+    /* per state [n_states] */
+    const uint8_t* state_wb;        /* states::WBStates: W=0 N=1 M=2 S=3 D=4 */
+    const float* state_infectious;
+    const uint8_t* state_susceptible;
+    const uint8_t* state_infected;
+    const float* state_acc_pcr;
+    const float* state_acc_antigen;
+    /* per variant [n_variants] */
+    const float* variant_multiplier;  /* --infectiousnessMultiplier */
+    const float* prog_scaling;        /* --diseaseProgressionScaling */
+    const float* death_scaling;       /* --diseaseProgressionDeathScaling */
+    /* progression tables, index (prog * n_states + state) */
+    const uint32_t* tr_bad_begin;
+    const uint32_t* tr_bad_count;
+    const uint32_t* tr_neu_begin;
+    const uint32_t* tr_neu_count;
+    const uint32_t* tr_next;          /* [n_trans] */
+    const float* tr_chance;           /* [n_trans] */
+    /* dwell lengths, index ((prog * n_states + state) * PSIM_MAX_STRAINS + variant) */
+    const float* len_avg;
+    const float* len_max;
+    const double* len_p;              /* geometric p after calculateModifiedP */
+    /* schedules: AgentTypeList (include/agentData/agentType.h:10-45) */
+    const uint32_t* event_offset;     /* [n_agent_types * 28 + 1] */
+    const uint32_t* ev_loc_type;      /* [n_events] */
+    const float* ev_chance;
+    const uint16_t* ev_start;         /* minutes of day, TimeDay semantics */
+    const uint16_t* ev_end;
+    const uint16_t* ev_duration;      /* minutes; >= 25*60 means "until midnight" */
+} psim_model;
+
+/* Agent state, structure of arrays [n_agents] unless noted. */
+typedef struct psim_agents {
+    uint32_t n;
+    uint32_t n_poss;                  /* entries of the per-agent location CSR */
+    /* immutable */
+    const uint8_t* type;              /* agent type index */
+    const uint8_t* age;
+    const uint8_t* band;              /* age band for the band susceptibility */
+    const uint16_t* prog_id;          /* progression table index */
+    const float* symptom_scaling;     /* BasicAgentMeta::getScalingSymptoms */
+    const uint32_t* loc_offset;       /* [n+1] per-agent location CSR */
+    const uint32_t* poss_loc;         /* [n_poss] */
+    const uint8_t* poss_type;         /* [n_poss] location type of each entry */
+    /* mutable */
+    uint32_t* location;
+    uint32_t* steps_until_move;
+    int8_t* state;
+    int16_t* days;                    /* daysBeforeNextState */
+    uint8_t* variant;
+    float* infectious;
+    float* susceptible;               /* [n_variants * n], variant-major */
+    uint8_t* diagnosed;
+    uint8_t* quarantined;
+    uint8_t* stayed_home;
+    uint8_t* no_work;
+    uint32_t* last_test;              /* DetailedTesting::lastTest */
+    /* AgentStats (include/agentData/agentStats.h:5-22) */
+    uint32_t* st_infected_ts;
+    uint32_t* st_infected_loc;
+    uint32_t* st_worst_ts;
+    uint32_t* st_worst_end_ts;
+    uint32_t* st_diagnosed_ts;
+    uint32_t* st_quarantined_ts;
+    uint32_t* st_quarantined_until;
+    uint32_t* st_days_in_quarantine;
+    uint32_t* st_hospitalized_ts;
+    uint32_t* st_hospitalized_until;
+    uint32_t* st_immunization_ts;
+    uint32_t* st_recovered_ts;
+    uint32_t* st_variant_mask;
+    uint8_t* st_immunization_count;
+    uint8_t* st_infected_count;
+    int8_t* st_worst_state;
+} psim_agents;
+
+/* Locations (include/locationList.h:46-67) [n_locations], cemetery last. */
+typedef struct psim_locations {
+    uint32_t n;
+    uint32_t n_schools;
+    uint32_t n_classrooms;
+    uint32_t pad0;
+    const uint8_t* type;
+    float* infectiousness;            /* w_l, multiplied by closure masks */
+    uint8_t* open;                    /* LocationsList::states */
+    const uint8_t* essential;
+    uint32_t* closed_until;
+    uint32_t* quarantine_until;
+    const uint32_t* schools;          /* [n_schools] */
+    const uint32_t* classrooms;       /* [n_classrooms] */
+    const uint32_t* classroom_offsets;/* [n_schools + 1] */
+} psim_locations;
+
+/* Run parameters.  Policies may change the mutable ones between days. */
+typedef struct psim_params {
+    uint32_t time_step;               /* minutes (--deltat) */
+    uint32_t start_day;               /* weekday of day 0, Monday = 0 (--startDay) */
+    uint32_t start_date;              /* day of year of day 0 (--startDate) */
+    uint32_t home_type, work_type, school_type, classroom_type;
+    uint32_t hospital_type, doctor_type, public_type, nursery_type;
+    uint32_t cemetery_loc;
+    uint32_t quarantine_policy;       /* --quarantinePolicy */
+    uint32_t quarantine_length;       /* days, --quarantineLength */
+    uint32_t enable_curfew;
+    uint32_t curfew_begin;            /* in steps of the day */
+    uint32_t curfew_end;              /* in steps of the day */
+    uint32_t school_age_restriction;
+    uint32_t holiday_mode;
+    uint32_t quarantine_immune;
+    uint32_t lockdown_nonvacc;
+    uint32_t testing_enabled;         /* DetailedTesting (1) or NoTesting (0) */
+    uint32_t testing_delay;           /* --testingRepeatDelay */
+    uint32_t use_pcr;
+    uint32_t n_bands;
+    uint32_t tracked;                 /* unused on the device */
+    uint32_t pad0;
+    double k;                         /* --infectionCoefficient */
+    double c0, trunc;                 /* seasonality, infectionPolicies.h:443-478 */
+    int32_t d_offset0, d_offset1, d_peak_offset, n_d_offset;
+    double t_random, t_home, t_work, t_school, t_hospital, t_nursery;
+    uint64_t seed;                    /* Philox key */
+    float sigma_band[PSIM_MAX_BANDS]; /* age-band susceptibility, 1 = reference */
+} psim_params;
+
+/* Replicas batched in one context (BASELINE-style ensembles).  Agents and
+ * locations of replica r occupy [agent_offset[r], agent_offset[r+1]) and
+ * [loc_offset[r], loc_offset[r+1]); location indices in the snapshot are
+ * global.  Each replica has its own Philox key and infection coefficient;
+ * draws are addressed by the agent's index inside its replica, so a replica
+ * gives the same trajectory alone or in a batch.  NULL = one replica made of
+ * the whole snapshot with params->seed, params->k and params->cemetery_loc. */
+typedef struct psim_replicas {
+    uint32_t n;
+    uint32_t pad0;
+    const uint32_t* agent_offset;   /* [n+1] */
+    const uint32_t* loc_offset;     /* [n+1] */
+    const uint64_t* seed;           /* [n] */
+    const double* k;                /* [n] */
+    const uint32_t* cemetery;       /* [n] */
+} psim_replicas;
+
+/* Per-day statistics row, the reference's TSV row (simulation.h:473-665). */
+#define PSIM_STATS_MAX 64
+typedef struct psim_day_stats {
+    uint32_t n;                        /* entries used in v */
+    uint32_t new_infections;           /* NI */
+    uint32_t v[PSIM_STATS_MAX];
+    uint32_t variant_counts[PSIM_MAX_STRAINS]; /* infected per variant (countVariantCases) */
+    double expected_new_infections;    /* sum of infection probabilities since the last midnight */
+} psim_day_stats;
+
+typedef struct psim_ctx psim_ctx;
+
+/* Library */
+const char* psim_version(void);
+/* sizeof of the ABI structs in the order model, agents, locations, params,
+ * replicas, day_stats: lets bindings verify their mirrors. */
+int psim_abi_sizes(uint64_t* out, int n);
+int psim_device_count(int* out);
+
+/* Context: allocates device storage for the snapshot's sizes on device `device`. */
+int psim_create(int device, const psim_model* model, const psim_agents* agents,
+                const psim_locations* locs, const psim_params* params,
+                const psim_replicas* replicas, psim_ctx** out);
+int psim_destroy(psim_ctx* ctx);
+const char* psim_last_error(const psim_ctx* ctx);
+
+/* State transfer: host SoA <-> device SoA (all mutable arrays). */
+int psim_upload(psim_ctx* ctx, const psim_agents* agents, const psim_locations* locs);
+int psim_download(psim_ctx* ctx, psim_agents* agents, psim_locations* locs);
+int psim_set_params(psim_ctx* ctx, const psim_params* params);
+
+/* Per-step phases (runSimulation, simulation.h:918-922). t = timestamp. */
+int psim_movement(psim_ctx* ctx, uint32_t t);          /* doMovement for all agents */
+int psim_regroup(psim_ctx* ctx);                        /* CSR of agents by location */
+int psim_infect(psim_ctx* ctx, uint32_t t, uint32_t variant); /* fused reduce + draw */
+int psim_step(psim_ctx* ctx, uint32_t t);              /* movement + regroup + infection of active variants */
+
+/* Midnight phases (simulation.h:906-917). */
+int psim_test_day(psim_ctx* ctx, uint32_t t, uint32_t* out_tpp /* [replicas*3] or NULL */);
+int psim_progress_day(psim_ctx* ctx, uint32_t t);
+int psim_stats_day(psim_ctx* ctx, uint32_t t, psim_day_stats* out /* [replicas] */);
+int psim_plan_day(psim_ctx* ctx, uint32_t t);
+int psim_midnight(psim_ctx* ctx, uint32_t t, psim_day_stats* out /* [replicas] */);
+
+/* All steps of one day as one CUDA graph launch (captured on first use and
+ * after any psim_set_params / psim_set_tracking). */
+int psim_run_steps(psim_ctx* ctx, uint32_t day);
+/* One day: psim_midnight at t = day*steps_per_day, then psim_run_steps. */
+int psim_run_day(psim_ctx* ctx, uint32_t day, psim_day_stats* out /* [replicas] */);
+
+/* Accumulate the expected new infections (sum of infection probabilities of
+ * susceptible agents, reported in psim_day_stats) during the steps. */
+int psim_set_tracking(psim_ctx* ctx, int expected);
+
+/* Location CSR (LocationsList::locationListOffsets / locationAgentList).
+ * With canonical != 0 each location's agents are sorted by id, which equals
+ * thrust::stable_sort_by_key's output (util.cpp:69). */
+int psim_get_csr(psim_ctx* ctx, int canonical, uint32_t* offsets /*[L+1]*/, uint32_t* agents /*[N]*/);
+/* Per-location hazard r_l of the last psim_infect call (infectionRatios). */
+int psim_get_hazard(psim_ctx* ctx, float* out /*[L]*/, int64_t* fixed_sum /*[L] or NULL*/);
+
+/* One step at timestamp t with a CUDA event around each of its three
+ * kernels (movement, scan, scatter+draw); ms[3] receives their durations. */
+int psim_time_step_kernels(psim_ctx* ctx, uint32_t t, float* ms /* [3] */);
+/* Timing of the last psim_run_steps graph launch, milliseconds. */
+int psim_last_day_ms(psim_ctx* ctx, float* ms);
+/* Counts of kernel launches issued by the library since creation. */
+int psim_launch_count(psim_ctx* ctx, uint64_t* out);
+/* The context's cudaStream_t (as void*), for callers that order their own work after it. */
+int psim_stream_handle(psim_ctx* ctx, void** out);
+/* Runs a device wait on a flag that nothing sets, bounded by `iters`
+ * iterations; returns PSIM_ERR_DEVICE when the bound expires (it always
+ * does) and leaves the context usable.  Exercises the error path of every
+ * bounded wait in the library without faulting the GPU. */
+int psim_bounded_wait_selftest(psim_ctx* ctx, uint32_t iters);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,1047 @@
+/*
+ * CPU oracle for the pansim_gb300 hot path — TEST INFRASTRUCTURE ONLY.
+ * Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it,
+ * as the checker.  Plain C restatement of khbence/pansim, one function per
+ * reference routine (citations are paths inside the reference project).
+ *
+ * Deterministic conventions shared with the GPU path (and stated where the
+ * reference itself has no defined result):
+ *  - random draws: Philox streams of pansim_gb300/csrc/psim_rng.h, one stream
+ *    per (replica seed, agent index within replica, timestamp, phase);
+ *  - location quarantine written during movement is read back only from the
+ *    next step on, and concurrent writes combine with max() (the reference
+ *    races, movementPolicies.h:203,240);
+ *  - setNoWorkToday picks the lowest agent id of a home (what the reference's
+ *    single-threaded CPU loop does; its GPU atomicAdd picks an arbitrary one);
+ *  - per-location sums are the exact 2^-40 fixed-point sums, the hazard is
+ *    1 - exp(-x) in FP64 rounded to FP32 (reference: 1 - expf(x) in FP32,
+ *    infectionPolicies.h:545).
+ * Build: gcc -O2 -ffp-contract=off (no FMA contraction: results must match
+ * the device bit for bit).
+ */
+#include "psim_oracle.h"
+#include "../pansim_gb300/csrc/psim_rng.h"
+#include <stdlib.h>
+#include <string.h>
+#include <math.h>
+
+#define NONE 0xFFFFFFFFu
+#define WB_W 0
+#define WB_N 1
+#define WB_M 2
+#define WB_S 3
+#define WB_D 4
+
+struct psim_oracle {
+    const psim_model* m;
+    psim_agents* a;
+    psim_locations* l;
+    psim_params p;
+    psim_oracle_replicas r;
+    uint32_t* agent_rep;   /* [N] */
+    uint32_t* loc_rep;     /* [L] */
+    uint32_t* csr_off;     /* [L+1] */
+    uint32_t* csr_agents;  /* [N] */
+    uint32_t* qu_pending;  /* [L] */
+    uint32_t* no_work_loc; /* [L] */
+    uint8_t* loc_flags;    /* [L] testing flags */
+    uint8_t* hcw;          /* [N] healthcare workers */
+    uint32_t* hcw_count;   /* [R] */
+    uint32_t* tpp;         /* [R*3] last testing stats */
+    uint32_t* variant_active; /* [R*V] */
+    double* expected;      /* [R] expected infections since the last midnight */
+    uint32_t spd;          /* steps per day */
+};
+
+static inline uint32_t wb_of(const psim_oracle* o, uint32_t i) { return o->m->state_wb[(uint8_t)o->a->state[i]]; }
+static inline int infected_of(const psim_oracle* o, uint32_t i) { return o->m->state_infected[(uint8_t)o->a->state[i]] != 0; }
+
+/* DynamicPPState::updateMeta, src/agentData/dynamicPPState.cpp:54-64 */
+static void update_meta(psim_oracle* o, uint32_t i) {
+    const psim_model* m = o->m;
+    uint8_t s = (uint8_t)o->a->state[i];
+    o->a->infectious[i] = m->state_infectious[s] * m->variant_multiplier[o->a->variant[i]];
+    float su = m->state_susceptible[s] ? 1.0f : 0.0f;
+    for (uint32_t v = 0; v < m->n_variants; ++v) o->a->susceptible[(size_t)v * o->a->n + i] = su;
+}
+
+/* RealMovementOps::findActualLocationForType, movementPolicies.h:69-122 */
+static uint32_t find_location(psim_oracle* o, uint32_t i, uint32_t loc_type, int retry, psim_stream* rng) {
+    const psim_params* p = &o->p;
+    const uint32_t* off = o->a->loc_offset;
+    const uint32_t* pl = o->a->poss_loc;
+    const uint8_t* pt = o->a->poss_type;
+    if (loc_type == p->home_type || loc_type == p->school_type || loc_type == p->work_type) {
+        for (uint32_t k = off[i]; k < off[i + 1]; ++k)
+            if (loc_type == pt[k]) return pl[k];
+        return NONE;
+    }
+    uint32_t counter = 0, pos = 0;
+    for (uint32_t k = off[i]; k < off[i + 1]; ++k) {
+        if (loc_type == pt[k]) {
+            if (counter == 0) pos = k;
+            counter++;
+        }
+    }
+    if (counter == 1) return pl[pos];
+    if (counter > 1) {
+        uint32_t counter2 = counter, rand_idx = counter2;
+        for (;;) {
+            while (rand_idx == counter2) rand_idx = psim_below(rng, counter);
+            counter2 = 0;
+            for (uint32_t k = pos; k < off[i + 1]; ++k) {
+                if (loc_type == pt[k]) {
+                    if (counter2 == rand_idx) {
+                        if (retry && o->l->open[pl[k]] == 0) {
+                            retry = 0;
+                            break;
+                        }
+                        return pl[k];
+                    }
+                    counter2++;
+                }
+            }
+        }
+    }
+    return NONE;
+}
+
+
+static void qu_write(psim_oracle* o, uint32_t loc, uint32_t until) {
+    if (loc == NONE || loc >= o->l->n) return;
+    if (o->qu_pending[loc] < until) o->qu_pending[loc] = until;
+}
+
+/* RealMovementOps::quarantineAgent, movementPolicies.h:176-245 */
+static void quarantine_agent(psim_oracle* o, uint32_t i, uint32_t t, uint32_t until, psim_stream* rng) {
+    const psim_params* p = &o->p;
+    psim_agents* a = o->a;
+    if (p->quarantine_policy == 0) return;
+    if (a->st_diagnosed_ts[i] > 0 && !infected_of(o, i) && !p->quarantine_immune) return;
+    if (!a->diagnosed[i] && a->st_immunization_ts[i] > 0 && !p->quarantine_immune) return;
+    a->quarantined[i] = 1;
+    a->st_quarantined_ts[i] = t;
+    uint32_t prev_until = a->st_quarantined_until[i];
+    a->st_quarantined_until[i] = until;
+    a->st_days_in_quarantine[i] += (until - t) / (24u * 60u / p->time_step);
+    if (a->diagnosed[i]) {
+        uint32_t my_home = find_location(o, i, p->home_type, 0, rng);
+        if (p->quarantine_policy > 1) qu_write(o, my_home, until);
+        if (p->quarantine_policy > 2 && prev_until < t) {
+            uint32_t classroom = find_location(o, i, p->classroom_type, 0, rng);
+            uint32_t work = find_location(o, i, p->work_type, 0, rng);
+            uint32_t to_close[2] = {classroom, work};
+            for (int c = 0; c < 2; ++c) {
+                uint32_t loc = to_close[c];
+                if (loc != NONE && (o->l->type[loc] == p->work_type || o->l->type[loc] == p->classroom_type) &&
+                    o->l->quarantine_until[loc] < t && o->l->open[loc] && o->l->closed_until[loc] < t)
+                    qu_write(o, loc, until);
+            }
+        }
+    }
+}
+
+static inline uint32_t steps_until_midnight(uint32_t minutes, uint32_t dt) { return (1440u - minutes) / dt; }
+
+static int is_quarantine_type(const psim_oracle* o, uint32_t loc) {
+    uint32_t ty = o->l->type[loc];
+    const psim_params* p = &o->p;
+    return ty == p->home_type || ty == p->school_type || ty == p->classroom_type || ty == p->work_type;
+}
+
+static void diagnose_and_quarantine(psim_oracle* o, uint32_t i, uint32_t t, uint32_t minutes, psim_stream* rng) {
+    psim_agents* a = o->a;
+    const psim_params* p = &o->p;
+    a->diagnosed[i] = 1;
+    a->st_diagnosed_ts[i] = t;
+    if (steps_until_midnight(minutes, p->time_step) == 24u * 60u / p->time_step) a->st_diagnosed_ts[i]++;
+    quarantine_agent(o, i, t, t + p->quarantine_length * 24u * 60u / p->time_step, rng);
+}
+
+/* RealMovementOps::doMovement, movementPolicies.h:263-1041 */
+static void do_movement(psim_oracle* o, uint32_t i, uint32_t t, uint32_t minutes, uint32_t day) {
+    psim_agents* a = o->a;
+    const psim_params* p = &o->p;
+    const psim_model* m = o->m;
+    const uint32_t dt = p->time_step;
+    const uint32_t rep = o->agent_rep[i];
+    const uint32_t li = i - o->r.agent_offset[rep];
+    const uint32_t cemetery = o->r.cemetery[rep];
+    const uint32_t agent_type = a->type[i];
+    psim_stream rng;
+    psim_stream_init(&rng, o->r.seed[rep], li, t, PSIM_PHASE_MOVE);
+    const uint32_t sum = steps_until_midnight(minutes, dt);
+
+    /* curfew, :267-326 */
+    if (p->enable_curfew && p->curfew_begin == minutes / dt) {
+        uint32_t wb = wb_of(o, i);
+        int dead_or_hosp = (wb == WB_D || wb == WB_S);
+        int hosp_noncovid = (a->st_hospitalized_ts[i] <= t && a->st_hospitalized_until[i] > t);
+        if (!dead_or_hosp && !hosp_noncovid) {
+            if (agent_type + 1 == 7) {
+                uint32_t workplace = find_location(o, i, p->work_type, 0, &rng);
+                if (a->location[i] != workplace || workplace == NONE || o->l->open[workplace] == 0) {
+                    a->location[i] = find_location(o, i, p->home_type, 0, &rng);
+                    if (workplace == NONE || o->l->open[workplace] == 0) {
+                        a->steps_until_move[i] = sum;
+                        return;
+                    }
+                }
+            } else {
+                a->steps_until_move[i] = sum;
+                a->location[i] = find_location(o, i, p->home_type, 0, &rng);
+                return;
+            }
+        }
+    }
+
+    /* countdown, :328-331 */
+    if (a->steps_until_move[i] > 0) {
+        a->steps_until_move[i]--;
+        return;
+    }
+
+    if (a->st_quarantined_until[i] <= t) a->quarantined[i] = 0;
+
+    uint32_t wb = wb_of(o, i);
+    if (wb == WB_D) {
+        a->steps_until_move[i] = NONE;
+        a->location[i] = cemetery;
+        return;
+    }
+
+    uint32_t agent_home = find_location(o, i, p->home_type, 0, &rng);
+
+    /* non-COVID hospitalization, :355-403 */
+    if (a->st_hospitalized_ts[i] <= t && a->st_hospitalized_until[i] > t && wb != WB_S && wb != WB_D) {
+        uint32_t x = a->st_hospitalized_until[i] - t - 1;
+        a->steps_until_move[i] = x < sum ? x : sum;
+        a->location[i] = find_location(o, i, p->hospital_type, 0, &rng);
+        if (!a->diagnosed[i] && a->infectious[i] != 0.0f) diagnose_and_quarantine(o, i, t, minutes, &rng);
+        return;
+    }
+
+    /* severe: hospital, :405-442 */
+    if (wb == WB_S) {
+        a->steps_until_move[i] = sum;
+        a->location[i] = find_location(o, i, p->hospital_type, 0, &rng);
+        if (!a->diagnosed[i] && a->infectious[i] != 0.0f) diagnose_and_quarantine(o, i, t, minutes, &rng);
+        return;
+    }
+
+    /* location under quarantine, :445-513 */
+    {
+        uint32_t loc = a->location[i];
+        if (p->quarantine_policy > 1 && t < o->l->quarantine_until[loc] && is_quarantine_type(o, loc)) {
+            if (a->quarantined[i] == 0) quarantine_agent(o, i, t, o->l->quarantine_until[loc], &rng);
+            if (a->quarantined[i]) {
+                uint32_t x = o->l->quarantine_until[a->location[i]] - t - 1;
+                a->steps_until_move[i] = x < sum ? x : sum;
+                uint32_t home_location = find_location(o, i, p->home_type, 0, &rng);
+                if (home_location != a->location[i]) a->location[i] = home_location;
+                if (agent_home != NONE && a->location[i] != agent_home && a->steps_until_move[i] > 60u / dt)
+                    a->stayed_home[i] = 0;
+                return;
+            }
+        }
+    }
+
+    /* recent diagnosis, :515-583 */
+    if ((p->quarantine_policy > 0 &&
+         (a->diagnosed[i] || (a->st_diagnosed_ts[i] > 0 &&
+                              (t - a->st_diagnosed_ts[i]) < p->quarantine_length * 24u * 60u / dt))) ||
+        (p->quarantine_policy > 0 && a->quarantined[i])) {
+        if (p->quarantine_policy > 0 && !a->quarantined[i])
+            quarantine_agent(o, i, t, t + p->quarantine_length * 24u * 60u / dt, &rng);
+        if (a->quarantined[i]) {
+            a->location[i] = find_location(o, i, p->home_type, 0, &rng);
+            a->steps_until_move[i] = sum;
+            if (agent_home != NONE && a->location[i] != agent_home && a->steps_until_move[i] > 60u / dt)
+                a->stayed_home[i] = 0;
+            return;
+        }
+    }
+
+    /* schedule window, :585-604 (AgentTypeList::getOffsetIndex, agentType.cpp:13-15) */
+    uint32_t off_idx = 7u * wb + day + agent_type * 28u;
+    uint32_t ev_b = m->event_offset[off_idx], ev_e = m->event_offset[off_idx + 1];
+    int act_b = -1, act_e = -1;
+    for (uint32_t j = ev_b; j < ev_e; ++j) {
+        if (minutes >= m->ev_start[j] && minutes < m->ev_end[j] && act_b == -1) act_b = (int)j;
+        if (minutes < m->ev_start[j]) {
+            act_e = (int)j;
+            break;
+        }
+        if (j == ev_e - 1) {
+            if (minutes >= m->ev_start[j] && minutes < m->ev_end[j]) act_e = (int)ev_e;
+        }
+    }
+
+    uint32_t new_type = NONE;
+    /* Case 1, :634-656 */
+    if (act_b == -1 && act_e == -1) {
+        new_type = wb == WB_S ? p->hospital_type : p->home_type;
+        a->location[i] = find_location(o, i, new_type, 0, &rng);
+        a->steps_until_move[i] = sum;
+    }
+    /* Case 2 and 4, :658-855 */
+    if (act_b != -1) {
+        uint32_t num_pot = (uint32_t)((act_e == -1 ? act_b + 1 : act_e) - act_b);
+        uint32_t picked = 0;
+        uint32_t dur = 0;
+        if (num_pot == 1) {
+            new_type = m->ev_loc_type[act_b];
+            dur = m->ev_duration[act_b];
+        } else {
+            double rnd = psim_u01(&rng) * 1.0;
+            double thr = m->ev_chance[act_b];
+            uint32_t idx = 0;
+            while (rnd > thr && idx < num_pot) {
+                idx++;
+                thr += m->ev_chance[act_b + idx];
+            }
+            if (idx == num_pot) idx--;
+            picked = idx;
+            new_type = m->ev_loc_type[act_b + idx];
+            dur = m->ev_duration[act_b + idx];
+        }
+        if (a->no_work[i] != 0 && new_type == p->work_type) {
+            new_type = p->home_type;
+            num_pot = 1;
+            if (a->quarantined[i] == 0) a->st_days_in_quarantine[i]++;
+        }
+        uint32_t new_loc = find_location(o, i, new_type, num_pot == 1, &rng);
+        int school_too_old = (new_type == p->school_type || new_type == p->classroom_type) &&
+                             a->age[i] >= p->school_age_restriction;
+        if (school_too_old ||
+            ((o->l->open[new_loc] == 0 || o->l->closed_until[new_loc] > t) && new_type != p->work_type) ||
+            (p->lockdown_nonvacc && a->st_immunization_ts[i] == 0)) {
+            if (num_pot > 1) {
+                double rnd = psim_u01(&rng) * 1.0;
+                double thr = (picked == 0) ? 0.0
+                                           : m->ev_chance[act_b] / (1.0 - m->ev_chance[act_b + picked]);
+                uint32_t idx = 0;
+                while (rnd > thr && idx < num_pot) {
+                    idx++;
+                    thr += (picked == idx) ? 0.0
+                                           : m->ev_chance[act_b + idx] / (1.0 - m->ev_chance[act_b + picked]);
+                }
+                if (idx == num_pot) idx--;
+                new_type = m->ev_loc_type[act_b + idx];
+                dur = m->ev_duration[act_b + idx];
+                new_loc = find_location(o, i, new_type, 0, &rng);
+                if (school_too_old ||
+                    ((o->l->open[new_loc] == 0 || o->l->closed_until[new_loc] > t) && new_type != p->work_type) ||
+                    (p->lockdown_nonvacc && a->st_immunization_ts[i] == 0)) {
+                    new_loc = find_location(o, i, p->home_type, 0, &rng);
+                }
+            } else {
+                new_loc = find_location(o, i, p->home_type, 0, &rng);
+            }
+        } else if (new_type == p->school_type) {
+            uint32_t my_class = find_location(o, i, p->classroom_type, 0, &rng);
+            if (my_class != NONE && o->l->closed_until[my_class] > t)
+                new_loc = find_location(o, i, p->home_type, 0, &rng);
+        }
+        a->location[i] = new_loc;
+        if (dur / 60u > 24u) {
+            a->steps_until_move[i] = sum;
+        } else if (act_e == -1) {
+            if (minutes + dur >= 1440u)
+                a->steps_until_move[i] = sum;
+            else
+                a->steps_until_move[i] = dur / dt;
+        } else {
+            uint32_t nstart = m->ev_start[act_e], nend = m->ev_end[act_e];
+            if (minutes + dur < nstart) {
+                a->steps_until_move[i] = dur / dt;
+            } else if (minutes + dur > nend) {
+                a->steps_until_move[i] = (nend - minutes) / dt - 1u;
+            } else {
+                uint32_t st = (nend - (minutes + dur)) / dt;
+                uint32_t extra = psim_below(&rng, st);
+                a->steps_until_move[i] = dur / dt + extra;
+            }
+        }
+        if (agent_type + 1 == 7 && p->enable_curfew &&
+            (p->curfew_begin <= minutes / dt || p->curfew_end > minutes / dt)) {
+            int work_closed = (new_type == p->work_type &&
+                               (o->l->open[new_loc] == 0 || o->l->closed_until[new_loc] > t));
+            if (work_closed || (new_type != p->work_type && new_type != p->home_type)) a->location[i] = agent_home;
+        }
+    }
+    /* Case 3, :858-911 */
+    if (act_b == -1 && act_e != -1) {
+        uint32_t length_steps = (uint32_t)(m->ev_end[act_e] - m->ev_start[act_e]) / dt;
+        uint32_t delay = psim_below(&rng, length_steps);
+        a->steps_until_move[i] = (m->ev_start[act_e] - minutes) / dt + delay;
+        uint32_t left = a->steps_until_move[i];
+        if (left < 30u / dt) {
+            /* 3a: stay */
+        } else if (left < 60u / dt) {
+            new_type = p->public_type;
+            a->location[i] = find_location(o, i, p->public_type, 0, &rng);
+        } else {
+            new_type = p->home_type;
+            a->location[i] = find_location(o, i, p->home_type, 0, &rng);
+        }
+    }
+
+    /* arrived at a quarantined place, :914-977 */
+    {
+        uint32_t loc = a->location[i];
+        if (p->quarantine_policy > 1 && t < o->l->quarantine_until[loc] && is_quarantine_type(o, loc)) {
+            if (!a->quarantined[i]) quarantine_agent(o, i, t, o->l->quarantine_until[loc], &rng);
+            if (a->quarantined[i]) {
+                uint32_t x = o->l->quarantine_until[a->location[i]] - t - 1;
+                a->steps_until_move[i] = x < sum ? x : sum;
+                uint32_t home_location = find_location(o, i, p->home_type, 0, &rng);
+                if (home_location != a->location[i]) a->location[i] = home_location;
+                if (agent_home != NONE && a->location[i] != agent_home && a->steps_until_move[i] > 60u / dt)
+                    a->stayed_home[i] = 0;
+                return;
+            }
+        }
+    }
+
+    /* diagnosis at hospital / doctor, :1012-1033 */
+    if (new_type == p->hospital_type || (new_type == p->doctor_type && psim_u01(&rng) * 1.0 < 0.7)) {
+        if (!a->diagnosed[i] && a->infectious[i] != 0.0f) diagnose_and_quarantine(o, i, t, minutes, &rng);
+    }
+    if (agent_home != NONE && a->location[i] != agent_home && a->steps_until_move[i] > 60u / dt)
+        a->stayed_home[i] = 0;
+    a->steps_until_move[i]--;
+}
+
+static uint32_t day_of_week(const psim_oracle* o, uint32_t t) {
+    if (o->p.holiday_mode) return 6u; /* Days::SUNDAY, movementPolicies.h:1713 */
+    return (o->p.start_day + t / o->spd) % 7u;
+}
+
+/* RealMovement::movement, movementPolicies.h:1625-1724 */
+void psim_oracle_movement(psim_oracle* o, uint32_t t) {
+    uint32_t minutes = (t % o->spd) * o->p.time_step;
+    uint32_t day = day_of_week(o, t);
+    for (uint32_t i = 0; i < o->a->n; ++i) do_movement(o, i, t, minutes, day);
+    /* location quarantine written this step becomes visible from the next one */
+    for (uint32_t l = 0; l < o->l->n; ++l) {
+        if (o->qu_pending[l] > o->l->quarantine_until[l]) o->l->quarantine_until[l] = o->qu_pending[l];
+        o->qu_pending[l] = 0;
+    }
+}
+
+/* Util::updatePerLocationAgentLists, util.cpp:55-108 with the stable sort of
+ * :69: agents grouped by location, ascending agent id within a location. */
+void psim_oracle_regroup(psim_oracle* o) {
+    uint32_t L = o->l->n, N = o->a->n;
+    memset(o->csr_off, 0, sizeof(uint32_t) * (L + 1));
+    for (uint32_t i = 0; i < N; ++i) o->csr_off[o->a->location[i] + 1]++;
+    for (uint32_t l = 0; l < L; ++l) o->csr_off[l + 1] += o->csr_off[l];
+    uint32_t* cur = (uint32_t*)malloc(sizeof(uint32_t) * (L + 1));
+    memcpy(cur, o->csr_off, sizeof(uint32_t) * (L + 1));
+    for (uint32_t i = 0; i < N; ++i) o->csr_agents[cur[o->a->location[i]]++] = i;
+    free(cur);
+}
+
+/* BasicInfection::infectionsAtLocations (infectionPolicies.h:481-546) and
+ * LocationsList::infectAgents (locationList.h:233-310). */
+void psim_oracle_infect(psim_oracle* o, uint32_t t, uint32_t v, float* hazard_f, int64_t* sum_fix,
+                        double* sum64, double* r64, double* p64, double* exp_out) {
+    psim_agents* a = o->a;
+    const psim_params* p = &o->p;
+    const psim_model* m = o->m;
+    uint32_t L = o->l->n, N = a->n;
+    float season_f = (float)psim_oracle_seasonality(p, t, o->spd);
+    double season_d = psim_oracle_seasonality(p, t, o->spd);
+    float* r = (float*)malloc(sizeof(float) * L);
+    for (uint32_t l = 0; l < L; ++l) {
+        uint32_t b = o->csr_off[l], e = o->csr_off[l + 1];
+        int64_t fix = 0;
+        double s64 = 0.0;
+        for (uint32_t j = b; j < e; ++j) {
+            uint32_t ag = o->csr_agents[j];
+            float inf = (a->variant[ag] == v) ? a->infectious[ag] : 0.0f;
+            fix += (int64_t)llrintf(inf * PSIM_FIX_SCALE_F);
+            s64 += (double)inf;
+        }
+        uint32_t rep = o->loc_rep[l];
+        float k_f = (float)o->r.k[rep];
+        float rf = 0.0f;
+        double rd = 0.0;
+        if (fix != 0 && e > b) {
+            double S = (double)fix * PSIM_FIX_INV;
+            double dens = S / (double)(e - b);
+            double x = (double)k_f * dens;
+            x = x * (double)o->l->infectiousness[l];
+            x = x * (double)season_f;
+            x = x * (double)p->time_step;
+            rf = (float)psim_one_minus_exp(x);
+        }
+        if (s64 != 0.0 && e > b) {
+            double x = o->r.k[rep] * (s64 / (double)(e - b)) * (double)o->l->infectiousness[l] * season_d *
+                       (double)p->time_step;
+            rd = -expm1(-x);
+        }
+        r[l] = rf;
+        if (hazard_f) hazard_f[l] = rf;
+        if (sum_fix) sum_fix[l] = fix;
+        if (sum64) sum64[l] = s64;
+        if (r64) r64[l] = rd;
+    }
+    if (exp_out)
+        for (uint32_t q = 0; q < o->r.n; ++q) exp_out[q] = 0.0;
+    for (uint32_t i = 0; i < N; ++i) {
+        uint32_t loc = a->location[i];
+        float su = a->susceptible[(size_t)v * N + i];
+        float s_eff = su * p->sigma_band[a->band[i]];
+        if (p64) {
+            p64[i] = (r64 ? r64[loc] : (double)r[loc]) * (double)su * (double)p->sigma_band[a->band[i]];
+        }
+        if (s_eff > 0.0f) {
+            float pf = r[loc] * s_eff;
+            uint32_t rep = o->agent_rep[i];
+            uint32_t li = i - o->r.agent_offset[rep];
+            double term = pf < 1.0f ? (double)pf : 1.0;
+            o->expected[rep] += term;
+            if (exp_out) exp_out[rep] += term;
+            double U = psim_u01_once(o->r.seed[rep], li, t, PSIM_PHASE_INFECT + v);
+            if (U < (double)pf) {
+                /* DynamicPPState::gotInfected, dynamicPPState.cpp:235-244 */
+                a->state[i] = (int8_t)m->first_infected_state;
+                a->variant[i] = (uint8_t)v;
+                a->days[i] = -2;
+                update_meta(o, i);
+                a->st_infected_ts[i] = t;
+                a->st_infected_count[i]++;
+                a->st_infected_loc[i] = loc;
+                a->st_worst_state[i] = a->state[i];
+                a->st_worst_ts[i] = t;
+                a->st_variant_mask[i] |= 1u << v;
+            }
+        }
+    }
+    free(r);
+}
+
+/* one step of Simulation::runSimulation, simulation.h:918-922 */
+void psim_oracle_step(psim_oracle* o, uint32_t t, const uint32_t* variant_active) {
+    psim_oracle_movement(o, t);
+    psim_oracle_regroup(o);
+    for (uint32_t v = 0; v < o->m->n_variants; ++v) {
+        int any = 0;
+        for (uint32_t q = 0; q < o->r.n; ++q) any |= (variant_active ? variant_active[q * o->m->n_variants + v]
+                                                                    : o->variant_active[q * o->m->n_variants + v]) != 0;
+        if (any) psim_oracle_infect(o, t, v, NULL, NULL, NULL, NULL, NULL, NULL);
+    }
+}
+
+/* LengthOfState::calculateDays, basicLengthAbstract.cpp:48-53 */
+static int calc_days(psim_oracle* o, uint32_t pid, uint32_t state, uint32_t v, psim_stream* rng) {
+    const psim_model* m = o->m;
+    size_t idx = ((size_t)pid * m->n_states + state) * PSIM_MAX_STRAINS + v;
+    if (m->len_avg[idx] == -1.0f) return -1;
+    uint32_t thr = psim_geometric_threshold(m->len_p[idx]);
+    int days = psim_geometric(rng, thr);
+    while (m->len_max[idx] < (float)days) days = psim_geometric(rng, thr);
+    return days;
+}
+
+/* MultiBadMatrix::NextStates::selectNext, multiBadMatrix.cpp:9-31 */
+static uint32_t select_next(psim_oracle* o, uint32_t pid, uint32_t state, float scaling, psim_stream* rng, int* bad) {
+    const psim_model* m = o->m;
+    size_t ti = (size_t)pid * m->n_states + state;
+    uint32_t bb = m->tr_bad_begin[ti], bc = m->tr_bad_count[ti];
+    uint32_t nb = m->tr_neu_begin[ti], nc = m->tr_neu_count[ti];
+    if (nc == 0) scaling = 1.0f;
+    double random = psim_u01(rng);
+    double pre = 0.0, bad_sum = 0.0;
+    for (uint32_t k = 0; k < bc; ++k) {
+        float c = m->tr_chance[bb + k] * scaling;
+        pre += (double)c;
+        if (random < pre) {
+            *bad = 1;
+            return m->tr_next[bb + k];
+        }
+        bad_sum += (double)m->tr_chance[bb + k];
+    }
+    double bad_scaling = 1.0 + ((bad_sum - pre) / (1.0 - bad_sum));
+    if (bc == 0) bad_scaling = 1.0;
+    uint32_t idx = 0;
+    do {
+        double c = (double)m->tr_chance[nb + idx] * bad_scaling;
+        pre += c;
+        ++idx;
+    } while (pre < random && idx < nc);
+    idx--;
+    *bad = 0;
+    return m->tr_next[nb + idx];
+}
+
+/* Simulation::updateAgents (simulation.h:425-471) -> DynamicPPState::update
+ * (dynamicPPState.cpp:246-303) -> MultiBadMatrix::calculateNextState
+ * (multiBadMatrix.cpp:120-125). */
+void psim_oracle_progress(psim_oracle* o, uint32_t t) {
+    psim_agents* a = o->a;
+    const psim_model* m = o->m;
+    const psim_params* p = &o->p;
+    for (uint32_t i = 0; i < a->n; ++i) {
+        uint32_t rep = o->agent_rep[i];
+        uint32_t li = i - o->r.agent_offset[rep];
+        psim_stream rng;
+        psim_stream_init(&rng, o->r.seed[rep], li, t, PSIM_PHASE_PROGRESS);
+        uint32_t v = a->variant[i];
+        uint32_t st = (uint8_t)a->state[i];
+        uint32_t pid = a->prog_id[i];
+        float meta = a->symptom_scaling[i];
+        float prog = (st == 7) ? m->death_scaling[v] / meta : m->prog_scaling[v];
+        float scaling = meta * prog;
+        int recovered = 0;
+        int16_t days = a->days[i];
+        int go = 1;
+        if (days == -2) {
+            days = (int16_t)calc_days(o, pid, st, v, &rng);
+            if (v >= 3) days = (days * 0.7 == 0) ? 1 : (int16_t)(days * 0.7);
+        } else if (days > 0) {
+            --days;
+            go = 0;
+        }
+        if (go && days == 0) {
+            uint32_t old_state = st;
+            int was_infected = m->state_infected[st] != 0;
+            int bad = 0;
+            uint32_t next = select_next(o, pid, st, scaling, &rng, &bad);
+            int nd = calc_days(o, pid, next, v, &rng);
+            a->state[i] = (int8_t)next;
+            update_meta(o, i);
+            days = (int16_t)nd;
+            if (v >= 3 && next < 8) {
+                float mul = next < 6 ? 0.7f : 0.5f;
+                days = (days * mul == 0) ? 1 : (int16_t)(days * mul);
+            }
+            if (bad) {
+                a->st_worst_state[i] = (int8_t)next;
+                a->st_worst_ts[i] = t;
+                a->st_worst_end_ts[i] = t + ((uint32_t)((int)days * 60 * 24)) / p->time_step;
+            } else if (old_state != next) {
+                if (was_infected && !m->state_infected[next]) {
+                    a->st_recovered_ts[i] = t;
+                    recovered = 1;
+                }
+            }
+        }
+        a->days[i] = days;
+        if (recovered) a->diagnosed[i] = 0;
+    }
+}
+
+static int quarantine_window_ok(uint32_t qu, uint32_t t, uint32_t ql_steps, uint32_t day_steps) {
+    /* testingPolicies.h:89-95 */
+    return qu == 0 || (qu != 0 && (qu - ql_steps >= t - day_steps || qu < t));
+}
+
+/* DetailedTesting::performTests, testingPolicies.h:370-475 (flagLocations
+ * :64-148, doTesting :162-281). */
+void psim_oracle_test(psim_oracle* o, uint32_t t, uint32_t* tpp) {
+    psim_agents* a = o->a;
+    const psim_params* p = &o->p;
+    const psim_model* m = o->m;
+    const uint32_t day_steps = 24u * 60u / p->time_step;
+    const uint32_t ql_steps = p->quarantine_length * 24u * 60u / p->time_step;
+    memset(o->loc_flags, 0, o->l->n);
+    for (uint32_t i = 0; i < a->n; ++i) {
+        if (a->st_diagnosed_ts[i] > t - day_steps) {
+            uint32_t rep_ = o->agent_rep[i];
+            psim_stream frng;
+            psim_stream_init(&frng, o->r.seed[rep_], i - o->r.agent_offset[rep_], t, PSIM_PHASE_TEST_FLAG);
+            
+            uint32_t home = find_location(o, i, p->home_type, 0, &frng);
+            if (home != NONE) o->loc_flags[home] = 1;
+            uint32_t work = find_location(o, i, p->work_type, 0, &frng);
+            if (work != NONE && quarantine_window_ok(o->l->quarantine_until[work], t, ql_steps, day_steps))
+                o->loc_flags[work] = 1;
+            uint32_t school = find_location(o, i, p->school_type, 0, &frng);
+            if (school != NONE && quarantine_window_ok(o->l->quarantine_until[school], t, ql_steps, day_steps)) {
+                o->loc_flags[school] = 1;
+                uint32_t classroom = find_location(o, i, p->classroom_type, 0, &frng);
+                if (classroom != NONE &&
+                    quarantine_window_ok(o->l->quarantine_until[classroom], t, ql_steps, day_steps))
+                    o->loc_flags[classroom] = 1;
+            }
+        }
+    }
+    const uint32_t delay_steps = p->testing_delay * 24u * 60u / p->time_step;
+    for (uint32_t i = 0; i < a->n; ++i) {
+        if (t > delay_steps && a->last_test[i] != NONE && a->last_test[i] > t - delay_steps) continue;
+        if (wb_of(o, i) == WB_D || a->diagnosed[i]) continue;
+        uint32_t rep = o->agent_rep[i];
+        uint32_t li = i - o->r.agent_offset[rep];
+        psim_stream rng;
+        psim_stream_init(&rng, o->r.seed[rep], li, t, PSIM_PHASE_TEST);
+        uint32_t home = find_location(o, i, p->home_type, 0, &rng);
+        int home_flag = home != NONE ? o->loc_flags[home] : 0;
+        uint32_t work = find_location(o, i, p->work_type, 0, &rng);
+        int work_flag = work != NONE ? o->loc_flags[work] : 0;
+        uint32_t school = find_location(o, i, p->school_type, 0, &rng);
+        int school_flag = 0, class_flag = 0;
+        if (school != NONE) {
+            school_flag = o->loc_flags[school];
+            uint32_t classroom = find_location(o, i, p->classroom_type, 0, &rng);
+            if (classroom != NONE) class_flag = 1;
+        }
+        double prob = p->t_random;
+        prob = prob + (double)home_flag * p->t_home;
+        prob = prob + (double)work_flag * p->t_work;
+        prob = prob + (double)school_flag * p->t_school;
+        prob = prob + ((double)class_flag * 3.0) * p->t_school;
+        if (work != NONE && (o->l->type[work] == p->doctor_type || o->l->type[work] == p->hospital_type))
+            prob = prob + p->t_hospital;
+        if (work != NONE && o->l->type[work] == p->nursery_type) prob = prob + p->t_nursery;
+        if (a->st_hospitalized_ts[i] <= t && a->st_hospitalized_until[i] > t) prob = prob + p->t_hospital;
+        if (prob > 1.0 || psim_u01(&rng) * 1.0 < prob) {
+            a->last_test[i] = t;
+            if (infected_of(o, i)) {
+                uint8_t st = (uint8_t)a->state[i];
+                float acc = p->use_pcr ? m->state_acc_pcr[st] : m->state_acc_antigen[st];
+                if ((double)acc > psim_u01(&rng) * 1.0) {
+                    a->diagnosed[i] = 1;
+                    a->st_diagnosed_ts[i] = t;
+                }
+            } else {
+                if (a->st_quarantined_until[i] > t && (home != NONE && o->l->quarantine_until[home] < t)) {
+                    if (a->st_days_in_quarantine[i] > 0)
+                        a->st_days_in_quarantine[i] -= (a->st_quarantined_until[i] - t) / day_steps;
+                    a->st_quarantined_until[i] = t;
+                }
+            }
+        }
+    }
+    for (uint32_t q = 0; q < o->r.n; ++q) {
+        uint32_t tests = 0, p1 = 0, p2 = 0;
+        for (uint32_t i = o->r.agent_offset[q]; i < o->r.agent_offset[q + 1]; ++i) {
+            tests += a->last_test[i] == t;
+            p1 += a->st_diagnosed_ts[i] == t;
+            p2 += (a->st_diagnosed_ts[i] < t && a->st_diagnosed_ts[i] > t - day_steps);
+        }
+        o->tpp[q * 3 + 0] = tests;
+        o->tpp[q * 3 + 1] = p1;
+        o->tpp[q * 3 + 2] = p2;
+        if (tpp) {
+            tpp[q * 3 + 0] = tests;
+            tpp[q * 3 + 1] = p1;
+            tpp[q * 3 + 2] = p2;
+        }
+    }
+}
+
+/* Simulation::refreshAndPrintStatistics, simulation.h:473-665, the TSV row
+ * per replica; also countVariantCases (:768-777). */
+void psim_oracle_stats(psim_oracle* o, uint32_t t, psim_day_stats* out) {
+    psim_agents* a = o->a;
+    const psim_model* m = o->m;
+    const psim_params* p = &o->p;
+    const uint32_t S = m->n_states, V = m->n_variants;
+    const uint32_t day_steps = 24u * 60u / p->time_step;
+    for (uint32_t q = 0; q < o->r.n; ++q) {
+        psim_day_stats* d = &out[q];
+        memset(d, 0, sizeof(*d));
+        uint32_t b = o->r.agent_offset[q], e = o->r.agent_offset[q + 1];
+        uint32_t hist[256] = {0};
+        uint32_t hosp = 0, qn = 0, qt = 0, nq = 0, stayed = 0, ni = 0, inf_once = 0, reinf = 0, bstr = 0;
+        uint32_t all_inf = 0, var_inf[PSIM_MAX_STRAINS] = {0}, infv[PSIM_MAX_STRAINS] = {0};
+        double imm[PSIM_MAX_STRAINS] = {0};
+        uint32_t hci = 0, hce = 0, infh = 0, vni = 0;
+        for (uint32_t i = b; i < e; ++i) {
+            uint8_t st = (uint8_t)a->state[i];
+            hist[st]++;
+            uint32_t wb = m->state_wb[st];
+            int inf = m->state_infected[st] != 0;
+            if (wb != WB_D && wb != WB_S && t < a->st_hospitalized_until[i]) hosp++;
+            int isq = a->st_quarantined_ts[i] <= t && a->st_quarantined_until[i] > t;
+            qn += isq;
+            qt += isq && inf;
+            nq += !isq && inf;
+            stayed += a->stayed_home[i] != 0;
+            int new_inf = a->st_infected_ts[i] > t - day_steps && a->st_infected_ts[i] <= t;
+            ni += new_inf;
+            inf_once += a->st_infected_count[i] > 0;
+            reinf += a->st_infected_count[i] > 1 ? a->st_infected_count[i] - 1u : 0u;
+            bstr += a->st_immunization_count[i] > 1 ? a->st_immunization_count[i] - 1u : 0u;
+            if (inf) {
+                all_inf++;
+                var_inf[a->variant[i]]++;
+            }
+            for (uint32_t v = 0; v < V; ++v) {
+                imm[v] += 1.0 - (double)a->susceptible[(size_t)v * a->n + i];
+                if (a->st_variant_mask[i] & (1u << v)) infv[v]++;
+            }
+            if (o->hcw[i]) {
+                hci += (inf || a->quarantined[i]) ? 1u : 0u;
+                hce += new_inf;
+            }
+            if (inf && o->l->type[a->location[i]] == p->hospital_type) infh++;
+            vni += a->st_infected_count[i] == 0 && a->st_immunization_count[i] > 0;
+        }
+        uint32_t n = 0;
+        for (uint32_t s = 0; s < S; ++s) d->v[n++] = hist[s];
+        d->v[n++] = hosp;
+        d->v[n++] = o->tpp[q * 3 + 0];
+        d->v[n++] = o->tpp[q * 3 + 1];
+        d->v[n++] = o->tpp[q * 3 + 2];
+        d->v[n++] = qn;
+        d->v[n++] = qt;
+        d->v[n++] = nq;
+        if (V > 1) {
+            for (uint32_t v = 1; v < V; ++v)
+                d->v[n++] = all_inf ? (uint32_t)((double)var_inf[v] / (double)all_inf * 100.0) : 0u;
+        } else {
+            d->v[n++] = 0;
+        }
+        d->v[n] = stayed - d->v[10] - d->v[11];
+        n++;
+        d->v[n++] = 0; /* immunized today */
+        d->v[n++] = ni;
+        d->v[n++] = inf_once;
+        d->v[n++] = reinf;
+        d->v[n++] = bstr;
+        for (uint32_t v = 0; v < V; ++v) d->v[n++] = (uint32_t)imm[v];
+        d->v[n++] = (hci * 100u) / (o->hcw_count[q] > 1 ? o->hcw_count[q] : 1u);
+        d->v[n++] = hce;
+        for (uint32_t v = 0; v < V; ++v) d->v[n++] = infv[v];
+        d->v[n++] = infh;
+        d->v[n++] = vni;
+        d->n = n;
+        d->new_infections = ni;
+        for (uint32_t v = 0; v < V; ++v) {
+            d->variant_counts[v] = var_inf[v];
+            o->variant_active[q * V + v] = var_inf[v] > 0;
+        }
+        d->expected_new_infections = o->expected[q];
+        o->expected[q] = 0.0;
+    }
+}
+
+/* RealMovement::planLocations, movementPolicies.h:1428-1622 */
+void psim_oracle_plan(psim_oracle* o, uint32_t t) {
+    psim_agents* a = o->a;
+    psim_locations* L = o->l;
+    const psim_params* p = &o->p;
+    for (uint32_t i = 0; i < a->n; ++i) {
+        a->steps_until_move[i] = p->curfew_end;
+        a->stayed_home[i] = 1;
+        a->no_work[i] = 0;
+    }
+    memset(o->no_work_loc, 0, sizeof(uint32_t) * L->n);
+    /* checkSchoolQuarantine, :1285-1310 */
+    if (p->quarantine_policy > 3) {
+        for (uint32_t s = 0; s < L->n_schools; ++s) {
+            uint32_t school = L->schools[s];
+            if (L->quarantine_until[school] > t) continue;
+            uint32_t counter = 0, mx = 0;
+            for (uint32_t c = L->classroom_offsets[s]; c < L->classroom_offsets[s + 1]; ++c) {
+                uint32_t cl = L->classrooms[c];
+                if (L->quarantine_until[cl] > t) {
+                    counter++;
+                    mx = mx > L->quarantine_until[cl] ? mx : L->quarantine_until[cl];
+                }
+            }
+            if (counter > 1) {
+                L->quarantine_until[school] = mx;
+                for (uint32_t c = L->classroom_offsets[s]; c < L->classroom_offsets[s + 1]; ++c)
+                    L->quarantine_until[L->classrooms[c]] = mx;
+            }
+        }
+    }
+    if (p->quarantine_policy > 2) {
+        /* checkSchoolWorkQuarantine, :1188-1240 */
+        for (uint32_t i = 0; i < a->n; ++i) {
+            if (a->quarantined[i]) continue;
+            if (a->st_diagnosed_ts[i] > 0 && !infected_of(o, i)) continue;
+            uint32_t rep_ = o->agent_rep[i];
+            psim_stream frng;
+            psim_stream_init(&frng, o->r.seed[rep_], i - o->r.agent_offset[rep_], t, PSIM_PHASE_PLAN_SWQ);
+            uint32_t work = find_location(o, i, p->work_type, 0, &frng);
+            uint32_t school = find_location(o, i, p->school_type, 0, &frng);
+            uint32_t classroom = find_location(o, i, p->classroom_type, 0, &frng);
+            uint32_t until = 0;
+            if (school != NONE && L->quarantine_until[school] > t)
+                until = L->quarantine_until[school];
+            else if (classroom != NONE && L->quarantine_until[classroom] > t)
+                until = L->quarantine_until[classroom];
+            else if (work != NONE && L->quarantine_until[work] > t)
+                until = L->quarantine_until[work];
+            if (until > 0) {
+                a->quarantined[i] = 1;
+                a->st_quarantined_ts[i] = t;
+                a->st_quarantined_until[i] = until;
+                a->st_days_in_quarantine[i] += (until - t) / (24u * 60u / p->time_step);
+            }
+        }
+        /* :1571-1583 */
+        for (uint32_t l = 0; l < L->n; ++l) {
+            uint32_t ty = L->type[l];
+            if (L->quarantine_until[l] > t && (ty == p->school_type || ty == p->classroom_type)) {
+                L->closed_until[l] = L->quarantine_until[l];
+                L->quarantine_until[l] = 0;
+            } else if (L->quarantine_until[l] > t && ty == p->work_type) {
+                L->quarantine_until[l] = 0;
+            }
+        }
+    }
+    /* checkUnderageAtHome, :1056-1094 */
+    for (uint32_t i = 0; i < a->n; ++i) {
+        if (a->age[i] > 14) continue;
+        uint32_t rep_ = o->agent_rep[i];
+        psim_stream frng;
+        psim_stream_init(&frng, o->r.seed[rep_], i - o->r.agent_offset[rep_], t, PSIM_PHASE_PLAN_UNDERAGE);
+        uint32_t home = find_location(o, i, p->home_type, 0, &frng);
+        if (a->quarantined[i]) {
+            if (home != NONE) o->no_work_loc[home] = 1;
+        } else {
+            uint32_t school = find_location(o, i, p->school_type, 0, &frng);
+            uint32_t classroom = find_location(o, i, p->classroom_type, 0, &frng);
+            int too_old = a->age[i] >= p->school_age_restriction;
+            if (too_old || (school != NONE && (L->open[school] == 0 || L->closed_until[school] > t)) ||
+                (classroom != NONE && (L->open[classroom] == 0 || L->closed_until[classroom] > t))) {
+                if (home != NONE) o->no_work_loc[home] = 1;
+            }
+        }
+    }
+    /* setNoWorkToday, :1137-1158 (sequential: first eligible adult of a home) */
+    for (uint32_t i = 0; i < a->n; ++i) {
+        if (a->age[i] > 26 && a->age[i] < 65) {
+            uint32_t rep_ = o->agent_rep[i];
+            psim_stream frng;
+            psim_stream_init(&frng, o->r.seed[rep_], i - o->r.agent_offset[rep_], t, PSIM_PHASE_PLAN_NOWORK);
+            uint32_t home = find_location(o, i, p->home_type, 0, &frng);
+            if (home != NONE && o->no_work_loc[home] == 1) {
+                o->no_work_loc[home] = 2;
+                a->no_work[i] = 1;
+            }
+        }
+    }
+}
+
+/* the midnight block of runSimulation, simulation.h:906-917 */
+void psim_oracle_midnight(psim_oracle* o, uint32_t t, psim_day_stats* out) {
+    if (t > 0 && o->p.testing_enabled) psim_oracle_test(o, t, NULL);
+    if (t > 0) psim_oracle_progress(o, t);
+    psim_oracle_stats(o, t, out);
+    psim_oracle_plan(o, t);
+}
+
+void psim_oracle_run_day(psim_oracle* o, uint32_t day, psim_day_stats* out) {
+    uint32_t t0 = day * o->spd;
+    psim_oracle_midnight(o, t0, out);
+    for (uint32_t s = 0; s < o->spd; ++s) psim_oracle_step(o, t0 + s, NULL);
+}
+
+/* Simulation::flagHealthcareWorkers, simulation.h:670-693 */
+static void flag_hcw(psim_oracle* o) {
+    psim_agents* a = o->a;
+    memset(o->hcw_count, 0, sizeof(uint32_t) * o->r.n);
+    for (uint32_t i = 0; i < a->n; ++i) {
+        uint8_t f = 0;
+        for (uint32_t k = a->loc_offset[i]; k < a->loc_offset[i + 1]; ++k) {
+            uint32_t lt = o->l->type[a->poss_loc[k]];
+            if (a->poss_type[k] == 4 && (lt == 12 || lt == 14)) {
+                f = 1;
+                break;
+            }
+        }
+        o->hcw[i] = f;
+        o->hcw_count[o->agent_rep[i]] += f;
+    }
+}
+
+psim_oracle* psim_oracle_create(const psim_model* m, psim_agents* a, psim_locations* l, const psim_params* p,
+                                const psim_oracle_replicas* reps) {
+    psim_oracle* o = (psim_oracle*)calloc(1, sizeof(psim_oracle));
+    o->m = m;
+    o->a = a;
+    o->l = l;
+    o->p = *p;
+    o->r = *reps;
+    o->spd = 1440u / p->time_step;
+    o->agent_rep = (uint32_t*)malloc(sizeof(uint32_t) * (a->n ? a->n : 1));
+    o->loc_rep = (uint32_t*)malloc(sizeof(uint32_t) * (l->n ? l->n : 1));
+    for (uint32_t q = 0; q < reps->n; ++q) {
+        for (uint32_t i = reps->agent_offset[q]; i < reps->agent_offset[q + 1]; ++i) o->agent_rep[i] = q;
+        for (uint32_t j = reps->loc_offset[q]; j < reps->loc_offset[q + 1]; ++j) o->loc_rep[j] = q;
+    }
+    o->csr_off = (uint32_t*)calloc(l->n + 1, sizeof(uint32_t));
+    o->csr_agents = (uint32_t*)calloc(a->n ? a->n : 1, sizeof(uint32_t));
+    o->qu_pending = (uint32_t*)calloc(l->n ? l->n : 1, sizeof(uint32_t));
+    o->no_work_loc = (uint32_t*)calloc(l->n ? l->n : 1, sizeof(uint32_t));
+    o->loc_flags = (uint8_t*)calloc(l->n ? l->n : 1, 1);
+    o->hcw = (uint8_t*)calloc(a->n ? a->n : 1, 1);
+    o->hcw_count = (uint32_t*)calloc(reps->n, sizeof(uint32_t));
+    o->tpp = (uint32_t*)calloc(reps->n * 3, sizeof(uint32_t));
+    o->variant_active = (uint32_t*)calloc((size_t)reps->n * m->n_variants, sizeof(uint32_t));
+    o->expected = (double*)calloc(reps->n, sizeof(double));
+    flag_hcw(o);
+    psim_oracle_regroup(o); /* LocationsList::initialize, locationList.h:224-230 */
+    /* countVariantCases before the first day */
+    for (uint32_t i = 0; i < a->n; ++i)
+        if (m->state_infected[(uint8_t)a->state[i]])
+            o->variant_active[o->agent_rep[i] * m->n_variants + a->variant[i]] = 1;
+    return o;
+}
+
+void psim_oracle_set_params(psim_oracle* o, const psim_params* p) { o->p = *p; }
+
+void psim_oracle_destroy(psim_oracle* o) {
+    if (!o) return;
+    free(o->agent_rep);
+    free(o->loc_rep);
+    free(o->csr_off);
+    free(o->csr_agents);
+    free(o->qu_pending);
+    free(o->no_work_loc);
+    free(o->loc_flags);
+    free(o->hcw);
+    free(o->hcw_count);
+    free(o->tpp);
+    free(o->variant_active);
+    free(o->expected);
+    free(o);
+}
+
+const uint32_t* psim_oracle_csr_offsets(psim_oracle* o) { return o->csr_off; }
+const uint32_t* psim_oracle_csr_agents(psim_oracle* o) { return o->csr_agents; }
+
+void psim_oracle_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+    psim_ctr4 c;
+    for (int i = 0; i < 4; ++i) c.v[i] = ctr[i];
+    psim_ctr4 r = psim_philox4x32_10(c, key[0], key[1]);
+    for (int i = 0; i < 4; ++i) out[i] = r.v[i];
+}
+
+double psim_oracle_one_minus_exp(double x) { return psim_one_minus_exp(x); }
+
+/* BasicInfection::seasonalityMultiplier, infectionPolicies.h:443-478 */
+double psim_oracle_seasonality(const psim_params* p, uint32_t t, uint32_t spd) {
+    unsigned sim_day = t / spd;
+    int d = (int)p->start_date + (int)sim_day;
+    int d_peak = 59 + 22;
+    d += 6;
+    double c0 = 3.08;
+    double trunc_val = 0.5;
+    if (sim_day > 250 && sim_day < 450) {
+        d += p->d_offset0;
+        d_peak += p->d_peak_offset;
+        c0 = p->c0;
+    } else if (sim_day > 600) {
+        trunc_val = p->trunc;
+        if (p->n_d_offset > 1) d += p->d_offset1;
+    }
+    int d_mod = d % 366;
+    if (d_mod > 366 / 2) d_mod = 366 - d_mod;
+    double a1 = 0.5 * c0 * cos(2.0 * M_PI * (double)(d_mod - d_peak) / 366.0);
+    double b1 = 1.0 - 0.5 * c0;
+    double a2 = 0.5 * c0 * cos(2.0 * M_PI * (double)(d_peak - d_peak) / 366.0);
+    double normed = (a1 + b1) / (a2 + b1);
+    double calc = normed > trunc_val ? normed : trunc_val;
+    calc = calc < 1.0 ? calc : 1.0;
+    if (d_mod < d_peak) return 1.0;
+    return calc;
+}

@@ -1,0 +1,83 @@
+"""ctypes mirrors of the structs in include/pansim_gb300.h.
+
+Field order and types must match the header exactly; tests compare the sizes
+with the ones the compiled library reports (psim_abi_sizes).
+"""
+import ctypes as C
+
+P = C.c_void_p
+PSIM_MAX_STRAINS = 7
+PSIM_MAX_BANDS = 16
+PSIM_STATS_MAX = 64
+
+
+class PsimModel(C.Structure):
+    _fields_ = [
+        ("n_states", C.c_uint32), ("n_variants", C.c_uint32), ("n_prog", C.c_uint32),
+        ("n_agent_types", C.c_uint32), ("n_trans", C.c_uint32), ("n_events", C.c_uint32),
+        ("first_infected_state", C.c_uint32), ("noncovid_dead_state", C.c_uint32),
+        ("dead_state", C.c_uint32), ("pad0", C.c_uint32),
+        ("state_wb", P), ("state_infectious", P), ("state_susceptible", P), ("state_infected", P),
+        ("state_acc_pcr", P), ("state_acc_antigen", P),
+        ("variant_multiplier", P), ("prog_scaling", P), ("death_scaling", P),
+        ("tr_bad_begin", P), ("tr_bad_count", P), ("tr_neu_begin", P), ("tr_neu_count", P),
+        ("tr_next", P), ("tr_chance", P),
+        ("len_avg", P), ("len_max", P), ("len_p", P),
+        ("event_offset", P), ("ev_loc_type", P), ("ev_chance", P), ("ev_start", P), ("ev_end", P),
+        ("ev_duration", P),
+    ]
+
+
+AGENT_PTR_FIELDS = [
+    "type", "age", "band", "prog_id", "symptom_scaling", "loc_offset", "poss_loc", "poss_type",
+    "location", "steps_until_move", "state", "days", "variant", "infectious", "susceptible",
+    "diagnosed", "quarantined", "stayed_home", "no_work", "last_test",
+    "st_infected_ts", "st_infected_loc", "st_worst_ts", "st_worst_end_ts", "st_diagnosed_ts",
+    "st_quarantined_ts", "st_quarantined_until", "st_days_in_quarantine", "st_hospitalized_ts",
+    "st_hospitalized_until", "st_immunization_ts", "st_recovered_ts", "st_variant_mask",
+    "st_immunization_count", "st_infected_count", "st_worst_state",
+]
+
+
+class PsimAgents(C.Structure):
+    _fields_ = [("n", C.c_uint32), ("n_poss", C.c_uint32)] + [(f, P) for f in AGENT_PTR_FIELDS]
+
+
+LOC_PTR_FIELDS = ["type", "infectiousness", "open", "essential", "closed_until", "quarantine_until",
+                  "schools", "classrooms", "classroom_offsets"]
+
+
+class PsimLocations(C.Structure):
+    _fields_ = [("n", C.c_uint32), ("n_schools", C.c_uint32), ("n_classrooms", C.c_uint32),
+                ("pad0", C.c_uint32)] + [(f, P) for f in LOC_PTR_FIELDS]
+
+
+PARAM_U32 = ["time_step", "start_day", "start_date", "home_type", "work_type", "school_type",
+             "classroom_type", "hospital_type", "doctor_type", "public_type", "nursery_type",
+             "cemetery_loc", "quarantine_policy", "quarantine_length", "enable_curfew", "curfew_begin",
+             "curfew_end", "school_age_restriction", "holiday_mode", "quarantine_immune",
+             "lockdown_nonvacc", "testing_enabled", "testing_delay", "use_pcr", "n_bands", "tracked",
+             "pad0"]
+
+
+class PsimParams(C.Structure):
+    _fields_ = ([(f, C.c_uint32) for f in PARAM_U32] +
+                [("k", C.c_double), ("c0", C.c_double), ("trunc", C.c_double),
+                 ("d_offset0", C.c_int32), ("d_offset1", C.c_int32), ("d_peak_offset", C.c_int32),
+                 ("n_d_offset", C.c_int32),
+                 ("t_random", C.c_double), ("t_home", C.c_double), ("t_work", C.c_double),
+                 ("t_school", C.c_double), ("t_hospital", C.c_double), ("t_nursery", C.c_double),
+                 ("seed", C.c_uint64), ("sigma_band", C.c_float * PSIM_MAX_BANDS)])
+
+
+class PsimReplicas(C.Structure):
+    _fields_ = [("n", C.c_uint32), ("pad0", C.c_uint32), ("agent_offset", P), ("loc_offset", P),
+                ("seed", P), ("k", P), ("cemetery", P)]
+
+
+class PsimDayStats(C.Structure):
+    _fields_ = [("n", C.c_uint32), ("new_infections", C.c_uint32), ("v", C.c_uint32 * PSIM_STATS_MAX),
+                ("variant_counts", C.c_uint32 * PSIM_MAX_STRAINS), ("expected_new_infections", C.c_double)]
+
+
+ABI_STRUCTS = [PsimModel, PsimAgents, PsimLocations, PsimParams, PsimReplicas, PsimDayStats]

@@ -1,0 +1,776 @@
+// C ABI of pansim_gb300 (include/pansim_gb300.h): context lifetime, host<->device
+// transfer of the SoA snapshot, the per-step and per-day phases, and the
+// per-day CUDA graph that replaces the reference's host loop with a
+// cudaDeviceSynchronize after every launch (simulation.h:899-926).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "psim_device.cuh"
+
+using namespace psim;
+
+struct psim_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    KArgs k{};
+    std::vector<void*> allocs;
+    uint32_t N = 0, L = 0, V = 0, R = 0, S = 0, spd = 144;
+    uint64_t n_poss = 0;
+    psim_params params{};
+    std::vector<uint32_t> rep_agent_off, rep_loc_off, rep_cemetery, hcw_count;
+    std::vector<uint64_t> rep_seed;
+    std::vector<double> rep_k;
+    // host copies of the per-day clock
+    DevClock h_clock{};
+    bool clock_valid = false;
+    // graph of the steps of one day
+    cudaGraphExec_t day_graph = nullptr;
+    bool graph_dirty = true;
+    uint64_t graph_kernels = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    float last_ms = 0.f;
+    uint64_t launches = 0;
+    bool uploaded = false;
+    bool csr_fresh = false;      // counts/rank of the current positions are built
+    std::vector<DevStatsAcc> h_stats;
+    std::vector<double> h_expected;
+};
+
+namespace {
+
+const char* kVersion = "pansim_gb300 0.1.0 (sm_103a)";
+
+int fail(psim_ctx* c, int code, const std::string& msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+#define CK(call)                                                                                      \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess)                                                                        \
+            return fail(c, PSIM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));        \
+    } while (0)
+
+template <typename T>
+int dalloc(psim_ctx* c, T** p, size_t count) {
+    size_t bytes = count * sizeof(T);
+    if (bytes == 0) bytes = 16;
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, bytes);
+    if (e != cudaSuccess) return fail(c, PSIM_ERR_ALLOC, std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
+    cudaMemsetAsync(q, 0, bytes, c->stream);
+    c->allocs.push_back(q);
+    *p = (T*)q;
+    return 0;
+}
+
+template <typename T>
+int dcopy_in(psim_ctx* c, const T* dptr, const T* host, size_t count) {
+    if (count == 0) return 0;
+    if (!host) return fail(c, PSIM_ERR_ARG, "missing host array");
+    CK(cudaMemcpyAsync((void*)dptr, host, count * sizeof(T), cudaMemcpyHostToDevice, c->stream));
+    return 0;
+}
+
+template <typename T>
+int dupload(psim_ctx* c, const T** dst, const T* host, size_t count) {
+    T* d = nullptr;
+    int rc = dalloc(c, &d, count);
+    if (rc) return rc;
+    rc = dcopy_in(c, d, host, count);
+    if (rc) return rc;
+    *dst = d;
+    return 0;
+}
+
+int check_device_err(psim_ctx* c) {
+    uint32_t e = 0;
+    CK(cudaMemcpyAsync(&e, c->k.err, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (e) {
+        CK(cudaMemsetAsync(c->k.err, 0, sizeof(uint32_t), c->stream));
+        std::string m = "device error flags 0x" + std::to_string(e) + ":";
+        if (e & ERR_SCAN_WAIT) m += " scan look-back wait expired;";
+        if (e & ERR_LOCATION) m += " agent on an invalid location;";
+        if (e & ERR_TEST_WAIT) m += " bounded wait expired;";
+        return fail(c, PSIM_ERR_DEVICE, m);
+    }
+    return 0;
+}
+
+int launch_check(psim_ctx* c) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(c, PSIM_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+    return 0;
+}
+
+// BasicInfection::seasonalityMultiplier, infectionPolicies.h:443-478
+double seasonality(const psim_params& p, uint32_t t, uint32_t spd) {
+    unsigned sim_day = t / spd;
+    int d = (int)p.start_date + (int)sim_day;
+    int d_peak = 59 + 22;
+    d += 6;
+    double c0 = 3.08;
+    double trunc_val = 0.5;
+    if (sim_day > 250 && sim_day < 450) {
+        d += p.d_offset0;
+        d_peak += p.d_peak_offset;
+        c0 = p.c0;
+    } else if (sim_day > 600) {
+        trunc_val = p.trunc;
+        if (p.n_d_offset > 1) d += p.d_offset1;
+    }
+    int d_mod = d % 366;
+    if (d_mod > 366 / 2) d_mod = 366 - d_mod;
+    double a1 = 0.5 * c0 * cos(2.0 * M_PI * (double)(d_mod - d_peak) / 366.0);
+    double b1 = 1.0 - 0.5 * c0;
+    double a2 = 0.5 * c0 * cos(2.0 * M_PI * (double)(d_peak - d_peak) / 366.0);
+    double normed = (a1 + b1) / (a2 + b1);
+    double calc = normed > trunc_val ? normed : trunc_val;
+    calc = calc < 1.0 ? calc : 1.0;
+    if (d_mod < d_peak) return 1.0;
+    return calc;
+}
+
+// set the device clock for the day containing t
+int set_clock(psim_ctx* c, uint32_t t) {
+    uint32_t t0 = t - t % c->spd;
+    DevClock nc = c->h_clock;
+    nc.t0 = t0;
+    nc.day_of_week = c->params.holiday_mode ? 6u : (c->params.start_day + t0 / c->spd) % 7u;
+    nc.season = (float)seasonality(c->params, t0, c->spd);
+    if (c->clock_valid && nc.t0 == c->h_clock.t0 && nc.day_of_week == c->h_clock.day_of_week &&
+        nc.season == c->h_clock.season)
+        return 0;
+    c->h_clock = nc;
+    // only the first three fields; the scan bookkeeping stays on the device
+    CK(cudaMemcpyAsync(c->k.clock, &c->h_clock, 3 * sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->clock_valid = true;
+    return 0;
+}
+
+int validate(psim_ctx* c, const psim_model* m, const psim_agents* a, const psim_locations* l) {
+    if (!m || !a || !l) return fail(c, PSIM_ERR_ARG, "null snapshot part");
+    if (m->n_variants == 0 || m->n_variants > PSIM_MAX_STRAINS) return fail(c, PSIM_ERR_ARG, "n_variants out of range");
+    if (m->n_states == 0 || m->n_states > 16) return fail(c, PSIM_ERR_ARG, "n_states must be 1..16");
+    if (l->n == 0) return fail(c, PSIM_ERR_ARG, "no locations");
+    const uint32_t N = a->n, L = l->n;
+    if (!a->loc_offset || a->loc_offset[0] != 0 || a->loc_offset[N] != a->n_poss)
+        return fail(c, PSIM_ERR_RANGE, "per-agent location offsets inconsistent");
+    for (uint32_t i = 0; i < N; ++i) {
+        if (a->loc_offset[i + 1] < a->loc_offset[i]) return fail(c, PSIM_ERR_RANGE, "per-agent offsets not monotonic");
+        if (a->location[i] >= L) return fail(c, PSIM_ERR_RANGE, "agent " + std::to_string(i) + " location out of range");
+        if ((uint8_t)a->state[i] >= m->n_states) return fail(c, PSIM_ERR_RANGE, "agent state out of range");
+        if (a->prog_id[i] >= m->n_prog) return fail(c, PSIM_ERR_RANGE, "progression id out of range");
+        if (a->type[i] >= m->n_agent_types) return fail(c, PSIM_ERR_RANGE, "agent type out of range");
+        if (a->variant[i] >= m->n_variants) return fail(c, PSIM_ERR_RANGE, "variant out of range");
+        if (a->band[i] >= PSIM_MAX_BANDS) return fail(c, PSIM_ERR_RANGE, "age band out of range");
+    }
+    for (uint32_t j = 0; j < a->n_poss; ++j)
+        if (a->poss_loc[j] >= L) return fail(c, PSIM_ERR_RANGE, "per-agent location entry out of range");
+    const uint32_t ne = m->event_offset[m->n_agent_types * 28];
+    if (ne != m->n_events) return fail(c, PSIM_ERR_ARG, "event offsets do not match n_events");
+    for (uint32_t s = 0; s < m->n_prog * m->n_states; ++s) {
+        if (m->tr_bad_begin[s] + m->tr_bad_count[s] > m->n_trans || m->tr_neu_begin[s] + m->tr_neu_count[s] > m->n_trans)
+            return fail(c, PSIM_ERR_RANGE, "transition table out of range");
+    }
+    for (uint32_t j = 0; j < m->n_trans; ++j)
+        if (m->tr_next[j] >= m->n_states) return fail(c, PSIM_ERR_RANGE, "transition target out of range");
+    for (uint32_t s = 0; s < l->n_schools; ++s)
+        if (l->schools[s] >= L) return fail(c, PSIM_ERR_RANGE, "school out of range");
+    for (uint32_t s = 0; s < l->n_classrooms; ++s)
+        if (l->classrooms[s] >= L) return fail(c, PSIM_ERR_RANGE, "classroom out of range");
+    return 0;
+}
+
+int upload_mutable(psim_ctx* c, const psim_agents* a, const psim_locations* l) {
+    const size_t N = c->N, L = c->L;
+    DevAgents& d = c->k.a;
+    int rc = 0;
+#define UP(field, cnt) \
+    if ((rc = dcopy_in(c, d.field, a->field, cnt))) return rc;
+    UP(location, N) UP(steps_until_move, N) UP(state, N) UP(days, N) UP(variant, N) UP(infectious, N)
+    UP(susceptible, N * c->V) UP(diagnosed, N) UP(quarantined, N) UP(stayed_home, N) UP(no_work, N) UP(last_test, N)
+    UP(st_infected_ts, N) UP(st_infected_loc, N) UP(st_worst_ts, N) UP(st_worst_end_ts, N) UP(st_diagnosed_ts, N)
+    UP(st_quarantined_ts, N) UP(st_quarantined_until, N) UP(st_days_in_quarantine, N) UP(st_hospitalized_ts, N)
+    UP(st_hospitalized_until, N) UP(st_immunization_ts, N) UP(st_recovered_ts, N) UP(st_variant_mask, N)
+    UP(st_immunization_count, N) UP(st_infected_count, N) UP(st_worst_state, N)
+#undef UP
+    DevLocs& dl = c->k.l;
+    if ((rc = dcopy_in(c, dl.infectiousness, l->infectiousness, L))) return rc;
+    if ((rc = dcopy_in(c, dl.open, l->open, L))) return rc;
+    if ((rc = dcopy_in(c, dl.closed_until, l->closed_until, L))) return rc;
+    if ((rc = dcopy_in(c, dl.quarantine_until, l->quarantine_until, L))) return rc;
+    return 0;
+}
+
+// LocationsList::initialize (locationList.h:224-230) and the variant gates
+int initial_regroup(psim_ctx* c) {
+    CK(cudaMemsetAsync(c->k.l.counts, 0, sizeof(uint32_t) * c->L, c->stream));
+    CK(cudaMemsetAsync(c->k.l.sfix, 0, sizeof(unsigned long long) * c->L * c->V, c->stream));
+    launch_count(c->k, c->stream);
+    launch_scan(c->k, 0, 1, 0, c->stream);
+    launch_scatter_draw(c->k, 0, 0, c->stream);
+    launch_stats(c->k, 0, c->stream);
+    c->launches += 5;
+    int rc = launch_check(c);
+    if (rc) return rc;
+    c->csr_fresh = true;
+    return check_device_err(c);
+}
+
+int do_step(psim_ctx* c, uint32_t step, bool draw, bool movement) {
+    const int merge_q = c->params.quarantine_policy > 1;
+    if (movement) launch_movement(c->k, step, c->stream);
+    launch_scan(c->k, step, 1, merge_q, c->stream);
+    launch_scatter_draw(c->k, step, draw ? 1 : 0, c->stream);
+    c->launches += movement ? 3 : 2;
+    return launch_check(c);
+}
+
+int capture_day_graph(psim_ctx* c) {
+    if (c->day_graph) {
+        cudaGraphExecDestroy(c->day_graph);
+        c->day_graph = nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    const int merge_q = c->params.quarantine_policy > 1;
+    for (uint32_t s = 0; s < c->spd; ++s) {
+        launch_movement(c->k, s, c->stream);
+        launch_scan(c->k, s, 1, merge_q, c->stream);
+        launch_scatter_draw(c->k, s, 1, c->stream);
+    }
+    cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (e != cudaSuccess) return fail(c, PSIM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&c->day_graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return fail(c, PSIM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    c->graph_kernels = 3ull * c->spd;
+    c->graph_dirty = false;
+    return 0;
+}
+
+void assemble_stats(psim_ctx* c, uint32_t t, psim_day_stats* out) {
+    const uint32_t S = c->S, V = c->V;
+    const bool tests = c->params.testing_enabled && t > 0;
+    for (uint32_t q = 0; q < c->R; ++q) {
+        const DevStatsAcc& a = c->h_stats[q];
+        psim_day_stats& d = out[q];
+        memset(&d, 0, sizeof(d));
+        uint32_t n = 0;
+        for (uint32_t s = 0; s < S; ++s) d.v[n++] = a.c[SC_HIST + s];
+        d.v[n++] = a.c[SC_HOSP];
+        d.v[n++] = tests ? a.c[SC_TESTS] : 0u;
+        d.v[n++] = tests ? a.c[SC_P1] : 0u;
+        d.v[n++] = tests ? a.c[SC_P2] : 0u;
+        d.v[n++] = a.c[SC_Q];
+        d.v[n++] = a.c[SC_QT];
+        d.v[n++] = a.c[SC_NQ];
+        if (V > 1) {
+            for (uint32_t v = 1; v < V; ++v)
+                d.v[n++] = a.c[SC_ALL_INF] ? (uint32_t)((double)a.c[SC_VAR + v] / (double)a.c[SC_ALL_INF] * 100.0) : 0u;
+        } else {
+            d.v[n++] = 0u;
+        }
+        d.v[n] = a.c[SC_STAYED] - d.v[10] - d.v[11];
+        n++;
+        d.v[n++] = 0u;  // immunized today
+        d.v[n++] = a.c[SC_NI];
+        d.v[n++] = a.c[SC_INF_ONCE];
+        d.v[n++] = a.c[SC_REINF];
+        d.v[n++] = a.c[SC_BSTR];
+        for (uint32_t v = 0; v < V; ++v) d.v[n++] = (uint32_t)a.imm[v];
+        d.v[n++] = (a.c[SC_HCI] * 100u) / (c->hcw_count[q] > 1 ? c->hcw_count[q] : 1u);
+        d.v[n++] = a.c[SC_HCE];
+        for (uint32_t v = 0; v < V; ++v) d.v[n++] = a.c[SC_INFV + v];
+        d.v[n++] = a.c[SC_INFH];
+        d.v[n++] = a.c[SC_VNI];
+        d.n = n;
+        d.new_infections = a.c[SC_NI];
+        for (uint32_t v = 0; v < V; ++v) d.variant_counts[v] = a.c[SC_VAR + v];
+        d.expected_new_infections = c->h_expected[q];
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* psim_version(void) { return kVersion; }
+
+int psim_abi_sizes(uint64_t* out, int n) {
+    const uint64_t s[6] = {sizeof(psim_model), sizeof(psim_agents), sizeof(psim_locations),
+                           sizeof(psim_params), sizeof(psim_replicas), sizeof(psim_day_stats)};
+    for (int i = 0; i < n && i < 6; ++i) out[i] = s[i];
+    return 0;
+}
+
+int psim_device_count(int* out) {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) n = 0;
+    if (out) *out = n;
+    return e == cudaSuccess ? 0 : PSIM_ERR_CUDA;
+}
+
+const char* psim_last_error(const psim_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int psim_create(int device, const psim_model* m, const psim_agents* a, const psim_locations* l,
+                const psim_params* p, const psim_replicas* reps, psim_ctx** out) {
+    if (!out) return PSIM_ERR_ARG;
+    *out = nullptr;
+    psim_ctx* c = new psim_ctx();
+    auto bail = [&](int rc) {
+        *out = c;  // keep the context so that psim_last_error works; caller destroys it
+        return rc;
+    };
+    if (!p) return bail(fail(c, PSIM_ERR_ARG, "null params"));
+    int rc = validate(c, m, a, l);
+    if (rc) return bail(rc);
+    if (p->time_step == 0 || 1440 % p->time_step) return bail(fail(c, PSIM_ERR_ARG, "time_step must divide 1440"));
+    c->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return bail(fail(c, PSIM_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e)));
+    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return bail(fail(c, PSIM_ERR_CUDA, std::string("stream: ") + cudaGetErrorString(e)));
+    cudaEventCreate(&c->ev0);
+    cudaEventCreate(&c->ev1);
+    c->N = a->n;
+    c->L = l->n;
+    c->V = m->n_variants;
+    c->S = m->n_states;
+    c->n_poss = a->n_poss;
+    c->params = *p;
+    c->spd = 1440 / p->time_step;
+    // replicas
+    if (reps && reps->n > 0) {
+        c->R = reps->n;
+        c->rep_agent_off.assign(reps->agent_offset, reps->agent_offset + c->R + 1);
+        c->rep_loc_off.assign(reps->loc_offset, reps->loc_offset + c->R + 1);
+        c->rep_seed.assign(reps->seed, reps->seed + c->R);
+        c->rep_k.assign(reps->k, reps->k + c->R);
+        c->rep_cemetery.assign(reps->cemetery, reps->cemetery + c->R);
+    } else {
+        c->R = 1;
+        c->rep_agent_off = {0u, c->N};
+        c->rep_loc_off = {0u, c->L};
+        c->rep_seed = {p->seed};
+        c->rep_k = {p->k};
+        c->rep_cemetery = {p->cemetery_loc};
+    }
+    if (c->R > 65535) return bail(fail(c, PSIM_ERR_ARG, "too many replicas"));
+    if (c->rep_agent_off[c->R] != c->N || c->rep_loc_off[c->R] != c->L || c->rep_agent_off[0] || c->rep_loc_off[0])
+        return bail(fail(c, PSIM_ERR_ARG, "replica offsets do not cover the snapshot"));
+    for (uint32_t q = 0; q < c->R; ++q) {
+        if (c->rep_agent_off[q + 1] < c->rep_agent_off[q] || c->rep_loc_off[q + 1] < c->rep_loc_off[q])
+            return bail(fail(c, PSIM_ERR_ARG, "replica offsets not monotonic"));
+        if (c->rep_cemetery[q] < c->rep_loc_off[q] || c->rep_cemetery[q] >= c->rep_loc_off[q + 1])
+            return bail(fail(c, PSIM_ERR_RANGE, "cemetery outside its replica"));
+    }
+    const size_t N = c->N, L = c->L, V = c->V, R = c->R;
+    KArgs& k = c->k;
+    // model tables
+    DevModel& dm = k.m;
+    dm.n_states = m->n_states;
+    dm.n_variants = m->n_variants;
+    dm.n_prog = m->n_prog;
+    dm.n_agent_types = m->n_agent_types;
+    dm.first_infected = m->first_infected_state;
+    dm.noncovid_dead = m->noncovid_dead_state;
+    dm.dead_state = m->dead_state;
+    dm.n_trans = m->n_trans;
+    const size_t S = m->n_states, PS = (size_t)m->n_prog * S;
+    std::vector<uint32_t> thr(PS * PSIM_MAX_STRAINS);
+    for (size_t j = 0; j < thr.size(); ++j) thr[j] = psim_geometric_threshold(m->len_p[j]);
+#define UPM(field, cnt) \
+    if ((rc = dupload(c, &dm.field, m->field, cnt))) return bail(rc);
+    UPM(state_wb, S) UPM(state_susceptible, S) UPM(state_infected, S) UPM(state_infectious, S) UPM(state_acc_pcr, S)
+    UPM(state_acc_antigen, S) UPM(variant_multiplier, V) UPM(prog_scaling, V) UPM(death_scaling, V)
+    UPM(tr_bad_begin, PS) UPM(tr_bad_count, PS) UPM(tr_neu_begin, PS) UPM(tr_neu_count, PS)
+    UPM(tr_next, m->n_trans) UPM(tr_chance, m->n_trans) UPM(len_avg, PS * PSIM_MAX_STRAINS)
+    UPM(len_max, PS * PSIM_MAX_STRAINS) UPM(event_offset, (size_t)m->n_agent_types * 28 + 1)
+    UPM(ev_loc_type, m->n_events) UPM(ev_chance, m->n_events) UPM(ev_start, m->n_events) UPM(ev_end, m->n_events)
+    UPM(ev_duration, m->n_events)
+#undef UPM
+    if ((rc = dupload(c, &dm.len_thr, thr.data(), thr.size()))) return bail(rc);
+    // agents: immutable
+    DevAgents& da = k.a;
+    da.n = c->N;
+    std::vector<uint16_t> arep(N), lrep(L);
+    for (uint32_t q = 0; q < c->R; ++q) {
+        for (uint32_t i = c->rep_agent_off[q]; i < c->rep_agent_off[q + 1]; ++i) arep[i] = (uint16_t)q;
+        for (uint32_t j = c->rep_loc_off[q]; j < c->rep_loc_off[q + 1]; ++j) lrep[j] = (uint16_t)q;
+    }
+#define UPA(field, cnt) \
+    if ((rc = dupload(c, &da.field, a->field, cnt))) return bail(rc);
+    UPA(type, N) UPA(age, N) UPA(band, N) UPA(prog_id, N) UPA(symptom_scaling, N) UPA(loc_offset, N + 1)
+    UPA(poss_loc, c->n_poss) UPA(poss_type, c->n_poss)
+#undef UPA
+    if ((rc = dupload(c, &da.rep, arep.data(), N))) return bail(rc);
+#define AL(field, cnt) \
+    if ((rc = dalloc(c, &da.field, cnt))) return bail(rc);
+    AL(location, N) AL(steps_until_move, N) AL(state, N) AL(days, N) AL(variant, N) AL(infectious, N)
+    AL(susceptible, N * V) AL(diagnosed, N) AL(quarantined, N) AL(stayed_home, N) AL(no_work, N) AL(last_test, N)
+    AL(st_infected_ts, N) AL(st_infected_loc, N) AL(st_worst_ts, N) AL(st_worst_end_ts, N) AL(st_diagnosed_ts, N)
+    AL(st_quarantined_ts, N) AL(st_quarantined_until, N) AL(st_days_in_quarantine, N) AL(st_hospitalized_ts, N)
+    AL(st_hospitalized_until, N) AL(st_immunization_ts, N) AL(st_recovered_ts, N) AL(st_variant_mask, N)
+    AL(st_immunization_count, N) AL(st_infected_count, N) AL(st_worst_state, N) AL(hcw, N) AL(rank, N)
+#undef AL
+    // locations
+    DevLocs& dl = k.l;
+    dl.n = c->L;
+    dl.n_schools = l->n_schools;
+    if ((rc = dupload(c, &dl.type, l->type, L))) return bail(rc);
+    if ((rc = dupload(c, &dl.essential, l->essential, L))) return bail(rc);
+    if ((rc = dupload(c, &dl.schools, l->schools, l->n_schools))) return bail(rc);
+    if ((rc = dupload(c, &dl.classrooms, l->classrooms, l->n_classrooms))) return bail(rc);
+    if ((rc = dupload(c, &dl.classroom_offsets, l->classroom_offsets, l->n_schools ? l->n_schools + 1 : 0)))
+        return bail(rc);
+    if ((rc = dupload(c, &dl.rep, lrep.data(), L))) return bail(rc);
+    if ((rc = dalloc(c, &dl.infectiousness, L))) return bail(rc);
+    if ((rc = dalloc(c, &dl.open, L))) return bail(rc);
+    if ((rc = dalloc(c, &dl.closed_until, L))) return bail(rc);
+    if ((rc = dalloc(c, &dl.quarantine_until, L))) return bail(rc);
+    if ((rc = dalloc(c, &dl.counts, L))) return bail(rc);
+    if ((rc = dalloc(c, &dl.csr_off, L + 1))) return bail(rc);
+    if ((rc = dalloc(c, &dl.csr_agents, N))) return bail(rc);
+    if ((rc = dalloc(c, &dl.qu_pending, L))) return bail(rc);
+    if ((rc = dalloc(c, &dl.sfix, L * V))) return bail(rc);
+    if ((rc = dalloc(c, &dl.hazard, L * V))) return bail(rc);
+    if ((rc = dalloc(c, &dl.no_work_loc, L))) return bail(rc);
+    if ((rc = dalloc(c, &dl.flags, L))) return bail(rc);
+    const size_t tiles = (L + 2047) / 2048 + 1;
+    if ((rc = dalloc(c, &dl.scan_status, tiles))) return bail(rc);
+    // replicas
+    DevReps& dr = k.r;
+    dr.n = c->R;
+    std::vector<float> kf(R);
+    for (size_t q = 0; q < R; ++q) kf[q] = (float)c->rep_k[q];
+    if ((rc = dupload(c, &dr.agent_off, c->rep_agent_off.data(), R + 1))) return bail(rc);
+    if ((rc = dupload(c, &dr.loc_off, c->rep_loc_off.data(), R + 1))) return bail(rc);
+    if ((rc = dupload(c, &dr.seed, (const unsigned long long*)c->rep_seed.data(), R))) return bail(rc);
+    if ((rc = dupload(c, &dr.k_f, kf.data(), R))) return bail(rc);
+    if ((rc = dupload(c, &dr.cemetery, c->rep_cemetery.data(), R))) return bail(rc);
+    if ((rc = dalloc(c, &dr.variant_active, R * V))) return bail(rc);
+    if ((rc = dalloc(c, &dr.expected, R))) return bail(rc);
+    if ((rc = dalloc(c, &k.clock, 1))) return bail(rc);
+    if ((rc = dalloc(c, &k.err, 1))) return bail(rc);
+    if ((rc = dalloc(c, &k.stats, R))) return bail(rc);
+    k.p = c->params;
+    k.spd = c->spd;
+    k.track_expected = 0;
+    c->h_stats.resize(R);
+    c->h_expected.assign(R, 0.0);
+    // healthcare workers per replica (Simulation::flagHealthcareWorkers, simulation.h:670-693)
+    c->hcw_count.assign(R, 0u);
+    for (uint32_t q = 0; q < c->R; ++q)
+        for (uint32_t i = c->rep_agent_off[q]; i < c->rep_agent_off[q + 1]; ++i)
+            for (uint32_t j = a->loc_offset[i]; j < a->loc_offset[i + 1]; ++j) {
+                const uint32_t lt = l->type[a->poss_loc[j]];
+                if (a->poss_type[j] == 4 && (lt == 12 || lt == 14)) {
+                    c->hcw_count[q]++;
+                    break;
+                }
+            }
+    if ((rc = upload_mutable(c, a, l))) return bail(rc);
+    if ((rc = set_clock(c, 0))) return bail(rc);
+    launch_flag_hcw(k, c->stream);
+    c->launches += 1;
+    if ((rc = initial_regroup(c))) return bail(rc);
+    c->uploaded = true;
+    *out = c;
+    return 0;
+}
+
+int psim_destroy(psim_ctx* c) {
+    if (!c) return 0;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->day_graph) cudaGraphExecDestroy(c->day_graph);
+    for (void* p : c->allocs) cudaFree(p);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return 0;
+}
+
+int psim_upload(psim_ctx* c, const psim_agents* a, const psim_locations* l) {
+    if (!c) return PSIM_ERR_ARG;
+    if (!a || !l || a->n != c->N || l->n != c->L) return fail(c, PSIM_ERR_ARG, "snapshot size mismatch");
+    for (uint32_t i = 0; i < c->N; ++i)
+        if (a->location[i] >= c->L) return fail(c, PSIM_ERR_RANGE, "agent location out of range");
+    int rc = upload_mutable(c, a, l);
+    if (rc) return rc;
+    return initial_regroup(c);
+}
+
+int psim_download(psim_ctx* c, psim_agents* a, psim_locations* l) {
+    if (!c) return PSIM_ERR_ARG;
+    if (!a || !l || a->n != c->N || l->n != c->L) return fail(c, PSIM_ERR_ARG, "snapshot size mismatch");
+    const size_t N = c->N, L = c->L;
+    const DevAgents& d = c->k.a;
+#define DN(field, cnt) \
+    if (a->field) CK(cudaMemcpyAsync(a->field, d.field, (cnt) * sizeof(*a->field), cudaMemcpyDeviceToHost, c->stream));
+    DN(location, N) DN(steps_until_move, N) DN(state, N) DN(days, N) DN(variant, N) DN(infectious, N)
+    DN(susceptible, N * c->V) DN(diagnosed, N) DN(quarantined, N) DN(stayed_home, N) DN(no_work, N) DN(last_test, N)
+    DN(st_infected_ts, N) DN(st_infected_loc, N) DN(st_worst_ts, N) DN(st_worst_end_ts, N) DN(st_diagnosed_ts, N)
+    DN(st_quarantined_ts, N) DN(st_quarantined_until, N) DN(st_days_in_quarantine, N) DN(st_hospitalized_ts, N)
+    DN(st_hospitalized_until, N) DN(st_immunization_ts, N) DN(st_recovered_ts, N) DN(st_variant_mask, N)
+    DN(st_immunization_count, N) DN(st_infected_count, N) DN(st_worst_state, N)
+#undef DN
+    const DevLocs& dl = c->k.l;
+    if (l->infectiousness) CK(cudaMemcpyAsync(l->infectiousness, dl.infectiousness, L * 4, cudaMemcpyDeviceToHost, c->stream));
+    if (l->open) CK(cudaMemcpyAsync(l->open, dl.open, L, cudaMemcpyDeviceToHost, c->stream));
+    if (l->closed_until) CK(cudaMemcpyAsync(l->closed_until, dl.closed_until, L * 4, cudaMemcpyDeviceToHost, c->stream));
+    if (l->quarantine_until)
+        CK(cudaMemcpyAsync(l->quarantine_until, dl.quarantine_until, L * 4, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return check_device_err(c);
+}
+
+int psim_set_params(psim_ctx* c, const psim_params* p) {
+    if (!c || !p) return PSIM_ERR_ARG;
+    if (p->time_step != c->params.time_step) return fail(c, PSIM_ERR_ARG, "time_step cannot change");
+    c->params = *p;
+    c->k.p = *p;
+    c->graph_dirty = true;
+    c->clock_valid = false;
+    return 0;
+}
+
+int psim_set_tracking(psim_ctx* c, int expected) {
+    if (!c) return PSIM_ERR_ARG;
+    c->k.track_expected = expected ? 1u : 0u;
+    c->graph_dirty = true;
+    return 0;
+}
+
+int psim_movement(psim_ctx* c, uint32_t t) {
+    if (!c || !c->uploaded) return PSIM_ERR_STATE;
+    int rc = set_clock(c, t);
+    if (rc) return rc;
+    launch_movement(c->k, t % c->spd, c->stream);
+    c->launches += 1;
+    c->csr_fresh = true;
+    rc = launch_check(c);
+    if (rc) return rc;
+    return check_device_err(c);
+}
+
+int psim_regroup(psim_ctx* c) {
+    if (!c || !c->uploaded) return PSIM_ERR_STATE;
+    if (!c->csr_fresh) {
+        CK(cudaMemsetAsync(c->k.l.counts, 0, sizeof(uint32_t) * c->L, c->stream));
+        CK(cudaMemsetAsync(c->k.l.sfix, 0, sizeof(unsigned long long) * c->L * c->V, c->stream));
+        launch_count(c->k, c->stream);
+        c->launches += 1;
+    }
+    launch_scan(c->k, 0, 1, c->params.quarantine_policy > 1, c->stream);
+    launch_scatter_draw(c->k, 0, 0, c->stream);
+    c->launches += 2;
+    c->csr_fresh = false;
+    int rc = launch_check(c);
+    if (rc) return rc;
+    return check_device_err(c);
+}
+
+int psim_infect(psim_ctx* c, uint32_t t, uint32_t variant) {
+    // the hazard of the last regroup was computed for all variants; the draw
+    // runs for the active ones (variant selects nothing more: draws of
+    // several variants are sequential per agent as in the reference)
+    if (!c || !c->uploaded) return PSIM_ERR_STATE;
+    (void)variant;
+    int rc = set_clock(c, t);
+    if (rc) return rc;
+    // re-run the scatter with the draw; the CSR write is idempotent
+    launch_scatter_draw(c->k, t % c->spd, 1, c->stream);
+    c->launches += 1;
+    rc = launch_check(c);
+    if (rc) return rc;
+    return check_device_err(c);
+}
+
+int psim_step(psim_ctx* c, uint32_t t) {
+    if (!c || !c->uploaded) return PSIM_ERR_STATE;
+    int rc = set_clock(c, t);
+    if (rc) return rc;
+    rc = do_step(c, t % c->spd, true, true);
+    if (rc) return rc;
+    c->csr_fresh = false;
+    return check_device_err(c);
+}
+
+int psim_test_day(psim_ctx* c, uint32_t t, uint32_t* tpp) {
+    if (!c || !c->uploaded) return PSIM_ERR_STATE;
+    launch_test(c->k, t, c->stream);
+    c->launches += 2;
+    int rc = launch_check(c);
+    if (rc) return rc;
+    if (tpp) {
+        launch_stats(c->k, t, c->stream);
+        c->launches += 2;
+        CK(cudaMemcpyAsync(c->h_stats.data(), c->k.stats, sizeof(DevStatsAcc) * c->R, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        for (uint32_t q = 0; q < c->R; ++q) {
+            tpp[3 * q + 0] = c->h_stats[q].c[SC_TESTS];
+            tpp[3 * q + 1] = c->h_stats[q].c[SC_P1];
+            tpp[3 * q + 2] = c->h_stats[q].c[SC_P2];
+        }
+    }
+    return check_device_err(c);
+}
+
+int psim_progress_day(psim_ctx* c, uint32_t t) {
+    if (!c || !c->uploaded) return PSIM_ERR_STATE;
+    launch_progress(c->k, t, c->stream);
+    c->launches += 1;
+    int rc = launch_check(c);
+    if (rc) return rc;
+    return check_device_err(c);
+}
+
+int psim_stats_day(psim_ctx* c, uint32_t t, psim_day_stats* out) {
+    if (!c || !c->uploaded) return PSIM_ERR_STATE;
+    launch_stats(c->k, t, c->stream);
+    c->launches += 2;
+    int rc = launch_check(c);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(c->h_stats.data(), c->k.stats, sizeof(DevStatsAcc) * c->R, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(c->h_expected.data(), c->k.r.expected, sizeof(double) * c->R, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemsetAsync(c->k.r.expected, 0, sizeof(double) * c->R, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (out) assemble_stats(c, t, out);
+    return check_device_err(c);
+}
+
+int psim_plan_day(psim_ctx* c, uint32_t t) {
+    if (!c || !c->uploaded) return PSIM_ERR_STATE;
+    launch_plan(c->k, t, c->stream);
+    c->launches += 5 + (c->params.quarantine_policy > 3 && c->k.l.n_schools ? 1 : 0);
+    int rc = launch_check(c);
+    if (rc) return rc;
+    return check_device_err(c);
+}
+
+int psim_midnight(psim_ctx* c, uint32_t t, psim_day_stats* out) {
+    if (!c || !c->uploaded) return PSIM_ERR_STATE;
+    int rc = 0;
+    if (t > 0 && c->params.testing_enabled) {
+        launch_test(c->k, t, c->stream);
+        c->launches += 2;
+    }
+    if (t > 0) {
+        launch_progress(c->k, t, c->stream);
+        c->launches += 1;
+    }
+    if ((rc = psim_stats_day(c, t, out))) return rc;
+    return psim_plan_day(c, t);
+}
+
+int psim_run_steps(psim_ctx* c, uint32_t day) {
+    if (!c || !c->uploaded) return PSIM_ERR_STATE;
+    int rc = set_clock(c, day * c->spd);
+    if (rc) return rc;
+    if (c->graph_dirty || !c->day_graph) {
+        if ((rc = capture_day_graph(c))) return rc;
+    }
+    CK(cudaEventRecord(c->ev0, c->stream));
+    CK(cudaGraphLaunch(c->day_graph, c->stream));
+    CK(cudaEventRecord(c->ev1, c->stream));
+    CK(cudaEventSynchronize(c->ev1));
+    CK(cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1));
+    c->launches += c->graph_kernels;
+    c->csr_fresh = false;
+    return check_device_err(c);
+}
+
+int psim_run_day(psim_ctx* c, uint32_t day, psim_day_stats* out) {
+    int rc = psim_midnight(c, day * (c ? c->spd : 144), out);
+    if (rc) return rc;
+    return psim_run_steps(c, day);
+}
+
+int psim_get_csr(psim_ctx* c, int canonical, uint32_t* offsets, uint32_t* agents) {
+    if (!c || !c->uploaded) return PSIM_ERR_STATE;
+    if (canonical) {
+        launch_canonical_csr(c->k, c->stream);
+        c->launches += 1;
+        int rc = launch_check(c);
+        if (rc) return rc;
+    }
+    if (offsets) CK(cudaMemcpyAsync(offsets, c->k.l.csr_off, sizeof(uint32_t) * (c->L + 1), cudaMemcpyDeviceToHost, c->stream));
+    if (agents) CK(cudaMemcpyAsync(agents, c->k.l.csr_agents, sizeof(uint32_t) * c->N, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return check_device_err(c);
+}
+
+int psim_get_hazard(psim_ctx* c, float* out, int64_t* fixed_sum) {
+    if (!c || !c->uploaded) return PSIM_ERR_STATE;
+    if (out) CK(cudaMemcpyAsync(out, c->k.l.hazard, sizeof(float) * c->L * c->V, cudaMemcpyDeviceToHost, c->stream));
+    (void)fixed_sum;
+    CK(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+int psim_last_day_ms(psim_ctx* c, float* ms) {
+    if (!c || !ms) return PSIM_ERR_ARG;
+    *ms = c->last_ms;
+    return 0;
+}
+
+int psim_launch_count(psim_ctx* c, uint64_t* out) {
+    if (!c || !out) return PSIM_ERR_ARG;
+    *out = c->launches;
+    return 0;
+}
+
+int psim_stream_handle(psim_ctx* c, void** out) {
+    if (!c || !out) return PSIM_ERR_ARG;
+    *out = (void*)c->stream;
+    return 0;
+}
+
+int psim_time_step_kernels(psim_ctx* c, uint32_t t, float* ms) {
+    if (!c || !c->uploaded || !ms) return PSIM_ERR_ARG;
+    int rc = set_clock(c, t);
+    if (rc) return rc;
+    cudaEvent_t ev[4];
+    for (int j = 0; j < 4; ++j) CK(cudaEventCreate(&ev[j]));
+    const uint32_t step = t % c->spd;
+    const int merge_q = c->params.quarantine_policy > 1;
+    CK(cudaEventRecord(ev[0], c->stream));
+    launch_movement(c->k, step, c->stream);
+    CK(cudaEventRecord(ev[1], c->stream));
+    launch_scan(c->k, step, 1, merge_q, c->stream);
+    CK(cudaEventRecord(ev[2], c->stream));
+    launch_scatter_draw(c->k, step, 1, c->stream);
+    CK(cudaEventRecord(ev[3], c->stream));
+    c->launches += 3;
+    CK(cudaEventSynchronize(ev[3]));
+    for (int j = 0; j < 3; ++j) CK(cudaEventElapsedTime(&ms[j], ev[j], ev[j + 1]));
+    for (int j = 0; j < 4; ++j) cudaEventDestroy(ev[j]);
+    c->csr_fresh = false;
+    rc = launch_check(c);
+    if (rc) return rc;
+    return check_device_err(c);
+}
+
+int psim_bounded_wait_selftest(psim_ctx* c, uint32_t iters) {
+    if (!c || !c->uploaded) return PSIM_ERR_STATE;
+    launch_bounded_wait_probe(c->k, iters, c->stream);
+    c->launches += 1;
+    int rc = launch_check(c);
+    if (rc) return rc;
+    return check_device_err(c);
+}
+
+}  // extern "C"

@@ -1,0 +1,180 @@
+// Device-side data layout of a pansim_gb300 context and the launch helpers
+// shared by psim_kernels.cu (kernels) and psim_api.cu (C ABI, graphs).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/pansim_gb300.h"
+#include "psim_rng.h"
+
+namespace psim {
+
+constexpr uint32_t NONE = 0xFFFFFFFFu;
+constexpr int WB_W = 0, WB_N = 1, WB_M = 2, WB_S = 3, WB_D = 4;
+
+// error bits written by kernels into DevCtx::err
+constexpr uint32_t ERR_SCAN_WAIT = 1u;     // scan look-back wait gave up
+constexpr uint32_t ERR_LOCATION = 2u;      // an agent ended on an invalid location
+constexpr uint32_t ERR_TEST_WAIT = 4u;     // bounded-wait self test expired (expected in tests)
+
+struct DevModel {
+    uint32_t n_states, n_variants, n_prog, n_agent_types;
+    uint32_t first_infected, noncovid_dead, dead_state, n_trans;
+    const uint8_t* state_wb;
+    const uint8_t* state_susceptible;
+    const uint8_t* state_infected;
+    const float* state_infectious;
+    const float* state_acc_pcr;
+    const float* state_acc_antigen;
+    const float* variant_multiplier;
+    const float* prog_scaling;
+    const float* death_scaling;
+    const uint32_t* tr_bad_begin;
+    const uint32_t* tr_bad_count;
+    const uint32_t* tr_neu_begin;
+    const uint32_t* tr_neu_count;
+    const uint32_t* tr_next;
+    const float* tr_chance;
+    const float* len_avg;
+    const float* len_max;
+    const uint32_t* len_thr;   // Bernoulli threshold of the geometric dwell draw
+    const uint32_t* event_offset;
+    const uint32_t* ev_loc_type;
+    const float* ev_chance;
+    const uint16_t* ev_start;
+    const uint16_t* ev_end;
+    const uint16_t* ev_duration;
+};
+
+struct DevAgents {
+    uint32_t n;
+    const uint8_t* type;
+    const uint8_t* age;
+    const uint8_t* band;
+    const uint16_t* prog_id;
+    const float* symptom_scaling;
+    const uint32_t* loc_offset;
+    const uint32_t* poss_loc;
+    const uint8_t* poss_type;
+    const uint16_t* rep;          // replica of each agent
+    uint32_t* location;
+    uint32_t* steps_until_move;
+    int8_t* state;
+    int16_t* days;
+    uint8_t* variant;
+    float* infectious;
+    float* susceptible;           // [V][N]
+    uint8_t* diagnosed;
+    uint8_t* quarantined;
+    uint8_t* stayed_home;
+    uint8_t* no_work;
+    uint32_t* last_test;
+    uint32_t* st_infected_ts;
+    uint32_t* st_infected_loc;
+    uint32_t* st_worst_ts;
+    uint32_t* st_worst_end_ts;
+    uint32_t* st_diagnosed_ts;
+    uint32_t* st_quarantined_ts;
+    uint32_t* st_quarantined_until;
+    uint32_t* st_days_in_quarantine;
+    uint32_t* st_hospitalized_ts;
+    uint32_t* st_hospitalized_until;
+    uint32_t* st_immunization_ts;
+    uint32_t* st_recovered_ts;
+    uint32_t* st_variant_mask;
+    uint8_t* st_immunization_count;
+    uint8_t* st_infected_count;
+    int8_t* st_worst_state;
+    uint8_t* hcw;                 // healthcare worker flag
+    uint32_t* rank;               // position of the agent inside its location's CSR segment
+};
+
+struct DevLocs {
+    uint32_t n;
+    uint32_t n_schools;
+    const uint8_t* type;
+    float* infectiousness;
+    uint8_t* open;
+    const uint8_t* essential;
+    uint32_t* closed_until;
+    uint32_t* quarantine_until;
+    const uint32_t* schools;
+    const uint32_t* classrooms;
+    const uint32_t* classroom_offsets;
+    const uint16_t* rep;
+    uint32_t* counts;             // agents per location, built by movement
+    uint32_t* csr_off;            // [n+1]
+    uint32_t* csr_agents;         // [N]
+    uint32_t* qu_pending;         // quarantine writes of the running step
+    unsigned long long* sfix;     // [V][n] fixed-point infectiousness sums
+    float* hazard;                // [V][n] infection ratio of the last step
+    uint32_t* no_work_loc;
+    uint8_t* flags;               // testing flags
+    unsigned long long* scan_status;  // look-back tile status
+};
+
+struct DevReps {
+    uint32_t n;
+    const uint32_t* agent_off;
+    const uint32_t* loc_off;
+    const unsigned long long* seed;
+    const float* k_f;             // (float)k, as the reference casts it
+    const uint32_t* cemetery;
+    uint8_t* variant_active;      // [R][V]
+    double* expected;             // [R] expected infections accumulated since the last midnight
+};
+
+// Clock of the running day, in device memory so that one captured day graph
+// can be replayed for every day.
+struct DevClock {
+    uint32_t t0;          // timestamp of the day's midnight
+    uint32_t day_of_week; // Days, holiday mode already applied
+    float season;         // seasonality multiplier of the day
+    uint32_t scan_epoch;  // look-back status epoch
+    uint32_t scan_ticket; // dynamic tile ids of the scan
+    uint32_t scan_done;
+    uint32_t pad[2];
+};
+
+struct DevStatsAcc {      // raw per-replica daily counters
+    unsigned int c[48];
+    double imm[PSIM_MAX_STRAINS];
+};
+
+struct KArgs {
+    DevModel m;
+    DevAgents a;
+    DevLocs l;
+    DevReps r;
+    psim_params p;
+    DevClock* clock;
+    uint32_t* err;
+    DevStatsAcc* stats;   // [R]
+    uint32_t spd;         // steps per day
+    uint32_t track_expected;
+};
+
+// raw counter slots of DevStatsAcc::c
+enum {
+    SC_HOSP = 0, SC_Q, SC_QT, SC_NQ, SC_STAYED, SC_NI, SC_INF_ONCE, SC_REINF, SC_BSTR,
+    SC_ALL_INF, SC_HCI, SC_HCE, SC_INFH, SC_VNI, SC_TESTS, SC_P1, SC_P2,
+    SC_HIST = 17,          // 16 state slots follow... histogram lives in c[SC_HIST + s] for s < 16
+    SC_VAR = 33,           // infected per variant, 7 slots
+    SC_INFV = 40           // ever infected per variant, 7 slots (ends at 47)
+};
+
+// launchers (psim_kernels.cu)
+void launch_movement(const KArgs& k, uint32_t step_in_day, cudaStream_t s);
+void launch_count(const KArgs& k, cudaStream_t s);
+void launch_scan(const KArgs& k, uint32_t step_in_day, int with_hazard, int merge_quarantine, cudaStream_t s);
+void launch_scatter_draw(const KArgs& k, uint32_t step_in_day, int draw, cudaStream_t s);
+void launch_canonical_csr(const KArgs& k, cudaStream_t s);
+void launch_progress(const KArgs& k, uint32_t t, cudaStream_t s);
+void launch_test(const KArgs& k, uint32_t t, cudaStream_t s);
+void launch_stats(const KArgs& k, uint32_t t, cudaStream_t s);
+void launch_plan(const KArgs& k, uint32_t t, cudaStream_t s);
+void launch_flag_hcw(const KArgs& k, cudaStream_t s);
+void launch_bounded_wait_probe(const KArgs& k, uint32_t iters, cudaStream_t s);
+uint64_t launches_per_step(int quarantine);
+
+}  // namespace psim

@@ -1,0 +1,1207 @@
+// Hand-written sm_103a kernels of the PanSim per-timestep agent loop.
+//
+// Per step (Simulation::runSimulation, simulation.h:918-922):
+//   k_movement      RealMovementOps::doMovement (movementPolicies.h:263-1041) for every
+//                   agent, fused with the per-location histogram (warp-aggregated
+//                   atomics, the rank of each agent inside its location) and with the
+//                   per-location infectiousness reduction (Util::reduce_by_location,
+//                   util.h:48-101) as exact 2^-40 fixed-point int64 sums.
+//   k_scan          exclusive scan of the histogram into CSR offsets (single pass,
+//                   decoupled look-back), infection ratio of every location
+//                   (infectionPolicies.h:520-546), reset of the per-step counters.
+//   k_scatter_draw  CSR scatter (replaces thrust::stable_sort_by_key, util.cpp:69) fused
+//                   with the per-agent infection draw (LocationsList::infectAgents,
+//                   locationList.h:233-310).
+// Per day: k_progress (DynamicPPState::update), k_test_flag/k_test (DetailedTesting),
+// k_stats (refreshAndPrintStatistics), k_plan_* (RealMovement::planLocations).
+//
+// Built with --fmad=false: no multiply-add contraction, so every floating-point
+// expression rounds exactly like the host oracle compiled with -ffp-contract=off.
+#include "psim_device.cuh"
+
+namespace psim {
+
+__device__ __forceinline__ uint32_t wb_of(const KArgs& k, uint32_t i) {
+    return k.m.state_wb[(uint8_t)k.a.state[i]];
+}
+__device__ __forceinline__ bool infected_of(const KArgs& k, uint32_t i) {
+    return k.m.state_infected[(uint8_t)k.a.state[i]] != 0;
+}
+__device__ __forceinline__ uint8_t loc_open(const KArgs& k, uint32_t l) { return l < k.l.n ? k.l.open[l] : 0; }
+__device__ __forceinline__ uint32_t loc_closed_until(const KArgs& k, uint32_t l) {
+    return l < k.l.n ? k.l.closed_until[l] : 0u;
+}
+__device__ __forceinline__ uint32_t loc_qu(const KArgs& k, uint32_t l) { return l < k.l.n ? k.l.quarantine_until[l] : 0u; }
+__device__ __forceinline__ uint32_t loc_type(const KArgs& k, uint32_t l) { return l < k.l.n ? k.l.type[l] : NONE; }
+
+// DynamicPPState::updateMeta, dynamicPPState.cpp:54-64
+__device__ __forceinline__ void update_meta(const KArgs& k, uint32_t i) {
+    uint8_t s = (uint8_t)k.a.state[i];
+    k.a.infectious[i] = k.m.state_infectious[s] * k.m.variant_multiplier[k.a.variant[i]];
+    float su = k.m.state_susceptible[s] ? 1.0f : 0.0f;
+    for (uint32_t v = 0; v < k.m.n_variants; ++v) k.a.susceptible[(size_t)v * k.a.n + i] = su;
+}
+
+// RealMovementOps::findActualLocationForType, movementPolicies.h:69-122
+__device__ uint32_t find_location(const KArgs& k, uint32_t i, uint32_t lt, int retry, psim_stream* rng) {
+    const uint32_t b = k.a.loc_offset[i], e = k.a.loc_offset[i + 1];
+    if (lt == k.p.home_type || lt == k.p.school_type || lt == k.p.work_type) {
+        for (uint32_t j = b; j < e; ++j)
+            if (lt == k.a.poss_type[j]) return k.a.poss_loc[j];
+        return NONE;
+    }
+    uint32_t counter = 0, pos = 0;
+    for (uint32_t j = b; j < e; ++j) {
+        if (lt == k.a.poss_type[j]) {
+            if (counter == 0) pos = j;
+            counter++;
+        }
+    }
+    if (counter == 1) return k.a.poss_loc[pos];
+    if (counter > 1) {
+        uint32_t counter2 = counter, rand_idx = counter2;
+        for (;;) {
+            while (rand_idx == counter2) rand_idx = psim_below(rng, counter);
+            counter2 = 0;
+            for (uint32_t j = pos; j < e; ++j) {
+                if (lt == k.a.poss_type[j]) {
+                    if (counter2 == rand_idx) {
+                        if (retry && loc_open(k, k.a.poss_loc[j]) == 0) {
+                            retry = 0;
+                            break;
+                        }
+                        return k.a.poss_loc[j];
+                    }
+                    counter2++;
+                }
+            }
+        }
+    }
+    return NONE;
+}
+
+__device__ __forceinline__ void qu_write(const KArgs& k, uint32_t loc, uint32_t until) {
+    if (loc < k.l.n) atomicMax(&k.l.qu_pending[loc], until);
+}
+
+// RealMovementOps::quarantineAgent, movementPolicies.h:176-245
+__device__ void quarantine_agent(const KArgs& k, uint32_t i, uint32_t t, uint32_t until, psim_stream* rng) {
+    const psim_params& p = k.p;
+    if (p.quarantine_policy == 0) return;
+    if (k.a.st_diagnosed_ts[i] > 0 && !infected_of(k, i) && !p.quarantine_immune) return;
+    if (!k.a.diagnosed[i] && k.a.st_immunization_ts[i] > 0 && !p.quarantine_immune) return;
+    k.a.quarantined[i] = 1;
+    k.a.st_quarantined_ts[i] = t;
+    uint32_t prev_until = k.a.st_quarantined_until[i];
+    k.a.st_quarantined_until[i] = until;
+    k.a.st_days_in_quarantine[i] += (until - t) / (24u * 60u / p.time_step);
+    if (k.a.diagnosed[i]) {
+        uint32_t my_home = find_location(k, i, p.home_type, 0, rng);
+        if (p.quarantine_policy > 1) qu_write(k, my_home, until);
+        if (p.quarantine_policy > 2 && prev_until < t) {
+            uint32_t classroom = find_location(k, i, p.classroom_type, 0, rng);
+            uint32_t work = find_location(k, i, p.work_type, 0, rng);
+            uint32_t to_close[2] = {classroom, work};
+            for (int c = 0; c < 2; ++c) {
+                uint32_t loc = to_close[c];
+                if (loc != NONE && (loc_type(k, loc) == p.work_type || loc_type(k, loc) == p.classroom_type) &&
+                    loc_qu(k, loc) < t && loc_open(k, loc) && loc_closed_until(k, loc) < t)
+                    qu_write(k, loc, until);
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ bool is_quarantine_type(const KArgs& k, uint32_t loc) {
+    uint32_t ty = loc_type(k, loc);
+    return ty == k.p.home_type || ty == k.p.school_type || ty == k.p.classroom_type || ty == k.p.work_type;
+}
+
+__device__ void diagnose_and_quarantine(const KArgs& k, uint32_t i, uint32_t t, uint32_t sum, psim_stream* rng) {
+    const uint32_t dt = k.p.time_step;
+    k.a.diagnosed[i] = 1;
+    k.a.st_diagnosed_ts[i] = t;
+    if (sum == 24u * 60u / dt) k.a.st_diagnosed_ts[i]++;
+    quarantine_agent(k, i, t, t + k.p.quarantine_length * 24u * 60u / dt, rng);
+}
+
+__device__ __forceinline__ void stayed_home_check(const KArgs& k, uint32_t i, uint32_t agent_home) {
+    if (agent_home != NONE && k.a.location[i] != agent_home && k.a.steps_until_move[i] > 60u / k.p.time_step)
+        k.a.stayed_home[i] = 0;
+}
+
+// The full per-agent decision of doMovement once the countdown reached zero
+// (movementPolicies.h:333-1040).  The curfew and countdown prologue is in
+// k_movement.
+__device__ void move_decide(const KArgs& k, uint32_t i, uint32_t t, uint32_t minutes, uint32_t day, uint32_t sum,
+                            psim_stream* rng) {
+    const psim_params& p = k.p;
+    const uint32_t dt = p.time_step;
+    uint32_t* sum_ptr = &k.a.steps_until_move[i];
+    if (k.a.st_quarantined_until[i] <= t) k.a.quarantined[i] = 0;
+
+    uint32_t wb = wb_of(k, i);
+    if (wb == WB_D) {
+        *sum_ptr = NONE;
+        k.a.location[i] = k.r.cemetery[k.a.rep[i]];
+        return;
+    }
+    uint32_t agent_home = find_location(k, i, p.home_type, 0, rng);
+
+    if (k.a.st_hospitalized_ts[i] <= t && k.a.st_hospitalized_until[i] > t && wb != WB_S && wb != WB_D) {
+        uint32_t x = k.a.st_hospitalized_until[i] - t - 1;
+        *sum_ptr = x < sum ? x : sum;
+        k.a.location[i] = find_location(k, i, p.hospital_type, 0, rng);
+        if (!k.a.diagnosed[i] && k.a.infectious[i] != 0.0f) diagnose_and_quarantine(k, i, t, sum, rng);
+        return;
+    }
+    if (wb == WB_S) {
+        *sum_ptr = sum;
+        k.a.location[i] = find_location(k, i, p.hospital_type, 0, rng);
+        if (!k.a.diagnosed[i] && k.a.infectious[i] != 0.0f) diagnose_and_quarantine(k, i, t, sum, rng);
+        return;
+    }
+    {
+        uint32_t loc = k.a.location[i];
+        if (p.quarantine_policy > 1 && t < loc_qu(k, loc) && is_quarantine_type(k, loc)) {
+            if (k.a.quarantined[i] == 0) quarantine_agent(k, i, t, loc_qu(k, loc), rng);
+            if (k.a.quarantined[i]) {
+                uint32_t x = loc_qu(k, k.a.location[i]) - t - 1;
+                *sum_ptr = x < sum ? x : sum;
+                uint32_t home_location = find_location(k, i, p.home_type, 0, rng);
+                if (home_location != k.a.location[i]) k.a.location[i] = home_location;
+                stayed_home_check(k, i, agent_home);
+                return;
+            }
+        }
+    }
+    if ((p.quarantine_policy > 0 &&
+         (k.a.diagnosed[i] ||
+          (k.a.st_diagnosed_ts[i] > 0 && (t - k.a.st_diagnosed_ts[i]) < p.quarantine_length * 24u * 60u / dt))) ||
+        (p.quarantine_policy > 0 && k.a.quarantined[i])) {
+        if (p.quarantine_policy > 0 && !k.a.quarantined[i])
+            quarantine_agent(k, i, t, t + p.quarantine_length * 24u * 60u / dt, rng);
+        if (k.a.quarantined[i]) {
+            k.a.location[i] = find_location(k, i, p.home_type, 0, rng);
+            *sum_ptr = sum;
+            stayed_home_check(k, i, agent_home);
+            return;
+        }
+    }
+
+    // schedule window (AgentTypeList::getOffsetIndex, agentType.cpp:13-15)
+    const uint32_t agent_type = k.a.type[i];
+    const uint32_t off_idx = 7u * wb + day + agent_type * 28u;
+    const uint32_t ev_b = k.m.event_offset[off_idx], ev_e = k.m.event_offset[off_idx + 1];
+    int act_b = -1, act_e = -1;
+    for (uint32_t j = ev_b; j < ev_e; ++j) {
+        uint32_t st = k.m.ev_start[j], en = k.m.ev_end[j];
+        if (minutes >= st && minutes < en && act_b == -1) act_b = (int)j;
+        if (minutes < st) {
+            act_e = (int)j;
+            break;
+        }
+        if (j == ev_e - 1 && minutes >= st && minutes < en) act_e = (int)ev_e;
+    }
+
+    uint32_t new_type = NONE;
+    if (act_b == -1 && act_e == -1) {  // Case 1
+        new_type = wb == WB_S ? p.hospital_type : p.home_type;
+        k.a.location[i] = find_location(k, i, new_type, 0, rng);
+        *sum_ptr = sum;
+    }
+    if (act_b != -1) {  // Case 2 and 4
+        uint32_t num_pot = (uint32_t)((act_e == -1 ? act_b + 1 : act_e) - act_b);
+        uint32_t picked = 0, dur = 0;
+        if (num_pot == 1) {
+            new_type = k.m.ev_loc_type[act_b];
+            dur = k.m.ev_duration[act_b];
+        } else {
+            double rnd = psim_u01(rng) * 1.0;
+            double thr = k.m.ev_chance[act_b];
+            uint32_t idx = 0;
+            while (rnd > thr && idx < num_pot) {
+                idx++;
+                thr += k.m.ev_chance[act_b + idx];
+            }
+            if (idx == num_pot) idx--;
+            picked = idx;
+            new_type = k.m.ev_loc_type[act_b + idx];
+            dur = k.m.ev_duration[act_b + idx];
+        }
+        if (k.a.no_work[i] != 0 && new_type == p.work_type) {
+            new_type = p.home_type;
+            num_pot = 1;
+            if (k.a.quarantined[i] == 0) k.a.st_days_in_quarantine[i]++;
+        }
+        uint32_t new_loc = find_location(k, i, new_type, num_pot == 1, rng);
+        bool too_old = (new_type == p.school_type || new_type == p.classroom_type) && k.a.age[i] >= p.school_age_restriction;
+        if (too_old || ((loc_open(k, new_loc) == 0 || loc_closed_until(k, new_loc) > t) && new_type != p.work_type) ||
+            (p.lockdown_nonvacc && k.a.st_immunization_ts[i] == 0)) {
+            if (num_pot > 1) {
+                double rnd = psim_u01(rng) * 1.0;
+                double pc = k.m.ev_chance[act_b + picked];
+                double thr = (picked == 0) ? 0.0 : k.m.ev_chance[act_b] / (1.0 - pc);
+                uint32_t idx = 0;
+                while (rnd > thr && idx < num_pot) {
+                    idx++;
+                    thr += (picked == idx) ? 0.0 : k.m.ev_chance[act_b + idx] / (1.0 - pc);
+                }
+                if (idx == num_pot) idx--;
+                new_type = k.m.ev_loc_type[act_b + idx];
+                dur = k.m.ev_duration[act_b + idx];
+                new_loc = find_location(k, i, new_type, 0, rng);
+                if (too_old ||
+                    ((loc_open(k, new_loc) == 0 || loc_closed_until(k, new_loc) > t) && new_type != p.work_type) ||
+                    (p.lockdown_nonvacc && k.a.st_immunization_ts[i] == 0))
+                    new_loc = find_location(k, i, p.home_type, 0, rng);
+            } else {
+                new_loc = find_location(k, i, p.home_type, 0, rng);
+            }
+        } else if (new_type == p.school_type) {
+            uint32_t my_class = find_location(k, i, p.classroom_type, 0, rng);
+            if (my_class != NONE && loc_closed_until(k, my_class) > t) new_loc = find_location(k, i, p.home_type, 0, rng);
+        }
+        k.a.location[i] = new_loc;
+        if (dur / 60u > 24u) {
+            *sum_ptr = sum;
+        } else if (act_e == -1) {
+            *sum_ptr = (minutes + dur >= 1440u) ? sum : dur / dt;
+        } else {
+            uint32_t nstart = k.m.ev_start[act_e], nend = k.m.ev_end[act_e];
+            if (minutes + dur < nstart) {
+                *sum_ptr = dur / dt;
+            } else if (minutes + dur > nend) {
+                *sum_ptr = (nend - minutes) / dt - 1u;
+            } else {
+                uint32_t st = (nend - (minutes + dur)) / dt;
+                uint32_t extra = psim_below(rng, st);
+                *sum_ptr = dur / dt + extra;
+            }
+        }
+        if (agent_type + 1 == 7 && p.enable_curfew && (p.curfew_begin <= minutes / dt || p.curfew_end > minutes / dt)) {
+            bool work_closed = new_type == p.work_type && (loc_open(k, new_loc) == 0 || loc_closed_until(k, new_loc) > t);
+            if (work_closed || (new_type != p.work_type && new_type != p.home_type)) k.a.location[i] = agent_home;
+        }
+    }
+    if (act_b == -1 && act_e != -1) {  // Case 3
+        uint32_t length_steps = (uint32_t)(k.m.ev_end[act_e] - k.m.ev_start[act_e]) / dt;
+        uint32_t delay = psim_below(rng, length_steps);
+        *sum_ptr = (k.m.ev_start[act_e] - minutes) / dt + delay;
+        uint32_t left = *sum_ptr;
+        if (left < 30u / dt) {
+        } else if (left < 60u / dt) {
+            new_type = p.public_type;
+            k.a.location[i] = find_location(k, i, p.public_type, 0, rng);
+        } else {
+            new_type = p.home_type;
+            k.a.location[i] = find_location(k, i, p.home_type, 0, rng);
+        }
+    }
+    {
+        uint32_t loc = k.a.location[i];
+        if (p.quarantine_policy > 1 && t < loc_qu(k, loc) && is_quarantine_type(k, loc)) {
+            if (!k.a.quarantined[i]) quarantine_agent(k, i, t, loc_qu(k, loc), rng);
+            if (k.a.quarantined[i]) {
+                uint32_t x = loc_qu(k, k.a.location[i]) - t - 1;
+                *sum_ptr = x < sum ? x : sum;
+                uint32_t home_location = find_location(k, i, p.home_type, 0, rng);
+                if (home_location != k.a.location[i]) k.a.location[i] = home_location;
+                stayed_home_check(k, i, agent_home);
+                return;
+            }
+        }
+    }
+    if (new_type == p.hospital_type || (new_type == p.doctor_type && psim_u01(rng) * 1.0 < 0.7)) {
+        if (!k.a.diagnosed[i] && k.a.infectious[i] != 0.0f) diagnose_and_quarantine(k, i, t, sum, rng);
+    }
+    stayed_home_check(k, i, agent_home);
+    *sum_ptr = *sum_ptr - 1u;
+}
+
+// curfew prologue of doMovement (movementPolicies.h:267-326); returns true if
+// the agent's step is finished.
+__device__ bool curfew_prologue(const KArgs& k, uint32_t i, uint32_t t, uint32_t sum, psim_stream* rng) {
+    const psim_params& p = k.p;
+    uint32_t wb = wb_of(k, i);
+    bool dead_or_hosp = (wb == WB_D || wb == WB_S);
+    bool hosp_noncovid = (k.a.st_hospitalized_ts[i] <= t && k.a.st_hospitalized_until[i] > t);
+    if (dead_or_hosp || hosp_noncovid) return false;
+    if (k.a.type[i] + 1u == 7u) {
+        uint32_t workplace = find_location(k, i, p.work_type, 0, rng);
+        if (k.a.location[i] != workplace || workplace == NONE || loc_open(k, workplace) == 0) {
+            k.a.location[i] = find_location(k, i, p.home_type, 0, rng);
+            if (workplace == NONE || loc_open(k, workplace) == 0) {
+                k.a.steps_until_move[i] = sum;
+                return true;
+            }
+        }
+        return false;
+    }
+    k.a.steps_until_move[i] = sum;
+    k.a.location[i] = find_location(k, i, p.home_type, 0, rng);
+    return true;
+}
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Movement of every agent + histogram/rank + fixed-point infectiousness sums.
+__global__ void __launch_bounds__(256) k_movement(KArgs k, uint32_t step) {
+    const uint32_t N = k.a.n;
+    const uint32_t t = k.clock->t0 + step;
+    const uint32_t dt = k.p.time_step;
+    const uint32_t minutes = step * dt;
+    const uint32_t day = k.clock->day_of_week;
+    const uint32_t sum = (1440u - minutes) / dt;
+    const bool curfew_now = k.p.enable_curfew && k.p.curfew_begin == minutes / dt;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t L = k.l.n;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < N; base += stride) {
+        const uint32_t i = base + threadIdx.x;
+        const bool act = i < N;
+        uint32_t loc = NONE;
+        if (act) {
+            uint32_t s = k.a.steps_until_move[i];
+            bool done = false;
+            if (curfew_now || s == 0) {
+                const uint32_t rep = k.a.rep[i];
+                psim_stream rng;
+                psim_stream_init(&rng, k.r.seed[rep], i - k.r.agent_off[rep], t, PSIM_PHASE_MOVE);
+                if (curfew_now) done = curfew_prologue(k, i, t, sum, &rng);
+                if (!done) {
+                    s = k.a.steps_until_move[i];
+                    if (s > 0) {
+                        k.a.steps_until_move[i] = s - 1;
+                    } else {
+                        move_decide(k, i, t, minutes, day, sum, &rng);
+                    }
+                }
+            } else {
+                k.a.steps_until_move[i] = s - 1;
+            }
+            loc = k.a.location[i];
+            if (loc >= L) {
+                atomicOr(k.err, ERR_LOCATION);
+                loc = NONE;
+            }
+        }
+        // histogram with warp-aggregated atomics; the rank of an agent among
+        // the warp's agents at the same location follows lane (= agent) order
+        const unsigned valid = __ballot_sync(0xffffffffu, act && loc != NONE);
+        if (act && loc != NONE) {
+            const unsigned peers = __match_any_sync(valid, loc);
+            const int leader = __ffs(peers) - 1;
+            uint32_t basecnt = 0;
+            if ((int)(threadIdx.x & 31) == leader) basecnt = atomicAdd(&k.l.counts[loc], (uint32_t)__popc(peers));
+            basecnt = __shfl_sync(peers, basecnt, leader);
+            k.a.rank[i] = basecnt + (uint32_t)__popc(peers & lanemask_lt());
+            const float inf = k.a.infectious[i];
+            if (inf > 0.0f) {
+                const long long q = __float2ll_rn(inf * PSIM_FIX_SCALE_F);
+                atomicAdd(&k.l.sfix[(size_t)k.a.variant[i] * L + loc], (unsigned long long)q);
+            }
+        } else if (act) {
+            k.a.rank[i] = NONE;
+        }
+    }
+}
+
+// Histogram + fixed-point sums without movement (regroup after an upload).
+__global__ void __launch_bounds__(256) k_count(KArgs k) {
+    const uint32_t N = k.a.n, L = k.l.n;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < N; base += stride) {
+        const uint32_t i = base + threadIdx.x;
+        const bool act = i < N;
+        uint32_t loc = act ? k.a.location[i] : NONE;
+        if (act && loc >= L) {
+            atomicOr(k.err, ERR_LOCATION);
+            loc = NONE;
+        }
+        const unsigned valid = __ballot_sync(0xffffffffu, act && loc != NONE);
+        if (act && loc != NONE) {
+            const unsigned peers = __match_any_sync(valid, loc);
+            const int leader = __ffs(peers) - 1;
+            uint32_t basecnt = 0;
+            if ((int)(threadIdx.x & 31) == leader) basecnt = atomicAdd(&k.l.counts[loc], (uint32_t)__popc(peers));
+            basecnt = __shfl_sync(peers, basecnt, leader);
+            k.a.rank[i] = basecnt + (uint32_t)__popc(peers & lanemask_lt());
+            const float inf = k.a.infectious[i];
+            if (inf > 0.0f) {
+                const long long q = __float2ll_rn(inf * PSIM_FIX_SCALE_F);
+                atomicAdd(&k.l.sfix[(size_t)k.a.variant[i] * L + loc], (unsigned long long)q);
+            }
+        } else if (act) {
+            k.a.rank[i] = NONE;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Scan of the histogram (decoupled look-back, Merrill & Garland 2016).
+// Tile status word: [63:62] flag (1 aggregate, 2 inclusive) [61:32] epoch [31:0] value
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 8;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+constexpr uint32_t SCAN_SPIN_LIMIT = 1u << 22;
+
+__device__ __forceinline__ unsigned long long pack_status(uint32_t flag, uint32_t epoch, uint32_t value) {
+    return ((unsigned long long)flag << 62) | ((unsigned long long)(epoch & 0x3FFFFFFFu) << 32) | value;
+}
+
+// infection ratio r_l = 1 - exp(-k * (S_l / n_l) * w_l * season * dt),
+// infectionPolicies.h:523-546, evaluated in FP64 and rounded to FP32.
+__device__ __forceinline__ float hazard_of(long long fix, uint32_t n, float k_f, float w, float season, uint32_t dt) {
+    if (fix == 0 || n == 0) return 0.0f;
+    double S = (double)fix * PSIM_FIX_INV;
+    double dens = S / (double)n;
+    double x = (double)k_f * dens;
+    x = x * (double)w;
+    x = x * (double)season;
+    x = x * (double)dt;
+    return (float)psim_one_minus_exp(x);
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, int with_hazard, int merge_q) {
+    __shared__ uint32_t s_tile, s_epoch, s_prefix;
+    __shared__ uint32_t s_warp[SCAN_THREADS / 32];
+    const uint32_t L = k.l.n;
+    DevClock* clk = k.clock;
+    if (threadIdx.x == 0) {
+        s_epoch = *((volatile uint32_t*)&clk->scan_epoch);
+        s_tile = atomicAdd(&clk->scan_ticket, 1u);
+    }
+    __syncthreads();
+    const uint32_t tile = s_tile, epoch = s_epoch;
+    const uint32_t first = tile * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
+    uint32_t c[SCAN_ITEMS];
+    uint32_t tsum = 0;
+#pragma unroll
+    for (int j = 0; j < SCAN_ITEMS; ++j) {
+        uint32_t l = first + j;
+        c[j] = l < L ? k.l.counts[l] : 0u;
+        tsum += c[j];
+    }
+    // block exclusive scan of thread sums
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = tsum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += y;
+    }
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < SCAN_THREADS / 32 ? s_warp[lane] : 0u;
+        uint32_t wi = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= o) wi += y;
+        }
+        if (lane < SCAN_THREADS / 32) s_warp[lane] = wi - w;  // exclusive warp offsets
+        if (lane == SCAN_THREADS / 32 - 1) {
+            // tile aggregate -> look-back
+            const uint32_t agg = wi;
+            volatile unsigned long long* st = (volatile unsigned long long*)k.l.scan_status;
+            uint32_t prefix = 0;
+            if (tile == 0) {
+                __threadfence();
+                st[0] = pack_status(2, epoch, agg);
+            } else {
+                __threadfence();
+                st[tile] = pack_status(1, epoch, agg);
+                int j = (int)tile - 1;
+                uint32_t spins = 0;
+                while (j >= 0) {
+                    unsigned long long w64 = st[j];
+                    uint32_t flag = (uint32_t)(w64 >> 62);
+                    uint32_t ep = (uint32_t)(w64 >> 32) & 0x3FFFFFFFu;
+                    if (ep != (epoch & 0x3FFFFFFFu)) flag = 0;
+                    if (flag == 0) {
+                        if (++spins > SCAN_SPIN_LIMIT) {
+                            atomicOr(k.err, ERR_SCAN_WAIT);
+                            break;
+                        }
+                        continue;
+                    }
+                    prefix += (uint32_t)w64;
+                    if (flag == 2) break;
+                    --j;
+                }
+                __threadfence();
+                st[tile] = pack_status(2, epoch, prefix + agg);
+            }
+            s_prefix = prefix;
+        }
+    }
+    __syncthreads();
+    uint32_t run = s_prefix + s_warp[warp] + (incl - tsum);
+    const uint32_t dt = k.p.time_step;
+    const float season = clk->season;
+#pragma unroll
+    for (int j = 0; j < SCAN_ITEMS; ++j) {
+        uint32_t l = first + j;
+        if (l < L) {
+            k.l.csr_off[l] = run;
+            k.l.counts[l] = 0u;
+            if (with_hazard) {
+                const uint32_t rep = k.l.rep[l];
+                const float kf = k.r.k_f[rep];
+                const float w = k.l.infectiousness[l];
+                for (uint32_t v = 0; v < k.m.n_variants; ++v) {
+                    const size_t idx = (size_t)v * L + l;
+                    const long long fix = (long long)k.l.sfix[idx];
+                    k.l.hazard[idx] = hazard_of(fix, c[j], kf, w, season, dt);
+                    if (fix != 0) k.l.sfix[idx] = 0ull;
+                }
+            }
+            if (merge_q) {
+                uint32_t q = k.l.qu_pending[l];
+                if (q) {
+                    if (q > k.l.quarantine_until[l]) k.l.quarantine_until[l] = q;
+                    k.l.qu_pending[l] = 0u;
+                }
+            }
+        }
+        run += c[j];
+        if (l + 1 == L) k.l.csr_off[L] = run;
+    }
+    // the last block to finish resets the tickets and advances the epoch
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        uint32_t done = atomicAdd(&clk->scan_done, 1u);
+        if (done == gridDim.x - 1) {
+            clk->scan_done = 0u;
+            clk->scan_ticket = 0u;
+            __threadfence();
+            clk->scan_epoch = epoch + 1u;
+        }
+    }
+}
+
+// CSR scatter + infection draw.
+__global__ void __launch_bounds__(256) k_scatter_draw(KArgs k, uint32_t step, int draw) {
+    const uint32_t N = k.a.n, L = k.l.n, V = k.m.n_variants;
+    const uint32_t t = k.clock->t0 + step;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < N; base += stride) {
+        const uint32_t i = base + threadIdx.x;
+        const bool act = i < N;
+        double term_sum = 0.0;
+        uint32_t rep = 0;
+        if (act) {
+            const uint32_t loc = k.a.location[i];
+            const uint32_t r = k.a.rank[i];
+            if (loc < L && r != NONE) k.l.csr_agents[k.l.csr_off[loc] + r] = i;
+            rep = k.a.rep[i];
+            if (draw && loc < L) {
+                for (uint32_t v = 0; v < V; ++v) {
+                    if (!k.r.variant_active[rep * V + v]) continue;
+                    const float h = k.l.hazard[(size_t)v * L + loc];
+                    if (h > 0.0f) {
+                        const float su = k.a.susceptible[(size_t)v * N + i];
+                        const float s_eff = su * k.p.sigma_band[k.a.band[i]];
+                        if (s_eff > 0.0f) {
+                            const float pf = h * s_eff;
+                            term_sum += pf < 1.0f ? (double)pf : 1.0;
+                            const double U = psim_u01_once(k.r.seed[rep], i - k.r.agent_off[rep], t, PSIM_PHASE_INFECT + v);
+                            if (U < (double)pf) {
+                                // DynamicPPState::gotInfected + stats, locationList.h:283-291
+                                k.a.state[i] = (int8_t)k.m.first_infected;
+                                k.a.variant[i] = (uint8_t)v;
+                                k.a.days[i] = -2;
+                                update_meta(k, i);
+                                k.a.st_infected_ts[i] = t;
+                                k.a.st_infected_count[i] = k.a.st_infected_count[i] + 1;
+                                k.a.st_infected_loc[i] = loc;
+                                k.a.st_worst_state[i] = (int8_t)k.m.first_infected;
+                                k.a.st_worst_ts[i] = t;
+                                k.a.st_variant_mask[i] |= 1u << v;
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        if (k.track_expected) {
+            // warp reduction per replica, one atomic per replica present in the warp
+            const unsigned am = __ballot_sync(0xffffffffu, act);
+            if (act) {
+                const unsigned peers = __match_any_sync(am, rep);
+                double s = term_sum;
+                // reduce within peer group: simple loop over peers
+                const int leader = __ffs(peers) - 1;
+                unsigned rest = peers;
+                double tot = 0.0;
+                while (rest) {
+                    int src = __ffs(rest) - 1;
+                    tot += __shfl_sync(peers, s, src);
+                    rest &= rest - 1;
+                }
+                if ((int)(threadIdx.x & 31) == leader && tot != 0.0) atomicAdd(&k.r.expected[rep], tot);
+            }
+        }
+    }
+}
+
+// Canonical CSR order (ascending agent id inside a location, the output of
+// thrust::stable_sort_by_key): the final position of agent x in its segment is
+// the number of agents of the segment with a smaller id.  O(sum n_l^2); used
+// on demand only.
+__global__ void k_canonical_rank(KArgs k, uint32_t* tmp) {
+    const uint32_t N = k.a.n;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < N; j += gridDim.x * blockDim.x) {
+        const uint32_t x = k.l.csr_agents[j];
+        const uint32_t l = k.a.location[x];
+        const uint32_t b = k.l.csr_off[l], e = k.l.csr_off[l + 1];
+        uint32_t c = 0;
+        for (uint32_t q = b; q < e; ++q) c += k.l.csr_agents[q] < x;
+        tmp[b + c] = x;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Daily progression: Simulation::updateAgents (simulation.h:425-471),
+// DynamicPPState::update (dynamicPPState.cpp:246-303),
+// MultiBadMatrix::calculateNextState / selectNext (multiBadMatrix.cpp:9-31,120-125),
+// LengthOfState::calculateDays (basicLengthAbstract.cpp:48-53).
+// The transition tables are staged in shared memory.
+struct ProgTables {
+    const uint32_t* bad_begin;
+    const uint32_t* bad_count;
+    const uint32_t* neu_begin;
+    const uint32_t* neu_count;
+    const uint32_t* next;
+    const float* chance;
+};
+
+__device__ int calc_days(const KArgs& k, uint32_t pid, uint32_t state, uint32_t v, psim_stream* rng) {
+    const size_t idx = ((size_t)pid * k.m.n_states + state) * PSIM_MAX_STRAINS + v;
+    if (k.m.len_avg[idx] == -1.0f) return -1;
+    const uint32_t thr = k.m.len_thr[idx];
+    const float mx = k.m.len_max[idx];
+    int days = psim_geometric(rng, thr);
+    while (mx < (float)days) days = psim_geometric(rng, thr);
+    return days;
+}
+
+__device__ uint32_t select_next(const ProgTables& T, size_t ti, float scaling, psim_stream* rng, int* bad) {
+    const uint32_t bb = T.bad_begin[ti], bc = T.bad_count[ti], nb = T.neu_begin[ti], nc = T.neu_count[ti];
+    if (nc == 0) scaling = 1.0f;
+    const double random = psim_u01(rng);
+    double pre = 0.0, bad_sum = 0.0;
+    for (uint32_t q = 0; q < bc; ++q) {
+        float c = T.chance[bb + q] * scaling;
+        pre += (double)c;
+        if (random < pre) {
+            *bad = 1;
+            return T.next[bb + q];
+        }
+        bad_sum += (double)T.chance[bb + q];
+    }
+    double bad_scaling = 1.0 + ((bad_sum - pre) / (1.0 - bad_sum));
+    if (bc == 0) bad_scaling = 1.0;
+    uint32_t idx = 0;
+    do {
+        double c = (double)T.chance[nb + idx] * bad_scaling;
+        pre += c;
+        ++idx;
+    } while (pre < random && idx < nc);
+    idx--;
+    *bad = 0;
+    return T.next[nb + idx];
+}
+
+__global__ void __launch_bounds__(256) k_progress(KArgs k, uint32_t t, int staged) {
+    extern __shared__ uint32_t smem[];
+    const uint32_t nt = k.m.n_prog * k.m.n_states;
+    ProgTables T;
+    if (staged) {
+        uint32_t* s = smem;
+        uint32_t* bb = s;
+        uint32_t* bc = bb + nt;
+        uint32_t* nb = bc + nt;
+        uint32_t* nc = nb + nt;
+        uint32_t* nx = nc + nt;
+        float* ch = (float*)(nx + k.m.n_trans);
+        for (uint32_t j = threadIdx.x; j < nt; j += blockDim.x) {
+            bb[j] = k.m.tr_bad_begin[j];
+            bc[j] = k.m.tr_bad_count[j];
+            nb[j] = k.m.tr_neu_begin[j];
+            nc[j] = k.m.tr_neu_count[j];
+        }
+        for (uint32_t j = threadIdx.x; j < k.m.n_trans; j += blockDim.x) {
+            nx[j] = k.m.tr_next[j];
+            ch[j] = k.m.tr_chance[j];
+        }
+        __syncthreads();
+        T = ProgTables{bb, bc, nb, nc, nx, ch};
+    } else {
+        T = ProgTables{k.m.tr_bad_begin, k.m.tr_bad_count, k.m.tr_neu_begin, k.m.tr_neu_count, k.m.tr_next,
+                       k.m.tr_chance};
+    }
+    const uint32_t N = k.a.n;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+        int16_t days = k.a.days[i];
+        if (days > 0) {  // the common case: count down
+            k.a.days[i] = days - 1;
+            continue;
+        }
+        if (days != -2 && days != 0) continue;
+        const uint32_t rep = k.a.rep[i];
+        psim_stream rng;
+        psim_stream_init(&rng, k.r.seed[rep], i - k.r.agent_off[rep], t, PSIM_PHASE_PROGRESS);
+        const uint32_t v = k.a.variant[i];
+        const uint32_t st = (uint8_t)k.a.state[i];
+        const uint32_t pid = k.a.prog_id[i];
+        const float meta = k.a.symptom_scaling[i];
+        const float prog = (st == 7) ? k.m.death_scaling[v] / meta : k.m.prog_scaling[v];
+        const float scaling = meta * prog;
+        if (days == -2) {
+            days = (int16_t)calc_days(k, pid, st, v, &rng);
+            if (v >= 3) days = (days * 0.7 == 0) ? 1 : (int16_t)(days * 0.7);
+        }
+        bool recovered = false;
+        if (days == 0) {
+            const bool was_infected = k.m.state_infected[st] != 0;
+            int bad = 0;
+            const uint32_t next = select_next(T, (size_t)pid * k.m.n_states + st, scaling, &rng, &bad);
+            const int nd = calc_days(k, pid, next, v, &rng);
+            k.a.state[i] = (int8_t)next;
+            update_meta(k, i);
+            days = (int16_t)nd;
+            if (v >= 3 && next < 8) {
+                const float mul = next < 6 ? 0.7f : 0.5f;
+                days = (days * mul == 0) ? 1 : (int16_t)(days * mul);
+            }
+            if (bad) {
+                k.a.st_worst_state[i] = (int8_t)next;
+                k.a.st_worst_ts[i] = t;
+                k.a.st_worst_end_ts[i] = t + ((uint32_t)((int)days * 60 * 24)) / k.p.time_step;
+            } else if (st != next) {
+                if (was_infected && !k.m.state_infected[next]) {
+                    k.a.st_recovered_ts[i] = t;
+                    recovered = true;
+                }
+            }
+        }
+        k.a.days[i] = days;
+        if (recovered) k.a.diagnosed[i] = 0;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Testing: DetailedTesting::performTests (testingPolicies.h:370-475)
+__device__ __forceinline__ bool quarantine_window_ok(uint32_t qu, uint32_t t, uint32_t ql_steps, uint32_t day_steps) {
+    return qu == 0 || (qu != 0 && (qu - ql_steps >= t - day_steps || qu < t));
+}
+
+// flagLocations, testingPolicies.h:64-148
+__global__ void __launch_bounds__(256) k_test_flag(KArgs k, uint32_t t) {
+    const psim_params& p = k.p;
+    const uint32_t day_steps = 24u * 60u / p.time_step;
+    const uint32_t ql_steps = p.quarantine_length * 24u * 60u / p.time_step;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < k.a.n; i += gridDim.x * blockDim.x) {
+        if (!(k.a.st_diagnosed_ts[i] > t - day_steps)) continue;
+        const uint32_t rep = k.a.rep[i];
+        psim_stream rng;
+        psim_stream_init(&rng, k.r.seed[rep], i - k.r.agent_off[rep], t, PSIM_PHASE_TEST_FLAG);
+        uint32_t home = find_location(k, i, p.home_type, 0, &rng);
+        if (home != NONE && home < k.l.n) k.l.flags[home] = 1;
+        uint32_t work = find_location(k, i, p.work_type, 0, &rng);
+        if (work != NONE && work < k.l.n && quarantine_window_ok(k.l.quarantine_until[work], t, ql_steps, day_steps))
+            k.l.flags[work] = 1;
+        uint32_t school = find_location(k, i, p.school_type, 0, &rng);
+        if (school != NONE && school < k.l.n &&
+            quarantine_window_ok(k.l.quarantine_until[school], t, ql_steps, day_steps)) {
+            k.l.flags[school] = 1;
+            uint32_t classroom = find_location(k, i, p.classroom_type, 0, &rng);
+            if (classroom != NONE && classroom < k.l.n &&
+                quarantine_window_ok(k.l.quarantine_until[classroom], t, ql_steps, day_steps))
+                k.l.flags[classroom] = 1;
+        }
+    }
+}
+
+// doTesting, testingPolicies.h:162-281
+__global__ void __launch_bounds__(256) k_test(KArgs k, uint32_t t) {
+    const psim_params& p = k.p;
+    const uint32_t day_steps = 24u * 60u / p.time_step;
+    const uint32_t delay_steps = p.testing_delay * 24u * 60u / p.time_step;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < k.a.n; i += gridDim.x * blockDim.x) {
+        if (t > delay_steps && k.a.last_test[i] != NONE && k.a.last_test[i] > t - delay_steps) continue;
+        if (wb_of(k, i) == WB_D || k.a.diagnosed[i]) continue;
+        const uint32_t rep = k.a.rep[i];
+        psim_stream rng;
+        psim_stream_init(&rng, k.r.seed[rep], i - k.r.agent_off[rep], t, PSIM_PHASE_TEST);
+        uint32_t home = find_location(k, i, p.home_type, 0, &rng);
+        int home_flag = (home != NONE && home < k.l.n) ? k.l.flags[home] : 0;
+        uint32_t work = find_location(k, i, p.work_type, 0, &rng);
+        int work_flag = (work != NONE && work < k.l.n) ? k.l.flags[work] : 0;
+        uint32_t school = find_location(k, i, p.school_type, 0, &rng);
+        int school_flag = 0, class_flag = 0;
+        if (school != NONE && school < k.l.n) {
+            school_flag = k.l.flags[school];
+            uint32_t classroom = find_location(k, i, p.classroom_type, 0, &rng);
+            if (classroom != NONE) class_flag = 1;
+        }
+        double prob = p.t_random;
+        prob = prob + (double)home_flag * p.t_home;
+        prob = prob + (double)work_flag * p.t_work;
+        prob = prob + (double)school_flag * p.t_school;
+        prob = prob + ((double)class_flag * 3.0) * p.t_school;
+        if (work != NONE && (loc_type(k, work) == p.doctor_type || loc_type(k, work) == p.hospital_type))
+            prob = prob + p.t_hospital;
+        if (work != NONE && loc_type(k, work) == p.nursery_type) prob = prob + p.t_nursery;
+        if (k.a.st_hospitalized_ts[i] <= t && k.a.st_hospitalized_until[i] > t) prob = prob + p.t_hospital;
+        if (prob > 1.0 || psim_u01(&rng) * 1.0 < prob) {
+            k.a.last_test[i] = t;
+            if (infected_of(k, i)) {
+                const uint8_t st = (uint8_t)k.a.state[i];
+                const float acc = p.use_pcr ? k.m.state_acc_pcr[st] : k.m.state_acc_antigen[st];
+                if ((double)acc > psim_u01(&rng) * 1.0) {
+                    k.a.diagnosed[i] = 1;
+                    k.a.st_diagnosed_ts[i] = t;
+                }
+            } else {
+                if (k.a.st_quarantined_until[i] > t && (home != NONE && loc_qu(k, home) < t)) {
+                    if (k.a.st_days_in_quarantine[i] > 0)
+                        k.a.st_days_in_quarantine[i] -= (k.a.st_quarantined_until[i] - t) / day_steps;
+                    k.a.st_quarantined_until[i] = t;
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Daily statistics (Simulation::refreshAndPrintStatistics, simulation.h:473-665;
+// Statistic::refreshandGetAfterMidnight, statistics.h:28-56; countVariantCases
+// :768-777; the testing counts of performTests, testingPolicies.h:458-473).
+// One pass over the agents; raw counters per replica, the row is assembled on
+// the host.
+constexpr int STAT_FIELDS = 48;
+
+__global__ void __launch_bounds__(256) k_stats(KArgs k, uint32_t t, int with_tests) {
+    const uint32_t N = k.a.n, V = k.m.n_variants;
+    const uint32_t day_steps = 24u * 60u / k.p.time_step;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool act = i < N;
+    unsigned c[STAT_FIELDS];
+#pragma unroll
+    for (int f = 0; f < STAT_FIELDS; ++f) c[f] = 0;
+    double imm[PSIM_MAX_STRAINS];
+#pragma unroll
+    for (int v = 0; v < PSIM_MAX_STRAINS; ++v) imm[v] = 0.0;
+    uint32_t rep = 0;
+    if (act) {
+        rep = k.a.rep[i];
+        const uint8_t st = (uint8_t)k.a.state[i];
+        const uint32_t wb = k.m.state_wb[st];
+        const bool inf = k.m.state_infected[st] != 0;
+        c[SC_HOSP] = (wb != WB_D && wb != WB_S && t < k.a.st_hospitalized_until[i]);
+        const bool isq = k.a.st_quarantined_ts[i] <= t && k.a.st_quarantined_until[i] > t;
+        c[SC_Q] = isq;
+        c[SC_QT] = isq && inf;
+        c[SC_NQ] = !isq && inf;
+        c[SC_STAYED] = k.a.stayed_home[i] != 0;
+        const bool new_inf = k.a.st_infected_ts[i] > t - day_steps && k.a.st_infected_ts[i] <= t;
+        c[SC_NI] = new_inf;
+        const uint32_t ic = k.a.st_infected_count[i], mc = k.a.st_immunization_count[i];
+        c[SC_INF_ONCE] = ic > 0;
+        c[SC_REINF] = ic > 1 ? ic - 1 : 0;
+        c[SC_BSTR] = mc > 1 ? mc - 1 : 0;
+        c[SC_ALL_INF] = inf;
+        if (k.a.hcw[i]) {
+            c[SC_HCI] = (inf || k.a.quarantined[i]) ? 1u : 0u;
+            c[SC_HCE] = new_inf;
+        }
+        c[SC_INFH] = inf && loc_type(k, k.a.location[i]) == k.p.hospital_type;
+        c[SC_VNI] = ic == 0 && mc > 0;
+        if (with_tests) {
+            c[SC_TESTS] = k.a.last_test[i] == t;
+            const uint32_t d = k.a.st_diagnosed_ts[i];
+            c[SC_P1] = d == t;
+            c[SC_P2] = d < t && d > t - day_steps;
+        }
+        if (st < 16) c[SC_HIST + st] = 1;
+        const uint32_t var = k.a.variant[i];
+        if (inf && var < PSIM_MAX_STRAINS) c[SC_VAR + var] = 1;
+        const uint32_t mask = k.a.st_variant_mask[i];
+        for (uint32_t v = 0; v < V; ++v) {
+            if (mask & (1u << v)) c[SC_INFV + v] = 1;
+            imm[v] = 1.0 - (double)k.a.susceptible[(size_t)v * N + i];
+        }
+    }
+    // warp reduction when the warp is within one replica, else per-thread atomics
+    const unsigned am = __ballot_sync(0xffffffffu, act);
+    const uint32_t rep0 = __shfl_sync(0xffffffffu, rep, 0);
+    const bool uniform = __all_sync(0xffffffffu, !act || rep == rep0);
+    if (uniform) {
+#pragma unroll
+        for (int f = 0; f < STAT_FIELDS; ++f) {
+            unsigned x = c[f];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+            c[f] = x;
+        }
+        for (uint32_t v = 0; v < V; ++v) {
+            double x = imm[v];
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+            imm[v] = x;
+        }
+        if ((threadIdx.x & 31) == 0 && am) {
+            DevStatsAcc* S = &k.stats[rep0];
+            for (int f = 0; f < STAT_FIELDS; ++f)
+                if (c[f]) atomicAdd(&S->c[f], c[f]);
+            for (uint32_t v = 0; v < V; ++v)
+                if (imm[v] != 0.0) atomicAdd(&S->imm[v], imm[v]);
+        }
+    } else if (act) {
+        DevStatsAcc* S = &k.stats[rep];
+        for (int f = 0; f < STAT_FIELDS; ++f)
+            if (c[f]) atomicAdd(&S->c[f], c[f]);
+        for (uint32_t v = 0; v < V; ++v)
+            if (imm[v] != 0.0) atomicAdd(&S->imm[v], imm[v]);
+    }
+}
+
+// variant gating of the next day (countVariantCases, simulation.h:768-777)
+__global__ void k_variant_active(KArgs k) {
+    const uint32_t R = k.r.n, V = k.m.n_variants;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < R * V; j += gridDim.x * blockDim.x) {
+        const uint32_t q = j / V, v = j % V;
+        k.r.variant_active[j] = k.stats[q].c[SC_VAR + v] > 0;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// planLocations, movementPolicies.h:1428-1622
+// checkSchoolQuarantine, :1285-1310 (quarantinePolicy > 3)
+__global__ void k_plan_schools(KArgs k, uint32_t t) {
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < k.l.n_schools; s += gridDim.x * blockDim.x) {
+        const uint32_t school = k.l.schools[s];
+        if (k.l.quarantine_until[school] > t) continue;
+        uint32_t counter = 0, mx = 0;
+        for (uint32_t c = k.l.classroom_offsets[s]; c < k.l.classroom_offsets[s + 1]; ++c) {
+            const uint32_t cl = k.l.classrooms[c];
+            const uint32_t q = k.l.quarantine_until[cl];
+            if (q > t) {
+                counter++;
+                mx = mx > q ? mx : q;
+            }
+        }
+        if (counter > 1) {
+            k.l.quarantine_until[school] = mx;
+            for (uint32_t c = k.l.classroom_offsets[s]; c < k.l.classroom_offsets[s + 1]; ++c)
+                k.l.quarantine_until[k.l.classrooms[c]] = mx;
+        }
+    }
+}
+
+// resets + checkSchoolWorkQuarantine (:1188-1240)
+__global__ void __launch_bounds__(256) k_plan_agents(KArgs k, uint32_t t) {
+    const psim_params& p = k.p;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < k.a.n; i += gridDim.x * blockDim.x) {
+        k.a.steps_until_move[i] = p.curfew_end;
+        k.a.stayed_home[i] = 1;
+        k.a.no_work[i] = 0;
+        if (p.quarantine_policy > 2) {
+            if (k.a.quarantined[i]) continue;
+            if (k.a.st_diagnosed_ts[i] > 0 && !infected_of(k, i)) continue;
+            const uint32_t rep = k.a.rep[i];
+            psim_stream rng;
+            psim_stream_init(&rng, k.r.seed[rep], i - k.r.agent_off[rep], t, PSIM_PHASE_PLAN_SWQ);
+            const uint32_t work = find_location(k, i, p.work_type, 0, &rng);
+            const uint32_t school = find_location(k, i, p.school_type, 0, &rng);
+            const uint32_t classroom = find_location(k, i, p.classroom_type, 0, &rng);
+            uint32_t until = 0;
+            if (school != NONE && loc_qu(k, school) > t)
+                until = loc_qu(k, school);
+            else if (classroom != NONE && loc_qu(k, classroom) > t)
+                until = loc_qu(k, classroom);
+            else if (work != NONE && loc_qu(k, work) > t)
+                until = loc_qu(k, work);
+            if (until > 0) {
+                k.a.quarantined[i] = 1;
+                k.a.st_quarantined_ts[i] = t;
+                k.a.st_quarantined_until[i] = until;
+                k.a.st_days_in_quarantine[i] += (until - t) / (24u * 60u / p.time_step);
+            }
+        }
+    }
+}
+
+// clear quarantine flags, close quarantined schools/classrooms (:1571-1583)
+__global__ void __launch_bounds__(256) k_plan_locations(KArgs k, uint32_t t) {
+    const psim_params& p = k.p;
+    for (uint32_t l = blockIdx.x * blockDim.x + threadIdx.x; l < k.l.n; l += gridDim.x * blockDim.x) {
+        k.l.no_work_loc[l] = 0u;
+        if (p.quarantine_policy > 2) {
+            const uint32_t ty = k.l.type[l];
+            const uint32_t q = k.l.quarantine_until[l];
+            if (q > t && (ty == p.school_type || ty == p.classroom_type)) {
+                k.l.closed_until[l] = q;
+                k.l.quarantine_until[l] = 0u;
+            } else if (q > t && ty == p.work_type) {
+                k.l.quarantine_until[l] = 0u;
+            }
+        }
+    }
+}
+
+// checkUnderageAtHome, :1056-1094 (flag = 0xFFFFFFFF)
+__global__ void __launch_bounds__(256) k_plan_underage(KArgs k, uint32_t t) {
+    const psim_params& p = k.p;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < k.a.n; i += gridDim.x * blockDim.x) {
+        if (k.a.age[i] > 14) continue;
+        const uint32_t rep = k.a.rep[i];
+        psim_stream rng;
+        psim_stream_init(&rng, k.r.seed[rep], i - k.r.agent_off[rep], t, PSIM_PHASE_PLAN_UNDERAGE);
+        const uint32_t home = find_location(k, i, p.home_type, 0, &rng);
+        bool flag = false;
+        if (k.a.quarantined[i]) {
+            flag = true;
+        } else {
+            const uint32_t school = find_location(k, i, p.school_type, 0, &rng);
+            const uint32_t classroom = find_location(k, i, p.classroom_type, 0, &rng);
+            const bool too_old = k.a.age[i] >= p.school_age_restriction;
+            flag = too_old || (school != NONE && (loc_open(k, school) == 0 || loc_closed_until(k, school) > t)) ||
+                   (classroom != NONE && (loc_open(k, classroom) == 0 || loc_closed_until(k, classroom) > t));
+        }
+        if (flag && home < k.l.n) k.l.no_work_loc[home] = NONE;
+    }
+}
+
+// setNoWorkToday, :1137-1158: the lowest-id eligible adult of a flagged home
+__global__ void __launch_bounds__(256) k_plan_nowork_min(KArgs k, uint32_t t) {
+    const psim_params& p = k.p;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < k.a.n; i += gridDim.x * blockDim.x) {
+        const uint8_t age = k.a.age[i];
+        if (!(age > 26 && age < 65)) continue;
+        const uint32_t rep = k.a.rep[i];
+        psim_stream rng;
+        psim_stream_init(&rng, k.r.seed[rep], i - k.r.agent_off[rep], t, PSIM_PHASE_PLAN_NOWORK);
+        const uint32_t home = find_location(k, i, p.home_type, 0, &rng);
+        if (home < k.l.n && k.l.no_work_loc[home] != 0u) atomicMin(&k.l.no_work_loc[home], i);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_plan_nowork_set(KArgs k, uint32_t t) {
+    const psim_params& p = k.p;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < k.a.n; i += gridDim.x * blockDim.x) {
+        const uint8_t age = k.a.age[i];
+        if (!(age > 26 && age < 65)) continue;
+        const uint32_t rep = k.a.rep[i];
+        psim_stream rng;
+        psim_stream_init(&rng, k.r.seed[rep], i - k.r.agent_off[rep], t, PSIM_PHASE_PLAN_NOWORK);
+        const uint32_t home = find_location(k, i, p.home_type, 0, &rng);
+        if (home < k.l.n && k.l.no_work_loc[home] == i) k.a.no_work[i] = 1;
+    }
+}
+
+// Simulation::flagHealthcareWorkers, simulation.h:670-693 (type ids 4 / 12 / 14 as
+// hard-coded in the reference)
+__global__ void k_flag_hcw(KArgs k) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < k.a.n; i += gridDim.x * blockDim.x) {
+        uint8_t f = 0;
+        for (uint32_t j = k.a.loc_offset[i]; j < k.a.loc_offset[i + 1]; ++j) {
+            const uint32_t lt = loc_type(k, k.a.poss_loc[j]);
+            if (k.a.poss_type[j] == 4 && (lt == 12 || lt == 14)) {
+                f = 1;
+                break;
+            }
+        }
+        k.a.hcw[i] = f;
+    }
+}
+
+// A wait on a flag that nothing sets, bounded by `iters`: reports
+// ERR_TEST_WAIT and returns.  Exercises the bounded-wait error path.
+__global__ void k_bounded_wait_probe(KArgs k, uint32_t iters) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    volatile uint32_t* flag = &k.clock->pad[0];
+    uint32_t n = 0;
+    while (*flag == 0u) {
+        if (++n >= iters) {
+            atomicOr(k.err, ERR_TEST_WAIT);
+            return;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+static int g_sm_count = 0;
+static int sm_count() {
+    if (g_sm_count == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_sm_count, cudaDevAttrMultiProcessorCount, dev);
+        if (g_sm_count <= 0) g_sm_count = 152;
+    }
+    return g_sm_count;
+}
+
+static unsigned grid_for(uint32_t n, int per_sm) {
+    unsigned want = (n + 255) / 256;
+    unsigned cap = (unsigned)(sm_count() * per_sm);
+    if (want > cap) want = cap;
+    return want ? want : 1u;
+}
+
+void launch_movement(const KArgs& k, uint32_t step, cudaStream_t s) {
+    k_movement<<<grid_for(k.a.n, 8), 256, 0, s>>>(k, step);
+}
+void launch_count(const KArgs& k, cudaStream_t s) { k_count<<<grid_for(k.a.n, 8), 256, 0, s>>>(k); }
+void launch_scan(const KArgs& k, uint32_t, int with_hazard, int merge_q, cudaStream_t s) {
+    unsigned tiles = (k.l.n + SCAN_TILE - 1) / SCAN_TILE;
+    k_scan<<<tiles ? tiles : 1, SCAN_THREADS, 0, s>>>(k, with_hazard, merge_q);
+}
+void launch_scatter_draw(const KArgs& k, uint32_t step, int draw, cudaStream_t s) {
+    k_scatter_draw<<<grid_for(k.a.n, 8), 256, 0, s>>>(k, step, draw);
+}
+void launch_canonical_csr(const KArgs& k, cudaStream_t s) {
+    // tmp = qu_pending is not free; use the rank array as scratch (rank is rebuilt every step)
+    k_canonical_rank<<<grid_for(k.a.n, 16), 256, 0, s>>>(k, k.a.rank);
+    cudaMemcpyAsync(k.l.csr_agents, k.a.rank, sizeof(uint32_t) * k.a.n, cudaMemcpyDeviceToDevice, s);
+}
+void launch_progress(const KArgs& k, uint32_t t, cudaStream_t s) {
+    const size_t nt = (size_t)k.m.n_prog * k.m.n_states;
+    const size_t bytes = nt * 4 * sizeof(uint32_t) + (size_t)k.m.n_trans * (sizeof(uint32_t) + sizeof(float));
+    const int staged = bytes <= 48 * 1024;
+    k_progress<<<grid_for(k.a.n, 8), 256, staged ? bytes : 0, s>>>(k, t, staged);
+}
+void launch_test(const KArgs& k, uint32_t t, cudaStream_t s) {
+    cudaMemsetAsync(k.l.flags, 0, k.l.n, s);
+    k_test_flag<<<grid_for(k.a.n, 8), 256, 0, s>>>(k, t);
+    k_test<<<grid_for(k.a.n, 8), 256, 0, s>>>(k, t);
+}
+void launch_stats(const KArgs& k, uint32_t t, cudaStream_t s) {
+    cudaMemsetAsync(k.stats, 0, sizeof(DevStatsAcc) * k.r.n, s);
+    unsigned blocks = (k.a.n + 255) / 256;
+    k_stats<<<blocks ? blocks : 1, 256, 0, s>>>(k, t, 1);
+    k_variant_active<<<1, 256, 0, s>>>(k);
+}
+void launch_plan(const KArgs& k, uint32_t t, cudaStream_t s) {
+    if (k.p.quarantine_policy > 3 && k.l.n_schools) k_plan_schools<<<grid_for(k.l.n_schools, 4), 256, 0, s>>>(k, t);
+    k_plan_agents<<<grid_for(k.a.n, 8), 256, 0, s>>>(k, t);
+    k_plan_locations<<<grid_for(k.l.n, 8), 256, 0, s>>>(k, t);
+    k_plan_underage<<<grid_for(k.a.n, 8), 256, 0, s>>>(k, t);
+    k_plan_nowork_min<<<grid_for(k.a.n, 8), 256, 0, s>>>(k, t);
+    k_plan_nowork_set<<<grid_for(k.a.n, 8), 256, 0, s>>>(k, t);
+}
+void launch_flag_hcw(const KArgs& k, cudaStream_t s) { k_flag_hcw<<<grid_for(k.a.n, 8), 256, 0, s>>>(k); }
+void launch_bounded_wait_probe(const KArgs& k, uint32_t iters, cudaStream_t s) {
+    k_bounded_wait_probe<<<1, 32, 0, s>>>(k, iters);
+}
+uint64_t launches_per_step(int) { return 3; }
+
+}  // namespace psim

@@ -1,0 +1,212 @@
+"""ctypes binding of libpansim_gb300.so (the C ABI in include/pansim_gb300.h).
+
+The library is built in-tree by pansim_gb300.build; there is no CPU
+fallback: a missing library or a missing GPU raises.
+"""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+from . import cabi
+from .build import LIB, ROOT, build
+
+_lib = None
+
+
+class PsimError(RuntimeError):
+    pass
+
+
+def header_symbols():
+    """Function names declared in include/pansim_gb300.h."""
+    txt = open(os.path.join(ROOT, "include", "pansim_gb300.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(psim_[a-z_0-9]+)\s*\(", txt)))
+
+
+def lib(auto_build=True):
+    global _lib
+    if _lib is None:
+        path = build() if auto_build else LIB
+        if not os.path.exists(path):
+            raise PsimError("libpansim_gb300.so is not built (run __graft_entry__.build())")
+        L = C.CDLL(path)
+        P, U32, I = C.c_void_p, C.c_uint32, C.c_int
+        L.psim_version.restype = C.c_char_p
+        L.psim_last_error.restype = C.c_char_p
+        L.psim_last_error.argtypes = [P]
+        L.psim_abi_sizes.argtypes = [P, I]
+        L.psim_device_count.argtypes = [P]
+        L.psim_create.argtypes = [I, P, P, P, P, P, C.POINTER(P)]
+        L.psim_destroy.argtypes = [P]
+        L.psim_upload.argtypes = [P, P, P]
+        L.psim_download.argtypes = [P, P, P]
+        L.psim_set_params.argtypes = [P, P]
+        L.psim_set_tracking.argtypes = [P, I]
+        for f in ["psim_movement", "psim_step", "psim_progress_day", "psim_plan_day", "psim_run_steps"]:
+            getattr(L, f).argtypes = [P, U32]
+        L.psim_regroup.argtypes = [P]
+        L.psim_infect.argtypes = [P, U32, U32]
+        L.psim_test_day.argtypes = [P, U32, P]
+        L.psim_stats_day.argtypes = [P, U32, P]
+        L.psim_midnight.argtypes = [P, U32, P]
+        L.psim_run_day.argtypes = [P, U32, P]
+        L.psim_get_csr.argtypes = [P, I, P, P]
+        L.psim_get_hazard.argtypes = [P, P, P]
+        L.psim_last_day_ms.argtypes = [P, C.POINTER(C.c_float)]
+        L.psim_launch_count.argtypes = [P, C.POINTER(C.c_uint64)]
+        L.psim_stream_handle.argtypes = [P, C.POINTER(P)]
+        L.psim_bounded_wait_selftest.argtypes = [P, U32]
+        L.psim_time_step_kernels.argtypes = [P, U32, P]
+        _lib = L
+    return _lib
+
+
+def abi_sizes():
+    out = np.zeros(6, np.uint64)
+    lib().psim_abi_sizes(out.ctypes.data_as(C.c_void_p), 6)
+    return [int(x) for x in out]
+
+
+def device_count():
+    n = C.c_int(0)
+    lib().psim_device_count(C.byref(n))
+    return n.value
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class GpuSim:
+    """One pansim_gb300 context on a snapshot.  Host arrays of the snapshot
+    are read at creation; download() writes the device state back into them."""
+
+    def __init__(self, snap, device=0):
+        self.snap = snap
+        self._structs = snap.structs()
+        m, a, lo, p, r = self._structs
+        h = C.c_void_p()
+        rc = lib().psim_create(device, C.byref(m), C.byref(a), C.byref(lo), C.byref(p), C.byref(r), C.byref(h))
+        self.h = h
+        if rc != 0:
+            msg = lib().psim_last_error(h).decode() if h else "psim_create failed"
+            if h:
+                lib().psim_destroy(h)
+                self.h = None
+            raise PsimError("psim_create: %d %s" % (rc, msg))
+
+    def _ck(self, rc, what):
+        if rc != 0:
+            raise PsimError("%s: %d %s" % (what, rc, lib().psim_last_error(self.h).decode()))
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().psim_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # phases
+    def movement(self, t):
+        self._ck(lib().psim_movement(self.h, t), "movement")
+
+    def regroup(self):
+        self._ck(lib().psim_regroup(self.h), "regroup")
+
+    def infect(self, t, v=0):
+        self._ck(lib().psim_infect(self.h, t, v), "infect")
+
+    def step(self, t):
+        self._ck(lib().psim_step(self.h, t), "step")
+
+    def test(self, t):
+        tpp = np.zeros(3 * self.snap.n_replicas, np.uint32)
+        self._ck(lib().psim_test_day(self.h, t, _p(tpp)), "test")
+        return tpp
+
+    def progress(self, t):
+        self._ck(lib().psim_progress_day(self.h, t), "progress")
+
+    def stats(self, t):
+        out = (cabi.PsimDayStats * self.snap.n_replicas)()
+        self._ck(lib().psim_stats_day(self.h, t, out), "stats")
+        return out
+
+    def plan(self, t):
+        self._ck(lib().psim_plan_day(self.h, t), "plan")
+
+    def midnight(self, t):
+        out = (cabi.PsimDayStats * self.snap.n_replicas)()
+        self._ck(lib().psim_midnight(self.h, t, out), "midnight")
+        return out
+
+    def run_steps(self, day):
+        self._ck(lib().psim_run_steps(self.h, day), "run_steps")
+
+    def run_day(self, day):
+        out = (cabi.PsimDayStats * self.snap.n_replicas)()
+        self._ck(lib().psim_run_day(self.h, day, out), "run_day")
+        return out
+
+    def set_params(self):
+        p = self.snap.params_struct()
+        self._structs = self._structs[:3] + (p,) + self._structs[4:]
+        self._ck(lib().psim_set_params(self.h, C.byref(p)), "set_params")
+
+    def set_tracking(self, expected=True):
+        self._ck(lib().psim_set_tracking(self.h, 1 if expected else 0), "set_tracking")
+
+    def download(self):
+        _, a, lo, _, _ = self._structs
+        self._ck(lib().psim_download(self.h, C.byref(a), C.byref(lo)), "download")
+        return self.snap
+
+    def upload(self):
+        _, a, lo, _, _ = self._structs
+        self._ck(lib().psim_upload(self.h, C.byref(a), C.byref(lo)), "upload")
+
+    def csr(self, canonical=True):
+        L, N = self.snap.n_locations, self.snap.n_agents
+        off = np.zeros(L + 1, np.uint32)
+        ag = np.zeros(max(N, 1), np.uint32)
+        self._ck(lib().psim_get_csr(self.h, 1 if canonical else 0, _p(off), _p(ag)), "csr")
+        return off, ag[:N]
+
+    def hazard(self):
+        V = int(self.snap.model["n_variants"])
+        out = np.zeros(self.snap.n_locations * V, np.float32)
+        self._ck(lib().psim_get_hazard(self.h, _p(out), None), "hazard")
+        return out
+
+    def last_day_ms(self):
+        ms = C.c_float(0)
+        lib().psim_last_day_ms(self.h, C.byref(ms))
+        return ms.value
+
+    def launch_count(self):
+        n = C.c_uint64(0)
+        lib().psim_launch_count(self.h, C.byref(n))
+        return n.value
+
+    def stream(self):
+        s = C.c_void_p()
+        lib().psim_stream_handle(self.h, C.byref(s))
+        return s.value
+
+    def time_step_kernels(self, t):
+        ms = np.zeros(3, np.float32)
+        self._ck(lib().psim_time_step_kernels(self.h, t, _p(ms)), "time_step_kernels")
+        return ms
+
+    def bounded_wait_selftest(self, iters):
+        return lib().psim_bounded_wait_selftest(self.h, iters)
+
+    def last_error(self):
+        return lib().psim_last_error(self.h).decode()

@@ -1,0 +1,148 @@
+"""GPU parity against the CPU oracle through the C ABI (gpu).
+
+Bit-exact: movement, location assignment, CSR (canonical order), per-location
+counts, fixed-point sums and hazards, infection outcomes, state transitions,
+daily plan, testing, statistics.  Hazards additionally within 1e-5 relative
+of the oracle's FP64 evaluation.
+"""
+import numpy as np
+import pytest
+
+from oracle import binding as ob
+from pansim_gb300.native import GpuSim
+from tests.helpers import diff_state, small_snapshot, stats_rows
+
+pytestmark = pytest.mark.gpu
+
+
+def _pair(**kw):
+    s_cpu = small_snapshot(**kw)
+    s_gpu = s_cpu.copy()
+    return s_cpu, s_gpu, ob.Oracle(s_cpu), GpuSim(s_gpu)
+
+
+def test_initial_csr(gpu_lib):
+    s_cpu, s_gpu, o, g = _pair(n=8000, locs=2000)
+    off_o, ag_o = o.csr()
+    off_g, ag_g = g.csr(canonical=True)
+    assert np.array_equal(off_o, off_g)
+    assert np.array_equal(ag_o, ag_g)
+
+
+def test_one_day_phase_by_phase(gpu_lib):
+    s_cpu, s_gpu, o, g = _pair(n=20000, locs=5000, initial_infected_frac=0.02)
+    st_o = o.midnight(0)
+    st_g = g.midnight(0)
+    assert stats_rows(st_o) == stats_rows(st_g)
+    for t in range(144):
+        o.movement(t)
+        g.movement(t)
+        o.regroup()
+        g.regroup()
+        out = o.infect(t)
+        g.infect(t)
+        if t % 24 == 5:
+            g.download()
+            assert diff_state(s_cpu, s_gpu) == [], t
+            off_o, ag_o = o.csr()
+            off_g, ag_g = g.csr(canonical=True)
+            assert np.array_equal(off_o, off_g), t
+            assert np.array_equal(ag_o, ag_g), t
+            hz = g.hazard()
+            assert np.array_equal(hz, out["hazard"]), t
+            nz = out["r64"] > 0
+            if nz.any():
+                rel = np.abs(hz[nz].astype(np.float64) - out["r64"][nz]) / out["r64"][nz]
+                assert rel.max() < 1e-5
+    g.download()
+    assert diff_state(s_cpu, s_gpu) == []
+    # next midnight: progression + stats + plan
+    o.progress(144)
+    g.progress(144)
+    g.download()
+    assert diff_state(s_cpu, s_gpu) == []
+    assert stats_rows(o.stats(144)) == stats_rows(g.stats(144))
+    o.plan(144)
+    g.plan(144)
+    g.download()
+    assert diff_state(s_cpu, s_gpu) == []
+
+
+def test_week_graph_bit_exact(gpu_lib):
+    s_cpu, s_gpu, o, g = _pair(n=30000, locs=7500, initial_infected_frac=0.01)
+    for d in range(7):
+        ro = stats_rows(o.run_day(d))
+        rg = stats_rows(g.run_day(d))
+        assert ro == rg, d
+    g.download()
+    assert diff_state(s_cpu, s_gpu) == []
+
+
+def test_quarantine_testing_policies_bit_exact(gpu_lib):
+    """quarantinePolicy 3, DetailedTesting with high probabilities."""
+    s_cpu, s_gpu, o, g = _pair(n=20000, locs=5000, initial_infected_frac=0.02, quarantine_policy=3, testing=True)
+    for s in (s_cpu, s_gpu):
+        s.params.update(t_random=0.02, t_home=0.3, t_work=0.1, t_school=0.1, t_hospital=0.2)
+    o.set_params()
+    g.set_params()
+    for d in range(6):
+        ro = stats_rows(o.run_day(d))
+        rg = stats_rows(g.run_day(d))
+        assert ro == rg, d
+    g.download()
+    assert diff_state(s_cpu, s_gpu) == []
+    assert s_cpu.agents["quarantined"].sum() > 0
+    assert (s_cpu.agents["last_test"] != 0xFFFFFFFF).sum() > 0
+
+
+def test_curfew_and_closures_bit_exact(gpu_lib):
+    s_cpu, s_gpu, o, g = _pair(n=15000, locs=4000, initial_infected_frac=0.02)
+    rng = np.random.default_rng(3)
+    closed = rng.random(s_cpu.n_locations) < 0.2
+    for s in (s_cpu, s_gpu):
+        s.params.update(enable_curfew=1, curfew_begin=120, curfew_end=30, school_age_restriction=12)
+        s.locs["open"][closed] = 0
+    o = ob.Oracle(s_cpu)
+    g = GpuSim(s_gpu)
+    for d in range(3):
+        assert stats_rows(o.run_day(d)) == stats_rows(g.run_day(d)), d
+    g.download()
+    assert diff_state(s_cpu, s_gpu) == []
+
+
+def test_replicas_batch_equals_single(gpu_lib):
+    """A replica gives the same trajectory alone and inside a batch."""
+    from pansim_gb300 import snapshot as snp, synth
+    parts = [synth.make_snapshot(n, n // 4, seed=1, pop_seed=100 + i, initial_infected_frac=0.01)
+             for i, n in enumerate([6000, 9000, 4000])]
+    seeds = [11, 22, 33]
+    ks = [2e-4, 5e-4, 9e-4]
+    batch = snp.concat(parts, seeds, ks)
+    gb = GpuSim(batch)
+    singles = []
+    for i, p in enumerate(parts):
+        q = p.copy()
+        q.params["seed"] = seeds[i]
+        q.params["k"] = ks[i]
+        q.reps["seed"][:] = seeds[i]
+        q.reps["k"][:] = ks[i]
+        singles.append((q, GpuSim(q)))
+    for d in range(3):
+        rb = stats_rows(gb.run_day(d))
+        for i, (q, gs) in enumerate(singles):
+            assert rb[i] == stats_rows(gs.run_day(d))[0], (d, i)
+    # the oracle agrees on the batch too
+    batch2 = snp.concat(parts, seeds, ks)
+    ob_ = ob.Oracle(batch2)
+    gb2 = GpuSim(batch2.copy())
+    for d in range(2):
+        assert stats_rows(ob_.run_day(d)) == stats_rows(gb2.run_day(d))
+
+
+def test_bounded_wait_reports_error_and_context_survives(gpu_lib):
+    s = small_snapshot(n=2000, locs=500)
+    g = GpuSim(s)
+    rc = g.bounded_wait_selftest(1 << 16)
+    assert rc == -5  # PSIM_ERR_DEVICE
+    assert "bounded wait expired" in g.last_error()
+    g.run_day(0)  # still usable
