@@ -138,7 +138,7 @@ def mutable_bytes(snap):
     return sum(snap.agents[k].nbytes for k in AGENT_MUTABLE) + sum(snap.locs[k].nbytes for k in LOC_MUTABLE)
 
 
-def cpu_baseline(snap, steps=24):
+def cpu_baseline(snap, steps=120):
     """The oracle port, single thread, on `steps` timesteps of the same workload."""
     from oracle import binding as ob
     s = snap.copy()
@@ -161,7 +161,7 @@ def run_reference(args, ws, rank):
     snap = make_snapshot(0)
     o = ob.Oracle(snap)
     o.midnight(0)
-    per_step_ts = 6  # timesteps per bench step: a bounded sample of a day
+    per_step_ts = 12  # timesteps per bench step: a bounded sample of a day
     t = 0
     for _ in range(args.warmup):
         for _ in range(per_step_ts):

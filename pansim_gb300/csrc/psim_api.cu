@@ -337,13 +337,6 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     int rc = validate(c, m, a, l);
     if (rc) return bail(rc);
     if (p->time_step == 0 || 1440 % p->time_step) return bail(fail(c, PSIM_ERR_ARG, "time_step must divide 1440"));
-    c->device = device;
-    cudaError_t e = cudaSetDevice(device);
-    if (e != cudaSuccess) return bail(fail(c, PSIM_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e)));
-    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
-    if (e != cudaSuccess) return bail(fail(c, PSIM_ERR_CUDA, std::string("stream: ") + cudaGetErrorString(e)));
-    cudaEventCreate(&c->ev0);
-    cudaEventCreate(&c->ev1);
     c->N = a->n;
     c->L = l->n;
     c->V = m->n_variants;
@@ -373,9 +366,17 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     for (uint32_t q = 0; q < c->R; ++q) {
         if (c->rep_agent_off[q + 1] < c->rep_agent_off[q] || c->rep_loc_off[q + 1] < c->rep_loc_off[q])
             return bail(fail(c, PSIM_ERR_ARG, "replica offsets not monotonic"));
-        if (c->rep_cemetery[q] < c->rep_loc_off[q] || c->rep_cemetery[q] >= c->rep_loc_off[q + 1])
-            return bail(fail(c, PSIM_ERR_RANGE, "cemetery outside its replica"));
+        // the cemetery is the location appended last (locationList.h:168-175)
+        if (c->rep_loc_off[q + 1] == c->rep_loc_off[q] || c->rep_cemetery[q] != c->rep_loc_off[q + 1] - 1)
+            return bail(fail(c, PSIM_ERR_RANGE, "cemetery is not the last location of its replica"));
     }
+    c->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return bail(fail(c, PSIM_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e)));
+    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return bail(fail(c, PSIM_ERR_CUDA, std::string("stream: ") + cudaGetErrorString(e)));
+    cudaEventCreate(&c->ev0);
+    cudaEventCreate(&c->ev1);
     const size_t N = c->N, L = c->L, V = c->V, R = c->R;
     KArgs& k = c->k;
     // model tables

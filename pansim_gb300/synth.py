@@ -141,7 +141,8 @@ def make_model(seed=0x5EED0000, n_variants=1, avg_len=1.0, max_len=0.0, acc_pcr=
 
 
 def make_schedules(rng, n_types=4):
-    """AgentTypeList events, offsets indexed 28*type + 7*WB + day."""
+    """AgentTypeList events, offsets indexed 28*type + 7*WB + day for WB in
+    W, N, M, S (agentType.cpp:13-19; D never looks up a schedule)."""
     primary = {0: SCHOOL, 1: WORK, 2: SHOP, 3: WORK}
     per_slot = {}
     for ty in range(n_types):
@@ -166,7 +167,7 @@ def make_schedules(rng, n_types=4):
     offsets = [0]
     ev = []
     for ty in range(n_types):
-        for wb in range(5):
+        for wb in range(4):
             for day in range(7):
                 if wb in (WB["W"], WB["N"]):
                     evs = per_slot[(ty, "weekday" if day < 5 else "weekend")]
