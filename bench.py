@@ -305,7 +305,7 @@ def main():
         }
         if host_snap is not None:
             line["cpu_baseline"] = cpu_baseline(host_snap)
-        print(json.dumps(line))
+        print(json.dumps(line, default=float))
     if dist:
         dist.barrier()
         dist.destroy_process_group()

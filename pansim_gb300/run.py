@@ -1,0 +1,49 @@
+"""Command-line runner: a seeded synthetic population stepped on the GPU.
+
+  python -m pansim_gb300.run --agents 2000000 --locs 500000 --days 2
+  python -m pansim_gb300.run --agents 2000000 --locs 500000 --steps 20   # individual psim_step launches
+
+Prints the daily statistics row (the reference's TSV columns,
+simulation.h:754) and the wall time.  --steps runs the timesteps of day 0
+one psim_step call at a time (no graph), which is the form used for kernel
+profiles.
+"""
+import argparse
+import sys
+import time
+
+from . import native, synth
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--agents", type=int, default=100_000)
+    ap.add_argument("--locs", type=int, default=20_000)
+    ap.add_argument("--days", type=int, default=0)
+    ap.add_argument("--steps", type=int, default=0)
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--pop-seed", type=int, default=0x5EED0002)
+    ap.add_argument("--quarantine-policy", type=int, default=0)
+    ap.add_argument("--testing", action="store_true")
+    ap.add_argument("--quiet", action="store_true")
+    a = ap.parse_args(argv)
+    snap = synth.make_snapshot(a.agents, a.locs, seed=a.seed, pop_seed=a.pop_seed,
+                               quarantine_policy=a.quarantine_policy, testing=a.testing)
+    g = native.GpuSim(snap)
+    t0 = time.perf_counter()
+    for d in range(a.days):
+        st = g.run_day(d)
+        if not a.quiet:
+            print("day %d\t" % d + "\t".join(str(x) for x in list(st[0].v)[: st[0].n]))
+    if a.steps:
+        g.midnight(a.days * 144)
+        for s in range(a.steps):
+            g.step(a.days * 144 + s)
+    dt = time.perf_counter() - t0
+    print("agents %d locations %d days %d steps %d wall %.3f s launches %d" % (
+        snap.n_agents, snap.n_locations, a.days, a.steps, dt, g.launch_count()))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
