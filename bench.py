@@ -32,8 +32,11 @@ UNIT = "agent-steps/s"
 # algorithmic bytes per step (per agent, per location) of the whole step,
 # 32*N + 20*L, and of each kernel of the step
 STEP_BYTES = (32, 20)
-KERNEL_BYTES = {"movement": (20, 4), "scan": (0, 30), "scatter_draw": (22, 0)}
-KERNEL_NAMES = ["movement", "scan", "scatter_draw"]
+# k_step_fused: location, rank, steps (r+w), infectiousness, replica, CSR offset
+# and hazard gathers, CSR and rank writes = 38 B/agent; k_scan: counts (r+w),
+# offsets, fixed-point sums, hazard, w_l, replica = 30 B/location
+KERNEL_BYTES = {"movement": (20, 4), "scan": (0, 30), "step_fused": (38, 0)}
+KERNEL_NAMES = ["movement", "scan", "step_fused"]
 
 
 def dist_env():
@@ -219,11 +222,16 @@ def main():
     for _ in range(args.warmup):
         g.run_day(day)
         day += 1
+    # autotune the step kernels on this workload (part of the warm-up)
+    from pansim_gb300 import autotune
+    best, table = autotune.autotune(g, day)
+    g.run_day(day)
+    day += 1
     # per-kernel timing (roofline): CUDA events around each kernel on the library's stream
     kt = []
     t_probe = day * 144
     for j in range(12):
-        kt.append(g.time_step_kernels(t_probe + j))
+        kt.append(g.time_step_kernels(t_probe + 2 * j))
     kms = np.mean(np.array(kt[2:]), axis=0)
     g.run_day(day)  # resynchronise the day
     day += 1
@@ -282,7 +290,7 @@ def main():
             bn, bl = KERNEL_BYTES[name]
             b = bn * N + bl * L
             kern[name] = {"ms": float(ms), "alg_bytes": b, "gbs": b / (ms * 1e-3) / 1e9}
-        step_ms = float(np.sum(kms))
+        step_ms = float(kern["scan"]["ms"] + kern["step_fused"]["ms"])
         step_bytes = STEP_BYTES[0] * N + STEP_BYTES[1] * L
         dom = max(kern, key=lambda k: kern[k]["ms"])
         tr = committed_traffic()
@@ -297,11 +305,13 @@ def main():
             "config": {"workload": "2M agents, 500k non-home locations (+homes), dt 10 min, 1 day per step",
                        "agents": N, "locations": L, "timesteps_per_step": 144,
                        "l2": "flushed between timed steps (256 MiB write)", "parallelism": "replicas" if ws > 1 else "1 gpu"},
-            "roofline": {"bound": "hbm", "kernel": "step (movement+scan+scatter_draw)", "achieved": ach, "peak": peak,
+            "roofline": {"bound": "hbm", "kernel": "one step: k_scan + k_step_fused", "achieved": ach, "peak": peak,
                          "unit": "GB/s", "frac": ach / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "alg_bytes_per_launch": step_bytes, "launch_ms": step_ms, "dominant": dom,
                          "per_kernel": kern},
             "clocks": clocks, "gpu_launches": int(launches), "e2e": e2e,
+            "tuning": {"best": best, "candidates": len(table),
+                       "worst_step_ms": max(x[1] for x in table), "best_step_ms": min(x[1] for x in table)},
         }
         if host_snap is not None:
             line["cpu_baseline"] = cpu_baseline(host_snap)

@@ -210,6 +210,15 @@ typedef struct psim_day_stats {
     double expected_new_infections;    /* sum of infection probabilities since the last midnight */
 } psim_day_stats;
 
+/* Launch and algorithm choices of the per-step kernels, picked per device
+ * and workload by the autotuner (pansim_gb300/autotune.py). */
+typedef struct psim_tuning {
+    uint32_t agg_count;      /* warp-aggregated per-location count reductions */
+    uint32_t agg_slot;       /* warp-aggregated CSR slot atomics */
+    uint32_t blocks_per_sm;  /* 256-thread blocks per SM of the per-agent kernels; 0 = occupancy */
+    uint32_t pad;
+} psim_tuning;
+
 typedef struct psim_ctx psim_ctx;
 
 /* Library */
@@ -250,6 +259,10 @@ int psim_run_steps(psim_ctx* ctx, uint32_t day);
 /* One day: psim_midnight at t = day*steps_per_day, then psim_run_steps. */
 int psim_run_day(psim_ctx* ctx, uint32_t day, psim_day_stats* out /* [replicas] */);
 
+/* Sets the tuning of the per-step kernels (recaptures the day graph). */
+int psim_set_tuning(psim_ctx* ctx, const psim_tuning* tuning);
+int psim_get_tuning(psim_ctx* ctx, psim_tuning* tuning);
+
 /* Accumulate the expected new infections (sum of infection probabilities of
  * susceptible agents, reported in psim_day_stats) during the steps. */
 int psim_set_tracking(psim_ctx* ctx, int expected);
@@ -261,8 +274,9 @@ int psim_get_csr(psim_ctx* ctx, int canonical, uint32_t* offsets /*[L+1]*/, uint
 /* Per-location hazard r_l of the last psim_infect call (infectionRatios). */
 int psim_get_hazard(psim_ctx* ctx, float* out /*[L]*/, int64_t* fixed_sum /*[L] or NULL*/);
 
-/* One step at timestamp t with a CUDA event around each of its three
- * kernels (movement, scan, scatter+draw); ms[3] receives their durations. */
+/* Steps t and t+1 (same day) as the day graph runs them, with CUDA events
+ * around movement(t), scan(t) and the fused scatter+draw(t)/movement(t+1)
+ * kernel; ms[3] receives those three durations. */
 int psim_time_step_kernels(psim_ctx* ctx, uint32_t t, float* ms /* [3] */);
 /* Timing of the last psim_run_steps graph launch, milliseconds. */
 int psim_last_day_ms(psim_ctx* ctx, float* ms);

@@ -60,6 +60,8 @@ def lib():
         L.psim_oracle_philox.argtypes = [P, P, P]
         L.psim_oracle_one_minus_exp.restype = D
         L.psim_oracle_one_minus_exp.argtypes = [D]
+        L.psim_oracle_one_minus_expf.restype = C.c_float
+        L.psim_oracle_one_minus_expf.argtypes = [C.c_float]
         L.psim_oracle_seasonality.restype = D
         L.psim_oracle_seasonality.argtypes = [P, U32, U32]
     return _lib
@@ -151,6 +153,10 @@ def philox(ctr, key):
 
 def one_minus_exp(x):
     return lib().psim_oracle_one_minus_exp(float(x))
+
+
+def one_minus_expf(x):
+    return lib().psim_oracle_one_minus_expf(float(x))
 
 
 def seasonality(snap, t):

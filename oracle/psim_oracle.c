@@ -14,8 +14,9 @@
  *  - setNoWorkToday picks the lowest agent id of a home (what the reference's
  *    single-threaded CPU loop does; its GPU atomicAdd picks an arbitrary one);
  *  - per-location sums are the exact 2^-40 fixed-point sums, the hazard is
- *    1 - exp(-x) in FP64 rounded to FP32 (reference: 1 - expf(x) in FP32,
- *    infectionPolicies.h:545).
+ *    psim_hazard(): FP32 operations with a cancellation-free 1 - exp(-x)
+ *    (reference: 1 - expf(x) in FP32, infectionPolicies.h:545); the FP64
+ *    evaluation is returned beside it for the tolerance checks.
  * Build: gcc -O2 -ffp-contract=off (no FMA contraction: results must match
  * the device bit for bit).
  */
@@ -468,15 +469,7 @@ void psim_oracle_infect(psim_oracle* o, uint32_t t, uint32_t v, float* hazard_f,
         float k_f = (float)o->r.k[rep];
         float rf = 0.0f;
         double rd = 0.0;
-        if (fix != 0 && e > b) {
-            double S = (double)fix * PSIM_FIX_INV;
-            double dens = S / (double)(e - b);
-            double x = (double)k_f * dens;
-            x = x * (double)o->l->infectiousness[l];
-            x = x * (double)season_f;
-            x = x * (double)p->time_step;
-            rf = (float)psim_one_minus_exp(x);
-        }
+        if (fix != 0 && e > b) rf = psim_hazard(fix, e - b, k_f, o->l->infectiousness[l], season_f, p->time_step);
         if (s64 != 0.0 && e > b) {
             double x = o->r.k[rep] * (s64 / (double)(e - b)) * (double)o->l->infectiousness[l] * season_d *
                        (double)p->time_step;
@@ -1017,6 +1010,7 @@ void psim_oracle_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t o
 }
 
 double psim_oracle_one_minus_exp(double x) { return psim_one_minus_exp(x); }
+float psim_oracle_one_minus_expf(float x) { return psim_one_minus_expf(x); }
 
 /* BasicInfection::seasonalityMultiplier, infectionPolicies.h:443-478 */
 double psim_oracle_seasonality(const psim_params* p, uint32_t t, uint32_t spd) {

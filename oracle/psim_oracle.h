@@ -51,6 +51,7 @@ const uint32_t* psim_oracle_csr_agents(psim_oracle* o);
 /* Philox self-check helper: raw block */
 void psim_oracle_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 double psim_oracle_one_minus_exp(double x);
+float psim_oracle_one_minus_expf(float x);
 /* seasonality multiplier of infectionPolicies.h:443-478 */
 double psim_oracle_seasonality(const psim_params* p, uint32_t t, uint32_t steps_per_day);
 

@@ -80,4 +80,9 @@ class PsimDayStats(C.Structure):
                 ("variant_counts", C.c_uint32 * PSIM_MAX_STRAINS), ("expected_new_infections", C.c_double)]
 
 
+class PsimTuning(C.Structure):
+    _fields_ = [("agg_count", C.c_uint32), ("agg_slot", C.c_uint32), ("blocks_per_sm", C.c_uint32),
+                ("pad", C.c_uint32)]
+
+
 ABI_STRUCTS = [PsimModel, PsimAgents, PsimLocations, PsimParams, PsimReplicas, PsimDayStats]

@@ -37,7 +37,7 @@ struct psim_ctx {
     float last_ms = 0.f;
     uint64_t launches = 0;
     bool uploaded = false;
-    bool csr_fresh = false;      // counts/rank of the current positions are built
+    bool csr_fresh = false;      // counts of the current positions are built
     std::vector<DevStatsAcc> h_stats;
     std::vector<double> h_expected;
 };
@@ -97,7 +97,6 @@ int check_device_err(psim_ctx* c) {
     if (e) {
         CK(cudaMemsetAsync(c->k.err, 0, sizeof(uint32_t), c->stream));
         std::string m = "device error flags 0x" + std::to_string(e) + ":";
-        if (e & ERR_SCAN_WAIT) m += " scan look-back wait expired;";
         if (e & ERR_LOCATION) m += " agent on an invalid location;";
         if (e & ERR_TEST_WAIT) m += " bounded wait expired;";
         return fail(c, PSIM_ERR_DEVICE, m);
@@ -218,9 +217,9 @@ int initial_regroup(psim_ctx* c) {
     CK(cudaMemsetAsync(c->k.l.sfix, 0, sizeof(unsigned long long) * c->L * c->V, c->stream));
     launch_count(c->k, c->stream);
     launch_scan(c->k, 0, 1, 0, c->stream);
-    launch_scatter_draw(c->k, 0, 0, c->stream);
+    launch_scatter_draw(c->k, 0, 1, 0, c->stream);
     launch_stats(c->k, 0, c->stream);
-    c->launches += 5;
+    c->launches += 6;
     int rc = launch_check(c);
     if (rc) return rc;
     c->csr_fresh = true;
@@ -231,8 +230,8 @@ int do_step(psim_ctx* c, uint32_t step, bool draw, bool movement) {
     const int merge_q = c->params.quarantine_policy > 1;
     if (movement) launch_movement(c->k, step, c->stream);
     launch_scan(c->k, step, 1, merge_q, c->stream);
-    launch_scatter_draw(c->k, step, draw ? 1 : 0, c->stream);
-    c->launches += movement ? 3 : 2;
+    launch_scatter_draw(c->k, step, 1, draw ? 1 : 0, c->stream);
+    c->launches += movement ? 4 : 3;
     return launch_check(c);
 }
 
@@ -244,17 +243,21 @@ int capture_day_graph(psim_ctx* c) {
     cudaGraph_t g = nullptr;
     CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     const int merge_q = c->params.quarantine_policy > 1;
+    // movement(0); then per step: scan(s), scatter+draw(s) fused with movement(s+1)
+    launch_movement(c->k, 0, c->stream);
     for (uint32_t s = 0; s < c->spd; ++s) {
-        launch_movement(c->k, s, c->stream);
         launch_scan(c->k, s, 1, merge_q, c->stream);
-        launch_scatter_draw(c->k, s, 1, c->stream);
+        if (s + 1 < c->spd)
+            launch_step_fused(c->k, s, c->stream);
+        else
+            launch_scatter_draw(c->k, s, 1, 1, c->stream);
     }
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     if (e != cudaSuccess) return fail(c, PSIM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
     e = cudaGraphInstantiate(&c->day_graph, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(c, PSIM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
-    c->graph_kernels = 3ull * c->spd;
+    c->graph_kernels = 3ull * c->spd + 1;
     c->graph_dirty = false;
     return 0;
 }
@@ -443,6 +446,7 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     if ((rc = dalloc(c, &dl.quarantine_until, L))) return bail(rc);
     if ((rc = dalloc(c, &dl.counts, L))) return bail(rc);
     if ((rc = dalloc(c, &dl.csr_off, L + 1))) return bail(rc);
+    if ((rc = dalloc(c, &dl.cursor, L))) return bail(rc);
     if ((rc = dalloc(c, &dl.csr_agents, N))) return bail(rc);
     if ((rc = dalloc(c, &dl.qu_pending, L))) return bail(rc);
     if ((rc = dalloc(c, &dl.sfix, L * V))) return bail(rc);
@@ -450,7 +454,7 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     if ((rc = dalloc(c, &dl.no_work_loc, L))) return bail(rc);
     if ((rc = dalloc(c, &dl.flags, L))) return bail(rc);
     const size_t tiles = (L + 2047) / 2048 + 1;
-    if ((rc = dalloc(c, &dl.scan_status, tiles))) return bail(rc);
+    if ((rc = dalloc(c, &dl.tile_sums, tiles))) return bail(rc);
     // replicas
     DevReps& dr = k.r;
     dr.n = c->R;
@@ -469,6 +473,9 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     k.p = c->params;
     k.spd = c->spd;
     k.track_expected = 0;
+    k.tune.agg_count = 1;
+    k.tune.agg_slot = 1;
+    k.tune.blocks_per_sm = 0;
     c->h_stats.resize(R);
     c->h_expected.assign(R, 0.0);
     // healthcare workers per replica (Simulation::flagHealthcareWorkers, simulation.h:670-693)
@@ -548,6 +555,25 @@ int psim_set_params(psim_ctx* c, const psim_params* p) {
     return 0;
 }
 
+int psim_set_tuning(psim_ctx* c, const psim_tuning* t) {
+    if (!c || !t) return PSIM_ERR_ARG;
+    if (t->blocks_per_sm > 64) return fail(c, PSIM_ERR_ARG, "blocks_per_sm out of range");
+    c->k.tune.agg_count = t->agg_count ? 1u : 0u;
+    c->k.tune.agg_slot = t->agg_slot ? 1u : 0u;
+    c->k.tune.blocks_per_sm = t->blocks_per_sm;
+    c->graph_dirty = true;
+    return 0;
+}
+
+int psim_get_tuning(psim_ctx* c, psim_tuning* t) {
+    if (!c || !t) return PSIM_ERR_ARG;
+    t->agg_count = c->k.tune.agg_count;
+    t->agg_slot = c->k.tune.agg_slot;
+    t->blocks_per_sm = c->k.tune.blocks_per_sm;
+    t->pad = 0;
+    return 0;
+}
+
 int psim_set_tracking(psim_ctx* c, int expected) {
     if (!c) return PSIM_ERR_ARG;
     c->k.track_expected = expected ? 1u : 0u;
@@ -576,8 +602,8 @@ int psim_regroup(psim_ctx* c) {
         c->launches += 1;
     }
     launch_scan(c->k, 0, 1, c->params.quarantine_policy > 1, c->stream);
-    launch_scatter_draw(c->k, 0, 0, c->stream);
-    c->launches += 2;
+    launch_scatter_draw(c->k, 0, 1, 0, c->stream);
+    c->launches += 3;
     c->csr_fresh = false;
     int rc = launch_check(c);
     if (rc) return rc;
@@ -592,8 +618,8 @@ int psim_infect(psim_ctx* c, uint32_t t, uint32_t variant) {
     (void)variant;
     int rc = set_clock(c, t);
     if (rc) return rc;
-    // re-run the scatter with the draw; the CSR write is idempotent
-    launch_scatter_draw(c->k, t % c->spd, 1, c->stream);
+    // the draw only (the CSR was scattered by psim_regroup)
+    launch_scatter_draw(c->k, t % c->spd, 0, 1, c->stream);
     c->launches += 1;
     rc = launch_check(c);
     if (rc) return rc;
@@ -702,6 +728,8 @@ int psim_run_day(psim_ctx* c, uint32_t day, psim_day_stats* out) {
 
 int psim_get_csr(psim_ctx* c, int canonical, uint32_t* offsets, uint32_t* agents) {
     if (!c || !c->uploaded) return PSIM_ERR_STATE;
+    launch_offsets(c->k, c->stream);
+    c->launches += 1;
     if (canonical) {
         launch_canonical_csr(c->k, c->stream);
         c->launches += 1;
@@ -742,21 +770,26 @@ int psim_stream_handle(psim_ctx* c, void** out) {
 
 int psim_time_step_kernels(psim_ctx* c, uint32_t t, float* ms) {
     if (!c || !c->uploaded || !ms) return PSIM_ERR_ARG;
+    if (t % c->spd + 1 >= c->spd) return fail(c, PSIM_ERR_ARG, "t and t+1 must lie in the same day");
     int rc = set_clock(c, t);
     if (rc) return rc;
     cudaEvent_t ev[4];
     for (int j = 0; j < 4; ++j) CK(cudaEventCreate(&ev[j]));
     const uint32_t step = t % c->spd;
     const int merge_q = c->params.quarantine_policy > 1;
+    // steps t and t+1 as in the day graph: movement(t) | scan(t) | scatter+draw(t) fused with
+    // movement(t+1); then scan(t+1) and scatter+draw(t+1) untimed
     CK(cudaEventRecord(ev[0], c->stream));
     launch_movement(c->k, step, c->stream);
     CK(cudaEventRecord(ev[1], c->stream));
     launch_scan(c->k, step, 1, merge_q, c->stream);
     CK(cudaEventRecord(ev[2], c->stream));
-    launch_scatter_draw(c->k, step, 1, c->stream);
+    launch_step_fused(c->k, step, c->stream);
     CK(cudaEventRecord(ev[3], c->stream));
-    c->launches += 3;
-    CK(cudaEventSynchronize(ev[3]));
+    launch_scan(c->k, step + 1, 1, merge_q, c->stream);
+    launch_scatter_draw(c->k, step + 1, 1, 1, c->stream);
+    c->launches += 7;
+    CK(cudaStreamSynchronize(c->stream));
     for (int j = 0; j < 3; ++j) CK(cudaEventElapsedTime(&ms[j], ev[j], ev[j + 1]));
     for (int j = 0; j < 4; ++j) cudaEventDestroy(ev[j]);
     c->csr_fresh = false;

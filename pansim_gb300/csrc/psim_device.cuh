@@ -13,7 +13,7 @@ constexpr uint32_t NONE = 0xFFFFFFFFu;
 constexpr int WB_W = 0, WB_N = 1, WB_M = 2, WB_S = 3, WB_D = 4;
 
 // error bits written by kernels into DevCtx::err
-constexpr uint32_t ERR_SCAN_WAIT = 1u;     // scan look-back wait gave up
+constexpr uint32_t ERR_SCAN_WAIT = 1u;     // (unused: the scan has no inter-block waits)
 constexpr uint32_t ERR_LOCATION = 2u;      // an agent ended on an invalid location
 constexpr uint32_t ERR_TEST_WAIT = 4u;     // bounded-wait self test expired (expected in tests)
 
@@ -86,7 +86,7 @@ struct DevAgents {
     uint8_t* st_infected_count;
     int8_t* st_worst_state;
     uint8_t* hcw;                 // healthcare worker flag
-    uint32_t* rank;               // position of the agent inside its location's CSR segment
+    uint32_t* rank;               // scratch of the canonical CSR ordering
 };
 
 struct DevLocs {
@@ -103,14 +103,15 @@ struct DevLocs {
     const uint32_t* classroom_offsets;
     const uint16_t* rep;
     uint32_t* counts;             // agents per location, built by movement
-    uint32_t* csr_off;            // [n+1]
+    uint32_t* cursor;             // [n] next free CSR slot of each location (scan: first slot)
+    uint32_t* csr_off;            // [n+1] CSR offsets, derived from the cursors on demand
     uint32_t* csr_agents;         // [N]
     uint32_t* qu_pending;         // quarantine writes of the running step
     unsigned long long* sfix;     // [V][n] fixed-point infectiousness sums
     float* hazard;                // [V][n] infection ratio of the last step
     uint32_t* no_work_loc;
     uint8_t* flags;               // testing flags
-    unsigned long long* scan_status;  // look-back tile status
+    uint32_t* tile_sums;          // per-tile sums of the histogram (scan, first pass)
 };
 
 struct DevReps {
@@ -130,15 +131,20 @@ struct DevClock {
     uint32_t t0;          // timestamp of the day's midnight
     uint32_t day_of_week; // Days, holiday mode already applied
     float season;         // seasonality multiplier of the day
-    uint32_t scan_epoch;  // look-back status epoch
-    uint32_t scan_ticket; // dynamic tile ids of the scan
-    uint32_t scan_done;
-    uint32_t pad[2];
+    uint32_t pad[5];
 };
 
 struct DevStatsAcc {      // raw per-replica daily counters
     unsigned int c[48];
     double imm[PSIM_MAX_STRAINS];
+};
+
+// launch/algorithm choices picked by the autotuner (psim_tuning)
+struct DevTune {
+    uint32_t agg_count;      // warp-aggregate the per-location count reductions
+    uint32_t agg_slot;       // warp-aggregate the CSR slot atomics
+    uint32_t blocks_per_sm;  // grid of the per-agent kernels (0 = one occupancy wave)
+    uint32_t pad;
 };
 
 struct KArgs {
@@ -152,6 +158,7 @@ struct KArgs {
     DevStatsAcc* stats;   // [R]
     uint32_t spd;         // steps per day
     uint32_t track_expected;
+    DevTune tune;
 };
 
 // raw counter slots of DevStatsAcc::c
@@ -167,7 +174,9 @@ enum {
 void launch_movement(const KArgs& k, uint32_t step_in_day, cudaStream_t s);
 void launch_count(const KArgs& k, cudaStream_t s);
 void launch_scan(const KArgs& k, uint32_t step_in_day, int with_hazard, int merge_quarantine, cudaStream_t s);
-void launch_scatter_draw(const KArgs& k, uint32_t step_in_day, int draw, cudaStream_t s);
+void launch_scatter_draw(const KArgs& k, uint32_t step_in_day, int scatter, int draw, cudaStream_t s);
+void launch_offsets(const KArgs& k, cudaStream_t s);
+void launch_step_fused(const KArgs& k, uint32_t step_in_day, cudaStream_t s);
 void launch_canonical_csr(const KArgs& k, cudaStream_t s);
 void launch_progress(const KArgs& k, uint32_t t, cudaStream_t s);
 void launch_test(const KArgs& k, uint32_t t, cudaStream_t s);

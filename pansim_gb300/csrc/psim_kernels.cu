@@ -17,6 +17,8 @@
 //
 // Built with --fmad=false: no multiply-add contraction, so every floating-point
 // expression rounds exactly like the host oracle compiled with -ffp-contract=off.
+#include <algorithm>
+
 #include "psim_device.cuh"
 
 namespace psim {
@@ -349,322 +351,390 @@ __device__ __forceinline__ unsigned lanemask_lt() {
     return m;
 }
 
-// Movement of every agent + histogram/rank + fixed-point infectiousness sums.
+// ---------------------------------------------------------------------------
+// Per-agent pieces of a step.
+
+struct StepClock {
+    uint32_t t, minutes, day, sum;
+    bool curfew_now;
+};
+
+__device__ __forceinline__ StepClock step_clock(const KArgs& k, uint32_t step) {
+    StepClock c;
+    const uint32_t dt = k.p.time_step;
+    c.t = k.clock->t0 + step;
+    c.minutes = step * dt;
+    c.day = k.clock->day_of_week;
+    c.sum = (1440u - c.minutes) / dt;
+    c.curfew_now = k.p.enable_curfew && k.p.curfew_begin == c.minutes / dt;
+    return c;
+}
+
+// doMovement for agent i (s = its steps_until_move, already loaded).
+__device__ __forceinline__ void move_agent(const KArgs& k, uint32_t i, const StepClock& c, uint32_t s) {
+    if (c.curfew_now || s == 0) {
+        const uint32_t rep = k.a.rep[i];
+        psim_stream rng;
+        psim_stream_init(&rng, k.r.seed[rep], i - k.r.agent_off[rep], c.t, PSIM_PHASE_MOVE);
+        bool done = false;
+        if (c.curfew_now) {
+            done = curfew_prologue(k, i, c.t, c.sum, &rng);
+            s = k.a.steps_until_move[i];
+        }
+        if (!done) {
+            if (s > 0)
+                k.a.steps_until_move[i] = s - 1;
+            else
+                move_decide(k, i, c.t, c.minutes, c.day, c.sum, &rng);
+        }
+    } else {
+        k.a.steps_until_move[i] = s - 1;
+    }
+}
+
+// Histogram and fixed-point infectiousness sum of the agent's location, as
+// fire-and-forget reductions (warp-aggregated per location).  Warp-collective:
+// every lane calls it, `act` false for lanes without an agent.
+__device__ __forceinline__ void count_agent(const KArgs& k, bool act, uint32_t loc, float inf, uint32_t variant) {
+    const uint32_t L = k.l.n;
+    if (act && loc >= L) {
+        atomicOr(k.err, ERR_LOCATION);
+        loc = NONE;
+    }
+    const bool ok = act && loc != NONE;
+    if (!k.tune.agg_count) {
+        if (ok) {
+            atomicAdd(&k.l.counts[loc], 1u);
+            if (inf > 0.0f) {
+                const long long q = __float2ll_rn(inf * PSIM_FIX_SCALE_F);
+                atomicAdd(&k.l.sfix[(size_t)variant * L + loc], (unsigned long long)q);
+            }
+        }
+        return;
+    }
+    const unsigned valid = __ballot_sync(0xffffffffu, ok);
+    if (ok) {
+        const unsigned peers = __match_any_sync(valid, loc);
+        if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&k.l.counts[loc], (uint32_t)__popc(peers));
+        if (inf > 0.0f) {
+            const long long q = __float2ll_rn(inf * PSIM_FIX_SCALE_F);
+            atomicAdd(&k.l.sfix[(size_t)variant * L + loc], (unsigned long long)q);
+        }
+    }
+}
+
+// CSR slot of an agent: a warp-aggregated returning atomic on the location's
+// cursor, which the scan set to the location's first slot.  Warp-collective.
+__device__ __forceinline__ uint32_t take_slot(const KArgs& k, bool ok, uint32_t loc) {
+    if (!k.tune.agg_slot) return ok ? atomicAdd(&k.l.cursor[loc], 1u) : NONE;
+    const unsigned valid = __ballot_sync(0xffffffffu, ok);
+    uint32_t pos = NONE;
+    if (ok) {
+        const unsigned peers = __match_any_sync(valid, loc);
+        const int leader = __ffs(peers) - 1;
+        uint32_t base = 0;
+        if ((int)(threadIdx.x & 31) == leader) base = atomicAdd(&k.l.cursor[loc], (uint32_t)__popc(peers));
+        base = __shfl_sync(peers, base, leader);
+        pos = base + (uint32_t)__popc(peers & lanemask_lt());
+    }
+    return pos;
+}
+
+__device__ __forceinline__ void store_slot(const KArgs& k, uint32_t pos, uint32_t i) {
+    if (pos < k.a.n)
+        k.l.csr_agents[pos] = i;
+    else
+        atomicOr(k.err, ERR_LOCATION);
+}
+
+// Infection draws of agent i at location loc with hazard h0 of variant 0
+// (LocationsList::infectAgents, locationList.h:233-310; DynamicPPState::gotInfected,
+// dynamicPPState.cpp:235-244).  Returns the sum of min(1, p) over the draws.
+__device__ __forceinline__ double draw_agent(const KArgs& k, uint32_t i, uint32_t loc, uint32_t t, float h0) {
+    const uint32_t N = k.a.n, L = k.l.n, V = k.m.n_variants;
+    const uint32_t rep = k.a.rep[i];
+    double term_sum = 0.0;
+    for (uint32_t v = 0; v < V; ++v) {
+        const float h = v == 0 ? h0 : k.l.hazard[(size_t)v * L + loc];
+        if (!(h > 0.0f)) continue;
+        if (!k.r.variant_active[rep * V + v]) continue;
+        const float su = k.a.susceptible[(size_t)v * N + i];
+        const float s_eff = su * k.p.sigma_band[k.a.band[i]];
+        if (!(s_eff > 0.0f)) continue;
+        const float pf = h * s_eff;
+        term_sum += pf < 1.0f ? (double)pf : 1.0;
+        const double U = psim_u01_once(k.r.seed[rep], i - k.r.agent_off[rep], t, PSIM_PHASE_INFECT + v);
+        if (U < (double)pf) {
+            k.a.state[i] = (int8_t)k.m.first_infected;
+            k.a.variant[i] = (uint8_t)v;
+            k.a.days[i] = -2;
+            update_meta(k, i);
+            k.a.st_infected_ts[i] = t;
+            k.a.st_infected_count[i] = k.a.st_infected_count[i] + 1;
+            k.a.st_infected_loc[i] = loc;
+            k.a.st_worst_state[i] = (int8_t)k.m.first_infected;
+            k.a.st_worst_ts[i] = t;
+            k.a.st_variant_mask[i] |= 1u << v;
+        }
+    }
+    return term_sum;
+}
+
+// expected-infection accumulation: one atomic per replica present in the warp
+__device__ __forceinline__ void add_expected(const KArgs& k, bool act, uint32_t i, double term) {
+    const unsigned am = __ballot_sync(0xffffffffu, act && term != 0.0);
+    if (!(act && term != 0.0)) return;
+    const uint32_t rep = k.a.rep[i];
+    const unsigned peers = __match_any_sync(am, rep);
+    const int leader = __ffs(peers) - 1;
+    unsigned rest = peers;
+    double tot = 0.0;
+    while (rest) {
+        const int src = __ffs(rest) - 1;
+        tot += __shfl_sync(peers, term, src);
+        rest &= rest - 1;
+    }
+    if ((int)(threadIdx.x & 31) == leader) atomicAdd(&k.r.expected[rep], tot);
+}
+
+// Movement of every agent + histogram + fixed-point infectiousness sums.
 __global__ void __launch_bounds__(256) k_movement(KArgs k, uint32_t step) {
     const uint32_t N = k.a.n;
-    const uint32_t t = k.clock->t0 + step;
-    const uint32_t dt = k.p.time_step;
-    const uint32_t minutes = step * dt;
-    const uint32_t day = k.clock->day_of_week;
-    const uint32_t sum = (1440u - minutes) / dt;
-    const bool curfew_now = k.p.enable_curfew && k.p.curfew_begin == minutes / dt;
+    const StepClock c = step_clock(k, step);
     const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t L = k.l.n;
     for (uint32_t base = blockIdx.x * blockDim.x; base < N; base += stride) {
         const uint32_t i = base + threadIdx.x;
         const bool act = i < N;
-        uint32_t loc = NONE;
+        uint32_t loc = NONE, var = 0;
+        float inf = 0.0f;
         if (act) {
-            uint32_t s = k.a.steps_until_move[i];
-            bool done = false;
-            if (curfew_now || s == 0) {
-                const uint32_t rep = k.a.rep[i];
-                psim_stream rng;
-                psim_stream_init(&rng, k.r.seed[rep], i - k.r.agent_off[rep], t, PSIM_PHASE_MOVE);
-                if (curfew_now) done = curfew_prologue(k, i, t, sum, &rng);
-                if (!done) {
-                    s = k.a.steps_until_move[i];
-                    if (s > 0) {
-                        k.a.steps_until_move[i] = s - 1;
-                    } else {
-                        move_decide(k, i, t, minutes, day, sum, &rng);
-                    }
-                }
-            } else {
-                k.a.steps_until_move[i] = s - 1;
-            }
-            loc = k.a.location[i];
-            if (loc >= L) {
-                atomicOr(k.err, ERR_LOCATION);
-                loc = NONE;
-            }
+            const uint32_t s = k.a.steps_until_move[i];
+            const uint32_t loc0 = k.a.location[i];
+            inf = k.a.infectious[i];
+            move_agent(k, i, c, s);
+            loc = (c.curfew_now || s == 0) ? k.a.location[i] : loc0;
+            if (inf > 0.0f) var = k.a.variant[i];
         }
-        // histogram with warp-aggregated atomics; the rank of an agent among
-        // the warp's agents at the same location follows lane (= agent) order
-        const unsigned valid = __ballot_sync(0xffffffffu, act && loc != NONE);
-        if (act && loc != NONE) {
-            const unsigned peers = __match_any_sync(valid, loc);
-            const int leader = __ffs(peers) - 1;
-            uint32_t basecnt = 0;
-            if ((int)(threadIdx.x & 31) == leader) basecnt = atomicAdd(&k.l.counts[loc], (uint32_t)__popc(peers));
-            basecnt = __shfl_sync(peers, basecnt, leader);
-            k.a.rank[i] = basecnt + (uint32_t)__popc(peers & lanemask_lt());
-            const float inf = k.a.infectious[i];
-            if (inf > 0.0f) {
-                const long long q = __float2ll_rn(inf * PSIM_FIX_SCALE_F);
-                atomicAdd(&k.l.sfix[(size_t)k.a.variant[i] * L + loc], (unsigned long long)q);
-            }
-        } else if (act) {
-            k.a.rank[i] = NONE;
-        }
+        count_agent(k, act, loc, inf, var);
     }
 }
 
 // Histogram + fixed-point sums without movement (regroup after an upload).
 __global__ void __launch_bounds__(256) k_count(KArgs k) {
-    const uint32_t N = k.a.n, L = k.l.n;
+    const uint32_t N = k.a.n;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < N; base += stride) {
         const uint32_t i = base + threadIdx.x;
         const bool act = i < N;
-        uint32_t loc = act ? k.a.location[i] : NONE;
-        if (act && loc >= L) {
-            atomicOr(k.err, ERR_LOCATION);
-            loc = NONE;
+        uint32_t loc = NONE, var = 0;
+        float inf = 0.0f;
+        if (act) {
+            loc = k.a.location[i];
+            inf = k.a.infectious[i];
+            if (inf > 0.0f) var = k.a.variant[i];
         }
-        const unsigned valid = __ballot_sync(0xffffffffu, act && loc != NONE);
-        if (act && loc != NONE) {
-            const unsigned peers = __match_any_sync(valid, loc);
-            const int leader = __ffs(peers) - 1;
-            uint32_t basecnt = 0;
-            if ((int)(threadIdx.x & 31) == leader) basecnt = atomicAdd(&k.l.counts[loc], (uint32_t)__popc(peers));
-            basecnt = __shfl_sync(peers, basecnt, leader);
-            k.a.rank[i] = basecnt + (uint32_t)__popc(peers & lanemask_lt());
-            const float inf = k.a.infectious[i];
-            if (inf > 0.0f) {
-                const long long q = __float2ll_rn(inf * PSIM_FIX_SCALE_F);
-                atomicAdd(&k.l.sfix[(size_t)k.a.variant[i] * L + loc], (unsigned long long)q);
-            }
-        } else if (act) {
-            k.a.rank[i] = NONE;
-        }
+        count_agent(k, act, loc, inf, var);
     }
 }
 
 // ---------------------------------------------------------------------------
-// Scan of the histogram (decoupled look-back, Merrill & Garland 2016).
-// Tile status word: [63:62] flag (1 aggregate, 2 inclusive) [61:32] epoch [31:0] value
+// Scan of the histogram in two passes (reduce, then scan): k_tile_sums adds up
+// each tile of 2048 locations; k_scan adds the sums of the tiles before its
+// own (every block reads at most a few thousand 4-byte sums, so the prefix
+// needs no inter-block waiting), scans its tile warp-striped (coalesced),
+// writes the cursor (exclusive prefix = first CSR slot of the location),
+// resets the histogram, and evaluates the infection ratio of every location
+// with a non-zero infectiousness sum.
 constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_ITEMS = 8;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
-constexpr uint32_t SCAN_SPIN_LIMIT = 1u << 22;
 
-__device__ __forceinline__ unsigned long long pack_status(uint32_t flag, uint32_t epoch, uint32_t value) {
-    return ((unsigned long long)flag << 62) | ((unsigned long long)(epoch & 0x3FFFFFFFu) << 32) | value;
+__device__ __forceinline__ uint32_t block_sum_256(uint32_t v, uint32_t* s_red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) s_red[warp] = v;
+    __syncthreads();
+    uint32_t tot = 0;
+#pragma unroll
+    for (int q = 0; q < SCAN_THREADS / 32; ++q) tot += s_red[q];
+    __syncthreads();
+    return tot;
 }
 
-// infection ratio r_l = 1 - exp(-k * (S_l / n_l) * w_l * season * dt),
-// infectionPolicies.h:523-546, evaluated in FP64 and rounded to FP32.
-__device__ __forceinline__ float hazard_of(long long fix, uint32_t n, float k_f, float w, float season, uint32_t dt) {
-    if (fix == 0 || n == 0) return 0.0f;
-    double S = (double)fix * PSIM_FIX_INV;
-    double dens = S / (double)n;
-    double x = (double)k_f * dens;
-    x = x * (double)w;
-    x = x * (double)season;
-    x = x * (double)dt;
-    return (float)psim_one_minus_exp(x);
+__global__ void __launch_bounds__(SCAN_THREADS) k_tile_sums(KArgs k) {
+    __shared__ uint32_t s_red[SCAN_THREADS / 32];
+    const uint32_t L = k.l.n;
+    const uint32_t base = blockIdx.x * SCAN_TILE;
+    uint32_t v = 0;
+#pragma unroll
+    for (int q = 0; q < SCAN_ITEMS; ++q) {
+        const uint32_t l = base + q * SCAN_THREADS + threadIdx.x;
+        v += l < L ? k.l.counts[l] : 0u;
+    }
+    v = block_sum_256(v, s_red);
+    if (threadIdx.x == 0) k.l.tile_sums[blockIdx.x] = v;
 }
 
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, int with_hazard, int merge_q) {
-    __shared__ uint32_t s_tile, s_epoch, s_prefix;
+    __shared__ uint32_t s_red[SCAN_THREADS / 32];
     __shared__ uint32_t s_warp[SCAN_THREADS / 32];
     const uint32_t L = k.l.n;
-    DevClock* clk = k.clock;
-    if (threadIdx.x == 0) {
-        s_epoch = *((volatile uint32_t*)&clk->scan_epoch);
-        s_tile = atomicAdd(&clk->scan_ticket, 1u);
-    }
-    __syncthreads();
-    const uint32_t tile = s_tile, epoch = s_epoch;
-    const uint32_t first = tile * SCAN_TILE + threadIdx.x * SCAN_ITEMS;
-    uint32_t c[SCAN_ITEMS];
-    uint32_t tsum = 0;
-#pragma unroll
-    for (int j = 0; j < SCAN_ITEMS; ++j) {
-        uint32_t l = first + j;
-        c[j] = l < L ? k.l.counts[l] : 0u;
-        tsum += c[j];
-    }
-    // block exclusive scan of thread sums
+    const uint32_t tile = blockIdx.x;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t incl = tsum;
+    const uint32_t wbase = tile * SCAN_TILE + (uint32_t)warp * (32 * SCAN_ITEMS);
+    uint32_t c[SCAN_ITEMS], ex[SCAN_ITEMS];
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += y;
+    for (int q = 0; q < SCAN_ITEMS; ++q) {
+        const uint32_t l = wbase + q * 32 + lane;
+        c[q] = l < L ? k.l.counts[l] : 0u;
     }
-    if (lane == 31) s_warp[warp] = incl;
-    __syncthreads();
-    if (warp == 0) {
-        uint32_t w = lane < SCAN_THREADS / 32 ? s_warp[lane] : 0u;
-        uint32_t wi = w;
+    // sum of the tiles before this one
+    uint32_t pre = 0;
+    for (uint32_t j = threadIdx.x; j < tile; j += SCAN_THREADS) pre += k.l.tile_sums[j];
+    const uint32_t prefix = block_sum_256(pre, s_red);
+    uint32_t carry = 0;
+#pragma unroll
+    for (int q = 0; q < SCAN_ITEMS; ++q) {
+        uint32_t x = c[q];
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            uint32_t y = __shfl_up_sync(0xffffffffu, wi, o);
-            if (lane >= o) wi += y;
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
         }
-        if (lane < SCAN_THREADS / 32) s_warp[lane] = wi - w;  // exclusive warp offsets
-        if (lane == SCAN_THREADS / 32 - 1) {
-            // tile aggregate -> look-back
-            const uint32_t agg = wi;
-            volatile unsigned long long* st = (volatile unsigned long long*)k.l.scan_status;
-            uint32_t prefix = 0;
-            if (tile == 0) {
-                __threadfence();
-                st[0] = pack_status(2, epoch, agg);
-            } else {
-                __threadfence();
-                st[tile] = pack_status(1, epoch, agg);
-                int j = (int)tile - 1;
-                uint32_t spins = 0;
-                while (j >= 0) {
-                    unsigned long long w64 = st[j];
-                    uint32_t flag = (uint32_t)(w64 >> 62);
-                    uint32_t ep = (uint32_t)(w64 >> 32) & 0x3FFFFFFFu;
-                    if (ep != (epoch & 0x3FFFFFFFu)) flag = 0;
-                    if (flag == 0) {
-                        if (++spins > SCAN_SPIN_LIMIT) {
-                            atomicOr(k.err, ERR_SCAN_WAIT);
-                            break;
-                        }
-                        continue;
-                    }
-                    prefix += (uint32_t)w64;
-                    if (flag == 2) break;
-                    --j;
-                }
-                __threadfence();
-                st[tile] = pack_status(2, epoch, prefix + agg);
-            }
-            s_prefix = prefix;
+        ex[q] = carry + x - c[q];
+        carry += __shfl_sync(0xffffffffu, x, 31);
+    }
+    if (lane == 0) s_warp[warp] = carry;
+    __syncthreads();
+    uint32_t woff = 0;
+    for (int q = 0; q < warp; ++q) woff += s_warp[q];
+    const uint32_t base = prefix + woff;
+    const uint32_t dt = k.p.time_step;
+    const float season = k.clock->season;
+    const uint32_t V = k.m.n_variants;
+#pragma unroll
+    for (int q = 0; q < SCAN_ITEMS; ++q) {
+        const uint32_t l = wbase + q * 32 + lane;
+        if (l < L) {
+            k.l.cursor[l] = base + ex[q];
+            k.l.counts[l] = 0u;
         }
     }
-    __syncthreads();
-    uint32_t run = s_prefix + s_warp[warp] + (incl - tsum);
-    const uint32_t dt = k.p.time_step;
-    const float season = clk->season;
+    if (with_hazard) {
+        for (uint32_t v = 0; v < V; ++v) {
 #pragma unroll
-    for (int j = 0; j < SCAN_ITEMS; ++j) {
-        uint32_t l = first + j;
-        if (l < L) {
-            k.l.csr_off[l] = run;
-            k.l.counts[l] = 0u;
-            if (with_hazard) {
-                const uint32_t rep = k.l.rep[l];
-                const float kf = k.r.k_f[rep];
-                const float w = k.l.infectiousness[l];
-                for (uint32_t v = 0; v < k.m.n_variants; ++v) {
+            for (int q = 0; q < SCAN_ITEMS; ++q) {
+                const uint32_t l = wbase + q * 32 + lane;
+                if (l < L) {
                     const size_t idx = (size_t)v * L + l;
                     const long long fix = (long long)k.l.sfix[idx];
-                    k.l.hazard[idx] = hazard_of(fix, c[j], kf, w, season, dt);
-                    if (fix != 0) k.l.sfix[idx] = 0ull;
+                    float h = 0.0f;
+                    if (fix != 0) {
+                        const uint32_t rep = k.l.rep[l];
+                        h = psim_hazard(fix, c[q], k.r.k_f[rep], k.l.infectiousness[l], season, dt);
+                        k.l.sfix[idx] = 0ull;
+                    }
+                    k.l.hazard[idx] = h;
                 }
             }
-            if (merge_q) {
-                uint32_t q = k.l.qu_pending[l];
-                if (q) {
-                    if (q > k.l.quarantine_until[l]) k.l.quarantine_until[l] = q;
+        }
+    }
+    if (merge_q) {
+#pragma unroll
+        for (int q = 0; q < SCAN_ITEMS; ++q) {
+            const uint32_t l = wbase + q * 32 + lane;
+            if (l < L) {
+                const uint32_t qq = k.l.qu_pending[l];
+                if (qq) {
+                    if (qq > k.l.quarantine_until[l]) k.l.quarantine_until[l] = qq;
                     k.l.qu_pending[l] = 0u;
                 }
             }
         }
-        run += c[j];
-        if (l + 1 == L) k.l.csr_off[L] = run;
-    }
-    // the last block to finish resets the tickets and advances the epoch
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        uint32_t done = atomicAdd(&clk->scan_done, 1u);
-        if (done == gridDim.x - 1) {
-            clk->scan_done = 0u;
-            clk->scan_ticket = 0u;
-            __threadfence();
-            clk->scan_epoch = epoch + 1u;
-        }
     }
 }
 
-// CSR scatter + infection draw.
-__global__ void __launch_bounds__(256) k_scatter_draw(KArgs k, uint32_t step, int draw) {
-    const uint32_t N = k.a.n, L = k.l.n, V = k.m.n_variants;
+// CSR scatter and/or infection draw of one step.
+__global__ void __launch_bounds__(256) k_scatter_draw(KArgs k, uint32_t step, int scatter, int draw) {
+    const uint32_t N = k.a.n, L = k.l.n;
     const uint32_t t = k.clock->t0 + step;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < N; base += stride) {
         const uint32_t i = base + threadIdx.x;
         const bool act = i < N;
-        double term_sum = 0.0;
-        uint32_t rep = 0;
+        double term = 0.0;
+        const uint32_t loc = act ? k.a.location[i] : NONE;
+        const bool ok = act && loc < L;
+        const float h0 = (draw && ok) ? k.l.hazard[loc] : 0.0f;
+        if (scatter) {
+            const uint32_t pos = take_slot(k, ok, loc);
+            if (ok) store_slot(k, pos, i);
+        }
+        if (ok && draw && (h0 > 0.0f || k.m.n_variants > 1)) term = draw_agent(k, i, loc, t, h0);
+        if (k.track_expected) add_expected(k, act, i, term);
+    }
+}
+
+// Scatter + draw of step `step` fused with the movement and histogram of
+// step + 1.  Both halves touch only agent i's own state and per-location
+// counters that the scan of `step` has already reset, so per agent they run
+// back to back in one pass; used inside the day graph.
+__global__ void __launch_bounds__(256) k_step_fused(KArgs k, uint32_t step) {
+    const uint32_t N = k.a.n, L = k.l.n;
+    const uint32_t t = k.clock->t0 + step;
+    const StepClock c = step_clock(k, step + 1);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < N; base += stride) {
+        const uint32_t i = base + threadIdx.x;
+        const bool act = i < N;
+        // independent loads first
+        const uint32_t loc0 = act ? k.a.location[i] : NONE;
+        const uint32_t s = act ? k.a.steps_until_move[i] : 0u;
+        float inf = act ? k.a.infectious[i] : 0.0f;
+        const bool ok = act && loc0 < L;
+        const float h0 = ok ? k.l.hazard[loc0] : 0.0f;
+        const uint32_t pos = take_slot(k, ok, loc0);
+        double term = 0.0;
+        uint32_t loc = NONE, var = 0;
+        if (ok) {
+            store_slot(k, pos, i);
+            if (h0 > 0.0f || k.m.n_variants > 1) {
+                term = draw_agent(k, i, loc0, t, h0);
+                inf = k.a.infectious[i];
+            }
+        }
         if (act) {
-            const uint32_t loc = k.a.location[i];
-            const uint32_t r = k.a.rank[i];
-            if (loc < L && r != NONE) k.l.csr_agents[k.l.csr_off[loc] + r] = i;
-            rep = k.a.rep[i];
-            if (draw && loc < L) {
-                for (uint32_t v = 0; v < V; ++v) {
-                    if (!k.r.variant_active[rep * V + v]) continue;
-                    const float h = k.l.hazard[(size_t)v * L + loc];
-                    if (h > 0.0f) {
-                        const float su = k.a.susceptible[(size_t)v * N + i];
-                        const float s_eff = su * k.p.sigma_band[k.a.band[i]];
-                        if (s_eff > 0.0f) {
-                            const float pf = h * s_eff;
-                            term_sum += pf < 1.0f ? (double)pf : 1.0;
-                            const double U = psim_u01_once(k.r.seed[rep], i - k.r.agent_off[rep], t, PSIM_PHASE_INFECT + v);
-                            if (U < (double)pf) {
-                                // DynamicPPState::gotInfected + stats, locationList.h:283-291
-                                k.a.state[i] = (int8_t)k.m.first_infected;
-                                k.a.variant[i] = (uint8_t)v;
-                                k.a.days[i] = -2;
-                                update_meta(k, i);
-                                k.a.st_infected_ts[i] = t;
-                                k.a.st_infected_count[i] = k.a.st_infected_count[i] + 1;
-                                k.a.st_infected_loc[i] = loc;
-                                k.a.st_worst_state[i] = (int8_t)k.m.first_infected;
-                                k.a.st_worst_ts[i] = t;
-                                k.a.st_variant_mask[i] |= 1u << v;
-                            }
-                        }
-                    }
-                }
-            }
+            move_agent(k, i, c, s);
+            loc = (c.curfew_now || s == 0) ? k.a.location[i] : loc0;
+            if (inf > 0.0f) var = k.a.variant[i];
         }
-        if (k.track_expected) {
-            // warp reduction per replica, one atomic per replica present in the warp
-            const unsigned am = __ballot_sync(0xffffffffu, act);
-            if (act) {
-                const unsigned peers = __match_any_sync(am, rep);
-                double s = term_sum;
-                // reduce within peer group: simple loop over peers
-                const int leader = __ffs(peers) - 1;
-                unsigned rest = peers;
-                double tot = 0.0;
-                while (rest) {
-                    int src = __ffs(rest) - 1;
-                    tot += __shfl_sync(peers, s, src);
-                    rest &= rest - 1;
-                }
-                if ((int)(threadIdx.x & 31) == leader && tot != 0.0) atomicAdd(&k.r.expected[rep], tot);
-            }
-        }
+        if (k.track_expected) add_expected(k, act, i, term);
+        count_agent(k, act, loc, inf, var);
     }
 }
 
 // Canonical CSR order (ascending agent id inside a location, the output of
 // thrust::stable_sort_by_key): the final position of agent x in its segment is
 // the number of agents of the segment with a smaller id.  O(sum n_l^2); used
-// on demand only.
-__global__ void k_canonical_rank(KArgs k, uint32_t* tmp) {
+// on demand only.  off = CSR offsets [L+1].
+__global__ void k_canonical_rank(KArgs k, const uint32_t* off, uint32_t* tmp) {
     const uint32_t N = k.a.n;
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < N; j += gridDim.x * blockDim.x) {
         const uint32_t x = k.l.csr_agents[j];
         const uint32_t l = k.a.location[x];
-        const uint32_t b = k.l.csr_off[l], e = k.l.csr_off[l + 1];
-        uint32_t c = 0;
-        for (uint32_t q = b; q < e; ++q) c += k.l.csr_agents[q] < x;
-        tmp[b + c] = x;
+        const uint32_t b = off[l], e = off[l + 1];
+        uint32_t cnt = 0;
+        for (uint32_t q = b; q < e; ++q) cnt += k.l.csr_agents[q] < x;
+        tmp[b + cnt] = x;
     }
+}
+
+// CSR offsets from the cursors after a complete scatter: cursor[l] = end of l.
+__global__ void k_offsets_from_cursor(KArgs k, uint32_t* off) {
+    const uint32_t L = k.l.n;
+    for (uint32_t l = blockIdx.x * blockDim.x + threadIdx.x; l <= L; l += gridDim.x * blockDim.x)
+        off[l] = l == 0 ? 0u : k.l.cursor[l - 1];
 }
 
 // ---------------------------------------------------------------------------
@@ -1157,20 +1227,47 @@ static unsigned grid_for(uint32_t n, int per_sm) {
     return want ? want : 1u;
 }
 
+// one full wave of resident 256-thread blocks (grid-stride kernels)
+template <typename K>
+static unsigned wave_grid(K kernel, uint32_t n) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 256, 0) != cudaSuccess || per_sm < 1) per_sm = 4;
+    return grid_for(n, per_sm);
+}
+
+static unsigned agent_grid(const KArgs& k, unsigned wave) {
+    unsigned g = k.tune.blocks_per_sm ? (unsigned)(sm_count() * k.tune.blocks_per_sm) : wave;
+    return std::min(g, grid_for(k.a.n, 1 << 20));
+}
+
 void launch_movement(const KArgs& k, uint32_t step, cudaStream_t s) {
-    k_movement<<<grid_for(k.a.n, 8), 256, 0, s>>>(k, step);
+    static unsigned g = 0;
+    if (!g) g = wave_grid(k_movement, 1u << 30);
+    k_movement<<<agent_grid(k, g), 256, 0, s>>>(k, step);
+}
+void launch_step_fused(const KArgs& k, uint32_t step, cudaStream_t s) {
+    static unsigned g = 0;
+    if (!g) g = wave_grid(k_step_fused, 1u << 30);
+    k_step_fused<<<agent_grid(k, g), 256, 0, s>>>(k, step);
 }
 void launch_count(const KArgs& k, cudaStream_t s) { k_count<<<grid_for(k.a.n, 8), 256, 0, s>>>(k); }
 void launch_scan(const KArgs& k, uint32_t, int with_hazard, int merge_q, cudaStream_t s) {
     unsigned tiles = (k.l.n + SCAN_TILE - 1) / SCAN_TILE;
-    k_scan<<<tiles ? tiles : 1, SCAN_THREADS, 0, s>>>(k, with_hazard, merge_q);
+    if (!tiles) tiles = 1;
+    k_tile_sums<<<tiles, SCAN_THREADS, 0, s>>>(k);
+    k_scan<<<tiles, SCAN_THREADS, 0, s>>>(k, with_hazard, merge_q);
 }
-void launch_scatter_draw(const KArgs& k, uint32_t step, int draw, cudaStream_t s) {
-    k_scatter_draw<<<grid_for(k.a.n, 8), 256, 0, s>>>(k, step, draw);
+void launch_scatter_draw(const KArgs& k, uint32_t step, int scatter, int draw, cudaStream_t s) {
+    static unsigned g = 0;
+    if (!g) g = wave_grid(k_scatter_draw, 1u << 30);
+    k_scatter_draw<<<agent_grid(k, g), 256, 0, s>>>(k, step, scatter, draw);
+}
+void launch_offsets(const KArgs& k, cudaStream_t s) {
+    k_offsets_from_cursor<<<grid_for(k.l.n + 1, 8), 256, 0, s>>>(k, k.l.csr_off);
 }
 void launch_canonical_csr(const KArgs& k, cudaStream_t s) {
-    // tmp = qu_pending is not free; use the rank array as scratch (rank is rebuilt every step)
-    k_canonical_rank<<<grid_for(k.a.n, 16), 256, 0, s>>>(k, k.a.rank);
+    // csr_off must be current (launch_offsets); the rank buffer is scratch
+    k_canonical_rank<<<grid_for(k.a.n, 16), 256, 0, s>>>(k, k.l.csr_off, k.a.rank);
     cudaMemcpyAsync(k.l.csr_agents, k.a.rank, sizeof(uint32_t) * k.a.n, cudaMemcpyDeviceToDevice, s);
 }
 void launch_progress(const KArgs& k, uint32_t t, cudaStream_t s) {
@@ -1202,6 +1299,6 @@ void launch_flag_hcw(const KArgs& k, cudaStream_t s) { k_flag_hcw<<<grid_for(k.a
 void launch_bounded_wait_probe(const KArgs& k, uint32_t iters, cudaStream_t s) {
     k_bounded_wait_probe<<<1, 32, 0, s>>>(k, iters);
 }
-uint64_t launches_per_step(int) { return 3; }
+uint64_t launches_per_step(int) { return 2; }
 
 }  // namespace psim

@@ -233,6 +233,63 @@ PSIM_HD double psim_one_minus_exp(double x) {
     return 1.0 - e * scale;
 }
 
+// 1 - exp(-x) for x >= 0 in FP32, deterministic across host and device
+// (explicit fmaf Horner steps; Taylor series of -expm1 below 0.5, of exp
+// after a two-part ln2 range reduction above).  Relative error a few ulp,
+// and no cancellation at small x.
+PSIM_HD float psim_one_minus_expf(float x) {
+    if (!(x > 0.0f)) return 0.0f;
+    if (x >= 20.0f) return 1.0f;
+    if (x < 0.5f) {
+        float p = 0x1.ae6456p-26f;               // k = 11
+        p = fmaf(p, x, -0x1.27e4fcp-22f);
+        p = fmaf(p, x, 0x1.71de3ap-19f);
+        p = fmaf(p, x, -0x1.a01a02p-16f);
+        p = fmaf(p, x, 0x1.a01a02p-13f);
+        p = fmaf(p, x, -0x1.6c16c2p-10f);
+        p = fmaf(p, x, 0x1.111112p-7f);
+        p = fmaf(p, x, -0x1.555556p-5f);
+        p = fmaf(p, x, 0x1.555556p-3f);
+        p = fmaf(p, x, -0x1.0p-1f);
+        p = fmaf(p, x, 1.0f);
+        return p * x;
+    }
+    const float n = floorf(fmaf(x, 0x1.715476p+0f, 0.5f));
+    float y = fmaf(-n, 0x1.63p-1f, x);
+    y = fmaf(-n, -0x1.bd0106p-13f, y);
+    const float z = -y;
+    float e = 0x1.27e4fcp-22f;                   // 1/10!
+    e = fmaf(e, z, 0x1.71de3ap-19f);
+    e = fmaf(e, z, 0x1.a01a02p-16f);
+    e = fmaf(e, z, 0x1.a01a02p-13f);
+    e = fmaf(e, z, 0x1.6c16c2p-10f);
+    e = fmaf(e, z, 0x1.111112p-7f);
+    e = fmaf(e, z, 0x1.555556p-5f);
+    e = fmaf(e, z, 0x1.555556p-3f);
+    e = fmaf(e, z, 0x1.0p-1f);
+    e = fmaf(e, z, 1.0f);
+    e = fmaf(e, z, 1.0f);
+    float scale = 1.0f;
+    const int ni = (int)n;
+    for (int i = 0; i < ni; ++i) scale *= 0.5f;
+    return 1.0f - e * scale;
+}
+
+// The infection ratio of a location (infectionPolicies.h:523-546):
+// r = 1 - exp(-k * (S / n) * w * season * dt) with S the exact fixed-point
+// sum, every step one IEEE single-precision operation.
+PSIM_HD float psim_hazard(long long fix, unsigned n, float k_f, float w, float season, unsigned dt) {
+    if (fix == 0 || n == 0) return 0.0f;
+    float S = (float)fix;
+    S = S * 0x1p-40f;
+    float x = S / (float)n;
+    x = k_f * x;
+    x = x * w;
+    x = x * season;
+    x = x * (float)dt;
+    return psim_one_minus_expf(x);
+}
+
 // Fixed-point scale for per-location infectiousness sums: every FP32 value
 // >= 2^-17 converts exactly, so the int64 sum is exact and independent of
 // summation order.

@@ -60,6 +60,8 @@ def lib(auto_build=True):
         L.psim_stream_handle.argtypes = [P, C.POINTER(P)]
         L.psim_bounded_wait_selftest.argtypes = [P, U32]
         L.psim_time_step_kernels.argtypes = [P, U32, P]
+        L.psim_set_tuning.argtypes = [P, P]
+        L.psim_get_tuning.argtypes = [P, P]
         _lib = L
     return _lib
 
@@ -204,6 +206,15 @@ class GpuSim:
         ms = np.zeros(3, np.float32)
         self._ck(lib().psim_time_step_kernels(self.h, t, _p(ms)), "time_step_kernels")
         return ms
+
+    def set_tuning(self, agg_count=1, agg_slot=1, blocks_per_sm=0):
+        t = cabi.PsimTuning(agg_count, agg_slot, blocks_per_sm, 0)
+        self._ck(lib().psim_set_tuning(self.h, C.byref(t)), "set_tuning")
+
+    def get_tuning(self):
+        t = cabi.PsimTuning()
+        self._ck(lib().psim_get_tuning(self.h, C.byref(t)), "get_tuning")
+        return dict(agg_count=t.agg_count, agg_slot=t.agg_slot, blocks_per_sm=t.blocks_per_sm)
 
     def bounded_wait_selftest(self, iters):
         return lib().psim_bounded_wait_selftest(self.h, iters)

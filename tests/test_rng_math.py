@@ -25,6 +25,17 @@ def test_one_minus_exp_matches_libm():
     assert ob.one_minus_exp(50.0) == 1.0
 
 
+def test_one_minus_expf_accuracy():
+    """The FP32 evaluation used for the hazard: a few ulp of the exact value
+    over the whole range, no cancellation at small x."""
+    xs = np.concatenate([np.logspace(-9, -0.31, 300), np.linspace(0.49, 25, 300)]).astype(np.float32)
+    for x in xs:
+        ref = -math.expm1(-float(x))
+        got = ob.one_minus_expf(float(x))
+        assert abs(got - ref) <= 4 * float(np.spacing(np.float32(ref))) + 1e-30, (x, got, ref)
+    assert ob.one_minus_expf(0.0) == 0.0 and ob.one_minus_expf(30.0) == 1.0
+
+
 def test_seasonality_day0():
     from pansim_gb300 import synth
     s = synth.make_snapshot(200, 50)
