@@ -216,7 +216,7 @@ typedef struct psim_tuning {
     uint32_t agg_count;      /* warp-aggregated per-location count reductions */
     uint32_t agg_slot;       /* warp-aggregated CSR slot atomics */
     uint32_t blocks_per_sm;  /* 256-thread blocks per SM of the per-agent kernels; 0 = occupancy */
-    uint32_t pad;
+    uint32_t variant;        /* register cap of the fused step kernel: 0 = 64, 1 = 40, 2 = 32 */
 } psim_tuning;
 
 typedef struct psim_ctx psim_ctx;

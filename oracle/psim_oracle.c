@@ -66,13 +66,15 @@ static void update_meta(psim_oracle* o, uint32_t i) {
     for (uint32_t v = 0; v < m->n_variants; ++v) o->a->susceptible[(size_t)v * o->a->n + i] = su;
 }
 
-/* RealMovementOps::findActualLocationForType, movementPolicies.h:69-122 */
-static uint32_t find_location(psim_oracle* o, uint32_t i, uint32_t loc_type, int retry, psim_stream* rng) {
-    const psim_params* p = &o->p;
+/* RealMovementOps::findActualLocationForType, movementPolicies.h:69-122.
+ * f0, f1, f2: the types resolved by first match (the callers pass home,
+ * school, work, except the plan helpers, :1073-1080, :1144, :1209-1214). */
+static uint32_t find_location3(psim_oracle* o, uint32_t i, uint32_t loc_type, int retry, psim_stream* rng,
+                               uint32_t f0, uint32_t f1, uint32_t f2) {
     const uint32_t* off = o->a->loc_offset;
     const uint32_t* pl = o->a->poss_loc;
     const uint8_t* pt = o->a->poss_type;
-    if (loc_type == p->home_type || loc_type == p->school_type || loc_type == p->work_type) {
+    if (loc_type == f0 || loc_type == f1 || loc_type == f2) {
         for (uint32_t k = off[i]; k < off[i + 1]; ++k)
             if (loc_type == pt[k]) return pl[k];
         return NONE;
@@ -105,6 +107,10 @@ static uint32_t find_location(psim_oracle* o, uint32_t i, uint32_t loc_type, int
         }
     }
     return NONE;
+}
+
+static uint32_t find_location(psim_oracle* o, uint32_t i, uint32_t loc_type, int retry, psim_stream* rng) {
+    return find_location3(o, i, loc_type, retry, rng, o->p.home_type, o->p.school_type, o->p.work_type);
 }
 
 
@@ -143,6 +149,10 @@ static void quarantine_agent(psim_oracle* o, uint32_t i, uint32_t t, uint32_t un
 }
 
 static inline uint32_t steps_until_midnight(uint32_t minutes, uint32_t dt) { return (1440u - minutes) / dt; }
+
+/* minutes of TimeDayDuration(unsigned mins) (timeDay.cpp:64): the hours are an
+ * unsigned char, so a difference that went negative folds modulo 256 hours */
+static inline uint32_t td_minutes(uint32_t mins) { return (uint32_t)(uint8_t)(mins / 60u) * 60u + mins % 60u; }
 
 static int is_quarantine_type(const psim_oracle* o, uint32_t loc) {
     uint32_t ty = o->l->type[loc];
@@ -353,13 +363,15 @@ static void do_movement(psim_oracle* o, uint32_t i, uint32_t t, uint32_t minutes
             else
                 a->steps_until_move[i] = dur / dt;
         } else {
-            uint32_t nstart = m->ev_start[act_e], nend = m->ev_end[act_e];
+            /* a read past the last event yields a 24:00 window */
+            uint32_t nstart = (uint32_t)act_e < m->n_events ? m->ev_start[act_e] : 1440u;
+            uint32_t nend = (uint32_t)act_e < m->n_events ? m->ev_end[act_e] : 1440u;
             if (minutes + dur < nstart) {
                 a->steps_until_move[i] = dur / dt;
             } else if (minutes + dur > nend) {
-                a->steps_until_move[i] = (nend - minutes) / dt - 1u;
+                a->steps_until_move[i] = td_minutes(nend - minutes) / dt - 1u;
             } else {
-                uint32_t st = (nend - (minutes + dur)) / dt;
+                uint32_t st = td_minutes(nend - (minutes + dur)) / dt;
                 uint32_t extra = psim_below(&rng, st);
                 a->steps_until_move[i] = dur / dt + extra;
             }
@@ -373,9 +385,9 @@ static void do_movement(psim_oracle* o, uint32_t i, uint32_t t, uint32_t minutes
     }
     /* Case 3, :858-911 */
     if (act_b == -1 && act_e != -1) {
-        uint32_t length_steps = (uint32_t)(m->ev_end[act_e] - m->ev_start[act_e]) / dt;
+        uint32_t length_steps = td_minutes((uint32_t)m->ev_end[act_e] - (uint32_t)m->ev_start[act_e]) / dt;
         uint32_t delay = psim_below(&rng, length_steps);
-        a->steps_until_move[i] = (m->ev_start[act_e] - minutes) / dt + delay;
+        a->steps_until_move[i] = td_minutes((uint32_t)m->ev_start[act_e] - minutes) / dt + delay;
         uint32_t left = a->steps_until_move[i];
         if (left < 30u / dt) {
             /* 3a: stay */
@@ -852,9 +864,9 @@ void psim_oracle_plan(psim_oracle* o, uint32_t t) {
             uint32_t rep_ = o->agent_rep[i];
             psim_stream frng;
             psim_stream_init(&frng, o->r.seed[rep_], i - o->r.agent_offset[rep_], t, PSIM_PHASE_PLAN_SWQ);
-            uint32_t work = find_location(o, i, p->work_type, 0, &frng);
-            uint32_t school = find_location(o, i, p->school_type, 0, &frng);
-            uint32_t classroom = find_location(o, i, p->classroom_type, 0, &frng);
+            uint32_t work = find_location3(o, i, p->work_type, 0, &frng, p->home_type, p->school_type, p->classroom_type);
+            uint32_t school = find_location3(o, i, p->school_type, 0, &frng, p->home_type, p->school_type, p->classroom_type);
+            uint32_t classroom = find_location3(o, i, p->classroom_type, 0, &frng, p->home_type, p->school_type, p->classroom_type);
             uint32_t until = 0;
             if (school != NONE && L->quarantine_until[school] > t)
                 until = L->quarantine_until[school];
@@ -886,12 +898,12 @@ void psim_oracle_plan(psim_oracle* o, uint32_t t) {
         uint32_t rep_ = o->agent_rep[i];
         psim_stream frng;
         psim_stream_init(&frng, o->r.seed[rep_], i - o->r.agent_offset[rep_], t, PSIM_PHASE_PLAN_UNDERAGE);
-        uint32_t home = find_location(o, i, p->home_type, 0, &frng);
+        uint32_t home = find_location3(o, i, p->home_type, 0, &frng, p->home_type, p->school_type, p->classroom_type);
         if (a->quarantined[i]) {
             if (home != NONE) o->no_work_loc[home] = 1;
         } else {
-            uint32_t school = find_location(o, i, p->school_type, 0, &frng);
-            uint32_t classroom = find_location(o, i, p->classroom_type, 0, &frng);
+            uint32_t school = find_location3(o, i, p->school_type, 0, &frng, p->home_type, p->school_type, p->classroom_type);
+            uint32_t classroom = find_location3(o, i, p->classroom_type, 0, &frng, p->home_type, p->school_type, p->classroom_type);
             int too_old = a->age[i] >= p->school_age_restriction;
             if (too_old || (school != NONE && (L->open[school] == 0 || L->closed_until[school] > t)) ||
                 (classroom != NONE && (L->open[classroom] == 0 || L->closed_until[classroom] > t))) {
@@ -905,7 +917,7 @@ void psim_oracle_plan(psim_oracle* o, uint32_t t) {
             uint32_t rep_ = o->agent_rep[i];
             psim_stream frng;
             psim_stream_init(&frng, o->r.seed[rep_], i - o->r.agent_offset[rep_], t, PSIM_PHASE_PLAN_NOWORK);
-            uint32_t home = find_location(o, i, p->home_type, 0, &frng);
+            uint32_t home = find_location3(o, i, p->home_type, 0, &frng, p->home_type, p->home_type, p->home_type);
             if (home != NONE && o->no_work_loc[home] == 1) {
                 o->no_work_loc[home] = 2;
                 a->no_work[i] = 1;

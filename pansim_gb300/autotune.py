@@ -11,12 +11,14 @@ import itertools
 
 import numpy as np
 
-DEFAULT_GRID = [0, 2, 4, 6, 8]
+DEFAULT_GRID = [0, 4, 8, 16]
 
 
 def candidates(grid=None):
-    for agg_count, agg_slot, bps in itertools.product([1, 0], [1, 0], grid or DEFAULT_GRID):
-        yield dict(agg_count=agg_count, agg_slot=agg_slot, blocks_per_sm=bps)
+    """variant: register cap of the fused kernel (64 / 40 / 32 registers);
+    blocks_per_sm 0 = one occupancy wave of that variant."""
+    for variant, agg_count, agg_slot, bps in itertools.product([0, 1, 2], [1, 0], [1, 0], grid or DEFAULT_GRID):
+        yield dict(agg_count=agg_count, agg_slot=agg_slot, blocks_per_sm=bps, variant=variant)
 
 
 def autotune(sim, day, reps=3, grid=None, verbose=False):

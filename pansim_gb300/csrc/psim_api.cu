@@ -392,6 +392,7 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     dm.noncovid_dead = m->noncovid_dead_state;
     dm.dead_state = m->dead_state;
     dm.n_trans = m->n_trans;
+    dm.n_events = m->n_events;
     const size_t S = m->n_states, PS = (size_t)m->n_prog * S;
     std::vector<uint32_t> thr(PS * PSIM_MAX_STRAINS);
     for (size_t j = 0; j < thr.size(); ++j) thr[j] = psim_geometric_threshold(m->len_p[j]);
@@ -476,6 +477,7 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     k.tune.agg_count = 1;
     k.tune.agg_slot = 1;
     k.tune.blocks_per_sm = 0;
+    k.tune.variant = 0;
     c->h_stats.resize(R);
     c->h_expected.assign(R, 0.0);
     // healthcare workers per replica (Simulation::flagHealthcareWorkers, simulation.h:670-693)
@@ -561,6 +563,8 @@ int psim_set_tuning(psim_ctx* c, const psim_tuning* t) {
     c->k.tune.agg_count = t->agg_count ? 1u : 0u;
     c->k.tune.agg_slot = t->agg_slot ? 1u : 0u;
     c->k.tune.blocks_per_sm = t->blocks_per_sm;
+    if (t->variant > 2) return fail(c, PSIM_ERR_ARG, "variant out of range");
+    c->k.tune.variant = t->variant;
     c->graph_dirty = true;
     return 0;
 }
@@ -570,7 +574,7 @@ int psim_get_tuning(psim_ctx* c, psim_tuning* t) {
     t->agg_count = c->k.tune.agg_count;
     t->agg_slot = c->k.tune.agg_slot;
     t->blocks_per_sm = c->k.tune.blocks_per_sm;
-    t->pad = 0;
+    t->variant = c->k.tune.variant;
     return 0;
 }
 

@@ -20,6 +20,7 @@ constexpr uint32_t ERR_TEST_WAIT = 4u;     // bounded-wait self test expired (ex
 struct DevModel {
     uint32_t n_states, n_variants, n_prog, n_agent_types;
     uint32_t first_infected, noncovid_dead, dead_state, n_trans;
+    uint32_t n_events, pad0;
     const uint8_t* state_wb;
     const uint8_t* state_susceptible;
     const uint8_t* state_infected;
@@ -144,7 +145,7 @@ struct DevTune {
     uint32_t agg_count;      // warp-aggregate the per-location count reductions
     uint32_t agg_slot;       // warp-aggregate the CSR slot atomics
     uint32_t blocks_per_sm;  // grid of the per-agent kernels (0 = one occupancy wave)
-    uint32_t pad;
+    uint32_t variant;        // register cap of the fused step kernel: 0 = 64, 1 = 40, 2 = 32 registers
 };
 
 struct KArgs {

@@ -44,10 +44,13 @@ __device__ __forceinline__ void update_meta(const KArgs& k, uint32_t i) {
     for (uint32_t v = 0; v < k.m.n_variants; ++v) k.a.susceptible[(size_t)v * k.a.n + i] = su;
 }
 
-// RealMovementOps::findActualLocationForType, movementPolicies.h:69-122
-__device__ uint32_t find_location(const KArgs& k, uint32_t i, uint32_t lt, int retry, psim_stream* rng) {
+// RealMovementOps::findActualLocationForType, movementPolicies.h:69-122.
+// f0, f1, f2: the types resolved by first match (home, school, work except in
+// the plan helpers, movementPolicies.h:1073-1080, :1144, :1209-1214).
+__device__ uint32_t find_location3(const KArgs& k, uint32_t i, uint32_t lt, int retry, psim_stream* rng, uint32_t f0,
+                                   uint32_t f1, uint32_t f2) {
     const uint32_t b = k.a.loc_offset[i], e = k.a.loc_offset[i + 1];
-    if (lt == k.p.home_type || lt == k.p.school_type || lt == k.p.work_type) {
+    if (lt == f0 || lt == f1 || lt == f2) {
         for (uint32_t j = b; j < e; ++j)
             if (lt == k.a.poss_type[j]) return k.a.poss_loc[j];
         return NONE;
@@ -82,6 +85,10 @@ __device__ uint32_t find_location(const KArgs& k, uint32_t i, uint32_t lt, int r
     return NONE;
 }
 
+__device__ __forceinline__ uint32_t find_location(const KArgs& k, uint32_t i, uint32_t lt, int retry, psim_stream* rng) {
+    return find_location3(k, i, lt, retry, rng, k.p.home_type, k.p.school_type, k.p.work_type);
+}
+
 __device__ __forceinline__ void qu_write(const KArgs& k, uint32_t loc, uint32_t until) {
     if (loc < k.l.n) atomicMax(&k.l.qu_pending[loc], until);
 }
@@ -113,6 +120,10 @@ __device__ void quarantine_agent(const KArgs& k, uint32_t i, uint32_t t, uint32_
         }
     }
 }
+
+// minutes of TimeDayDuration(unsigned mins) (timeDay.cpp:64): the hours are
+// an unsigned char, so a difference that went negative folds modulo 256 hours
+__device__ __forceinline__ uint32_t td_minutes(uint32_t mins) { return (uint32_t)(uint8_t)(mins / 60u) * 60u + mins % 60u; }
 
 __device__ __forceinline__ bool is_quarantine_type(const KArgs& k, uint32_t loc) {
     uint32_t ty = loc_type(k, loc);
@@ -270,13 +281,15 @@ __device__ void move_decide(const KArgs& k, uint32_t i, uint32_t t, uint32_t min
         } else if (act_e == -1) {
             *sum_ptr = (minutes + dur >= 1440u) ? sum : dur / dt;
         } else {
-            uint32_t nstart = k.m.ev_start[act_e], nend = k.m.ev_end[act_e];
+            // a read past the last event yields a 24:00 window
+            const bool in = (uint32_t)act_e < k.m.n_events;
+            uint32_t nstart = in ? k.m.ev_start[act_e] : 1440u, nend = in ? k.m.ev_end[act_e] : 1440u;
             if (minutes + dur < nstart) {
                 *sum_ptr = dur / dt;
             } else if (minutes + dur > nend) {
-                *sum_ptr = (nend - minutes) / dt - 1u;
+                *sum_ptr = td_minutes(nend - minutes) / dt - 1u;
             } else {
-                uint32_t st = (nend - (minutes + dur)) / dt;
+                uint32_t st = td_minutes(nend - (minutes + dur)) / dt;
                 uint32_t extra = psim_below(rng, st);
                 *sum_ptr = dur / dt + extra;
             }
@@ -287,9 +300,9 @@ __device__ void move_decide(const KArgs& k, uint32_t i, uint32_t t, uint32_t min
         }
     }
     if (act_b == -1 && act_e != -1) {  // Case 3
-        uint32_t length_steps = (uint32_t)(k.m.ev_end[act_e] - k.m.ev_start[act_e]) / dt;
+        uint32_t length_steps = td_minutes((uint32_t)k.m.ev_end[act_e] - (uint32_t)k.m.ev_start[act_e]) / dt;
         uint32_t delay = psim_below(rng, length_steps);
-        *sum_ptr = (k.m.ev_start[act_e] - minutes) / dt + delay;
+        *sum_ptr = td_minutes((uint32_t)k.m.ev_start[act_e] - minutes) / dt + delay;
         uint32_t left = *sum_ptr;
         if (left < 30u / dt) {
         } else if (left < 60u / dt) {
@@ -680,7 +693,8 @@ __global__ void __launch_bounds__(256) k_scatter_draw(KArgs k, uint32_t step, in
 // step + 1.  Both halves touch only agent i's own state and per-location
 // counters that the scan of `step` has already reset, so per agent they run
 // back to back in one pass; used inside the day graph.
-__global__ void __launch_bounds__(256) k_step_fused(KArgs k, uint32_t step) {
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) k_step_fused(KArgs k, uint32_t step) {
     const uint32_t N = k.a.n, L = k.l.n;
     const uint32_t t = k.clock->t0 + step;
     const StepClock c = step_clock(k, step + 1);
@@ -1089,9 +1103,9 @@ __global__ void __launch_bounds__(256) k_plan_agents(KArgs k, uint32_t t) {
             const uint32_t rep = k.a.rep[i];
             psim_stream rng;
             psim_stream_init(&rng, k.r.seed[rep], i - k.r.agent_off[rep], t, PSIM_PHASE_PLAN_SWQ);
-            const uint32_t work = find_location(k, i, p.work_type, 0, &rng);
-            const uint32_t school = find_location(k, i, p.school_type, 0, &rng);
-            const uint32_t classroom = find_location(k, i, p.classroom_type, 0, &rng);
+            const uint32_t work = find_location3(k, i, p.work_type, 0, &rng, p.home_type, p.school_type, p.classroom_type);
+            const uint32_t school = find_location3(k, i, p.school_type, 0, &rng, p.home_type, p.school_type, p.classroom_type);
+            const uint32_t classroom = find_location3(k, i, p.classroom_type, 0, &rng, p.home_type, p.school_type, p.classroom_type);
             uint32_t until = 0;
             if (school != NONE && loc_qu(k, school) > t)
                 until = loc_qu(k, school);
@@ -1135,13 +1149,13 @@ __global__ void __launch_bounds__(256) k_plan_underage(KArgs k, uint32_t t) {
         const uint32_t rep = k.a.rep[i];
         psim_stream rng;
         psim_stream_init(&rng, k.r.seed[rep], i - k.r.agent_off[rep], t, PSIM_PHASE_PLAN_UNDERAGE);
-        const uint32_t home = find_location(k, i, p.home_type, 0, &rng);
+        const uint32_t home = find_location3(k, i, p.home_type, 0, &rng, p.home_type, p.school_type, p.classroom_type);
         bool flag = false;
         if (k.a.quarantined[i]) {
             flag = true;
         } else {
-            const uint32_t school = find_location(k, i, p.school_type, 0, &rng);
-            const uint32_t classroom = find_location(k, i, p.classroom_type, 0, &rng);
+            const uint32_t school = find_location3(k, i, p.school_type, 0, &rng, p.home_type, p.school_type, p.classroom_type);
+            const uint32_t classroom = find_location3(k, i, p.classroom_type, 0, &rng, p.home_type, p.school_type, p.classroom_type);
             const bool too_old = k.a.age[i] >= p.school_age_restriction;
             flag = too_old || (school != NONE && (loc_open(k, school) == 0 || loc_closed_until(k, school) > t)) ||
                    (classroom != NONE && (loc_open(k, classroom) == 0 || loc_closed_until(k, classroom) > t));
@@ -1159,7 +1173,7 @@ __global__ void __launch_bounds__(256) k_plan_nowork_min(KArgs k, uint32_t t) {
         const uint32_t rep = k.a.rep[i];
         psim_stream rng;
         psim_stream_init(&rng, k.r.seed[rep], i - k.r.agent_off[rep], t, PSIM_PHASE_PLAN_NOWORK);
-        const uint32_t home = find_location(k, i, p.home_type, 0, &rng);
+        const uint32_t home = find_location3(k, i, p.home_type, 0, &rng, p.home_type, p.home_type, p.home_type);
         if (home < k.l.n && k.l.no_work_loc[home] != 0u) atomicMin(&k.l.no_work_loc[home], i);
     }
 }
@@ -1172,7 +1186,7 @@ __global__ void __launch_bounds__(256) k_plan_nowork_set(KArgs k, uint32_t t) {
         const uint32_t rep = k.a.rep[i];
         psim_stream rng;
         psim_stream_init(&rng, k.r.seed[rep], i - k.r.agent_off[rep], t, PSIM_PHASE_PLAN_NOWORK);
-        const uint32_t home = find_location(k, i, p.home_type, 0, &rng);
+        const uint32_t home = find_location3(k, i, p.home_type, 0, &rng, p.home_type, p.home_type, p.home_type);
         if (home < k.l.n && k.l.no_work_loc[home] == i) k.a.no_work[i] = 1;
     }
 }
@@ -1245,10 +1259,24 @@ void launch_movement(const KArgs& k, uint32_t step, cudaStream_t s) {
     if (!g) g = wave_grid(k_movement, 1u << 30);
     k_movement<<<agent_grid(k, g), 256, 0, s>>>(k, step);
 }
+// register-capped instantiations of the fused step kernel: a tighter cap
+// raises occupancy for the hot path and spills on the rare cold path; the
+// autotuner picks one (DevTune::variant)
 void launch_step_fused(const KArgs& k, uint32_t step, cudaStream_t s) {
-    static unsigned g = 0;
-    if (!g) g = wave_grid(k_step_fused, 1u << 30);
-    k_step_fused<<<agent_grid(k, g), 256, 0, s>>>(k, step);
+    static unsigned g[3] = {0, 0, 0};
+    const uint32_t v = k.tune.variant < 3 ? k.tune.variant : 0;
+    if (!g[0]) {
+        g[0] = wave_grid(k_step_fused<4>, 1u << 30);
+        g[1] = wave_grid(k_step_fused<6>, 1u << 30);
+        g[2] = wave_grid(k_step_fused<8>, 1u << 30);
+    }
+    const unsigned grid = agent_grid(k, g[v]);
+    if (v == 0)
+        k_step_fused<4><<<grid, 256, 0, s>>>(k, step);
+    else if (v == 1)
+        k_step_fused<6><<<grid, 256, 0, s>>>(k, step);
+    else
+        k_step_fused<8><<<grid, 256, 0, s>>>(k, step);
 }
 void launch_count(const KArgs& k, cudaStream_t s) { k_count<<<grid_for(k.a.n, 8), 256, 0, s>>>(k); }
 void launch_scan(const KArgs& k, uint32_t, int with_hazard, int merge_q, cudaStream_t s) {

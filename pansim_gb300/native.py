@@ -207,14 +207,14 @@ class GpuSim:
         self._ck(lib().psim_time_step_kernels(self.h, t, _p(ms)), "time_step_kernels")
         return ms
 
-    def set_tuning(self, agg_count=1, agg_slot=1, blocks_per_sm=0):
-        t = cabi.PsimTuning(agg_count, agg_slot, blocks_per_sm, 0)
+    def set_tuning(self, agg_count=1, agg_slot=1, blocks_per_sm=0, variant=0):
+        t = cabi.PsimTuning(agg_count, agg_slot, blocks_per_sm, variant)
         self._ck(lib().psim_set_tuning(self.h, C.byref(t)), "set_tuning")
 
     def get_tuning(self):
         t = cabi.PsimTuning()
         self._ck(lib().psim_get_tuning(self.h, C.byref(t)), "get_tuning")
-        return dict(agg_count=t.agg_count, agg_slot=t.agg_slot, blocks_per_sm=t.blocks_per_sm)
+        return dict(agg_count=t.agg_count, agg_slot=t.agg_slot, blocks_per_sm=t.blocks_per_sm, variant=t.variant)
 
     def bounded_wait_selftest(self, iters):
         return lib().psim_bounded_wait_selftest(self.h, iters)

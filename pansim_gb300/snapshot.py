@@ -183,6 +183,35 @@ class Snapshot:
         return True
 
 
+def save(snap, path, compress=True):
+    """Binary snapshot (numpy .npz): every array and scalar of the model,
+    agents, locations, parameters and replicas."""
+    out = {}
+    for k, v in snap.model.items():
+        out["model/" + k] = np.asarray(v)
+    for k, v in snap.agents.items():
+        out["agents/" + k] = v
+    for k, v in snap.locs.items():
+        out["locs/" + k] = v
+    for k, v in snap.params.items():
+        out["params/" + k] = np.asarray(v)
+    for k, v in snap.reps.items():
+        out["reps/" + k] = v
+    (np.savez_compressed if compress else np.savez)(path, **out)
+
+
+def load(path):
+    d = np.load(path, allow_pickle=False)
+    parts = {"model": {}, "agents": {}, "locs": {}, "params": {}, "reps": {}}
+    for key in d.files:
+        group, name = key.split("/", 1)
+        v = d[key]
+        if group in ("model", "params") and v.ndim == 0:
+            v = v.item()
+        parts[group][name] = v
+    return Snapshot(parts["model"], parts["agents"], parts["locs"], parts["params"], parts["reps"])
+
+
 def concat(snaps, seeds, ks):
     """Batch replicas into one snapshot (agents and locations concatenated,
     per-agent location indices shifted)."""

@@ -171,6 +171,13 @@ def make_schedules(rng, n_types=4):
             for day in range(7):
                 if wb in (WB["W"], WB["N"]):
                     evs = per_slot[(ty, "weekday" if day < 5 else "weekend")]
+                elif ty == n_types - 1 and wb == WB["S"] and day == 6:
+                    # padding: when the last event of a slot is active the
+                    # reference reads the event after it as the next window
+                    # (movementPolicies.h:601-603, 794-811); for the last slot
+                    # with events that is this one, a 24:00 window.  S-state
+                    # agents never look up a schedule, so it is never active.
+                    evs = [(HOME, 1.0, 1440, 1440, 0)]
                 else:
                     evs = []
                 ev.extend(evs)

@@ -1,0 +1,80 @@
+"""The oracle pinned against the reference's own C++ (CPU).
+
+oracle/ref_harness compiles the reference's hot-path sources (doMovement,
+quarantine/plan helpers, DetailedTesting ops, DynamicPPState/MultiBadMatrix,
+Util::updatePerLocationAgentLists, TimeDay/AgentTypeList) with an interposed
+RandomGenerator drawing from the same Philox streams.  Every agent and
+location array must equal the oracle's bit for bit.  Skipped where the
+reference tree is absent.
+"""
+import numpy as np
+import pytest
+
+from oracle import binding as ob
+from tests.helpers import diff_state, small_snapshot
+
+rb = pytest.importorskip("oracle.ref_binding")
+if not rb.ref_build.available():
+    pytest.skip("reference tree not available", allow_module_level=True)
+
+
+def _run_pair(snap, days):
+    s_ref = snap.copy()
+    o = ob.Oracle(snap)
+    r = rb.RefSim(s_ref)
+    for d in range(days):
+        o.run_day(d)
+        r.run_day(d)
+        r.sync()
+        assert diff_state(snap, s_ref) == [], "day %d" % d
+    return o, r, snap, s_ref
+
+
+def test_schedule_encoding_matches_reference_timeday():
+    s = small_snapshot(2000, 500)
+    r = rb.RefSim(s.copy())
+    st, en, du = r.event_minutes()
+    assert np.array_equal(st, s.model["ev_start"])
+    assert np.array_equal(en, s.model["ev_end"])
+    assert np.array_equal(du, s.model["ev_duration"])
+
+
+def test_pin_plain_week():
+    o, r, a, b = _run_pair(small_snapshot(8000, 2000, seed=5, initial_infected_frac=0.02), 7)
+    assert (a.agents["st_infected_count"] > 0).sum() > 100
+
+
+def test_pin_quarantine_testing():
+    s = small_snapshot(8000, 2000, seed=9, initial_infected_frac=0.02, quarantine_policy=3, testing=True)
+    s.params.update(t_random=0.02, t_home=0.3, t_work=0.1, t_school=0.1, t_hospital=0.2)
+    o, r, a, b = _run_pair(s, 8)
+    assert a.agents["quarantined"].sum() > 50
+    assert (a.agents["last_test"] != 0xFFFFFFFF).sum() > 100
+
+
+def test_pin_curfew_closures_school_age():
+    s = small_snapshot(6000, 1500, seed=13, initial_infected_frac=0.03)
+    s.params.update(enable_curfew=1, curfew_begin=120, curfew_end=36, school_age_restriction=10)
+    rng = np.random.default_rng(4)
+    s.locs["open"][rng.random(s.n_locations) < 0.25] = 0
+    s.locs["closed_until"][rng.random(s.n_locations) < 0.1] = 400
+    _run_pair(s, 4)
+
+
+def test_pin_csr_matches_stable_sort():
+    s = small_snapshot(5000, 1200, seed=2)
+    s_ref = s.copy()
+    o = ob.Oracle(s)
+    r = rb.RefSim(s_ref)
+    o.midnight(0)
+    r.midnight(0)
+    for t in range(0, 70):
+        o.step(t)
+        r.step(t)
+    off_o, ag_o = o.csr()
+    off_r, ag_r = r.csr()
+    assert np.array_equal(ag_o, ag_r)
+    # the reference's OpenMP extractOffsets (util.cpp:39-53) leaves the offsets
+    # of empty locations below the first occupied one unwritten
+    first = int(np.min(s.agents["location"]))
+    assert np.array_equal(off_o[first + 1:], off_r[first + 1:])
