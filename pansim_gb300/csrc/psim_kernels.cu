@@ -1174,7 +1174,8 @@ __global__ void __launch_bounds__(256) k_plan_nowork_min(KArgs k, uint32_t t) {
         psim_stream rng;
         psim_stream_init(&rng, k.r.seed[rep], i - k.r.agent_off[rep], t, PSIM_PHASE_PLAN_NOWORK);
         const uint32_t home = find_location3(k, i, p.home_type, 0, &rng, p.home_type, p.home_type, p.home_type);
-        if (home < k.l.n && k.l.no_work_loc[home] != 0u) atomicMin(&k.l.no_work_loc[home], i);
+        // 0 = home not flagged, NONE = flagged, else 1 + the lowest claiming id
+        if (home < k.l.n && k.l.no_work_loc[home] != 0u) atomicMin(&k.l.no_work_loc[home], i + 1u);
     }
 }
 
@@ -1187,7 +1188,7 @@ __global__ void __launch_bounds__(256) k_plan_nowork_set(KArgs k, uint32_t t) {
         psim_stream rng;
         psim_stream_init(&rng, k.r.seed[rep], i - k.r.agent_off[rep], t, PSIM_PHASE_PLAN_NOWORK);
         const uint32_t home = find_location3(k, i, p.home_type, 0, &rng, p.home_type, p.home_type, p.home_type);
-        if (home < k.l.n && k.l.no_work_loc[home] == i) k.a.no_work[i] = 1;
+        if (home < k.l.n && k.l.no_work_loc[home] == i + 1u) k.a.no_work[i] = 1;
     }
 }
 
