@@ -290,6 +290,29 @@ int psim_stream_handle(psim_ctx* ctx, void** out);
  * bounded wait in the library without faulting the GPU. */
 int psim_bounded_wait_selftest(psim_ctx* ctx, uint32_t iters);
 
+/* psim_csr_build_noalloc — no counterpart in the reference.
+ * For callers that cannot call cudaMalloc (their device memory belongs to
+ * another allocator such as a framework's caching allocator or a pool set up
+ * once, plug-ins that must not grow the device footprint, latency-sensitive
+ * loops where cudaMalloc/cudaFree would synchronize the device): builds the
+ * location CSR of a device array d_location[n_agents] (values < n_locations)
+ * into caller-owned device buffers d_offsets[n_locations+1] and
+ * d_agents[n_agents], on `stream` (a cudaStream_t, may be NULL), allocating
+ * nothing.  Its scratch is one file-scope __device__ array sized for
+ * PSIM_NOALLOC_MAX_LOCATIONS locations (about 16.8 MB, held by every GPU that
+ * loads the library until the process exits); larger sizes are rejected with
+ * PSIM_ERR_ARG and a message in psim_noalloc_last_error().  The first call on
+ * a device looks up the array's device address (cudaGetSymbolAddress): make
+ * that first call before any stream capture.  All calls share the array and
+ * it keeps the last call's contents (the histogram is cleared at the start of
+ * each call); calls that overlap on the GPU race.  The order of the agents
+ * within a location is unspecified; locations >= n_locations are left out. */
+#define PSIM_NOALLOC_MAX_LOCATIONS (1u << 21)
+#define PSIM_NOALLOC_MAX_AGENTS 0xFFFFFFF0u
+int psim_csr_build_noalloc(const uint32_t* d_location, uint32_t n_agents, uint32_t n_locations,
+                           uint32_t* d_offsets, uint32_t* d_agents, void* stream);
+const char* psim_noalloc_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -61,6 +61,8 @@ def lib(auto_build=True):
         L.psim_bounded_wait_selftest.argtypes = [P, U32]
         L.psim_time_step_kernels.argtypes = [P, U32, P]
         L.psim_set_tuning.argtypes = [P, P]
+        L.psim_csr_build_noalloc.argtypes = [P, U32, U32, P, P, P]
+        L.psim_noalloc_last_error.restype = C.c_char_p
         L.psim_get_tuning.argtypes = [P, P]
         _lib = L
     return _lib
