@@ -263,6 +263,27 @@ int psim_run_day(psim_ctx* ctx, uint32_t day, psim_day_stats* out /* [replicas] 
 int psim_set_tuning(psim_ctx* ctx, const psim_tuning* tuning);
 int psim_get_tuning(psim_ctx* ctx, psim_tuning* tuning);
 
+/* Differentiable calibration (no counterpart in the reference; SURVEY
+ * config 5).  theta = (k, location-type weights, age-band susceptibilities).
+ * w_l = w_by_type[type_l]; slot_of_type[type] = weight slot 0..7 of that type
+ * in the gradient (-1: not a parameter; NULL keeps the current table). */
+int psim_set_type_weights(psim_ctx* ctx, const float* w_by_type /*[256]*/, const int8_t* slot_of_type /*[256]*/);
+/* infection coefficient per replica */
+int psim_set_replica_k(psim_ctx* ctx, const double* k /*[replicas]*/);
+/* on != 0: while the steps run, accumulate sum_r weights[r] * d E_r / d theta,
+ * E_r = sum over the steps of min(1, p_i) of susceptible agents (the expected
+ * new infections given the sampled state), in FP64; weights NULL keeps them. */
+int psim_set_adjoint(psim_ctx* ctx, int on, const double* weights /*[replicas]*/);
+/* out[0] = d/dk, out[1..8] = d/dw of weight slots 0..7, out[9..24] = d/dsigma
+ * of age bands 0..15 */
+int psim_get_gradient(psim_ctx* ctx, double* out /*[25]*/, int reset);
+/* device copies of the whole mutable state (per-day checkpoints: the backward
+ * pass restores a day and recomputes its movement and draws) */
+int psim_checkpoint_save(psim_ctx* ctx, uint32_t slot);
+int psim_checkpoint_restore(psim_ctx* ctx, uint32_t slot);
+int psim_checkpoint_free(psim_ctx* ctx);
+int psim_checkpoint_bytes(psim_ctx* ctx, uint64_t* out);
+
 /* Accumulate the expected new infections (sum of infection probabilities of
  * susceptible agents, reported in psim_day_stats) during the steps. */
 int psim_set_tracking(psim_ctx* ctx, int expected);

@@ -40,6 +40,15 @@ struct psim_ctx {
     bool csr_fresh = false;      // counts of the current positions are built
     std::vector<DevStatsAcc> h_stats;
     std::vector<double> h_expected;
+    // adjoint
+    double* d_adj_weight = nullptr;
+    double* d_grad = nullptr;
+    int8_t* d_type_slot = nullptr;
+    float* d_w_by_type = nullptr;
+    // per-day checkpoints of the mutable state (device copies)
+    std::vector<std::pair<void*, size_t>> regions;
+    size_t checkpoint_bytes = 0;
+    std::vector<void*> checkpoints;
 };
 
 namespace {
@@ -452,6 +461,7 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     if ((rc = dalloc(c, &dl.qu_pending, L))) return bail(rc);
     if ((rc = dalloc(c, &dl.sfix, L * V))) return bail(rc);
     if ((rc = dalloc(c, &dl.hazard, L * V))) return bail(rc);
+    if ((rc = dalloc(c, &dl.hazard_x, L * V))) return bail(rc);
     if ((rc = dalloc(c, &dl.no_work_loc, L))) return bail(rc);
     if ((rc = dalloc(c, &dl.flags, L))) return bail(rc);
     const size_t tiles = (L + 2047) / 2048 + 1;
@@ -471,6 +481,34 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     if ((rc = dalloc(c, &k.clock, 1))) return bail(rc);
     if ((rc = dalloc(c, &k.err, 1))) return bail(rc);
     if ((rc = dalloc(c, &k.stats, R))) return bail(rc);
+    if ((rc = dalloc(c, &c->d_adj_weight, R))) return bail(rc);
+    if ((rc = dalloc(c, &c->d_grad, 32))) return bail(rc);
+    if ((rc = dalloc(c, &c->d_type_slot, 256))) return bail(rc);
+    if ((rc = dalloc(c, &c->d_w_by_type, 256))) return bail(rc);
+    {
+        std::vector<int8_t> none(256, (int8_t)-1);
+        if ((rc = dcopy_in(c, c->d_type_slot, none.data(), 256))) return bail(rc);
+    }
+    k.adj.on = 0;
+    k.adj.weight = c->d_adj_weight;
+    k.adj.grad = c->d_grad;
+    k.adj.type_slot = c->d_type_slot;
+    // the mutable state saved by a checkpoint
+    {
+        auto add = [&](void* ptr, size_t bytes) { c->regions.push_back({ptr, bytes}); c->checkpoint_bytes += bytes; };
+        DevAgents& a2 = k.a;
+        add(a2.location, 4 * N); add(a2.steps_until_move, 4 * N); add(a2.state, N); add(a2.days, 2 * N);
+        add(a2.variant, N); add(a2.infectious, 4 * N); add(a2.susceptible, 4 * N * V); add(a2.diagnosed, N);
+        add(a2.quarantined, N); add(a2.stayed_home, N); add(a2.no_work, N); add(a2.last_test, 4 * N);
+        add(a2.st_infected_ts, 4 * N); add(a2.st_infected_loc, 4 * N); add(a2.st_worst_ts, 4 * N);
+        add(a2.st_worst_end_ts, 4 * N); add(a2.st_diagnosed_ts, 4 * N); add(a2.st_quarantined_ts, 4 * N);
+        add(a2.st_quarantined_until, 4 * N); add(a2.st_days_in_quarantine, 4 * N); add(a2.st_hospitalized_ts, 4 * N);
+        add(a2.st_hospitalized_until, 4 * N); add(a2.st_immunization_ts, 4 * N); add(a2.st_recovered_ts, 4 * N);
+        add(a2.st_variant_mask, 4 * N); add(a2.st_immunization_count, N); add(a2.st_infected_count, N);
+        add(a2.st_worst_state, N);
+        add(dl.infectiousness, 4 * L); add(dl.open, L); add(dl.closed_until, 4 * L); add(dl.quarantine_until, 4 * L);
+        add(dr.variant_active, R * V); add(dr.expected, 8 * R);
+    }
     k.p = c->params;
     k.spd = c->spd;
     k.track_expected = 0;
@@ -504,6 +542,8 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
 int psim_destroy(psim_ctx* c) {
     if (!c) return 0;
     if (c->stream) cudaStreamSynchronize(c->stream);
+    for (void* p : c->checkpoints)
+        if (p) cudaFree(p);
     if (c->day_graph) cudaGraphExecDestroy(c->day_graph);
     for (void* p : c->allocs) cudaFree(p);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -575,6 +615,105 @@ int psim_get_tuning(psim_ctx* c, psim_tuning* t) {
     t->agg_slot = c->k.tune.agg_slot;
     t->blocks_per_sm = c->k.tune.blocks_per_sm;
     t->variant = c->k.tune.variant;
+    return 0;
+}
+
+int psim_set_type_weights(psim_ctx* c, const float* w_by_type, const int8_t* slot_of_type) {
+    if (!c || !c->uploaded || !w_by_type) return PSIM_ERR_ARG;
+    if (slot_of_type) {
+        for (int j = 0; j < 256; ++j)
+            if (slot_of_type[j] >= 8) return fail(c, PSIM_ERR_ARG, "weight slot must be < 8 (or -1)");
+        CK(cudaMemcpyAsync(c->d_type_slot, slot_of_type, 256, cudaMemcpyHostToDevice, c->stream));
+    }
+    CK(cudaMemcpyAsync(c->d_w_by_type, w_by_type, 256 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    launch_type_weights(c->k, c->d_w_by_type, c->stream);
+    c->launches += 1;
+    int rc = launch_check(c);
+    if (rc) return rc;
+    return check_device_err(c);
+}
+
+int psim_set_replica_k(psim_ctx* c, const double* k) {
+    if (!c || !k) return PSIM_ERR_ARG;
+    std::vector<float> kf(c->R);
+    for (uint32_t q = 0; q < c->R; ++q) {
+        c->rep_k[q] = k[q];
+        kf[q] = (float)k[q];
+    }
+    CK(cudaMemcpyAsync((void*)c->k.r.k_f, kf.data(), sizeof(float) * c->R, cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+int psim_set_adjoint(psim_ctx* c, int on, const double* weights) {
+    if (!c) return PSIM_ERR_ARG;
+    if (weights) {
+        CK(cudaMemcpyAsync(c->d_adj_weight, weights, sizeof(double) * c->R, cudaMemcpyHostToDevice, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+    }
+    const uint32_t o = on ? 1u : 0u;
+    if (o != c->k.adj.on) {
+        c->k.adj.on = o;
+        c->graph_dirty = true;
+    }
+    return 0;
+}
+
+int psim_get_gradient(psim_ctx* c, double* out, int reset) {
+    if (!c || !out) return PSIM_ERR_ARG;
+    CK(cudaMemcpyAsync(out, c->d_grad, sizeof(double) * GRAD_N, cudaMemcpyDeviceToHost, c->stream));
+    if (reset) CK(cudaMemsetAsync(c->d_grad, 0, sizeof(double) * 32, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+int psim_checkpoint_save(psim_ctx* c, uint32_t slot) {
+    if (!c || !c->uploaded) return PSIM_ERR_STATE;
+    if (slot > 100000) return fail(c, PSIM_ERR_ARG, "checkpoint slot out of range");
+    if (c->checkpoints.size() <= slot) c->checkpoints.resize(slot + 1, nullptr);
+    if (!c->checkpoints[slot]) {
+        void* p = nullptr;
+        cudaError_t e = cudaMalloc(&p, c->checkpoint_bytes);
+        if (e != cudaSuccess) return fail(c, PSIM_ERR_ALLOC, std::string("checkpoint: ") + cudaGetErrorString(e));
+        c->checkpoints[slot] = p;
+    }
+    char* dst = (char*)c->checkpoints[slot];
+    for (auto& r : c->regions) {
+        CK(cudaMemcpyAsync(dst, r.first, r.second, cudaMemcpyDeviceToDevice, c->stream));
+        dst += r.second;
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+int psim_checkpoint_restore(psim_ctx* c, uint32_t slot) {
+    if (!c || !c->uploaded) return PSIM_ERR_STATE;
+    if (slot >= c->checkpoints.size() || !c->checkpoints[slot]) return fail(c, PSIM_ERR_ARG, "no such checkpoint");
+    const char* src = (const char*)c->checkpoints[slot];
+    for (auto& r : c->regions) {
+        CK(cudaMemcpyAsync(r.first, src, r.second, cudaMemcpyDeviceToDevice, c->stream));
+        src += r.second;
+    }
+    CK(cudaStreamSynchronize(c->stream));
+    c->csr_fresh = false;
+    return 0;
+}
+
+int psim_checkpoint_free(psim_ctx* c) {
+    if (!c) return PSIM_ERR_ARG;
+    cudaStreamSynchronize(c->stream);
+    for (void*& p : c->checkpoints)
+        if (p) {
+            cudaFree(p);
+            p = nullptr;
+        }
+    c->checkpoints.clear();
+    return 0;
+}
+
+int psim_checkpoint_bytes(psim_ctx* c, uint64_t* out) {
+    if (!c || !out) return PSIM_ERR_ARG;
+    *out = c->checkpoint_bytes;
     return 0;
 }
 

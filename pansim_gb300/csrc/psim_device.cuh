@@ -110,6 +110,7 @@ struct DevLocs {
     uint32_t* qu_pending;         // quarantine writes of the running step
     unsigned long long* sfix;     // [V][n] fixed-point infectiousness sums
     float* hazard;                // [V][n] infection ratio of the last step
+    float* hazard_x;              // [V][n] its argument x = k*S/n*w*season*dt (adjoint mode)
     uint32_t* no_work_loc;
     uint8_t* flags;               // testing flags
     uint32_t* tile_sums;          // per-tile sums of the histogram (scan, first pass)
@@ -148,6 +149,20 @@ struct DevTune {
     uint32_t variant;        // register cap of the fused step kernel: 0 = 64, 1 = 40, 2 = 32 registers
 };
 
+// Adjoint accumulation (gradient of the expected new infections with respect
+// to k, the location-type weights and the age-band susceptibilities)
+constexpr int GRAD_K = 0;
+constexpr int GRAD_W = 1;       // 8 location-type slots
+constexpr int GRAD_SIGMA = 9;   // 16 age bands
+constexpr int GRAD_N = 25;
+struct DevAdjoint {
+    uint32_t on;
+    uint32_t pad;
+    const double* weight;         // [R] dL/dE of the replica for the running day
+    double* grad;                 // [GRAD_N] accumulated sum over replicas
+    const int8_t* type_slot;      // [256] location type -> weight slot (-1: none)
+};
+
 struct KArgs {
     DevModel m;
     DevAgents a;
@@ -160,6 +175,7 @@ struct KArgs {
     uint32_t spd;         // steps per day
     uint32_t track_expected;
     DevTune tune;
+    DevAdjoint adj;
 };
 
 // raw counter slots of DevStatsAcc::c
@@ -185,6 +201,7 @@ void launch_stats(const KArgs& k, uint32_t t, cudaStream_t s);
 void launch_plan(const KArgs& k, uint32_t t, cudaStream_t s);
 void launch_flag_hcw(const KArgs& k, cudaStream_t s);
 void launch_bounded_wait_probe(const KArgs& k, uint32_t iters, cudaStream_t s);
+void launch_type_weights(const KArgs& k, const float* w_by_type, cudaStream_t s);
 uint64_t launches_per_step(int quarantine);
 
 }  // namespace psim

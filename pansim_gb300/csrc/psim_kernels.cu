@@ -463,7 +463,25 @@ __device__ __forceinline__ void store_slot(const KArgs& k, uint32_t pos, uint32_
 // Infection draws of agent i at location loc with hazard h0 of variant 0
 // (LocationsList::infectAgents, locationList.h:233-310; DynamicPPState::gotInfected,
 // dynamicPPState.cpp:235-244).  Returns the sum of min(1, p) over the draws.
-__device__ __forceinline__ double draw_agent(const KArgs& k, uint32_t i, uint32_t loc, uint32_t t, float h0) {
+// d p / d theta of one draw (p = r * s * sigma_band, r = 1 - exp(-x),
+// x = k * S/n * w * season * dt), weighted by the replica's dL/dE, added to the
+// block's FP64 accumulators
+__device__ __noinline__ void adjoint_terms(const KArgs& k, uint32_t i, uint32_t loc, uint32_t v, uint32_t rep, float r,
+                                           float su, float s_eff, double* s_grad) {
+    const double g = k.adj.weight[rep];
+    if (g == 0.0) return;
+    const double x = (double)k.l.hazard_x[(size_t)v * k.l.n + loc];
+    const double dpdx = (double)s_eff * (1.0 - (double)r);
+    const double kf = (double)k.r.k_f[rep];
+    if (kf != 0.0) atomicAdd(&s_grad[GRAD_K], g * dpdx * x / kf);
+    const int slot = k.adj.type_slot[k.l.type[loc]];
+    const double w = (double)k.l.infectiousness[loc];
+    if (slot >= 0 && w != 0.0) atomicAdd(&s_grad[GRAD_W + slot], g * dpdx * x / w);
+    atomicAdd(&s_grad[GRAD_SIGMA + k.a.band[i]], g * (double)r * (double)su);
+}
+
+__device__ __forceinline__ double draw_agent(const KArgs& k, uint32_t i, uint32_t loc, uint32_t t, float h0,
+                                             double* s_grad) {
     const uint32_t N = k.a.n, L = k.l.n, V = k.m.n_variants;
     const uint32_t rep = k.a.rep[i];
     double term_sum = 0.0;
@@ -476,6 +494,7 @@ __device__ __forceinline__ double draw_agent(const KArgs& k, uint32_t i, uint32_
         if (!(s_eff > 0.0f)) continue;
         const float pf = h * s_eff;
         term_sum += pf < 1.0f ? (double)pf : 1.0;
+        if (k.adj.on && pf < 1.0f) adjoint_terms(k, i, loc, v, rep, h, su, s_eff, s_grad);
         const double U = psim_u01_once(k.r.seed[rep], i - k.r.agent_off[rep], t, PSIM_PHASE_INFECT + v);
         if (U < (double)pf) {
             k.a.state[i] = (int8_t)k.m.first_infected;
@@ -491,6 +510,19 @@ __device__ __forceinline__ double draw_agent(const KArgs& k, uint32_t i, uint32_
         }
     }
     return term_sum;
+}
+
+__device__ __forceinline__ void grad_begin(const KArgs& k, double* s_grad) {
+    if (!k.adj.on) return;
+    if (threadIdx.x < GRAD_N) s_grad[threadIdx.x] = 0.0;
+    __syncthreads();
+}
+
+// one global atomic per block and parameter
+__device__ __forceinline__ void grad_end(const KArgs& k, double* s_grad) {
+    if (!k.adj.on) return;
+    __syncthreads();
+    if (threadIdx.x < GRAD_N && s_grad[threadIdx.x] != 0.0) atomicAdd(&k.adj.grad[threadIdx.x], s_grad[threadIdx.x]);
 }
 
 // expected-infection accumulation: one atomic per replica present in the warp
@@ -642,13 +674,14 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, int with_hazard,
                 if (l < L) {
                     const size_t idx = (size_t)v * L + l;
                     const long long fix = (long long)k.l.sfix[idx];
-                    float h = 0.0f;
+                    float h = 0.0f, x = 0.0f;
                     if (fix != 0) {
                         const uint32_t rep = k.l.rep[l];
-                        h = psim_hazard(fix, c[q], k.r.k_f[rep], k.l.infectiousness[l], season, dt);
+                        h = psim_hazard_x(fix, c[q], k.r.k_f[rep], k.l.infectiousness[l], season, dt, &x);
                         k.l.sfix[idx] = 0ull;
                     }
                     k.l.hazard[idx] = h;
+                    if (k.adj.on) k.l.hazard_x[idx] = x;
                 }
             }
         }
@@ -670,6 +703,8 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, int with_hazard,
 
 // CSR scatter and/or infection draw of one step.
 __global__ void __launch_bounds__(256) k_scatter_draw(KArgs k, uint32_t step, int scatter, int draw) {
+    __shared__ double s_grad[GRAD_N];
+    grad_begin(k, s_grad);
     const uint32_t N = k.a.n, L = k.l.n;
     const uint32_t t = k.clock->t0 + step;
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -684,9 +719,10 @@ __global__ void __launch_bounds__(256) k_scatter_draw(KArgs k, uint32_t step, in
             const uint32_t pos = take_slot(k, ok, loc);
             if (ok) store_slot(k, pos, i);
         }
-        if (ok && draw && (h0 > 0.0f || k.m.n_variants > 1)) term = draw_agent(k, i, loc, t, h0);
+        if (ok && draw && (h0 > 0.0f || k.m.n_variants > 1)) term = draw_agent(k, i, loc, t, h0, s_grad);
         if (k.track_expected) add_expected(k, act, i, term);
     }
+    grad_end(k, s_grad);
 }
 
 // Scatter + draw of step `step` fused with the movement and histogram of
@@ -695,6 +731,8 @@ __global__ void __launch_bounds__(256) k_scatter_draw(KArgs k, uint32_t step, in
 // back to back in one pass; used inside the day graph.
 template <int MINB>
 __global__ void __launch_bounds__(256, MINB) k_step_fused(KArgs k, uint32_t step) {
+    __shared__ double s_grad[GRAD_N];
+    grad_begin(k, s_grad);
     const uint32_t N = k.a.n, L = k.l.n;
     const uint32_t t = k.clock->t0 + step;
     const StepClock c = step_clock(k, step + 1);
@@ -714,7 +752,7 @@ __global__ void __launch_bounds__(256, MINB) k_step_fused(KArgs k, uint32_t step
         if (ok) {
             store_slot(k, pos, i);
             if (h0 > 0.0f || k.m.n_variants > 1) {
-                term = draw_agent(k, i, loc0, t, h0);
+                term = draw_agent(k, i, loc0, t, h0, s_grad);
                 inf = k.a.infectious[i];
             }
         }
@@ -726,6 +764,7 @@ __global__ void __launch_bounds__(256, MINB) k_step_fused(KArgs k, uint32_t step
         if (k.track_expected) add_expected(k, act, i, term);
         count_agent(k, act, loc, inf, var);
     }
+    grad_end(k, s_grad);
 }
 
 // Canonical CSR order (ascending agent id inside a location, the output of
@@ -1208,6 +1247,12 @@ __global__ void k_flag_hcw(KArgs k) {
     }
 }
 
+// w_l = w of the location's type (psim_set_type_weights)
+__global__ void k_type_weights(KArgs k, const float* w_by_type) {
+    for (uint32_t l = blockIdx.x * blockDim.x + threadIdx.x; l < k.l.n; l += gridDim.x * blockDim.x)
+        k.l.infectiousness[l] = w_by_type[k.l.type[l]];
+}
+
 // A wait on a flag that nothing sets, bounded by `iters`: reports
 // ERR_TEST_WAIT and returns.  Exercises the bounded-wait error path.
 __global__ void k_bounded_wait_probe(KArgs k, uint32_t iters) {
@@ -1325,6 +1370,9 @@ void launch_plan(const KArgs& k, uint32_t t, cudaStream_t s) {
     k_plan_nowork_set<<<grid_for(k.a.n, 8), 256, 0, s>>>(k, t);
 }
 void launch_flag_hcw(const KArgs& k, cudaStream_t s) { k_flag_hcw<<<grid_for(k.a.n, 8), 256, 0, s>>>(k); }
+void launch_type_weights(const KArgs& k, const float* w_by_type, cudaStream_t s) {
+    k_type_weights<<<grid_for(k.l.n, 8), 256, 0, s>>>(k, w_by_type);
+}
 void launch_bounded_wait_probe(const KArgs& k, uint32_t iters, cudaStream_t s) {
     k_bounded_wait_probe<<<1, 32, 0, s>>>(k, iters);
 }

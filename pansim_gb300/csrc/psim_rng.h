@@ -278,8 +278,11 @@ PSIM_HD float psim_one_minus_expf(float x) {
 // The infection ratio of a location (infectionPolicies.h:523-546):
 // r = 1 - exp(-k * (S / n) * w * season * dt) with S the exact fixed-point
 // sum, every step one IEEE single-precision operation.
-PSIM_HD float psim_hazard(long long fix, unsigned n, float k_f, float w, float season, unsigned dt) {
-    if (fix == 0 || n == 0) return 0.0f;
+PSIM_HD float psim_hazard_x(long long fix, unsigned n, float k_f, float w, float season, unsigned dt, float* x_out) {
+    if (fix == 0 || n == 0) {
+        *x_out = 0.0f;
+        return 0.0f;
+    }
     float S = (float)fix;
     S = S * 0x1p-40f;
     float x = S / (float)n;
@@ -287,7 +290,13 @@ PSIM_HD float psim_hazard(long long fix, unsigned n, float k_f, float w, float s
     x = x * w;
     x = x * season;
     x = x * (float)dt;
+    *x_out = x;
     return psim_one_minus_expf(x);
+}
+
+PSIM_HD float psim_hazard(long long fix, unsigned n, float k_f, float w, float season, unsigned dt) {
+    float x;
+    return psim_hazard_x(fix, n, k_f, w, season, dt, &x);
 }
 
 // Fixed-point scale for per-location infectiousness sums: every FP32 value

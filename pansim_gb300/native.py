@@ -62,6 +62,14 @@ def lib(auto_build=True):
         L.psim_time_step_kernels.argtypes = [P, U32, P]
         L.psim_set_tuning.argtypes = [P, P]
         L.psim_csr_build_noalloc.argtypes = [P, U32, U32, P, P, P]
+        L.psim_set_type_weights.argtypes = [P, P, P]
+        L.psim_set_replica_k.argtypes = [P, P]
+        L.psim_set_adjoint.argtypes = [P, I, P]
+        L.psim_get_gradient.argtypes = [P, P, I]
+        L.psim_checkpoint_save.argtypes = [P, U32]
+        L.psim_checkpoint_restore.argtypes = [P, U32]
+        L.psim_checkpoint_free.argtypes = [P]
+        L.psim_checkpoint_bytes.argtypes = [P, C.POINTER(C.c_uint64)]
         L.psim_noalloc_last_error.restype = C.c_char_p
         L.psim_get_tuning.argtypes = [P, P]
         _lib = L
@@ -217,6 +225,40 @@ class GpuSim:
         t = cabi.PsimTuning()
         self._ck(lib().psim_get_tuning(self.h, C.byref(t)), "get_tuning")
         return dict(agg_count=t.agg_count, agg_slot=t.agg_slot, blocks_per_sm=t.blocks_per_sm, variant=t.variant)
+
+    # differentiable calibration
+    def set_type_weights(self, w_by_type, slot_of_type=None):
+        w = np.ascontiguousarray(w_by_type, np.float32)
+        assert w.shape == (256,)
+        sl = None if slot_of_type is None else np.ascontiguousarray(slot_of_type, np.int8)
+        self._ck(lib().psim_set_type_weights(self.h, _p(w), _p(sl)), "set_type_weights")
+
+    def set_replica_k(self, k):
+        kk = np.ascontiguousarray(k, np.float64)
+        self._ck(lib().psim_set_replica_k(self.h, _p(kk)), "set_replica_k")
+
+    def set_adjoint(self, on, weights=None):
+        w = None if weights is None else np.ascontiguousarray(weights, np.float64)
+        self._ck(lib().psim_set_adjoint(self.h, 1 if on else 0, _p(w)), "set_adjoint")
+
+    def gradient(self, reset=True):
+        out = np.zeros(25, np.float64)
+        self._ck(lib().psim_get_gradient(self.h, _p(out), 1 if reset else 0), "get_gradient")
+        return out
+
+    def checkpoint_save(self, slot):
+        self._ck(lib().psim_checkpoint_save(self.h, slot), "checkpoint_save")
+
+    def checkpoint_restore(self, slot):
+        self._ck(lib().psim_checkpoint_restore(self.h, slot), "checkpoint_restore")
+
+    def checkpoint_free(self):
+        self._ck(lib().psim_checkpoint_free(self.h), "checkpoint_free")
+
+    def checkpoint_bytes(self):
+        n = C.c_uint64(0)
+        lib().psim_checkpoint_bytes(self.h, C.byref(n))
+        return n.value
 
     def bounded_wait_selftest(self, iters):
         return lib().psim_bounded_wait_selftest(self.h, iters)
