@@ -189,6 +189,88 @@ def run_reference(args, ws, rank):
     return 0
 
 
+def run_batched(args):
+    """64 replicas, agent counts log-uniform on [250k, 2M], k log-uniform on
+    [1e-4, 1e-3], independent seeds: one context over the concatenation vs the
+    same 64 runs one after another (same days, same per-replica results)."""
+    import numpy as np
+    import torch
+    from pansim_gb300 import autotune, native, snapshot as snp, synth
+    n, ks, seeds = synth.batch_sizes(64)
+    scale = args.scale
+    n = np.maximum((n * scale).astype(np.int64), 1000)
+    parts = [synth.make_snapshot(int(n[r]), int(n[r]) // 4, seed=int(seeds[r]), pop_seed=0x5EED0004 + r, k=float(ks[r]))
+             for r in range(len(n))]
+    for r, p in enumerate(parts):
+        p.reps["seed"][:] = seeds[r]
+        p.reps["k"][:] = ks[r]
+    batch = snp.concat(parts, seeds, ks)
+    days = args.days
+    g = native.GpuSim(batch)
+    g.run_day(0)
+    best, _ = autotune.autotune(g, 1)
+    g.run_day(1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    rows_b = []
+    for d in range(2, 2 + days):
+        rows_b.append([list(x.v)[: x.n] for x in g.run_day(d)])
+    tb = time.perf_counter() - t0
+    launches_b = g.launch_count()
+    g.close()
+    del g
+    ts = 0.0
+    same = True
+    for r, p in enumerate(parts):
+        gs = native.GpuSim(p)
+        gs.set_tuning(**best)
+        for d in range(2):
+            gs.run_day(d)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for j, d in enumerate(range(2, 2 + days)):
+            row = [list(x.v)[: x.n] for x in gs.run_day(d)][0]
+            same = same and row == rows_b[j][r]
+        ts += time.perf_counter() - t0
+        gs.close()
+    tot = int(n.sum()) * 144 * days
+    line = {"metric": "64-replica batched vs sequential", "value": ts / tb, "unit": "x", "higher_is_better": True,
+            "batched_agent_steps_per_s": tot / tb, "sequential_agent_steps_per_s": tot / ts,
+            "batched_s": tb, "sequential_s": ts, "days": days, "replicas": int(len(n)), "agents_total": int(n.sum()),
+            "identical_per_replica_statistics": bool(same), "tuning": best, "data": "synthetic",
+            "config": {"workload": "64 replicas, agents log-uniform 250k-2M x%g, k log-uniform 1e-4..1e-3" % scale}}
+    print(json.dumps(line, default=float))
+
+
+def run_adjoint(args):
+    """16 replicas x 1M agents, 28 days: forward with per-day checkpoints,
+    backward replay with the adjoint accumulation."""
+    import numpy as np
+    import torch
+    from pansim_gb300 import adjoint, snapshot as snp, synth
+    R, n = 16, int(1_000_000 * args.scale)
+    parts = [synth.make_snapshot(n, n // 4, seed=100 + r, pop_seed=0x5EED0005 + r) for r in range(R)]
+    batch = snp.concat(parts, [100 + r for r in range(R)], [3.74e-4] * R)
+    days = args.days
+    runner = adjoint.CalibrationRunner(batch, days)
+    theta = adjoint.theta_of(batch)
+    runner.set_theta(theta)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    E = runner.forward()
+    tf = time.perf_counter() - t0
+    target = E.mean(axis=0) * 0.9
+    gE = 2.0 * (E - target[None, :])
+    t0 = time.perf_counter()
+    grad = runner.backward(gE)
+    tbw = time.perf_counter() - t0
+    line = {"metric": "adjoint grad time", "value": tbw, "unit": "s", "higher_is_better": False,
+            "forward_s": tf, "backward_s": tbw, "replicas": R, "agents_per_replica": n, "days": days,
+            "checkpoint_bytes_per_day": runner.g.checkpoint_bytes(), "grad_norm": float(np.linalg.norm(grad)),
+            "data": "synthetic", "config": {"workload": "16 replicas x 1M agents x %d days, theta = k, 5 type weights, 9 band susceptibilities" % days}}
+    print(json.dumps(line, default=float))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -197,7 +279,14 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="step", choices=["step", "batched", "adjoint"])
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--days", type=int, default=2)
     args = ap.parse_args()
+    if args.workload == "batched":
+        return run_batched(args) or 0
+    if args.workload == "adjoint":
+        return run_adjoint(args) or 0
     if args.warmup < 3:
         args.warmup = 3
     ws, rank, local = dist_env()

@@ -216,7 +216,8 @@ typedef struct psim_tuning {
     uint32_t agg_count;      /* warp-aggregated per-location count reductions */
     uint32_t agg_slot;       /* warp-aggregated CSR slot atomics */
     uint32_t blocks_per_sm;  /* 256-thread blocks per SM of the per-agent kernels; 0 = occupancy */
-    uint32_t variant;        /* register cap of the fused step kernel: 0 = 64, 1 = 40, 2 = 32 */
+    uint32_t variant;        /* fused step kernel: 0/1/2 = one kernel capped at 64/40/32
+                                registers, 3 = hot/cold split */
 } psim_tuning;
 
 typedef struct psim_ctx psim_ctx;
@@ -281,6 +282,7 @@ int psim_get_gradient(psim_ctx* ctx, double* out /*[25]*/, int reset);
  * pass restores a day and recomputes its movement and draws) */
 int psim_checkpoint_save(psim_ctx* ctx, uint32_t slot);
 int psim_checkpoint_restore(psim_ctx* ctx, uint32_t slot);
+int psim_checkpoint_drop(psim_ctx* ctx, uint32_t slot);
 int psim_checkpoint_free(psim_ctx* ctx);
 int psim_checkpoint_bytes(psim_ctx* ctx, uint64_t* out);
 

@@ -15,15 +15,22 @@ DEFAULT_GRID = [0, 4, 8, 16]
 
 
 def candidates(grid=None):
-    """variant: register cap of the fused kernel (64 / 40 / 32 registers);
+    """variant: register cap of the fused kernel (64 / 40 / 32 registers) or
+    3 = hot/cold split;
     blocks_per_sm 0 = one occupancy wave of that variant."""
-    for variant, agg_count, agg_slot, bps in itertools.product([0, 1, 2], [1, 0], [1, 0], grid or DEFAULT_GRID):
+    for variant, agg_count, agg_slot, bps in itertools.product([0, 1, 2, 3], [1, 0], [1, 0], grid or DEFAULT_GRID):
         yield dict(agg_count=agg_count, agg_slot=agg_slot, blocks_per_sm=bps, variant=variant)
 
 
-def autotune(sim, day, reps=3, grid=None, verbose=False):
-    """Tries the candidates on the steps of `day` (the state advances by those
-    steps); returns (best tuning, table of (tuning, step ms))."""
+TUNE_SLOT = 1 << 16
+
+
+def autotune(sim, day, reps=3, grid=None, verbose=False, keep_state=True):
+    """Tries the candidates on steps of `day`; returns (best tuning, table of
+    (tuning, step ms)).  With keep_state the simulation state is saved to a
+    checkpoint first and restored afterwards, so tuning leaves no trace."""
+    if keep_state:
+        sim.checkpoint_save(TUNE_SLOT)
     table = []
     t = day * sim.snap.steps_per_day
     for cand in candidates(grid):
@@ -40,4 +47,7 @@ def autotune(sim, day, reps=3, grid=None, verbose=False):
             print("tune", cand, "%.2f us" % (1000 * table[-1][1]))
     best = min(table, key=lambda x: x[1])[0]
     sim.set_tuning(**best)
+    if keep_state:
+        sim.checkpoint_restore(TUNE_SLOT)
+        sim.checkpoint_drop(TUNE_SLOT)
     return best, table

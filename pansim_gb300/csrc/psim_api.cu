@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <string>
 #include <vector>
 
@@ -48,7 +49,7 @@ struct psim_ctx {
     // per-day checkpoints of the mutable state (device copies)
     std::vector<std::pair<void*, size_t>> regions;
     size_t checkpoint_bytes = 0;
-    std::vector<void*> checkpoints;
+    std::map<uint32_t, void*> checkpoints;
 };
 
 namespace {
@@ -266,7 +267,7 @@ int capture_day_graph(psim_ctx* c) {
     e = cudaGraphInstantiate(&c->day_graph, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(c, PSIM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
-    c->graph_kernels = 3ull * c->spd + 1;
+    c->graph_kernels = (2ull + (uint64_t)step_fused_kernels(c->k)) * c->spd + 1;
     c->graph_dirty = false;
     return 0;
 }
@@ -438,6 +439,7 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     AL(st_quarantined_ts, N) AL(st_quarantined_until, N) AL(st_days_in_quarantine, N) AL(st_hospitalized_ts, N)
     AL(st_hospitalized_until, N) AL(st_immunization_ts, N) AL(st_recovered_ts, N) AL(st_variant_mask, N)
     AL(st_immunization_count, N) AL(st_infected_count, N) AL(st_worst_state, N) AL(hcw, N) AL(rank, N)
+    AL(worklist, N) AL(work_count, 1)
 #undef AL
     // locations
     DevLocs& dl = k.l;
@@ -542,8 +544,8 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
 int psim_destroy(psim_ctx* c) {
     if (!c) return 0;
     if (c->stream) cudaStreamSynchronize(c->stream);
-    for (void* p : c->checkpoints)
-        if (p) cudaFree(p);
+    for (auto& kv : c->checkpoints)
+        if (kv.second) cudaFree(kv.second);
     if (c->day_graph) cudaGraphExecDestroy(c->day_graph);
     for (void* p : c->allocs) cudaFree(p);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -603,7 +605,7 @@ int psim_set_tuning(psim_ctx* c, const psim_tuning* t) {
     c->k.tune.agg_count = t->agg_count ? 1u : 0u;
     c->k.tune.agg_slot = t->agg_slot ? 1u : 0u;
     c->k.tune.blocks_per_sm = t->blocks_per_sm;
-    if (t->variant > 2) return fail(c, PSIM_ERR_ARG, "variant out of range");
+    if (t->variant > 3) return fail(c, PSIM_ERR_ARG, "variant out of range");
     c->k.tune.variant = t->variant;
     c->graph_dirty = true;
     return 0;
@@ -669,9 +671,7 @@ int psim_get_gradient(psim_ctx* c, double* out, int reset) {
 
 int psim_checkpoint_save(psim_ctx* c, uint32_t slot) {
     if (!c || !c->uploaded) return PSIM_ERR_STATE;
-    if (slot > 100000) return fail(c, PSIM_ERR_ARG, "checkpoint slot out of range");
-    if (c->checkpoints.size() <= slot) c->checkpoints.resize(slot + 1, nullptr);
-    if (!c->checkpoints[slot]) {
+    if (!c->checkpoints.count(slot) || !c->checkpoints[slot]) {
         void* p = nullptr;
         cudaError_t e = cudaMalloc(&p, c->checkpoint_bytes);
         if (e != cudaSuccess) return fail(c, PSIM_ERR_ALLOC, std::string("checkpoint: ") + cudaGetErrorString(e));
@@ -688,8 +688,9 @@ int psim_checkpoint_save(psim_ctx* c, uint32_t slot) {
 
 int psim_checkpoint_restore(psim_ctx* c, uint32_t slot) {
     if (!c || !c->uploaded) return PSIM_ERR_STATE;
-    if (slot >= c->checkpoints.size() || !c->checkpoints[slot]) return fail(c, PSIM_ERR_ARG, "no such checkpoint");
-    const char* src = (const char*)c->checkpoints[slot];
+    auto it = c->checkpoints.find(slot);
+    if (it == c->checkpoints.end() || !it->second) return fail(c, PSIM_ERR_ARG, "no such checkpoint");
+    const char* src = (const char*)it->second;
     for (auto& r : c->regions) {
         CK(cudaMemcpyAsync(r.first, src, r.second, cudaMemcpyDeviceToDevice, c->stream));
         src += r.second;
@@ -702,12 +703,19 @@ int psim_checkpoint_restore(psim_ctx* c, uint32_t slot) {
 int psim_checkpoint_free(psim_ctx* c) {
     if (!c) return PSIM_ERR_ARG;
     cudaStreamSynchronize(c->stream);
-    for (void*& p : c->checkpoints)
-        if (p) {
-            cudaFree(p);
-            p = nullptr;
-        }
+    for (auto& kv : c->checkpoints)
+        if (kv.second) cudaFree(kv.second);
     c->checkpoints.clear();
+    return 0;
+}
+
+int psim_checkpoint_drop(psim_ctx* c, uint32_t slot) {
+    if (!c) return PSIM_ERR_ARG;
+    auto it = c->checkpoints.find(slot);
+    if (it == c->checkpoints.end()) return 0;
+    cudaStreamSynchronize(c->stream);
+    if (it->second) cudaFree(it->second);
+    c->checkpoints.erase(it);
     return 0;
 }
 
@@ -931,7 +939,7 @@ int psim_time_step_kernels(psim_ctx* c, uint32_t t, float* ms) {
     CK(cudaEventRecord(ev[3], c->stream));
     launch_scan(c->k, step + 1, 1, merge_q, c->stream);
     launch_scatter_draw(c->k, step + 1, 1, 1, c->stream);
-    c->launches += 7;
+    c->launches += 6 + (uint64_t)step_fused_kernels(c->k);
     CK(cudaStreamSynchronize(c->stream));
     for (int j = 0; j < 3; ++j) CK(cudaEventElapsedTime(&ms[j], ev[j], ev[j + 1]));
     for (int j = 0; j < 4; ++j) cudaEventDestroy(ev[j]);

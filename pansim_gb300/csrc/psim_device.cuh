@@ -88,6 +88,8 @@ struct DevAgents {
     int8_t* st_worst_state;
     uint8_t* hcw;                 // healthcare worker flag
     uint32_t* rank;               // scratch of the canonical CSR ordering
+    uint32_t* worklist;           // agents queued for the cold half of a step (hot/cold variant)
+    uint32_t* work_count;         // their number
 };
 
 struct DevLocs {
@@ -146,7 +148,8 @@ struct DevTune {
     uint32_t agg_count;      // warp-aggregate the per-location count reductions
     uint32_t agg_slot;       // warp-aggregate the CSR slot atomics
     uint32_t blocks_per_sm;  // grid of the per-agent kernels (0 = one occupancy wave)
-    uint32_t variant;        // register cap of the fused step kernel: 0 = 64, 1 = 40, 2 = 32 registers
+    uint32_t variant;        // fused step kernel: 0/1/2 = one kernel capped at 64/40/32 registers,
+                             // 3 = hot/cold split (lean kernel + queued cold agents)
 };
 
 // Adjoint accumulation (gradient of the expected new infections with respect
@@ -194,6 +197,7 @@ void launch_scan(const KArgs& k, uint32_t step_in_day, int with_hazard, int merg
 void launch_scatter_draw(const KArgs& k, uint32_t step_in_day, int scatter, int draw, cudaStream_t s);
 void launch_offsets(const KArgs& k, cudaStream_t s);
 void launch_step_fused(const KArgs& k, uint32_t step_in_day, cudaStream_t s);
+int step_fused_kernels(const KArgs& k);
 void launch_canonical_csr(const KArgs& k, cudaStream_t s);
 void launch_progress(const KArgs& k, uint32_t t, cudaStream_t s);
 void launch_test(const KArgs& k, uint32_t t, cudaStream_t s);

@@ -628,6 +628,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, int with_hazard,
     const uint32_t tile = blockIdx.x;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t wbase = tile * SCAN_TILE + (uint32_t)warp * (32 * SCAN_ITEMS);
+    if (tile == 0 && threadIdx.x == 0) *k.a.work_count = 0u;  // queue of the next step's cold agents
     uint32_t c[SCAN_ITEMS], ex[SCAN_ITEMS];
 #pragma unroll
     for (int q = 0; q < SCAN_ITEMS; ++q) {
@@ -757,6 +758,85 @@ __global__ void __launch_bounds__(256, MINB) k_step_fused(KArgs k, uint32_t step
             }
         }
         if (act) {
+            move_agent(k, i, c, s);
+            loc = (c.curfew_now || s == 0) ? k.a.location[i] : loc0;
+            if (inf > 0.0f) var = k.a.variant[i];
+        }
+        if (k.track_expected) add_expected(k, act, i, term);
+        count_agent(k, act, loc, inf, var);
+    }
+    grad_end(k, s_grad);
+}
+
+// Hot/cold form of k_step_fused.  The hot kernel does, for every agent, the
+// CSR slot of step `step`; agents that neither draw (no hazard at their
+// location) nor move at step + 1 (countdown > 0, no curfew transition) also
+// count down and join the histogram here.  The others are queued (warp-
+// aggregated append) for k_step_cold, which runs their draw, movement and
+// histogram with the full register budget.  Per agent the operations and
+// their order are those of k_step_fused.
+__global__ void __launch_bounds__(256, 8) k_step_hot(KArgs k, uint32_t step) {
+    const uint32_t N = k.a.n, L = k.l.n;
+    const uint32_t dt = k.p.time_step;
+    const uint32_t minutes = (step + 1) * dt;
+    const bool curfew_now = k.p.enable_curfew && k.p.curfew_begin == minutes / dt;
+    const bool multi = k.m.n_variants > 1;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < N; base += stride) {
+        const uint32_t i = base + threadIdx.x;
+        const bool act = i < N;
+        const uint32_t loc0 = act ? k.a.location[i] : NONE;
+        const uint32_t s = act ? k.a.steps_until_move[i] : 0u;
+        const float inf = act ? k.a.infectious[i] : 0.0f;
+        const bool ok = act && loc0 < L;
+        const float h0 = ok ? k.l.hazard[loc0] : 0.0f;
+        const uint32_t pos = take_slot(k, ok, loc0);
+        if (ok) store_slot(k, pos, i);
+        const bool cold = act && (curfew_now || s == 0 || h0 > 0.0f || multi || !ok);
+        const bool hot = act && !cold;
+        if (hot) k.a.steps_until_move[i] = s - 1;
+        // queue the cold agents
+        const unsigned cm = __ballot_sync(0xffffffffu, cold);
+        if (cm) {
+            const int lane = threadIdx.x & 31;
+            uint32_t basew = 0;
+            if (lane == __ffs(cm) - 1) basew = atomicAdd(k.a.work_count, (uint32_t)__popc(cm));
+            basew = __shfl_sync(0xffffffffu, basew, __ffs(cm) - 1);
+            if (cold) k.a.worklist[basew + __popc(cm & lanemask_lt())] = i;
+        }
+        uint32_t var = 0;
+        if (hot && inf > 0.0f) var = k.a.variant[i];
+        count_agent(k, hot, loc0, inf, var);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_step_cold(KArgs k, uint32_t step) {
+    __shared__ double s_grad[GRAD_N];
+    grad_begin(k, s_grad);
+    const uint32_t L = k.l.n;
+    const uint32_t t = k.clock->t0 + step;
+    const StepClock c = step_clock(k, step + 1);
+    const uint32_t n = *((volatile uint32_t*)k.a.work_count);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t trips = (n + stride - 1) / stride;  // uniform per block (grid-wide bound)
+    for (uint32_t it = 0; it < trips; ++it) {
+        const uint32_t j = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        const bool act = j < n;
+        const uint32_t i = act ? k.a.worklist[j] : 0u;
+        double term = 0.0;
+        uint32_t loc = NONE, var = 0;
+        float inf = 0.0f;
+        if (act) {
+            const uint32_t loc0 = k.a.location[i];
+            const uint32_t s = k.a.steps_until_move[i];
+            inf = k.a.infectious[i];
+            if (loc0 < L) {
+                const float h0 = k.l.hazard[loc0];
+                if (h0 > 0.0f || k.m.n_variants > 1) {
+                    term = draw_agent(k, i, loc0, t, h0, s_grad);
+                    inf = k.a.infectious[i];
+                }
+            }
             move_agent(k, i, c, s);
             loc = (c.curfew_now || s == 0) ? k.a.location[i] : loc0;
             if (inf > 0.0f) var = k.a.variant[i];
@@ -1309,12 +1389,19 @@ void launch_movement(const KArgs& k, uint32_t step, cudaStream_t s) {
 // raises occupancy for the hot path and spills on the rare cold path; the
 // autotuner picks one (DevTune::variant)
 void launch_step_fused(const KArgs& k, uint32_t step, cudaStream_t s) {
-    static unsigned g[3] = {0, 0, 0};
-    const uint32_t v = k.tune.variant < 3 ? k.tune.variant : 0;
+    static unsigned g[5] = {0, 0, 0, 0, 0};
+    const uint32_t v = k.tune.variant < 4 ? k.tune.variant : 0;
     if (!g[0]) {
         g[0] = wave_grid(k_step_fused<4>, 1u << 30);
         g[1] = wave_grid(k_step_fused<6>, 1u << 30);
         g[2] = wave_grid(k_step_fused<8>, 1u << 30);
+        g[3] = wave_grid(k_step_hot, 1u << 30);
+        g[4] = wave_grid(k_step_cold, 1u << 30);
+    }
+    if (v == 3) {
+        k_step_hot<<<agent_grid(k, g[3]), 256, 0, s>>>(k, step);
+        k_step_cold<<<g[4], 256, 0, s>>>(k, step);
+        return;
     }
     const unsigned grid = agent_grid(k, g[v]);
     if (v == 0)
@@ -1324,6 +1411,7 @@ void launch_step_fused(const KArgs& k, uint32_t step, cudaStream_t s) {
     else
         k_step_fused<8><<<grid, 256, 0, s>>>(k, step);
 }
+int step_fused_kernels(const KArgs& k) { return k.tune.variant == 3 ? 2 : 1; }
 void launch_count(const KArgs& k, cudaStream_t s) { k_count<<<grid_for(k.a.n, 8), 256, 0, s>>>(k); }
 void launch_scan(const KArgs& k, uint32_t, int with_hazard, int merge_q, cudaStream_t s) {
     unsigned tiles = (k.l.n + SCAN_TILE - 1) / SCAN_TILE;

@@ -69,6 +69,7 @@ def lib(auto_build=True):
         L.psim_checkpoint_save.argtypes = [P, U32]
         L.psim_checkpoint_restore.argtypes = [P, U32]
         L.psim_checkpoint_free.argtypes = [P]
+        L.psim_checkpoint_drop.argtypes = [P, U32]
         L.psim_checkpoint_bytes.argtypes = [P, C.POINTER(C.c_uint64)]
         L.psim_noalloc_last_error.restype = C.c_char_p
         L.psim_get_tuning.argtypes = [P, P]
@@ -251,6 +252,9 @@ class GpuSim:
 
     def checkpoint_restore(self, slot):
         self._ck(lib().psim_checkpoint_restore(self.h, slot), "checkpoint_restore")
+
+    def checkpoint_drop(self, slot):
+        self._ck(lib().psim_checkpoint_drop(self.h, slot), "checkpoint_drop")
 
     def checkpoint_free(self):
         self._ck(lib().psim_checkpoint_free(self.h), "checkpoint_free")
