@@ -73,7 +73,7 @@ class ClockSampler:
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
         try:
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(gpu_index), "--query-gpu=" + q,
-                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                       "--format=csv,noheader,nounits", "-lms", "100"],
                                       stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.p = None
@@ -274,7 +274,7 @@ def run_adjoint(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=7)
+    ap.add_argument("--steps", type=int, default=40)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=3)
@@ -316,13 +316,10 @@ def main():
     best, table = autotune.autotune(g, day)
     g.run_day(day)
     day += 1
-    # per-kernel timing (roofline): CUDA events around each kernel on the library's stream
-    kt = []
-    t_probe = day * 144
-    for j in range(12):
-        kt.append(g.time_step_kernels(t_probe + 2 * j))
-    kms = np.mean(np.array(kt[2:]), axis=0)
-    g.run_day(day)  # resynchronise the day
+    # per-kernel timing (roofline): event-record nodes inside the day graph, on
+    # the library's stream, around every kernel group of every timed day
+    g.set_profiling(True)
+    g.run_day(day)  # captures the profiled graph outside the timed region
     day += 1
     sampler = ClockSampler(local)
     launches0 = g.launch_count()
@@ -330,6 +327,7 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     total_ms = 0.0
+    kms_sum = np.zeros(4)
     for _ in range(args.steps):
         flush.fill_(1.0)  # L2 flush between timed days (buffer 2x L2)
         torch.cuda.synchronize()
@@ -339,6 +337,7 @@ def main():
         e1.record(ext)
         e1.synchronize()
         total_ms += e0.elapsed_time(e1)
+        kms_sum += g.day_kernel_ms()
         day += 1
     torch.cuda.synchronize()
     launches = g.launch_count() - launches0
@@ -348,6 +347,22 @@ def main():
         tt = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         t_max = float(tt.item())
+    spd = snap.steps_per_day
+    # average launch durations: movement(0) once a day, scan every step, fused
+    # scatter/draw/movement on all steps but the last
+    kms = [kms_sum[0] / args.steps, kms_sum[1] / (args.steps * spd), kms_sum[2] / (args.steps * (spd - 1))]
+    # the same days without the event nodes (their cost, for the record)
+    g.set_profiling(False)
+    g.run_day(day)
+    day += 1
+    plain_ms = 0.0
+    for _ in range(min(args.steps, 10)):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        g.run_day(day)
+        plain_ms += g.last_day_ms()
+        day += 1
+    plain_ms /= min(args.steps, 10)
     agent_steps = snap.n_agents * 144 * args.steps * ws
     value = agent_steps / (t_max / 1000.0)
 
@@ -399,6 +414,7 @@ def main():
                          "alg_bytes_per_launch": step_bytes, "launch_ms": step_ms, "dominant": dom,
                          "per_kernel": kern},
             "clocks": clocks, "gpu_launches": int(launches), "e2e": e2e,
+            "graph_ms_per_day_without_event_nodes": plain_ms,
             "tuning": {"best": best, "candidates": len(table),
                        "worst_step_ms": max(x[1] for x in table), "best_step_ms": min(x[1] for x in table)},
         }

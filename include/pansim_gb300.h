@@ -303,6 +303,13 @@ int psim_get_hazard(psim_ctx* ctx, float* out /*[L]*/, int64_t* fixed_sum /*[L] 
 int psim_time_step_kernels(psim_ctx* ctx, uint32_t t, float* ms /* [3] */);
 /* Timing of the last psim_run_steps graph launch, milliseconds. */
 int psim_last_day_ms(psim_ctx* ctx, float* ms);
+/* With on != 0 the day graph is captured with event-record nodes around
+ * each of its kernel groups; psim_day_kernel_ms then gives, for the last
+ * psim_run_steps, the summed durations ms[4] = {movement of step 0, the
+ * scans of all steps (tile sums + scan), the fused scatter/draw/movement
+ * kernels of steps 0..spd-2, the scatter/draw of the last step}. */
+int psim_set_profiling(psim_ctx* ctx, int on);
+int psim_day_kernel_ms(psim_ctx* ctx, float* ms /* [4] */);
 /* Counts of kernel launches issued by the library since creation. */
 int psim_launch_count(psim_ctx* ctx, uint64_t* out);
 /* The context's cudaStream_t (as void*), for callers that order their own work after it. */

@@ -1,10 +1,13 @@
 """Autotuner of the per-step kernels.
 
-Times each candidate tuning (warp aggregation of the count reductions and of
-the CSR slot atomics, blocks per SM of the per-agent kernels) on the live
-workload with CUDA events (psim_time_step_kernels: scan + fused
-scatter/draw/movement, as the day graph runs them) and keeps the fastest.
-The choice depends on the device and on the population (location sizes,
+Times each candidate tuning (fused-kernel variant, warp aggregation of the
+count reductions and of the CSR slot atomics, blocks per SM of the per-agent
+kernels) on the live workload: every candidate runs the same whole day (the
+day graph, all its steps) from the same checkpoint taken after that day's
+midnight phases, timed with CUDA events, and the fastest is kept.  Steps at
+different times of day differ several-fold in cost (movers, infectious
+locations), so candidates are never compared on different steps.  The
+choice depends on the device and on the population (location sizes,
 household structure), so it is made per context.
 """
 import itertools
@@ -12,42 +15,50 @@ import itertools
 import numpy as np
 
 DEFAULT_GRID = [0, 4, 8, 16]
+DEFAULT_VARIANTS = [0, 1, 2, 3]
+LARGE_AGENTS = 8_000_000
 
 
-def candidates(grid=None):
+def candidates(grid=None, variants=None):
     """variant: register cap of the fused kernel (64 / 40 / 32 registers) or
     3 = hot/cold split;
     blocks_per_sm 0 = one occupancy wave of that variant."""
-    for variant, agg_count, agg_slot, bps in itertools.product([0, 1, 2, 3], [1, 0], [1, 0], grid or DEFAULT_GRID):
+    for variant, agg_count, agg_slot, bps in itertools.product(variants or DEFAULT_VARIANTS, [1, 0], [1, 0],
+                                                               grid or DEFAULT_GRID):
         yield dict(agg_count=agg_count, agg_slot=agg_slot, blocks_per_sm=bps, variant=variant)
 
 
 TUNE_SLOT = 1 << 16
 
 
-def autotune(sim, day, reps=3, grid=None, verbose=False, keep_state=True):
-    """Tries the candidates on steps of `day`; returns (best tuning, table of
-    (tuning, step ms)).  With keep_state the simulation state is saved to a
-    checkpoint first and restored afterwards, so tuning leaves no trace."""
-    if keep_state:
-        sim.checkpoint_save(TUNE_SLOT)
+def autotune(sim, day, reps=2, grid=None, variants=None, verbose=False):
+    """Tries the candidates on the steps of `day` (the simulation must be at
+    the start of that day); returns (best tuning, table of (tuning, day ms)).
+    The simulation state is saved first and restored afterwards, so tuning
+    leaves no trace.  Populations above LARGE_AGENTS get a reduced candidate
+    set and one repetition (a day there takes a good fraction of a second)."""
+    if sim.snap.n_agents > LARGE_AGENTS:
+        grid = grid or [0, 16]
+        variants = variants or [0, 3]
+        reps = 1
+    spd = sim.snap.steps_per_day
+    sim.checkpoint_save(TUNE_SLOT)
+    sim.midnight(day * spd)
+    sim.checkpoint_save(TUNE_SLOT + 1)
     table = []
-    t = day * sim.snap.steps_per_day
-    for cand in candidates(grid):
+    for cand in candidates(grid, variants):
         sim.set_tuning(**cand)
         ms = []
         for _ in range(reps):
-            if t % sim.snap.steps_per_day + 1 >= sim.snap.steps_per_day:
-                t += 2
-            k = sim.time_step_kernels(t)
-            ms.append(float(k[1] + k[2]))
-            t += 2
-        table.append((cand, float(np.median(ms))))
+            sim.checkpoint_restore(TUNE_SLOT + 1)
+            sim.run_steps(day)
+            ms.append(sim.last_day_ms())
+        table.append((cand, float(min(ms))))
         if verbose:
-            print("tune", cand, "%.2f us" % (1000 * table[-1][1]))
+            print("tune", cand, "%.3f ms/day" % table[-1][1])
     best = min(table, key=lambda x: x[1])[0]
     sim.set_tuning(**best)
-    if keep_state:
-        sim.checkpoint_restore(TUNE_SLOT)
-        sim.checkpoint_drop(TUNE_SLOT)
+    sim.checkpoint_restore(TUNE_SLOT)
+    sim.checkpoint_drop(TUNE_SLOT)
+    sim.checkpoint_drop(TUNE_SLOT + 1)
     return best, table

@@ -50,6 +50,11 @@ struct psim_ctx {
     std::vector<std::pair<void*, size_t>> regions;
     size_t checkpoint_bytes = 0;
     std::map<uint32_t, void*> checkpoints;
+    // per-kernel timing inside the day graph: event-record nodes around the
+    // movement of step 0, every scan, every fused step and the last scatter
+    bool profile = false;
+    std::vector<cudaEvent_t> prof_ev;
+    bool prof_valid = false;
 };
 
 namespace {
@@ -251,16 +256,31 @@ int capture_day_graph(psim_ctx* c) {
         c->day_graph = nullptr;
     }
     cudaGraph_t g = nullptr;
+    // 2 * spd + 2 events: [0] before movement(0), then one after every kernel group
+    const size_t n_ev = c->profile ? 2ull * c->spd + 2 : 0;
+    while (c->prof_ev.size() < n_ev) {
+        cudaEvent_t ev = nullptr;
+        CK(cudaEventCreate(&ev));
+        c->prof_ev.push_back(ev);
+    }
+    size_t ev_i = 0;
+    auto mark = [&]() {
+        if (c->profile) cudaEventRecordWithFlags(c->prof_ev[ev_i++], c->stream, cudaEventRecordExternal);
+    };
     CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     const int merge_q = c->params.quarantine_policy > 1;
     // movement(0); then per step: scan(s), scatter+draw(s) fused with movement(s+1)
+    mark();
     launch_movement(c->k, 0, c->stream);
+    mark();
     for (uint32_t s = 0; s < c->spd; ++s) {
         launch_scan(c->k, s, 1, merge_q, c->stream);
+        mark();
         if (s + 1 < c->spd)
             launch_step_fused(c->k, s, c->stream);
         else
             launch_scatter_draw(c->k, s, 1, 1, c->stream);
+        mark();
     }
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     if (e != cudaSuccess) return fail(c, PSIM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
@@ -269,6 +289,7 @@ int capture_day_graph(psim_ctx* c) {
     if (e != cudaSuccess) return fail(c, PSIM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
     c->graph_kernels = (2ull + (uint64_t)step_fused_kernels(c->k)) * c->spd + 1;
     c->graph_dirty = false;
+    c->prof_valid = false;
     return 0;
 }
 
@@ -547,6 +568,7 @@ int psim_destroy(psim_ctx* c) {
     for (auto& kv : c->checkpoints)
         if (kv.second) cudaFree(kv.second);
     if (c->day_graph) cudaGraphExecDestroy(c->day_graph);
+    for (cudaEvent_t ev : c->prof_ev) cudaEventDestroy(ev);
     for (void* p : c->allocs) cudaFree(p);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
@@ -867,6 +889,7 @@ int psim_run_steps(psim_ctx* c, uint32_t day) {
     CK(cudaEventSynchronize(c->ev1));
     CK(cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1));
     c->launches += c->graph_kernels;
+    c->prof_valid = c->profile;
     c->csr_fresh = false;
     return check_device_err(c);
 }
@@ -904,6 +927,32 @@ int psim_get_hazard(psim_ctx* c, float* out, int64_t* fixed_sum) {
 int psim_last_day_ms(psim_ctx* c, float* ms) {
     if (!c || !ms) return PSIM_ERR_ARG;
     *ms = c->last_ms;
+    return 0;
+}
+
+int psim_set_profiling(psim_ctx* c, int on) {
+    if (!c) return PSIM_ERR_ARG;
+    if ((on != 0) != c->profile) {
+        c->profile = on != 0;
+        c->graph_dirty = true;
+    }
+    c->prof_valid = false;
+    return 0;
+}
+
+int psim_day_kernel_ms(psim_ctx* c, float* ms) {
+    if (!c || !ms) return PSIM_ERR_ARG;
+    if (!c->prof_valid) return fail(c, PSIM_ERR_STATE, "no profiled day: psim_set_profiling(1), then psim_run_steps");
+    float t = 0.f;
+    CK(cudaEventElapsedTime(&t, c->prof_ev[0], c->prof_ev[1]));
+    ms[0] = t;
+    ms[1] = ms[2] = ms[3] = 0.f;
+    for (uint32_t s = 0; s < c->spd; ++s) {
+        CK(cudaEventElapsedTime(&t, c->prof_ev[1 + 2 * s], c->prof_ev[2 + 2 * s]));
+        ms[1] += t;
+        CK(cudaEventElapsedTime(&t, c->prof_ev[2 + 2 * s], c->prof_ev[3 + 2 * s]));
+        ms[s + 1 < c->spd ? 2 : 3] += t;
+    }
     return 0;
 }
 

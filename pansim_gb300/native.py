@@ -56,6 +56,8 @@ def lib(auto_build=True):
         L.psim_get_csr.argtypes = [P, I, P, P]
         L.psim_get_hazard.argtypes = [P, P, P]
         L.psim_last_day_ms.argtypes = [P, C.POINTER(C.c_float)]
+        L.psim_set_profiling.argtypes = [P, C.c_int]
+        L.psim_day_kernel_ms.argtypes = [P, C.c_void_p]
         L.psim_launch_count.argtypes = [P, C.POINTER(C.c_uint64)]
         L.psim_stream_handle.argtypes = [P, C.POINTER(P)]
         L.psim_bounded_wait_selftest.argtypes = [P, U32]
@@ -202,6 +204,16 @@ class GpuSim:
         ms = C.c_float(0)
         lib().psim_last_day_ms(self.h, C.byref(ms))
         return ms.value
+
+    def set_profiling(self, on=True):
+        self._ck(lib().psim_set_profiling(self.h, 1 if on else 0), "set_profiling")
+
+    def day_kernel_ms(self):
+        """Summed kernel durations of the last profiled day: movement(0), scans,
+        fused steps, last scatter/draw."""
+        ms = np.zeros(4, np.float32)
+        self._ck(lib().psim_day_kernel_ms(self.h, _p(ms)), "day_kernel_ms")
+        return ms
 
     def launch_count(self):
         n = C.c_uint64(0)

@@ -160,3 +160,17 @@ def test_tuning_choices_do_not_change_results(gpu_lib, tuning):
         assert stats_rows(o.run_day(d)) == stats_rows(g.run_day(d)), (d, tuning)
     g.download()
     assert diff_state(s_cpu, s_gpu) == []
+
+
+def test_profiled_graph_same_results_and_kernel_times(gpu_lib):
+    s_cpu, s_gpu, o, g = _pair(n=12000, locs=3000, initial_infected_frac=0.02)
+    g.set_profiling(True)
+    for d in range(2):
+        assert stats_rows(o.run_day(d)) == stats_rows(g.run_day(d)), d
+        ms = g.day_kernel_ms()
+        assert (ms > 0).all()
+        assert ms.sum() <= g.last_day_ms() * 1.001
+    g.set_profiling(False)
+    assert stats_rows(o.run_day(2)) == stats_rows(g.run_day(2))
+    g.download()
+    assert diff_state(s_cpu, s_gpu) == []
