@@ -252,7 +252,54 @@ int psim_test_day(psim_ctx* ctx, uint32_t t, uint32_t* out_tpp /* [replicas*3] o
 int psim_progress_day(psim_ctx* ctx, uint32_t t);
 int psim_stats_day(psim_ctx* ctx, uint32_t t, psim_day_stats* out /* [replicas] */);
 int psim_plan_day(psim_ctx* ctx, uint32_t t);
+/* test (t > 0) -> progress (t > 0) -> statistics -> closure rules (when set)
+ * -> plan, the midnight block of runSimulation. */
 int psim_midnight(psim_ctx* ctx, uint32_t t, psim_day_stats* out /* [replicas] */);
+
+/* Closure rules: RuleClosure (closurePolicies.h:48-479) with the rule list of
+ * closureRules.json (closuresFormat.h:7-22).  Rule names Masks, Curfew,
+ * HolidayMode, QuarantineImmune, LockdownNonvacc, QuarantinePolicy,
+ * SchoolAgeRestriction, ExposeToMutation, ReduceMovement and TestingProb act
+ * on the named policy switch; any other name closes its location types.
+ * Condition types: afterDays, hospitalizedFraction, newDeadFraction
+ * (closurePolicies.h:109-232) and newCasesFraction, which has no reference
+ * counterpart: the fraction of the population newly infected in the last
+ * 24 h (the NI column), with hospitalizedFraction's close/open hysteresis.
+ * `header` is the statistics header (state names, then H, T, P1, ...; the
+ * statesHeader of simulation.h:749); hospital states are the columns whose
+ * name contains "_h", the dead column is "D1".  With enable_closures == 0
+ * only the named switches are kept (closurePolicies.h:103-108).  Rules are
+ * evaluated by psim_midnight after the statistics, on the row of replica 0;
+ * contexts with more than one replica reject rules.  n_rules == 0 removes
+ * the rules. */
+#define PSIM_CLOSURE_MAX_TYPES 10
+typedef struct psim_closure_rule {
+    char name[64];
+    char condition_type[32];
+    double threshold;
+    double threshold2;
+    char parameter[64];               /* the rule's parameter as text ("0.8", "2000-0500", ...) */
+    int32_t close_after;
+    int32_t open_after;
+    uint32_t n_types;                 /* entries of types, < PSIM_CLOSURE_MAX_TYPES */
+    int32_t types[PSIM_CLOSURE_MAX_TYPES]; /* locationTypesToClose */
+} psim_closure_rule;
+int psim_closures_init(psim_ctx* ctx, const psim_closure_rule* rules, uint32_t n_rules, const char* header,
+                       int enable_closures);
+/* Evaluates the rules on a statistics row (what psim_midnight does after its
+ * statistics); `t` is the midnight timestamp. */
+int psim_closures_midnight(psim_ctx* ctx, uint32_t t, const psim_day_stats* row);
+/* State of the engine: per condition its active flag, per rule whether its
+ * locations/switch are open (previousOpenState); either pointer may be NULL. */
+int psim_closures_status(psim_ctx* ctx, uint8_t* cond_active /* [n_rules] */, uint8_t* rule_open /* [n_rules] */,
+                         uint32_t* n_rules);
+/* The current run parameters (closure rules change curfew, policy, testing
+ * probabilities, ...). */
+int psim_get_params(psim_ctx* ctx, psim_params* out);
+/* The current schedule table (ReduceMovement edits it): event_offset
+ * [n_agent_types*28+1] and, when non-NULL, up to `capacity` events. */
+int psim_get_events(psim_ctx* ctx, uint32_t* event_offset, uint32_t* loc_type, float* chance, uint16_t* start,
+                    uint16_t* end, uint16_t* duration, uint32_t capacity, uint32_t* n_events);
 
 /* All steps of one day as one CUDA graph launch (captured on first use and
  * after any psim_set_params / psim_set_tracking). */

@@ -53,6 +53,7 @@ def lib():
         L.psim_oracle_stats.argtypes = [P, U32, P]
         L.psim_oracle_midnight.argtypes = [P, U32, P]
         L.psim_oracle_run_day.argtypes = [P, U32, P]
+        L.psim_oracle_expose.argtypes = [P, U32, U32, D]
         L.psim_oracle_csr_offsets.restype = C.POINTER(C.c_uint32)
         L.psim_oracle_csr_offsets.argtypes = [P]
         L.psim_oracle_csr_agents.restype = C.POINTER(C.c_uint32)

@@ -940,6 +940,34 @@ void psim_oracle_run_day(psim_oracle* o, uint32_t day, psim_day_stats* out) {
     for (uint32_t s = 0; s < o->spd; ++s) psim_oracle_step(o, t0 + s, NULL);
 }
 
+/* Closure rule ExposeToMutation, closurePolicies.h:349-392: each agent with
+ * susceptibility s > 0 for the variant is infected when a uniform draw is
+ * below fraction * s; the draw comes from the agent's EXPOSE stream. */
+void psim_oracle_expose(psim_oracle* o, uint32_t t, uint32_t v, double fraction) {
+    psim_agents* a = o->a;
+    const psim_model* m = o->m;
+    const uint32_t N = a->n;
+    for (uint32_t i = 0; i < N; ++i) {
+        float su = a->susceptible[(size_t)v * N + i];
+        if (!(su > 0.0f)) continue;
+        uint32_t rep = o->agent_rep[i];
+        uint32_t li = i - o->r.agent_offset[rep];
+        double U = psim_u01_once(o->r.seed[rep], li, t, PSIM_PHASE_EXPOSE);
+        if (U < fraction * (double)su) {
+            a->state[i] = (int8_t)m->first_infected_state;
+            a->variant[i] = (uint8_t)v;
+            a->days[i] = -2;
+            update_meta(o, i);
+            a->st_infected_ts[i] = t;
+            a->st_infected_loc[i] = a->location[i];
+            a->st_infected_count[i]++;
+            a->st_worst_state[i] = a->state[i];
+            a->st_worst_ts[i] = t;
+            a->st_variant_mask[i] |= 1u << v;
+        }
+    }
+}
+
 /* Simulation::flagHealthcareWorkers, simulation.h:670-693 */
 static void flag_hcw(psim_oracle* o) {
     psim_agents* a = o->a;

@@ -43,7 +43,15 @@ def autotune(sim, day, reps=2, grid=None, variants=None, verbose=False):
         reps = 1
     spd = sim.snap.steps_per_day
     sim.checkpoint_save(TUNE_SLOT)
-    sim.midnight(day * spd)
+    # the midnight phases without closure rules, whose host-side state a
+    # checkpoint does not hold
+    t = day * spd
+    if t > 0 and int(sim.snap.params.get("testing_enabled", 0)):
+        sim.test(t)
+    if t > 0:
+        sim.progress(t)
+    sim.stats(t)
+    sim.plan(t)
     sim.checkpoint_save(TUNE_SLOT + 1)
     table = []
     for cand in candidates(grid, variants):

@@ -85,4 +85,13 @@ class PsimTuning(C.Structure):
                 ("variant", C.c_uint32)]
 
 
+PSIM_CLOSURE_MAX_TYPES = 10
+
+
+class PsimClosureRule(C.Structure):
+    _fields_ = [("name", C.c_char * 64), ("condition_type", C.c_char * 32), ("threshold", C.c_double),
+                ("threshold2", C.c_double), ("parameter", C.c_char * 64), ("close_after", C.c_int32),
+                ("open_after", C.c_int32), ("n_types", C.c_uint32), ("types", C.c_int32 * PSIM_CLOSURE_MAX_TYPES)]
+
+
 ABI_STRUCTS = [PsimModel, PsimAgents, PsimLocations, PsimParams, PsimReplicas, PsimDayStats]

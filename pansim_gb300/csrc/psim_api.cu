@@ -11,67 +11,13 @@
 #include <string>
 #include <vector>
 
-#include "psim_device.cuh"
+#include "psim_ctx.h"
 
 using namespace psim;
-
-struct psim_ctx {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    std::string err;
-    KArgs k{};
-    std::vector<void*> allocs;
-    uint32_t N = 0, L = 0, V = 0, R = 0, S = 0, spd = 144;
-    uint64_t n_poss = 0;
-    psim_params params{};
-    std::vector<uint32_t> rep_agent_off, rep_loc_off, rep_cemetery, hcw_count;
-    std::vector<uint64_t> rep_seed;
-    std::vector<double> rep_k;
-    // host copies of the per-day clock
-    DevClock h_clock{};
-    bool clock_valid = false;
-    // graph of the steps of one day
-    cudaGraphExec_t day_graph = nullptr;
-    bool graph_dirty = true;
-    uint64_t graph_kernels = 0;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    float last_ms = 0.f;
-    uint64_t launches = 0;
-    bool uploaded = false;
-    bool csr_fresh = false;      // counts of the current positions are built
-    std::vector<DevStatsAcc> h_stats;
-    std::vector<double> h_expected;
-    // adjoint
-    double* d_adj_weight = nullptr;
-    double* d_grad = nullptr;
-    int8_t* d_type_slot = nullptr;
-    float* d_w_by_type = nullptr;
-    // per-day checkpoints of the mutable state (device copies)
-    std::vector<std::pair<void*, size_t>> regions;
-    size_t checkpoint_bytes = 0;
-    std::map<uint32_t, void*> checkpoints;
-    // per-kernel timing inside the day graph: event-record nodes around the
-    // movement of step 0, every scan, every fused step and the last scatter
-    bool profile = false;
-    std::vector<cudaEvent_t> prof_ev;
-    bool prof_valid = false;
-};
 
 namespace {
 
 const char* kVersion = "pansim_gb300 0.1.0 (sm_103a)";
-
-int fail(psim_ctx* c, int code, const std::string& msg) {
-    if (c) c->err = msg;
-    return code;
-}
-
-#define CK(call)                                                                                      \
-    do {                                                                                              \
-        cudaError_t e_ = (call);                                                                      \
-        if (e_ != cudaSuccess)                                                                        \
-            return fail(c, PSIM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));        \
-    } while (0)
 
 template <typename T>
 int dalloc(psim_ctx* c, T** p, size_t count) {
@@ -437,6 +383,15 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     UPM(ev_loc_type, m->n_events) UPM(ev_chance, m->n_events) UPM(ev_start, m->n_events) UPM(ev_end, m->n_events)
     UPM(ev_duration, m->n_events)
 #undef UPM
+    {
+        const size_t no = (size_t)m->n_agent_types * 28 + 1, ne = m->n_events;
+        c->h_event_offset.assign(m->event_offset, m->event_offset + no);
+        c->h_ev_loc_type.assign(m->ev_loc_type, m->ev_loc_type + ne);
+        c->h_ev_chance.assign(m->ev_chance, m->ev_chance + ne);
+        c->h_ev_start.assign(m->ev_start, m->ev_start + ne);
+        c->h_ev_end.assign(m->ev_end, m->ev_end + ne);
+        c->h_ev_duration.assign(m->ev_duration, m->ev_duration + ne);
+    }
     if ((rc = dupload(c, &dm.len_thr, thr.data(), thr.size()))) return bail(rc);
     // agents: immutable
     DevAgents& da = k.a;
@@ -565,6 +520,7 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
 int psim_destroy(psim_ctx* c) {
     if (!c) return 0;
     if (c->stream) cudaStreamSynchronize(c->stream);
+    closures_free(c);
     for (auto& kv : c->checkpoints)
         if (kv.second) cudaFree(kv.second);
     if (c->day_graph) cudaGraphExecDestroy(c->day_graph);
@@ -609,6 +565,27 @@ int psim_download(psim_ctx* c, psim_agents* a, psim_locations* l) {
         CK(cudaMemcpyAsync(l->quarantine_until, dl.quarantine_until, L * 4, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     return check_device_err(c);
+}
+
+int psim_get_params(psim_ctx* c, psim_params* out) {
+    if (!c || !out) return PSIM_ERR_ARG;
+    *out = c->params;
+    return 0;
+}
+
+int psim_get_events(psim_ctx* c, uint32_t* event_offset, uint32_t* loc_type, float* chance, uint16_t* start,
+                    uint16_t* end, uint16_t* duration, uint32_t capacity, uint32_t* n_events) {
+    if (!c) return PSIM_ERR_ARG;
+    const size_t ne = c->h_ev_loc_type.size();
+    if (n_events) *n_events = (uint32_t)ne;
+    if (event_offset) std::memcpy(event_offset, c->h_event_offset.data(), sizeof(uint32_t) * c->h_event_offset.size());
+    const size_t m = ne < capacity ? ne : capacity;
+    if (loc_type) std::memcpy(loc_type, c->h_ev_loc_type.data(), sizeof(uint32_t) * m);
+    if (chance) std::memcpy(chance, c->h_ev_chance.data(), sizeof(float) * m);
+    if (start) std::memcpy(start, c->h_ev_start.data(), sizeof(uint16_t) * m);
+    if (end) std::memcpy(end, c->h_ev_end.data(), sizeof(uint16_t) * m);
+    if (duration) std::memcpy(duration, c->h_ev_duration.data(), sizeof(uint16_t) * m);
+    return 0;
 }
 
 int psim_set_params(psim_ctx* c, const psim_params* p) {
@@ -872,7 +849,15 @@ int psim_midnight(psim_ctx* c, uint32_t t, psim_day_stats* out) {
         launch_progress(c->k, t, c->stream);
         c->launches += 1;
     }
-    if ((rc = psim_stats_day(c, t, out))) return rc;
+    if (c->closures) {
+        // the rules read replica 0's row even when the caller passes no buffer
+        std::vector<psim_day_stats> rows(c->R);
+        if ((rc = psim_stats_day(c, t, rows.data()))) return rc;
+        if (out) std::memcpy(out, rows.data(), sizeof(psim_day_stats) * c->R);
+        if ((rc = closures_apply(c, t, &rows[0]))) return rc;
+    } else if ((rc = psim_stats_day(c, t, out))) {
+        return rc;
+    }
     return psim_plan_day(c, t);
 }
 

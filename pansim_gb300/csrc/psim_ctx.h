@@ -1,0 +1,84 @@
+// Host-side context of the C ABI, shared by the translation units that
+// implement it (psim_api.cu, psim_closures.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "psim_device.cuh"
+
+namespace psim {
+struct ClosureEngine;
+struct ImmunizationEngine;
+}  // namespace psim
+
+using psim::KArgs;
+using psim::DevClock;
+using psim::DevStatsAcc;
+
+struct psim_ctx {
+    // host copy of the schedule table (closure rule ReduceMovement edits it)
+    std::vector<uint32_t> h_event_offset, h_ev_loc_type;
+    std::vector<float> h_ev_chance;
+    std::vector<uint16_t> h_ev_start, h_ev_end, h_ev_duration;
+    psim::ClosureEngine* closures = nullptr;
+    psim::ImmunizationEngine* immunization = nullptr;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    KArgs k{};
+    std::vector<void*> allocs;
+    uint32_t N = 0, L = 0, V = 0, R = 0, S = 0, spd = 144;
+    uint64_t n_poss = 0;
+    psim_params params{};
+    std::vector<uint32_t> rep_agent_off, rep_loc_off, rep_cemetery, hcw_count;
+    std::vector<uint64_t> rep_seed;
+    std::vector<double> rep_k;
+    // host copies of the per-day clock
+    DevClock h_clock{};
+    bool clock_valid = false;
+    // graph of the steps of one day
+    cudaGraphExec_t day_graph = nullptr;
+    bool graph_dirty = true;
+    uint64_t graph_kernels = 0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    float last_ms = 0.f;
+    uint64_t launches = 0;
+    bool uploaded = false;
+    bool csr_fresh = false;      // counts of the current positions are built
+    std::vector<DevStatsAcc> h_stats;
+    std::vector<double> h_expected;
+    // adjoint
+    double* d_adj_weight = nullptr;
+    double* d_grad = nullptr;
+    int8_t* d_type_slot = nullptr;
+    float* d_w_by_type = nullptr;
+    // per-day checkpoints of the mutable state (device copies)
+    std::vector<std::pair<void*, size_t>> regions;
+    size_t checkpoint_bytes = 0;
+    std::map<uint32_t, void*> checkpoints;
+    // per-kernel timing inside the day graph: event-record nodes around the
+    // movement of step 0, every scan, every fused step and the last scatter
+    bool profile = false;
+    std::vector<cudaEvent_t> prof_ev;
+    bool prof_valid = false;
+};
+
+
+inline int fail(psim_ctx* c, int code, const std::string& msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+#define CK(call)                                                                                      \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess)                                                                        \
+            return fail(c, PSIM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));        \
+    } while (0)
+
+// closure rules (psim_closures.cu)
+void closures_free(psim_ctx* c);
+int closures_apply(psim_ctx* c, uint32_t t, const psim_day_stats* row);

@@ -197,6 +197,14 @@ void launch_scan(const KArgs& k, uint32_t step_in_day, int with_hazard, int merg
 void launch_scatter_draw(const KArgs& k, uint32_t step_in_day, int scatter, int draw, cudaStream_t s);
 void launch_offsets(const KArgs& k, cudaStream_t s);
 void launch_step_fused(const KArgs& k, uint32_t step_in_day, cudaStream_t s);
+// closure rules
+struct ClosureTypes {
+    uint32_t n;
+    uint32_t v[10];
+};
+void launch_masks(const KArgs& k, uint32_t home_type, double coef, int open, cudaStream_t s);
+void launch_close_types(const KArgs& k, const ClosureTypes& ty, int open, cudaStream_t s);
+void launch_expose(const KArgs& k, uint32_t t, uint32_t variant, double fraction, cudaStream_t s);
 int step_fused_kernels(const KArgs& k);
 void launch_canonical_csr(const KArgs& k, cudaStream_t s);
 void launch_progress(const KArgs& k, uint32_t t, cudaStream_t s);

@@ -1333,6 +1333,56 @@ __global__ void k_type_weights(KArgs k, const float* w_by_type) {
         k.l.infectiousness[l] = w_by_type[k.l.type[l]];
 }
 
+// Closure rule Masks (closurePolicies.h:236-268): the w of every non-home
+// location multiplied (masks on) or divided (masks off) by the coefficient,
+// float * double rounded to float as in the reference's lambda.
+__global__ void k_masks(KArgs k, uint32_t home_type, double coef, int open) {
+    for (uint32_t l = blockIdx.x * blockDim.x + threadIdx.x; l < k.l.n; l += gridDim.x * blockDim.x) {
+        if (k.l.type[l] == home_type) continue;
+        const double w = (double)k.l.infectiousness[l];
+        k.l.infectiousness[l] = (float)(open ? w / coef : w * coef);
+    }
+}
+
+// A closure rule over location types (closurePolicies.h:424-468): every
+// non-essential location whose type is listed becomes open/closed.
+__global__ void k_close_types(KArgs k, ClosureTypes ty, int open) {
+    for (uint32_t l = blockIdx.x * blockDim.x + threadIdx.x; l < k.l.n; l += gridDim.x * blockDim.x) {
+        if (k.l.essential[l] == 1) continue;
+        const uint32_t t = k.l.type[l];
+        for (uint32_t q = 0; q < ty.n; ++q)
+            if (t == ty.v[q]) {
+                k.l.open[l] = open ? 1 : 0;
+                break;
+            }
+    }
+}
+
+// Closure rule ExposeToMutation (closurePolicies.h:349-392): every agent with
+// susceptibility s > 0 for the variant is infected with it when a uniform
+// draw is below fraction * s.
+__global__ void k_expose(KArgs k, uint32_t t, uint32_t v, double fraction) {
+    const uint32_t N = k.a.n;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+        const float su = k.a.susceptible[(size_t)v * N + i];
+        if (!(su > 0.0f)) continue;
+        const uint32_t rep = k.a.rep[i];
+        const double U = psim_u01_once(k.r.seed[rep], i - k.r.agent_off[rep], t, PSIM_PHASE_EXPOSE);
+        if (U < fraction * (double)su) {
+            k.a.state[i] = (int8_t)k.m.first_infected;
+            k.a.variant[i] = (uint8_t)v;
+            k.a.days[i] = -2;
+            update_meta(k, i);
+            k.a.st_infected_ts[i] = t;
+            k.a.st_infected_loc[i] = k.a.location[i];
+            k.a.st_infected_count[i] = k.a.st_infected_count[i] + 1;
+            k.a.st_worst_state[i] = (int8_t)k.m.first_infected;
+            k.a.st_worst_ts[i] = t;
+            k.a.st_variant_mask[i] |= 1u << v;
+        }
+    }
+}
+
 // A wait on a flag that nothing sets, bounded by `iters`: reports
 // ERR_TEST_WAIT and returns.  Exercises the bounded-wait error path.
 __global__ void k_bounded_wait_probe(KArgs k, uint32_t iters) {
@@ -1460,6 +1510,15 @@ void launch_plan(const KArgs& k, uint32_t t, cudaStream_t s) {
 void launch_flag_hcw(const KArgs& k, cudaStream_t s) { k_flag_hcw<<<grid_for(k.a.n, 8), 256, 0, s>>>(k); }
 void launch_type_weights(const KArgs& k, const float* w_by_type, cudaStream_t s) {
     k_type_weights<<<grid_for(k.l.n, 8), 256, 0, s>>>(k, w_by_type);
+}
+void launch_masks(const KArgs& k, uint32_t home_type, double coef, int open, cudaStream_t s) {
+    k_masks<<<grid_for(k.l.n, 8), 256, 0, s>>>(k, home_type, coef, open);
+}
+void launch_close_types(const KArgs& k, const ClosureTypes& ty, int open, cudaStream_t s) {
+    k_close_types<<<grid_for(k.l.n, 8), 256, 0, s>>>(k, ty, open);
+}
+void launch_expose(const KArgs& k, uint32_t t, uint32_t variant, double fraction, cudaStream_t s) {
+    k_expose<<<grid_for(k.a.n, 8), 256, 0, s>>>(k, t, variant, fraction);
 }
 void launch_bounded_wait_probe(const KArgs& k, uint32_t iters, cudaStream_t s) {
     k_bounded_wait_probe<<<1, 32, 0, s>>>(k, iters);

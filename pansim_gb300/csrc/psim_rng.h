@@ -47,7 +47,11 @@ enum {
     PSIM_PHASE_PLAN_SWQ = 19, // planLocations: school/work quarantine lookups
     PSIM_PHASE_PLAN_UNDERAGE = 20,
     PSIM_PHASE_PLAN_NOWORK = 21,
-    PSIM_PHASE_TEST_FLAG = 22 // testing: flagLocations lookups
+    PSIM_PHASE_TEST_FLAG = 22, // testing: flagLocations lookups
+    PSIM_PHASE_EXPOSE = 23,    // closure rule ExposeToMutation at the midnight timestamp
+    PSIM_PHASE_IMM_CATEGORY = 24, // immunization categories, + category pass (10 passes)
+    PSIM_PHASE_IMM_BOOSTER = 40,  // immunization boosters, + round
+    PSIM_PHASE_IMM_PRIMARY = 56   // immunization first doses, + category
 };
 
 typedef struct psim_ctr4 {

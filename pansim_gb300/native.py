@@ -57,6 +57,11 @@ def lib(auto_build=True):
         L.psim_get_hazard.argtypes = [P, P, P]
         L.psim_last_day_ms.argtypes = [P, C.POINTER(C.c_float)]
         L.psim_set_profiling.argtypes = [P, C.c_int]
+        L.psim_closures_init.argtypes = [P, P, U32, C.c_char_p, I]
+        L.psim_closures_midnight.argtypes = [P, U32, P]
+        L.psim_closures_status.argtypes = [P, P, P, P]
+        L.psim_get_params.argtypes = [P, P]
+        L.psim_get_events.argtypes = [P, P, P, P, P, P, P, U32, P]
         L.psim_day_kernel_ms.argtypes = [P, C.c_void_p]
         L.psim_launch_count.argtypes = [P, C.POINTER(C.c_uint64)]
         L.psim_stream_handle.argtypes = [P, C.POINTER(P)]
@@ -204,6 +209,39 @@ class GpuSim:
         ms = C.c_float(0)
         lib().psim_last_day_ms(self.h, C.byref(ms))
         return ms.value
+
+    # closure rules (RuleClosure)
+    def closures_init(self, rules, header, enable_closures=True):
+        """rules: closures.Rule list or dicts with the closureRules.json keys."""
+        from . import closures
+        arr = closures.rule_array(rules)
+        self._rules = arr
+        self._ck(lib().psim_closures_init(self.h, arr, len(arr), header.encode(), 1 if enable_closures else 0),
+                 "closures_init")
+
+    def closures_status(self):
+        n = C.c_uint32(0)
+        lib().psim_closures_status(self.h, None, None, C.byref(n))
+        act = np.zeros(max(n.value, 1), np.uint8)
+        op = np.zeros(max(n.value, 1), np.uint8)
+        self._ck(lib().psim_closures_status(self.h, _p(act), _p(op), C.byref(n)), "closures_status")
+        return act[: n.value].astype(bool), op[: n.value].astype(bool)
+
+    def get_params(self):
+        p = cabi.PsimParams()
+        self._ck(lib().psim_get_params(self.h, C.byref(p)), "get_params")
+        return p
+
+    def get_events(self):
+        n = C.c_uint32(0)
+        off = np.zeros(int(self.snap.model["n_agent_types"]) * 28 + 1, np.uint32)
+        self._ck(lib().psim_get_events(self.h, _p(off), None, None, None, None, None, 0, C.byref(n)), "get_events")
+        ne = n.value
+        ev = dict(event_offset=off, ev_loc_type=np.zeros(ne, np.uint32), ev_chance=np.zeros(ne, np.float32),
+                  ev_start=np.zeros(ne, np.uint16), ev_end=np.zeros(ne, np.uint16), ev_duration=np.zeros(ne, np.uint16))
+        self._ck(lib().psim_get_events(self.h, _p(off), _p(ev["ev_loc_type"]), _p(ev["ev_chance"]), _p(ev["ev_start"]),
+                                       _p(ev["ev_end"]), _p(ev["ev_duration"]), ne, C.byref(n)), "get_events")
+        return ev
 
     def set_profiling(self, on=True):
         self._ck(lib().psim_set_profiling(self.h, 1 if on else 0), "set_profiling")
