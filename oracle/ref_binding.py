@@ -29,6 +29,15 @@ def lib():
         L.ref_csr.argtypes = [P, P, P]
         L.ref_event_minutes.argtypes = [P, P, P, P]
         L.ref_threads.restype = C.c_int
+        L.ref_midnight_pre.argtypes = [P, U32]
+        L.ref_plan.argtypes = [P, U32]
+        L.ref_get_params.argtypes = [P, P]
+        L.ref_closures_init.restype = C.c_int
+        L.ref_closures_init.argtypes = [P, P, U32, C.c_char_p, C.c_int]
+        L.ref_closures_midnight.argtypes = [P, U32, P, U32]
+        L.ref_closures_status.argtypes = [P, P, P, P]
+        L.ref_events.restype = U32
+        L.ref_events.argtypes = [P, P, P, P, U32]
         _lib = L
     return _lib
 
@@ -97,3 +106,45 @@ class RefSim:
         s, e, d = (np.zeros(n, np.uint16) for _ in range(3))
         lib().ref_event_minutes(self.h, _p(s), _p(e), _p(d))
         return s, e, d
+
+    # closure rules through the reference's RuleClosure
+    def midnight_pre(self, t):
+        lib().ref_midnight_pre(self.h, t)
+
+    def plan(self, t):
+        lib().ref_plan(self.h, t)
+
+    def params(self):
+        from pansim_gb300 import cabi
+        p = cabi.PsimParams()
+        lib().ref_get_params(self.h, C.byref(p))
+        return p
+
+    def closures_init(self, rules, header, enable=True):
+        from pansim_gb300 import closures
+        self._rules = closures.rule_array(rules)
+        rc = lib().ref_closures_init(self.h, self._rules, len(rules), header.encode(), 1 if enable else 0)
+        if rc:
+            raise ValueError("reference RuleClosure::init threw")
+
+    def closures_midnight(self, t, row):
+        v = np.array(list(row.v)[: row.n], np.uint32)
+        lib().ref_closures_midnight(self.h, t, _p(v), len(v))
+
+    def closures_status(self):
+        n = C.c_uint32(0)
+        a = np.zeros(64, np.uint8)
+        o = np.zeros(64, np.uint8)
+        lib().ref_closures_status(self.h, _p(a), _p(o), C.byref(n))
+        return a[: n.value].astype(bool), o[: n.value].astype(bool)
+
+    def events(self):
+        off = np.zeros(int(self.snap.model["n_agent_types"]) * 28 + 1, np.uint32)
+        cap = 4 * len(self.snap.model["ev_loc_type"]) + 64
+        ty = np.zeros(cap, np.uint32)
+        ch = np.zeros(cap, np.float32)
+        n = lib().ref_events(self.h, _p(off), _p(ty), _p(ch), cap)
+        s, e, d = (np.zeros(max(n, cap), np.uint16) for _ in range(3))
+        lib().ref_event_minutes(self.h, _p(s), _p(e), _p(d))
+        return dict(event_offset=off, ev_loc_type=ty[:n], ev_chance=ch[:n], ev_start=s[:n], ev_end=e[:n],
+                    ev_duration=d[:n])

@@ -10,7 +10,10 @@
 //   Util::updatePerLocationAgentLists, Util::reduce_by_location (src/tools/util.cpp, util.h)
 //   DynamicPPState::initTransitionMatrix / update / gotInfected (src/agentData/dynamicPPState.cpp)
 //   MultiBadMatrix, LengthOfState (src/tools/progressionMatrices/*.cpp)
-//   AgentTypeList::addSchedule, TimeDay, Timehandler (src/agentData/agentType.cpp, src/tools/*.cpp)
+//   AgentTypeList::addSchedule / setStayHome / unsetStayHome, TimeDay, Timehandler
+//                                (src/agentData/agentType.cpp, src/tools/*.cpp)
+//   RuleClosure::init / midnight (include/policies/closurePolicies.h), driven
+//                                through a minimal stand-in of Simulation
 // The per-step and per-day orchestration (simulation.h:899-926, 425-471;
 // movementPolicies.h:1428-1622, 1625-1724; testingPolicies.h:370-475;
 // locationList.h:233-310) is restated here around those calls.
@@ -43,6 +46,11 @@
 #include "progressionType.h"
 #include "movementPolicies.h"
 #include "testingPolicies.h"
+// closurePolicies.h relies on its includer for these
+#include <functional>
+#include "closuresFormat.h"
+#include "locationTypesFormat.h"
+#include "closurePolicies.h"
 
 #include <cfloat>
 #include <cmath>
@@ -603,6 +611,78 @@ void plan(Harness& h, uint32_t t) {
     }
 }
 
+
+// ---------------------------------------------------------------------------
+// RuleClosure driven through a stand-in of Simulation: the members and
+// switches RuleClosure reaches through its CRTP cast (closurePolicies.h:84-471,
+// simulation.h:963-973), backed by the harness state.  Location and agent
+// arrays are copied into the stand-in's containers around each midnight call.
+struct ClosureLocs {
+    thrust::device_vector<float> infectiousness;
+    thrust::device_vector<unsigned> locType;
+    thrust::device_vector<bool> states;
+    thrust::device_vector<uint8_t> essential;
+};
+struct ClosureAgents {
+    thrust::device_vector<unsigned>& location;
+    thrust::device_vector<DynamicPPState>& PPValues;
+    thrust::device_vector<AgentStats> agentStats;
+    AgentTypeList& agentTypes;
+};
+struct ClosureSim : public RuleClosure<ClosureSim> {
+    using TypeOfLocation_t = unsigned;
+    using PPState_t = DynamicPPState;
+    Harness* h = nullptr;
+    ClosureLocs locsStore;
+    ClosureLocs* locs = &locsStore;
+    std::unique_ptr<ClosureAgents> agentsStore;
+    ClosureAgents* agents = nullptr;
+    double currentMaskValue = 1.0;
+    std::vector<float> infectiousnessMultiplier;
+    uint32_t now = 0;
+    // Simulation::toggle* (simulation.h:963-973); the harness keeps curfew
+    // times in steps, which RealMovement::planLocations converts to on its
+    // next call (movementPolicies.h:1440-1444)
+    void toggleCurfew(bool enable, unsigned b, unsigned e) {
+        h->p.enable_curfew = enable;
+        h->p.curfew_begin = b / h->p.time_step;
+        h->p.curfew_end = e / h->p.time_step;
+    }
+    void setSchoolAgeRestriction(unsigned limit) { h->p.school_age_restriction = limit; }
+    void toggleHolidayMode(bool enable) { h->p.holiday_mode = enable; }
+    void toggleQuarantineImmune(bool enable) { h->p.quarantine_immune = enable; }
+    void toggleLockdownNonvacc(bool enable) { h->p.lockdown_nonvacc = enable; }
+    void quarantinePolicy(unsigned qp) { h->p.quarantine_policy = qp; }
+    // DetailedTesting::updateTestingProbs (testingPolicies.h:328-338)
+    void updateTestingProbs(const std::string& probs) {
+        std::vector<double> v = splitStringDouble(probs, ',');
+        double* dst[6] = {&h->p.t_random, &h->p.t_home, &h->p.t_work, &h->p.t_school, &h->p.t_hospital, &h->p.t_nursery};
+        for (size_t q = 0; q < v.size() && q < 6; ++q) *dst[q] = v[q];
+    }
+    Timehandler getSimTime() {
+        Timehandler th(h->p.time_step, 0, Days::MONDAY, 0);
+        for (uint32_t q = 0; q < now; ++q) ++th;
+        return th;
+    }
+    void pull() {
+        const uint32_t L = h->L;
+        locs->infectiousness.assign(h->sl->infectiousness, h->sl->infectiousness + L);
+        locs->locType.assign(h->locType.begin(), h->locType.end());
+        locs->states.resize(L);
+        for (uint32_t j = 0; j < L; ++j) locs->states[j] = h->locStates[j];
+        locs->essential.assign(h->essential.begin(), h->essential.end());
+        agents->agentStats.assign(h->stats.begin(), h->stats.end());
+    }
+    void push() {
+        for (uint32_t j = 0; j < h->L; ++j) {
+            h->sl->infectiousness[j] = locs->infectiousness[j];
+            h->locStates[j] = locs->states[j];
+        }
+        for (uint32_t i = 0; i < h->N; ++i) h->stats[i] = agents->agentStats[i];
+    }
+};
+std::unique_ptr<ClosureSim> g_closure;
+
 }  // namespace
 
 extern "C" {
@@ -743,5 +823,94 @@ void ref_event_minutes(void* hp, uint16_t* start, uint16_t* end, uint16_t* dur) 
 }
 
 int ref_threads(void) { return omp_get_max_threads(); }
+
+// test + progression (the midnight block before the statistics)
+void ref_midnight_pre(void* hp, uint32_t t) {
+    Harness& h = *(Harness*)hp;
+    if (t > 0 && h.p.testing_enabled) testing(h, t);
+    if (t > 0) progress(h, t);
+}
+
+// daily plan, then the variant gate (the midnight block after the rules)
+void ref_plan(void* hp, uint32_t t) {
+    Harness& h = *(Harness*)hp;
+    plan(h, t);
+    count_variants(h);
+}
+
+void ref_get_params(void* hp, psim_params* out) { *out = ((Harness*)hp)->p; }
+
+// RuleClosure::init with the rules given as C-ABI structs
+int ref_closures_init(void* hp, const psim_closure_rule* rules, uint32_t n, const char* header, int enable) {
+    Harness& h = *(Harness*)hp;
+    g_closure.reset(new ClosureSim());
+    ClosureSim& cs = *g_closure;
+    cs.h = &h;
+    cs.agentsStore.reset(new ClosureAgents{h.location, h.pp, {}, h.types});
+    cs.agents = cs.agentsStore.get();
+    cs.infectiousnessMultiplier.assign(h.V, 1.0f);
+    cs.enableClosures = enable ? 1u : 0u;
+    cs.diagnosticLevel = 0;
+    cs.pull();
+    parser::LocationTypes lt{};
+    lt.home = h.p.home_type;
+    parser::ClosureRules cr;
+    for (uint32_t q = 0; q < n; ++q) {
+        parser::ClosureRules::Rule r;
+        r.name = rules[q].name;
+        r.conditionType = rules[q].condition_type;
+        r.threshold = rules[q].threshold;
+        r.threshold2 = rules[q].threshold2;
+        r.parameter = rules[q].parameter;
+        r.closeAfter = rules[q].close_after;
+        r.openAfter = rules[q].open_after;
+        for (uint32_t j = 0; j < rules[q].n_types; ++j) r.locationTypesToClose.push_back(rules[q].types[j]);
+        cr.rules.push_back(r);
+    }
+    try {
+        cs.init(lt, cr, std::string(header));
+    } catch (const std::exception&) {
+        return 1;
+    }
+    return 0;
+}
+
+// RuleClosure::midnight on a statistics row
+void ref_closures_midnight(void* hp, uint32_t t, const uint32_t* row, uint32_t n) {
+    ClosureSim& cs = *g_closure;
+    cs.now = t;
+    std::vector<unsigned> stats(row, row + n);
+    cs.pull();
+    Timehandler th = cs.getSimTime();
+    // ExposeToMutation draws inside a for_each that does not expose the agent
+    // index: one shared stream (tests make those draws outcome-free)
+    psim_stream s;
+    set_stream(&s, *cs.h, 0, t, PSIM_PHASE_EXPOSE);
+    cs.midnight(th, cs.h->p.time_step, stats);
+    harness_rng::current = nullptr;
+    cs.push();
+}
+
+void ref_closures_status(void* hp, uint8_t* active, uint8_t* open, uint32_t* n) {
+    ClosureSim& cs = *g_closure;
+    *n = (uint32_t)cs.rules.size();
+    for (size_t q = 0; q < cs.rules.size(); ++q) {
+        active[q] = cs.rules[q].conditions[0]->active ? 1 : 0;
+        open[q] = cs.rules[q].previousOpenState ? 1 : 0;
+    }
+}
+
+// the schedule table: offsets, then per event type and chance
+uint32_t ref_events(void* hp, uint32_t* offsets, uint32_t* types, float* chance, uint32_t cap) {
+    Harness& h = *(Harness*)hp;
+    for (size_t j = 0; j < h.types.eventOffset.size(); ++j) offsets[j] = h.types.eventOffset[j];
+    const size_t ne = h.types.events.size();
+    for (size_t j = 0; j < ne && j < cap; ++j) {
+        AgentTypeList::Event e = h.types.events[j];
+        types[j] = e.locationType;
+        chance[j] = e.chance;
+    }
+    return (uint32_t)ne;
+}
 
 }  // extern "C"

@@ -78,3 +78,82 @@ def test_pin_csr_matches_stable_sort():
     # of empty locations below the first occupied one unwritten
     first = int(np.min(s.agents["location"]))
     assert np.array_equal(off_o[first + 1:], off_r[first + 1:])
+
+
+def _closure_pin(snap, rules, days, header, enable=True):
+    """oracle + its closure restatement vs the reference harness + the
+    reference's own RuleClosure, fed the same statistics row each midnight."""
+    from oracle import closures as oc
+    s_ref = snap.copy()
+    o = ob.Oracle(snap)
+    r = rb.RefSim(s_ref)
+    eng = oc.OracleClosures(o, rules, header, enable)
+    r.closures_init(rules, header, enable)
+    fired = set()
+    for d in range(days):
+        t0 = d * snap.steps_per_day
+        if t0 > 0 and int(snap.params.get("testing_enabled", 0)):
+            o.test(t0)
+        if t0 > 0:
+            o.progress(t0)
+        r.midnight_pre(t0)
+        row = o.stats(t0)[0]
+        eng.midnight(t0, row)
+        r.closures_midnight(t0, row)
+        a_o, op_o = eng.status()
+        a_r, op_r = r.closures_status()
+        assert np.array_equal(a_o, a_r) and np.array_equal(op_o, op_r), d
+        fired.update(i for i in range(len(a_o)) if a_o[i])
+        p = r.params()
+        for k in ["enable_curfew", "curfew_begin", "curfew_end", "school_age_restriction", "holiday_mode",
+                  "quarantine_policy", "quarantine_immune", "lockdown_nonvacc"]:
+            assert getattr(p, k) == int(snap.params.get(k, 0)), (d, k)
+        for k in ["t_random", "t_home", "t_work", "t_school", "t_hospital"]:
+            assert getattr(p, k) == float(snap.params.get(k, 0.0)), (d, k)
+        ev = r.events()
+        for k in ev:
+            assert np.array_equal(ev[k], snap.model[k]), (d, k)
+        o.plan(t0)
+        r.plan(t0)
+        for s in range(snap.steps_per_day):
+            o.step(t0 + s)
+            r.step(t0 + s)
+        r.sync()
+        assert diff_state(snap, s_ref) == [], "day %d" % d
+    return fired
+
+
+def test_pin_closure_rules_scheduled():
+    from tests.test_closures import SCHEDULED, header
+    snap = small_snapshot(n=6000, locs=1500, initial_infected_frac=0.02, testing=True)
+    fired = _closure_pin(snap, SCHEDULED, 6, header())
+    assert len(fired) == len(SCHEDULED)
+
+
+def test_pin_closure_rules_triggered():
+    from tests.test_closures import TRIGGERED, header
+    # newCasesFraction has no reference counterpart: the reference's init
+    # rejects it, and it is checked against the oracle only
+    rules = [r for r in TRIGGERED if r["conditionType"] != "newCasesFraction"]
+    snap = small_snapshot(n=6000, locs=1500, initial_infected_frac=0.05, quarantine_policy=3, testing=True)
+    fired = _closure_pin(snap, rules, 8, header())
+    assert fired
+
+
+def test_reference_rejects_unknown_condition_type():
+    from tests.test_closures import TRIGGERED, header
+    snap = small_snapshot(n=1000, locs=300)
+    r = rb.RefSim(snap)
+    with pytest.raises(ValueError):
+        r.closures_init([TRIGGERED[0]], header())
+
+
+def test_pin_closure_rules_disabled_and_expose():
+    from tests.test_closures import SCHEDULED, header
+    snap = small_snapshot(n=5000, locs=1200, initial_infected_frac=0.01, n_variants=2)
+    # fraction * s >= 1 makes every exposure certain, so the reference's
+    # single-stream draws inside its for_each cannot change the outcome
+    rules = SCHEDULED + [dict(name="ExposeToMutation", conditionType="afterDays", threshold=1, threshold2=1,
+                              openAfter=1, closeAfter=-1, parameter=1e6, locationTypesToClose=[])]
+    _closure_pin(snap, rules, 3, header(), enable=False)
+    assert (snap.agents["st_variant_mask"] & 2).any()
