@@ -23,6 +23,18 @@ extern int native_mode;
 extern thread_local psim_stream* current;
 extern std::vector<std::mt19937_64> generators;
 void seed_native(unsigned long long seed);
+// the calling thread's stream; threads the harness did not give one (workers
+// of a reference for_each whose draws do not decide anything) use a fixed one
+inline psim_stream* stream() {
+    if (current) return current;
+    thread_local psim_stream fallback;
+    thread_local bool ready = false;
+    if (!ready) {
+        psim_stream_init(&fallback, 0, 0, 0, 0);
+        ready = true;
+    }
+    return &fallback;
+}
 }  // namespace harness_rng
 
 class RandomGenerator {
@@ -34,14 +46,14 @@ public:
             std::uniform_real_distribution<double> dis(0, 1);
             return dis(harness_rng::generators[omp_get_thread_num()]);
         }
-        return psim_u01(harness_rng::current);
+        return psim_u01(harness_rng::stream());
     }
     [[nodiscard]] static double randomReal(double max) {
         if (harness_rng::native_mode) {
             std::uniform_real_distribution<double> dis(0, max);
             return dis(harness_rng::generators[omp_get_thread_num()]);
         }
-        return max * psim_u01(harness_rng::current);
+        return max * psim_u01(harness_rng::stream());
     }
     [[nodiscard]] static unsigned randomUnsigned(unsigned max) {
         if (max == 0) return 0u;
@@ -49,13 +61,13 @@ public:
             std::uniform_int_distribution<unsigned> dis(0, max - 1);
             return dis(harness_rng::generators[omp_get_thread_num()]);
         }
-        return psim_below(harness_rng::current, max);
+        return psim_below(harness_rng::stream(), max);
     }
     [[nodiscard]] static int geometric(double p) {
         if (harness_rng::native_mode) {
             std::geometric_distribution<> dis(p);
             return dis(harness_rng::generators[omp_get_thread_num()]);
         }
-        return psim_geometric(harness_rng::current, psim_geometric_threshold(p));
+        return psim_geometric(harness_rng::stream(), psim_geometric_threshold(p));
     }
 };
