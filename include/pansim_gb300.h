@@ -133,6 +133,12 @@ typedef struct psim_agents {
     uint8_t* st_immunization_count;
     uint8_t* st_infected_count;
     int8_t* st_worst_state;
+    /* immunization (include/immunization.h); each may be NULL */
+    const uint8_t* precond;           /* BasicAgentMeta::preCondIdx; NULL = 0 */
+    uint8_t* imm_round;               /* Immunization::immunizationRound; NULL = 0 */
+    float* symptom_scaling_v;         /* [n_variants * n], variant-major: BasicAgentMeta::scalingSymptoms
+                                         of the states up to 6 (agentMeta.cpp:83-84), which the
+                                         immunization rescales; NULL = symptom_scaling */
 } psim_agents;
 
 /* Locations (include/locationList.h:46-67) [n_locations], cemetery last. */
@@ -293,6 +299,44 @@ int psim_closures_midnight(psim_ctx* ctx, uint32_t t, const psim_day_stats* row)
  * locations/switch are open (previousOpenState); either pointer may be NULL. */
 int psim_closures_status(psim_ctx* ctx, uint8_t* cond_active /* [n_rules] */, uint8_t* rule_open /* [n_rules] */,
                          uint32_t* n_rules);
+/* Immunization (include/immunization.h:24-900): categories, first doses in
+ * category order, booster rounds by age group, and the daily waning of
+ * susceptibility and symptom scaling of susceptible agents.  The location
+ * and per-agent-location types of the categories are the reference's fixed
+ * ids (work entry 4, hospital 12/14, nursery 22, school 3).  A context with
+ * immunization set runs Immunization::update in psim_midnight after the
+ * progression (simulation.h:912) and reports the day's doses in the VAC
+ * column; contexts with more than one replica reject it. */
+#define PSIM_IMM_CATEGORIES 10
+#define PSIM_IMM_MAX_ROUNDS 8
+#define PSIM_IMM_MAX_WEEKS 160
+typedef struct psim_immunization {
+    uint32_t start_after_day;         /* --immunizationStart */
+    uint32_t daily_doses;             /* --immunizationsPerWeek given as a number: that / 7 */
+    uint32_t n_vacc_weeks;            /* > 0: --immunizationsPerWeek given as a file of weekly doses */
+    uint32_t n_booster_rounds;        /* entries of --boosterStart */
+    uint32_t daily_boosters;          /* --boostersPerWeek given as a number: that / 7 */
+    uint32_t pad0;
+    float vacc_per_week[PSIM_IMM_MAX_WEEKS];
+    int32_t booster_start_after_day[PSIM_IMM_MAX_ROUNDS];
+    uint32_t n_booster_weeks[PSIM_IMM_MAX_ROUNDS];   /* 0: daily_boosters */
+    float booster_per_week[PSIM_IMM_MAX_ROUNDS][PSIM_IMM_MAX_WEEKS];
+    float booster_age_percent[PSIM_IMM_MAX_ROUNDS][10];
+    int32_t order[PSIM_IMM_CATEGORIES];              /* --immunizationOrder */
+    float group_level[PSIM_IMM_CATEGORIES];          /* --vaccinationGroupLevel */
+    float protection_infection[10], protection_infection_waning[10];
+    float protection_symptomatic[10], protection_symptomatic_waning[10];
+    float protection_hospitalization[10], protection_hospitalization_waning[10];
+    int32_t variant_similarity[PSIM_MAX_STRAINS];
+    float variant_similar_multiplier[PSIM_MAX_STRAINS];
+} psim_immunization;
+/* Sets the parameters and assigns the categories (Immunization::initCategories,
+ * immunization.h:263-437: one draw per agent and category pass, stream
+ * (agent, 0, IMM_CATEGORY + pass)).  imm == NULL switches immunization off. */
+int psim_immunization_init(psim_ctx* ctx, const psim_immunization* imm);
+/* Immunization::update for the midnight at t (what psim_midnight runs). */
+int psim_immunize_day(psim_ctx* ctx, uint32_t t, uint32_t* immunized_today);
+
 /* The current run parameters (closure rules change curfew, policy, testing
  * probabilities, ...). */
 int psim_get_params(psim_ctx* ctx, psim_params* out);

@@ -54,6 +54,9 @@ def lib():
         L.psim_oracle_midnight.argtypes = [P, U32, P]
         L.psim_oracle_run_day.argtypes = [P, U32, P]
         L.psim_oracle_expose.argtypes = [P, U32, U32, D]
+        L.psim_oracle_immunization_init.argtypes = [P, P]
+        L.psim_oracle_immunize.restype = U32
+        L.psim_oracle_immunize.argtypes = [P, U32]
         L.psim_oracle_csr_offsets.restype = C.POINTER(C.c_uint32)
         L.psim_oracle_csr_offsets.argtypes = [P]
         L.psim_oracle_csr_agents.restype = C.POINTER(C.c_uint32)
@@ -142,6 +145,13 @@ class Oracle:
         out = (cabi.PsimDayStats * self.snap.n_replicas)()
         lib().psim_oracle_run_day(self.h, day, out)
         return out
+
+    def immunization_init(self, imm):
+        self._imm = imm
+        lib().psim_oracle_immunization_init(self.h, C.byref(imm) if imm is not None else None)
+
+    def immunize(self, t):
+        return lib().psim_oracle_immunize(self.h, t)
 
 
 def philox(ctr, key):

@@ -22,6 +22,7 @@
  */
 #include "psim_oracle.h"
 #include "../pansim_gb300/csrc/psim_rng.h"
+#include "../pansim_gb300/csrc/psim_immunity.h"
 #include <stdlib.h>
 #include <string.h>
 #include <math.h>
@@ -52,6 +53,14 @@ struct psim_oracle {
     uint32_t* variant_active; /* [R*V] */
     double* expected;      /* [R] expected infections since the last midnight */
     uint32_t spd;          /* steps per day */
+    /* immunization (include/immunization.h) */
+    int imm_on;
+    psim_immunization imm;
+    psim_imm_tables imm_tab;
+    int imm_groups_ready;
+    float imm_frac[PSIM_IMM_MAX_ROUNDS][10];
+    uint32_t imm_category;   /* Immunization::currentCategory */
+    uint32_t imm_today;      /* immunizedToday */
 };
 
 static inline uint32_t wb_of(const psim_oracle* o, uint32_t i) { return o->m->state_wb[(uint8_t)o->a->state[i]]; }
@@ -597,7 +606,11 @@ void psim_oracle_progress(psim_oracle* o, uint32_t t) {
         uint32_t v = a->variant[i];
         uint32_t st = (uint8_t)a->state[i];
         uint32_t pid = a->prog_id[i];
-        float meta = a->symptom_scaling[i];
+        /* BasicAgentMeta::getScalingSymptoms(v, st), agentMeta.cpp:84: slot
+         * v*7 + max(6, st) -- the per-variant slot 6 up to state 6, the
+         * unscaled value (slot never written) beyond */
+        float meta = (st <= 6u && a->symptom_scaling_v) ? a->symptom_scaling_v[(size_t)v * a->n + i]
+                                                       : a->symptom_scaling[i];
         float prog = (st == 7) ? m->death_scaling[v] / meta : m->prog_scaling[v];
         float scaling = meta * prog;
         int recovered = 0;
@@ -803,7 +816,7 @@ void psim_oracle_stats(psim_oracle* o, uint32_t t, psim_day_stats* out) {
         }
         d->v[n] = stayed - d->v[10] - d->v[11];
         n++;
-        d->v[n++] = 0; /* immunized today */
+        d->v[n++] = o->imm_on ? o->imm_today : 0; /* VAC: immunized today */
         d->v[n++] = ni;
         d->v[n++] = inf_once;
         d->v[n++] = reinf;
@@ -930,6 +943,7 @@ void psim_oracle_plan(psim_oracle* o, uint32_t t) {
 void psim_oracle_midnight(psim_oracle* o, uint32_t t, psim_day_stats* out) {
     if (t > 0 && o->p.testing_enabled) psim_oracle_test(o, t, NULL);
     if (t > 0) psim_oracle_progress(o, t);
+    if (o->imm_on) psim_oracle_immunize(o, t);
     psim_oracle_stats(o, t, out);
     psim_oracle_plan(o, t);
 }
@@ -966,6 +980,198 @@ void psim_oracle_expose(psim_oracle* o, uint32_t t, uint32_t v, double fraction)
             a->st_variant_mask[i] |= 1u << v;
         }
     }
+}
+
+/* ---- Immunization (include/immunization.h:24-900) ---------------------- */
+
+static int imm_has_entry(const psim_oracle* o, uint32_t i, uint32_t pa, uint32_t pb, uint32_t la, uint32_t lb,
+                         int essential) {
+    const psim_agents* a = o->a;
+    for (uint32_t q = a->loc_offset[i]; q < a->loc_offset[i + 1]; ++q) {
+        uint32_t pt = a->poss_type[q];
+        if (pt != pa && pt != pb) continue;
+        uint32_t loc = a->poss_loc[q];
+        if (essential) {
+            if (o->l->essential[loc] == 1) return 1;
+        } else {
+            uint32_t lt = o->l->type[loc];
+            if (lt == la || lt == lb) return 1;
+        }
+    }
+    return 0;
+}
+
+/* the category lambdas of initCategories, immunization.h:277-375 */
+static int imm_in_category(const psim_oracle* o, uint32_t i, uint32_t g) {
+    uint32_t age = o->a->age[i], pre = o->a->precond ? o->a->precond[i] : 0;
+    switch (g) {
+        case 0: return imm_has_entry(o, i, 4, 4, 12, 14, 0);
+        case 1: return imm_has_entry(o, i, 4, 2, 22, 22, 0);
+        case 2: return pre > 0 && age >= 60;
+        case 3: return age >= 60;
+        case 4: return pre > 0 && age >= 18 && age < 60;
+        case 5: return imm_has_entry(o, i, 4, 4, 0, 0, 1);
+        case 6: return imm_has_entry(o, i, 4, 4, 3, 3, 0);
+        case 7: return age > 17 && age < 60;
+        case 8: return age >= 12 && age < 18;
+        default: return age >= 5 && age < 12;
+    }
+}
+
+/* age group of initAgeGroups / the booster passes: [10g, 10g+10), the last [90, 200) */
+static uint32_t imm_age_group(uint32_t age) { return age >= 200u ? 10u : (age >= 90u ? 9u : age / 10u); }
+
+static uint32_t imm_local(const psim_oracle* o, uint32_t i, uint64_t* seed) {
+    uint32_t rep = o->agent_rep[i];
+    *seed = o->r.seed[rep];
+    return i - o->r.agent_offset[rep];
+}
+
+/* Immunization::initializeArgs + initCategories, immunization.h:170-437 */
+void psim_oracle_immunization_init(psim_oracle* o, const psim_immunization* imm) {
+    psim_agents* a = o->a;
+    o->imm_on = imm != NULL;
+    if (!imm) return;
+    o->imm = *imm;
+    psim_imm_make_tables(&o->imm_tab, imm->protection_infection, imm->protection_infection_waning,
+                         imm->protection_symptomatic, imm->protection_symptomatic_waning,
+                         imm->protection_hospitalization, imm->protection_hospitalization_waning,
+                         imm->variant_similarity, imm->variant_similar_multiplier);
+    o->imm_groups_ready = 0;
+    o->imm_category = 0;
+    o->imm_today = 0;
+    for (int v = 1; v <= PSIM_IMM_CATEGORIES; ++v)
+        for (uint32_t g = 0; g < PSIM_IMM_CATEGORIES; ++g) {
+            if (imm->order[g] != v) continue;
+            for (uint32_t i = 0; i < a->n; ++i) {
+                if (a->imm_round[i] != 0 || !imm_in_category(o, i, g)) continue;
+                uint64_t seed;
+                uint32_t li = imm_local(o, i, &seed);
+                double U = psim_u01_once(seed, li, 0, PSIM_PHASE_IMM_CATEGORY + g);
+                a->imm_round[i] = U < (double)imm->group_level[g] ? (uint8_t)imm->order[g] : (uint8_t)255;
+            }
+        }
+}
+
+static uint32_t imm_vaccines_today(const psim_immunization* p, uint32_t t, uint32_t spd) {
+    uint32_t day = t / spd;
+    if (day < p->start_after_day) return 0;
+    if (p->n_vacc_weeks == 0) return p->daily_doses;
+    uint32_t week = (day - p->start_after_day) / 7;
+    return (uint32_t)(p->vacc_per_week[week >= p->n_vacc_weeks ? p->n_vacc_weeks - 1 : week] / 7.0);
+}
+
+static uint32_t imm_boosters_today(const psim_immunization* p, uint32_t t, uint32_t spd, uint32_t r) {
+    uint32_t day = t / spd;
+    if (day < (uint32_t)p->booster_start_after_day[r]) return 0;
+    if (p->n_booster_weeks[r] == 0) return p->daily_boosters;
+    uint32_t week = (day - (uint32_t)p->booster_start_after_day[r]) / 7;
+    return (uint32_t)(p->booster_per_week[r][week >= p->n_booster_weeks[r] ? p->n_booster_weeks[r] - 1 : week] / 7.0);
+}
+
+static int imm_booster_ok(const psim_oracle* o, uint32_t i, uint32_t ts, uint32_t spd) {
+    const psim_agents* a = o->a;
+    return a->st_immunization_ts[i] > 0 && a->st_immunization_count[i] >= 1 &&
+           (ts - a->st_immunization_ts[i]) / spd > 120u && wb_of(o, i) == 0 && ts >= spd * 90u &&
+           a->st_diagnosed_ts[i] < ts - spd * 120u;
+}
+
+static int imm_primary_ok(const psim_oracle* o, uint32_t i, uint32_t ts, uint32_t spd) {
+    const psim_agents* a = o->a;
+    uint32_t d = a->st_diagnosed_ts[i];
+    return a->st_immunization_count[i] == 0 && wb_of(o, i) == 0 &&
+           ((ts < spd * 90u && d == 0) || (ts >= spd * 90u && d < ts - spd * 90u));
+}
+
+/* Immunization::update, immunization.h:481-900 */
+uint32_t psim_oracle_immunize(psim_oracle* o, uint32_t t) {
+    psim_agents* a = o->a;
+    const psim_immunization* p = &o->imm;
+    const uint32_t N = a->n, V = o->m->n_variants, spd = o->spd;
+    if (!o->imm_on) return 0;
+    if (!o->imm_groups_ready) {
+        uint32_t hist[11] = {0};
+        for (uint32_t i = 0; i < N; ++i) hist[imm_age_group(a->age[i])]++;
+        for (uint32_t r = 0; r < p->n_booster_rounds; ++r) {
+            uint32_t size[10], sum = 0;
+            for (int g = 0; g < 10; ++g) {
+                size[g] = (uint32_t)((float)hist[g] * p->booster_age_percent[r][g]);
+                sum += size[g];
+            }
+            for (int g = 0; g < 10; ++g) o->imm_frac[r][g] = (float)size[g] / (float)sum;
+        }
+        o->imm_groups_ready = 1;
+    }
+    uint32_t ts = t == 0 ? 1u : t;
+    /* waning of every susceptible agent */
+    for (uint32_t i = 0; i < N; ++i) {
+        if (a->state[i] != 0) continue;
+        float susc[PSIM_MAX_STRAINS], scale[PSIM_MAX_STRAINS];
+        uint8_t set[PSIM_MAX_STRAINS];
+        uint32_t wi = (ts - a->st_infected_ts[i]) / (7u * spd);
+        uint32_t wv = (ts - a->st_immunization_ts[i]) / (7u * spd);
+        psim_imm_wane(&o->imm_tab, V, a->st_infected_count[i], a->st_immunization_count[i], wi, wv,
+                      a->st_variant_mask[i], susc, scale, set);
+        for (uint32_t v = 0; v < V; ++v) {
+            if (set[v]) a->symptom_scaling_v[(size_t)v * N + i] = a->symptom_scaling[i] * scale[v];
+            a->susceptible[(size_t)v * N + i] = susc[v];
+        }
+    }
+    /* booster rounds */
+    for (uint32_t r = 0; r < p->n_booster_rounds; ++r) {
+        uint32_t available = imm_boosters_today(p, t, spd, r);
+        if (!available) continue;
+        uint32_t counts[11] = {0};
+        for (uint32_t i = 0; i < N; ++i)
+            if (imm_booster_ok(o, i, ts, spd)) counts[imm_age_group(a->age[i])]++;
+        for (uint32_t g = 0; g < 10; ++g) {
+            uint32_t avail_g = (uint32_t)((float)available * o->imm_frac[r][g]);
+            float prob = counts[g] < avail_g ? 1.0f : (float)avail_g / (float)counts[g];
+            for (uint32_t i = 0; i < N; ++i) {
+                if (imm_age_group(a->age[i]) != g || !imm_booster_ok(o, i, ts, spd)) continue;
+                int give = prob == 1.0f;
+                if (!give) {
+                    uint64_t seed;
+                    uint32_t li = imm_local(o, i, &seed);
+                    give = psim_u01_once(seed, li, ts, PSIM_PHASE_IMM_BOOSTER + r) < (double)prob;
+                }
+                if (give) {
+                    a->st_immunization_ts[i] = ts;
+                    a->st_immunization_count[i]++;
+                }
+            }
+        }
+    }
+    /* first doses in category order */
+    uint32_t available = imm_vaccines_today(p, t, spd);
+    while (available > 0 && o->imm_category < PSIM_IMM_CATEGORIES) {
+        uint32_t count = 0;
+        while (count == 0 && o->imm_category <= PSIM_IMM_CATEGORIES) {
+            uint32_t cc = o->imm_category + 1;
+            for (uint32_t i = 0; i < N; ++i)
+                if ((a->imm_round[i] == cc || cc == PSIM_IMM_CATEGORIES + 1) && imm_primary_ok(o, i, ts, spd)) count++;
+            if (count == 0) o->imm_category++;
+        }
+        float prob = count < available ? 1.0f : (float)available / (float)count;
+        uint32_t cc = o->imm_category + 1;
+        for (uint32_t i = 0; i < N; ++i) {
+            if (a->imm_round[i] != cc || !imm_primary_ok(o, i, ts, spd)) continue;
+            int give = prob == 1.0f;
+            if (!give) {
+                uint64_t seed;
+                uint32_t li = imm_local(o, i, &seed);
+                give = psim_u01_once(seed, li, ts, PSIM_PHASE_IMM_PRIMARY + o->imm_category) < (double)prob;
+            }
+            if (give) {
+                a->st_immunization_ts[i] = ts;
+                a->st_immunization_count[i] = 1;
+            }
+        }
+        available -= count < available ? count : available;
+    }
+    o->imm_today = 0;
+    for (uint32_t i = 0; i < N; ++i) o->imm_today += a->st_immunization_ts[i] == ts;
+    return o->imm_today;
 }
 
 /* Simulation::flagHealthcareWorkers, simulation.h:670-693 */

@@ -36,6 +36,10 @@ def lib():
         L.ref_closures_init.argtypes = [P, P, U32, C.c_char_p, C.c_int]
         L.ref_closures_midnight.argtypes = [P, U32, P, U32]
         L.ref_closures_status.argtypes = [P, P, P, P]
+        L.ref_immunization_init.restype = C.c_int
+        L.ref_immunization_init.argtypes = [P, P, C.c_char_p]
+        L.ref_immunize.restype = U32
+        L.ref_immunize.argtypes = [P, U32]
         L.ref_events.restype = U32
         L.ref_events.argtypes = [P, P, P, P, U32]
         _lib = L
@@ -148,3 +152,12 @@ class RefSim:
         lib().ref_event_minutes(self.h, _p(s), _p(e), _p(d))
         return dict(event_offset=off, ev_loc_type=ty[:n], ev_chance=ch[:n], ev_start=s[:n], ev_end=e[:n],
                     ev_duration=d[:n])
+
+    # immunization through the reference's Immunization
+    def immunization_init(self, imm, workdir):
+        self._imm = imm
+        if lib().ref_immunization_init(self.h, C.byref(imm), str(workdir).encode()):
+            raise ValueError("reference Immunization::initializeArgs threw")
+
+    def immunize(self, t):
+        return lib().ref_immunize(self.h, t)

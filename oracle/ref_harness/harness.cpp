@@ -51,6 +51,7 @@
 #include "closuresFormat.h"
 #include "locationTypesFormat.h"
 #include "closurePolicies.h"
+#include "immunization.h"
 
 #include <cfloat>
 #include <cmath>
@@ -288,6 +289,11 @@ void init_meta(Harness& h) {
         std::memcpy(&mir, (const void*)&bm, sizeof(mir));
         for (int j = 0; j < 7 * MAX_STRAINS; ++j) mir.scalingSymptoms[j] = h.sa->symptom_scaling[i];
         mir.scalingAgeSex = h.sa->symptom_scaling[i];
+        // slot v*7+6: the per-variant scaling the immunization rewrites
+        if (h.sa->symptom_scaling_v)
+            for (uint32_t v = 0; v < h.m->n_variants; ++v)
+                mir.scalingSymptoms[v * 7 + 6] = h.sa->symptom_scaling_v[(size_t)v * h.N + i];
+        mir.preCondIdx = h.sa->precond ? h.sa->precond[i] : 0;
         std::memcpy((void*)&bm, &mir, sizeof(mir));
         h.meta.push_back(bm);
     }
@@ -683,6 +689,61 @@ struct ClosureSim : public RuleClosure<ClosureSim> {
 };
 std::unique_ptr<ClosureSim> g_closure;
 
+// ---------------------------------------------------------------------------
+// Immunization driven through a stand-in of Simulation (the members
+// Immunization reaches through its `sim` pointer, immunization.h:25-900),
+// with the harness state copied in and out around each call.
+struct ImmAgents {
+    thrust::device_vector<DynamicPPState>& PPValues;
+    thrust::device_vector<AgentStats> agentStats;
+    thrust::device_vector<BasicAgentMeta> agentMetaData;
+    thrust::device_vector<unsigned long> locationOffset;
+    thrust::device_vector<unsigned> possibleTypes, possibleLocations;
+};
+struct ImmLocs {
+    thrust::device_vector<unsigned> locType;
+    thrust::device_vector<uint8_t> essential;
+};
+struct ImmSim {
+    using PPState_t = DynamicPPState;
+    using AgentMeta_t = BasicAgentMeta;
+    ImmAgents* agents = nullptr;
+    ImmLocs* locs = nullptr;
+    std::vector<float> infectiousnessMultiplier;
+};
+struct ImmHarness {
+    Harness* h = nullptr;
+    std::unique_ptr<ImmAgents> agents;
+    ImmLocs locs;
+    ImmSim sim;
+    std::unique_ptr<Immunization<ImmSim>> imm;
+    void pull() {
+        agents->agentStats.assign(h->stats.begin(), h->stats.end());
+        agents->agentMetaData.assign(h->meta.begin(), h->meta.end());
+    }
+    void push() {
+        for (uint32_t i = 0; i < h->N; ++i) {
+            h->stats[i] = agents->agentStats[i];
+            h->meta[i] = agents->agentMetaData[i];
+        }
+    }
+};
+std::unique_ptr<ImmHarness> g_imm;
+std::string join_floats(const float* v, int n) {
+    std::string s;
+    char buf[64];
+    for (int q = 0; q < n; ++q) {
+        std::snprintf(buf, sizeof(buf), "%.9g", (double)v[q]);
+        s += (q ? "," : "") + std::string(buf);
+    }
+    return s;
+}
+std::string join_ints(const int32_t* v, int n) {
+    std::string s;
+    for (int q = 0; q < n; ++q) s += (q ? "," : "") + std::to_string(v[q]);
+    return s;
+}
+
 }  // namespace
 
 extern "C" {
@@ -797,6 +858,11 @@ void ref_sync_out(void* hp) {
         a->stayed_home[i] = h.stayedHome[i] ? 1 : 0;
         a->no_work[i] = h.noWorkAgent[i];
         a->last_test[i] = h.lastTest[i];
+        if (a->symptom_scaling_v) {
+            MetaMirror mir;
+            std::memcpy(&mir, (const void*)&h.meta[i], sizeof(mir));
+            for (uint32_t v = 0; v < h.m->n_variants; ++v) a->symptom_scaling_v[(size_t)v * h.N + i] = mir.scalingSymptoms[v * 7 + 6];
+        }
     }
     for (uint32_t j = 0; j < h.L; ++j) {
         h.sl->closed_until[j] = h.closedUntil[j];
@@ -898,6 +964,80 @@ void ref_closures_status(void* hp, uint8_t* active, uint8_t* open, uint32_t* n) 
         active[q] = cs.rules[q].conditions[0]->active ? 1 : 0;
         open[q] = cs.rules[q].previousOpenState ? 1 : 0;
     }
+}
+
+// Immunization::initializeArgs (options given as the reference's strings; the
+// weekly schedules as files under `dir`) + initCategories
+int ref_immunization_init(void* hp, const psim_immunization* p, const char* dir) {
+    Harness& h = *(Harness*)hp;
+    g_imm.reset(new ImmHarness());
+    ImmHarness& ih = *g_imm;
+    ih.h = &h;
+    ih.agents.reset(new ImmAgents{h.pp, {}, {}, {}, {}, {}});
+    ih.agents->locationOffset.assign(h.locOffset.begin(), h.locOffset.end());
+    ih.agents->possibleTypes.assign(h.possType.begin(), h.possType.end());
+    ih.agents->possibleLocations.assign(h.possLoc.begin(), h.possLoc.end());
+    ih.locs.locType.assign(h.locType.begin(), h.locType.end());
+    ih.locs.essential.assign(h.essential.begin(), h.essential.end());
+    ih.sim.agents = ih.agents.get();
+    ih.sim.locs = &ih.locs;
+    ih.sim.infectiousnessMultiplier.assign(h.V, 1.0f);
+    cxxopts::ParseResult r;
+    const std::string d(dir);
+    r.values["immunizationStart"] = std::to_string(p->start_after_day);
+    std::string bs;
+    for (uint32_t q = 0; q < p->n_booster_rounds; ++q) bs += (q ? "," : "") + std::to_string(p->booster_start_after_day[q]);
+    r.values["boosterStart"] = bs;
+    if (p->n_vacc_weeks) {
+        std::ofstream f(d + "/vacc.txt");
+        f << join_floats(p->vacc_per_week, (int)p->n_vacc_weeks);
+        r.values["immunizationsPerWeek"] = d + "/vacc.txt";
+    } else {
+        r.values["immunizationsPerWeek"] = std::to_string(p->daily_doses * 7u);
+    }
+    {
+        std::ofstream f(d + "/booster.txt");
+        for (uint32_t q = 0; q < p->n_booster_rounds; ++q) {
+            f << join_floats(p->booster_per_week[q], (int)p->n_booster_weeks[q]) << '\n';
+            f << join_floats(p->booster_age_percent[q], 10) << '\n';
+        }
+        r.values["boostersPerWeek"] = d + "/booster.txt";
+    }
+    r.values["immunizationOrder"] = join_ints(p->order, 10);
+    r.values["vaccinationGroupLevel"] = join_floats(p->group_level, 10);
+    r.values["protectionInfection"] = join_floats(p->protection_infection, 10);
+    r.values["protectionInfectionWaning"] = join_floats(p->protection_infection_waning, 10);
+    r.values["protectionSymptomatic"] = join_floats(p->protection_symptomatic, 10);
+    r.values["protectionSymptomaticWaning"] = join_floats(p->protection_symptomatic_waning, 10);
+    r.values["protectionHospitalization"] = join_floats(p->protection_hospitalization, 10);
+    r.values["protectionHospitalizationWaning"] = join_floats(p->protection_hospitalization_waning, 10);
+    r.values["variantSimilarity"] = join_ints(p->variant_similarity, PSIM_MAX_STRAINS);
+    r.values["variantSimilarMultiplier"] = join_floats(p->variant_similar_multiplier, PSIM_MAX_STRAINS);
+    r.values["diags"] = "0";
+    ih.imm.reset(new Immunization<ImmSim>(&ih.sim));
+    try {
+        ih.imm->initializeArgs(r);
+        ih.pull();
+        ih.imm->initCategories();
+        ih.push();
+    } catch (const std::exception&) {
+        return 1;
+    }
+    return 0;
+}
+
+// Immunization::update at the midnight t; returns immunizedToday
+uint32_t ref_immunize(void* hp, uint32_t t) {
+    ImmHarness& ih = *g_imm;
+    ih.pull();
+    Timehandler th(ih.h->p.time_step, 0, Days::MONDAY, 0);
+    for (uint32_t q = 0; q < t; ++q) ++th;
+    psim_stream s;
+    set_stream(&s, *ih.h, 0, t, PSIM_PHASE_IMMUNIZE);
+    ih.imm->update(th, ih.h->p.time_step);
+    harness_rng::current = nullptr;
+    ih.push();
+    return ih.imm->immunizedToday;
 }
 
 // the schedule table: offsets, then per event type and chance

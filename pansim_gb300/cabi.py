@@ -35,7 +35,7 @@ AGENT_PTR_FIELDS = [
     "st_infected_ts", "st_infected_loc", "st_worst_ts", "st_worst_end_ts", "st_diagnosed_ts",
     "st_quarantined_ts", "st_quarantined_until", "st_days_in_quarantine", "st_hospitalized_ts",
     "st_hospitalized_until", "st_immunization_ts", "st_recovered_ts", "st_variant_mask",
-    "st_immunization_count", "st_infected_count", "st_worst_state",
+    "st_immunization_count", "st_infected_count", "st_worst_state", "precond", "imm_round", "symptom_scaling_v",
 ]
 
 
@@ -83,6 +83,28 @@ class PsimDayStats(C.Structure):
 class PsimTuning(C.Structure):
     _fields_ = [("agg_count", C.c_uint32), ("agg_slot", C.c_uint32), ("blocks_per_sm", C.c_uint32),
                 ("variant", C.c_uint32)]
+
+
+PSIM_IMM_CATEGORIES = 10
+PSIM_IMM_MAX_ROUNDS = 8
+PSIM_IMM_MAX_WEEKS = 160
+
+
+class PsimImmunization(C.Structure):
+    _fields_ = [("start_after_day", C.c_uint32), ("daily_doses", C.c_uint32), ("n_vacc_weeks", C.c_uint32),
+                ("n_booster_rounds", C.c_uint32), ("daily_boosters", C.c_uint32), ("pad0", C.c_uint32),
+                ("vacc_per_week", C.c_float * PSIM_IMM_MAX_WEEKS),
+                ("booster_start_after_day", C.c_int32 * PSIM_IMM_MAX_ROUNDS),
+                ("n_booster_weeks", C.c_uint32 * PSIM_IMM_MAX_ROUNDS),
+                ("booster_per_week", (C.c_float * PSIM_IMM_MAX_WEEKS) * PSIM_IMM_MAX_ROUNDS),
+                ("booster_age_percent", (C.c_float * 10) * PSIM_IMM_MAX_ROUNDS),
+                ("order", C.c_int32 * PSIM_IMM_CATEGORIES), ("group_level", C.c_float * PSIM_IMM_CATEGORIES),
+                ("protection_infection", C.c_float * 10), ("protection_infection_waning", C.c_float * 10),
+                ("protection_symptomatic", C.c_float * 10), ("protection_symptomatic_waning", C.c_float * 10),
+                ("protection_hospitalization", C.c_float * 10),
+                ("protection_hospitalization_waning", C.c_float * 10),
+                ("variant_similarity", C.c_int32 * PSIM_MAX_STRAINS),
+                ("variant_similar_multiplier", C.c_float * PSIM_MAX_STRAINS)]
 
 
 PSIM_CLOSURE_MAX_TYPES = 10

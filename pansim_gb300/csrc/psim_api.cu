@@ -164,6 +164,18 @@ int upload_mutable(psim_ctx* c, const psim_agents* a, const psim_locations* l) {
     UP(st_hospitalized_until, N) UP(st_immunization_ts, N) UP(st_recovered_ts, N) UP(st_variant_mask, N)
     UP(st_immunization_count, N) UP(st_infected_count, N) UP(st_worst_state, N)
 #undef UP
+    // optional immunization fields: neutral values when absent
+    if (a->imm_round) {
+        if ((rc = dcopy_in(c, d.imm_round, a->imm_round, N))) return rc;
+    } else {
+        CK(cudaMemsetAsync(d.imm_round, 0, N, c->stream));
+    }
+    if (a->symptom_scaling_v) {
+        if ((rc = dcopy_in(c, d.scaling_v, a->symptom_scaling_v, N * c->V))) return rc;
+    } else {
+        for (uint32_t v = 0; v < c->V; ++v)
+            CK(cudaMemcpyAsync(d.scaling_v + (size_t)v * N, d.symptom_scaling, 4 * N, cudaMemcpyDeviceToDevice, c->stream));
+    }
     DevLocs& dl = c->k.l;
     if ((rc = dcopy_in(c, dl.infectiousness, l->infectiousness, L))) return rc;
     if ((rc = dcopy_in(c, dl.open, l->open, L))) return rc;
@@ -263,7 +275,7 @@ void assemble_stats(psim_ctx* c, uint32_t t, psim_day_stats* out) {
         }
         d.v[n] = a.c[SC_STAYED] - d.v[10] - d.v[11];
         n++;
-        d.v[n++] = 0u;  // immunized today
+        d.v[n++] = immunized_today(c);  // VAC: immunized today
         d.v[n++] = a.c[SC_NI];
         d.v[n++] = a.c[SC_INF_ONCE];
         d.v[n++] = a.c[SC_REINF];
@@ -406,6 +418,13 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     UPA(type, N) UPA(age, N) UPA(band, N) UPA(prog_id, N) UPA(symptom_scaling, N) UPA(loc_offset, N + 1)
     UPA(poss_loc, c->n_poss) UPA(poss_type, c->n_poss)
 #undef UPA
+    if (a->precond) {
+        if ((rc = dupload(c, &da.precond, a->precond, N))) return bail(rc);
+    } else {
+        uint8_t* z = nullptr;
+        if ((rc = dalloc(c, &z, N))) return bail(rc);
+        da.precond = z;
+    }
     if ((rc = dupload(c, &da.rep, arep.data(), N))) return bail(rc);
 #define AL(field, cnt) \
     if ((rc = dalloc(c, &da.field, cnt))) return bail(rc);
@@ -415,7 +434,7 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     AL(st_quarantined_ts, N) AL(st_quarantined_until, N) AL(st_days_in_quarantine, N) AL(st_hospitalized_ts, N)
     AL(st_hospitalized_until, N) AL(st_immunization_ts, N) AL(st_recovered_ts, N) AL(st_variant_mask, N)
     AL(st_immunization_count, N) AL(st_infected_count, N) AL(st_worst_state, N) AL(hcw, N) AL(rank, N)
-    AL(worklist, N) AL(work_count, 1)
+    AL(worklist, N) AL(work_count, 1) AL(imm_round, N) AL(scaling_v, (size_t)N * V)
 #undef AL
     // locations
     DevLocs& dl = k.l;
@@ -483,7 +502,7 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
         add(a2.st_quarantined_until, 4 * N); add(a2.st_days_in_quarantine, 4 * N); add(a2.st_hospitalized_ts, 4 * N);
         add(a2.st_hospitalized_until, 4 * N); add(a2.st_immunization_ts, 4 * N); add(a2.st_recovered_ts, 4 * N);
         add(a2.st_variant_mask, 4 * N); add(a2.st_immunization_count, N); add(a2.st_infected_count, N);
-        add(a2.st_worst_state, N);
+        add(a2.st_worst_state, N); add(a2.imm_round, N); add(a2.scaling_v, 4 * N * V);
         add(dl.infectiousness, 4 * L); add(dl.open, L); add(dl.closed_until, 4 * L); add(dl.quarantine_until, 4 * L);
         add(dr.variant_active, R * V); add(dr.expected, 8 * R);
     }
@@ -521,6 +540,7 @@ int psim_destroy(psim_ctx* c) {
     if (!c) return 0;
     if (c->stream) cudaStreamSynchronize(c->stream);
     closures_free(c);
+    immunization_free(c);
     for (auto& kv : c->checkpoints)
         if (kv.second) cudaFree(kv.second);
     if (c->day_graph) cudaGraphExecDestroy(c->day_graph);
@@ -555,8 +575,10 @@ int psim_download(psim_ctx* c, psim_agents* a, psim_locations* l) {
     DN(st_infected_ts, N) DN(st_infected_loc, N) DN(st_worst_ts, N) DN(st_worst_end_ts, N) DN(st_diagnosed_ts, N)
     DN(st_quarantined_ts, N) DN(st_quarantined_until, N) DN(st_days_in_quarantine, N) DN(st_hospitalized_ts, N)
     DN(st_hospitalized_until, N) DN(st_immunization_ts, N) DN(st_recovered_ts, N) DN(st_variant_mask, N)
-    DN(st_immunization_count, N) DN(st_infected_count, N) DN(st_worst_state, N)
+    DN(st_immunization_count, N) DN(st_infected_count, N) DN(st_worst_state, N) DN(imm_round, N)
 #undef DN
+    if (a->symptom_scaling_v)
+        CK(cudaMemcpyAsync(a->symptom_scaling_v, d.scaling_v, 4 * N * c->V, cudaMemcpyDeviceToHost, c->stream));
     const DevLocs& dl = c->k.l;
     if (l->infectiousness) CK(cudaMemcpyAsync(l->infectiousness, dl.infectiousness, L * 4, cudaMemcpyDeviceToHost, c->stream));
     if (l->open) CK(cudaMemcpyAsync(l->open, dl.open, L, cudaMemcpyDeviceToHost, c->stream));
@@ -849,6 +871,7 @@ int psim_midnight(psim_ctx* c, uint32_t t, psim_day_stats* out) {
         launch_progress(c->k, t, c->stream);
         c->launches += 1;
     }
+    if (c->immunization && (rc = immunization_apply(c, t))) return rc;
     if (c->closures) {
         // the rules read replica 0's row even when the caller passes no buffer
         std::vector<psim_day_stats> rows(c->R);

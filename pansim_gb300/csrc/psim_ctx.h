@@ -79,6 +79,11 @@ inline int fail(psim_ctx* c, int code, const std::string& msg) {
             return fail(c, PSIM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));        \
     } while (0)
 
+// immunization (psim_immunization.cu)
+void immunization_free(psim_ctx* c);
+int immunization_apply(psim_ctx* c, uint32_t t);
+uint32_t immunized_today(const psim_ctx* c);
+
 // closure rules (psim_closures.cu)
 void closures_free(psim_ctx* c);
 int closures_apply(psim_ctx* c, uint32_t t, const psim_day_stats* row);

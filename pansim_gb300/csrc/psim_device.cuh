@@ -86,6 +86,9 @@ struct DevAgents {
     uint8_t* st_immunization_count;
     uint8_t* st_infected_count;
     int8_t* st_worst_state;
+    const uint8_t* precond;       // pre-condition index (immunization categories)
+    uint8_t* imm_round;           // immunization category round (0 = unassigned, 255 = declined)
+    float* scaling_v;             // [V*N] symptom scaling of the states up to 6, per variant
     uint8_t* hcw;                 // healthcare worker flag
     uint32_t* rank;               // scratch of the canonical CSR ordering
     uint32_t* worklist;           // agents queued for the cold half of a step (hot/cold variant)

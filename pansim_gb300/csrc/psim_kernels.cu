@@ -964,7 +964,9 @@ __global__ void __launch_bounds__(256) k_progress(KArgs k, uint32_t t, int stage
         const uint32_t v = k.a.variant[i];
         const uint32_t st = (uint8_t)k.a.state[i];
         const uint32_t pid = k.a.prog_id[i];
-        const float meta = k.a.symptom_scaling[i];
+        // BasicAgentMeta::getScalingSymptoms(v, st) reads slot v*7 + max(6, st):
+        // the per-variant slot 6 for states up to 6, the unscaled value beyond
+        const float meta = st <= 6u ? k.a.scaling_v[(size_t)v * k.a.n + i] : k.a.symptom_scaling[i];
         const float prog = (st == 7) ? k.m.death_scaling[v] / meta : k.m.prog_scaling[v];
         const float scaling = meta * prog;
         if (days == -2) {

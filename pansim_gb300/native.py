@@ -61,6 +61,8 @@ def lib(auto_build=True):
         L.psim_closures_midnight.argtypes = [P, U32, P]
         L.psim_closures_status.argtypes = [P, P, P, P]
         L.psim_get_params.argtypes = [P, P]
+        L.psim_immunization_init.argtypes = [P, P]
+        L.psim_immunize_day.argtypes = [P, U32, P]
         L.psim_get_events.argtypes = [P, P, P, P, P, P, P, U32, P]
         L.psim_day_kernel_ms.argtypes = [P, C.c_void_p]
         L.psim_launch_count.argtypes = [P, C.POINTER(C.c_uint64)]
@@ -226,6 +228,18 @@ class GpuSim:
         op = np.zeros(max(n.value, 1), np.uint8)
         self._ck(lib().psim_closures_status(self.h, _p(act), _p(op), C.byref(n)), "closures_status")
         return act[: n.value].astype(bool), op[: n.value].astype(bool)
+
+    # immunization
+    def immunization_init(self, imm):
+        """imm: cabi.PsimImmunization (pansim_gb300.immunization.options) or None."""
+        self._imm = imm
+        self._ck(lib().psim_immunization_init(self.h, C.byref(imm) if imm is not None else None),
+                 "immunization_init")
+
+    def immunize(self, t):
+        n = C.c_uint32(0)
+        self._ck(lib().psim_immunize_day(self.h, t, C.byref(n)), "immunize")
+        return n.value
 
     def get_params(self):
         p = cabi.PsimParams()

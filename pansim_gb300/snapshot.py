@@ -28,6 +28,7 @@ AGENT_DTYPES = {
     "st_hospitalized_ts": np.uint32, "st_hospitalized_until": np.uint32,
     "st_immunization_ts": np.uint32, "st_recovered_ts": np.uint32, "st_variant_mask": np.uint32,
     "st_immunization_count": np.uint8, "st_infected_count": np.uint8, "st_worst_state": np.int8,
+    "precond": np.uint8, "imm_round": np.uint8, "symptom_scaling_v": np.float32,
 }
 AGENT_MUTABLE = [
     "location", "steps_until_move", "state", "days", "variant", "infectious", "susceptible",
@@ -35,7 +36,7 @@ AGENT_MUTABLE = [
     "st_infected_ts", "st_infected_loc", "st_worst_ts", "st_worst_end_ts", "st_diagnosed_ts",
     "st_quarantined_ts", "st_quarantined_until", "st_days_in_quarantine", "st_hospitalized_ts",
     "st_hospitalized_until", "st_immunization_ts", "st_recovered_ts", "st_variant_mask",
-    "st_immunization_count", "st_infected_count", "st_worst_state",
+    "st_immunization_count", "st_infected_count", "st_worst_state", "imm_round", "symptom_scaling_v",
 ]
 LOC_DTYPES = {
     "type": np.uint8, "infectiousness": np.float32, "open": np.uint8, "essential": np.uint8,
@@ -86,6 +87,15 @@ class Snapshot:
         self._normalize()
 
     def _normalize(self):
+        # immunization fields absent from older snapshots: their neutral values
+        n = len(self.agents["location"])
+        V = int(self.model["n_variants"])
+        if "precond" not in self.agents:
+            self.agents["precond"] = np.zeros(n, np.uint8)
+        if "imm_round" not in self.agents:
+            self.agents["imm_round"] = np.zeros(n, np.uint8)
+        if "symptom_scaling_v" not in self.agents:
+            self.agents["symptom_scaling_v"] = np.tile(np.asarray(self.agents["symptom_scaling"], np.float32), V)
         for k, dt in AGENT_DTYPES.items():
             self.agents[k] = np.ascontiguousarray(self.agents[k], dtype=dt)
         for k, dt in LOC_DTYPES.items():
@@ -234,7 +244,7 @@ def concat(snaps, seeds, ks):
             parts.append(x)
         if k == "loc_offset":
             parts.append(np.array([sum(len(q.agents["poss_loc"]) for q in snaps)], np.uint32))
-        if k == "susceptible":
+        if k in ("susceptible", "symptom_scaling_v"):
             V = int(base.model["n_variants"])
             parts = [np.concatenate([s.agents[k].reshape(V, -1)[v] for s in snaps]) for v in range(V)]
         agents[k] = np.concatenate(parts).astype(AGENT_DTYPES[k])

@@ -157,3 +157,42 @@ def test_pin_closure_rules_disabled_and_expose():
                               openAfter=1, closeAfter=-1, parameter=1e6, locationTypesToClose=[])]
     _closure_pin(snap, rules, 3, header(), enable=False)
     assert (snap.agents["st_variant_mask"] & 2).any()
+
+
+def test_pin_immunization(tmp_path):
+    """oracle vs the reference's Immunization (categories, waning, boosters,
+    first doses) with group levels of 0 or 1 and budgets that cover every
+    eligible agent, so no draw decides anything and the reference's shared
+    stream inside its for_each cannot matter."""
+    from tests.test_immunization import DAY0, history_snapshot, random_options
+    snap = history_snapshot(n=6000, locs=1500)
+    s_ref = snap.copy()
+    o = ob.Oracle(snap)
+    r = rb.RefSim(s_ref)
+    opt = random_options(levels="1,0,1,1,0,1,1,0,1,1", doses=7_000_000, boosters=7_000_000)
+    o.immunization_init(opt)
+    r.immunization_init(opt, tmp_path)
+    r.sync()
+    assert diff_state(snap, s_ref, fields=["symptom_scaling_v", "st_immunization_ts"]) == []
+    doses = 0
+    for d in range(DAY0, DAY0 + 4):
+        t0 = d * snap.steps_per_day
+        o.progress(t0)
+        r.midnight_pre(t0)
+        n_o = o.immunize(t0)
+        n_r = r.immunize(t0)
+        assert n_o == n_r, d
+        doses += n_o
+        o.plan(t0)
+        r.plan(t0)
+        for s in range(snap.steps_per_day):
+            o.step(t0 + s)
+            r.step(t0 + s)
+        r.sync()
+        bad = [k for k in diff_state(snap, s_ref) if not k.startswith("imm_round")]
+        assert bad == [], "day %d" % d
+    assert doses > 0
+    assert (snap.agents["st_immunization_count"] >= 2).any()
+    s0 = snap.agents["state"] == 0
+    su = snap.agents["susceptible"].reshape(2, -1)
+    assert (su[:, s0] < 1.0).any()  # waning protection applied
