@@ -223,7 +223,8 @@ typedef struct psim_tuning {
     uint32_t agg_slot;       /* warp-aggregated CSR slot atomics */
     uint32_t blocks_per_sm;  /* 256-thread blocks per SM of the per-agent kernels; 0 = occupancy */
     uint32_t variant;        /* fused step kernel: 0/1/2 = one kernel capped at 64/40/32
-                                registers, 3 = hot/cold split */
+                                registers, 3 = hot/cold split, 4/5 = 2/4 agents per
+                                thread in flight (plain slot atomics) */
 } psim_tuning;
 
 typedef struct psim_ctx psim_ctx;

@@ -15,13 +15,13 @@ import itertools
 import numpy as np
 
 DEFAULT_GRID = [0, 4, 8, 16]
-DEFAULT_VARIANTS = [0, 1, 2, 3]
+DEFAULT_VARIANTS = [0, 1, 2, 3, 4, 5]
 LARGE_AGENTS = 8_000_000
 
 
 def candidates(grid=None, variants=None):
-    """variant: register cap of the fused kernel (64 / 40 / 32 registers) or
-    3 = hot/cold split;
+    """variant: register cap of the fused kernel (64 / 40 / 32 registers),
+    3 = hot/cold split, 4 / 5 = 2 / 4 agents per thread in flight;
     blocks_per_sm 0 = one occupancy wave of that variant."""
     for variant, agg_count, agg_slot, bps in itertools.product(variants or DEFAULT_VARIANTS, [1, 0], [1, 0],
                                                                grid or DEFAULT_GRID):
@@ -39,7 +39,7 @@ def autotune(sim, day, reps=2, grid=None, variants=None, verbose=False):
     set and one repetition (a day there takes a good fraction of a second)."""
     if sim.snap.n_agents > LARGE_AGENTS:
         grid = grid or [0, 16]
-        variants = variants or [0, 3]
+        variants = variants or [0, 5]
         reps = 1
     spd = sim.snap.steps_per_day
     sim.checkpoint_save(TUNE_SLOT)

@@ -626,7 +626,7 @@ int psim_set_tuning(psim_ctx* c, const psim_tuning* t) {
     c->k.tune.agg_count = t->agg_count ? 1u : 0u;
     c->k.tune.agg_slot = t->agg_slot ? 1u : 0u;
     c->k.tune.blocks_per_sm = t->blocks_per_sm;
-    if (t->variant > 3) return fail(c, PSIM_ERR_ARG, "variant out of range");
+    if (t->variant > 5) return fail(c, PSIM_ERR_ARG, "variant out of range");
     c->k.tune.variant = t->variant;
     c->graph_dirty = true;
     return 0;

@@ -152,7 +152,8 @@ struct DevTune {
     uint32_t agg_slot;       // warp-aggregate the CSR slot atomics
     uint32_t blocks_per_sm;  // grid of the per-agent kernels (0 = one occupancy wave)
     uint32_t variant;        // fused step kernel: 0/1/2 = one kernel capped at 64/40/32 registers,
-                             // 3 = hot/cold split (lean kernel + queued cold agents)
+                             // 3 = hot/cold split (lean kernel + queued cold agents),
+                             // 4/5 = 2/4 agents per thread in flight
 };
 
 // Adjoint accumulation (gradient of the expected new infections with respect

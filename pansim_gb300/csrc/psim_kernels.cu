@@ -768,6 +768,66 @@ __global__ void __launch_bounds__(256, MINB) k_step_fused(KArgs k, uint32_t step
     grad_end(k, s_grad);
 }
 
+// k_step_fused with U agents per thread in flight: the location, countdown
+// and infectiousness loads of all U agents are issued first, then their
+// hazard gathers and CSR slot atomics (plain returning atomics), then the
+// slot stores; the draw / movement / histogram of each agent follows as in
+// k_step_fused.  The per-agent chain load -> gather/atomic -> store is what
+// bounds the single-agent form, so U independent chains per thread multiply
+// the memory-level parallelism at the same occupancy.
+template <int U>
+__global__ void __launch_bounds__(256) k_step_ilp(KArgs k, uint32_t step) {
+    __shared__ double s_grad[GRAD_N];
+    grad_begin(k, s_grad);
+    const uint32_t N = k.a.n, L = k.l.n;
+    const uint32_t t = k.clock->t0 + step;
+    const StepClock c = step_clock(k, step + 1);
+    const uint32_t chunk = 256u * U;
+    for (uint32_t base = blockIdx.x * chunk; base < N; base += gridDim.x * chunk) {
+        uint32_t loc0[U], s[U], pos[U];
+        float inf[U], h0[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint32_t i = base + u * 256u + threadIdx.x;
+            const bool act = i < N;
+            loc0[u] = act ? k.a.location[i] : NONE;
+            s[u] = act ? k.a.steps_until_move[i] : 0u;
+            inf[u] = act ? k.a.infectious[i] : 0.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const bool ok = loc0[u] < L;
+            h0[u] = ok ? k.l.hazard[loc0[u]] : 0.0f;
+            pos[u] = ok ? atomicAdd(&k.l.cursor[loc0[u]], 1u) : NONE;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint32_t i = base + u * 256u + threadIdx.x;
+            if (loc0[u] < L) store_slot(k, pos[u], i);
+        }
+#pragma unroll 1
+        for (int u = 0; u < U; ++u) {
+            const uint32_t i = base + u * 256u + threadIdx.x;
+            const bool act = i < N;
+            double term = 0.0;
+            uint32_t loc = NONE, var = 0;
+            float fi = inf[u];
+            if (act && loc0[u] < L && (h0[u] > 0.0f || k.m.n_variants > 1)) {
+                term = draw_agent(k, i, loc0[u], t, h0[u], s_grad);
+                fi = k.a.infectious[i];
+            }
+            if (act) {
+                move_agent(k, i, c, s[u]);
+                loc = (c.curfew_now || s[u] == 0) ? k.a.location[i] : loc0[u];
+                if (fi > 0.0f) var = k.a.variant[i];
+            }
+            if (k.track_expected) add_expected(k, act, i, term);
+            count_agent(k, act, loc, fi, var);
+        }
+    }
+    grad_end(k, s_grad);
+}
+
 // Hot/cold form of k_step_fused.  The hot kernel does, for every agent, the
 // CSR slot of step `step`; agents that neither draw (no hazard at their
 // location) nor move at step + 1 (countdown > 0, no curfew transition) also
@@ -1441,18 +1501,30 @@ void launch_movement(const KArgs& k, uint32_t step, cudaStream_t s) {
 // raises occupancy for the hot path and spills on the rare cold path; the
 // autotuner picks one (DevTune::variant)
 void launch_step_fused(const KArgs& k, uint32_t step, cudaStream_t s) {
-    static unsigned g[5] = {0, 0, 0, 0, 0};
-    const uint32_t v = k.tune.variant < 4 ? k.tune.variant : 0;
+    static unsigned g[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const uint32_t v = k.tune.variant < 6 ? k.tune.variant : 0;
     if (!g[0]) {
         g[0] = wave_grid(k_step_fused<4>, 1u << 30);
         g[1] = wave_grid(k_step_fused<6>, 1u << 30);
         g[2] = wave_grid(k_step_fused<8>, 1u << 30);
         g[3] = wave_grid(k_step_hot, 1u << 30);
         g[4] = wave_grid(k_step_cold, 1u << 30);
+        g[5] = wave_grid(k_step_ilp<2>, 1u << 30);
+        g[6] = wave_grid(k_step_ilp<4>, 1u << 30);
     }
     if (v == 3) {
         k_step_hot<<<agent_grid(k, g[3]), 256, 0, s>>>(k, step);
         k_step_cold<<<g[4], 256, 0, s>>>(k, step);
+        return;
+    }
+    if (v == 4 || v == 5) {
+        const int U = v == 4 ? 2 : 4;
+        unsigned grid = k.tune.blocks_per_sm ? (unsigned)(sm_count() * k.tune.blocks_per_sm) : g[v == 4 ? 5 : 6];
+        grid = std::min(grid, grid_for((k.a.n + U - 1) / U, 1 << 20));
+        if (v == 4)
+            k_step_ilp<2><<<grid, 256, 0, s>>>(k, step);
+        else
+            k_step_ilp<4><<<grid, 256, 0, s>>>(k, step);
         return;
     }
     const unsigned grid = agent_grid(k, g[v]);
