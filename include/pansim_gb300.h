@@ -219,7 +219,7 @@ typedef struct psim_day_stats {
 /* Launch and algorithm choices of the per-step kernels, picked per device
  * and workload by the autotuner (pansim_gb300/autotune.py). */
 typedef struct psim_tuning {
-    uint32_t agg_count;      /* warp-aggregated per-location count reductions */
+    uint32_t agg_count;      /* no effect (the histogram is updated by movers only) */
     uint32_t agg_slot;       /* warp-aggregated CSR slot atomics */
     uint32_t blocks_per_sm;  /* 256-thread blocks per SM of the per-agent kernels; 0 = occupancy */
     uint32_t variant;        /* fused step kernel: 0/1/2 = one kernel capped at 64/40/32

@@ -459,6 +459,7 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     if ((rc = dalloc(c, &dl.sfix, L * V))) return bail(rc);
     if ((rc = dalloc(c, &dl.hazard, L * V))) return bail(rc);
     if ((rc = dalloc(c, &dl.hazard_x, L * V))) return bail(rc);
+    if ((rc = dalloc(c, &dl.hmask, ((size_t)L + 2047) / 2048 * 64 + 64))) return bail(rc);
     if ((rc = dalloc(c, &dl.no_work_loc, L))) return bail(rc);
     if ((rc = dalloc(c, &dl.flags, L))) return bail(rc);
     const size_t tiles = (L + 2047) / 2048 + 1;
@@ -504,6 +505,8 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
         add(a2.st_variant_mask, 4 * N); add(a2.st_immunization_count, N); add(a2.st_infected_count, N);
         add(a2.st_worst_state, N); add(a2.imm_round, N); add(a2.scaling_v, 4 * N * V);
         add(dl.infectiousness, 4 * L); add(dl.open, L); add(dl.closed_until, 4 * L); add(dl.quarantine_until, 4 * L);
+        // the histogram is kept incrementally across steps and days
+        add(dl.counts, 4 * L); add(dl.sfix, 8 * L * V);
         add(dr.variant_active, R * V); add(dr.expected, 8 * R);
     }
     k.p = c->params;

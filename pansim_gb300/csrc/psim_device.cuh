@@ -115,6 +115,7 @@ struct DevLocs {
     uint32_t* qu_pending;         // quarantine writes of the running step
     unsigned long long* sfix;     // [V][n] fixed-point infectiousness sums
     float* hazard;                // [V][n] infection ratio of the last step
+    uint32_t* hmask;              // bit l: some variant's hazard at location l is > 0
     float* hazard_x;              // [V][n] its argument x = k*S/n*w*season*dt (adjoint mode)
     uint32_t* no_work_loc;
     uint8_t* flags;               // testing flags
@@ -148,7 +149,7 @@ struct DevStatsAcc {      // raw per-replica daily counters
 
 // launch/algorithm choices picked by the autotuner (psim_tuning)
 struct DevTune {
-    uint32_t agg_count;      // warp-aggregate the per-location count reductions
+    uint32_t agg_count;      // no effect: the histogram is updated by movers only
     uint32_t agg_slot;       // warp-aggregate the CSR slot atomics
     uint32_t blocks_per_sm;  // grid of the per-agent kernels (0 = one occupancy wave)
     uint32_t variant;        // fused step kernel: 0/1/2 = one kernel capped at 64/40/32 registers,

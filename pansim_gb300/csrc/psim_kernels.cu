@@ -364,6 +364,15 @@ __device__ __forceinline__ unsigned lanemask_lt() {
     return m;
 }
 
+// Hazard of variant 0 at `loc` and whether any variant's hazard there is > 0:
+// the bit mask written by the scan is read through L1, so the hazard itself
+// is gathered only at infectious locations.
+__device__ __forceinline__ float hazard_at(const KArgs& k, uint32_t loc, bool* any) {
+    const uint32_t w = __ldg(&k.l.hmask[loc >> 5]);
+    *any = ((w >> (loc & 31u)) & 1u) != 0;
+    return *any ? k.l.hazard[loc] : 0.0f;
+}
+
 // ---------------------------------------------------------------------------
 // Per-agent pieces of a step.
 
@@ -405,34 +414,40 @@ __device__ __forceinline__ void move_agent(const KArgs& k, uint32_t i, const Ste
     }
 }
 
-// Histogram and fixed-point infectiousness sum of the agent's location, as
-// fire-and-forget reductions (warp-aggregated per location).  Warp-collective:
-// every lane calls it, `act` false for lanes without an agent.
-__device__ __forceinline__ void count_agent(const KArgs& k, bool act, uint32_t loc, float inf, uint32_t variant) {
+// The per-location agent counts are kept up to date incrementally: an agent
+// whose location changed from loc0 to loc moves one count (two fire-and-
+// forget reductions); agents that stay do not touch the histogram.  The
+// fixed-point infectiousness sums are rebuilt every step: every infectious
+// agent adds its term at its (new) location, and the scan consumes them.
+__device__ __forceinline__ void count_agent(const KArgs& k, bool act, uint32_t loc0, uint32_t loc, float inf,
+                                            uint32_t variant) {
     const uint32_t L = k.l.n;
     if (act && loc >= L) {
         atomicOr(k.err, ERR_LOCATION);
         loc = NONE;
     }
-    const bool ok = act && loc != NONE;
-    if (!k.tune.agg_count) {
-        if (ok) {
-            atomicAdd(&k.l.counts[loc], 1u);
-            if (inf > 0.0f) {
-                const long long q = __float2ll_rn(inf * PSIM_FIX_SCALE_F);
-                atomicAdd(&k.l.sfix[(size_t)variant * L + loc], (unsigned long long)q);
-            }
-        }
+    if (act && loc != loc0) {
+        if (loc0 < L) atomicSub(&k.l.counts[loc0], 1u);
+        if (loc != NONE) atomicAdd(&k.l.counts[loc], 1u);
+    }
+    if (act && loc != NONE && inf > 0.0f) {
+        const long long q = __float2ll_rn(inf * PSIM_FIX_SCALE_F);
+        atomicAdd(&k.l.sfix[(size_t)variant * L + loc], (unsigned long long)q);
+    }
+}
+
+// The full histogram of the current positions (after a reset of counts and sums).
+__device__ __forceinline__ void count_full(const KArgs& k, bool act, uint32_t loc, float inf, uint32_t variant) {
+    const uint32_t L = k.l.n;
+    if (!act) return;
+    if (loc >= L) {
+        atomicOr(k.err, ERR_LOCATION);
         return;
     }
-    const unsigned valid = __ballot_sync(0xffffffffu, ok);
-    if (ok) {
-        const unsigned peers = __match_any_sync(valid, loc);
-        if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&k.l.counts[loc], (uint32_t)__popc(peers));
-        if (inf > 0.0f) {
-            const long long q = __float2ll_rn(inf * PSIM_FIX_SCALE_F);
-            atomicAdd(&k.l.sfix[(size_t)variant * L + loc], (unsigned long long)q);
-        }
+    atomicAdd(&k.l.counts[loc], 1u);
+    if (inf > 0.0f) {
+        const long long q = __float2ll_rn(inf * PSIM_FIX_SCALE_F);
+        atomicAdd(&k.l.sfix[(size_t)variant * L + loc], (unsigned long long)q);
     }
 }
 
@@ -550,17 +565,17 @@ __global__ void __launch_bounds__(256) k_movement(KArgs k, uint32_t step) {
     for (uint32_t base = blockIdx.x * blockDim.x; base < N; base += stride) {
         const uint32_t i = base + threadIdx.x;
         const bool act = i < N;
-        uint32_t loc = NONE, var = 0;
+        uint32_t loc = NONE, loc0 = NONE, var = 0;
         float inf = 0.0f;
         if (act) {
             const uint32_t s = k.a.steps_until_move[i];
-            const uint32_t loc0 = k.a.location[i];
+            loc0 = k.a.location[i];
             inf = k.a.infectious[i];
             move_agent(k, i, c, s);
             loc = (c.curfew_now || s == 0) ? k.a.location[i] : loc0;
             if (inf > 0.0f) var = k.a.variant[i];
         }
-        count_agent(k, act, loc, inf, var);
+        count_agent(k, act, loc0, loc, inf, var);
     }
 }
 
@@ -578,7 +593,7 @@ __global__ void __launch_bounds__(256) k_count(KArgs k) {
             inf = k.a.infectious[i];
             if (inf > 0.0f) var = k.a.variant[i];
         }
-        count_agent(k, act, loc, inf, var);
+        count_full(k, act, loc, inf, var);
     }
 }
 
@@ -587,8 +602,8 @@ __global__ void __launch_bounds__(256) k_count(KArgs k) {
 // each tile of 2048 locations; k_scan adds the sums of the tiles before its
 // own (every block reads at most a few thousand 4-byte sums, so the prefix
 // needs no inter-block waiting), scans its tile warp-striped (coalesced),
-// writes the cursor (exclusive prefix = first CSR slot of the location),
-// resets the histogram, and evaluates the infection ratio of every location
+// writes the cursor (exclusive prefix = first CSR slot of the location)
+// and evaluates the infection ratio of every location
 // with a non-zero infectiousness sum.
 constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_ITEMS = 8;
@@ -662,12 +677,10 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, int with_hazard,
 #pragma unroll
     for (int q = 0; q < SCAN_ITEMS; ++q) {
         const uint32_t l = wbase + q * 32 + lane;
-        if (l < L) {
-            k.l.cursor[l] = base + ex[q];
-            k.l.counts[l] = 0u;
-        }
+        if (l < L) k.l.cursor[l] = base + ex[q];
     }
     if (with_hazard) {
+        uint32_t any = 0;  // bit q: some variant's hazard of this lane's location q is > 0
         for (uint32_t v = 0; v < V; ++v) {
 #pragma unroll
             for (int q = 0; q < SCAN_ITEMS; ++q) {
@@ -682,9 +695,16 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, int with_hazard,
                         k.l.sfix[idx] = 0ull;
                     }
                     k.l.hazard[idx] = h;
+                    if (h > 0.0f) any |= 1u << q;
                     if (k.adj.on) k.l.hazard_x[idx] = x;
                 }
             }
+        }
+        // one mask word per 32 locations (wbase is a multiple of 32)
+#pragma unroll
+        for (int q = 0; q < SCAN_ITEMS; ++q) {
+            const unsigned word = __ballot_sync(0xffffffffu, (any >> q) & 1u);
+            if (lane == 0) k.l.hmask[(wbase + q * 32) >> 5] = word;
         }
     }
     if (merge_q) {
@@ -715,12 +735,13 @@ __global__ void __launch_bounds__(256) k_scatter_draw(KArgs k, uint32_t step, in
         double term = 0.0;
         const uint32_t loc = act ? k.a.location[i] : NONE;
         const bool ok = act && loc < L;
-        const float h0 = (draw && ok) ? k.l.hazard[loc] : 0.0f;
+        bool hz = false;
+        const float h0 = (draw && ok) ? hazard_at(k, loc, &hz) : 0.0f;
         if (scatter) {
             const uint32_t pos = take_slot(k, ok, loc);
             if (ok) store_slot(k, pos, i);
         }
-        if (ok && draw && (h0 > 0.0f || k.m.n_variants > 1)) term = draw_agent(k, i, loc, t, h0, s_grad);
+        if (ok && draw && hz) term = draw_agent(k, i, loc, t, h0, s_grad);
         if (k.track_expected) add_expected(k, act, i, term);
     }
     grad_end(k, s_grad);
@@ -746,13 +767,14 @@ __global__ void __launch_bounds__(256, MINB) k_step_fused(KArgs k, uint32_t step
         const uint32_t s = act ? k.a.steps_until_move[i] : 0u;
         float inf = act ? k.a.infectious[i] : 0.0f;
         const bool ok = act && loc0 < L;
-        const float h0 = ok ? k.l.hazard[loc0] : 0.0f;
+        bool hz = false;
+        const float h0 = ok ? hazard_at(k, loc0, &hz) : 0.0f;
         const uint32_t pos = take_slot(k, ok, loc0);
         double term = 0.0;
         uint32_t loc = NONE, var = 0;
         if (ok) {
             store_slot(k, pos, i);
-            if (h0 > 0.0f || k.m.n_variants > 1) {
+            if (hz) {
                 term = draw_agent(k, i, loc0, t, h0, s_grad);
                 inf = k.a.infectious[i];
             }
@@ -763,7 +785,7 @@ __global__ void __launch_bounds__(256, MINB) k_step_fused(KArgs k, uint32_t step
             if (inf > 0.0f) var = k.a.variant[i];
         }
         if (k.track_expected) add_expected(k, act, i, term);
-        count_agent(k, act, loc, inf, var);
+        count_agent(k, act, loc0, loc, inf, var);
     }
     grad_end(k, s_grad);
 }
@@ -786,6 +808,7 @@ __global__ void __launch_bounds__(256) k_step_ilp(KArgs k, uint32_t step) {
     for (uint32_t base = blockIdx.x * chunk; base < N; base += gridDim.x * chunk) {
         uint32_t loc0[U], s[U], pos[U];
         float inf[U], h0[U];
+        bool hz[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const uint32_t i = base + u * 256u + threadIdx.x;
@@ -797,7 +820,8 @@ __global__ void __launch_bounds__(256) k_step_ilp(KArgs k, uint32_t step) {
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const bool ok = loc0[u] < L;
-            h0[u] = ok ? k.l.hazard[loc0[u]] : 0.0f;
+            hz[u] = false;
+            h0[u] = ok ? hazard_at(k, loc0[u], &hz[u]) : 0.0f;
             pos[u] = ok ? atomicAdd(&k.l.cursor[loc0[u]], 1u) : NONE;
         }
 #pragma unroll
@@ -812,7 +836,7 @@ __global__ void __launch_bounds__(256) k_step_ilp(KArgs k, uint32_t step) {
             double term = 0.0;
             uint32_t loc = NONE, var = 0;
             float fi = inf[u];
-            if (act && loc0[u] < L && (h0[u] > 0.0f || k.m.n_variants > 1)) {
+            if (act && loc0[u] < L && hz[u]) {
                 term = draw_agent(k, i, loc0[u], t, h0[u], s_grad);
                 fi = k.a.infectious[i];
             }
@@ -822,7 +846,7 @@ __global__ void __launch_bounds__(256) k_step_ilp(KArgs k, uint32_t step) {
                 if (fi > 0.0f) var = k.a.variant[i];
             }
             if (k.track_expected) add_expected(k, act, i, term);
-            count_agent(k, act, loc, fi, var);
+            count_agent(k, act, loc0[u], loc, fi, var);
         }
     }
     grad_end(k, s_grad);
@@ -840,7 +864,6 @@ __global__ void __launch_bounds__(256, 8) k_step_hot(KArgs k, uint32_t step) {
     const uint32_t dt = k.p.time_step;
     const uint32_t minutes = (step + 1) * dt;
     const bool curfew_now = k.p.enable_curfew && k.p.curfew_begin == minutes / dt;
-    const bool multi = k.m.n_variants > 1;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < N; base += stride) {
         const uint32_t i = base + threadIdx.x;
@@ -849,10 +872,11 @@ __global__ void __launch_bounds__(256, 8) k_step_hot(KArgs k, uint32_t step) {
         const uint32_t s = act ? k.a.steps_until_move[i] : 0u;
         const float inf = act ? k.a.infectious[i] : 0.0f;
         const bool ok = act && loc0 < L;
-        const float h0 = ok ? k.l.hazard[loc0] : 0.0f;
+        bool hz = false;
+        if (ok) hazard_at(k, loc0, &hz);
         const uint32_t pos = take_slot(k, ok, loc0);
         if (ok) store_slot(k, pos, i);
-        const bool cold = act && (curfew_now || s == 0 || h0 > 0.0f || multi || !ok);
+        const bool cold = act && (curfew_now || s == 0 || hz || !ok);
         const bool hot = act && !cold;
         if (hot) k.a.steps_until_move[i] = s - 1;
         // queue the cold agents
@@ -866,7 +890,7 @@ __global__ void __launch_bounds__(256, 8) k_step_hot(KArgs k, uint32_t step) {
         }
         uint32_t var = 0;
         if (hot && inf > 0.0f) var = k.a.variant[i];
-        count_agent(k, hot, loc0, inf, var);
+        count_agent(k, hot, loc0, loc0, inf, var);
     }
 }
 
@@ -884,15 +908,16 @@ __global__ void __launch_bounds__(256) k_step_cold(KArgs k, uint32_t step) {
         const bool act = j < n;
         const uint32_t i = act ? k.a.worklist[j] : 0u;
         double term = 0.0;
-        uint32_t loc = NONE, var = 0;
+        uint32_t loc = NONE, loc0 = NONE, var = 0;
         float inf = 0.0f;
         if (act) {
-            const uint32_t loc0 = k.a.location[i];
+            loc0 = k.a.location[i];
             const uint32_t s = k.a.steps_until_move[i];
             inf = k.a.infectious[i];
             if (loc0 < L) {
-                const float h0 = k.l.hazard[loc0];
-                if (h0 > 0.0f || k.m.n_variants > 1) {
+                bool hz = false;
+                const float h0 = hazard_at(k, loc0, &hz);
+                if (hz) {
                     term = draw_agent(k, i, loc0, t, h0, s_grad);
                     inf = k.a.infectious[i];
                 }
@@ -902,7 +927,7 @@ __global__ void __launch_bounds__(256) k_step_cold(KArgs k, uint32_t step) {
             if (inf > 0.0f) var = k.a.variant[i];
         }
         if (k.track_expected) add_expected(k, act, i, term);
-        count_agent(k, act, loc, inf, var);
+        count_agent(k, act, loc0, loc, inf, var);
     }
     grad_end(k, s_grad);
 }
