@@ -188,6 +188,7 @@ int upload_mutable(psim_ctx* c, const psim_agents* a, const psim_locations* l) {
 int initial_regroup(psim_ctx* c) {
     CK(cudaMemsetAsync(c->k.l.counts, 0, sizeof(uint32_t) * c->L, c->stream));
     CK(cudaMemsetAsync(c->k.l.sfix, 0, sizeof(unsigned long long) * c->L * c->V, c->stream));
+    CK(cudaMemsetAsync(c->k.l.smask, 0, sizeof(uint32_t) * (((size_t)c->L + 2047) / 2048 * 64 + 64), c->stream));
     launch_count(c->k, c->stream);
     launch_scan(c->k, 0, 1, 0, c->stream);
     launch_scatter_draw(c->k, 0, 1, 0, c->stream);
@@ -460,6 +461,7 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     if ((rc = dalloc(c, &dl.hazard, L * V))) return bail(rc);
     if ((rc = dalloc(c, &dl.hazard_x, L * V))) return bail(rc);
     if ((rc = dalloc(c, &dl.hmask, ((size_t)L + 2047) / 2048 * 64 + 64))) return bail(rc);
+    if ((rc = dalloc(c, &dl.smask, ((size_t)L + 2047) / 2048 * 64 + 64))) return bail(rc);
     if ((rc = dalloc(c, &dl.no_work_loc, L))) return bail(rc);
     if ((rc = dalloc(c, &dl.flags, L))) return bail(rc);
     const size_t tiles = (L + 2047) / 2048 + 1;
@@ -506,7 +508,7 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
         add(a2.st_worst_state, N); add(a2.imm_round, N); add(a2.scaling_v, 4 * N * V);
         add(dl.infectiousness, 4 * L); add(dl.open, L); add(dl.closed_until, 4 * L); add(dl.quarantine_until, 4 * L);
         // the histogram is kept incrementally across steps and days
-        add(dl.counts, 4 * L); add(dl.sfix, 8 * L * V);
+        add(dl.counts, 4 * L); add(dl.sfix, 8 * L * V); add(dl.smask, 4 * ((L + 2047) / 2048 * 64 + 64));
         add(dr.variant_active, R * V); add(dr.expected, 8 * R);
     }
     k.p = c->params;
@@ -773,6 +775,8 @@ int psim_regroup(psim_ctx* c) {
     if (!c->csr_fresh) {
         CK(cudaMemsetAsync(c->k.l.counts, 0, sizeof(uint32_t) * c->L, c->stream));
         CK(cudaMemsetAsync(c->k.l.sfix, 0, sizeof(unsigned long long) * c->L * c->V, c->stream));
+        CK(cudaMemsetAsync(c->k.l.smask, 0, sizeof(uint32_t) * (((size_t)c->L + 2047) / 2048 * 64 + 64), c->stream));
+    CK(cudaMemsetAsync(c->k.l.smask, 0, sizeof(uint32_t) * (((size_t)c->L + 2047) / 2048 * 64 + 64), c->stream));
         launch_count(c->k, c->stream);
         c->launches += 1;
     }
@@ -929,9 +933,16 @@ int psim_get_csr(psim_ctx* c, int canonical, uint32_t* offsets, uint32_t* agents
 
 int psim_get_hazard(psim_ctx* c, float* out, int64_t* fixed_sum) {
     if (!c || !c->uploaded) return PSIM_ERR_STATE;
-    if (out) CK(cudaMemcpyAsync(out, c->k.l.hazard, sizeof(float) * c->L * c->V, cudaMemcpyDeviceToHost, c->stream));
     (void)fixed_sum;
+    if (!out) return 0;
+    // hazards are kept only where the mask says some variant's is > 0
+    std::vector<uint32_t> mask((c->L + 31) / 32);
+    CK(cudaMemcpyAsync(out, c->k.l.hazard, sizeof(float) * c->L * c->V, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(mask.data(), c->k.l.hmask, sizeof(uint32_t) * mask.size(), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    for (uint32_t l = 0; l < c->L; ++l)
+        if (!((mask[l >> 5] >> (l & 31)) & 1u))
+            for (uint32_t v = 0; v < c->V; ++v) out[(size_t)v * c->L + l] = 0.0f;
     return 0;
 }
 

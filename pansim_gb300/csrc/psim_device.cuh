@@ -116,6 +116,7 @@ struct DevLocs {
     unsigned long long* sfix;     // [V][n] fixed-point infectiousness sums
     float* hazard;                // [V][n] infection ratio of the last step
     uint32_t* hmask;              // bit l: some variant's hazard at location l is > 0
+    uint32_t* smask;              // bit l: some variant's fixed-point sum at l received a term this step
     float* hazard_x;              // [V][n] its argument x = k*S/n*w*season*dt (adjoint mode)
     uint32_t* no_work_loc;
     uint8_t* flags;               // testing flags

@@ -433,6 +433,7 @@ __device__ __forceinline__ void count_agent(const KArgs& k, bool act, uint32_t l
     if (act && loc != NONE && inf > 0.0f) {
         const long long q = __float2ll_rn(inf * PSIM_FIX_SCALE_F);
         atomicAdd(&k.l.sfix[(size_t)variant * L + loc], (unsigned long long)q);
+        atomicOr(&k.l.smask[loc >> 5], 1u << (loc & 31u));
     }
 }
 
@@ -448,6 +449,7 @@ __device__ __forceinline__ void count_full(const KArgs& k, bool act, uint32_t lo
     if (inf > 0.0f) {
         const long long q = __float2ll_rn(inf * PSIM_FIX_SCALE_F);
         atomicAdd(&k.l.sfix[(size_t)variant * L + loc], (unsigned long long)q);
+        atomicOr(&k.l.smask[loc >> 5], 1u << (loc & 31u));
     }
 }
 
@@ -680,24 +682,31 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, int with_hazard,
         if (l < L) k.l.cursor[l] = base + ex[q];
     }
     if (with_hazard) {
+        // only locations that received infectiousness this step (sum mask)
+        // are read; elsewhere the hazard is 0 and stays unwritten, the hazard
+        // mask keeping readers away from it
         uint32_t any = 0;  // bit q: some variant's hazard of this lane's location q is > 0
-        for (uint32_t v = 0; v < V; ++v) {
 #pragma unroll
-            for (int q = 0; q < SCAN_ITEMS; ++q) {
-                const uint32_t l = wbase + q * 32 + lane;
-                if (l < L) {
-                    const size_t idx = (size_t)v * L + l;
-                    const long long fix = (long long)k.l.sfix[idx];
-                    float h = 0.0f, x = 0.0f;
-                    if (fix != 0) {
-                        const uint32_t rep = k.l.rep[l];
-                        h = psim_hazard_x(fix, c[q], k.r.k_f[rep], k.l.infectiousness[l], season, dt, &x);
-                        k.l.sfix[idx] = 0ull;
-                    }
-                    k.l.hazard[idx] = h;
-                    if (h > 0.0f) any |= 1u << q;
-                    if (k.adj.on) k.l.hazard_x[idx] = x;
+        for (int q = 0; q < SCAN_ITEMS; ++q) {
+            const uint32_t l = wbase + q * 32 + lane;
+            const uint32_t wi = (wbase + q * 32) >> 5;
+            const uint32_t sw = k.l.smask[wi];
+            if (!sw) continue;  // warp-uniform
+            __syncwarp();
+            if (lane == 0) k.l.smask[wi] = 0u;
+            if (l >= L || !((sw >> lane) & 1u)) continue;
+            const uint32_t rep = k.l.rep[l];
+            for (uint32_t v = 0; v < V; ++v) {
+                const size_t idx = (size_t)v * L + l;
+                const long long fix = (long long)k.l.sfix[idx];
+                float h = 0.0f, x = 0.0f;
+                if (fix != 0) {
+                    h = psim_hazard_x(fix, c[q], k.r.k_f[rep], k.l.infectiousness[l], season, dt, &x);
+                    k.l.sfix[idx] = 0ull;
                 }
+                k.l.hazard[idx] = h;
+                if (h > 0.0f) any |= 1u << q;
+                if (k.adj.on) k.l.hazard_x[idx] = x;
             }
         }
         // one mask word per 32 locations (wbase is a multiple of 32)
