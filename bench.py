@@ -415,7 +415,7 @@ def main():
             "config": {"workload": "2M agents, 500k non-home locations (+homes), dt 10 min, 1 day per step",
                        "agents": N, "locations": L, "timesteps_per_step": 144,
                        "l2": "flushed between timed steps (256 MiB write)", "parallelism": "replicas" if ws > 1 else "1 gpu"},
-            "roofline": {"bound": "hbm", "kernel": "one timestep: k_tile_sums + k_scan + k_step_fused",
+            "roofline": {"bound": "hbm", "kernel": "one timestep: k_scan + k_step_fused",
                          "achieved": ach, "peak": peak,
                          "unit": "GB/s", "frac": ach / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "alg_bytes_per_launch": step_bytes, "launch_ms": step_ms, "dominant": dom,

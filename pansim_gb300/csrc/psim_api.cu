@@ -190,10 +190,11 @@ int initial_regroup(psim_ctx* c) {
     CK(cudaMemsetAsync(c->k.l.sfix, 0, sizeof(unsigned long long) * c->L * c->V, c->stream));
     CK(cudaMemsetAsync(c->k.l.smask, 0, sizeof(uint32_t) * (((size_t)c->L + 2047) / 2048 * 64 + 64), c->stream));
     launch_count(c->k, c->stream);
+    launch_tile_sums(c->k, c->stream);
     launch_scan(c->k, 0, 1, 0, c->stream);
     launch_scatter_draw(c->k, 0, 1, 0, c->stream);
     launch_stats(c->k, 0, c->stream);
-    c->launches += 6;
+    c->launches += 7;
     int rc = launch_check(c);
     if (rc) return rc;
     c->csr_fresh = true;
@@ -205,7 +206,7 @@ int do_step(psim_ctx* c, uint32_t step, bool draw, bool movement) {
     if (movement) launch_movement(c->k, step, c->stream);
     launch_scan(c->k, step, 1, merge_q, c->stream);
     launch_scatter_draw(c->k, step, 1, draw ? 1 : 0, c->stream);
-    c->launches += movement ? 4 : 3;
+    c->launches += movement ? 3 : 2;
     return launch_check(c);
 }
 
@@ -246,7 +247,7 @@ int capture_day_graph(psim_ctx* c) {
     e = cudaGraphInstantiate(&c->day_graph, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(c, PSIM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
-    c->graph_kernels = (2ull + (uint64_t)step_fused_kernels(c->k)) * c->spd + 1;
+    c->graph_kernels = (1ull + (uint64_t)step_fused_kernels(c->k)) * c->spd + 1;
     c->graph_dirty = false;
     c->prof_valid = false;
     return 0;
@@ -509,6 +510,7 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
         add(dl.infectiousness, 4 * L); add(dl.open, L); add(dl.closed_until, 4 * L); add(dl.quarantine_until, 4 * L);
         // the histogram is kept incrementally across steps and days
         add(dl.counts, 4 * L); add(dl.sfix, 8 * L * V); add(dl.smask, 4 * ((L + 2047) / 2048 * 64 + 64));
+        add(dl.tile_sums, 4 * ((L + 2047) / 2048 + 1));
         add(dr.variant_active, R * V); add(dr.expected, 8 * R);
     }
     k.p = c->params;
@@ -778,11 +780,12 @@ int psim_regroup(psim_ctx* c) {
         CK(cudaMemsetAsync(c->k.l.smask, 0, sizeof(uint32_t) * (((size_t)c->L + 2047) / 2048 * 64 + 64), c->stream));
     CK(cudaMemsetAsync(c->k.l.smask, 0, sizeof(uint32_t) * (((size_t)c->L + 2047) / 2048 * 64 + 64), c->stream));
         launch_count(c->k, c->stream);
-        c->launches += 1;
+        launch_tile_sums(c->k, c->stream);
+        c->launches += 2;
     }
     launch_scan(c->k, 0, 1, c->params.quarantine_policy > 1, c->stream);
     launch_scatter_draw(c->k, 0, 1, 0, c->stream);
-    c->launches += 3;
+    c->launches += 2;
     c->csr_fresh = false;
     int rc = launch_check(c);
     if (rc) return rc;
@@ -1010,7 +1013,7 @@ int psim_time_step_kernels(psim_ctx* c, uint32_t t, float* ms) {
     CK(cudaEventRecord(ev[3], c->stream));
     launch_scan(c->k, step + 1, 1, merge_q, c->stream);
     launch_scatter_draw(c->k, step + 1, 1, 1, c->stream);
-    c->launches += 6 + (uint64_t)step_fused_kernels(c->k);
+    c->launches += 4 + (uint64_t)step_fused_kernels(c->k);
     CK(cudaStreamSynchronize(c->stream));
     for (int j = 0; j < 3; ++j) CK(cudaEventElapsedTime(&ms[j], ev[j], ev[j + 1]));
     for (int j = 0; j < 4; ++j) cudaEventDestroy(ev[j]);

@@ -414,6 +414,11 @@ __device__ __forceinline__ void move_agent(const KArgs& k, uint32_t i, const Ste
     }
 }
 
+// Scan tiles: 256 threads x 8 locations.
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 8;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
 // The per-location agent counts are kept up to date incrementally: an agent
 // whose location changed from loc0 to loc moves one count (two fire-and-
 // forget reductions); agents that stay do not touch the histogram.  The
@@ -426,9 +431,26 @@ __device__ __forceinline__ void count_agent(const KArgs& k, bool act, uint32_t l
         atomicOr(k.err, ERR_LOCATION);
         loc = NONE;
     }
-    if (act && loc != loc0) {
+    const bool mv = act && loc != loc0;
+    if (mv) {
         if (loc0 < L) atomicSub(&k.l.counts[loc0], 1u);
         if (loc != NONE) atomicAdd(&k.l.counts[loc], 1u);
+    }
+    // the per-tile sums of the scan follow the counts; movers of a warp
+    // mostly share their tiles, so one reduction per distinct tile
+    // (warp-collective: every lane calls count_agent)
+    const uint32_t t_old = (mv && loc0 < L) ? loc0 / (uint32_t)SCAN_TILE : NONE;
+    const uint32_t t_new = (mv && loc != NONE) ? loc / (uint32_t)SCAN_TILE : NONE;
+    const bool dec = t_old != NONE && t_old != t_new, inc = t_new != NONE && t_old != t_new;
+    const unsigned md = __ballot_sync(0xffffffffu, dec), mi = __ballot_sync(0xffffffffu, inc);
+    const int lane = threadIdx.x & 31;
+    if (dec) {
+        const unsigned peers = __match_any_sync(md, t_old);
+        if (lane == __ffs(peers) - 1) atomicSub(&k.l.tile_sums[t_old], (uint32_t)__popc(peers));
+    }
+    if (inc) {
+        const unsigned peers = __match_any_sync(mi, t_new);
+        if (lane == __ffs(peers) - 1) atomicAdd(&k.l.tile_sums[t_new], (uint32_t)__popc(peers));
     }
     if (act && loc != NONE && inf > 0.0f) {
         const long long q = __float2ll_rn(inf * PSIM_FIX_SCALE_F);
@@ -600,16 +622,14 @@ __global__ void __launch_bounds__(256) k_count(KArgs k) {
 }
 
 // ---------------------------------------------------------------------------
-// Scan of the histogram in two passes (reduce, then scan): k_tile_sums adds up
-// each tile of 2048 locations; k_scan adds the sums of the tiles before its
+// Scan of the histogram.  The sums of the tiles of 2048 locations are kept up
+// to date with the counts (k_tile_sums rebuilds them after a full recount);
+// k_scan adds the sums of the tiles before its
 // own (every block reads at most a few thousand 4-byte sums, so the prefix
 // needs no inter-block waiting), scans its tile warp-striped (coalesced),
 // writes the cursor (exclusive prefix = first CSR slot of the location)
 // and evaluates the infection ratio of every location
 // with a non-zero infectiousness sum.
-constexpr int SCAN_THREADS = 256;
-constexpr int SCAN_ITEMS = 8;
-constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
 
 __device__ __forceinline__ uint32_t block_sum_256(uint32_t v, uint32_t* s_red) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -654,7 +674,18 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, int with_hazard,
     }
     // sum of the tiles before this one
     uint32_t pre = 0;
-    for (uint32_t j = threadIdx.x; j < tile; j += SCAN_THREADS) pre += k.l.tile_sums[j];
+    {
+        uint32_t p0 = 0, p1 = 0, p2 = 0, p3 = 0;
+        uint32_t j = threadIdx.x;
+        for (; j + 3 * SCAN_THREADS < tile; j += 4 * SCAN_THREADS) {
+            p0 += k.l.tile_sums[j];
+            p1 += k.l.tile_sums[j + SCAN_THREADS];
+            p2 += k.l.tile_sums[j + 2 * SCAN_THREADS];
+            p3 += k.l.tile_sums[j + 3 * SCAN_THREADS];
+        }
+        for (; j < tile; j += SCAN_THREADS) p0 += k.l.tile_sums[j];
+        pre = p0 + p1 + p2 + p3;
+    }
     const uint32_t prefix = block_sum_256(pre, s_red);
     uint32_t carry = 0;
 #pragma unroll
@@ -686,11 +717,14 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, int with_hazard,
         // are read; elsewhere the hazard is 0 and stays unwritten, the hazard
         // mask keeping readers away from it
         uint32_t any = 0;  // bit q: some variant's hazard of this lane's location q is > 0
+        uint32_t sws[SCAN_ITEMS];
+#pragma unroll
+        for (int q = 0; q < SCAN_ITEMS; ++q) sws[q] = k.l.smask[(wbase + q * 32) >> 5];
 #pragma unroll
         for (int q = 0; q < SCAN_ITEMS; ++q) {
             const uint32_t l = wbase + q * 32 + lane;
             const uint32_t wi = (wbase + q * 32) >> 5;
-            const uint32_t sw = k.l.smask[wi];
+            const uint32_t sw = sws[q];
             if (!sw) continue;  // warp-uniform
             __syncwarp();
             if (lane == 0) k.l.smask[wi] = 0u;
@@ -1571,11 +1605,17 @@ void launch_step_fused(const KArgs& k, uint32_t step, cudaStream_t s) {
 }
 int step_fused_kernels(const KArgs& k) { return k.tune.variant == 3 ? 2 : 1; }
 void launch_count(const KArgs& k, cudaStream_t s) { k_count<<<grid_for(k.a.n, 8), 256, 0, s>>>(k); }
+// the scan reads the per-tile sums kept by the movement kernels; after a
+// full recount they are rebuilt by launch_tile_sums
 void launch_scan(const KArgs& k, uint32_t, int with_hazard, int merge_q, cudaStream_t s) {
     unsigned tiles = (k.l.n + SCAN_TILE - 1) / SCAN_TILE;
     if (!tiles) tiles = 1;
-    k_tile_sums<<<tiles, SCAN_THREADS, 0, s>>>(k);
     k_scan<<<tiles, SCAN_THREADS, 0, s>>>(k, with_hazard, merge_q);
+}
+void launch_tile_sums(const KArgs& k, cudaStream_t s) {
+    unsigned tiles = (k.l.n + SCAN_TILE - 1) / SCAN_TILE;
+    if (!tiles) tiles = 1;
+    k_tile_sums<<<tiles, SCAN_THREADS, 0, s>>>(k);
 }
 void launch_scatter_draw(const KArgs& k, uint32_t step, int scatter, int draw, cudaStream_t s) {
     static unsigned g = 0;
