@@ -225,6 +225,7 @@ typedef struct psim_tuning {
     uint32_t variant;        /* fused step kernel: 0/1/2 = one kernel capped at 64/40/32
                                 registers, 3 = hot/cold split, 4/5 = 2/4 agents per
                                 thread in flight (plain slot atomics) */
+    uint32_t scan_items;     /* locations per thread of the scan: 2, 4 or 8 (0 = 8) */
 } psim_tuning;
 
 typedef struct psim_ctx psim_ctx;

@@ -190,7 +190,6 @@ int initial_regroup(psim_ctx* c) {
     CK(cudaMemsetAsync(c->k.l.sfix, 0, sizeof(unsigned long long) * c->L * c->V, c->stream));
     CK(cudaMemsetAsync(c->k.l.smask, 0, sizeof(uint32_t) * (((size_t)c->L + 2047) / 2048 * 64 + 64), c->stream));
     launch_count(c->k, c->stream);
-    launch_tile_sums(c->k, c->stream);
     launch_scan(c->k, 0, 1, 0, c->stream);
     launch_scatter_draw(c->k, 0, 1, 0, c->stream);
     launch_stats(c->k, 0, c->stream);
@@ -206,7 +205,7 @@ int do_step(psim_ctx* c, uint32_t step, bool draw, bool movement) {
     if (movement) launch_movement(c->k, step, c->stream);
     launch_scan(c->k, step, 1, merge_q, c->stream);
     launch_scatter_draw(c->k, step, 1, draw ? 1 : 0, c->stream);
-    c->launches += movement ? 3 : 2;
+    c->launches += movement ? 4 : 3;
     return launch_check(c);
 }
 
@@ -247,7 +246,7 @@ int capture_day_graph(psim_ctx* c) {
     e = cudaGraphInstantiate(&c->day_graph, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(c, PSIM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
-    c->graph_kernels = (1ull + (uint64_t)step_fused_kernels(c->k)) * c->spd + 1;
+    c->graph_kernels = (2ull + (uint64_t)step_fused_kernels(c->k)) * c->spd + 1;
     c->graph_dirty = false;
     c->prof_valid = false;
     return 0;
@@ -465,7 +464,7 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     if ((rc = dalloc(c, &dl.smask, ((size_t)L + 2047) / 2048 * 64 + 64))) return bail(rc);
     if ((rc = dalloc(c, &dl.no_work_loc, L))) return bail(rc);
     if ((rc = dalloc(c, &dl.flags, L))) return bail(rc);
-    const size_t tiles = (L + 2047) / 2048 + 1;
+    const size_t tiles = (L + 511) / 512 + 1;
     if ((rc = dalloc(c, &dl.tile_sums, tiles))) return bail(rc);
     // replicas
     DevReps& dr = k.r;
@@ -510,13 +509,13 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
         add(dl.infectiousness, 4 * L); add(dl.open, L); add(dl.closed_until, 4 * L); add(dl.quarantine_until, 4 * L);
         // the histogram is kept incrementally across steps and days
         add(dl.counts, 4 * L); add(dl.sfix, 8 * L * V); add(dl.smask, 4 * ((L + 2047) / 2048 * 64 + 64));
-        add(dl.tile_sums, 4 * ((L + 2047) / 2048 + 1));
         add(dr.variant_active, R * V); add(dr.expected, 8 * R);
     }
     k.p = c->params;
     k.spd = c->spd;
     k.track_expected = 0;
     k.tune.agg_count = 1;
+    k.tune.scan_items = 8;
     k.tune.agg_slot = 1;
     k.tune.blocks_per_sm = 0;
     k.tune.variant = 0;
@@ -635,6 +634,9 @@ int psim_set_tuning(psim_ctx* c, const psim_tuning* t) {
     c->k.tune.blocks_per_sm = t->blocks_per_sm;
     if (t->variant > 5) return fail(c, PSIM_ERR_ARG, "variant out of range");
     c->k.tune.variant = t->variant;
+    if (t->scan_items != 0 && t->scan_items != 2 && t->scan_items != 4 && t->scan_items != 8)
+        return fail(c, PSIM_ERR_ARG, "scan_items must be 2, 4 or 8");
+    c->k.tune.scan_items = t->scan_items ? t->scan_items : 8u;
     c->graph_dirty = true;
     return 0;
 }
@@ -645,6 +647,7 @@ int psim_get_tuning(psim_ctx* c, psim_tuning* t) {
     t->agg_slot = c->k.tune.agg_slot;
     t->blocks_per_sm = c->k.tune.blocks_per_sm;
     t->variant = c->k.tune.variant;
+    t->scan_items = c->k.tune.scan_items;
     return 0;
 }
 
@@ -780,12 +783,11 @@ int psim_regroup(psim_ctx* c) {
         CK(cudaMemsetAsync(c->k.l.smask, 0, sizeof(uint32_t) * (((size_t)c->L + 2047) / 2048 * 64 + 64), c->stream));
     CK(cudaMemsetAsync(c->k.l.smask, 0, sizeof(uint32_t) * (((size_t)c->L + 2047) / 2048 * 64 + 64), c->stream));
         launch_count(c->k, c->stream);
-        launch_tile_sums(c->k, c->stream);
-        c->launches += 2;
+        c->launches += 1;
     }
     launch_scan(c->k, 0, 1, c->params.quarantine_policy > 1, c->stream);
     launch_scatter_draw(c->k, 0, 1, 0, c->stream);
-    c->launches += 2;
+    c->launches += 3;
     c->csr_fresh = false;
     int rc = launch_check(c);
     if (rc) return rc;
@@ -1013,7 +1015,7 @@ int psim_time_step_kernels(psim_ctx* c, uint32_t t, float* ms) {
     CK(cudaEventRecord(ev[3], c->stream));
     launch_scan(c->k, step + 1, 1, merge_q, c->stream);
     launch_scatter_draw(c->k, step + 1, 1, 1, c->stream);
-    c->launches += 4 + (uint64_t)step_fused_kernels(c->k);
+    c->launches += 6 + (uint64_t)step_fused_kernels(c->k);
     CK(cudaStreamSynchronize(c->stream));
     for (int j = 0; j < 3; ++j) CK(cudaEventElapsedTime(&ms[j], ev[j], ev[j + 1]));
     for (int j = 0; j < 4; ++j) cudaEventDestroy(ev[j]);

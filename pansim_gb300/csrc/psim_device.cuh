@@ -120,7 +120,7 @@ struct DevLocs {
     float* hazard_x;              // [V][n] its argument x = k*S/n*w*season*dt (adjoint mode)
     uint32_t* no_work_loc;
     uint8_t* flags;               // testing flags
-    uint32_t* tile_sums;          // per-tile sums of the histogram, kept with the counts
+    uint32_t* tile_sums;          // per-tile sums of the histogram (scan, first pass)
 };
 
 struct DevReps {
@@ -156,6 +156,7 @@ struct DevTune {
     uint32_t variant;        // fused step kernel: 0/1/2 = one kernel capped at 64/40/32 registers,
                              // 3 = hot/cold split (lean kernel + queued cold agents),
                              // 4/5 = 2/4 agents per thread in flight
+    uint32_t scan_items;     // locations per scan thread: 2, 4 or 8 (tile = 256 x items)
 };
 
 // Adjoint accumulation (gradient of the expected new infections with respect
@@ -203,7 +204,6 @@ void launch_scan(const KArgs& k, uint32_t step_in_day, int with_hazard, int merg
 void launch_scatter_draw(const KArgs& k, uint32_t step_in_day, int scatter, int draw, cudaStream_t s);
 void launch_offsets(const KArgs& k, cudaStream_t s);
 void launch_step_fused(const KArgs& k, uint32_t step_in_day, cudaStream_t s);
-void launch_tile_sums(const KArgs& k, cudaStream_t s);
 // closure rules
 struct ClosureTypes {
     uint32_t n;

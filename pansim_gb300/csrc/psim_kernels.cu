@@ -414,10 +414,11 @@ __device__ __forceinline__ void move_agent(const KArgs& k, uint32_t i, const Ste
     }
 }
 
-// Scan tiles: 256 threads x 8 locations.
+// Scan tiles: 256 threads x ITEMS locations (ITEMS = 2, 4 or 8, a tuning
+// choice); the masks hold one 32-bit word per warp and item.
 constexpr int SCAN_THREADS = 256;
-constexpr int SCAN_ITEMS = 8;
-constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+constexpr int SCAN_ITEMS_MAX = 8;
+constexpr int SCAN_TILE_MAX = SCAN_THREADS * SCAN_ITEMS_MAX;
 
 // The per-location agent counts are kept up to date incrementally: an agent
 // whose location changed from loc0 to loc moves one count (two fire-and-
@@ -435,22 +436,6 @@ __device__ __forceinline__ void count_agent(const KArgs& k, bool act, uint32_t l
     if (mv) {
         if (loc0 < L) atomicSub(&k.l.counts[loc0], 1u);
         if (loc != NONE) atomicAdd(&k.l.counts[loc], 1u);
-    }
-    // the per-tile sums of the scan follow the counts; movers of a warp
-    // mostly share their tiles, so one reduction per distinct tile
-    // (warp-collective: every lane calls count_agent)
-    const uint32_t t_old = (mv && loc0 < L) ? loc0 / (uint32_t)SCAN_TILE : NONE;
-    const uint32_t t_new = (mv && loc != NONE) ? loc / (uint32_t)SCAN_TILE : NONE;
-    const bool dec = t_old != NONE && t_old != t_new, inc = t_new != NONE && t_old != t_new;
-    const unsigned md = __ballot_sync(0xffffffffu, dec), mi = __ballot_sync(0xffffffffu, inc);
-    const int lane = threadIdx.x & 31;
-    if (dec) {
-        const unsigned peers = __match_any_sync(md, t_old);
-        if (lane == __ffs(peers) - 1) atomicSub(&k.l.tile_sums[t_old], (uint32_t)__popc(peers));
-    }
-    if (inc) {
-        const unsigned peers = __match_any_sync(mi, t_new);
-        if (lane == __ffs(peers) - 1) atomicAdd(&k.l.tile_sums[t_new], (uint32_t)__popc(peers));
     }
     if (act && loc != NONE && inf > 0.0f) {
         const long long q = __float2ll_rn(inf * PSIM_FIX_SCALE_F);
@@ -622,9 +607,8 @@ __global__ void __launch_bounds__(256) k_count(KArgs k) {
 }
 
 // ---------------------------------------------------------------------------
-// Scan of the histogram.  The sums of the tiles of 2048 locations are kept up
-// to date with the counts (k_tile_sums rebuilds them after a full recount);
-// k_scan adds the sums of the tiles before its
+// Scan of the histogram in two passes (reduce, then scan): k_tile_sums adds up
+// each tile of 256 x ITEMS locations; k_scan adds the sums of the tiles before its
 // own (every block reads at most a few thousand 4-byte sums, so the prefix
 // needs no inter-block waiting), scans its tile warp-striped (coalesced),
 // writes the cursor (exclusive prefix = first CSR slot of the location)
@@ -644,13 +628,15 @@ __device__ __forceinline__ uint32_t block_sum_256(uint32_t v, uint32_t* s_red) {
     return tot;
 }
 
+template <int ITEMS>
 __global__ void __launch_bounds__(SCAN_THREADS) k_tile_sums(KArgs k) {
+    constexpr int TILE = SCAN_THREADS * ITEMS;
     __shared__ uint32_t s_red[SCAN_THREADS / 32];
     const uint32_t L = k.l.n;
-    const uint32_t base = blockIdx.x * SCAN_TILE;
+    const uint32_t base = blockIdx.x * TILE;
     uint32_t v = 0;
 #pragma unroll
-    for (int q = 0; q < SCAN_ITEMS; ++q) {
+    for (int q = 0; q < ITEMS; ++q) {
         const uint32_t l = base + q * SCAN_THREADS + threadIdx.x;
         v += l < L ? k.l.counts[l] : 0u;
     }
@@ -658,17 +644,19 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_tile_sums(KArgs k) {
     if (threadIdx.x == 0) k.l.tile_sums[blockIdx.x] = v;
 }
 
+template <int ITEMS>
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, int with_hazard, int merge_q) {
+    constexpr int TILE = SCAN_THREADS * ITEMS;
     __shared__ uint32_t s_red[SCAN_THREADS / 32];
     __shared__ uint32_t s_warp[SCAN_THREADS / 32];
     const uint32_t L = k.l.n;
     const uint32_t tile = blockIdx.x;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t wbase = tile * SCAN_TILE + (uint32_t)warp * (32 * SCAN_ITEMS);
+    const uint32_t wbase = tile * TILE + (uint32_t)warp * (32 * ITEMS);
     if (tile == 0 && threadIdx.x == 0) *k.a.work_count = 0u;  // queue of the next step's cold agents
-    uint32_t c[SCAN_ITEMS], ex[SCAN_ITEMS];
+    uint32_t c[ITEMS], ex[ITEMS];
 #pragma unroll
-    for (int q = 0; q < SCAN_ITEMS; ++q) {
+    for (int q = 0; q < ITEMS; ++q) {
         const uint32_t l = wbase + q * 32 + lane;
         c[q] = l < L ? k.l.counts[l] : 0u;
     }
@@ -689,7 +677,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, int with_hazard,
     const uint32_t prefix = block_sum_256(pre, s_red);
     uint32_t carry = 0;
 #pragma unroll
-    for (int q = 0; q < SCAN_ITEMS; ++q) {
+    for (int q = 0; q < ITEMS; ++q) {
         uint32_t x = c[q];
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -708,7 +696,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, int with_hazard,
     const float season = k.clock->season;
     const uint32_t V = k.m.n_variants;
 #pragma unroll
-    for (int q = 0; q < SCAN_ITEMS; ++q) {
+    for (int q = 0; q < ITEMS; ++q) {
         const uint32_t l = wbase + q * 32 + lane;
         if (l < L) k.l.cursor[l] = base + ex[q];
     }
@@ -717,11 +705,11 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, int with_hazard,
         // are read; elsewhere the hazard is 0 and stays unwritten, the hazard
         // mask keeping readers away from it
         uint32_t any = 0;  // bit q: some variant's hazard of this lane's location q is > 0
-        uint32_t sws[SCAN_ITEMS];
+        uint32_t sws[ITEMS];
 #pragma unroll
-        for (int q = 0; q < SCAN_ITEMS; ++q) sws[q] = k.l.smask[(wbase + q * 32) >> 5];
+        for (int q = 0; q < ITEMS; ++q) sws[q] = k.l.smask[(wbase + q * 32) >> 5];
 #pragma unroll
-        for (int q = 0; q < SCAN_ITEMS; ++q) {
+        for (int q = 0; q < ITEMS; ++q) {
             const uint32_t l = wbase + q * 32 + lane;
             const uint32_t wi = (wbase + q * 32) >> 5;
             const uint32_t sw = sws[q];
@@ -745,14 +733,14 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, int with_hazard,
         }
         // one mask word per 32 locations (wbase is a multiple of 32)
 #pragma unroll
-        for (int q = 0; q < SCAN_ITEMS; ++q) {
+        for (int q = 0; q < ITEMS; ++q) {
             const unsigned word = __ballot_sync(0xffffffffu, (any >> q) & 1u);
             if (lane == 0) k.l.hmask[(wbase + q * 32) >> 5] = word;
         }
     }
     if (merge_q) {
 #pragma unroll
-        for (int q = 0; q < SCAN_ITEMS; ++q) {
+        for (int q = 0; q < ITEMS; ++q) {
             const uint32_t l = wbase + q * 32 + lane;
             if (l < L) {
                 const uint32_t qq = k.l.qu_pending[l];
@@ -1605,17 +1593,21 @@ void launch_step_fused(const KArgs& k, uint32_t step, cudaStream_t s) {
 }
 int step_fused_kernels(const KArgs& k) { return k.tune.variant == 3 ? 2 : 1; }
 void launch_count(const KArgs& k, cudaStream_t s) { k_count<<<grid_for(k.a.n, 8), 256, 0, s>>>(k); }
-// the scan reads the per-tile sums kept by the movement kernels; after a
-// full recount they are rebuilt by launch_tile_sums
+// tile sums, then the scan, with 256 x tune.scan_items locations per tile
 void launch_scan(const KArgs& k, uint32_t, int with_hazard, int merge_q, cudaStream_t s) {
-    unsigned tiles = (k.l.n + SCAN_TILE - 1) / SCAN_TILE;
+    const uint32_t items = k.tune.scan_items == 2 || k.tune.scan_items == 4 ? k.tune.scan_items : 8u;
+    unsigned tiles = (k.l.n + SCAN_THREADS * items - 1) / (SCAN_THREADS * items);
     if (!tiles) tiles = 1;
-    k_scan<<<tiles, SCAN_THREADS, 0, s>>>(k, with_hazard, merge_q);
-}
-void launch_tile_sums(const KArgs& k, cudaStream_t s) {
-    unsigned tiles = (k.l.n + SCAN_TILE - 1) / SCAN_TILE;
-    if (!tiles) tiles = 1;
-    k_tile_sums<<<tiles, SCAN_THREADS, 0, s>>>(k);
+    if (items == 2) {
+        k_tile_sums<2><<<tiles, SCAN_THREADS, 0, s>>>(k);
+        k_scan<2><<<tiles, SCAN_THREADS, 0, s>>>(k, with_hazard, merge_q);
+    } else if (items == 4) {
+        k_tile_sums<4><<<tiles, SCAN_THREADS, 0, s>>>(k);
+        k_scan<4><<<tiles, SCAN_THREADS, 0, s>>>(k, with_hazard, merge_q);
+    } else {
+        k_tile_sums<8><<<tiles, SCAN_THREADS, 0, s>>>(k);
+        k_scan<8><<<tiles, SCAN_THREADS, 0, s>>>(k, with_hazard, merge_q);
+    }
 }
 void launch_scatter_draw(const KArgs& k, uint32_t step, int scatter, int draw, cudaStream_t s) {
     static unsigned g = 0;
