@@ -141,49 +141,57 @@ def mutable_bytes(snap):
     return sum(snap.agents[k].nbytes for k in AGENT_MUTABLE) + sum(snap.locs[k].nbytes for k in LOC_MUTABLE)
 
 
-def cpu_baseline(snap, steps=120):
-    """The oracle port, single thread, on `steps` timesteps of the same workload."""
+def cpu_baseline(snap, min_seconds=8.0):
+    """The oracle port on all host threads (OpenMP): whole days (midnight
+    phases + 144 timesteps) of the same workload until `min_seconds` elapsed."""
     from oracle import binding as ob
     s = snap.copy()
     o = ob.Oracle(s)
-    o.midnight(0)
+    spd = s.steps_per_day
+    days = 0
     t0 = time.perf_counter()
-    for t in range(steps):
-        o.step(t)
-    dt = time.perf_counter() - t0
+    while True:
+        o.run_day(days)
+        days += 1
+        dt = time.perf_counter() - t0
+        if dt >= min_seconds:
+            break
     o.close()
-    return {"value": s.n_agents * steps / dt, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": "%d timesteps from midnight of day 0 of the 2M-agent workload (oracle port, 1 thread)" % steps,
+    return {"value": s.n_agents * spd * days / dt, "unit": UNIT, "cores": ob.threads(), "kind": "port",
+            "sample": "%d whole days (midnight + %d timesteps) of the 2M-agent workload from day 0, "
+                      "oracle port on %d threads" % (days, spd, ob.threads()),
             "seconds": round(dt, 3)}
 
 
 def run_reference(args, ws, rank):
+    """The reference path's CPU implementation on the host cores: the oracle
+    port (OpenMP over agents and locations), one bench step = one simulated
+    day (midnight phases + 144 timesteps), as in the GPU arm."""
     if rank != 0:
         return 0
     from oracle import binding as ob
     snap = make_snapshot(0)
     o = ob.Oracle(snap)
-    o.midnight(0)
-    per_step_ts = 12  # timesteps per bench step: a bounded sample of a day
-    t = 0
+    spd = snap.steps_per_day
+    day = 0
     for _ in range(args.warmup):
-        for _ in range(per_step_ts):
-            o.step(t)
-            t += 1
+        o.run_day(day)
+        day += 1
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        for _ in range(per_step_ts):
-            o.step(t)
-            t += 1
+        o.run_day(day)
+        day += 1
     dt = time.perf_counter() - t0
-    value = snap.n_agents * per_step_ts * args.steps / dt
+    value = snap.n_agents * spd * args.steps / dt
+    cores = ob.threads()
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dt * 1000 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "2M agents, 500k non-home locations, dt 10 min", "agents": snap.n_agents,
-                       "locations": snap.n_locations, "timesteps_per_step": per_step_ts},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
-                             "sample": "%d timesteps per step of the 2M-agent workload, oracle port" % per_step_ts},
+            "config": {"workload": "2M agents, 500k non-home locations (+homes), dt 10 min, 1 day per step",
+                       "agents": snap.n_agents, "locations": snap.n_locations, "timesteps_per_step": spd},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "%d simulated days after %d warm-up days, oracle port on %d threads"
+                                       % (args.steps, args.warmup, cores)},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0

@@ -17,16 +17,19 @@ LIB = os.path.join(BUILD, "libpsim_oracle.so")
 
 
 def build(force=False):
-    """gcc -O2 -ffp-contract=off: no FMA contraction, so FP results match the device."""
+    """gcc -O2 -ffp-contract=off -fopenmp: no FMA contraction, so FP results
+    match the device; the per-step loops run on all host threads (the results
+    do not depend on their number)."""
     src = os.path.join(HERE, "psim_oracle.c")
     deps = [src, os.path.join(HERE, "psim_oracle.h"),
             os.path.join(HERE, "..", "pansim_gb300", "csrc", "psim_rng.h"),
+            os.path.join(HERE, "..", "pansim_gb300", "csrc", "psim_immunity.h"),
             os.path.join(HERE, "..", "include", "pansim_gb300.h")]
     if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     tmp = LIB + ".%d.tmp" % os.getpid()
-    subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-o", tmp, src, "-lm"])
+    subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-o", tmp, src, "-lm"])
     os.replace(tmp, LIB)
     return LIB
 
@@ -54,6 +57,8 @@ def lib():
         L.psim_oracle_midnight.argtypes = [P, U32, P]
         L.psim_oracle_run_day.argtypes = [P, U32, P]
         L.psim_oracle_expose.argtypes = [P, U32, U32, D]
+        L.psim_oracle_threads.restype = C.c_int
+        L.psim_oracle_threads.argtypes = []
         L.psim_oracle_immunization_init.argtypes = [P, P]
         L.psim_oracle_immunize.restype = U32
         L.psim_oracle_immunize.argtypes = [P, U32]
@@ -152,6 +157,11 @@ class Oracle:
 
     def immunize(self, t):
         return lib().psim_oracle_immunize(self.h, t)
+
+
+def threads():
+    """Host threads the oracle's parallel loops use."""
+    return lib().psim_oracle_threads()
 
 
 def philox(ctr, key):

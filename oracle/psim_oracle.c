@@ -26,6 +26,9 @@
 #include <stdlib.h>
 #include <string.h>
 #include <math.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 #define NONE 0xFFFFFFFFu
 #define WB_W 0
@@ -44,6 +47,7 @@ struct psim_oracle {
     uint32_t* loc_rep;     /* [L] */
     uint32_t* csr_off;     /* [L+1] */
     uint32_t* csr_agents;  /* [N] */
+    uint32_t* cursor;      /* [L+1] scatter cursors of the regroup */
     uint32_t* qu_pending;  /* [L] */
     uint32_t* no_work_loc; /* [L] */
     uint8_t* loc_flags;    /* [L] testing flags */
@@ -123,9 +127,14 @@ static uint32_t find_location(psim_oracle* o, uint32_t i, uint32_t loc_type, int
 }
 
 
+/* quarantine written during a step: combined with max (atomically, as agents
+ * move in parallel) and made visible from the next step */
 static void qu_write(psim_oracle* o, uint32_t loc, uint32_t until) {
     if (loc == NONE || loc >= o->l->n) return;
-    if (o->qu_pending[loc] < until) o->qu_pending[loc] = until;
+    uint32_t cur = __atomic_load_n(&o->qu_pending[loc], __ATOMIC_RELAXED);
+    while (cur < until &&
+           !__atomic_compare_exchange_n(&o->qu_pending[loc], &cur, until, 1, __ATOMIC_RELAXED, __ATOMIC_RELAXED)) {
+    }
 }
 
 /* RealMovementOps::quarantineAgent, movementPolicies.h:176-245 */
@@ -444,9 +453,14 @@ static uint32_t day_of_week(const psim_oracle* o, uint32_t t) {
 void psim_oracle_movement(psim_oracle* o, uint32_t t) {
     uint32_t minutes = (t % o->spd) * o->p.time_step;
     uint32_t day = day_of_week(o, t);
-    for (uint32_t i = 0; i < o->a->n; ++i) do_movement(o, i, t, minutes, day);
+    const int64_t N = o->a->n, L = o->l->n;
+    /* every agent touches only its own state (plus the max-combined
+     * quarantine writes), so the agents run in parallel */
+#pragma omp parallel for schedule(dynamic, 4096)
+    for (int64_t i = 0; i < N; ++i) do_movement(o, (uint32_t)i, t, minutes, day);
     /* location quarantine written this step becomes visible from the next one */
-    for (uint32_t l = 0; l < o->l->n; ++l) {
+#pragma omp parallel for schedule(static)
+    for (int64_t l = 0; l < L; ++l) {
         if (o->qu_pending[l] > o->l->quarantine_until[l]) o->l->quarantine_until[l] = o->qu_pending[l];
         o->qu_pending[l] = 0;
     }
@@ -454,15 +468,64 @@ void psim_oracle_movement(psim_oracle* o, uint32_t t) {
 
 /* Util::updatePerLocationAgentLists, util.cpp:55-108 with the stable sort of
  * :69: agents grouped by location, ascending agent id within a location. */
+static int cmp_u32(const void* x, const void* y) {
+    uint32_t a = *(const uint32_t*)x, b = *(const uint32_t*)y;
+    return a < b ? -1 : a > b;
+}
+
 void psim_oracle_regroup(psim_oracle* o) {
-    uint32_t L = o->l->n, N = o->a->n;
+    const int64_t L = o->l->n, N = o->a->n;
     memset(o->csr_off, 0, sizeof(uint32_t) * (L + 1));
-    for (uint32_t i = 0; i < N; ++i) o->csr_off[o->a->location[i] + 1]++;
-    for (uint32_t l = 0; l < L; ++l) o->csr_off[l + 1] += o->csr_off[l];
-    uint32_t* cur = (uint32_t*)malloc(sizeof(uint32_t) * (L + 1));
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < N; ++i) __atomic_fetch_add(&o->csr_off[o->a->location[i] + 1], 1u, __ATOMIC_RELAXED);
+    /* inclusive prefix of csr_off[1..L]: per-chunk sums, then the chunks in parallel */
+    {
+        enum { CHUNKS = 64 };
+        uint32_t part[CHUNKS + 1];
+        const int64_t per = (L + CHUNKS - 1) / CHUNKS;
+        part[0] = 0;
+#pragma omp parallel for schedule(static)
+        for (int c = 0; c < CHUNKS; ++c) {
+            uint32_t acc = 0;
+            const int64_t b = 1 + (int64_t)c * per, e = b + per < L + 1 ? b + per : L + 1;
+            for (int64_t l = b; l < e; ++l) acc += o->csr_off[l];
+            part[c + 1] = acc;
+        }
+        for (int c = 0; c < CHUNKS; ++c) part[c + 1] += part[c];
+#pragma omp parallel for schedule(static)
+        for (int c = 0; c < CHUNKS; ++c) {
+            uint32_t acc = part[c];
+            const int64_t b = 1 + (int64_t)c * per, e = b + per < L + 1 ? b + per : L + 1;
+            for (int64_t l = b; l < e; ++l) {
+                acc += o->csr_off[l];
+                o->csr_off[l] = acc;
+            }
+        }
+    }
+    uint32_t* cur = o->cursor;
     memcpy(cur, o->csr_off, sizeof(uint32_t) * (L + 1));
-    for (uint32_t i = 0; i < N; ++i) o->csr_agents[cur[o->a->location[i]]++] = i;
-    free(cur);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < N; ++i)
+        o->csr_agents[__atomic_fetch_add(&cur[o->a->location[i]], 1u, __ATOMIC_RELAXED)] = (uint32_t)i;
+    /* ascending agent id inside each location (the stable sort's order) */
+#pragma omp parallel for schedule(dynamic, 4096)
+    for (int64_t l = 0; l < L; ++l) {
+        uint32_t b = o->csr_off[l], e = o->csr_off[l + 1];
+        uint32_t* x = o->csr_agents + b;
+        uint32_t n = e - b;
+        if (n > 32) {
+            qsort(x, n, sizeof(uint32_t), cmp_u32);
+            continue;
+        }
+        for (uint32_t j = 1; j < n; ++j) {
+            uint32_t v = x[j], q = j;
+            while (q > 0 && x[q - 1] > v) {
+                x[q] = x[q - 1];
+                --q;
+            }
+            x[q] = v;
+        }
+    }
 }
 
 /* BasicInfection::infectionsAtLocations (infectionPolicies.h:481-546) and
@@ -476,7 +539,9 @@ void psim_oracle_infect(psim_oracle* o, uint32_t t, uint32_t v, float* hazard_f,
     float season_f = (float)psim_oracle_seasonality(p, t, o->spd);
     double season_d = psim_oracle_seasonality(p, t, o->spd);
     float* r = (float*)malloc(sizeof(float) * L);
-    for (uint32_t l = 0; l < L; ++l) {
+#pragma omp parallel for schedule(dynamic, 4096)
+    for (int64_t ll = 0; ll < (int64_t)L; ++ll) {
+        uint32_t l = (uint32_t)ll;
         uint32_t b = o->csr_off[l], e = o->csr_off[l + 1];
         int64_t fix = 0;
         double s64 = 0.0;
@@ -504,20 +569,36 @@ void psim_oracle_infect(psim_oracle* o, uint32_t t, uint32_t v, float* hazard_f,
     }
     if (exp_out)
         for (uint32_t q = 0; q < o->r.n; ++q) exp_out[q] = 0.0;
-    for (uint32_t i = 0; i < N; ++i) {
+    /* per-thread partial sums of the expected infections, added in thread order */
+    int nt = 1;
+#ifdef _OPENMP
+    nt = omp_get_max_threads();
+#endif
+    const uint32_t R = o->r.n;
+    double* part = (double*)calloc((size_t)nt * R, sizeof(double));
+#pragma omp parallel
+    {
+    int tid = 0;
+#ifdef _OPENMP
+    tid = omp_get_thread_num();
+#endif
+    double* mine = part + (size_t)tid * R;
+#pragma omp for schedule(static)
+    for (int64_t ii = 0; ii < (int64_t)N; ++ii) {
+        uint32_t i = (uint32_t)ii;
         uint32_t loc = a->location[i];
         float su = a->susceptible[(size_t)v * N + i];
         float s_eff = su * p->sigma_band[a->band[i]];
         if (p64) {
             p64[i] = (r64 ? r64[loc] : (double)r[loc]) * (double)su * (double)p->sigma_band[a->band[i]];
         }
-        if (s_eff > 0.0f) {
+        /* a zero ratio cannot infect (U >= 0): no draw */
+        if (s_eff > 0.0f && r[loc] > 0.0f) {
             float pf = r[loc] * s_eff;
             uint32_t rep = o->agent_rep[i];
             uint32_t li = i - o->r.agent_offset[rep];
             double term = pf < 1.0f ? (double)pf : 1.0;
-            o->expected[rep] += term;
-            if (exp_out) exp_out[rep] += term;
+            mine[rep] += term;
             double U = psim_u01_once(o->r.seed[rep], li, t, PSIM_PHASE_INFECT + v);
             if (U < (double)pf) {
                 /* DynamicPPState::gotInfected, dynamicPPState.cpp:235-244 */
@@ -534,6 +615,13 @@ void psim_oracle_infect(psim_oracle* o, uint32_t t, uint32_t v, float* hazard_f,
             }
         }
     }
+    }
+    for (int q = 0; q < nt; ++q)
+        for (uint32_t rr = 0; rr < R; ++rr) {
+            o->expected[rr] += part[(size_t)q * R + rr];
+            if (exp_out) exp_out[rr] += part[(size_t)q * R + rr];
+        }
+    free(part);
     free(r);
 }
 
@@ -598,7 +686,9 @@ void psim_oracle_progress(psim_oracle* o, uint32_t t) {
     psim_agents* a = o->a;
     const psim_model* m = o->m;
     const psim_params* p = &o->p;
-    for (uint32_t i = 0; i < a->n; ++i) {
+#pragma omp parallel for schedule(dynamic, 4096)
+    for (int64_t ii = 0; ii < (int64_t)a->n; ++ii) {
+        uint32_t i = (uint32_t)ii;
         uint32_t rep = o->agent_rep[i];
         uint32_t li = i - o->r.agent_offset[rep];
         psim_stream rng;
@@ -954,6 +1044,15 @@ void psim_oracle_run_day(psim_oracle* o, uint32_t day, psim_day_stats* out) {
     for (uint32_t s = 0; s < o->spd; ++s) psim_oracle_step(o, t0 + s, NULL);
 }
 
+/* host threads the parallel loops use */
+int psim_oracle_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
 /* Closure rule ExposeToMutation, closurePolicies.h:349-392: each agent with
  * susceptibility s > 0 for the variant is infected when a uniform draw is
  * below fraction * s; the draw comes from the agent's EXPOSE stream. */
@@ -1209,6 +1308,7 @@ psim_oracle* psim_oracle_create(const psim_model* m, psim_agents* a, psim_locati
     }
     o->csr_off = (uint32_t*)calloc(l->n + 1, sizeof(uint32_t));
     o->csr_agents = (uint32_t*)calloc(a->n ? a->n : 1, sizeof(uint32_t));
+    o->cursor = (uint32_t*)calloc(l->n + 1, sizeof(uint32_t));
     o->qu_pending = (uint32_t*)calloc(l->n ? l->n : 1, sizeof(uint32_t));
     o->no_work_loc = (uint32_t*)calloc(l->n ? l->n : 1, sizeof(uint32_t));
     o->loc_flags = (uint8_t*)calloc(l->n ? l->n : 1, 1);
@@ -1234,6 +1334,7 @@ void psim_oracle_destroy(psim_oracle* o) {
     free(o->loc_rep);
     free(o->csr_off);
     free(o->csr_agents);
+    free(o->cursor);
     free(o->qu_pending);
     free(o->no_work_loc);
     free(o->loc_flags);

@@ -45,6 +45,8 @@ void psim_oracle_midnight(psim_oracle* o, uint32_t t, psim_day_stats* out /* [R]
 void psim_oracle_run_day(psim_oracle* o, uint32_t day, psim_day_stats* out /* [R] */);
 /* closure rule ExposeToMutation: infect with variant v at timestamp t */
 void psim_oracle_expose(psim_oracle* o, uint32_t t, uint32_t v, double fraction);
+/* host threads of the parallel loops (OpenMP) */
+int psim_oracle_threads(void);
 /* immunization: categories (init), Immunization::update (immunize; returns immunizedToday) */
 void psim_oracle_immunization_init(psim_oracle* o, const psim_immunization* imm);
 uint32_t psim_oracle_immunize(psim_oracle* o, uint32_t t);
