@@ -46,6 +46,20 @@ def dist_env():
     return ws, rank, local
 
 
+def whole_job(total_ms, agents_per_rank, timesteps_per_step, steps, ws, dist=None, device="cuda"):
+    """(max over ranks of the timed milliseconds, whole-job agent-steps/s):
+    every rank runs its own replica of the same size (weak scaling), so the
+    job processes ws times the per-rank agent-steps in the slowest rank's time."""
+    t_max = float(total_ms)
+    if dist is not None and ws > 1:
+        import torch
+        tt = torch.tensor([float(total_ms)], device=device, dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max = float(tt.item())
+    value = agents_per_rank * ws * timesteps_per_step * steps / (t_max / 1000.0)
+    return t_max, value
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -345,12 +359,8 @@ def main():
     torch.cuda.synchronize()
     launches = g.launch_count() - launches0
     clocks = sampler.stop()
-    t_max = total_ms
-    if dist:
-        tt = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt.item())
     spd = snap.steps_per_day
+    t_max, value = whole_job(total_ms, snap.n_agents, spd, args.steps, ws, dist, "cuda")
     # per-kernel launch durations (roofline): the same days again with
     # event-record nodes around every kernel group of the day graph, on the
     # library's stream.  The nodes add gaps between kernels, so this pass is
@@ -372,8 +382,6 @@ def main():
     # average launch durations: movement(0) once a day, scan every step, fused
     # scatter/draw/movement on all steps but the last
     kms = [kms_sum[0] / n_prof, kms_sum[1] / (n_prof * spd), kms_sum[2] / (n_prof * (spd - 1))]
-    agent_steps = snap.n_agents * 144 * args.steps * ws
-    value = agent_steps / (t_max / 1000.0)
 
     # end to end through the C ABI with pinned host buffers: per step, the
     # full mutable state host->device, one day, the full state device->host
