@@ -562,11 +562,13 @@ int psim_destroy(psim_ctx* c) {
 int psim_upload(psim_ctx* c, const psim_agents* a, const psim_locations* l) {
     if (!c) return PSIM_ERR_ARG;
     if (!a || !l || a->n != c->N || l->n != c->L) return fail(c, PSIM_ERR_ARG, "snapshot size mismatch");
-    for (uint32_t i = 0; i < c->N; ++i)
-        if (a->location[i] >= c->L) return fail(c, PSIM_ERR_RANGE, "agent location out of range");
     int rc = upload_mutable(c, a, l);
     if (rc) return rc;
-    return initial_regroup(c);
+    // locations are checked on the device by the histogram pass
+    rc = initial_regroup(c);
+    if (rc == PSIM_ERR_DEVICE && c->err.find("invalid location") != std::string::npos)
+        return fail(c, PSIM_ERR_RANGE, "agent location out of range");
+    return rc;
 }
 
 int psim_download(psim_ctx* c, psim_agents* a, psim_locations* l) {

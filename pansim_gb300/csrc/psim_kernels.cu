@@ -1210,88 +1210,114 @@ __global__ void __launch_bounds__(256) k_test(KArgs k, uint32_t t) {
 // the host.
 constexpr int STAT_FIELDS = 48;
 
-__global__ void __launch_bounds__(256) k_stats(KArgs k, uint32_t t, int with_tests) {
-    const uint32_t N = k.a.n, V = k.m.n_variants;
-    const uint32_t day_steps = 24u * 60u / k.p.time_step;
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool act = i < N;
-    unsigned c[STAT_FIELDS];
-#pragma unroll
-    for (int f = 0; f < STAT_FIELDS; ++f) c[f] = 0;
-    double imm[PSIM_MAX_STRAINS];
-#pragma unroll
-    for (int v = 0; v < PSIM_MAX_STRAINS; ++v) imm[v] = 0.0;
-    uint32_t rep = 0;
-    if (act) {
-        rep = k.a.rep[i];
-        const uint8_t st = (uint8_t)k.a.state[i];
-        const uint32_t wb = k.m.state_wb[st];
-        const bool inf = k.m.state_infected[st] != 0;
-        c[SC_HOSP] = (wb != WB_D && wb != WB_S && t < k.a.st_hospitalized_until[i]);
-        const bool isq = k.a.st_quarantined_ts[i] <= t && k.a.st_quarantined_until[i] > t;
-        c[SC_Q] = isq;
-        c[SC_QT] = isq && inf;
-        c[SC_NQ] = !isq && inf;
-        c[SC_STAYED] = k.a.stayed_home[i] != 0;
-        const bool new_inf = k.a.st_infected_ts[i] > t - day_steps && k.a.st_infected_ts[i] <= t;
-        c[SC_NI] = new_inf;
-        const uint32_t ic = k.a.st_infected_count[i], mc = k.a.st_immunization_count[i];
-        c[SC_INF_ONCE] = ic > 0;
-        c[SC_REINF] = ic > 1 ? ic - 1 : 0;
-        c[SC_BSTR] = mc > 1 ? mc - 1 : 0;
-        c[SC_ALL_INF] = inf;
-        if (k.a.hcw[i]) {
-            c[SC_HCI] = (inf || k.a.quarantined[i]) ? 1u : 0u;
-            c[SC_HCE] = new_inf;
-        }
-        c[SC_INFH] = inf && loc_type(k, k.a.location[i]) == k.p.hospital_type;
-        c[SC_VNI] = ic == 0 && mc > 0;
-        if (with_tests) {
-            c[SC_TESTS] = k.a.last_test[i] == t;
-            const uint32_t d = k.a.st_diagnosed_ts[i];
-            c[SC_P1] = d == t;
-            c[SC_P2] = d < t && d > t - day_steps;
-        }
-        if (st < 16) c[SC_HIST + st] = 1;
-        const uint32_t var = k.a.variant[i];
-        if (inf && var < PSIM_MAX_STRAINS) c[SC_VAR + var] = 1;
-        const uint32_t mask = k.a.st_variant_mask[i];
-        for (uint32_t v = 0; v < V; ++v) {
-            if (mask & (1u << v)) c[SC_INFV + v] = 1;
-            imm[v] = 1.0 - (double)k.a.susceptible[(size_t)v * N + i];
-        }
-    }
-    // warp reduction when the warp is within one replica, else per-thread atomics
-    const unsigned am = __ballot_sync(0xffffffffu, act);
+// reduce the per-thread counters of a warp whose lanes all hold replica
+// `rep` (else per-lane) into the replica's accumulator
+__device__ __forceinline__ void stats_flush(const KArgs& k, uint32_t rep, unsigned* c, double* imm, uint32_t V) {
     const uint32_t rep0 = __shfl_sync(0xffffffffu, rep, 0);
-    const bool uniform = __all_sync(0xffffffffu, !act || rep == rep0);
+    const bool uniform = __all_sync(0xffffffffu, rep == rep0);
+    const bool lead = (threadIdx.x & 31) == 0;
     if (uniform) {
 #pragma unroll
         for (int f = 0; f < STAT_FIELDS; ++f) {
             unsigned x = c[f];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-            c[f] = x;
+            if (lead && rep0 != NONE && x) atomicAdd(&k.stats[rep0].c[f], x);
+            c[f] = 0;
         }
-        for (uint32_t v = 0; v < V; ++v) {
-            double x = imm[v];
-            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-            imm[v] = x;
+#pragma unroll
+        for (int v = 0; v < PSIM_MAX_STRAINS; ++v) {
+            if ((uint32_t)v < V) {
+                double x = imm[v];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+                if (lead && rep0 != NONE && x != 0.0) atomicAdd(&k.stats[rep0].imm[v], x);
+            }
+            imm[v] = 0.0;
         }
-        if ((threadIdx.x & 31) == 0 && am) {
-            DevStatsAcc* S = &k.stats[rep0];
-            for (int f = 0; f < STAT_FIELDS; ++f)
-                if (c[f]) atomicAdd(&S->c[f], c[f]);
-            for (uint32_t v = 0; v < V; ++v)
-                if (imm[v] != 0.0) atomicAdd(&S->imm[v], imm[v]);
+    } else {
+#pragma unroll
+        for (int f = 0; f < STAT_FIELDS; ++f) {
+            if (rep != NONE && c[f]) atomicAdd(&k.stats[rep].c[f], c[f]);
+            c[f] = 0;
         }
-    } else if (act) {
-        DevStatsAcc* S = &k.stats[rep];
-        for (int f = 0; f < STAT_FIELDS; ++f)
-            if (c[f]) atomicAdd(&S->c[f], c[f]);
-        for (uint32_t v = 0; v < V; ++v)
-            if (imm[v] != 0.0) atomicAdd(&S->imm[v], imm[v]);
+#pragma unroll
+        for (int v = 0; v < PSIM_MAX_STRAINS; ++v) {
+            if ((uint32_t)v < V && rep != NONE && imm[v] != 0.0) atomicAdd(&k.stats[rep].imm[v], imm[v]);
+            imm[v] = 0.0;
+        }
     }
+}
+
+// The statistics row (Simulation::refreshAndPrintStatistics, simulation.h:473-665)
+// in one pass: each block walks a contiguous range of agents, every thread
+// accumulates its agents' counters in registers and flushes them (one
+// reduction per warp) when its replica changes and at the end.
+__global__ void __launch_bounds__(256) k_stats(KArgs k, uint32_t t, int with_tests) {
+    const uint32_t N = k.a.n, V = k.m.n_variants;
+    const uint32_t day_steps = 24u * 60u / k.p.time_step;
+    unsigned c[STAT_FIELDS];
+#pragma unroll
+    for (int f = 0; f < STAT_FIELDS; ++f) c[f] = 0;
+    double imm[PSIM_MAX_STRAINS];
+#pragma unroll
+    for (int v = 0; v < PSIM_MAX_STRAINS; ++v) imm[v] = 0.0;
+    const uint32_t per = ((N + gridDim.x - 1) / gridDim.x + 255u) & ~255u;
+    const uint32_t begin = blockIdx.x * per, end = min(N, begin + per);
+    uint32_t cur = NONE;
+    for (uint32_t base = begin; base < end; base += 256u) {
+        const uint32_t i = base + threadIdx.x;
+        const bool act = i < end;
+        const uint32_t rep = act ? (uint32_t)k.a.rep[i] : cur;
+        // a replica boundary inside the warp: flush what was gathered so far
+        if (__any_sync(0xffffffffu, rep != cur)) {
+            stats_flush(k, cur, c, imm, V);
+            cur = rep;
+        }
+        if (!act) continue;
+        const uint8_t st = (uint8_t)k.a.state[i];
+        const uint32_t wb = k.m.state_wb[st];
+        const bool inf = k.m.state_infected[st] != 0;
+        c[SC_HOSP] += (wb != WB_D && wb != WB_S && t < k.a.st_hospitalized_until[i]);
+        const bool isq = k.a.st_quarantined_ts[i] <= t && k.a.st_quarantined_until[i] > t;
+        c[SC_Q] += isq;
+        c[SC_QT] += isq && inf;
+        c[SC_NQ] += !isq && inf;
+        c[SC_STAYED] += k.a.stayed_home[i] != 0;
+        const bool new_inf = k.a.st_infected_ts[i] > t - day_steps && k.a.st_infected_ts[i] <= t;
+        c[SC_NI] += new_inf;
+        const uint32_t ic = k.a.st_infected_count[i], mc = k.a.st_immunization_count[i];
+        c[SC_INF_ONCE] += ic > 0;
+        c[SC_REINF] += ic > 1 ? ic - 1 : 0;
+        c[SC_BSTR] += mc > 1 ? mc - 1 : 0;
+        c[SC_ALL_INF] += inf;
+        if (k.a.hcw[i]) {
+            c[SC_HCI] += (inf || k.a.quarantined[i]) ? 1u : 0u;
+            c[SC_HCE] += new_inf;
+        }
+        c[SC_INFH] += inf && loc_type(k, k.a.location[i]) == k.p.hospital_type;
+        c[SC_VNI] += ic == 0 && mc > 0;
+        if (with_tests) {
+            c[SC_TESTS] += k.a.last_test[i] == t;
+            const uint32_t d = k.a.st_diagnosed_ts[i];
+            c[SC_P1] += d == t;
+            c[SC_P2] += d < t && d > t - day_steps;
+        }
+#pragma unroll
+        for (int q = 0; q < 16; ++q) c[SC_HIST + q] += st == (uint8_t)q;
+        const uint32_t var = k.a.variant[i];
+#pragma unroll
+        for (int v = 0; v < PSIM_MAX_STRAINS; ++v) c[SC_VAR + v] += inf && var == (uint32_t)v;
+        const uint32_t mask = k.a.st_variant_mask[i];
+#pragma unroll
+        for (int v = 0; v < PSIM_MAX_STRAINS; ++v) {
+            if ((uint32_t)v < V) {
+                c[SC_INFV + v] += (mask >> v) & 1u;
+                imm[v] += 1.0 - (double)k.a.susceptible[(size_t)v * N + i];
+            }
+        }
+    }
+    stats_flush(k, cur, c, imm, V);
 }
 
 // variant gating of the next day (countVariantCases, simulation.h:768-777)
@@ -1635,7 +1661,9 @@ void launch_test(const KArgs& k, uint32_t t, cudaStream_t s) {
 }
 void launch_stats(const KArgs& k, uint32_t t, cudaStream_t s) {
     cudaMemsetAsync(k.stats, 0, sizeof(DevStatsAcc) * k.r.n, s);
-    unsigned blocks = (k.a.n + 255) / 256;
+    static unsigned g = 0;
+    if (!g) g = wave_grid(k_stats, 1u << 30);
+    unsigned blocks = std::min(g, (unsigned)((k.a.n + 255) / 256));
     k_stats<<<blocks ? blocks : 1, 256, 0, s>>>(k, t, 1);
     k_variant_active<<<1, 256, 0, s>>>(k);
 }
