@@ -211,6 +211,56 @@ def run_reference(args, ws, rank):
     return 0
 
 
+def run_policy(args):
+    """Config 3: 20M agents, 5M locations, quarantine policy 3 (10 days),
+    testing (5e-5 / 1e-2 / 5e-4 / 5e-4 / 5e-3, PCR), closures of work, school
+    and shops while daily new infections exceed 0.05% of the population, and
+    immunization of 50k a day from day 7 in a 6-category order."""
+    import numpy as np
+    import torch
+    from pansim_gb300 import closures, immunization, native, synth
+    snap = synth.config_snapshot(3, scale=args.scale)
+    N = snap.n_agents
+    g = native.GpuSim(snap)
+    rules = [dict(name="lockdown", conditionType="newCasesFraction", threshold=0.0005, threshold2=0.00025,
+                  closeAfter=1, openAfter=7, parameter=0,
+                  locationTypesToClose=[synth.WORK, synth.SCHOOL, synth.SHOP])]
+    g.closures_init(rules, closures.stats_header(synth.STATE_NAMES))
+    g.immunization_init(immunization.options(immunizations_per_week=int(350_000 * args.scale), immunizationStart=7,
+                                             immunizationOrder="1,2,3,4,5,6,0,0,0,0", boosterStart="1000",
+                                             boosters_per_week=[([0], [1.0] * 10)]))
+    spd = snap.steps_per_day
+    days = args.days if args.days > 2 else 28
+    for d in range(args.warmup):
+        g.run_day(d)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    graph_ms = 0.0
+    rows = []
+    for d in range(args.warmup, days):
+        st = g.run_day(d)
+        graph_ms += g.last_day_ms()
+        rows.append(list(st[0].v)[: st[0].n])
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    n_days = days - args.warmup
+    act, op = g.closures_status()
+    vac_col = len(synth.STATE_NAMES) + 9
+    line = {"metric": "agent-steps/s at 20M agents, policy-heavy", "value": N * spd * n_days / dt,
+            "unit": UNIT, "higher_is_better": True, "days": n_days, "warmup_days": args.warmup,
+            "graph_ms_per_day": graph_ms / n_days, "ms_per_day": dt * 1000 / n_days,
+            "step_roofline_frac": (STEP_BYTES[0] * N + STEP_BYTES[1] * snap.n_locations) /
+                                  (graph_ms / n_days / spd * 1e-3) / 1e9 / peaks()[0],
+            "immunized_total": int(sum(r[vac_col] for r in rows)),
+            "closure_rule_active_at_end": bool(act[0]) if len(act) else None,
+            "data": "synthetic", "dtype": "f32",
+            "config": {"workload": "20M agents, 5M non-home locations (+homes), quarantine 3, testing, closures, "
+                                   "immunization", "agents": N, "locations": snap.n_locations, "scale": args.scale}}
+    print(json.dumps(line, default=float))
+    g.close()
+    return 0
+
+
 def run_batched(args):
     """64 replicas, agent counts log-uniform on [250k, 2M], k log-uniform on
     [1e-4, 1e-3], independent seeds: one context over the concatenation vs the
@@ -301,7 +351,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=40)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="step", choices=["step", "batched", "adjoint"])
+    ap.add_argument("--workload", default="step", choices=["step", "batched", "adjoint", "policy"])
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--days", type=int, default=2)
     args = ap.parse_args()
@@ -309,6 +359,8 @@ def main():
         return run_batched(args) or 0
     if args.workload == "adjoint":
         return run_adjoint(args) or 0
+    if args.workload == "policy":
+        return run_policy(args) or 0
     if args.warmup < 3:
         args.warmup = 3
     ws, rank, local = dist_env()
