@@ -122,6 +122,7 @@ int validate(psim_ctx* c, const psim_model* m, const psim_agents* a, const psim_
     if (m->n_variants == 0 || m->n_variants > PSIM_MAX_STRAINS) return fail(c, PSIM_ERR_ARG, "n_variants out of range");
     if (m->n_states == 0 || m->n_states > 16) return fail(c, PSIM_ERR_ARG, "n_states must be 1..16");
     if (l->n == 0) return fail(c, PSIM_ERR_ARG, "no locations");
+    if (a->n == 0) return fail(c, PSIM_ERR_ARG, "no agents");
     const uint32_t N = a->n, L = l->n;
     if (!a->loc_offset || a->loc_offset[0] != 0 || a->loc_offset[N] != a->n_poss)
         return fail(c, PSIM_ERR_RANGE, "per-agent location offsets inconsistent");
@@ -362,6 +363,15 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
         // the cemetery is the location appended last (locationList.h:168-175)
         if (c->rep_loc_off[q + 1] == c->rep_loc_off[q] || c->rep_cemetery[q] != c->rep_loc_off[q + 1] - 1)
             return bail(fail(c, PSIM_ERR_RANGE, "cemetery is not the last location of its replica"));
+        // replicas do not share locations
+        for (uint32_t i = c->rep_agent_off[q]; i < c->rep_agent_off[q + 1]; ++i) {
+            if (a->location[i] < c->rep_loc_off[q] || a->location[i] >= c->rep_loc_off[q + 1])
+                return bail(fail(c, PSIM_ERR_RANGE, "agent " + std::to_string(i) + " outside its replica's locations"));
+            for (uint32_t j = a->loc_offset[i]; j < a->loc_offset[i + 1]; ++j)
+                if (a->poss_loc[j] < c->rep_loc_off[q] || a->poss_loc[j] >= c->rep_loc_off[q + 1])
+                    return bail(fail(c, PSIM_ERR_RANGE,
+                                     "agent " + std::to_string(i) + " has a location outside its replica"));
+        }
     }
     c->device = device;
     cudaError_t e = cudaSetDevice(device);

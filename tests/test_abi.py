@@ -69,3 +69,24 @@ def test_create_without_device_fails_cleanly():
         return
     rc, msg = _create(small_snapshot(500, 120))
     assert rc == -2, (rc, msg)
+
+
+def test_create_rejects_empty_population_and_shared_replica_locations():
+    import numpy as np
+    from pansim_gb300 import snapshot as snp
+    from tests.helpers import small_snapshot
+    s = small_snapshot(300, 80)
+    empty = s.copy()
+    for k in list(empty.agents):
+        if k == "loc_offset":
+            empty.agents[k] = np.zeros(1, np.uint32)
+        else:
+            empty.agents[k] = empty.agents[k][:0]
+    empty.reps["agent_offset"][:] = [0, 0]
+    rc, msg = _create(empty)
+    assert rc == -1 and "no agents" in msg
+    a, b = small_snapshot(300, 80, seed=1), small_snapshot(200, 60, seed=2)
+    batch = snp.concat([a, b], [1, 2], [3e-4, 3e-4])
+    batch.agents["location"][5] = batch.reps["loc_offset"][1] + 3  # an agent of replica 0 placed in replica 1
+    rc, msg = _create(batch)
+    assert rc == -4 and "outside its replica" in msg

@@ -176,3 +176,31 @@ def test_profiled_graph_same_results_and_kernel_times(gpu_lib):
     assert stats_rows(o.run_day(2)) == stats_rows(g.run_day(2))
     g.download()
     assert diff_state(s_cpu, s_gpu) == []
+
+
+@pytest.mark.parametrize("n,locs,frac", [(1, 4, 1.0), (3, 5, 0.0), (257, 64, 0.5), (5000, 1200, 0.0)])
+def test_tiny_ragged_and_uninfected_populations(gpu_lib, n, locs, frac):
+    """A single agent, a few agents, sizes off the warp/block multiples, and
+    days with no infectious agent at all (empty hazard masks)."""
+    s_cpu, s_gpu, o, g = _pair(n=n, locs=locs, initial_infected_frac=frac)
+    for d in range(2):
+        assert stats_rows(o.run_day(d)) == stats_rows(g.run_day(d)), d
+    g.download()
+    assert diff_state(s_cpu, s_gpu) == []
+    off_o, ag_o = o.csr()
+    off_g, ag_g = g.csr(canonical=True)
+    assert np.array_equal(off_o, off_g) and np.array_equal(ag_o, ag_g)
+
+
+def test_uneven_tiny_replicas_match_single_runs(gpu_lib):
+    from pansim_gb300 import snapshot as snp
+    from tests.helpers import small_snapshot
+    parts = [small_snapshot(n=n, locs=max(4, n // 4), seed=10 + i, initial_infected_frac=0.2)
+             for i, n in enumerate([1, 33, 700])]
+    batch = snp.concat([p.copy() for p in parts], [10, 11, 12], [3.74e-4] * 3)
+    gb = GpuSim(batch)
+    singles = [GpuSim(p.copy()) for p in parts]
+    for d in range(2):
+        rows_b = stats_rows(gb.run_day(d))
+        for r, gs in enumerate(singles):
+            assert stats_rows(gs.run_day(d))[0] == rows_b[r], (d, r)
