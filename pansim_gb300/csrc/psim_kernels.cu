@@ -364,32 +364,6 @@ __device__ __forceinline__ unsigned lanemask_lt() {
     return m;
 }
 
-
-// Programmatic dependent launch: the per-step kernels are launched with
-// programmatic stream serialization, so each is staged while the previous one
-// drains; every such kernel waits for its predecessor's completion (and the
-// visibility of its writes) before touching shared data.
-__device__ __forceinline__ void wait_previous_kernel() {
-#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 900
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-#endif
-}
-
-template <typename... P, typename... A>
-static void launch_pdl(void (*kernel)(P...), unsigned grid, unsigned block, cudaStream_t s, A... args) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(block);
-    cfg.dynamicSmemBytes = 0;
-    cfg.stream = s;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, kernel, args...);
-}
-
 // Hazard of variant 0 at `loc` and whether any variant's hazard there is > 0:
 // the bit mask written by the scan is read through L1, so the hazard itself
 // is gathered only at infectious locations.
@@ -594,7 +568,6 @@ __device__ __forceinline__ void add_expected(const KArgs& k, bool act, uint32_t 
 
 // Movement of every agent + histogram + fixed-point infectiousness sums.
 __global__ void __launch_bounds__(256) k_movement(KArgs k, uint32_t step) {
-    wait_previous_kernel();
     const uint32_t N = k.a.n;
     const StepClock c = step_clock(k, step);
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -657,7 +630,6 @@ __device__ __forceinline__ uint32_t block_sum_256(uint32_t v, uint32_t* s_red) {
 
 template <int ITEMS>
 __global__ void __launch_bounds__(SCAN_THREADS) k_tile_sums(KArgs k) {
-    wait_previous_kernel();
     constexpr int TILE = SCAN_THREADS * ITEMS;
     __shared__ uint32_t s_red[SCAN_THREADS / 32];
     const uint32_t L = k.l.n;
@@ -674,7 +646,6 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_tile_sums(KArgs k) {
 
 template <int ITEMS>
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, int with_hazard, int merge_q) {
-    wait_previous_kernel();
     constexpr int TILE = SCAN_THREADS * ITEMS;
     __shared__ uint32_t s_red[SCAN_THREADS / 32];
     __shared__ uint32_t s_warp[SCAN_THREADS / 32];
@@ -784,7 +755,6 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, int with_hazard,
 
 // CSR scatter and/or infection draw of one step.
 __global__ void __launch_bounds__(256) k_scatter_draw(KArgs k, uint32_t step, int scatter, int draw) {
-    wait_previous_kernel();
     __shared__ double s_grad[GRAD_N];
     grad_begin(k, s_grad);
     const uint32_t N = k.a.n, L = k.l.n;
@@ -814,7 +784,6 @@ __global__ void __launch_bounds__(256) k_scatter_draw(KArgs k, uint32_t step, in
 // back to back in one pass; used inside the day graph.
 template <int MINB>
 __global__ void __launch_bounds__(256, MINB) k_step_fused(KArgs k, uint32_t step) {
-    wait_previous_kernel();
     __shared__ double s_grad[GRAD_N];
     grad_begin(k, s_grad);
     const uint32_t N = k.a.n, L = k.l.n;
@@ -861,7 +830,6 @@ __global__ void __launch_bounds__(256, MINB) k_step_fused(KArgs k, uint32_t step
 // the memory-level parallelism at the same occupancy.
 template <int U>
 __global__ void __launch_bounds__(256) k_step_ilp(KArgs k, uint32_t step) {
-    wait_previous_kernel();
     __shared__ double s_grad[GRAD_N];
     grad_begin(k, s_grad);
     const uint32_t N = k.a.n, L = k.l.n;
@@ -923,7 +891,6 @@ __global__ void __launch_bounds__(256) k_step_ilp(KArgs k, uint32_t step) {
 // histogram with the full register budget.  Per agent the operations and
 // their order are those of k_step_fused.
 __global__ void __launch_bounds__(256, 8) k_step_hot(KArgs k, uint32_t step) {
-    wait_previous_kernel();
     const uint32_t N = k.a.n, L = k.l.n;
     const uint32_t dt = k.p.time_step;
     const uint32_t minutes = (step + 1) * dt;
@@ -959,7 +926,6 @@ __global__ void __launch_bounds__(256, 8) k_step_hot(KArgs k, uint32_t step) {
 }
 
 __global__ void __launch_bounds__(256) k_step_cold(KArgs k, uint32_t step) {
-    wait_previous_kernel();
     __shared__ double s_grad[GRAD_N];
     grad_begin(k, s_grad);
     const uint32_t L = k.l.n;
@@ -1611,7 +1577,7 @@ static unsigned agent_grid(const KArgs& k, unsigned wave) {
 void launch_movement(const KArgs& k, uint32_t step, cudaStream_t s) {
     static unsigned g = 0;
     if (!g) g = wave_grid(k_movement, 1u << 30);
-    launch_pdl(k_movement, agent_grid(k, g), 256, s, k, step);
+    k_movement<<<agent_grid(k, g), 256, 0, s>>>(k, step);
 }
 // register-capped instantiations of the fused step kernel: a tighter cap
 // raises occupancy for the hot path and spills on the rare cold path; the
@@ -1629,8 +1595,8 @@ void launch_step_fused(const KArgs& k, uint32_t step, cudaStream_t s) {
         g[6] = wave_grid(k_step_ilp<4>, 1u << 30);
     }
     if (v == 3) {
-        launch_pdl(k_step_hot, agent_grid(k, g[3]), 256, s, k, step);
-        launch_pdl(k_step_cold, g[4], 256, s, k, step);
+        k_step_hot<<<agent_grid(k, g[3]), 256, 0, s>>>(k, step);
+        k_step_cold<<<g[4], 256, 0, s>>>(k, step);
         return;
     }
     if (v == 4 || v == 5) {
@@ -1638,18 +1604,18 @@ void launch_step_fused(const KArgs& k, uint32_t step, cudaStream_t s) {
         unsigned grid = k.tune.blocks_per_sm ? (unsigned)(sm_count() * k.tune.blocks_per_sm) : g[v == 4 ? 5 : 6];
         grid = std::min(grid, grid_for((k.a.n + U - 1) / U, 1 << 20));
         if (v == 4)
-            launch_pdl(k_step_ilp<2>, grid, 256, s, k, step);
+            k_step_ilp<2><<<grid, 256, 0, s>>>(k, step);
         else
-            launch_pdl(k_step_ilp<4>, grid, 256, s, k, step);
+            k_step_ilp<4><<<grid, 256, 0, s>>>(k, step);
         return;
     }
     const unsigned grid = agent_grid(k, g[v]);
     if (v == 0)
-        launch_pdl(k_step_fused<4>, grid, 256, s, k, step);
+        k_step_fused<4><<<grid, 256, 0, s>>>(k, step);
     else if (v == 1)
-        launch_pdl(k_step_fused<6>, grid, 256, s, k, step);
+        k_step_fused<6><<<grid, 256, 0, s>>>(k, step);
     else
-        launch_pdl(k_step_fused<8>, grid, 256, s, k, step);
+        k_step_fused<8><<<grid, 256, 0, s>>>(k, step);
 }
 int step_fused_kernels(const KArgs& k) { return k.tune.variant == 3 ? 2 : 1; }
 void launch_count(const KArgs& k, cudaStream_t s) { k_count<<<grid_for(k.a.n, 8), 256, 0, s>>>(k); }
@@ -1659,20 +1625,20 @@ void launch_scan(const KArgs& k, uint32_t, int with_hazard, int merge_q, cudaStr
     unsigned tiles = (k.l.n + SCAN_THREADS * items - 1) / (SCAN_THREADS * items);
     if (!tiles) tiles = 1;
     if (items == 2) {
-        launch_pdl(k_tile_sums<2>, tiles, SCAN_THREADS, s, k);
-        launch_pdl(k_scan<2>, tiles, SCAN_THREADS, s, k, with_hazard, merge_q);
+        k_tile_sums<2><<<tiles, SCAN_THREADS, 0, s>>>(k);
+        k_scan<2><<<tiles, SCAN_THREADS, 0, s>>>(k, with_hazard, merge_q);
     } else if (items == 4) {
-        launch_pdl(k_tile_sums<4>, tiles, SCAN_THREADS, s, k);
-        launch_pdl(k_scan<4>, tiles, SCAN_THREADS, s, k, with_hazard, merge_q);
+        k_tile_sums<4><<<tiles, SCAN_THREADS, 0, s>>>(k);
+        k_scan<4><<<tiles, SCAN_THREADS, 0, s>>>(k, with_hazard, merge_q);
     } else {
-        launch_pdl(k_tile_sums<8>, tiles, SCAN_THREADS, s, k);
-        launch_pdl(k_scan<8>, tiles, SCAN_THREADS, s, k, with_hazard, merge_q);
+        k_tile_sums<8><<<tiles, SCAN_THREADS, 0, s>>>(k);
+        k_scan<8><<<tiles, SCAN_THREADS, 0, s>>>(k, with_hazard, merge_q);
     }
 }
 void launch_scatter_draw(const KArgs& k, uint32_t step, int scatter, int draw, cudaStream_t s) {
     static unsigned g = 0;
     if (!g) g = wave_grid(k_scatter_draw, 1u << 30);
-    launch_pdl(k_scatter_draw, agent_grid(k, g), 256, s, k, step, scatter, draw);
+    k_scatter_draw<<<agent_grid(k, g), 256, 0, s>>>(k, step, scatter, draw);
 }
 void launch_offsets(const KArgs& k, cudaStream_t s) {
     k_offsets_from_cursor<<<grid_for(k.l.n + 1, 8), 256, 0, s>>>(k, k.l.csr_off);
