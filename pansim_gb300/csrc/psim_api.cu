@@ -445,7 +445,8 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     AL(st_quarantined_ts, N) AL(st_quarantined_until, N) AL(st_days_in_quarantine, N) AL(st_hospitalized_ts, N)
     AL(st_hospitalized_until, N) AL(st_immunization_ts, N) AL(st_recovered_ts, N) AL(st_variant_mask, N)
     AL(st_immunization_count, N) AL(st_infected_count, N) AL(st_worst_state, N) AL(hcw, N) AL(rank, N)
-    AL(worklist, N) AL(work_count, 1) AL(imm_round, N) AL(scaling_v, (size_t)N * V)
+    AL(worklist, (size_t)N + (size_t)WORK_MAX_BLOCKS * 256) AL(seg_count, WORK_MAX_BLOCKS)
+    AL(imm_round, N) AL(scaling_v, (size_t)N * V)
 #undef AL
     // locations
     DevLocs& dl = k.l;

@@ -91,8 +91,9 @@ struct DevAgents {
     float* scaling_v;             // [V*N] symptom scaling of the states up to 6, per variant
     uint8_t* hcw;                 // healthcare worker flag
     uint32_t* rank;               // scratch of the canonical CSR ordering
-    uint32_t* worklist;           // agents queued for the cold half of a step (hot/cold variant)
-    uint32_t* work_count;         // their number
+    uint32_t* worklist;           // agents queued for the cold half of a step (hot/cold variant),
+                                  // one segment per hot block
+    uint32_t* seg_count;          // queued agents per segment
 };
 
 struct DevLocs {
@@ -205,6 +206,9 @@ void launch_scatter_draw(const KArgs& k, uint32_t step_in_day, int scatter, int 
 void launch_offsets(const KArgs& k, cudaStream_t s);
 void launch_step_fused(const KArgs& k, uint32_t step_in_day, cudaStream_t s);
 // closure rules
+// work-list segments of the hot/cold step (blocks of the hot kernel at most)
+constexpr uint32_t WORK_MAX_BLOCKS = 152u * 64u;
+
 struct ClosureTypes {
     uint32_t n;
     uint32_t v[10];

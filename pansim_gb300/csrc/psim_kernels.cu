@@ -653,7 +653,6 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, int with_hazard,
     const uint32_t tile = blockIdx.x;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t wbase = tile * TILE + (uint32_t)warp * (32 * ITEMS);
-    if (tile == 0 && threadIdx.x == 0) *k.a.work_count = 0u;  // queue of the next step's cold agents
     uint32_t c[ITEMS], ex[ITEMS];
 #pragma unroll
     for (int q = 0; q < ITEMS; ++q) {
@@ -886,16 +885,23 @@ __global__ void __launch_bounds__(256) k_step_ilp(KArgs k, uint32_t step) {
 // Hot/cold form of k_step_fused.  The hot kernel does, for every agent, the
 // CSR slot of step `step`; agents that neither draw (no hazard at their
 // location) nor move at step + 1 (countdown > 0, no curfew transition) also
-// count down and join the histogram here.  The others are queued (warp-
-// aggregated append) for k_step_cold, which runs their draw, movement and
-// histogram with the full register budget.  Per agent the operations and
-// their order are those of k_step_fused.
-__global__ void __launch_bounds__(256, 8) k_step_hot(KArgs k, uint32_t step) {
+// count down here.  The others -- a few percent per step, each with a long
+// chain of dependent loads in the movement decision -- are queued in the
+// block's own segment of the work list (shared-memory counter, no global
+// contention), and k_step_cold runs them densely, a block per segment, with
+// the full register budget.  Per agent the operations and their order are
+// those of k_step_fused.
+__global__ void __launch_bounds__(256, 8) k_step_hot(KArgs k, uint32_t step, uint32_t cap) {
+    __shared__ uint32_t s_cnt;
+    if (threadIdx.x == 0) s_cnt = 0u;
+    __syncthreads();
     const uint32_t N = k.a.n, L = k.l.n;
     const uint32_t dt = k.p.time_step;
     const uint32_t minutes = (step + 1) * dt;
     const bool curfew_now = k.p.enable_curfew && k.p.curfew_begin == minutes / dt;
     const uint32_t stride = gridDim.x * blockDim.x;
+    uint32_t* seg = k.a.worklist + (size_t)blockIdx.x * cap;
+    const int lane = threadIdx.x & 31;
     for (uint32_t base = blockIdx.x * blockDim.x; base < N; base += stride) {
         const uint32_t i = base + threadIdx.x;
         const bool act = i < N;
@@ -910,34 +916,34 @@ __global__ void __launch_bounds__(256, 8) k_step_hot(KArgs k, uint32_t step) {
         const bool cold = act && (curfew_now || s == 0 || hz || !ok);
         const bool hot = act && !cold;
         if (hot) k.a.steps_until_move[i] = s - 1;
-        // queue the cold agents
         const unsigned cm = __ballot_sync(0xffffffffu, cold);
         if (cm) {
-            const int lane = threadIdx.x & 31;
             uint32_t basew = 0;
-            if (lane == __ffs(cm) - 1) basew = atomicAdd(k.a.work_count, (uint32_t)__popc(cm));
+            if (lane == __ffs(cm) - 1) basew = atomicAdd(&s_cnt, (uint32_t)__popc(cm));
             basew = __shfl_sync(0xffffffffu, basew, __ffs(cm) - 1);
-            if (cold) k.a.worklist[basew + __popc(cm & lanemask_lt())] = i;
+            if (cold) seg[basew + __popc(cm & lanemask_lt())] = i;
         }
         uint32_t var = 0;
         if (hot && inf > 0.0f) var = k.a.variant[i];
         count_agent(k, hot, loc0, loc0, inf, var);
     }
+    __syncthreads();
+    if (threadIdx.x == 0) k.a.seg_count[blockIdx.x] = s_cnt;
 }
 
-__global__ void __launch_bounds__(256) k_step_cold(KArgs k, uint32_t step) {
+__global__ void __launch_bounds__(256) k_step_cold(KArgs k, uint32_t step, uint32_t cap) {
     __shared__ double s_grad[GRAD_N];
     grad_begin(k, s_grad);
     const uint32_t L = k.l.n;
     const uint32_t t = k.clock->t0 + step;
     const StepClock c = step_clock(k, step + 1);
-    const uint32_t n = *((volatile uint32_t*)k.a.work_count);
-    const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t trips = (n + stride - 1) / stride;  // uniform per block (grid-wide bound)
+    const uint32_t n = k.a.seg_count[blockIdx.x];
+    const uint32_t* seg = k.a.worklist + (size_t)blockIdx.x * cap;
+    const uint32_t trips = (n + blockDim.x - 1) / blockDim.x;  // uniform per block
     for (uint32_t it = 0; it < trips; ++it) {
-        const uint32_t j = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        const uint32_t j = it * blockDim.x + threadIdx.x;
         const bool act = j < n;
-        const uint32_t i = act ? k.a.worklist[j] : 0u;
+        const uint32_t i = act ? seg[j] : 0u;
         double term = 0.0;
         uint32_t loc = NONE, loc0 = NONE, var = 0;
         float inf = 0.0f;
@@ -1595,8 +1601,11 @@ void launch_step_fused(const KArgs& k, uint32_t step, cudaStream_t s) {
         g[6] = wave_grid(k_step_ilp<4>, 1u << 30);
     }
     if (v == 3) {
-        k_step_hot<<<agent_grid(k, g[3]), 256, 0, s>>>(k, step);
-        k_step_cold<<<g[4], 256, 0, s>>>(k, step);
+        // one work-list segment per hot block, as many as the block visits
+        const unsigned grid = std::min(agent_grid(k, g[3]), (unsigned)WORK_MAX_BLOCKS);
+        const uint32_t cap = (uint32_t)((((size_t)k.a.n + (size_t)grid * 256 - 1) / ((size_t)grid * 256)) * 256);
+        k_step_hot<<<grid, 256, 0, s>>>(k, step, cap);
+        k_step_cold<<<grid, 256, 0, s>>>(k, step, cap);
         return;
     }
     if (v == 4 || v == 5) {
