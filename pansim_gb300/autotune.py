@@ -1,7 +1,8 @@
 """Autotuner of the per-step kernels.
 
 Times each candidate tuning (fused-kernel variant, warp aggregation of the
-CSR slot atomics, blocks per SM of the per-agent kernels, scan tile size) on the live workload: every candidate runs the same whole day (the
+CSR slot atomics, blocks per SM of the per-agent kernels, scan tile size and
+single-pass or two-pass scan) on the live workload: every candidate runs the same whole day (the
 day graph, all its steps) from the same checkpoint taken after that day's
 midnight phases, timed with CUDA events, and the fastest is kept.  Steps at
 different times of day differ several-fold in cost (movers, infectious
@@ -14,7 +15,7 @@ import itertools
 import numpy as np
 
 DEFAULT_GRID = [0, 4, 8, 16]
-DEFAULT_VARIANTS = [0, 1, 3, 5]
+DEFAULT_VARIANTS = [0, 3]
 LARGE_AGENTS = 8_000_000
 
 
@@ -22,9 +23,10 @@ def candidates(grid=None, variants=None):
     """variant: register cap of the fused kernel (64 / 40 / 32 registers),
     3 = hot/cold split, 4 / 5 = 2 / 4 agents per thread in flight;
     blocks_per_sm 0 = one occupancy wave of that variant."""
-    for variant, agg_slot, bps, items in itertools.product(variants or DEFAULT_VARIANTS, [1, 0], grid or DEFAULT_GRID,
-                                                           [8, 4, 2]):
-        yield dict(agg_count=0, agg_slot=agg_slot, blocks_per_sm=bps, variant=variant, scan_items=items)
+    for variant, agg_slot, bps, items, mode in itertools.product(variants or DEFAULT_VARIANTS, [1, 0],
+                                                                 grid or DEFAULT_GRID, [8, 4, 2], [0, 1]):
+        yield dict(agg_count=0, agg_slot=agg_slot, blocks_per_sm=bps, variant=variant, scan_items=items,
+                   scan_mode=mode)
 
 
 TUNE_SLOT = 1 << 16

@@ -82,7 +82,7 @@ class PsimDayStats(C.Structure):
 
 class PsimTuning(C.Structure):
     _fields_ = [("agg_count", C.c_uint32), ("agg_slot", C.c_uint32), ("blocks_per_sm", C.c_uint32),
-                ("variant", C.c_uint32), ("scan_items", C.c_uint32)]
+                ("variant", C.c_uint32), ("scan_items", C.c_uint32), ("scan_mode", C.c_uint32)]
 
 
 PSIM_IMM_CATEGORIES = 10

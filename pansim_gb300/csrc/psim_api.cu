@@ -60,6 +60,7 @@ int check_device_err(psim_ctx* c) {
         std::string m = "device error flags 0x" + std::to_string(e) + ":";
         if (e & ERR_LOCATION) m += " agent on an invalid location;";
         if (e & ERR_TEST_WAIT) m += " bounded wait expired;";
+        if (e & ERR_SCAN_WAIT) m += " scan tile wait expired;";
         return fail(c, PSIM_ERR_DEVICE, m);
     }
     return 0;
@@ -194,7 +195,7 @@ int initial_regroup(psim_ctx* c) {
     launch_scan(c->k, 0, 1, 0, c->stream);
     launch_scatter_draw(c->k, 0, 1, 0, c->stream);
     launch_stats(c->k, 0, c->stream);
-    c->launches += 7;
+    c->launches += 4 + (uint64_t)scan_kernels(c->k);
     int rc = launch_check(c);
     if (rc) return rc;
     c->csr_fresh = true;
@@ -206,7 +207,7 @@ int do_step(psim_ctx* c, uint32_t step, bool draw, bool movement) {
     if (movement) launch_movement(c->k, step, c->stream);
     launch_scan(c->k, step, 1, merge_q, c->stream);
     launch_scatter_draw(c->k, step, 1, draw ? 1 : 0, c->stream);
-    c->launches += movement ? 4 : 3;
+    c->launches += (movement ? 2 : 1) + (uint64_t)scan_kernels(c->k);
     return launch_check(c);
 }
 
@@ -247,7 +248,7 @@ int capture_day_graph(psim_ctx* c) {
     e = cudaGraphInstantiate(&c->day_graph, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(c, PSIM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
-    c->graph_kernels = (2ull + (uint64_t)step_fused_kernels(c->k)) * c->spd + 1;
+    c->graph_kernels = ((uint64_t)scan_kernels(c->k) + (uint64_t)step_fused_kernels(c->k)) * c->spd + 1;
     c->graph_dirty = false;
     c->prof_valid = false;
     return 0;
@@ -477,6 +478,8 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     if ((rc = dalloc(c, &dl.flags, L))) return bail(rc);
     const size_t tiles = (L + 511) / 512 + 1;
     if ((rc = dalloc(c, &dl.tile_sums, tiles))) return bail(rc);
+    if ((rc = dalloc(c, &dl.scan_status, tiles))) return bail(rc);
+    if ((rc = dalloc(c, &dl.scan_state, 2))) return bail(rc);
     // replicas
     DevReps& dr = k.r;
     dr.n = c->R;
@@ -527,6 +530,7 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     k.track_expected = 0;
     k.tune.agg_count = 1;
     k.tune.scan_items = 8;
+    k.tune.scan_mode = 0;
     k.tune.agg_slot = 1;
     k.tune.blocks_per_sm = 0;
     k.tune.variant = 0;
@@ -650,6 +654,8 @@ int psim_set_tuning(psim_ctx* c, const psim_tuning* t) {
     if (t->scan_items != 0 && t->scan_items != 2 && t->scan_items != 4 && t->scan_items != 8)
         return fail(c, PSIM_ERR_ARG, "scan_items must be 2, 4 or 8");
     c->k.tune.scan_items = t->scan_items ? t->scan_items : 8u;
+    if (t->scan_mode > 1) return fail(c, PSIM_ERR_ARG, "scan_mode must be 0 or 1");
+    c->k.tune.scan_mode = t->scan_mode;
     c->graph_dirty = true;
     return 0;
 }
@@ -661,6 +667,7 @@ int psim_get_tuning(psim_ctx* c, psim_tuning* t) {
     t->blocks_per_sm = c->k.tune.blocks_per_sm;
     t->variant = c->k.tune.variant;
     t->scan_items = c->k.tune.scan_items;
+    t->scan_mode = c->k.tune.scan_mode;
     return 0;
 }
 
@@ -800,7 +807,7 @@ int psim_regroup(psim_ctx* c) {
     }
     launch_scan(c->k, 0, 1, c->params.quarantine_policy > 1, c->stream);
     launch_scatter_draw(c->k, 0, 1, 0, c->stream);
-    c->launches += 3;
+    c->launches += 1 + (uint64_t)scan_kernels(c->k);
     c->csr_fresh = false;
     int rc = launch_check(c);
     if (rc) return rc;
@@ -1028,7 +1035,7 @@ int psim_time_step_kernels(psim_ctx* c, uint32_t t, float* ms) {
     CK(cudaEventRecord(ev[3], c->stream));
     launch_scan(c->k, step + 1, 1, merge_q, c->stream);
     launch_scatter_draw(c->k, step + 1, 1, 1, c->stream);
-    c->launches += 6 + (uint64_t)step_fused_kernels(c->k);
+    c->launches += 2 + 2 * (uint64_t)scan_kernels(c->k) + (uint64_t)step_fused_kernels(c->k);
     CK(cudaStreamSynchronize(c->stream));
     for (int j = 0; j < 3; ++j) CK(cudaEventElapsedTime(&ms[j], ev[j], ev[j + 1]));
     for (int j = 0; j < 4; ++j) cudaEventDestroy(ev[j]);

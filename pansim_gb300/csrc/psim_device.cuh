@@ -13,9 +13,9 @@ constexpr uint32_t NONE = 0xFFFFFFFFu;
 constexpr int WB_W = 0, WB_N = 1, WB_M = 2, WB_S = 3, WB_D = 4;
 
 // error bits written by kernels into DevCtx::err
-constexpr uint32_t ERR_SCAN_WAIT = 1u;     // (unused: the scan has no inter-block waits)
 constexpr uint32_t ERR_LOCATION = 2u;      // an agent ended on an invalid location
 constexpr uint32_t ERR_TEST_WAIT = 4u;     // bounded-wait self test expired (expected in tests)
+constexpr uint32_t ERR_SCAN_WAIT = 1u;     // a scan tile gave up waiting for its predecessors
 
 struct DevModel {
     uint32_t n_states, n_variants, n_prog, n_agent_types;
@@ -121,7 +121,9 @@ struct DevLocs {
     float* hazard_x;              // [V][n] its argument x = k*S/n*w*season*dt (adjoint mode)
     uint32_t* no_work_loc;
     uint8_t* flags;               // testing flags
-    uint32_t* tile_sums;          // per-tile sums of the histogram (scan, first pass)
+    uint32_t* tile_sums;          // per-tile sums of the histogram (two-pass scan)
+    uint64_t* scan_status;        // per-tile status words of the single-pass scan (epoch | flag | value)
+    uint32_t* scan_state;         // [0] epoch of the next single-pass scan, [1] its tile ticket
 };
 
 struct DevReps {
@@ -158,6 +160,7 @@ struct DevTune {
                              // 3 = hot/cold split (lean kernel + queued cold agents),
                              // 4/5 = 2/4 agents per thread in flight
     uint32_t scan_items;     // locations per scan thread: 2, 4 or 8 (tile = 256 x items)
+    uint32_t scan_mode;      // 0 = single pass with decoupled look-back, 1 = tile sums + scan
 };
 
 // Adjoint accumulation (gradient of the expected new infections with respect
@@ -205,6 +208,7 @@ void launch_scan(const KArgs& k, uint32_t step_in_day, int with_hazard, int merg
 void launch_scatter_draw(const KArgs& k, uint32_t step_in_day, int scatter, int draw, cudaStream_t s);
 void launch_offsets(const KArgs& k, cudaStream_t s);
 void launch_step_fused(const KArgs& k, uint32_t step_in_day, cudaStream_t s);
+int scan_kernels(const KArgs& k);
 // closure rules
 // work-list segments of the hot/cold step (blocks of the hot kernel at most)
 constexpr uint32_t WORK_MAX_BLOCKS = 152u * 64u;

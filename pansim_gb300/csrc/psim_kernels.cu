@@ -644,14 +644,39 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_tile_sums(KArgs k) {
     if (threadIdx.x == 0) k.l.tile_sums[blockIdx.x] = v;
 }
 
-template <int ITEMS>
+// Single-pass form (LOOKBACK): decoupled look-back (Merrill & Garland, "Single-
+// pass parallel prefix scan with decoupled look-back", 2016).  A tile takes a
+// ticket (so every tile it waits on has already started), publishes its
+// aggregate, and warp 0 walks back over the predecessors' status words 32 at
+// a time until it meets an inclusive prefix.  Status words carry a launch
+// epoch, so they need no reset between launches; every wait is bounded
+// (ERR_SCAN_WAIT, then the tile proceeds).
+constexpr uint32_t SCAN_SPIN_LIMIT = 1u << 22;
+
+__device__ __forceinline__ uint64_t ld_volatile_u64(const uint64_t* p) {
+    return *((const volatile uint64_t*)p);
+}
+
+template <int ITEMS, bool LOOKBACK>
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, int with_hazard, int merge_q) {
     constexpr int TILE = SCAN_THREADS * ITEMS;
     __shared__ uint32_t s_red[SCAN_THREADS / 32];
     __shared__ uint32_t s_warp[SCAN_THREADS / 32];
+    __shared__ uint32_t s_tile, s_epoch, s_prefix;
     const uint32_t L = k.l.n;
-    const uint32_t tile = blockIdx.x;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t tile = blockIdx.x, epoch = 0;
+    if (LOOKBACK) {
+        if (threadIdx.x == 0) {
+            // the epoch is read before the ticket: the last ticket advances it
+            s_epoch = *((volatile uint32_t*)&k.l.scan_state[0]);
+            __threadfence();
+            s_tile = atomicAdd(&k.l.scan_state[1], 1u);
+        }
+        __syncthreads();
+        tile = s_tile;
+        epoch = s_epoch & 0x3FFFFFFFu;
+    }
     const uint32_t wbase = tile * TILE + (uint32_t)warp * (32 * ITEMS);
     uint32_t c[ITEMS], ex[ITEMS];
 #pragma unroll
@@ -659,6 +684,62 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, int with_hazard,
         const uint32_t l = wbase + q * 32 + lane;
         c[q] = l < L ? k.l.counts[l] : 0u;
     }
+    uint32_t prefix = 0;
+    if (LOOKBACK) {
+        uint32_t mine = 0;
+#pragma unroll
+        for (int q = 0; q < ITEMS; ++q) mine += c[q];
+        const uint32_t agg = block_sum_256(mine, s_red);
+        uint64_t* st = k.l.scan_status;
+        const uint64_t ep = (uint64_t)epoch << 34;
+        if (threadIdx.x == 0)
+            *((volatile uint64_t*)&st[tile]) = ep | ((uint64_t)(tile == 0 ? 2u : 1u) << 32) | agg;
+        if (warp == 0) {
+            uint32_t acc = 0;
+            if (tile > 0) {
+                int32_t look = (int32_t)tile - 1;
+                for (;;) {
+                    const int32_t idx = look - lane;
+                    uint64_t w = 0;
+                    uint32_t fl = 2u;  // before tile 0: an empty prefix
+                    for (uint32_t spin = 0;; ++spin) {
+                        if (idx >= 0) {
+                            w = ld_volatile_u64(&st[idx]);
+                            fl = (uint32_t)(w >> 34) == epoch ? (uint32_t)(w >> 32) & 3u : 0u;
+                        }
+                        if (__all_sync(0xffffffffu, fl != 0u)) break;
+                        if (spin >= SCAN_SPIN_LIMIT) {
+                            if (lane == 0) atomicOr(k.err, ERR_SCAN_WAIT);
+                            if (fl == 0u) {
+                                fl = 2u;
+                                w = 0;
+                            }
+                            break;
+                        }
+                    }
+                    const unsigned pm = __ballot_sync(0xffffffffu, fl == 2u);
+                    const int first_p = pm ? __ffs(pm) - 1 : 31;
+                    uint32_t v = lane <= first_p ? (uint32_t)w : 0u;
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                    acc += v;
+                    if (pm) break;
+                    look -= 32;
+                }
+                if (lane == 0) *((volatile uint64_t*)&st[tile]) = ep | (2ull << 32) | (uint64_t)(acc + agg);
+            }
+            if (lane == 0) s_prefix = acc;
+        }
+        __syncthreads();
+        prefix = s_prefix;
+        // the last ticket: every tile has its ticket, so reset the ticket
+        // counter and advance the epoch for the next launch
+        if (threadIdx.x == 0 && tile == gridDim.x - 1) {
+            k.l.scan_state[1] = 0u;
+            __threadfence();
+            k.l.scan_state[0] = s_epoch + 1u;
+        }
+    } else {
     // sum of the tiles before this one
     uint32_t pre = 0;
     {
@@ -673,7 +754,8 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, int with_hazard,
         for (; j < tile; j += SCAN_THREADS) p0 += k.l.tile_sums[j];
         pre = p0 + p1 + p2 + p3;
     }
-    const uint32_t prefix = block_sum_256(pre, s_red);
+    prefix = block_sum_256(pre, s_red);
+    }
     uint32_t carry = 0;
 #pragma unroll
     for (int q = 0; q < ITEMS; ++q) {
@@ -1628,22 +1710,29 @@ void launch_step_fused(const KArgs& k, uint32_t step, cudaStream_t s) {
 }
 int step_fused_kernels(const KArgs& k) { return k.tune.variant == 3 ? 2 : 1; }
 void launch_count(const KArgs& k, cudaStream_t s) { k_count<<<grid_for(k.a.n, 8), 256, 0, s>>>(k); }
-// tile sums, then the scan, with 256 x tune.scan_items locations per tile
-void launch_scan(const KArgs& k, uint32_t, int with_hazard, int merge_q, cudaStream_t s) {
-    const uint32_t items = k.tune.scan_items == 2 || k.tune.scan_items == 4 ? k.tune.scan_items : 8u;
-    unsigned tiles = (k.l.n + SCAN_THREADS * items - 1) / (SCAN_THREADS * items);
+// the scan of the histogram with 256 x tune.scan_items locations per tile:
+// single pass with decoupled look-back (tune.scan_mode 0) or tile sums, then
+// the scan (scan_mode 1)
+template <int ITEMS>
+static void launch_scan_items(const KArgs& k, int with_hazard, int merge_q, cudaStream_t s) {
+    unsigned tiles = (k.l.n + SCAN_THREADS * ITEMS - 1) / (SCAN_THREADS * ITEMS);
     if (!tiles) tiles = 1;
-    if (items == 2) {
-        k_tile_sums<2><<<tiles, SCAN_THREADS, 0, s>>>(k);
-        k_scan<2><<<tiles, SCAN_THREADS, 0, s>>>(k, with_hazard, merge_q);
-    } else if (items == 4) {
-        k_tile_sums<4><<<tiles, SCAN_THREADS, 0, s>>>(k);
-        k_scan<4><<<tiles, SCAN_THREADS, 0, s>>>(k, with_hazard, merge_q);
+    if (k.tune.scan_mode == 0) {
+        k_scan<ITEMS, true><<<tiles, SCAN_THREADS, 0, s>>>(k, with_hazard, merge_q);
     } else {
-        k_tile_sums<8><<<tiles, SCAN_THREADS, 0, s>>>(k);
-        k_scan<8><<<tiles, SCAN_THREADS, 0, s>>>(k, with_hazard, merge_q);
+        k_tile_sums<ITEMS><<<tiles, SCAN_THREADS, 0, s>>>(k);
+        k_scan<ITEMS, false><<<tiles, SCAN_THREADS, 0, s>>>(k, with_hazard, merge_q);
     }
 }
+void launch_scan(const KArgs& k, uint32_t, int with_hazard, int merge_q, cudaStream_t s) {
+    if (k.tune.scan_items == 2)
+        launch_scan_items<2>(k, with_hazard, merge_q, s);
+    else if (k.tune.scan_items == 4)
+        launch_scan_items<4>(k, with_hazard, merge_q, s);
+    else
+        launch_scan_items<8>(k, with_hazard, merge_q, s);
+}
+int scan_kernels(const KArgs& k) { return k.tune.scan_mode == 0 ? 1 : 2; }
 void launch_scatter_draw(const KArgs& k, uint32_t step, int scatter, int draw, cudaStream_t s) {
     static unsigned g = 0;
     if (!g) g = wave_grid(k_scatter_draw, 1u << 30);

@@ -282,15 +282,15 @@ class GpuSim:
         self._ck(lib().psim_time_step_kernels(self.h, t, _p(ms)), "time_step_kernels")
         return ms
 
-    def set_tuning(self, agg_count=1, agg_slot=1, blocks_per_sm=0, variant=0, scan_items=8):
-        t = cabi.PsimTuning(agg_count, agg_slot, blocks_per_sm, variant, scan_items)
+    def set_tuning(self, agg_count=1, agg_slot=1, blocks_per_sm=0, variant=0, scan_items=8, scan_mode=0):
+        t = cabi.PsimTuning(agg_count, agg_slot, blocks_per_sm, variant, scan_items, scan_mode)
         self._ck(lib().psim_set_tuning(self.h, C.byref(t)), "set_tuning")
 
     def get_tuning(self):
         t = cabi.PsimTuning()
         self._ck(lib().psim_get_tuning(self.h, C.byref(t)), "get_tuning")
         return dict(agg_count=t.agg_count, agg_slot=t.agg_slot, blocks_per_sm=t.blocks_per_sm, variant=t.variant,
-                    scan_items=t.scan_items)
+                    scan_items=t.scan_items, scan_mode=t.scan_mode)
 
     # differentiable calibration
     def set_type_weights(self, w_by_type, slot_of_type=None):

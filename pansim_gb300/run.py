@@ -30,12 +30,15 @@ def main(argv=None):
     ap.add_argument("--agg-count", type=int, default=1)
     ap.add_argument("--agg-slot", type=int, default=1)
     ap.add_argument("--blocks-per-sm", type=int, default=0)
+    ap.add_argument("--scan-items", type=int, default=8)
+    ap.add_argument("--scan-mode", type=int, default=0)
     a = ap.parse_args(argv)
     snap = synth.make_snapshot(a.agents, a.locs, seed=a.seed, pop_seed=a.pop_seed,
                                quarantine_policy=a.quarantine_policy, testing=a.testing)
     g = native.GpuSim(snap)
     if a.variant is not None:
-        g.set_tuning(agg_count=a.agg_count, agg_slot=a.agg_slot, blocks_per_sm=a.blocks_per_sm, variant=a.variant)
+        g.set_tuning(agg_count=a.agg_count, agg_slot=a.agg_slot, blocks_per_sm=a.blocks_per_sm, variant=a.variant,
+                     scan_items=a.scan_items, scan_mode=a.scan_mode)
     t0 = time.perf_counter()
     for d in range(a.days):
         st = g.run_day(d)
