@@ -530,7 +530,7 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     k.track_expected = 0;
     k.tune.agg_count = 1;
     k.tune.scan_items = 8;
-    k.tune.scan_mode = 0;
+    k.tune.scan_mode = 1;
     k.tune.agg_slot = 1;
     k.tune.blocks_per_sm = 0;
     k.tune.variant = 0;
