@@ -364,9 +364,10 @@ __device__ __forceinline__ unsigned lanemask_lt() {
     return m;
 }
 
-// Hazard of variant 0 at `loc` and whether any variant's hazard there is > 0:
-// the bit mask written by the scan is read through L1, so the hazard itself
-// is gathered only at infectious locations.
+// Hazard of variant 0 at `loc` and whether an infectious agent is there (the
+// scan computed the location's hazards this step; elsewhere every hazard is
+// 0): the bit mask written by the scan is read through L1, so the hazard
+// itself is gathered only at infectious locations.
 __device__ __forceinline__ float hazard_at(const KArgs& k, uint32_t loc, bool* any) {
     const uint32_t w = __ldg(&k.l.hmask[loc >> 5]);
     *any = ((w >> (loc & 31u)) & 1u) != 0;
@@ -417,8 +418,6 @@ __device__ __forceinline__ void move_agent(const KArgs& k, uint32_t i, const Ste
 // Scan tiles: 256 threads x ITEMS locations (ITEMS = 2, 4 or 8, a tuning
 // choice); the masks hold one 32-bit word per warp and item.
 constexpr int SCAN_THREADS = 256;
-constexpr int SCAN_ITEMS_MAX = 8;
-constexpr int SCAN_TILE_MAX = SCAN_THREADS * SCAN_ITEMS_MAX;
 
 // The per-location agent counts are kept up to date incrementally: an agent
 // whose location changed from loc0 to loc moves one count (two fire-and-
@@ -785,7 +784,6 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, int with_hazard,
         // only locations that received infectiousness this step (sum mask)
         // are read; elsewhere the hazard is 0 and stays unwritten, the hazard
         // mask keeping readers away from it
-        uint32_t any = 0;  // bit q: some variant's hazard of this lane's location q is > 0
         uint32_t sws[ITEMS];
 #pragma unroll
         for (int q = 0; q < ITEMS; ++q) sws[q] = k.l.smask[(wbase + q * 32) >> 5];
@@ -808,15 +806,15 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, int with_hazard,
                     k.l.sfix[idx] = 0ull;
                 }
                 k.l.hazard[idx] = h;
-                if (h > 0.0f) any |= 1u << q;
                 if (k.adj.on) k.l.hazard_x[idx] = x;
             }
         }
-        // one mask word per 32 locations (wbase is a multiple of 32)
+        // the hazard mask of this step: the locations with an infectious
+        // agent, whose hazards were just computed (one word per 32
+        // locations; wbase is a multiple of 32)
+        if (lane == 0) {
 #pragma unroll
-        for (int q = 0; q < ITEMS; ++q) {
-            const unsigned word = __ballot_sync(0xffffffffu, (any >> q) & 1u);
-            if (lane == 0) k.l.hmask[(wbase + q * 32) >> 5] = word;
+            for (int q = 0; q < ITEMS; ++q) k.l.hmask[(wbase + q * 32) >> 5] = sws[q];
         }
     }
     if (merge_q) {
@@ -965,9 +963,10 @@ __global__ void __launch_bounds__(256) k_step_ilp(KArgs k, uint32_t step) {
 }
 
 // Hot/cold form of k_step_fused.  The hot kernel does, for every agent, the
-// CSR slot of step `step`; agents that neither draw (no hazard at their
-// location) nor move at step + 1 (countdown > 0, no curfew transition) also
-// count down here.  The others -- a few percent per step, each with a long
+// CSR slot of step `step`; agents that neither draw (no infectious agent at
+// their location, so they are not infectious themselves) nor move at step + 1
+// (countdown > 0, no curfew transition) also count down here and need no
+// histogram work (they stay, with nothing to add to the sums).  The others -- a few percent per step, each with a long
 // chain of dependent loads in the movement decision -- are queued in the
 // block's own segment of the work list (shared-memory counter, no global
 // contention), and k_step_cold runs them densely, a block per segment, with
@@ -984,12 +983,23 @@ __global__ void __launch_bounds__(256, 8) k_step_hot(KArgs k, uint32_t step, uin
     const uint32_t stride = gridDim.x * blockDim.x;
     uint32_t* seg = k.a.worklist + (size_t)blockIdx.x * cap;
     const int lane = threadIdx.x & 31;
-    for (uint32_t base = blockIdx.x * blockDim.x; base < N; base += stride) {
+    // the next iteration's agent columns are loaded one iteration ahead
+    uint32_t base = blockIdx.x * blockDim.x;
+    uint32_t n_loc = NONE, n_s = 0u;
+    if (base + threadIdx.x < N) {
+        n_loc = k.a.location[base + threadIdx.x];
+        n_s = k.a.steps_until_move[base + threadIdx.x];
+    }
+    for (; base < N; base += stride) {
         const uint32_t i = base + threadIdx.x;
         const bool act = i < N;
-        const uint32_t loc0 = act ? k.a.location[i] : NONE;
-        const uint32_t s = act ? k.a.steps_until_move[i] : 0u;
-        const float inf = act ? k.a.infectious[i] : 0.0f;
+        const uint32_t loc0 = n_loc;
+        const uint32_t s = n_s;
+        const uint32_t j = i + stride;
+        if (j < N) {
+            n_loc = k.a.location[j];
+            n_s = k.a.steps_until_move[j];
+        }
         const bool ok = act && loc0 < L;
         bool hz = false;
         if (ok) hazard_at(k, loc0, &hz);
@@ -1005,22 +1015,20 @@ __global__ void __launch_bounds__(256, 8) k_step_hot(KArgs k, uint32_t step, uin
             basew = __shfl_sync(0xffffffffu, basew, __ffs(cm) - 1);
             if (cold) seg[basew + __popc(cm & lanemask_lt())] = i;
         }
-        uint32_t var = 0;
-        if (hot && inf > 0.0f) var = k.a.variant[i];
-        count_agent(k, hot, loc0, loc0, inf, var);
     }
     __syncthreads();
     if (threadIdx.x == 0) k.a.seg_count[blockIdx.x] = s_cnt;
 }
 
-__global__ void __launch_bounds__(256) k_step_cold(KArgs k, uint32_t step, uint32_t cap) {
+__global__ void __launch_bounds__(256) k_step_cold(KArgs k, uint32_t step, uint32_t cap, uint32_t n_seg) {
     __shared__ double s_grad[GRAD_N];
     grad_begin(k, s_grad);
     const uint32_t L = k.l.n;
     const uint32_t t = k.clock->t0 + step;
     const StepClock c = step_clock(k, step + 1);
-    const uint32_t n = k.a.seg_count[blockIdx.x];
-    const uint32_t* seg = k.a.worklist + (size_t)blockIdx.x * cap;
+    for (uint32_t sg = blockIdx.x; sg < n_seg; sg += gridDim.x) {
+    const uint32_t n = k.a.seg_count[sg];
+    const uint32_t* seg = k.a.worklist + (size_t)sg * cap;
     const uint32_t trips = (n + blockDim.x - 1) / blockDim.x;  // uniform per block
     for (uint32_t it = 0; it < trips; ++it) {
         const uint32_t j = it * blockDim.x + threadIdx.x;
@@ -1047,6 +1055,7 @@ __global__ void __launch_bounds__(256) k_step_cold(KArgs k, uint32_t step, uint3
         }
         if (k.track_expected) add_expected(k, act, i, term);
         count_agent(k, act, loc0, loc, inf, var);
+    }
     }
     grad_end(k, s_grad);
 }
@@ -1687,7 +1696,9 @@ void launch_step_fused(const KArgs& k, uint32_t step, cudaStream_t s) {
         const unsigned grid = std::min(agent_grid(k, g[3]), (unsigned)WORK_MAX_BLOCKS);
         const uint32_t cap = (uint32_t)((((size_t)k.a.n + (size_t)grid * 256 - 1) / ((size_t)grid * 256)) * 256);
         k_step_hot<<<grid, 256, 0, s>>>(k, step, cap);
-        k_step_cold<<<grid, 256, 0, s>>>(k, step, cap);
+        // the cold agents are a few percent: at most one wave of cold blocks,
+        // each taking segments in turn
+        k_step_cold<<<std::min(grid, g[4]), 256, 0, s>>>(k, step, cap, grid);
         return;
     }
     if (v == 4 || v == 5) {
