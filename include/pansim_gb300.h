@@ -227,7 +227,8 @@ typedef struct psim_tuning {
                                 thread in flight (plain slot atomics) */
     uint32_t scan_items;     /* locations per thread of the scan: 2, 4 or 8 (0 = 8) */
     uint32_t scan_mode;      /* 0 = single pass with decoupled look-back, 1 = tile sums + scan
-                                (the default; faster on GB300 at 1.3M locations) */
+                                (the default), 2 = tile sums + scan with each thread owning
+                                consecutive locations (scan_items 4 or 8; 2 falls back to 1) */
 } psim_tuning;
 
 typedef struct psim_ctx psim_ctx;

@@ -24,7 +24,7 @@ def candidates(grid=None, variants=None):
     3 = hot/cold split, 4 / 5 = 2 / 4 agents per thread in flight;
     blocks_per_sm 0 = one occupancy wave of that variant."""
     for variant, agg_slot, bps, items, mode in itertools.product(variants or DEFAULT_VARIANTS, [1, 0],
-                                                                 grid or DEFAULT_GRID, [8, 4, 2], [0, 1]):
+                                                                 grid or DEFAULT_GRID, [8, 4, 2], [1, 2]):
         yield dict(agg_count=0, agg_slot=agg_slot, blocks_per_sm=bps, variant=variant, scan_items=items,
                    scan_mode=mode)
 

@@ -654,7 +654,7 @@ int psim_set_tuning(psim_ctx* c, const psim_tuning* t) {
     if (t->scan_items != 0 && t->scan_items != 2 && t->scan_items != 4 && t->scan_items != 8)
         return fail(c, PSIM_ERR_ARG, "scan_items must be 2, 4 or 8");
     c->k.tune.scan_items = t->scan_items ? t->scan_items : 8u;
-    if (t->scan_mode > 1) return fail(c, PSIM_ERR_ARG, "scan_mode must be 0 or 1");
+    if (t->scan_mode > 2) return fail(c, PSIM_ERR_ARG, "scan_mode must be 0, 1 or 2");
     c->k.tune.scan_mode = t->scan_mode;
     c->graph_dirty = true;
     return 0;

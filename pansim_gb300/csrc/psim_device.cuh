@@ -160,7 +160,8 @@ struct DevTune {
                              // 3 = hot/cold split (lean kernel + queued cold agents),
                              // 4/5 = 2/4 agents per thread in flight
     uint32_t scan_items;     // locations per scan thread: 2, 4 or 8 (tile = 256 x items)
-    uint32_t scan_mode;      // 0 = single pass with decoupled look-back, 1 = tile sums + scan
+    uint32_t scan_mode;      // 0 = single pass with decoupled look-back, 1 = tile sums + scan,
+                             // 2 = tile sums + scan with thread-contiguous locations (items 4, 8)
 };
 
 // Adjoint accumulation (gradient of the expected new infections with respect

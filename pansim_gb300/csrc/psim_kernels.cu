@@ -832,6 +832,148 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, int with_hazard,
     }
 }
 
+// Thread-contiguous form of the two-pass scan (scan_mode 2): every thread
+// owns 4 x Q consecutive locations, loaded and stored as 16-byte vectors; the
+// in-thread prefix is serial, so a thread total needs one 5-step warp scan
+// instead of one per item.  Same outputs as k_tile_sums + k_scan.
+template <int Q>
+__device__ __forceinline__ void load_counts4(const KArgs& k, uint32_t l0, uint32_t* c) {
+    const uint32_t L = k.l.n;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const uint32_t l = l0 + 4u * q;
+        if (l + 3u < L) {
+            const uint4 v = *reinterpret_cast<const uint4*>(k.l.counts + l);
+            c[4 * q] = v.x;
+            c[4 * q + 1] = v.y;
+            c[4 * q + 2] = v.z;
+            c[4 * q + 3] = v.w;
+        } else {
+#pragma unroll
+            for (int e = 0; e < 4; ++e) c[4 * q + e] = l + e < L ? k.l.counts[l + e] : 0u;
+        }
+    }
+}
+
+template <int Q>
+__global__ void __launch_bounds__(SCAN_THREADS) k_tile_sums_v(KArgs k) {
+    constexpr int PER = 4 * Q;
+    __shared__ uint32_t s_red[SCAN_THREADS / 32];
+    uint32_t c[PER];
+    load_counts4<Q>(k, blockIdx.x * (SCAN_THREADS * PER) + threadIdx.x * PER, c);
+    uint32_t v = 0;
+#pragma unroll
+    for (int e = 0; e < PER; ++e) v += c[e];
+    v = block_sum_256(v, s_red);
+    if (threadIdx.x == 0) k.l.tile_sums[blockIdx.x] = v;
+}
+
+template <int Q>
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_v(KArgs k, int with_hazard, int merge_q) {
+    constexpr int PER = 4 * Q;
+    __shared__ uint32_t s_red[SCAN_THREADS / 32];
+    __shared__ uint32_t s_warp[SCAN_THREADS / 32];
+    const uint32_t L = k.l.n;
+    const uint32_t tile = blockIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t l0 = tile * (SCAN_THREADS * PER) + threadIdx.x * PER;
+    uint32_t c[PER];
+    load_counts4<Q>(k, l0, c);
+    // sum of the tiles before this one
+    uint32_t pre = 0;
+    {
+        uint32_t p0 = 0, p1 = 0, p2 = 0, p3 = 0;
+        uint32_t j = threadIdx.x;
+        for (; j + 3 * SCAN_THREADS < tile; j += 4 * SCAN_THREADS) {
+            p0 += k.l.tile_sums[j];
+            p1 += k.l.tile_sums[j + SCAN_THREADS];
+            p2 += k.l.tile_sums[j + 2 * SCAN_THREADS];
+            p3 += k.l.tile_sums[j + 3 * SCAN_THREADS];
+        }
+        for (; j < tile; j += SCAN_THREADS) p0 += k.l.tile_sums[j];
+        pre = p0 + p1 + p2 + p3;
+    }
+    const uint32_t prefix = block_sum_256(pre, s_red);
+    // in-thread exclusive prefix, then the warp and block offsets
+    uint32_t ex[PER];
+    uint32_t tot = 0;
+#pragma unroll
+    for (int e = 0; e < PER; ++e) {
+        ex[e] = tot;
+        tot += c[e];
+    }
+    uint32_t x = tot;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    uint32_t woff = 0;
+    for (int q = 0; q < warp; ++q) woff += s_warp[q];
+    const uint32_t base = prefix + woff + x - tot;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const uint32_t l = l0 + 4u * q;
+        if (l + 3u < L) {
+            *reinterpret_cast<uint4*>(k.l.cursor + l) =
+                make_uint4(base + ex[4 * q], base + ex[4 * q + 1], base + ex[4 * q + 2], base + ex[4 * q + 3]);
+        } else {
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+                if (l + e < L) k.l.cursor[l + e] = base + ex[4 * q + e];
+        }
+    }
+    if (with_hazard) {
+        const uint32_t dt = k.p.time_step;
+        const float season = k.clock->season;
+        const uint32_t V = k.m.n_variants;
+        // PER consecutive locations lie in one mask word (PER divides 32)
+        const uint32_t wi = l0 >> 5;
+        const uint32_t sw = k.l.smask[wi];
+        const uint32_t mine = (sw >> (l0 & 31u)) & ((PER == 32) ? 0xFFFFFFFFu : ((1u << PER) - 1u));
+        __syncwarp();
+        if ((l0 & 31u) == 0u) {
+            k.l.hmask[wi] = sw;
+            if (sw) k.l.smask[wi] = 0u;
+        }
+        if (mine) {
+#pragma unroll
+            for (int e = 0; e < PER; ++e) {
+                if (!((mine >> e) & 1u)) continue;
+                const uint32_t l = l0 + e;
+                if (l >= L) continue;
+                const uint32_t rep = k.l.rep[l];
+                for (uint32_t v = 0; v < V; ++v) {
+                    const size_t idx = (size_t)v * L + l;
+                    const long long fix = (long long)k.l.sfix[idx];
+                    float h = 0.0f, xx = 0.0f;
+                    if (fix != 0) {
+                        h = psim_hazard_x(fix, c[e], k.r.k_f[rep], k.l.infectiousness[l], season, dt, &xx);
+                        k.l.sfix[idx] = 0ull;
+                    }
+                    k.l.hazard[idx] = h;
+                    if (k.adj.on) k.l.hazard_x[idx] = xx;
+                }
+            }
+        }
+    }
+    if (merge_q) {
+#pragma unroll
+        for (int e = 0; e < PER; ++e) {
+            const uint32_t l = l0 + e;
+            if (l < L) {
+                const uint32_t qq = k.l.qu_pending[l];
+                if (qq) {
+                    if (qq > k.l.quarantine_until[l]) k.l.quarantine_until[l] = qq;
+                    k.l.qu_pending[l] = 0u;
+                }
+            }
+        }
+    }
+}
+
 // CSR scatter and/or infection draw of one step.
 __global__ void __launch_bounds__(256) k_scatter_draw(KArgs k, uint32_t step, int scatter, int draw) {
     __shared__ double s_grad[GRAD_N];
@@ -1728,6 +1870,13 @@ template <int ITEMS>
 static void launch_scan_items(const KArgs& k, int with_hazard, int merge_q, cudaStream_t s) {
     unsigned tiles = (k.l.n + SCAN_THREADS * ITEMS - 1) / (SCAN_THREADS * ITEMS);
     if (!tiles) tiles = 1;
+    if (k.tune.scan_mode == 2 && (ITEMS == 4 || ITEMS == 8)) {
+        // thread-contiguous: ITEMS / 4 vectors of 4 locations per thread
+        constexpr int Q = ITEMS >= 8 ? 2 : 1;
+        k_tile_sums_v<Q><<<tiles, SCAN_THREADS, 0, s>>>(k);
+        k_scan_v<Q><<<tiles, SCAN_THREADS, 0, s>>>(k, with_hazard, merge_q);
+        return;
+    }
     if (k.tune.scan_mode == 0) {
         k_scan<ITEMS, true><<<tiles, SCAN_THREADS, 0, s>>>(k, with_hazard, merge_q);
     } else {
