@@ -528,12 +528,14 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     k.p = c->params;
     k.spd = c->spd;
     k.track_expected = 0;
-    k.tune.agg_count = 1;
-    k.tune.scan_items = 8;
-    k.tune.scan_mode = 1;
-    k.tune.agg_slot = 1;
-    k.tune.blocks_per_sm = 0;
-    k.tune.variant = 0;
+    // the fastest choice measured on GB300 at 2M agents; the autotuner
+    // (pansim_gb300/autotune.py) picks per device and workload
+    k.tune.agg_count = 0;
+    k.tune.scan_items = 4;
+    k.tune.scan_mode = 2;
+    k.tune.agg_slot = 0;
+    k.tune.blocks_per_sm = 4;
+    k.tune.variant = 3;
     c->h_stats.resize(R);
     c->h_expected.assign(R, 0.0);
     // healthcare workers per replica (Simulation::flagHealthcareWorkers, simulation.h:670-693)

@@ -282,7 +282,7 @@ class GpuSim:
         self._ck(lib().psim_time_step_kernels(self.h, t, _p(ms)), "time_step_kernels")
         return ms
 
-    def set_tuning(self, agg_count=1, agg_slot=1, blocks_per_sm=0, variant=0, scan_items=8, scan_mode=1):
+    def set_tuning(self, agg_count=0, agg_slot=0, blocks_per_sm=4, variant=3, scan_items=4, scan_mode=2):
         t = cabi.PsimTuning(agg_count, agg_slot, blocks_per_sm, variant, scan_items, scan_mode)
         self._ck(lib().psim_set_tuning(self.h, C.byref(t)), "set_tuning")
 
