@@ -33,10 +33,15 @@ UNIT = "agent-steps/s"
 # 32*N + 20*L, and of each kernel of the step
 STEP_BYTES = (32, 20)
 # k_step_fused: location, rank, steps (r+w), infectiousness, replica, CSR offset
-# and hazard gathers, CSR and rank writes = 38 B/agent; k_scan: counts (r+w),
-# offsets, fixed-point sums, hazard, w_l, replica = 30 B/location
-KERNEL_BYTES = {"movement": (20, 4), "scan": (0, 30), "step_fused": (38, 0)}
-KERNEL_NAMES = ["movement", "scan", "step_fused"]
+# and hazard gathers, CSR and rank writes = 38 B/agent; k_step_hot: location,
+# steps (r+w), CSR write = 16 B/agent, cursor (r+w) = 8 B/location; k_step_cold
+# works on the queued agents only (their number is not known here, so no
+# bytes); k_scan: counts (r+w), offsets, fixed-point sums, hazard, w_l,
+# replica = 30 B/location
+KERNEL_BYTES = {"movement": (20, 4), "scan": (0, 30), "step_fused": (38, 0), "step_hot": (16, 8),
+                "step_cold": None}
+KERNEL_LABELS = {"scan": "k_tile_sums + k_scan", "step_fused": "k_step_fused", "step_hot": "k_step_hot",
+                 "step_cold": "k_step_cold"}
 
 
 def dist_env():
@@ -427,7 +432,7 @@ def main():
     g.run_day(day)  # captures the profiled graph
     day += 1
     n_prof = min(args.steps, 10)
-    kms_sum = np.zeros(4)
+    kms_sum = np.zeros(5)
     prof_day_ms = 0.0
     for _ in range(n_prof):
         flush.fill_(1.0)
@@ -437,9 +442,13 @@ def main():
         prof_day_ms += g.last_day_ms()
         day += 1
     g.set_profiling(False)
-    # average launch durations: movement(0) once a day, scan every step, fused
-    # scatter/draw/movement on all steps but the last
+    # average launch durations: movement(0) once a day, scan every step, the
+    # step kernels (fused, or hot + cold) on all steps but the last
+    split = best.get("variant") == 3
+    names = ["movement", "scan"] + (["step_hot", "step_cold"] if split else ["step_fused"])
     kms = [kms_sum[0] / n_prof, kms_sum[1] / (n_prof * spd), kms_sum[2] / (n_prof * (spd - 1))]
+    if split:
+        kms.append(kms_sum[4] / (n_prof * (spd - 1)))
 
     # end to end through the C ABI with pinned host buffers: per step, the
     # full mutable state host->device, one day, the full state device->host
@@ -470,7 +479,10 @@ def main():
         peak, peak_kind = peaks()
         N, L = snap.n_agents, snap.n_locations
         kern = {}
-        for name, ms in zip(KERNEL_NAMES, kms):
+        for name, ms in zip(names, kms):
+            if KERNEL_BYTES[name] is None:
+                kern[name] = {"ms": float(ms), "alg_bytes": None, "gbs": None}
+                continue
             bn, bl = KERNEL_BYTES[name]
             b = bn * N + bl * L
             kern[name] = {"ms": float(ms), "alg_bytes": b, "gbs": b / (ms * 1e-3) / 1e9}
@@ -480,10 +492,11 @@ def main():
         # event-timed pass and serve as shares
         step_ms = graph_ms / (args.steps * spd)
         step_bytes = STEP_BYTES[0] * N + STEP_BYTES[1] * L
-        tot_k = sum(x["ms"] for x in kern.values() if x is not kern["movement"]) or 1.0
-        for name in ("scan", "step_fused"):
+        step_names = names[1:]
+        tot_k = sum(kern[n]["ms"] for n in step_names) or 1.0
+        for name in step_names:
             kern[name]["share_of_step"] = kern[name]["ms"] / tot_k
-        dom = max(("scan", "step_fused"), key=lambda k: kern[k]["ms"])
+        dom = max(step_names, key=lambda k: kern[k]["ms"])
         tr = committed_traffic()
         traffic = tr.get("step") if tr else None
         ach = step_bytes / (step_ms * 1e-3) / 1e9
@@ -494,7 +507,7 @@ def main():
             "config": {"workload": "2M agents, 500k non-home locations (+homes), dt 10 min, 1 day per step",
                        "agents": N, "locations": L, "timesteps_per_step": 144,
                        "l2": "flushed between timed steps (256 MiB write)", "parallelism": "replicas" if ws > 1 else "1 gpu"},
-            "roofline": {"bound": "hbm", "kernel": "one timestep: k_scan + k_step_fused",
+            "roofline": {"bound": "hbm", "kernel": "one timestep: " + " + ".join(KERNEL_LABELS[n] for n in step_names),
                          "achieved": ach, "peak": peak,
                          "unit": "GB/s", "frac": ach / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "alg_bytes_per_launch": step_bytes, "launch_ms": step_ms, "dominant": dom,

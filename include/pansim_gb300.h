@@ -226,7 +226,8 @@ typedef struct psim_tuning {
     uint32_t blocks_per_sm;  /* 256-thread blocks per SM of the per-agent kernels; 0 = occupancy */
     uint32_t variant;        /* fused step kernel: 0/1/2 = one kernel capped at 64/40/32
                                 registers, 3 = hot/cold split, 4/5 = 2/4 agents per
-                                thread in flight (plain slot atomics) */
+                                thread in flight (plain slot atomics), 6 = hot/cold
+                                split with 2 agents per hot thread in flight */
     uint32_t scan_items;     /* locations per thread of the scan: 2, 4 or 8 (0 = 8) */
     uint32_t scan_mode;      /* 0 = single pass with decoupled look-back, 1 = tile sums + scan,
                                 2 = tile sums + scan with each thread owning consecutive
@@ -403,11 +404,13 @@ int psim_time_step_kernels(psim_ctx* ctx, uint32_t t, float* ms /* [3] */);
 int psim_last_day_ms(psim_ctx* ctx, float* ms);
 /* With on != 0 the day graph is captured with event-record nodes around
  * each of its kernel groups; psim_day_kernel_ms then gives, for the last
- * psim_run_steps, the summed durations ms[4] = {movement of step 0, the
- * scans of all steps (tile sums + scan), the fused scatter/draw/movement
- * kernels of steps 0..spd-2, the scatter/draw of the last step}. */
+ * psim_run_steps, the summed durations ms[5] = {movement of step 0, the
+ * scans of all steps (tile sums + scan), the first step kernel of steps
+ * 0..spd-2 (the fused scatter/draw/movement kernel, or the hot kernel of the
+ * hot/cold form), the scatter/draw of the last step, the cold kernel of steps
+ * 0..spd-2 (0 for the fused forms)}. */
 int psim_set_profiling(psim_ctx* ctx, int on);
-int psim_day_kernel_ms(psim_ctx* ctx, float* ms /* [4] */);
+int psim_day_kernel_ms(psim_ctx* ctx, float* ms /* [5] */);
 /* Counts of kernel launches issued by the library since creation. */
 int psim_launch_count(psim_ctx* ctx, uint64_t* out);
 /* The context's cudaStream_t (as void*), for callers that order their own work after it. */

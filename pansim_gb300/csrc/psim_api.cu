@@ -217,8 +217,9 @@ int capture_day_graph(psim_ctx* c) {
         c->day_graph = nullptr;
     }
     cudaGraph_t g = nullptr;
-    // 2 * spd + 2 events: [0] before movement(0), then one after every kernel group
-    const size_t n_ev = c->profile ? 2ull * c->spd + 2 : 0;
+    // 3 * spd + 2 events: [0] before movement(0), then one after every kernel
+    // group (movement; per step the scan, the first and the second step kernel)
+    const size_t n_ev = c->profile ? 3ull * c->spd + 2 : 0;
     while (c->prof_ev.size() < n_ev) {
         cudaEvent_t ev = nullptr;
         CK(cudaEventCreate(&ev));
@@ -238,9 +239,11 @@ int capture_day_graph(psim_ctx* c) {
         launch_scan(c->k, s, 1, merge_q, c->stream);
         mark();
         if (s + 1 < c->spd)
-            launch_step_fused(c->k, s, c->stream);
+            launch_step_fused(c->k, s, c->stream, 0);
         else
             launch_scatter_draw(c->k, s, 1, 1, c->stream);
+        mark();
+        if (s + 1 < c->spd) launch_step_fused(c->k, s, c->stream, 1);
         mark();
     }
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
@@ -248,7 +251,8 @@ int capture_day_graph(psim_ctx* c) {
     e = cudaGraphInstantiate(&c->day_graph, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(c, PSIM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
-    c->graph_kernels = ((uint64_t)scan_kernels(c->k) + (uint64_t)step_fused_kernels(c->k)) * c->spd + 1;
+    // movement(0), the scans, the step kernels of all steps but the last, the last scatter/draw
+    c->graph_kernels = 2 + (uint64_t)scan_kernels(c->k) * c->spd + (uint64_t)step_fused_kernels(c->k) * (c->spd - 1);
     c->graph_dirty = false;
     c->prof_valid = false;
     return 0;
@@ -651,7 +655,7 @@ int psim_set_tuning(psim_ctx* c, const psim_tuning* t) {
     c->k.tune.agg_count = t->agg_count ? 1u : 0u;
     c->k.tune.agg_slot = t->agg_slot ? 1u : 0u;
     c->k.tune.blocks_per_sm = t->blocks_per_sm;
-    if (t->variant > 5) return fail(c, PSIM_ERR_ARG, "variant out of range");
+    if (t->variant > 6) return fail(c, PSIM_ERR_ARG, "variant out of range");
     c->k.tune.variant = t->variant;
     if (t->scan_items != 0 && t->scan_items != 2 && t->scan_items != 4 && t->scan_items != 8)
         return fail(c, PSIM_ERR_ARG, "scan_items must be 2, 4 or 8");
@@ -995,12 +999,15 @@ int psim_day_kernel_ms(psim_ctx* c, float* ms) {
     float t = 0.f;
     CK(cudaEventElapsedTime(&t, c->prof_ev[0], c->prof_ev[1]));
     ms[0] = t;
-    ms[1] = ms[2] = ms[3] = 0.f;
+    ms[1] = ms[2] = ms[3] = ms[4] = 0.f;
     for (uint32_t s = 0; s < c->spd; ++s) {
-        CK(cudaEventElapsedTime(&t, c->prof_ev[1 + 2 * s], c->prof_ev[2 + 2 * s]));
+        const size_t e = 1 + 3 * (size_t)s;
+        CK(cudaEventElapsedTime(&t, c->prof_ev[e], c->prof_ev[e + 1]));
         ms[1] += t;
-        CK(cudaEventElapsedTime(&t, c->prof_ev[2 + 2 * s], c->prof_ev[3 + 2 * s]));
+        CK(cudaEventElapsedTime(&t, c->prof_ev[e + 1], c->prof_ev[e + 2]));
         ms[s + 1 < c->spd ? 2 : 3] += t;
+        CK(cudaEventElapsedTime(&t, c->prof_ev[e + 2], c->prof_ev[e + 3]));
+        ms[4] += t;
     }
     return 0;
 }

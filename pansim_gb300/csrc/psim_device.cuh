@@ -208,7 +208,7 @@ void launch_count(const KArgs& k, cudaStream_t s);
 void launch_scan(const KArgs& k, uint32_t step_in_day, int with_hazard, int merge_quarantine, cudaStream_t s);
 void launch_scatter_draw(const KArgs& k, uint32_t step_in_day, int scatter, int draw, cudaStream_t s);
 void launch_offsets(const KArgs& k, cudaStream_t s);
-void launch_step_fused(const KArgs& k, uint32_t step_in_day, cudaStream_t s);
+void launch_step_fused(const KArgs& k, uint32_t step_in_day, cudaStream_t s, int part = -1);
 int scan_kernels(const KArgs& k);
 // closure rules
 // work-list segments of the hot/cold step (blocks of the hot kernel at most)

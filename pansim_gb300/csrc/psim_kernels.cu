@@ -1162,6 +1162,61 @@ __global__ void __launch_bounds__(256, 8) k_step_hot(KArgs k, uint32_t step, uin
     if (threadIdx.x == 0) k.a.seg_count[blockIdx.x] = s_cnt;
 }
 
+// k_step_hot with U agents per thread in flight: the loads, mask reads and
+// slot atomics of all U agents are issued before any of them is needed.  A
+// block visits U * 256 consecutive agents per trip; its work-list segment
+// holds `cap` entries (a multiple of U * 256).
+template <int U>
+__global__ void __launch_bounds__(256, 8) k_step_hot_ilp(KArgs k, uint32_t step, uint32_t cap) {
+    __shared__ uint32_t s_cnt;
+    if (threadIdx.x == 0) s_cnt = 0u;
+    __syncthreads();
+    const uint32_t N = k.a.n, L = k.l.n;
+    const uint32_t dt = k.p.time_step;
+    const uint32_t minutes = (step + 1) * dt;
+    const bool curfew_now = k.p.enable_curfew && k.p.curfew_begin == minutes / dt;
+    uint32_t* seg = k.a.worklist + (size_t)blockIdx.x * cap;
+    const int lane = threadIdx.x & 31;
+    for (uint32_t base = blockIdx.x * (256u * U); base < N; base += gridDim.x * (256u * U)) {
+        uint32_t loc[U], sv[U], pos[U];
+        bool hz[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint32_t i = base + u * 256u + threadIdx.x;
+            loc[u] = NONE;
+            sv[u] = 0u;
+            if (i < N) {
+                loc[u] = k.a.location[i];
+                sv[u] = k.a.steps_until_move[i];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            hz[u] = false;
+            if (loc[u] < L) hazard_at(k, loc[u], &hz[u]);
+            pos[u] = take_slot(k, loc[u] < L, loc[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const uint32_t i = base + u * 256u + threadIdx.x;
+            const bool act = i < N;
+            const bool ok = act && loc[u] < L;
+            if (ok) store_slot(k, pos[u], i);
+            const bool cold = act && (curfew_now || sv[u] == 0 || hz[u] || !ok);
+            if (act && !cold) k.a.steps_until_move[i] = sv[u] - 1;
+            const unsigned cm = __ballot_sync(0xffffffffu, cold);
+            if (cm) {
+                uint32_t basew = 0;
+                if (lane == __ffs(cm) - 1) basew = atomicAdd(&s_cnt, (uint32_t)__popc(cm));
+                basew = __shfl_sync(0xffffffffu, basew, __ffs(cm) - 1);
+                if (cold) seg[basew + __popc(cm & lanemask_lt())] = i;
+            }
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) k.a.seg_count[blockIdx.x] = s_cnt;
+}
+
 __global__ void __launch_bounds__(256) k_step_cold(KArgs k, uint32_t step, uint32_t cap, uint32_t n_seg) {
     __shared__ double s_grad[GRAD_N];
     grad_begin(k, s_grad);
@@ -1821,9 +1876,11 @@ void launch_movement(const KArgs& k, uint32_t step, cudaStream_t s) {
 // register-capped instantiations of the fused step kernel: a tighter cap
 // raises occupancy for the hot path and spills on the rare cold path; the
 // autotuner picks one (DevTune::variant)
-void launch_step_fused(const KArgs& k, uint32_t step, cudaStream_t s) {
+// part: -1 both kernels of the step; 0 the first (the fused kernel, or the hot
+// kernel of variant 3); 1 the second (the cold kernel of variant 3, else nothing)
+void launch_step_fused(const KArgs& k, uint32_t step, cudaStream_t s, int part) {
     static unsigned g[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    const uint32_t v = k.tune.variant < 6 ? k.tune.variant : 0;
+    const uint32_t v = k.tune.variant < 7 ? k.tune.variant : 0;
     if (!g[0]) {
         g[0] = wave_grid(k_step_fused<4>, 1u << 30);
         g[1] = wave_grid(k_step_fused<6>, 1u << 30);
@@ -1832,17 +1889,30 @@ void launch_step_fused(const KArgs& k, uint32_t step, cudaStream_t s) {
         g[4] = wave_grid(k_step_cold, 1u << 30);
         g[5] = wave_grid(k_step_ilp<2>, 1u << 30);
         g[6] = wave_grid(k_step_ilp<4>, 1u << 30);
+        g[7] = wave_grid(k_step_hot_ilp<2>, 1u << 30);
+    }
+    if (v == 6) {
+        // hot/cold with two agents per hot thread in flight
+        const uint32_t tile = 512;
+        unsigned grid = k.tune.blocks_per_sm ? (unsigned)(sm_count() * k.tune.blocks_per_sm) : g[7];
+        // grid * cap < N + grid * 512 <= N + WORK_MAX_BLOCKS * 256 (the work list's size)
+        grid = std::min(std::min(grid, grid_for((k.a.n + 1) / 2, 1 << 20)), (unsigned)WORK_MAX_BLOCKS / 2);
+        const uint32_t cap = (uint32_t)((((size_t)k.a.n + (size_t)grid * tile - 1) / ((size_t)grid * tile)) * tile);
+        if (part != 1) k_step_hot_ilp<2><<<grid, 256, 0, s>>>(k, step, cap);
+        if (part != 0) k_step_cold<<<std::min(grid, g[4]), 256, 0, s>>>(k, step, cap, grid);
+        return;
     }
     if (v == 3) {
         // one work-list segment per hot block, as many as the block visits
         const unsigned grid = std::min(agent_grid(k, g[3]), (unsigned)WORK_MAX_BLOCKS);
         const uint32_t cap = (uint32_t)((((size_t)k.a.n + (size_t)grid * 256 - 1) / ((size_t)grid * 256)) * 256);
-        k_step_hot<<<grid, 256, 0, s>>>(k, step, cap);
+        if (part != 1) k_step_hot<<<grid, 256, 0, s>>>(k, step, cap);
         // the cold agents are a few percent: at most one wave of cold blocks,
         // each taking segments in turn
-        k_step_cold<<<std::min(grid, g[4]), 256, 0, s>>>(k, step, cap, grid);
+        if (part != 0) k_step_cold<<<std::min(grid, g[4]), 256, 0, s>>>(k, step, cap, grid);
         return;
     }
+    if (part == 1) return;
     if (v == 4 || v == 5) {
         const int U = v == 4 ? 2 : 4;
         unsigned grid = k.tune.blocks_per_sm ? (unsigned)(sm_count() * k.tune.blocks_per_sm) : g[v == 4 ? 5 : 6];
@@ -1861,7 +1931,7 @@ void launch_step_fused(const KArgs& k, uint32_t step, cudaStream_t s) {
     else
         k_step_fused<8><<<grid, 256, 0, s>>>(k, step);
 }
-int step_fused_kernels(const KArgs& k) { return k.tune.variant == 3 ? 2 : 1; }
+int step_fused_kernels(const KArgs& k) { return k.tune.variant == 3 || k.tune.variant == 6 ? 2 : 1; }
 void launch_count(const KArgs& k, cudaStream_t s) { k_count<<<grid_for(k.a.n, 8), 256, 0, s>>>(k); }
 // the scan of the histogram with 256 x tune.scan_items locations per tile:
 // single pass with decoupled look-back (tune.scan_mode 0) or tile sums, then

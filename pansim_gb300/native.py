@@ -262,8 +262,8 @@ class GpuSim:
 
     def day_kernel_ms(self):
         """Summed kernel durations of the last profiled day: movement(0), scans,
-        fused steps, last scatter/draw."""
-        ms = np.zeros(4, np.float32)
+        fused (or hot) step kernels, last scatter/draw, cold step kernels."""
+        ms = np.zeros(5, np.float32)
         self._ck(lib().psim_day_kernel_ms(self.h, _p(ms)), "day_kernel_ms")
         return ms
 
