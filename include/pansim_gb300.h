@@ -139,6 +139,7 @@ typedef struct psim_agents {
     float* symptom_scaling_v;         /* [n_variants * n], variant-major: BasicAgentMeta::scalingSymptoms
                                          of the states up to 6 (agentMeta.cpp:83-84), which the
                                          immunization rescales; NULL = symptom_scaling */
+    const uint8_t* sex;               /* BasicAgentMeta::sex: 0 = F, 1 = M (agentMeta.cpp:53-60); NULL = 0 */
 } psim_agents;
 
 /* Locations (include/locationList.h:46-67) [n_locations], cemetery last. */
@@ -344,6 +345,32 @@ typedef struct psim_immunization {
 int psim_immunization_init(psim_ctx* ctx, const psim_immunization* imm);
 /* Immunization::update for the midnight at t (what psim_midnight runs). */
 int psim_immunize_day(psim_ctx* ctx, uint32_t t, uint32_t* immunized_today);
+
+/* Non-COVID hospitalization and death (Simulation::otherDisease,
+ * include/simulation.h:169-423; --otherDisease, on by default in the
+ * reference, off in a new context).  Per living agent at each midnight, from
+ * the stream (agent, t, OTHER_DISEASE): the end of a non-COVID hospital stay
+ * kills with the table's probability; agents not dead, not severe and not in
+ * hospital draw the (disabled) sudden death and then a hospitalization, whose
+ * length in days is geometric with mean (unsigned)avgLength.  The
+ * hospitalization probability is the table's times the yearly occupancy
+ * multiplier, or, on the days that total_hospitalizations covers, times
+ * max(0, target - in_hospital_with_covid * 9730000/179500) / 48000, with
+ * in_hospital_with_covid counted per replica as in the reference
+ * (due_with_covid 0: states 6..8; 1: infected agents at a hospital location
+ * not discharged today).  psim_midnight runs it after the immunization
+ * (simulation.h:911-912). */
+typedef struct psim_other_disease {
+    uint32_t enabled;                       /* --otherDisease */
+    uint32_t due_with_covid;                /* --dueWithCOVID */
+    uint32_t n_targets;                     /* days of --totalHospitalizations (0: none) */
+    uint32_t pad0;
+    const int32_t* total_hospitalizations;  /* [n_targets], per simulated day */
+} psim_other_disease;
+/* od == NULL or od->enabled == 0 switches it off. */
+int psim_other_disease_init(psim_ctx* ctx, const psim_other_disease* od);
+/* Simulation::otherDisease for the midnight at t (what psim_midnight runs). */
+int psim_other_disease_day(psim_ctx* ctx, uint32_t t);
 
 /* The current run parameters (closure rules change curfew, policy, testing
  * probabilities, ...). */

@@ -62,6 +62,8 @@ def lib():
         L.psim_oracle_immunization_init.argtypes = [P, P]
         L.psim_oracle_immunize.restype = U32
         L.psim_oracle_immunize.argtypes = [P, U32]
+        L.psim_oracle_other_disease_init.argtypes = [P, P]
+        L.psim_oracle_other_disease.argtypes = [P, U32]
         L.psim_oracle_csr_offsets.restype = C.POINTER(C.c_uint32)
         L.psim_oracle_csr_offsets.argtypes = [P]
         L.psim_oracle_csr_agents.restype = C.POINTER(C.c_uint32)
@@ -157,6 +159,13 @@ class Oracle:
 
     def immunize(self, t):
         return lib().psim_oracle_immunize(self.h, t)
+
+    def other_disease_init(self, od):
+        self._od = od
+        lib().psim_oracle_other_disease_init(self.h, C.byref(od) if od is not None else None)
+
+    def other_disease(self, t):
+        lib().psim_oracle_other_disease(self.h, t)
 
 
 def threads():

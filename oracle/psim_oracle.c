@@ -23,6 +23,7 @@
 #include "psim_oracle.h"
 #include "../pansim_gb300/csrc/psim_rng.h"
 #include "../pansim_gb300/csrc/psim_immunity.h"
+#include "../pansim_gb300/csrc/psim_other_disease.h"
 #include <stdlib.h>
 #include <string.h>
 #include <math.h>
@@ -65,6 +66,11 @@ struct psim_oracle {
     float imm_frac[PSIM_IMM_MAX_ROUNDS][10];
     uint32_t imm_category;   /* Immunization::currentCategory */
     uint32_t imm_today;      /* immunizedToday */
+    /* non-COVID hospitalization and death (simulation.h:169-423) */
+    int od_on;
+    uint32_t od_due_with_covid;
+    uint32_t od_n_targets;
+    int32_t* od_targets;
 };
 
 static inline uint32_t wb_of(const psim_oracle* o, uint32_t i) { return o->m->state_wb[(uint8_t)o->a->state[i]]; }
@@ -1034,6 +1040,7 @@ void psim_oracle_midnight(psim_oracle* o, uint32_t t, psim_day_stats* out) {
     if (t > 0 && o->p.testing_enabled) psim_oracle_test(o, t, NULL);
     if (t > 0) psim_oracle_progress(o, t);
     if (o->imm_on) psim_oracle_immunize(o, t);
+    if (o->od_on) psim_oracle_other_disease(o, t);
     psim_oracle_stats(o, t, out);
     psim_oracle_plan(o, t);
 }
@@ -1340,6 +1347,7 @@ void psim_oracle_destroy(psim_oracle* o) {
     free(o->loc_flags);
     free(o->hcw);
     free(o->hcw_count);
+    free(o->od_targets);
     free(o->tpp);
     free(o->variant_active);
     free(o->expected);
@@ -1385,4 +1393,98 @@ double psim_oracle_seasonality(const psim_params* p, uint32_t t, uint32_t spd) {
     calc = calc < 1.0 ? calc : 1.0;
     if (d_mod < d_peak) return 1.0;
     return calc;
+}
+
+/* Simulation::otherDisease, include/simulation.h:169-423, per replica.
+ * In hospital with COVID (:177-195): dueWithCOVID 0 counts the states 6..8
+ * of the reference's model; 1 counts infected agents whose location is a
+ * hospital, less those of WB below S discharged today. */
+static uint32_t od_with_covid(psim_oracle* o, uint32_t q, uint32_t t) {
+    const psim_agents* a = o->a;
+    uint32_t n = 0;
+    for (uint32_t i = o->r.agent_offset[q]; i < o->r.agent_offset[q + 1]; ++i) {
+        uint32_t s = (uint8_t)a->state[i];
+        if (o->od_due_with_covid == 0) {
+            n += (s >= 6 && s <= 8);
+        } else {
+            uint32_t loc = a->location[i];
+            uint32_t lt = loc < o->l->n ? o->l->type[loc] : NONE;
+            int discharged = wb_of(o, i) < WB_S && t > 0 && a->st_hospitalized_until[i] == t;
+            n += o->m->state_infected[s] && lt == o->p.hospital_type && !discharged;
+        }
+    }
+    return n;
+}
+
+void psim_oracle_other_disease_init(psim_oracle* o, const psim_other_disease* od) {
+    free(o->od_targets);
+    o->od_targets = NULL;
+    o->od_on = od && od->enabled;
+    o->od_n_targets = 0;
+    if (!o->od_on) return;
+    o->od_due_with_covid = od->due_with_covid;
+    o->od_n_targets = od->n_targets;
+    if (od->n_targets) {
+        o->od_targets = (int32_t*)malloc(sizeof(int32_t) * od->n_targets);
+        memcpy(o->od_targets, od->total_hospitalizations, sizeof(int32_t) * od->n_targets);
+    }
+}
+
+/* the agents' pass (:214-421) for the midnight at t */
+void psim_oracle_other_disease(psim_oracle* o, uint32_t t) {
+    psim_agents* a = o->a;
+    const psim_model* m = o->m;
+    const uint32_t R = o->r.n, dt = o->p.time_step;
+    const uint32_t day = t / o->spd;
+    float* mul = (float*)calloc(R ? R : 1, sizeof(float));
+    if (day < o->od_n_targets)
+        for (uint32_t q = 0; q < R; ++q) {
+            /* targetHospitalized (unsigned) and probabilityMul (float), :199-203 */
+            double x = (double)o->od_targets[day] - (double)od_with_covid(o, q, t) * (9730000.0 / 179500.0);
+            unsigned target = (unsigned)(x > 0.0 ? x : 0.0);
+            mul[q] = (float)((double)(float)target / 48000.0);
+        }
+    /* the yearly occupancy multiplier (:389-393); past day 1194 the last one */
+    uint32_t yi = 0;
+    while (yi < 3 && (int32_t)day > psim_od_year_day[yi]) yi++;
+#pragma omp parallel for schedule(static)
+    for (int64_t ii = 0; ii < (int64_t)a->n; ++ii) {
+        uint32_t i = (uint32_t)ii;
+        uint32_t wb = wb_of(o, i);
+        if (wb == WB_D) continue;
+        uint32_t rep = o->agent_rep[i];
+        psim_stream rng;
+        psim_stream_init(&rng, o->r.seed[rep], i - o->r.agent_offset[rep], t, PSIM_PHASE_OTHER_DISEASE);
+        uint32_t age = a->age[i];
+        uint32_t ag = age < 5 ? 0 : age < 15 ? 1 : age < 30 ? 2 : age < 60 ? 3 : age < 70 ? 4 : age < 80 ? 5 : 6;
+        uint32_t sex = (a->sex && a->sex[i]) ? 1 : 0;
+        uint32_t pre = a->precond ? a->precond[i] : 0;
+        uint32_t kind = pre == 2 ? 1 : (pre == 4 ? 2 : 0);
+        /* the end of a non-COVID stay (:350-365) */
+        if (t > 0 && a->st_hospitalized_until[i] == t) {
+            if (psim_u01(&rng) * 1.0 < psim_od_prob[kind][1][sex][ag]) {
+                /* DynamicPPState::die(false), dynamicPPState.cpp:313-325 */
+                a->state[i] = (int8_t)m->noncovid_dead_state;
+                a->days[i] = -1;
+                update_meta(o, i);
+                a->st_worst_state[i] = (int8_t)m->noncovid_dead_state;
+                a->st_worst_ts[i] = t;
+                continue;
+            }
+        }
+        /* dead, severe or in hospital (:371-373) */
+        if (wb == WB_S || t < a->st_hospitalized_until[i]) continue;
+        /* sudden death (:376): the draw happens, the comparison is ANDed with false */
+        (void)psim_u01(&rng);
+        /* hospitalization (:395-416) */
+        double prob = psim_od_prob[kind][0][sex][ag] * (mul[rep] > 0.0f ? (double)mul[rep] : psim_od_year_mult[yi]);
+        if (psim_u01(&rng) * 1.0 < prob) {
+            unsigned avg = (unsigned)psim_od_avg_length[kind];
+            unsigned len = (unsigned)psim_geometric(&rng, psim_geometric_threshold(1.0 / (double)avg));
+            if (len == 0) len = 1;
+            a->st_hospitalized_ts[i] = t;
+            a->st_hospitalized_until[i] = t + len * 24u * 60u / dt;
+        }
+    }
+    free(mul);
 }

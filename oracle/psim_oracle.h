@@ -50,6 +50,9 @@ int psim_oracle_threads(void);
 /* immunization: categories (init), Immunization::update (immunize; returns immunizedToday) */
 void psim_oracle_immunization_init(psim_oracle* o, const psim_immunization* imm);
 uint32_t psim_oracle_immunize(psim_oracle* o, uint32_t t);
+/* Simulation::otherDisease: options (NULL or enabled 0 = off) and the pass at midnight t */
+void psim_oracle_other_disease_init(psim_oracle* o, const psim_other_disease* od);
+void psim_oracle_other_disease(psim_oracle* o, uint32_t t);
 
 /* CSR access */
 const uint32_t* psim_oracle_csr_offsets(psim_oracle* o);

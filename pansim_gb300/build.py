@@ -14,7 +14,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libpansim_gb300.so")
-SOURCES = ["psim_kernels.cu", "psim_api.cu", "psim_closures.cu", "psim_immunization.cu", "psim_noalloc.cu"]
+SOURCES = ["psim_kernels.cu", "psim_api.cu", "psim_closures.cu", "psim_immunization.cu", "psim_other_disease.cu",
+           "psim_noalloc.cu"]
 HEADERS = ["psim_device.cuh", "psim_rng.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

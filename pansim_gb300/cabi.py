@@ -36,6 +36,7 @@ AGENT_PTR_FIELDS = [
     "st_quarantined_ts", "st_quarantined_until", "st_days_in_quarantine", "st_hospitalized_ts",
     "st_hospitalized_until", "st_immunization_ts", "st_recovered_ts", "st_variant_mask",
     "st_immunization_count", "st_infected_count", "st_worst_state", "precond", "imm_round", "symptom_scaling_v",
+    "sex",
 ]
 
 
@@ -105,6 +106,26 @@ class PsimImmunization(C.Structure):
                 ("protection_hospitalization_waning", C.c_float * 10),
                 ("variant_similarity", C.c_int32 * PSIM_MAX_STRAINS),
                 ("variant_similar_multiplier", C.c_float * PSIM_MAX_STRAINS)]
+
+
+class PsimOtherDisease(C.Structure):
+    _fields_ = [("enabled", C.c_uint32), ("due_with_covid", C.c_uint32), ("n_targets", C.c_uint32),
+                ("pad0", C.c_uint32), ("total_hospitalizations", P)]
+
+
+def other_disease_options(enabled=1, due_with_covid=0, total_hospitalizations=None):
+    """psim_other_disease for --otherDisease, --dueWithCOVID and the per-day
+    --totalHospitalizations targets (None: the yearly multipliers)."""
+    import numpy as np
+    od = PsimOtherDisease()
+    od.enabled = int(enabled)
+    od.due_with_covid = int(due_with_covid)
+    if total_hospitalizations is not None and len(total_hospitalizations):
+        arr = np.ascontiguousarray(total_hospitalizations, dtype=np.int32)
+        od._targets = arr  # keeps the buffer alive with the struct
+        od.n_targets = len(arr)
+        od.total_hospitalizations = arr.ctypes.data
+    return od
 
 
 PSIM_CLOSURE_MAX_TYPES = 10

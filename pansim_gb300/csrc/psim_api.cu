@@ -15,6 +15,22 @@
 
 using namespace psim;
 
+// the kernels' error flags: reads and clears them
+int check_device_err(psim_ctx* c) {
+    uint32_t e = 0;
+    CK(cudaMemcpyAsync(&e, c->k.err, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (e) {
+        CK(cudaMemsetAsync(c->k.err, 0, sizeof(uint32_t), c->stream));
+        std::string m = "device error flags 0x" + std::to_string(e) + ":";
+        if (e & ERR_LOCATION) m += " agent on an invalid location;";
+        if (e & ERR_TEST_WAIT) m += " bounded wait expired;";
+        if (e & ERR_SCAN_WAIT) m += " scan tile wait expired;";
+        return fail(c, PSIM_ERR_DEVICE, m);
+    }
+    return 0;
+}
+
 namespace {
 
 const char* kVersion = "pansim_gb300 0.1.0 (sm_103a)";
@@ -48,21 +64,6 @@ int dupload(psim_ctx* c, const T** dst, const T* host, size_t count) {
     rc = dcopy_in(c, d, host, count);
     if (rc) return rc;
     *dst = d;
-    return 0;
-}
-
-int check_device_err(psim_ctx* c) {
-    uint32_t e = 0;
-    CK(cudaMemcpyAsync(&e, c->k.err, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-    if (e) {
-        CK(cudaMemsetAsync(c->k.err, 0, sizeof(uint32_t), c->stream));
-        std::string m = "device error flags 0x" + std::to_string(e) + ":";
-        if (e & ERR_LOCATION) m += " agent on an invalid location;";
-        if (e & ERR_TEST_WAIT) m += " bounded wait expired;";
-        if (e & ERR_SCAN_WAIT) m += " scan tile wait expired;";
-        return fail(c, PSIM_ERR_DEVICE, m);
-    }
     return 0;
 }
 
@@ -441,6 +442,13 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
         if ((rc = dalloc(c, &z, N))) return bail(rc);
         da.precond = z;
     }
+    if (a->sex) {
+        if ((rc = dupload(c, &da.sex, a->sex, N))) return bail(rc);
+    } else {
+        uint8_t* z = nullptr;
+        if ((rc = dalloc(c, &z, N))) return bail(rc);
+        da.sex = z;
+    }
     if ((rc = dupload(c, &da.rep, arep.data(), N))) return bail(rc);
 #define AL(field, cnt) \
     if ((rc = dalloc(c, &da.field, cnt))) return bail(rc);
@@ -568,6 +576,7 @@ int psim_destroy(psim_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     closures_free(c);
     immunization_free(c);
+    other_disease_free(c);
     for (auto& kv : c->checkpoints)
         if (kv.second) cudaFree(kv.second);
     if (c->day_graph) cudaGraphExecDestroy(c->day_graph);
@@ -655,7 +664,7 @@ int psim_set_tuning(psim_ctx* c, const psim_tuning* t) {
     c->k.tune.agg_count = t->agg_count ? 1u : 0u;
     c->k.tune.agg_slot = t->agg_slot ? 1u : 0u;
     c->k.tune.blocks_per_sm = t->blocks_per_sm;
-    if (t->variant > 6) return fail(c, PSIM_ERR_ARG, "variant out of range");
+    if (t->variant > 7) return fail(c, PSIM_ERR_ARG, "variant out of range");
     c->k.tune.variant = t->variant;
     if (t->scan_items != 0 && t->scan_items != 2 && t->scan_items != 4 && t->scan_items != 8)
         return fail(c, PSIM_ERR_ARG, "scan_items must be 2, 4 or 8");
@@ -910,6 +919,7 @@ int psim_midnight(psim_ctx* c, uint32_t t, psim_day_stats* out) {
         c->launches += 1;
     }
     if (c->immunization && (rc = immunization_apply(c, t))) return rc;
+    if (c->other_disease && (rc = other_disease_apply(c, t))) return rc;
     if (c->closures) {
         // the rules read replica 0's row even when the caller passes no buffer
         std::vector<psim_day_stats> rows(c->R);

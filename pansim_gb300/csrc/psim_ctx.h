@@ -1,5 +1,6 @@
 // Host-side context of the C ABI, shared by the translation units that
-// implement it (psim_api.cu, psim_closures.cu).
+// implement it (psim_api.cu, psim_closures.cu, psim_immunization.cu,
+// psim_other_disease.cu).
 #pragma once
 #include <cuda_runtime.h>
 
@@ -12,6 +13,7 @@
 namespace psim {
 struct ClosureEngine;
 struct ImmunizationEngine;
+struct OtherDiseaseEngine;
 }  // namespace psim
 
 using psim::KArgs;
@@ -25,6 +27,7 @@ struct psim_ctx {
     std::vector<uint16_t> h_ev_start, h_ev_end, h_ev_duration;
     psim::ClosureEngine* closures = nullptr;
     psim::ImmunizationEngine* immunization = nullptr;
+    psim::OtherDiseaseEngine* other_disease = nullptr;
     int device = 0;
     cudaStream_t stream = nullptr;
     std::string err;
@@ -78,6 +81,13 @@ inline int fail(psim_ctx* c, int code, const std::string& msg) {
         if (e_ != cudaSuccess)                                                                        \
             return fail(c, PSIM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));        \
     } while (0)
+
+// device error flags of the kernels since the last check (psim_api.cu)
+int check_device_err(psim_ctx* c);
+
+// non-COVID hospitalization and death (psim_other_disease.cu)
+void other_disease_free(psim_ctx* c);
+int other_disease_apply(psim_ctx* c, uint32_t t);
 
 // immunization (psim_immunization.cu)
 void immunization_free(psim_ctx* c);

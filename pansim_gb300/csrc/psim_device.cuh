@@ -86,7 +86,8 @@ struct DevAgents {
     uint8_t* st_immunization_count;
     uint8_t* st_infected_count;
     int8_t* st_worst_state;
-    const uint8_t* precond;       // pre-condition index (immunization categories)
+    const uint8_t* precond;       // pre-condition index (immunization categories, other disease)
+    const uint8_t* sex;           // 0 = F, 1 = M (other disease)
     uint8_t* imm_round;           // immunization category round (0 = unassigned, 255 = declined)
     float* scaling_v;             // [V*N] symptom scaling of the states up to 6, per variant
     uint8_t* hcw;                 // healthcare worker flag
@@ -202,6 +203,16 @@ enum {
     SC_INFV = 40           // ever infected per variant, 7 slots (ends at 47)
 };
 
+#if defined(__CUDACC__)
+// DynamicPPState::updateMeta, dynamicPPState.cpp:54-64
+__device__ __forceinline__ void update_meta(const KArgs& k, uint32_t i) {
+    uint8_t s = (uint8_t)k.a.state[i];
+    k.a.infectious[i] = k.m.state_infectious[s] * k.m.variant_multiplier[k.a.variant[i]];
+    float su = k.m.state_susceptible[s] ? 1.0f : 0.0f;
+    for (uint32_t v = 0; v < k.m.n_variants; ++v) k.a.susceptible[(size_t)v * k.a.n + i] = su;
+}
+#endif
+
 // launchers (psim_kernels.cu)
 void launch_movement(const KArgs& k, uint32_t step_in_day, cudaStream_t s);
 void launch_count(const KArgs& k, cudaStream_t s);
@@ -210,10 +221,10 @@ void launch_scatter_draw(const KArgs& k, uint32_t step_in_day, int scatter, int 
 void launch_offsets(const KArgs& k, cudaStream_t s);
 void launch_step_fused(const KArgs& k, uint32_t step_in_day, cudaStream_t s, int part = -1);
 int scan_kernels(const KArgs& k);
-// closure rules
 // work-list segments of the hot/cold step (blocks of the hot kernel at most)
 constexpr uint32_t WORK_MAX_BLOCKS = 152u * 64u;
 
+// closure rules
 struct ClosureTypes {
     uint32_t n;
     uint32_t v[10];

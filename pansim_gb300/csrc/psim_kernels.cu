@@ -36,14 +36,6 @@ __device__ __forceinline__ uint32_t loc_closed_until(const KArgs& k, uint32_t l)
 __device__ __forceinline__ uint32_t loc_qu(const KArgs& k, uint32_t l) { return l < k.l.n ? k.l.quarantine_until[l] : 0u; }
 __device__ __forceinline__ uint32_t loc_type(const KArgs& k, uint32_t l) { return l < k.l.n ? k.l.type[l] : NONE; }
 
-// DynamicPPState::updateMeta, dynamicPPState.cpp:54-64
-__device__ __forceinline__ void update_meta(const KArgs& k, uint32_t i) {
-    uint8_t s = (uint8_t)k.a.state[i];
-    k.a.infectious[i] = k.m.state_infectious[s] * k.m.variant_multiplier[k.a.variant[i]];
-    float su = k.m.state_susceptible[s] ? 1.0f : 0.0f;
-    for (uint32_t v = 0; v < k.m.n_variants; ++v) k.a.susceptible[(size_t)v * k.a.n + i] = su;
-}
-
 // RealMovementOps::findActualLocationForType, movementPolicies.h:69-122.
 // f0, f1, f2: the types resolved by first match (home, school, work except in
 // the plan helpers, movementPolicies.h:1073-1080, :1144, :1209-1214).
@@ -1217,6 +1209,29 @@ __global__ void __launch_bounds__(256, 8) k_step_hot_ilp(KArgs k, uint32_t step,
     if (threadIdx.x == 0) k.a.seg_count[blockIdx.x] = s_cnt;
 }
 
+__device__ __forceinline__ void prefetch_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+
+// The per-agent fields that the draw and the movement decision read, behind
+// branches that keep the compiler from issuing them together: prefetched into
+// L1 at once, so that the decision's chain of dependent loads finds them there.
+__device__ __forceinline__ void prefetch_agent(const KArgs& k, uint32_t i) {
+    prefetch_l1(k.a.rep + i);
+    prefetch_l1(k.a.state + i);
+    prefetch_l1(k.a.type + i);
+    prefetch_l1(k.a.band + i);
+    prefetch_l1(k.a.loc_offset + i);
+    prefetch_l1(k.a.susceptible + i);
+    prefetch_l1(k.a.st_quarantined_until + i);
+    prefetch_l1(k.a.st_hospitalized_ts + i);
+    prefetch_l1(k.a.st_hospitalized_until + i);
+    prefetch_l1(k.a.diagnosed + i);
+    prefetch_l1(k.a.quarantined + i);
+    prefetch_l1(k.a.no_work + i);
+    prefetch_l1(k.a.stayed_home + i);
+    if (k.p.quarantine_policy > 0) prefetch_l1(k.a.st_diagnosed_ts + i);
+}
+
+template <bool PF>
 __global__ void __launch_bounds__(256) k_step_cold(KArgs k, uint32_t step, uint32_t cap, uint32_t n_seg) {
     __shared__ double s_grad[GRAD_N];
     grad_begin(k, s_grad);
@@ -1234,6 +1249,7 @@ __global__ void __launch_bounds__(256) k_step_cold(KArgs k, uint32_t step, uint3
         double term = 0.0;
         uint32_t loc = NONE, loc0 = NONE, var = 0;
         float inf = 0.0f;
+        if (PF && act) prefetch_agent(k, i);
         if (act) {
             loc0 = k.a.location[i];
             const uint32_t s = k.a.steps_until_move[i];
@@ -1880,13 +1896,13 @@ void launch_movement(const KArgs& k, uint32_t step, cudaStream_t s) {
 // kernel of variant 3); 1 the second (the cold kernel of variant 3, else nothing)
 void launch_step_fused(const KArgs& k, uint32_t step, cudaStream_t s, int part) {
     static unsigned g[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    const uint32_t v = k.tune.variant < 7 ? k.tune.variant : 0;
+    const uint32_t v = k.tune.variant < 8 ? k.tune.variant : 0;
     if (!g[0]) {
         g[0] = wave_grid(k_step_fused<4>, 1u << 30);
         g[1] = wave_grid(k_step_fused<6>, 1u << 30);
         g[2] = wave_grid(k_step_fused<8>, 1u << 30);
         g[3] = wave_grid(k_step_hot, 1u << 30);
-        g[4] = wave_grid(k_step_cold, 1u << 30);
+        g[4] = wave_grid(k_step_cold<false>, 1u << 30);
         g[5] = wave_grid(k_step_ilp<2>, 1u << 30);
         g[6] = wave_grid(k_step_ilp<4>, 1u << 30);
         g[7] = wave_grid(k_step_hot_ilp<2>, 1u << 30);
@@ -1899,17 +1915,22 @@ void launch_step_fused(const KArgs& k, uint32_t step, cudaStream_t s, int part) 
         grid = std::min(std::min(grid, grid_for((k.a.n + 1) / 2, 1 << 20)), (unsigned)WORK_MAX_BLOCKS / 2);
         const uint32_t cap = (uint32_t)((((size_t)k.a.n + (size_t)grid * tile - 1) / ((size_t)grid * tile)) * tile);
         if (part != 1) k_step_hot_ilp<2><<<grid, 256, 0, s>>>(k, step, cap);
-        if (part != 0) k_step_cold<<<std::min(grid, g[4]), 256, 0, s>>>(k, step, cap, grid);
+        if (part != 0) k_step_cold<false><<<std::min(grid, g[4]), 256, 0, s>>>(k, step, cap, grid);
         return;
     }
-    if (v == 3) {
+    if (v == 3 || v == 7) {
         // one work-list segment per hot block, as many as the block visits
         const unsigned grid = std::min(agent_grid(k, g[3]), (unsigned)WORK_MAX_BLOCKS);
         const uint32_t cap = (uint32_t)((((size_t)k.a.n + (size_t)grid * 256 - 1) / ((size_t)grid * 256)) * 256);
         if (part != 1) k_step_hot<<<grid, 256, 0, s>>>(k, step, cap);
         // the cold agents are a few percent: at most one wave of cold blocks,
         // each taking segments in turn
-        if (part != 0) k_step_cold<<<std::min(grid, g[4]), 256, 0, s>>>(k, step, cap, grid);
+        if (part != 0) {
+            if (v == 7)
+                k_step_cold<true><<<std::min(grid, g[4]), 256, 0, s>>>(k, step, cap, grid);
+            else
+                k_step_cold<false><<<std::min(grid, g[4]), 256, 0, s>>>(k, step, cap, grid);
+        }
         return;
     }
     if (part == 1) return;
@@ -1931,7 +1952,9 @@ void launch_step_fused(const KArgs& k, uint32_t step, cudaStream_t s, int part) 
     else
         k_step_fused<8><<<grid, 256, 0, s>>>(k, step);
 }
-int step_fused_kernels(const KArgs& k) { return k.tune.variant == 3 || k.tune.variant == 6 ? 2 : 1; }
+int step_fused_kernels(const KArgs& k) {
+    return k.tune.variant == 3 || k.tune.variant == 6 || k.tune.variant == 7 ? 2 : 1;
+}
 void launch_count(const KArgs& k, cudaStream_t s) { k_count<<<grid_for(k.a.n, 8), 256, 0, s>>>(k); }
 // the scan of the histogram with 256 x tune.scan_items locations per tile:
 // single pass with decoupled look-back (tune.scan_mode 0) or tile sums, then

@@ -51,7 +51,8 @@ enum {
     PSIM_PHASE_EXPOSE = 23,    // closure rule ExposeToMutation at the midnight timestamp
     PSIM_PHASE_IMM_CATEGORY = 24, // immunization categories, + category pass (10 passes)
     PSIM_PHASE_IMM_BOOSTER = 40,  // immunization boosters, + round
-    PSIM_PHASE_IMM_PRIMARY = 56   // immunization first doses, + category
+    PSIM_PHASE_IMM_PRIMARY = 56,  // immunization first doses, + category
+    PSIM_PHASE_OTHER_DISEASE = 66 // non-COVID hospitalization and death at the midnight timestamp
 };
 
 typedef struct psim_ctr4 {

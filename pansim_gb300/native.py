@@ -63,6 +63,8 @@ def lib(auto_build=True):
         L.psim_get_params.argtypes = [P, P]
         L.psim_immunization_init.argtypes = [P, P]
         L.psim_immunize_day.argtypes = [P, U32, P]
+        L.psim_other_disease_init.argtypes = [P, P]
+        L.psim_other_disease_day.argtypes = [P, U32]
         L.psim_get_events.argtypes = [P, P, P, P, P, P, P, U32, P]
         L.psim_day_kernel_ms.argtypes = [P, C.c_void_p]
         L.psim_launch_count.argtypes = [P, C.POINTER(C.c_uint64)]
@@ -240,6 +242,16 @@ class GpuSim:
         n = C.c_uint32(0)
         self._ck(lib().psim_immunize_day(self.h, t, C.byref(n)), "immunize")
         return n.value
+
+    # non-COVID hospitalization and death
+    def other_disease_init(self, od):
+        """od: cabi.PsimOtherDisease (cabi.other_disease_options) or None."""
+        self._od = od
+        self._ck(lib().psim_other_disease_init(self.h, C.byref(od) if od is not None else None),
+                 "other_disease_init")
+
+    def other_disease(self, t):
+        self._ck(lib().psim_other_disease_day(self.h, t), "other_disease")
 
     def get_params(self):
         p = cabi.PsimParams()

@@ -28,7 +28,7 @@ AGENT_DTYPES = {
     "st_hospitalized_ts": np.uint32, "st_hospitalized_until": np.uint32,
     "st_immunization_ts": np.uint32, "st_recovered_ts": np.uint32, "st_variant_mask": np.uint32,
     "st_immunization_count": np.uint8, "st_infected_count": np.uint8, "st_worst_state": np.int8,
-    "precond": np.uint8, "imm_round": np.uint8, "symptom_scaling_v": np.float32,
+    "precond": np.uint8, "imm_round": np.uint8, "symptom_scaling_v": np.float32, "sex": np.uint8,
 }
 AGENT_MUTABLE = [
     "location", "steps_until_move", "state", "days", "variant", "infectious", "susceptible",
@@ -87,9 +87,12 @@ class Snapshot:
         self._normalize()
 
     def _normalize(self):
-        # immunization fields absent from older snapshots: their neutral values
+        # immunization and other-disease fields absent from older snapshots:
+        # their neutral values
         n = len(self.agents["location"])
         V = int(self.model["n_variants"])
+        if "sex" not in self.agents:
+            self.agents["sex"] = np.zeros(n, np.uint8)
         if "precond" not in self.agents:
             self.agents["precond"] = np.zeros(n, np.uint8)
         if "imm_round" not in self.agents:

@@ -293,9 +293,11 @@ def make_population(model, n_agents, n_other_locs, pop_seed, initial_infected_fr
     # draws above do not change: 10% of agents, index 1..3
     rng_pc = np.random.default_rng(pop_seed + 0x9C)
     precond = ((rng_pc.random(N) < 0.1) * rng_pc.integers(1, 4, N)).astype(np.uint8)
+    # sex (non-COVID hospitalization tables), its own stream too: half F (0), half M (1)
+    sex = np.random.default_rng(pop_seed + 0x9D).integers(0, 2, N).astype(np.uint8)
     agents = {
         "type": atype, "age": age, "band": band, "prog_id": band.astype(np.uint16),
-        "symptom_scaling": np.ones(N, np.float32), "precond": precond,
+        "symptom_scaling": np.ones(N, np.float32), "precond": precond, "sex": sex,
         "loc_offset": off.astype(np.uint32), "poss_loc": pl, "poss_type": pt,
         "location": home.astype(np.uint32), "steps_until_move": z32.copy(),
         "state": state, "days": days, "variant": variant, "infectious": infectious,

@@ -168,7 +168,9 @@ def test_bounded_wait_reports_error_and_context_survives(gpu_lib):
                                     dict(agg_count=0, agg_slot=0, blocks_per_sm=8, variant=6, scan_items=4,
                                          scan_mode=2),
                                     dict(agg_count=0, agg_slot=1, blocks_per_sm=0, variant=6, scan_items=2,
-                                         scan_mode=1)])
+                                         scan_mode=1),
+                                    dict(agg_count=0, agg_slot=0, blocks_per_sm=4, variant=7, scan_items=4,
+                                         scan_mode=2)])
 def test_tuning_choices_do_not_change_results(gpu_lib, tuning):
     s_cpu, s_gpu, o, g = _pair(n=12000, locs=3000, initial_infected_frac=0.02)
     g.set_tuning(**tuning)
