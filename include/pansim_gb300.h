@@ -228,7 +228,8 @@ typedef struct psim_tuning {
     uint32_t variant;        /* fused step kernel: 0/1/2 = one kernel capped at 64/40/32
                                 registers, 3 = hot/cold split, 4/5 = 2/4 agents per
                                 thread in flight (plain slot atomics), 6 = hot/cold
-                                split with 2 agents per hot thread in flight */
+                                split with 2 agents per hot thread in flight, 7 = hot/cold
+                                split with the cold agents spread evenly over the grid */
     uint32_t scan_items;     /* locations per thread of the scan: 2, 4 or 8 (0 = 8) */
     uint32_t scan_mode;      /* 0 = single pass with decoupled look-back, 1 = tile sums + scan,
                                 2 = tile sums + scan with each thread owning consecutive

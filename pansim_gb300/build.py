@@ -16,7 +16,8 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libpansim_gb300.so")
 SOURCES = ["psim_kernels.cu", "psim_api.cu", "psim_closures.cu", "psim_immunization.cu", "psim_other_disease.cu",
            "psim_noalloc.cu"]
-HEADERS = ["psim_device.cuh", "psim_rng.h"]
+# every header of csrc/: a change to any of them rebuilds every object
+HEADERS = sorted(f for f in os.listdir(CSRC) if f.endswith((".h", ".cuh")))
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

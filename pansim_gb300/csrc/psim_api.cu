@@ -188,7 +188,15 @@ int upload_mutable(psim_ctx* c, const psim_agents* a, const psim_locations* l) {
 }
 
 // LocationsList::initialize (locationList.h:224-230) and the variant gates
+// the next scan rebuilds the CSR whatever moved
+int force_rebuild(psim_ctx* c) {
+    CK(cudaMemsetAsync(c->k.l.build + 1, 0xFF, sizeof(uint32_t), c->stream));
+    return 0;
+}
+
 int initial_regroup(psim_ctx* c) {
+    int rc0 = force_rebuild(c);
+    if (rc0) return rc0;
     CK(cudaMemsetAsync(c->k.l.counts, 0, sizeof(uint32_t) * c->L, c->stream));
     CK(cudaMemsetAsync(c->k.l.sfix, 0, sizeof(unsigned long long) * c->L * c->V, c->stream));
     CK(cudaMemsetAsync(c->k.l.smask, 0, sizeof(uint32_t) * (((size_t)c->L + 2047) / 2048 * 64 + 64), c->stream));
@@ -492,6 +500,7 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     if ((rc = dalloc(c, &dl.tile_sums, tiles))) return bail(rc);
     if ((rc = dalloc(c, &dl.scan_status, tiles))) return bail(rc);
     if ((rc = dalloc(c, &dl.scan_state, 2))) return bail(rc);
+    if ((rc = dalloc(c, &dl.build, 3))) return bail(rc);
     // replicas
     DevReps& dr = k.r;
     dr.n = c->R;
@@ -664,7 +673,7 @@ int psim_set_tuning(psim_ctx* c, const psim_tuning* t) {
     c->k.tune.agg_count = t->agg_count ? 1u : 0u;
     c->k.tune.agg_slot = t->agg_slot ? 1u : 0u;
     c->k.tune.blocks_per_sm = t->blocks_per_sm;
-    if (t->variant > 7) return fail(c, PSIM_ERR_ARG, "variant out of range");
+    if (t->variant > 9) return fail(c, PSIM_ERR_ARG, "variant out of range");
     c->k.tune.variant = t->variant;
     if (t->scan_items != 0 && t->scan_items != 2 && t->scan_items != 4 && t->scan_items != 8)
         return fail(c, PSIM_ERR_ARG, "scan_items must be 2, 4 or 8");
@@ -761,6 +770,9 @@ int psim_checkpoint_restore(psim_ctx* c, uint32_t slot) {
         CK(cudaMemcpyAsync(r.first, src, r.second, cudaMemcpyDeviceToDevice, c->stream));
         src += r.second;
     }
+    // the restored locations need not match the agent list of the last step
+    int rc = force_rebuild(c);
+    if (rc) return rc;
     CK(cudaStreamSynchronize(c->stream));
     c->csr_fresh = false;
     return 0;
@@ -812,11 +824,12 @@ int psim_movement(psim_ctx* c, uint32_t t) {
 
 int psim_regroup(psim_ctx* c) {
     if (!c || !c->uploaded) return PSIM_ERR_STATE;
+    int rc0 = force_rebuild(c);
+    if (rc0) return rc0;
     if (!c->csr_fresh) {
         CK(cudaMemsetAsync(c->k.l.counts, 0, sizeof(uint32_t) * c->L, c->stream));
         CK(cudaMemsetAsync(c->k.l.sfix, 0, sizeof(unsigned long long) * c->L * c->V, c->stream));
         CK(cudaMemsetAsync(c->k.l.smask, 0, sizeof(uint32_t) * (((size_t)c->L + 2047) / 2048 * 64 + 64), c->stream));
-    CK(cudaMemsetAsync(c->k.l.smask, 0, sizeof(uint32_t) * (((size_t)c->L + 2047) / 2048 * 64 + 64), c->stream));
         launch_count(c->k, c->stream);
         c->launches += 1;
     }

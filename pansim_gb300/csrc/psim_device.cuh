@@ -125,7 +125,19 @@ struct DevLocs {
     uint32_t* tile_sums;          // per-tile sums of the histogram (two-pass scan)
     uint64_t* scan_status;        // per-tile status words of the single-pass scan (epoch | flag | value)
     uint32_t* scan_state;         // [0] epoch of the next single-pass scan, [1] its tile ticket
+    uint32_t* build;              // [0] timestamp at which agents last took new locations,
+                                  // [1] BUILD_PENDING (rebuild at the next scan) or the timestamp
+                                  //     of the scan that took the pending rebuild,
+                                  // [2] the timestamp of the last step that rebuilt (decided by
+                                  //     the step's first scan kernel, read by its later kernels)
 };
+
+// Incremental CSR: at most steps of a day no agent moves, and then the
+// histogram, the offsets and the agent list of the step before are this
+// step's too.  A step rebuilds them (tile sums, prefix, cursors, slot
+// atomics, CSR writes) only when agents took new locations for it, or after
+// the state was replaced (upload, restore, explicit regroup).
+constexpr uint32_t BUILD_PENDING = 0xFFFFFFFFu;
 
 struct DevReps {
     uint32_t n;
@@ -204,6 +216,33 @@ enum {
 };
 
 #if defined(__CUDACC__)
+// The first scan kernel of the step at timestamp t decides whether the CSR is
+// rebuilt (agents took new locations for t, or a rebuild is pending) and
+// records the decision in build[2]; its block 0 turns BUILD_PENDING into t,
+// which leaves the decision of its other blocks unchanged.  Movers of the
+// same launch only write build[0] for t + 1, which this launch does not
+// read after its start.
+// The words are written by earlier kernels (or by block 0 here, which leaves
+// the decision unchanged): plain loads, so that the warps of an SM share one
+// L1 line instead of queueing on one L2 address.
+__device__ __forceinline__ bool csr_decide(const KArgs& k, uint32_t t) {
+    const uint32_t moved = k.l.build[0];
+    const uint32_t force = k.l.build[1];
+    const bool r = moved == t || force == t || force == BUILD_PENDING;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (force == BUILD_PENDING) k.l.build[1] = t;
+        k.l.build[2] = r ? t : NONE;
+    }
+    return r;
+}
+// the decision, in the later kernels of the step at t
+__device__ __forceinline__ bool csr_rebuild(const KArgs& k, uint32_t t) { return k.l.build[2] == t; }
+// movers of a block publish the timestamp of their new locations (one store
+// per block; every thread of the block calls this)
+__device__ __forceinline__ void publish_moved(const KArgs& k, bool any, uint32_t t_new) {
+    if (__syncthreads_or(any) && threadIdx.x == 0) k.l.build[0] = t_new;
+}
+
 // DynamicPPState::updateMeta, dynamicPPState.cpp:54-64
 __device__ __forceinline__ void update_meta(const KArgs& k, uint32_t i) {
     uint8_t s = (uint8_t)k.a.state[i];

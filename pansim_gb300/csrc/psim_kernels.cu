@@ -416,7 +416,9 @@ constexpr int SCAN_THREADS = 256;
 // forget reductions); agents that stay do not touch the histogram.  The
 // fixed-point infectiousness sums are rebuilt every step: every infectious
 // agent adds its term at its (new) location, and the scan consumes them.
-__device__ __forceinline__ void count_agent(const KArgs& k, bool act, uint32_t loc0, uint32_t loc, float inf,
+// Returns whether the agent took a new location (its kernel then publishes
+// the timestamp of the new locations, publish_moved).
+__device__ __forceinline__ bool count_agent(const KArgs& k, bool act, uint32_t loc0, uint32_t loc, float inf,
                                             uint32_t variant) {
     const uint32_t L = k.l.n;
     if (act && loc >= L) {
@@ -433,6 +435,7 @@ __device__ __forceinline__ void count_agent(const KArgs& k, bool act, uint32_t l
         atomicAdd(&k.l.sfix[(size_t)variant * L + loc], (unsigned long long)q);
         atomicOr(&k.l.smask[loc >> 5], 1u << (loc & 31u));
     }
+    return mv;
 }
 
 // The full histogram of the current positions (after a reset of counts and sums).
@@ -453,7 +456,11 @@ __device__ __forceinline__ void count_full(const KArgs& k, bool act, uint32_t lo
 
 // CSR slot of an agent: a warp-aggregated returning atomic on the location's
 // cursor, which the scan set to the location's first slot.  Warp-collective.
-__device__ __forceinline__ uint32_t take_slot(const KArgs& k, bool ok, uint32_t loc) {
+// the slot of an agent whose step keeps the agent list of the step before
+constexpr uint32_t SLOT_KEEP = 0xFFFFFFFEu;
+
+__device__ __forceinline__ uint32_t take_slot(const KArgs& k, bool ok, uint32_t loc, bool rebuild) {
+    if (!rebuild) return SLOT_KEEP;
     if (!k.tune.agg_slot) return ok ? atomicAdd(&k.l.cursor[loc], 1u) : NONE;
     const unsigned valid = __ballot_sync(0xffffffffu, ok);
     uint32_t pos = NONE;
@@ -469,6 +476,7 @@ __device__ __forceinline__ uint32_t take_slot(const KArgs& k, bool ok, uint32_t 
 }
 
 __device__ __forceinline__ void store_slot(const KArgs& k, uint32_t pos, uint32_t i) {
+    if (pos == SLOT_KEEP) return;
     if (pos < k.a.n)
         k.l.csr_agents[pos] = i;
     else
@@ -562,6 +570,7 @@ __global__ void __launch_bounds__(256) k_movement(KArgs k, uint32_t step) {
     const uint32_t N = k.a.n;
     const StepClock c = step_clock(k, step);
     const uint32_t stride = gridDim.x * blockDim.x;
+    bool moved = false;
     for (uint32_t base = blockIdx.x * blockDim.x; base < N; base += stride) {
         const uint32_t i = base + threadIdx.x;
         const bool act = i < N;
@@ -575,8 +584,9 @@ __global__ void __launch_bounds__(256) k_movement(KArgs k, uint32_t step) {
             loc = (c.curfew_now || s == 0) ? k.a.location[i] : loc0;
             if (inf > 0.0f) var = k.a.variant[i];
         }
-        count_agent(k, act, loc0, loc, inf, var);
+        moved |= count_agent(k, act, loc0, loc, inf, var);
     }
+    publish_moved(k, moved, c.t);
 }
 
 // Histogram + fixed-point sums without movement (regroup after an upload).
@@ -620,9 +630,10 @@ __device__ __forceinline__ uint32_t block_sum_256(uint32_t v, uint32_t* s_red) {
 }
 
 template <int ITEMS>
-__global__ void __launch_bounds__(SCAN_THREADS) k_tile_sums(KArgs k) {
+__global__ void __launch_bounds__(SCAN_THREADS) k_tile_sums(KArgs k, uint32_t step) {
     constexpr int TILE = SCAN_THREADS * ITEMS;
     __shared__ uint32_t s_red[SCAN_THREADS / 32];
+    if (!csr_decide(k, k.clock->t0 + step)) return;  // the tile sums serve the rebuild only
     const uint32_t L = k.l.n;
     const uint32_t base = blockIdx.x * TILE;
     uint32_t v = 0;
@@ -649,15 +660,21 @@ __device__ __forceinline__ uint64_t ld_volatile_u64(const uint64_t* p) {
 }
 
 template <int ITEMS, bool LOOKBACK>
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, int with_hazard, int merge_q) {
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, uint32_t step, int with_hazard, int merge_q) {
     constexpr int TILE = SCAN_THREADS * ITEMS;
     __shared__ uint32_t s_red[SCAN_THREADS / 32];
     __shared__ uint32_t s_warp[SCAN_THREADS / 32];
     __shared__ uint32_t s_tile, s_epoch, s_prefix;
     const uint32_t L = k.l.n;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // the single-pass form is the step's first kernel and decides; the
+    // two-pass form reads the decision of its tile-sum kernel.  Without a
+    // rebuild no ticket is taken and the cursors keep the ends of the step
+    // before (no prefix, no cursor writes).
+    const uint32_t t_step = k.clock->t0 + step;
+    const bool rebuild = LOOKBACK ? csr_decide(k, t_step) : csr_rebuild(k, t_step);
     uint32_t tile = blockIdx.x, epoch = 0;
-    if (LOOKBACK) {
+    if (LOOKBACK && rebuild) {
         if (threadIdx.x == 0) {
             // the epoch is read before the ticket: the last ticket advances it
             s_epoch = *((volatile uint32_t*)&k.l.scan_state[0]);
@@ -676,7 +693,8 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, int with_hazard,
         c[q] = l < L ? k.l.counts[l] : 0u;
     }
     uint32_t prefix = 0;
-    if (LOOKBACK) {
+    if (!rebuild) {
+    } else if (LOOKBACK) {
         uint32_t mine = 0;
 #pragma unroll
         for (int q = 0; q < ITEMS; ++q) mine += c[q];
@@ -747,31 +765,33 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, int with_hazard,
     }
     prefix = block_sum_256(pre, s_red);
     }
-    uint32_t carry = 0;
+    if (rebuild) {
+        uint32_t carry = 0;
 #pragma unroll
-    for (int q = 0; q < ITEMS; ++q) {
-        uint32_t x = c[q];
+        for (int q = 0; q < ITEMS; ++q) {
+            uint32_t x = c[q];
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x += y;
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+                if (lane >= o) x += y;
+            }
+            ex[q] = carry + x - c[q];
+            carry += __shfl_sync(0xffffffffu, x, 31);
         }
-        ex[q] = carry + x - c[q];
-        carry += __shfl_sync(0xffffffffu, x, 31);
+        if (lane == 0) s_warp[warp] = carry;
+        __syncthreads();
+        uint32_t woff = 0;
+        for (int q = 0; q < warp; ++q) woff += s_warp[q];
+        const uint32_t base = prefix + woff;
+#pragma unroll
+        for (int q = 0; q < ITEMS; ++q) {
+            const uint32_t l = wbase + q * 32 + lane;
+            if (l < L) k.l.cursor[l] = base + ex[q];
+        }
     }
-    if (lane == 0) s_warp[warp] = carry;
-    __syncthreads();
-    uint32_t woff = 0;
-    for (int q = 0; q < warp; ++q) woff += s_warp[q];
-    const uint32_t base = prefix + woff;
     const uint32_t dt = k.p.time_step;
     const float season = k.clock->season;
     const uint32_t V = k.m.n_variants;
-#pragma unroll
-    for (int q = 0; q < ITEMS; ++q) {
-        const uint32_t l = wbase + q * 32 + lane;
-        if (l < L) k.l.cursor[l] = base + ex[q];
-    }
     if (with_hazard) {
         // only locations that received infectiousness this step (sum mask)
         // are read; elsewhere the hazard is 0 and stays unwritten, the hazard
@@ -848,9 +868,10 @@ __device__ __forceinline__ void load_counts4(const KArgs& k, uint32_t l0, uint32
 }
 
 template <int Q>
-__global__ void __launch_bounds__(SCAN_THREADS) k_tile_sums_v(KArgs k) {
+__global__ void __launch_bounds__(SCAN_THREADS) k_tile_sums_v(KArgs k, uint32_t step) {
     constexpr int PER = 4 * Q;
     __shared__ uint32_t s_red[SCAN_THREADS / 32];
+    if (!csr_decide(k, k.clock->t0 + step)) return;  // the tile sums serve the rebuild only
     uint32_t c[PER];
     load_counts4<Q>(k, blockIdx.x * (SCAN_THREADS * PER) + threadIdx.x * PER, c);
     uint32_t v = 0;
@@ -861,7 +882,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_tile_sums_v(KArgs k) {
 }
 
 template <int Q>
-__global__ void __launch_bounds__(SCAN_THREADS) k_scan_v(KArgs k, int with_hazard, int merge_q) {
+__global__ void __launch_bounds__(SCAN_THREADS) k_scan_v(KArgs k, uint32_t step, int with_hazard, int merge_q) {
     constexpr int PER = 4 * Q;
     __shared__ uint32_t s_red[SCAN_THREADS / 32];
     __shared__ uint32_t s_warp[SCAN_THREADS / 32];
@@ -869,52 +890,57 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_v(KArgs k, int with_hazar
     const uint32_t tile = blockIdx.x;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t l0 = tile * (SCAN_THREADS * PER) + threadIdx.x * PER;
-    uint32_t c[PER];
-    load_counts4<Q>(k, l0, c);
-    // sum of the tiles before this one
-    uint32_t pre = 0;
-    {
-        uint32_t p0 = 0, p1 = 0, p2 = 0, p3 = 0;
-        uint32_t j = threadIdx.x;
-        for (; j + 3 * SCAN_THREADS < tile; j += 4 * SCAN_THREADS) {
-            p0 += k.l.tile_sums[j];
-            p1 += k.l.tile_sums[j + SCAN_THREADS];
-            p2 += k.l.tile_sums[j + 2 * SCAN_THREADS];
-            p3 += k.l.tile_sums[j + 3 * SCAN_THREADS];
+    // without a rebuild the cursors keep the ends of the step before, and
+    // the counts are read at the flagged locations only
+    const bool rebuild = csr_rebuild(k, k.clock->t0 + step);
+    uint32_t c[PER] = {};
+    if (rebuild) {
+        load_counts4<Q>(k, l0, c);
+        // sum of the tiles before this one
+        uint32_t pre = 0;
+        {
+            uint32_t p0 = 0, p1 = 0, p2 = 0, p3 = 0;
+            uint32_t j = threadIdx.x;
+            for (; j + 3 * SCAN_THREADS < tile; j += 4 * SCAN_THREADS) {
+                p0 += k.l.tile_sums[j];
+                p1 += k.l.tile_sums[j + SCAN_THREADS];
+                p2 += k.l.tile_sums[j + 2 * SCAN_THREADS];
+                p3 += k.l.tile_sums[j + 3 * SCAN_THREADS];
+            }
+            for (; j < tile; j += SCAN_THREADS) p0 += k.l.tile_sums[j];
+            pre = p0 + p1 + p2 + p3;
         }
-        for (; j < tile; j += SCAN_THREADS) p0 += k.l.tile_sums[j];
-        pre = p0 + p1 + p2 + p3;
-    }
-    const uint32_t prefix = block_sum_256(pre, s_red);
-    // in-thread exclusive prefix, then the warp and block offsets
-    uint32_t ex[PER];
-    uint32_t tot = 0;
+        const uint32_t prefix = block_sum_256(pre, s_red);
+        // in-thread exclusive prefix, then the warp and block offsets
+        uint32_t ex[PER];
+        uint32_t tot = 0;
 #pragma unroll
-    for (int e = 0; e < PER; ++e) {
-        ex[e] = tot;
-        tot += c[e];
-    }
-    uint32_t x = tot;
+        for (int e = 0; e < PER; ++e) {
+            ex[e] = tot;
+            tot += c[e];
+        }
+        uint32_t x = tot;
 #pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-    }
-    if (lane == 31) s_warp[warp] = x;
-    __syncthreads();
-    uint32_t woff = 0;
-    for (int q = 0; q < warp; ++q) woff += s_warp[q];
-    const uint32_t base = prefix + woff + x - tot;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) s_warp[warp] = x;
+        __syncthreads();
+        uint32_t woff = 0;
+        for (int q = 0; q < warp; ++q) woff += s_warp[q];
+        const uint32_t base = prefix + woff + x - tot;
 #pragma unroll
-    for (int q = 0; q < Q; ++q) {
-        const uint32_t l = l0 + 4u * q;
-        if (l + 3u < L) {
-            *reinterpret_cast<uint4*>(k.l.cursor + l) =
-                make_uint4(base + ex[4 * q], base + ex[4 * q + 1], base + ex[4 * q + 2], base + ex[4 * q + 3]);
-        } else {
+        for (int q = 0; q < Q; ++q) {
+            const uint32_t l = l0 + 4u * q;
+            if (l + 3u < L) {
+                *reinterpret_cast<uint4*>(k.l.cursor + l) =
+                    make_uint4(base + ex[4 * q], base + ex[4 * q + 1], base + ex[4 * q + 2], base + ex[4 * q + 3]);
+            } else {
 #pragma unroll
-            for (int e = 0; e < 4; ++e)
-                if (l + e < L) k.l.cursor[l + e] = base + ex[4 * q + e];
+                for (int e = 0; e < 4; ++e)
+                    if (l + e < L) k.l.cursor[l + e] = base + ex[4 * q + e];
+            }
         }
     }
     if (with_hazard) {
@@ -942,7 +968,8 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_v(KArgs k, int with_hazar
                     const long long fix = (long long)k.l.sfix[idx];
                     float h = 0.0f, xx = 0.0f;
                     if (fix != 0) {
-                        h = psim_hazard_x(fix, c[e], k.r.k_f[rep], k.l.infectiousness[l], season, dt, &xx);
+                        const uint32_t n_l = rebuild ? c[e] : k.l.counts[l];
+                        h = psim_hazard_x(fix, n_l, k.r.k_f[rep], k.l.infectiousness[l], season, dt, &xx);
                         k.l.sfix[idx] = 0ull;
                     }
                     k.l.hazard[idx] = h;
@@ -972,6 +999,7 @@ __global__ void __launch_bounds__(256) k_scatter_draw(KArgs k, uint32_t step, in
     grad_begin(k, s_grad);
     const uint32_t N = k.a.n, L = k.l.n;
     const uint32_t t = k.clock->t0 + step;
+    const bool rebuild = csr_rebuild(k, t);
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x; base < N; base += stride) {
         const uint32_t i = base + threadIdx.x;
@@ -982,7 +1010,7 @@ __global__ void __launch_bounds__(256) k_scatter_draw(KArgs k, uint32_t step, in
         bool hz = false;
         const float h0 = (draw && ok) ? hazard_at(k, loc, &hz) : 0.0f;
         if (scatter) {
-            const uint32_t pos = take_slot(k, ok, loc);
+            const uint32_t pos = take_slot(k, ok, loc, rebuild);
             if (ok) store_slot(k, pos, i);
         }
         if (ok && draw && hz) term = draw_agent(k, i, loc, t, h0, s_grad);
@@ -1001,8 +1029,10 @@ __global__ void __launch_bounds__(256, MINB) k_step_fused(KArgs k, uint32_t step
     grad_begin(k, s_grad);
     const uint32_t N = k.a.n, L = k.l.n;
     const uint32_t t = k.clock->t0 + step;
+    const bool rebuild = csr_rebuild(k, t);
     const StepClock c = step_clock(k, step + 1);
     const uint32_t stride = gridDim.x * blockDim.x;
+    bool moved = false;
     for (uint32_t base = blockIdx.x * blockDim.x; base < N; base += stride) {
         const uint32_t i = base + threadIdx.x;
         const bool act = i < N;
@@ -1013,7 +1043,7 @@ __global__ void __launch_bounds__(256, MINB) k_step_fused(KArgs k, uint32_t step
         const bool ok = act && loc0 < L;
         bool hz = false;
         const float h0 = ok ? hazard_at(k, loc0, &hz) : 0.0f;
-        const uint32_t pos = take_slot(k, ok, loc0);
+        const uint32_t pos = take_slot(k, ok, loc0, rebuild);
         double term = 0.0;
         uint32_t loc = NONE, var = 0;
         if (ok) {
@@ -1029,8 +1059,9 @@ __global__ void __launch_bounds__(256, MINB) k_step_fused(KArgs k, uint32_t step
             if (inf > 0.0f) var = k.a.variant[i];
         }
         if (k.track_expected) add_expected(k, act, i, term);
-        count_agent(k, act, loc0, loc, inf, var);
+        moved |= count_agent(k, act, loc0, loc, inf, var);
     }
+    publish_moved(k, moved, c.t);
     grad_end(k, s_grad);
 }
 
@@ -1048,7 +1079,9 @@ __global__ void __launch_bounds__(256) k_step_ilp(KArgs k, uint32_t step) {
     const uint32_t N = k.a.n, L = k.l.n;
     const uint32_t t = k.clock->t0 + step;
     const StepClock c = step_clock(k, step + 1);
+    const bool rebuild = csr_rebuild(k, t);
     const uint32_t chunk = 256u * U;
+    bool moved = false;
     for (uint32_t base = blockIdx.x * chunk; base < N; base += gridDim.x * chunk) {
         uint32_t loc0[U], s[U], pos[U];
         float inf[U], h0[U];
@@ -1066,7 +1099,7 @@ __global__ void __launch_bounds__(256) k_step_ilp(KArgs k, uint32_t step) {
             const bool ok = loc0[u] < L;
             hz[u] = false;
             h0[u] = ok ? hazard_at(k, loc0[u], &hz[u]) : 0.0f;
-            pos[u] = ok ? atomicAdd(&k.l.cursor[loc0[u]], 1u) : NONE;
+            pos[u] = !rebuild ? SLOT_KEEP : ok ? atomicAdd(&k.l.cursor[loc0[u]], 1u) : NONE;
         }
 #pragma unroll
         for (int u = 0; u < U; ++u) {
@@ -1090,9 +1123,10 @@ __global__ void __launch_bounds__(256) k_step_ilp(KArgs k, uint32_t step) {
                 if (fi > 0.0f) var = k.a.variant[i];
             }
             if (k.track_expected) add_expected(k, act, i, term);
-            count_agent(k, act, loc0[u], loc, fi, var);
+            moved |= count_agent(k, act, loc0[u], loc, fi, var);
         }
     }
+    publish_moved(k, moved, c.t);
     grad_end(k, s_grad);
 }
 
@@ -1114,6 +1148,7 @@ __global__ void __launch_bounds__(256, 8) k_step_hot(KArgs k, uint32_t step, uin
     const uint32_t dt = k.p.time_step;
     const uint32_t minutes = (step + 1) * dt;
     const bool curfew_now = k.p.enable_curfew && k.p.curfew_begin == minutes / dt;
+    const bool rebuild = csr_rebuild(k, k.clock->t0 + step);
     const uint32_t stride = gridDim.x * blockDim.x;
     uint32_t* seg = k.a.worklist + (size_t)blockIdx.x * cap;
     const int lane = threadIdx.x & 31;
@@ -1137,7 +1172,7 @@ __global__ void __launch_bounds__(256, 8) k_step_hot(KArgs k, uint32_t step, uin
         const bool ok = act && loc0 < L;
         bool hz = false;
         if (ok) hazard_at(k, loc0, &hz);
-        const uint32_t pos = take_slot(k, ok, loc0);
+        const uint32_t pos = take_slot(k, ok, loc0, rebuild);
         if (ok) store_slot(k, pos, i);
         const bool cold = act && (curfew_now || s == 0 || hz || !ok);
         const bool hot = act && !cold;
@@ -1167,6 +1202,7 @@ __global__ void __launch_bounds__(256, 8) k_step_hot_ilp(KArgs k, uint32_t step,
     const uint32_t dt = k.p.time_step;
     const uint32_t minutes = (step + 1) * dt;
     const bool curfew_now = k.p.enable_curfew && k.p.curfew_begin == minutes / dt;
+    const bool rebuild = csr_rebuild(k, k.clock->t0 + step);
     uint32_t* seg = k.a.worklist + (size_t)blockIdx.x * cap;
     const int lane = threadIdx.x & 31;
     for (uint32_t base = blockIdx.x * (256u * U); base < N; base += gridDim.x * (256u * U)) {
@@ -1186,7 +1222,7 @@ __global__ void __launch_bounds__(256, 8) k_step_hot_ilp(KArgs k, uint32_t step,
         for (int u = 0; u < U; ++u) {
             hz[u] = false;
             if (loc[u] < L) hazard_at(k, loc[u], &hz[u]);
-            pos[u] = take_slot(k, loc[u] < L, loc[u]);
+            pos[u] = take_slot(k, loc[u] < L, loc[u], rebuild);
         }
 #pragma unroll
         for (int u = 0; u < U; ++u) {
@@ -1209,67 +1245,121 @@ __global__ void __launch_bounds__(256, 8) k_step_hot_ilp(KArgs k, uint32_t step,
     if (threadIdx.x == 0) k.a.seg_count[blockIdx.x] = s_cnt;
 }
 
-__device__ __forceinline__ void prefetch_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
-
-// The per-agent fields that the draw and the movement decision read, behind
-// branches that keep the compiler from issuing them together: prefetched into
-// L1 at once, so that the decision's chain of dependent loads finds them there.
-__device__ __forceinline__ void prefetch_agent(const KArgs& k, uint32_t i) {
-    prefetch_l1(k.a.rep + i);
-    prefetch_l1(k.a.state + i);
-    prefetch_l1(k.a.type + i);
-    prefetch_l1(k.a.band + i);
-    prefetch_l1(k.a.loc_offset + i);
-    prefetch_l1(k.a.susceptible + i);
-    prefetch_l1(k.a.st_quarantined_until + i);
-    prefetch_l1(k.a.st_hospitalized_ts + i);
-    prefetch_l1(k.a.st_hospitalized_until + i);
-    prefetch_l1(k.a.diagnosed + i);
-    prefetch_l1(k.a.quarantined + i);
-    prefetch_l1(k.a.no_work + i);
-    prefetch_l1(k.a.stayed_home + i);
-    if (k.p.quarantine_policy > 0) prefetch_l1(k.a.st_diagnosed_ts + i);
+// The cold agents of one step, one per thread: queued agent i (its location
+// loc0 and countdown s at the hot kernel) draws at loc0, then moves; the
+// histogram and the sums follow.
+__device__ __forceinline__ bool cold_agent(const KArgs& k, bool act, uint32_t i, uint32_t t, const StepClock& c,
+                                           double* s_grad) {
+    const uint32_t L = k.l.n;
+    double term = 0.0;
+    uint32_t loc = NONE, loc0 = NONE, var = 0;
+    float inf = 0.0f;
+    if (act) {
+        loc0 = k.a.location[i];
+        const uint32_t s = k.a.steps_until_move[i];
+        inf = k.a.infectious[i];
+        if (loc0 < L) {
+            bool hz = false;
+            const float h0 = hazard_at(k, loc0, &hz);
+            if (hz) {
+                term = draw_agent(k, i, loc0, t, h0, s_grad);
+                inf = k.a.infectious[i];
+            }
+        }
+        move_agent(k, i, c, s);
+        loc = (c.curfew_now || s == 0) ? k.a.location[i] : loc0;
+        if (inf > 0.0f) var = k.a.variant[i];
+    }
+    if (k.track_expected) add_expected(k, act, i, term);
+    return count_agent(k, act, loc0, loc, inf, var);
 }
 
-template <bool PF>
+// The cold half, one segment per block: block b runs the agents that hot
+// block b queued (and segments b + gridDim.x, ...).
 __global__ void __launch_bounds__(256) k_step_cold(KArgs k, uint32_t step, uint32_t cap, uint32_t n_seg) {
     __shared__ double s_grad[GRAD_N];
     grad_begin(k, s_grad);
-    const uint32_t L = k.l.n;
     const uint32_t t = k.clock->t0 + step;
     const StepClock c = step_clock(k, step + 1);
+    bool moved = false;
     for (uint32_t sg = blockIdx.x; sg < n_seg; sg += gridDim.x) {
-    const uint32_t n = k.a.seg_count[sg];
-    const uint32_t* seg = k.a.worklist + (size_t)sg * cap;
-    const uint32_t trips = (n + blockDim.x - 1) / blockDim.x;  // uniform per block
-    for (uint32_t it = 0; it < trips; ++it) {
-        const uint32_t j = it * blockDim.x + threadIdx.x;
-        const bool act = j < n;
-        const uint32_t i = act ? seg[j] : 0u;
-        double term = 0.0;
-        uint32_t loc = NONE, loc0 = NONE, var = 0;
-        float inf = 0.0f;
-        if (PF && act) prefetch_agent(k, i);
-        if (act) {
-            loc0 = k.a.location[i];
-            const uint32_t s = k.a.steps_until_move[i];
-            inf = k.a.infectious[i];
-            if (loc0 < L) {
-                bool hz = false;
-                const float h0 = hazard_at(k, loc0, &hz);
-                if (hz) {
-                    term = draw_agent(k, i, loc0, t, h0, s_grad);
-                    inf = k.a.infectious[i];
-                }
-            }
-            move_agent(k, i, c, s);
-            loc = (c.curfew_now || s == 0) ? k.a.location[i] : loc0;
-            if (inf > 0.0f) var = k.a.variant[i];
+        const uint32_t n = k.a.seg_count[sg];
+        const uint32_t* seg = k.a.worklist + (size_t)sg * cap;
+        const uint32_t trips = (n + blockDim.x - 1) / blockDim.x;  // uniform per block
+        for (uint32_t it = 0; it < trips; ++it) {
+            const uint32_t j = it * blockDim.x + threadIdx.x;
+            const bool act = j < n;
+            moved |= cold_agent(k, act, act ? seg[j] : 0u, t, c, s_grad);
         }
-        if (k.track_expected) add_expected(k, act, i, term);
-        count_agent(k, act, loc0, loc, inf, var);
     }
+    publish_moved(k, moved, c.t);
+    grad_end(k, s_grad);
+}
+
+// The cold half with the queued agents of all segments spread evenly over the
+// grid: the movers of a step cluster in a few hot blocks (agents of one type
+// leave for the same event together), and one block per segment then makes
+// several trips through the movement decision's long chain of dependent
+// loads while the other SMs idle.  Every block scans the segment counts into
+// shared memory (dynamic, n_seg + 1 words); work index w lies in segment
+// sg with pre[sg] <= w < pre[sg + 1].
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) k_step_cold_spread(KArgs k, uint32_t step, uint32_t cap, uint32_t n_seg) {
+    extern __shared__ uint32_t s_pre[];  // [n_seg + 1]
+    __shared__ double s_grad[GRAD_N];
+    __shared__ uint32_t s_warp[8];
+    grad_begin(k, s_grad);
+    const uint32_t t = k.clock->t0 + step;
+    const StepClock c = step_clock(k, step + 1);
+    // exclusive prefix of seg_count: each thread sums a run of consecutive
+    // segments, then a block scan of the run totals
+    const uint32_t per = (n_seg + blockDim.x - 1) / blockDim.x;
+    const uint32_t b0 = threadIdx.x * per;
+    uint32_t run = 0;
+    for (uint32_t q = 0; q < per; ++q)
+        if (b0 + q < n_seg) run += k.a.seg_count[b0 + q];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = run;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
     }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    uint32_t woff = 0;
+    for (int q = 0; q < warp; ++q) woff += s_warp[q];
+    uint32_t acc = woff + x - run;
+    for (uint32_t q = 0; q < per; ++q)
+        if (b0 + q < n_seg) {
+            s_pre[b0 + q] = acc;
+            acc += k.a.seg_count[b0 + q];
+        }
+    if (threadIdx.x == blockDim.x - 1) s_pre[n_seg] = woff + x;
+    __syncthreads();
+    const uint32_t total = s_pre[n_seg];
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t trips = (total + stride - 1) / stride;  // uniform over the grid
+    bool moved = false;
+    for (uint32_t it = 0; it < trips; ++it) {
+        const uint32_t w = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        const bool act = w < total;
+        uint32_t i = 0u;
+        if (act) {
+            // the last segment whose start is <= w
+            uint32_t lo = 0, hi = n_seg - 1;
+            while (lo < hi) {
+                const uint32_t mid = (lo + hi + 1) >> 1;
+                if (s_pre[mid] <= w)
+                    lo = mid;
+                else
+                    hi = mid - 1;
+            }
+            i = k.a.worklist[(size_t)lo * cap + (w - s_pre[lo])];
+        }
+        moved |= cold_agent(k, act, i, t, c, s_grad);
+    }
+    publish_moved(k, moved, c.t);
     grad_end(k, s_grad);
 }
 
@@ -1895,17 +1985,20 @@ void launch_movement(const KArgs& k, uint32_t step, cudaStream_t s) {
 // part: -1 both kernels of the step; 0 the first (the fused kernel, or the hot
 // kernel of variant 3); 1 the second (the cold kernel of variant 3, else nothing)
 void launch_step_fused(const KArgs& k, uint32_t step, cudaStream_t s, int part) {
-    static unsigned g[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-    const uint32_t v = k.tune.variant < 8 ? k.tune.variant : 0;
+    static unsigned g[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const uint32_t v = k.tune.variant < 10 ? k.tune.variant : 0;
     if (!g[0]) {
         g[0] = wave_grid(k_step_fused<4>, 1u << 30);
         g[1] = wave_grid(k_step_fused<6>, 1u << 30);
         g[2] = wave_grid(k_step_fused<8>, 1u << 30);
         g[3] = wave_grid(k_step_hot, 1u << 30);
-        g[4] = wave_grid(k_step_cold<false>, 1u << 30);
+        g[4] = wave_grid(k_step_cold, 1u << 30);
         g[5] = wave_grid(k_step_ilp<2>, 1u << 30);
         g[6] = wave_grid(k_step_ilp<4>, 1u << 30);
         g[7] = wave_grid(k_step_hot_ilp<2>, 1u << 30);
+        g[8] = wave_grid(k_step_cold_spread<4>, 1u << 30);
+        g[9] = wave_grid(k_step_cold_spread<6>, 1u << 30);
+        g[10] = wave_grid(k_step_cold_spread<8>, 1u << 30);
     }
     if (v == 6) {
         // hot/cold with two agents per hot thread in flight
@@ -1915,10 +2008,10 @@ void launch_step_fused(const KArgs& k, uint32_t step, cudaStream_t s, int part) 
         grid = std::min(std::min(grid, grid_for((k.a.n + 1) / 2, 1 << 20)), (unsigned)WORK_MAX_BLOCKS / 2);
         const uint32_t cap = (uint32_t)((((size_t)k.a.n + (size_t)grid * tile - 1) / ((size_t)grid * tile)) * tile);
         if (part != 1) k_step_hot_ilp<2><<<grid, 256, 0, s>>>(k, step, cap);
-        if (part != 0) k_step_cold<false><<<std::min(grid, g[4]), 256, 0, s>>>(k, step, cap, grid);
+        if (part != 0) k_step_cold<<<std::min(grid, g[4]), 256, 0, s>>>(k, step, cap, grid);
         return;
     }
-    if (v == 3 || v == 7) {
+    if (v == 3 || v >= 7) {
         // one work-list segment per hot block, as many as the block visits
         const unsigned grid = std::min(agent_grid(k, g[3]), (unsigned)WORK_MAX_BLOCKS);
         const uint32_t cap = (uint32_t)((((size_t)k.a.n + (size_t)grid * 256 - 1) / ((size_t)grid * 256)) * 256);
@@ -1926,10 +2019,15 @@ void launch_step_fused(const KArgs& k, uint32_t step, cudaStream_t s, int part) 
         // the cold agents are a few percent: at most one wave of cold blocks,
         // each taking segments in turn
         if (part != 0) {
+            const size_t sh = (grid + 1) * sizeof(uint32_t);
             if (v == 7)
-                k_step_cold<true><<<std::min(grid, g[4]), 256, 0, s>>>(k, step, cap, grid);
+                k_step_cold_spread<4><<<g[8], 256, sh, s>>>(k, step, cap, grid);
+            else if (v == 8)
+                k_step_cold_spread<6><<<g[9], 256, sh, s>>>(k, step, cap, grid);
+            else if (v == 9)
+                k_step_cold_spread<8><<<g[10], 256, sh, s>>>(k, step, cap, grid);
             else
-                k_step_cold<false><<<std::min(grid, g[4]), 256, 0, s>>>(k, step, cap, grid);
+                k_step_cold<<<std::min(grid, g[4]), 256, 0, s>>>(k, step, cap, grid);
         }
         return;
     }
@@ -1953,37 +2051,39 @@ void launch_step_fused(const KArgs& k, uint32_t step, cudaStream_t s, int part) 
         k_step_fused<8><<<grid, 256, 0, s>>>(k, step);
 }
 int step_fused_kernels(const KArgs& k) {
-    return k.tune.variant == 3 || k.tune.variant == 6 || k.tune.variant == 7 ? 2 : 1;
+    return k.tune.variant == 3 || (k.tune.variant >= 6 && k.tune.variant <= 9) ? 2 : 1;
 }
 void launch_count(const KArgs& k, cudaStream_t s) { k_count<<<grid_for(k.a.n, 8), 256, 0, s>>>(k); }
 // the scan of the histogram with 256 x tune.scan_items locations per tile:
 // single pass with decoupled look-back (tune.scan_mode 0) or tile sums, then
 // the scan (scan_mode 1)
 template <int ITEMS>
-static void launch_scan_items(const KArgs& k, int with_hazard, int merge_q, cudaStream_t s) {
+static void launch_scan_items(const KArgs& k, uint32_t step, int with_hazard, int merge_q, cudaStream_t s) {
     unsigned tiles = (k.l.n + SCAN_THREADS * ITEMS - 1) / (SCAN_THREADS * ITEMS);
     if (!tiles) tiles = 1;
     if (k.tune.scan_mode == 2 && (ITEMS == 4 || ITEMS == 8)) {
         // thread-contiguous: ITEMS / 4 vectors of 4 locations per thread
         constexpr int Q = ITEMS >= 8 ? 2 : 1;
-        k_tile_sums_v<Q><<<tiles, SCAN_THREADS, 0, s>>>(k);
-        k_scan_v<Q><<<tiles, SCAN_THREADS, 0, s>>>(k, with_hazard, merge_q);
+        k_tile_sums_v<Q><<<tiles, SCAN_THREADS, 0, s>>>(k, step);
+        k_scan_v<Q><<<tiles, SCAN_THREADS, 0, s>>>(k, step, with_hazard, merge_q);
         return;
     }
     if (k.tune.scan_mode == 0) {
-        k_scan<ITEMS, true><<<tiles, SCAN_THREADS, 0, s>>>(k, with_hazard, merge_q);
+        k_scan<ITEMS, true><<<tiles, SCAN_THREADS, 0, s>>>(k, step, with_hazard, merge_q);
     } else {
-        k_tile_sums<ITEMS><<<tiles, SCAN_THREADS, 0, s>>>(k);
-        k_scan<ITEMS, false><<<tiles, SCAN_THREADS, 0, s>>>(k, with_hazard, merge_q);
+        k_tile_sums<ITEMS><<<tiles, SCAN_THREADS, 0, s>>>(k, step);
+        k_scan<ITEMS, false><<<tiles, SCAN_THREADS, 0, s>>>(k, step, with_hazard, merge_q);
     }
 }
-void launch_scan(const KArgs& k, uint32_t, int with_hazard, int merge_q, cudaStream_t s) {
+// step: the step in the day whose CSR the scan prepares (rebuilt only when
+// agents took new locations for it, see csr_decide)
+void launch_scan(const KArgs& k, uint32_t step, int with_hazard, int merge_q, cudaStream_t s) {
     if (k.tune.scan_items == 2)
-        launch_scan_items<2>(k, with_hazard, merge_q, s);
+        launch_scan_items<2>(k, step, with_hazard, merge_q, s);
     else if (k.tune.scan_items == 4)
-        launch_scan_items<4>(k, with_hazard, merge_q, s);
+        launch_scan_items<4>(k, step, with_hazard, merge_q, s);
     else
-        launch_scan_items<8>(k, with_hazard, merge_q, s);
+        launch_scan_items<8>(k, step, with_hazard, merge_q, s);
 }
 int scan_kernels(const KArgs& k) { return k.tune.scan_mode == 0 ? 1 : 2; }
 void launch_scatter_draw(const KArgs& k, uint32_t step, int scatter, int draw, cudaStream_t s) {

@@ -170,12 +170,23 @@ def test_bounded_wait_reports_error_and_context_survives(gpu_lib):
                                     dict(agg_count=0, agg_slot=1, blocks_per_sm=0, variant=6, scan_items=2,
                                          scan_mode=1),
                                     dict(agg_count=0, agg_slot=0, blocks_per_sm=4, variant=7, scan_items=4,
-                                         scan_mode=2)])
+                                         scan_mode=2),
+                                    dict(agg_count=0, agg_slot=1, blocks_per_sm=8, variant=8, scan_items=8,
+                                         scan_mode=2),
+                                    dict(agg_count=0, agg_slot=0, blocks_per_sm=0, variant=9, scan_items=4,
+                                         scan_mode=1)])
 def test_tuning_choices_do_not_change_results(gpu_lib, tuning):
+    """Every tuning against the oracle over three days: statistics, state and
+    the agent list at the end of each day.  Most steps of a day move nobody
+    and keep the agent list of the step before (incremental CSR); the
+    canonical read also reorders the kept segments in place."""
     s_cpu, s_gpu, o, g = _pair(n=12000, locs=3000, initial_infected_frac=0.02)
     g.set_tuning(**tuning)
     for d in range(3):
         assert stats_rows(o.run_day(d)) == stats_rows(g.run_day(d)), (d, tuning)
+        off_o, ag_o = o.csr()
+        off_g, ag_g = g.csr(canonical=True)
+        assert np.array_equal(off_o, off_g) and np.array_equal(ag_o, ag_g), (d, tuning)
     g.download()
     assert diff_state(s_cpu, s_gpu) == []
 
@@ -220,3 +231,23 @@ def test_uneven_tiny_replicas_match_single_runs(gpu_lib):
         rows_b = stats_rows(gb.run_day(d))
         for r, gs in enumerate(singles):
             assert stats_rows(gs.run_day(d))[0] == rows_b[r], (d, r)
+
+
+def test_restored_day_rebuilds_the_agent_list(gpu_lib):
+    """A day replayed from a checkpoint (as the autotuner and the adjoint do)
+    gives the oracle's state, statistics and agent list: the restore forces
+    the next step to rebuild the CSR, which the checkpoint does not hold."""
+    s_cpu, s_gpu, o, g = _pair(n=12000, locs=3000, initial_infected_frac=0.02)
+    for d in range(2):
+        assert stats_rows(o.run_day(d)) == stats_rows(g.run_day(d)), d
+    g.checkpoint_save(7)
+    g.run_day(2)
+    g.run_day(3)
+    g.checkpoint_restore(7)
+    assert stats_rows(o.run_day(2)) == stats_rows(g.run_day(2))
+    g.download()
+    assert diff_state(s_cpu, s_gpu) == []
+    off_o, ag_o = o.csr()
+    off_g, ag_g = g.csr(canonical=True)
+    assert np.array_equal(off_o, off_g) and np.array_equal(ag_o, ag_g)
+    g.checkpoint_drop(7)
