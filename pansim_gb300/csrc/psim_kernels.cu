@@ -39,9 +39,9 @@ __device__ __forceinline__ uint32_t loc_type(const KArgs& k, uint32_t l) { retur
 // RealMovementOps::findActualLocationForType, movementPolicies.h:69-122.
 // f0, f1, f2: the types resolved by first match (home, school, work except in
 // the plan helpers, movementPolicies.h:1073-1080, :1144, :1209-1214).
-__device__ uint32_t find_location3(const KArgs& k, uint32_t i, uint32_t lt, int retry, psim_stream* rng, uint32_t f0,
-                                   uint32_t f1, uint32_t f2) {
-    const uint32_t b = k.a.loc_offset[i], e = k.a.loc_offset[i + 1];
+// [b, e): the agent's entries in the per-agent location list.
+__device__ uint32_t find_location_range(const KArgs& k, uint32_t b, uint32_t e, uint32_t lt, int retry,
+                                        psim_stream* rng, uint32_t f0, uint32_t f1, uint32_t f2) {
     if (lt == f0 || lt == f1 || lt == f2) {
         for (uint32_t j = b; j < e; ++j)
             if (lt == k.a.poss_type[j]) return k.a.poss_loc[j];
@@ -75,6 +75,11 @@ __device__ uint32_t find_location3(const KArgs& k, uint32_t i, uint32_t lt, int 
         }
     }
     return NONE;
+}
+
+__device__ __forceinline__ uint32_t find_location3(const KArgs& k, uint32_t i, uint32_t lt, int retry, psim_stream* rng,
+                                                   uint32_t f0, uint32_t f1, uint32_t f2) {
+    return find_location_range(k, k.a.loc_offset[i], k.a.loc_offset[i + 1], lt, retry, rng, f0, f1, f2);
 }
 
 __device__ __forceinline__ uint32_t find_location(const KArgs& k, uint32_t i, uint32_t lt, int retry, psim_stream* rng) {
@@ -143,37 +148,53 @@ __device__ void move_decide(const KArgs& k, uint32_t i, uint32_t t, uint32_t min
     const psim_params& p = k.p;
     const uint32_t dt = p.time_step;
     uint32_t* sum_ptr = &k.a.steps_until_move[i];
-    if (k.a.st_quarantined_until[i] <= t) k.a.quarantined[i] = 0;
+    // The agent's fields that the decision reads, loaded together: read where
+    // they are needed, behind branches and stores, each costs a round trip
+    // of its own.  None of them is written before that point.
+    const uint32_t q_until = k.a.st_quarantined_until[i];
+    const uint8_t state_i = (uint8_t)k.a.state[i];
+    const uint32_t h_ts = k.a.st_hospitalized_ts[i];
+    const uint32_t h_until = k.a.st_hospitalized_until[i];
+    const uint32_t lb = k.a.loc_offset[i], le = k.a.loc_offset[i + 1];
+    const uint32_t agent_type = k.a.type[i];
+    const uint32_t loc_now = k.a.location[i];
+    const uint8_t diag = k.a.diagnosed[i];
+    const uint8_t no_work = k.a.no_work[i];
+    const uint8_t age = k.a.age[i];
+    auto fl = [&](uint32_t lt, int retry) {
+        return find_location_range(k, lb, le, lt, retry, rng, p.home_type, p.school_type, p.work_type);
+    };
+    if (q_until <= t) k.a.quarantined[i] = 0;
 
-    uint32_t wb = wb_of(k, i);
+    uint32_t wb = k.m.state_wb[state_i];
     if (wb == WB_D) {
         *sum_ptr = NONE;
         k.a.location[i] = k.r.cemetery[k.a.rep[i]];
         return;
     }
-    uint32_t agent_home = find_location(k, i, p.home_type, 0, rng);
+    uint32_t agent_home = fl(p.home_type, 0);
 
-    if (k.a.st_hospitalized_ts[i] <= t && k.a.st_hospitalized_until[i] > t && wb != WB_S && wb != WB_D) {
-        uint32_t x = k.a.st_hospitalized_until[i] - t - 1;
+    if (h_ts <= t && h_until > t && wb != WB_S && wb != WB_D) {
+        uint32_t x = h_until - t - 1;
         *sum_ptr = x < sum ? x : sum;
-        k.a.location[i] = find_location(k, i, p.hospital_type, 0, rng);
-        if (!k.a.diagnosed[i] && k.a.infectious[i] != 0.0f) diagnose_and_quarantine(k, i, t, sum, rng);
+        k.a.location[i] = fl(p.hospital_type, 0);
+        if (!diag && k.a.infectious[i] != 0.0f) diagnose_and_quarantine(k, i, t, sum, rng);
         return;
     }
     if (wb == WB_S) {
         *sum_ptr = sum;
-        k.a.location[i] = find_location(k, i, p.hospital_type, 0, rng);
-        if (!k.a.diagnosed[i] && k.a.infectious[i] != 0.0f) diagnose_and_quarantine(k, i, t, sum, rng);
+        k.a.location[i] = fl(p.hospital_type, 0);
+        if (!diag && k.a.infectious[i] != 0.0f) diagnose_and_quarantine(k, i, t, sum, rng);
         return;
     }
     {
-        uint32_t loc = k.a.location[i];
+        uint32_t loc = loc_now;
         if (p.quarantine_policy > 1 && t < loc_qu(k, loc) && is_quarantine_type(k, loc)) {
             if (k.a.quarantined[i] == 0) quarantine_agent(k, i, t, loc_qu(k, loc), rng);
             if (k.a.quarantined[i]) {
                 uint32_t x = loc_qu(k, k.a.location[i]) - t - 1;
                 *sum_ptr = x < sum ? x : sum;
-                uint32_t home_location = find_location(k, i, p.home_type, 0, rng);
+                uint32_t home_location = fl(p.home_type, 0);
                 if (home_location != k.a.location[i]) k.a.location[i] = home_location;
                 stayed_home_check(k, i, agent_home);
                 return;
@@ -181,13 +202,13 @@ __device__ void move_decide(const KArgs& k, uint32_t i, uint32_t t, uint32_t min
         }
     }
     if ((p.quarantine_policy > 0 &&
-         (k.a.diagnosed[i] ||
+         (diag ||
           (k.a.st_diagnosed_ts[i] > 0 && (t - k.a.st_diagnosed_ts[i]) < p.quarantine_length * 24u * 60u / dt))) ||
         (p.quarantine_policy > 0 && k.a.quarantined[i])) {
         if (p.quarantine_policy > 0 && !k.a.quarantined[i])
             quarantine_agent(k, i, t, t + p.quarantine_length * 24u * 60u / dt, rng);
         if (k.a.quarantined[i]) {
-            k.a.location[i] = find_location(k, i, p.home_type, 0, rng);
+            k.a.location[i] = fl(p.home_type, 0);
             *sum_ptr = sum;
             stayed_home_check(k, i, agent_home);
             return;
@@ -195,7 +216,6 @@ __device__ void move_decide(const KArgs& k, uint32_t i, uint32_t t, uint32_t min
     }
 
     // schedule window (AgentTypeList::getOffsetIndex, agentType.cpp:13-15)
-    const uint32_t agent_type = k.a.type[i];
     const uint32_t off_idx = 7u * wb + day + agent_type * 28u;
     const uint32_t ev_b = k.m.event_offset[off_idx], ev_e = k.m.event_offset[off_idx + 1];
     int act_b = -1, act_e = -1;
@@ -212,7 +232,7 @@ __device__ void move_decide(const KArgs& k, uint32_t i, uint32_t t, uint32_t min
     uint32_t new_type = NONE;
     if (act_b == -1 && act_e == -1) {  // Case 1
         new_type = wb == WB_S ? p.hospital_type : p.home_type;
-        k.a.location[i] = find_location(k, i, new_type, 0, rng);
+        k.a.location[i] = fl(new_type, 0);
         *sum_ptr = sum;
     }
     if (act_b != -1) {  // Case 2 and 4
@@ -234,13 +254,13 @@ __device__ void move_decide(const KArgs& k, uint32_t i, uint32_t t, uint32_t min
             new_type = k.m.ev_loc_type[act_b + idx];
             dur = k.m.ev_duration[act_b + idx];
         }
-        if (k.a.no_work[i] != 0 && new_type == p.work_type) {
+        if (no_work != 0 && new_type == p.work_type) {
             new_type = p.home_type;
             num_pot = 1;
             if (k.a.quarantined[i] == 0) k.a.st_days_in_quarantine[i]++;
         }
-        uint32_t new_loc = find_location(k, i, new_type, num_pot == 1, rng);
-        bool too_old = (new_type == p.school_type || new_type == p.classroom_type) && k.a.age[i] >= p.school_age_restriction;
+        uint32_t new_loc = fl(new_type, num_pot == 1);
+        bool too_old = (new_type == p.school_type || new_type == p.classroom_type) && age >= p.school_age_restriction;
         if (too_old || ((loc_open(k, new_loc) == 0 || loc_closed_until(k, new_loc) > t) && new_type != p.work_type) ||
             (p.lockdown_nonvacc && k.a.st_immunization_ts[i] == 0)) {
             if (num_pot > 1) {
@@ -255,17 +275,17 @@ __device__ void move_decide(const KArgs& k, uint32_t i, uint32_t t, uint32_t min
                 if (idx == num_pot) idx--;
                 new_type = k.m.ev_loc_type[act_b + idx];
                 dur = k.m.ev_duration[act_b + idx];
-                new_loc = find_location(k, i, new_type, 0, rng);
+                new_loc = fl(new_type, 0);
                 if (too_old ||
                     ((loc_open(k, new_loc) == 0 || loc_closed_until(k, new_loc) > t) && new_type != p.work_type) ||
                     (p.lockdown_nonvacc && k.a.st_immunization_ts[i] == 0))
-                    new_loc = find_location(k, i, p.home_type, 0, rng);
+                    new_loc = fl(p.home_type, 0);
             } else {
-                new_loc = find_location(k, i, p.home_type, 0, rng);
+                new_loc = fl(p.home_type, 0);
             }
         } else if (new_type == p.school_type) {
-            uint32_t my_class = find_location(k, i, p.classroom_type, 0, rng);
-            if (my_class != NONE && loc_closed_until(k, my_class) > t) new_loc = find_location(k, i, p.home_type, 0, rng);
+            uint32_t my_class = fl(p.classroom_type, 0);
+            if (my_class != NONE && loc_closed_until(k, my_class) > t) new_loc = fl(p.home_type, 0);
         }
         k.a.location[i] = new_loc;
         if (dur / 60u > 24u) {
@@ -299,10 +319,10 @@ __device__ void move_decide(const KArgs& k, uint32_t i, uint32_t t, uint32_t min
         if (left < 30u / dt) {
         } else if (left < 60u / dt) {
             new_type = p.public_type;
-            k.a.location[i] = find_location(k, i, p.public_type, 0, rng);
+            k.a.location[i] = fl(p.public_type, 0);
         } else {
             new_type = p.home_type;
-            k.a.location[i] = find_location(k, i, p.home_type, 0, rng);
+            k.a.location[i] = fl(p.home_type, 0);
         }
     }
     {
@@ -312,7 +332,7 @@ __device__ void move_decide(const KArgs& k, uint32_t i, uint32_t t, uint32_t min
             if (k.a.quarantined[i]) {
                 uint32_t x = loc_qu(k, k.a.location[i]) - t - 1;
                 *sum_ptr = x < sum ? x : sum;
-                uint32_t home_location = find_location(k, i, p.home_type, 0, rng);
+                uint32_t home_location = fl(p.home_type, 0);
                 if (home_location != k.a.location[i]) k.a.location[i] = home_location;
                 stayed_home_check(k, i, agent_home);
                 return;
@@ -320,7 +340,7 @@ __device__ void move_decide(const KArgs& k, uint32_t i, uint32_t t, uint32_t min
         }
     }
     if (new_type == p.hospital_type || (new_type == p.doctor_type && psim_u01(rng) * 1.0 < 0.7)) {
-        if (!k.a.diagnosed[i] && k.a.infectious[i] != 0.0f) diagnose_and_quarantine(k, i, t, sum, rng);
+        if (!diag && k.a.infectious[i] != 0.0f) diagnose_and_quarantine(k, i, t, sum, rng);
     }
     stayed_home_check(k, i, agent_home);
     *sum_ptr = *sum_ptr - 1u;
