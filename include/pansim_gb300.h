@@ -144,7 +144,7 @@ typedef struct psim_agents {
 
 /* Locations (include/locationList.h:46-67) [n_locations], cemetery last. */
 typedef struct psim_locations {
-    uint32_t n;
+    uint32_t n;                       /* at most 2^30 - 2 */
     uint32_t n_schools;
     uint32_t n_classrooms;
     uint32_t pad0;

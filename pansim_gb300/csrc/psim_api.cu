@@ -345,6 +345,8 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     int rc = validate(c, m, a, l);
     if (rc) return bail(rc);
     if (p->time_step == 0 || 1440 % p->time_step) return bail(fail(c, PSIM_ERR_ARG, "time_step must divide 1440"));
+    // the hot/cold step hands a queued agent's location on in 30 bits
+    if (l->n >= WORK_LOC_MASK) return bail(fail(c, PSIM_ERR_ARG, "more than 2^30 - 2 locations"));
     c->N = a->n;
     c->L = l->n;
     c->V = m->n_variants;
@@ -466,7 +468,8 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     AL(st_quarantined_ts, N) AL(st_quarantined_until, N) AL(st_days_in_quarantine, N) AL(st_hospitalized_ts, N)
     AL(st_hospitalized_until, N) AL(st_immunization_ts, N) AL(st_recovered_ts, N) AL(st_variant_mask, N)
     AL(st_immunization_count, N) AL(st_infected_count, N) AL(st_worst_state, N) AL(hcw, N) AL(rank, N)
-    AL(worklist, (size_t)N + (size_t)WORK_MAX_BLOCKS * 256) AL(seg_count, WORK_MAX_BLOCKS)
+    AL(worklist, (size_t)N + (size_t)WORK_MAX_BLOCKS * 256) AL(worklist_loc, (size_t)N + (size_t)WORK_MAX_BLOCKS * 256)
+    AL(seg_count, WORK_MAX_BLOCKS)
     AL(imm_round, N) AL(scaling_v, (size_t)N * V)
 #undef AL
     // locations

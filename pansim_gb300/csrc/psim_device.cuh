@@ -94,6 +94,8 @@ struct DevAgents {
     uint32_t* rank;               // scratch of the canonical CSR ordering
     uint32_t* worklist;           // agents queued for the cold half of a step (hot/cold variant),
                                   // one segment per hot block
+    uint32_t* worklist_loc;       // beside each: its location (low 30 bits, WORK_LOC_MASK for an
+                                  // invalid one) | WORK_HZ | WORK_MOVE
     uint32_t* seg_count;          // queued agents per segment
 };
 
@@ -262,6 +264,12 @@ void launch_step_fused(const KArgs& k, uint32_t step_in_day, cudaStream_t s, int
 int scan_kernels(const KArgs& k);
 // work-list segments of the hot/cold step (blocks of the hot kernel at most)
 constexpr uint32_t WORK_MAX_BLOCKS = 152u * 64u;
+// the second word of a work-list entry: the agent draws (an infectious
+// agent is at its location), the agent moves at the next step (countdown at
+// zero or curfew; hazard-only agents have counted down in the hot kernel)
+constexpr uint32_t WORK_LOC_MASK = 0x3FFFFFFFu;
+constexpr uint32_t WORK_HZ = 0x80000000u;
+constexpr uint32_t WORK_MOVE = 0x40000000u;
 
 // closure rules
 struct ClosureTypes {

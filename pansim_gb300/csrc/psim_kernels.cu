@@ -1171,6 +1171,7 @@ __global__ void __launch_bounds__(256, 8) k_step_hot(KArgs k, uint32_t step, uin
     const bool rebuild = csr_rebuild(k, k.clock->t0 + step);
     const uint32_t stride = gridDim.x * blockDim.x;
     uint32_t* seg = k.a.worklist + (size_t)blockIdx.x * cap;
+    uint32_t* segl = k.a.worklist_loc + (size_t)blockIdx.x * cap;
     const int lane = threadIdx.x & 31;
     // the next iteration's agent columns are loaded one iteration ahead
     uint32_t base = blockIdx.x * blockDim.x;
@@ -1194,15 +1195,22 @@ __global__ void __launch_bounds__(256, 8) k_step_hot(KArgs k, uint32_t step, uin
         if (ok) hazard_at(k, loc0, &hz);
         const uint32_t pos = take_slot(k, ok, loc0, rebuild);
         if (ok) store_slot(k, pos, i);
-        const bool cold = act && (curfew_now || s == 0 || hz || !ok);
-        const bool hot = act && !cold;
-        if (hot) k.a.steps_until_move[i] = s - 1;
+        // movers (countdown at zero, curfew) go to the cold kernel whole;
+        // the others count down here and go there only to draw (or to
+        // report an invalid location)
+        const bool mover = act && (curfew_now || s == 0);
+        const bool cold = mover || (act && (hz || !ok));
+        if (act && !mover) k.a.steps_until_move[i] = s - 1;
         const unsigned cm = __ballot_sync(0xffffffffu, cold);
         if (cm) {
             uint32_t basew = 0;
             if (lane == __ffs(cm) - 1) basew = atomicAdd(&s_cnt, (uint32_t)__popc(cm));
             basew = __shfl_sync(0xffffffffu, basew, __ffs(cm) - 1);
-            if (cold) seg[basew + __popc(cm & lanemask_lt())] = i;
+            if (cold) {
+                const uint32_t q = basew + __popc(cm & lanemask_lt());
+                seg[q] = i;
+                segl[q] = (ok ? loc0 : WORK_LOC_MASK) | (hz ? WORK_HZ : 0u) | (mover ? WORK_MOVE : 0u);
+            }
         }
     }
     __syncthreads();
@@ -1224,6 +1232,7 @@ __global__ void __launch_bounds__(256, 8) k_step_hot_ilp(KArgs k, uint32_t step,
     const bool curfew_now = k.p.enable_curfew && k.p.curfew_begin == minutes / dt;
     const bool rebuild = csr_rebuild(k, k.clock->t0 + step);
     uint32_t* seg = k.a.worklist + (size_t)blockIdx.x * cap;
+    uint32_t* segl = k.a.worklist_loc + (size_t)blockIdx.x * cap;
     const int lane = threadIdx.x & 31;
     for (uint32_t base = blockIdx.x * (256u * U); base < N; base += gridDim.x * (256u * U)) {
         uint32_t loc[U], sv[U], pos[U];
@@ -1250,14 +1259,19 @@ __global__ void __launch_bounds__(256, 8) k_step_hot_ilp(KArgs k, uint32_t step,
             const bool act = i < N;
             const bool ok = act && loc[u] < L;
             if (ok) store_slot(k, pos[u], i);
-            const bool cold = act && (curfew_now || sv[u] == 0 || hz[u] || !ok);
-            if (act && !cold) k.a.steps_until_move[i] = sv[u] - 1;
+            const bool mover = act && (curfew_now || sv[u] == 0);
+            const bool cold = mover || (act && (hz[u] || !ok));
+            if (act && !mover) k.a.steps_until_move[i] = sv[u] - 1;
             const unsigned cm = __ballot_sync(0xffffffffu, cold);
             if (cm) {
                 uint32_t basew = 0;
                 if (lane == __ffs(cm) - 1) basew = atomicAdd(&s_cnt, (uint32_t)__popc(cm));
                 basew = __shfl_sync(0xffffffffu, basew, __ffs(cm) - 1);
-                if (cold) seg[basew + __popc(cm & lanemask_lt())] = i;
+                if (cold) {
+                    const uint32_t q = basew + __popc(cm & lanemask_lt());
+                    seg[q] = i;
+                    segl[q] = (ok ? loc[u] : WORK_LOC_MASK) | (hz[u] ? WORK_HZ : 0u) | (mover ? WORK_MOVE : 0u);
+                }
             }
         }
     }
@@ -1265,29 +1279,28 @@ __global__ void __launch_bounds__(256, 8) k_step_hot_ilp(KArgs k, uint32_t step,
     if (threadIdx.x == 0) k.a.seg_count[blockIdx.x] = s_cnt;
 }
 
-// The cold agents of one step, one per thread: queued agent i (its location
-// loc0 and countdown s at the hot kernel) draws at loc0, then moves; the
-// histogram and the sums follow.
-__device__ __forceinline__ bool cold_agent(const KArgs& k, bool act, uint32_t i, uint32_t t, const StepClock& c,
-                                           double* s_grad) {
-    const uint32_t L = k.l.n;
+// The cold agents of one step, one per thread: queued agent i with the hot
+// kernel's word w (its location, whether it draws, whether it moves) draws
+// at its location, then moves; the histogram and the sums follow.
+__device__ __forceinline__ bool cold_agent(const KArgs& k, bool act, uint32_t i, uint32_t w, uint32_t t,
+                                           const StepClock& c, double* s_grad) {
     double term = 0.0;
     uint32_t loc = NONE, loc0 = NONE, var = 0;
     float inf = 0.0f;
     if (act) {
-        loc0 = k.a.location[i];
-        const uint32_t s = k.a.steps_until_move[i];
+        loc0 = (w & WORK_LOC_MASK) == WORK_LOC_MASK ? NONE : (w & WORK_LOC_MASK);
         inf = k.a.infectious[i];
-        if (loc0 < L) {
-            bool hz = false;
-            const float h0 = hazard_at(k, loc0, &hz);
-            if (hz) {
-                term = draw_agent(k, i, loc0, t, h0, s_grad);
-                inf = k.a.infectious[i];
-            }
+        if (w & WORK_HZ) {
+            term = draw_agent(k, i, loc0, t, k.l.hazard[loc0], s_grad);
+            inf = k.a.infectious[i];
         }
-        move_agent(k, i, c, s);
-        loc = (c.curfew_now || s == 0) ? k.a.location[i] : loc0;
+        if (w & WORK_MOVE) {
+            // the countdown is at zero (or the curfew step reloads it)
+            move_agent(k, i, c, 0u);
+            loc = k.a.location[i];
+        } else {
+            loc = loc0;
+        }
         if (inf > 0.0f) var = k.a.variant[i];
     }
     if (k.track_expected) add_expected(k, act, i, term);
@@ -1305,11 +1318,12 @@ __global__ void __launch_bounds__(256) k_step_cold(KArgs k, uint32_t step, uint3
     for (uint32_t sg = blockIdx.x; sg < n_seg; sg += gridDim.x) {
         const uint32_t n = k.a.seg_count[sg];
         const uint32_t* seg = k.a.worklist + (size_t)sg * cap;
+        const uint32_t* segl = k.a.worklist_loc + (size_t)sg * cap;
         const uint32_t trips = (n + blockDim.x - 1) / blockDim.x;  // uniform per block
         for (uint32_t it = 0; it < trips; ++it) {
             const uint32_t j = it * blockDim.x + threadIdx.x;
             const bool act = j < n;
-            moved |= cold_agent(k, act, act ? seg[j] : 0u, t, c, s_grad);
+            moved |= cold_agent(k, act, act ? seg[j] : 0u, act ? segl[j] : 0u, t, c, s_grad);
         }
     }
     publish_moved(k, moved, c.t);
@@ -1364,7 +1378,7 @@ __global__ void __launch_bounds__(256, MINB) k_step_cold_spread(KArgs k, uint32_
     for (uint32_t it = 0; it < trips; ++it) {
         const uint32_t w = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
         const bool act = w < total;
-        uint32_t i = 0u;
+        uint32_t i = 0u, lw = 0u;
         if (act) {
             // the last segment whose start is <= w
             uint32_t lo = 0, hi = n_seg - 1;
@@ -1375,9 +1389,11 @@ __global__ void __launch_bounds__(256, MINB) k_step_cold_spread(KArgs k, uint32_
                 else
                     hi = mid - 1;
             }
-            i = k.a.worklist[(size_t)lo * cap + (w - s_pre[lo])];
+            const size_t q = (size_t)lo * cap + (w - s_pre[lo]);
+            i = k.a.worklist[q];
+            lw = k.a.worklist_loc[q];
         }
-        moved |= cold_agent(k, act, i, t, c, s_grad);
+        moved |= cold_agent(k, act, i, lw, t, c, s_grad);
     }
     publish_moved(k, moved, c.t);
     grad_end(k, s_grad);
