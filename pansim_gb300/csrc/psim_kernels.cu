@@ -828,13 +828,16 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, uint32_t step, i
             __syncwarp();
             if (lane == 0) k.l.smask[wi] = 0u;
             if (l >= L || !((sw >> lane) & 1u)) continue;
+            // the location's fields load together with its sums
             const uint32_t rep = k.l.rep[l];
+            const float w_l = k.l.infectiousness[l];
+            const float k_f = k.r.k_f[rep];
             for (uint32_t v = 0; v < V; ++v) {
                 const size_t idx = (size_t)v * L + l;
                 const long long fix = (long long)k.l.sfix[idx];
                 float h = 0.0f, x = 0.0f;
                 if (fix != 0) {
-                    h = psim_hazard_x(fix, c[q], k.r.k_f[rep], k.l.infectiousness[l], season, dt, &x);
+                    h = psim_hazard_x(fix, c[q], k_f, w_l, season, dt, &x);
                     k.l.sfix[idx] = 0ull;
                 }
                 k.l.hazard[idx] = h;
@@ -982,14 +985,17 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_v(KArgs k, uint32_t step,
                 if (!((mine >> e) & 1u)) continue;
                 const uint32_t l = l0 + e;
                 if (l >= L) continue;
+                // the location's fields load together with its sums
                 const uint32_t rep = k.l.rep[l];
+                const float w_l = k.l.infectiousness[l];
+                const uint32_t n_l = rebuild ? c[e] : k.l.counts[l];
+                const float k_f = k.r.k_f[rep];
                 for (uint32_t v = 0; v < V; ++v) {
                     const size_t idx = (size_t)v * L + l;
                     const long long fix = (long long)k.l.sfix[idx];
                     float h = 0.0f, xx = 0.0f;
                     if (fix != 0) {
-                        const uint32_t n_l = rebuild ? c[e] : k.l.counts[l];
-                        h = psim_hazard_x(fix, n_l, k.r.k_f[rep], k.l.infectiousness[l], season, dt, &xx);
+                        h = psim_hazard_x(fix, n_l, k_f, w_l, season, dt, &xx);
                         k.l.sfix[idx] = 0ull;
                     }
                     k.l.hazard[idx] = h;
