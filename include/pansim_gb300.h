@@ -220,7 +220,7 @@ typedef struct psim_day_stats {
 /* Launch and algorithm choices of the per-step kernels, picked per device
  * and workload by the autotuner (pansim_gb300/autotune.py).  A new context
  * starts with variant 3, agg_slot 0, blocks_per_sm 4, scan_items 4,
- * scan_mode 2 (the fastest measured on GB300 at 2M agents). */
+ * scan_mode 3 (the fastest measured on GB300 at 2M agents). */
 typedef struct psim_tuning {
     uint32_t agg_count;      /* no effect (the histogram is updated by movers only) */
     uint32_t agg_slot;       /* warp-aggregated CSR slot atomics */
@@ -233,7 +233,9 @@ typedef struct psim_tuning {
     uint32_t scan_items;     /* locations per thread of the scan: 2, 4 or 8 (0 = 8) */
     uint32_t scan_mode;      /* 0 = single pass with decoupled look-back, 1 = tile sums + scan,
                                 2 = tile sums + scan with each thread owning consecutive
-                                locations (scan_items 4 or 8; with 2 it falls back to 1) */
+                                locations (scan_items 4 or 8; with 2 it falls back to 1),
+                                3 = single pass with look-back, consecutive locations per
+                                thread (scan_items 4 or 8; with 2 it falls back to 0) */
 } psim_tuning;
 
 typedef struct psim_ctx psim_ctx;

@@ -22,9 +22,11 @@ LARGE_AGENTS = 8_000_000
 def candidates(grid=None, variants=None):
     """variant: register cap of the fused kernel (64 / 40 / 32 registers),
     3 = hot/cold split, 4 / 5 = 2 / 4 agents per thread in flight;
-    blocks_per_sm 0 = one occupancy wave of that variant."""
+    blocks_per_sm 0 = one occupancy wave of that variant; scan_mode 2 / 3 =
+    two passes / one pass with look-back over consecutive locations per
+    thread."""
     for variant, agg_slot, bps, items, mode in itertools.product(variants or DEFAULT_VARIANTS, [1, 0],
-                                                                 grid or DEFAULT_GRID, [8, 4, 2], [1, 2]):
+                                                                 grid or DEFAULT_GRID, [8, 4, 2], [2, 3]):
         yield dict(agg_count=0, agg_slot=agg_slot, blocks_per_sm=bps, variant=variant, scan_items=items,
                    scan_mode=mode)
 
@@ -40,7 +42,7 @@ def autotune(sim, day, reps=2, grid=None, variants=None, verbose=False):
     set and one repetition (a day there takes a good fraction of a second)."""
     if sim.snap.n_agents > LARGE_AGENTS:
         grid = grid or [0, 16]
-        variants = variants or [0, 5]
+        variants = variants or [0, 3]
         reps = 1
     spd = sim.snap.steps_per_day
     sim.checkpoint_save(TUNE_SLOT)

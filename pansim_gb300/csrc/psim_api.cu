@@ -556,7 +556,7 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     // (pansim_gb300/autotune.py) picks per device and workload
     k.tune.agg_count = 0;
     k.tune.scan_items = 4;
-    k.tune.scan_mode = 2;
+    k.tune.scan_mode = 3;
     k.tune.agg_slot = 0;
     k.tune.blocks_per_sm = 4;
     k.tune.variant = 3;
@@ -681,7 +681,7 @@ int psim_set_tuning(psim_ctx* c, const psim_tuning* t) {
     if (t->scan_items != 0 && t->scan_items != 2 && t->scan_items != 4 && t->scan_items != 8)
         return fail(c, PSIM_ERR_ARG, "scan_items must be 2, 4 or 8");
     c->k.tune.scan_items = t->scan_items ? t->scan_items : 8u;
-    if (t->scan_mode > 2) return fail(c, PSIM_ERR_ARG, "scan_mode must be 0, 1 or 2");
+    if (t->scan_mode > 3) return fail(c, PSIM_ERR_ARG, "scan_mode must be 0, 1, 2 or 3");
     c->k.tune.scan_mode = t->scan_mode;
     c->graph_dirty = true;
     return 0;

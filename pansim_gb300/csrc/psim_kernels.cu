@@ -526,19 +526,25 @@ __device__ __noinline__ void adjoint_terms(const KArgs& k, uint32_t i, uint32_t 
 __device__ __forceinline__ double draw_agent(const KArgs& k, uint32_t i, uint32_t loc, uint32_t t, float h0,
                                              double* s_grad) {
     const uint32_t N = k.a.n, L = k.l.n, V = k.m.n_variants;
+    // the agent's fields load together (variant 0's susceptibility: a draw
+    // that infects rewrites the later variants' before they are read)
     const uint32_t rep = k.a.rep[i];
+    const float sigma = k.p.sigma_band[k.a.band[i]];
+    const float su0 = k.a.susceptible[i];
+    const unsigned long long seed = k.r.seed[rep];
+    const uint32_t li = i - k.r.agent_off[rep];
     double term_sum = 0.0;
     for (uint32_t v = 0; v < V; ++v) {
         const float h = v == 0 ? h0 : k.l.hazard[(size_t)v * L + loc];
         if (!(h > 0.0f)) continue;
         if (!k.r.variant_active[rep * V + v]) continue;
-        const float su = k.a.susceptible[(size_t)v * N + i];
-        const float s_eff = su * k.p.sigma_band[k.a.band[i]];
+        const float su = v == 0 ? su0 : k.a.susceptible[(size_t)v * N + i];
+        const float s_eff = su * sigma;
         if (!(s_eff > 0.0f)) continue;
         const float pf = h * s_eff;
         term_sum += pf < 1.0f ? (double)pf : 1.0;
         if (k.adj.on && pf < 1.0f) adjoint_terms(k, i, loc, v, rep, h, su, s_eff, s_grad);
-        const double U = psim_u01_once(k.r.seed[rep], i - k.r.agent_off[rep], t, PSIM_PHASE_INFECT + v);
+        const double U = psim_u01_once(seed, li, t, PSIM_PHASE_INFECT + v);
         if (U < (double)pf) {
             k.a.state[i] = (int8_t)k.m.first_infected;
             k.a.variant[i] = (uint8_t)v;
@@ -679,6 +685,74 @@ __device__ __forceinline__ uint64_t ld_volatile_u64(const uint64_t* p) {
     return *((const volatile uint64_t*)p);
 }
 
+// the block's tile (its ticket) and the launch epoch, in shared memory
+__device__ __forceinline__ void scan_take_ticket(const KArgs& k, uint32_t* s_tile, uint32_t* s_epoch) {
+    if (threadIdx.x == 0) {
+        // the epoch is read before the ticket: the last ticket advances it
+        *s_epoch = *((volatile uint32_t*)&k.l.scan_state[0]);
+        __threadfence();
+        *s_tile = atomicAdd(&k.l.scan_state[1], 1u);
+    }
+    __syncthreads();
+}
+
+// Publishes the tile's aggregate, lets warp 0 walk back over the
+// predecessors' status words to an inclusive prefix, publishes that, and
+// returns the exclusive prefix (every thread calls it).  The block holding
+// the last ticket resets the ticket counter and advances the epoch.
+__device__ __forceinline__ uint32_t scan_lookback(const KArgs& k, uint32_t tile, uint32_t epoch_raw, uint32_t agg,
+                                                  uint32_t* s_prefix) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t epoch = epoch_raw & 0x3FFFFFFFu;
+    uint64_t* st = k.l.scan_status;
+    const uint64_t ep = (uint64_t)epoch << 34;
+    if (threadIdx.x == 0) *((volatile uint64_t*)&st[tile]) = ep | ((uint64_t)(tile == 0 ? 2u : 1u) << 32) | agg;
+    if (warp == 0) {
+        uint32_t acc = 0;
+        if (tile > 0) {
+            int32_t look = (int32_t)tile - 1;
+            for (;;) {
+                const int32_t idx = look - lane;
+                uint64_t w = 0;
+                uint32_t fl = 2u;  // before tile 0: an empty prefix
+                for (uint32_t spin = 0;; ++spin) {
+                    if (idx >= 0) {
+                        w = ld_volatile_u64(&st[idx]);
+                        fl = (uint32_t)(w >> 34) == epoch ? (uint32_t)(w >> 32) & 3u : 0u;
+                    }
+                    if (__all_sync(0xffffffffu, fl != 0u)) break;
+                    if (spin >= SCAN_SPIN_LIMIT) {
+                        if (lane == 0) atomicOr(k.err, ERR_SCAN_WAIT);
+                        if (fl == 0u) {
+                            fl = 2u;
+                            w = 0;
+                        }
+                        break;
+                    }
+                }
+                const unsigned pm = __ballot_sync(0xffffffffu, fl == 2u);
+                const int first_p = pm ? __ffs(pm) - 1 : 31;
+                uint32_t v = lane <= first_p ? (uint32_t)w : 0u;
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+                acc += v;
+                if (pm) break;
+                look -= 32;
+            }
+            if (lane == 0) *((volatile uint64_t*)&st[tile]) = ep | (2ull << 32) | (uint64_t)(acc + agg);
+        }
+        if (lane == 0) *s_prefix = acc;
+    }
+    __syncthreads();
+    const uint32_t prefix = *s_prefix;
+    if (threadIdx.x == 0 && tile == gridDim.x - 1) {
+        k.l.scan_state[1] = 0u;
+        __threadfence();
+        k.l.scan_state[0] = epoch_raw + 1u;
+    }
+    return prefix;
+}
+
 template <int ITEMS, bool LOOKBACK>
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, uint32_t step, int with_hazard, int merge_q) {
     constexpr int TILE = SCAN_THREADS * ITEMS;
@@ -693,17 +767,10 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, uint32_t step, i
     // before (no prefix, no cursor writes).
     const uint32_t t_step = k.clock->t0 + step;
     const bool rebuild = LOOKBACK ? csr_decide(k, t_step) : csr_rebuild(k, t_step);
-    uint32_t tile = blockIdx.x, epoch = 0;
+    uint32_t tile = blockIdx.x;
     if (LOOKBACK && rebuild) {
-        if (threadIdx.x == 0) {
-            // the epoch is read before the ticket: the last ticket advances it
-            s_epoch = *((volatile uint32_t*)&k.l.scan_state[0]);
-            __threadfence();
-            s_tile = atomicAdd(&k.l.scan_state[1], 1u);
-        }
-        __syncthreads();
+        scan_take_ticket(k, &s_tile, &s_epoch);
         tile = s_tile;
-        epoch = s_epoch & 0x3FFFFFFFu;
     }
     const uint32_t wbase = tile * TILE + (uint32_t)warp * (32 * ITEMS);
     uint32_t c[ITEMS], ex[ITEMS];
@@ -718,56 +785,7 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, uint32_t step, i
         uint32_t mine = 0;
 #pragma unroll
         for (int q = 0; q < ITEMS; ++q) mine += c[q];
-        const uint32_t agg = block_sum_256(mine, s_red);
-        uint64_t* st = k.l.scan_status;
-        const uint64_t ep = (uint64_t)epoch << 34;
-        if (threadIdx.x == 0)
-            *((volatile uint64_t*)&st[tile]) = ep | ((uint64_t)(tile == 0 ? 2u : 1u) << 32) | agg;
-        if (warp == 0) {
-            uint32_t acc = 0;
-            if (tile > 0) {
-                int32_t look = (int32_t)tile - 1;
-                for (;;) {
-                    const int32_t idx = look - lane;
-                    uint64_t w = 0;
-                    uint32_t fl = 2u;  // before tile 0: an empty prefix
-                    for (uint32_t spin = 0;; ++spin) {
-                        if (idx >= 0) {
-                            w = ld_volatile_u64(&st[idx]);
-                            fl = (uint32_t)(w >> 34) == epoch ? (uint32_t)(w >> 32) & 3u : 0u;
-                        }
-                        if (__all_sync(0xffffffffu, fl != 0u)) break;
-                        if (spin >= SCAN_SPIN_LIMIT) {
-                            if (lane == 0) atomicOr(k.err, ERR_SCAN_WAIT);
-                            if (fl == 0u) {
-                                fl = 2u;
-                                w = 0;
-                            }
-                            break;
-                        }
-                    }
-                    const unsigned pm = __ballot_sync(0xffffffffu, fl == 2u);
-                    const int first_p = pm ? __ffs(pm) - 1 : 31;
-                    uint32_t v = lane <= first_p ? (uint32_t)w : 0u;
-#pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-                    acc += v;
-                    if (pm) break;
-                    look -= 32;
-                }
-                if (lane == 0) *((volatile uint64_t*)&st[tile]) = ep | (2ull << 32) | (uint64_t)(acc + agg);
-            }
-            if (lane == 0) s_prefix = acc;
-        }
-        __syncthreads();
-        prefix = s_prefix;
-        // the last ticket: every tile has its ticket, so reset the ticket
-        // counter and advance the epoch for the next launch
-        if (threadIdx.x == 0 && tile == gridDim.x - 1) {
-            k.l.scan_state[1] = 0u;
-            __threadfence();
-            k.l.scan_state[0] = s_epoch + 1u;
-        }
+        prefix = scan_lookback(k, tile, s_epoch, block_sum_256(mine, s_red), &s_prefix);
     } else {
     // sum of the tiles before this one
     uint32_t pre = 0;
@@ -904,24 +922,43 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_tile_sums_v(KArgs k, uint32_t 
     if (threadIdx.x == 0) k.l.tile_sums[blockIdx.x] = v;
 }
 
-template <int Q>
+// LOOKBACK: the single-pass form (decoupled look-back, as k_scan<ITEMS, true>):
+// the step's only scan kernel, so it decides the rebuild and needs no tile
+// sums; a step without a rebuild launches nothing else for its scan.
+template <int Q, bool LOOKBACK>
 __global__ void __launch_bounds__(SCAN_THREADS) k_scan_v(KArgs k, uint32_t step, int with_hazard, int merge_q) {
     constexpr int PER = 4 * Q;
     __shared__ uint32_t s_red[SCAN_THREADS / 32];
     __shared__ uint32_t s_warp[SCAN_THREADS / 32];
+    __shared__ uint32_t s_tile, s_epoch, s_prefix;
     const uint32_t L = k.l.n;
-    const uint32_t tile = blockIdx.x;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t l0 = tile * (SCAN_THREADS * PER) + threadIdx.x * PER;
     // without a rebuild the cursors keep the ends of the step before, and
     // the counts are read at the flagged locations only
-    const bool rebuild = csr_rebuild(k, k.clock->t0 + step);
+    const uint32_t t_step = k.clock->t0 + step;
+    const bool rebuild = LOOKBACK ? csr_decide(k, t_step) : csr_rebuild(k, t_step);
+    uint32_t tile = blockIdx.x;
+    if (LOOKBACK && rebuild) {
+        scan_take_ticket(k, &s_tile, &s_epoch);
+        tile = s_tile;
+    }
+    const uint32_t l0 = tile * (SCAN_THREADS * PER) + threadIdx.x * PER;
     uint32_t c[PER] = {};
     if (rebuild) {
         load_counts4<Q>(k, l0, c);
-        // sum of the tiles before this one
-        uint32_t pre = 0;
-        {
+        // in-thread exclusive prefix
+        uint32_t ex[PER];
+        uint32_t tot = 0;
+#pragma unroll
+        for (int e = 0; e < PER; ++e) {
+            ex[e] = tot;
+            tot += c[e];
+        }
+        // the sum of the tiles before this one
+        uint32_t prefix;
+        if (LOOKBACK) {
+            prefix = scan_lookback(k, tile, s_epoch, block_sum_256(tot, s_red), &s_prefix);
+        } else {
             uint32_t p0 = 0, p1 = 0, p2 = 0, p3 = 0;
             uint32_t j = threadIdx.x;
             for (; j + 3 * SCAN_THREADS < tile; j += 4 * SCAN_THREADS) {
@@ -931,17 +968,9 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_v(KArgs k, uint32_t step,
                 p3 += k.l.tile_sums[j + 3 * SCAN_THREADS];
             }
             for (; j < tile; j += SCAN_THREADS) p0 += k.l.tile_sums[j];
-            pre = p0 + p1 + p2 + p3;
+            prefix = block_sum_256(p0 + p1 + p2 + p3, s_red);
         }
-        const uint32_t prefix = block_sum_256(pre, s_red);
-        // in-thread exclusive prefix, then the warp and block offsets
-        uint32_t ex[PER];
-        uint32_t tot = 0;
-#pragma unroll
-        for (int e = 0; e < PER; ++e) {
-            ex[e] = tot;
-            tot += c[e];
-        }
+        // the warp and block offsets
         uint32_t x = tot;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -1315,7 +1344,10 @@ __device__ __forceinline__ bool cold_agent(const KArgs& k, bool act, uint32_t i,
 
 // The cold half, one segment per block: block b runs the agents that hot
 // block b queued (and segments b + gridDim.x, ...).
-__global__ void __launch_bounds__(256) k_step_cold(KArgs k, uint32_t step, uint32_t cap, uint32_t n_seg) {
+// four blocks per SM: the movers' decision chains are latency bound, and
+// fewer resident warps (the registers the compiler would otherwise take)
+// measured slower than the few spills
+__global__ void __launch_bounds__(256, 4) k_step_cold(KArgs k, uint32_t step, uint32_t cap, uint32_t n_seg) {
     __shared__ double s_grad[GRAD_N];
     grad_begin(k, s_grad);
     const uint32_t t = k.clock->t0 + step;
@@ -2103,14 +2135,19 @@ template <int ITEMS>
 static void launch_scan_items(const KArgs& k, uint32_t step, int with_hazard, int merge_q, cudaStream_t s) {
     unsigned tiles = (k.l.n + SCAN_THREADS * ITEMS - 1) / (SCAN_THREADS * ITEMS);
     if (!tiles) tiles = 1;
-    if (k.tune.scan_mode == 2 && (ITEMS == 4 || ITEMS == 8)) {
-        // thread-contiguous: ITEMS / 4 vectors of 4 locations per thread
+    if ((k.tune.scan_mode == 2 || k.tune.scan_mode == 3) && (ITEMS == 4 || ITEMS == 8)) {
+        // thread-contiguous: ITEMS / 4 vectors of 4 locations per thread;
+        // two passes (2) or one with look-back (3)
         constexpr int Q = ITEMS >= 8 ? 2 : 1;
-        k_tile_sums_v<Q><<<tiles, SCAN_THREADS, 0, s>>>(k, step);
-        k_scan_v<Q><<<tiles, SCAN_THREADS, 0, s>>>(k, step, with_hazard, merge_q);
+        if (k.tune.scan_mode == 3) {
+            k_scan_v<Q, true><<<tiles, SCAN_THREADS, 0, s>>>(k, step, with_hazard, merge_q);
+        } else {
+            k_tile_sums_v<Q><<<tiles, SCAN_THREADS, 0, s>>>(k, step);
+            k_scan_v<Q, false><<<tiles, SCAN_THREADS, 0, s>>>(k, step, with_hazard, merge_q);
+        }
         return;
     }
-    if (k.tune.scan_mode == 0) {
+    if (k.tune.scan_mode == 0 || k.tune.scan_mode == 3) {
         k_scan<ITEMS, true><<<tiles, SCAN_THREADS, 0, s>>>(k, step, with_hazard, merge_q);
     } else {
         k_tile_sums<ITEMS><<<tiles, SCAN_THREADS, 0, s>>>(k, step);
@@ -2127,7 +2164,7 @@ void launch_scan(const KArgs& k, uint32_t step, int with_hazard, int merge_q, cu
     else
         launch_scan_items<8>(k, step, with_hazard, merge_q, s);
 }
-int scan_kernels(const KArgs& k) { return k.tune.scan_mode == 0 ? 1 : 2; }
+int scan_kernels(const KArgs& k) { return k.tune.scan_mode == 0 || k.tune.scan_mode == 3 ? 1 : 2; }
 void launch_scatter_draw(const KArgs& k, uint32_t step, int scatter, int draw, cudaStream_t s) {
     static unsigned g = 0;
     if (!g) g = wave_grid(k_scatter_draw, 1u << 30);

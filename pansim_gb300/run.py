@@ -31,7 +31,7 @@ def main(argv=None):
     ap.add_argument("--agg-slot", type=int, default=1)
     ap.add_argument("--blocks-per-sm", type=int, default=0)
     ap.add_argument("--scan-items", type=int, default=4)
-    ap.add_argument("--scan-mode", type=int, default=2)
+    ap.add_argument("--scan-mode", type=int, default=3)
     a = ap.parse_args(argv)
     snap = synth.make_snapshot(a.agents, a.locs, seed=a.seed, pop_seed=a.pop_seed,
                                quarantine_policy=a.quarantine_policy, testing=a.testing)

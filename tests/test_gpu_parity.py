@@ -174,7 +174,13 @@ def test_bounded_wait_reports_error_and_context_survives(gpu_lib):
                                     dict(agg_count=0, agg_slot=1, blocks_per_sm=8, variant=8, scan_items=8,
                                          scan_mode=2),
                                     dict(agg_count=0, agg_slot=0, blocks_per_sm=0, variant=9, scan_items=4,
-                                         scan_mode=1)])
+                                         scan_mode=1),
+                                    dict(agg_count=0, agg_slot=0, blocks_per_sm=4, variant=3, scan_items=4,
+                                         scan_mode=3),
+                                    dict(agg_count=0, agg_slot=1, blocks_per_sm=0, variant=0, scan_items=8,
+                                         scan_mode=3),
+                                    dict(agg_count=0, agg_slot=0, blocks_per_sm=8, variant=6, scan_items=2,
+                                         scan_mode=3)])
 def test_tuning_choices_do_not_change_results(gpu_lib, tuning):
     """Every tuning against the oracle over three days: statistics, state and
     the agent list at the end of each day.  Most steps of a day move nobody
