@@ -188,6 +188,15 @@ int upload_mutable(psim_ctx* c, const psim_agents* a, const psim_locations* l) {
 }
 
 // LocationsList::initialize (locationList.h:224-230) and the variant gates
+// The per-location sums start afresh: zero, and every location marked for
+// the next scan.  Called before a pass that adds every agent's term
+// (k_movement, k_count): the first step of each day and the regroups.
+int reset_sums(psim_ctx* c) {
+    CK(cudaMemsetAsync(c->k.l.sfix, 0, sizeof(unsigned long long) * c->L * c->V, c->stream));
+    CK(cudaMemsetAsync(c->k.l.smask, 0xFF, sizeof(uint32_t) * (((size_t)c->L + 2047) / 2048 * 64 + 64), c->stream));
+    return 0;
+}
+
 // the next scan rebuilds the CSR whatever moved
 int force_rebuild(psim_ctx* c) {
     CK(cudaMemsetAsync(c->k.l.build + 1, 0xFF, sizeof(uint32_t), c->stream));
@@ -198,8 +207,7 @@ int initial_regroup(psim_ctx* c) {
     int rc0 = force_rebuild(c);
     if (rc0) return rc0;
     CK(cudaMemsetAsync(c->k.l.counts, 0, sizeof(uint32_t) * c->L, c->stream));
-    CK(cudaMemsetAsync(c->k.l.sfix, 0, sizeof(unsigned long long) * c->L * c->V, c->stream));
-    CK(cudaMemsetAsync(c->k.l.smask, 0, sizeof(uint32_t) * (((size_t)c->L + 2047) / 2048 * 64 + 64), c->stream));
+    if ((rc0 = reset_sums(c))) return rc0;
     launch_count(c->k, c->stream);
     launch_scan(c->k, 0, 1, 0, c->stream);
     launch_scatter_draw(c->k, 0, 1, 0, c->stream);
@@ -213,7 +221,11 @@ int initial_regroup(psim_ctx* c) {
 
 int do_step(psim_ctx* c, uint32_t step, bool draw, bool movement) {
     const int merge_q = c->params.quarantine_policy > 1;
-    if (movement) launch_movement(c->k, step, c->stream);
+    if (movement) {
+        int rc = reset_sums(c);
+        if (rc) return rc;
+        launch_movement(c->k, step, c->stream);
+    }
     launch_scan(c->k, step, 1, merge_q, c->stream);
     launch_scatter_draw(c->k, step, 1, draw ? 1 : 0, c->stream);
     c->launches += (movement ? 2 : 1) + (uint64_t)scan_kernels(c->k);
@@ -240,8 +252,13 @@ int capture_day_graph(psim_ctx* c) {
     };
     CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     const int merge_q = c->params.quarantine_policy > 1;
-    // movement(0); then per step: scan(s), scatter+draw(s) fused with movement(s+1)
+    // movement(0) with the sums afresh; then per step: scan(s), scatter+draw(s)
+    // fused with movement(s+1), which update the sums
     mark();
+    // (the capture stays open until EndCapture: errors are checked after it)
+    cudaError_t me = cudaMemsetAsync(c->k.l.sfix, 0, sizeof(unsigned long long) * c->L * c->V, c->stream);
+    if (me == cudaSuccess)
+        me = cudaMemsetAsync(c->k.l.smask, 0xFF, sizeof(uint32_t) * (((size_t)c->L + 2047) / 2048 * 64 + 64), c->stream);
     launch_movement(c->k, 0, c->stream);
     mark();
     for (uint32_t s = 0; s < c->spd; ++s) {
@@ -256,6 +273,10 @@ int capture_day_graph(psim_ctx* c) {
         mark();
     }
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+    if (e == cudaSuccess && me != cudaSuccess) {
+        cudaGraphDestroy(g);
+        e = me;
+    }
     if (e != cudaSuccess) return fail(c, PSIM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
     e = cudaGraphInstantiate(&c->day_graph, g, 0);
     cudaGraphDestroy(g);
@@ -817,6 +838,7 @@ int psim_movement(psim_ctx* c, uint32_t t) {
     if (!c || !c->uploaded) return PSIM_ERR_STATE;
     int rc = set_clock(c, t);
     if (rc) return rc;
+    if ((rc = reset_sums(c))) return rc;
     launch_movement(c->k, t % c->spd, c->stream);
     c->launches += 1;
     c->csr_fresh = true;
@@ -831,8 +853,7 @@ int psim_regroup(psim_ctx* c) {
     if (rc0) return rc0;
     if (!c->csr_fresh) {
         CK(cudaMemsetAsync(c->k.l.counts, 0, sizeof(uint32_t) * c->L, c->stream));
-        CK(cudaMemsetAsync(c->k.l.sfix, 0, sizeof(unsigned long long) * c->L * c->V, c->stream));
-        CK(cudaMemsetAsync(c->k.l.smask, 0, sizeof(uint32_t) * (((size_t)c->L + 2047) / 2048 * 64 + 64), c->stream));
+        if ((rc0 = reset_sums(c))) return rc0;
         launch_count(c->k, c->stream);
         c->launches += 1;
     }
@@ -1062,6 +1083,7 @@ int psim_time_step_kernels(psim_ctx* c, uint32_t t, float* ms) {
     // steps t and t+1 as in the day graph: movement(t) | scan(t) | scatter+draw(t) fused with
     // movement(t+1); then scan(t+1) and scatter+draw(t+1) untimed
     CK(cudaEventRecord(ev[0], c->stream));
+    if ((rc = reset_sums(c))) return rc;
     launch_movement(c->k, step, c->stream);
     CK(cudaEventRecord(ev[1], c->stream));
     launch_scan(c->k, step, 1, merge_q, c->stream);

@@ -458,6 +458,54 @@ __device__ __forceinline__ bool count_agent(const KArgs& k, bool act, uint32_t l
     return mv;
 }
 
+// Within a day the per-location sums persist: an agent changes them only
+// when it moves or its infectiousness changes (a draw that infects), and the
+// scan recomputes the hazards of the locations marked dirty (the sum mask)
+// only.  The first step of a day (k_movement after a reset of the sums and
+// a mark on every location) adds every agent's term afresh.
+__device__ __forceinline__ void mark_dirty(const KArgs& k, uint32_t loc) {
+    atomicOr(&k.l.smask[loc >> 5], 1u << (loc & 31u));
+}
+
+// The agent went from (loc0, inf0, var0) to (loc, inf, var): its count moves,
+// its fixed-point term leaves (loc0, var0) and joins (loc, var).  A count
+// change alone marks a location only if its sum is nonzero (else its hazard
+// is 0 whatever the count).  Returns whether the agent took a new location.
+__device__ __forceinline__ bool count_agent_delta(const KArgs& k, bool act, uint32_t loc0, uint32_t loc, float inf0,
+                                                  uint32_t var0, float inf, uint32_t var) {
+    const uint32_t L = k.l.n;
+    if (act && loc >= L) {
+        atomicOr(k.err, ERR_LOCATION);
+        loc = NONE;
+    }
+    const bool mv = act && loc != loc0;
+    if (mv) {
+        if (loc0 < L) {
+            atomicSub(&k.l.counts[loc0], 1u);
+            if ((k.l.hmask[loc0 >> 5] >> (loc0 & 31u)) & 1u) mark_dirty(k, loc0);
+        }
+        if (loc != NONE) {
+            atomicAdd(&k.l.counts[loc], 1u);
+            if ((k.l.hmask[loc >> 5] >> (loc & 31u)) & 1u) mark_dirty(k, loc);
+        }
+    }
+    if (act) {
+        const long long q0 = (loc0 < L && inf0 > 0.0f) ? __float2ll_rn(inf0 * PSIM_FIX_SCALE_F) : 0ll;
+        const long long q1 = (loc != NONE && inf > 0.0f) ? __float2ll_rn(inf * PSIM_FIX_SCALE_F) : 0ll;
+        if (mv || q0 != q1 || var0 != var) {
+            if (q0) {
+                atomicAdd(&k.l.sfix[(size_t)var0 * L + loc0], (unsigned long long)(-q0));
+                mark_dirty(k, loc0);
+            }
+            if (q1) {
+                atomicAdd(&k.l.sfix[(size_t)var * L + loc], (unsigned long long)q1);
+                mark_dirty(k, loc);
+            }
+        }
+    }
+    return mv;
+}
+
 // The full histogram of the current positions (after a reset of counts and sums).
 __device__ __forceinline__ void count_full(const KArgs& k, bool act, uint32_t loc, float inf, uint32_t variant) {
     const uint32_t L = k.l.n;
@@ -831,9 +879,10 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, uint32_t step, i
     const float season = k.clock->season;
     const uint32_t V = k.m.n_variants;
     if (with_hazard) {
-        // only locations that received infectiousness this step (sum mask)
-        // are read; elsewhere the hazard is 0 and stays unwritten, the hazard
-        // mask keeping readers away from it
+        // only the locations marked dirty (their sum or, with a nonzero sum,
+        // their count changed) are read; their hazards are recomputed from
+        // the persistent sums and their hazard-mask bits (sum nonzero)
+        // rewritten.  Elsewhere hazards and mask bits stay as they are.
         uint32_t sws[ITEMS];
 #pragma unroll
         for (int q = 0; q < ITEMS; ++q) sws[q] = k.l.smask[(wbase + q * 32) >> 5];
@@ -843,31 +892,30 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, uint32_t step, i
             const uint32_t wi = (wbase + q * 32) >> 5;
             const uint32_t sw = sws[q];
             if (!sw) continue;  // warp-uniform
-            __syncwarp();
-            if (lane == 0) k.l.smask[wi] = 0u;
-            if (l >= L || !((sw >> lane) & 1u)) continue;
-            // the location's fields load together with its sums
-            const uint32_t rep = k.l.rep[l];
-            const float w_l = k.l.infectiousness[l];
-            const float k_f = k.r.k_f[rep];
-            for (uint32_t v = 0; v < V; ++v) {
-                const size_t idx = (size_t)v * L + l;
-                const long long fix = (long long)k.l.sfix[idx];
-                float h = 0.0f, x = 0.0f;
-                if (fix != 0) {
-                    h = psim_hazard_x(fix, c[q], k_f, w_l, season, dt, &x);
-                    k.l.sfix[idx] = 0ull;
+            bool nz = false;
+            if (l < L && ((sw >> lane) & 1u)) {
+                // the location's fields load together with its sums
+                const uint32_t rep = k.l.rep[l];
+                const float w_l = k.l.infectiousness[l];
+                const float k_f = k.r.k_f[rep];
+                for (uint32_t v = 0; v < V; ++v) {
+                    const size_t idx = (size_t)v * L + l;
+                    const long long fix = (long long)k.l.sfix[idx];
+                    float h = 0.0f, x = 0.0f;
+                    if (fix != 0) {
+                        h = psim_hazard_x(fix, c[q], k_f, w_l, season, dt, &x);
+                        nz = true;
+                    }
+                    k.l.hazard[idx] = h;
+                    if (k.adj.on) k.l.hazard_x[idx] = x;
                 }
-                k.l.hazard[idx] = h;
-                if (k.adj.on) k.l.hazard_x[idx] = x;
             }
-        }
-        // the hazard mask of this step: the locations with an infectious
-        // agent, whose hazards were just computed (one word per 32
-        // locations; wbase is a multiple of 32)
-        if (lane == 0) {
-#pragma unroll
-            for (int q = 0; q < ITEMS; ++q) k.l.hmask[(wbase + q * 32) >> 5] = sws[q];
+            // one word per 32 locations (wbase is a multiple of 32)
+            const unsigned nzw = __ballot_sync(0xffffffffu, nz);
+            if (lane == 0) {
+                k.l.hmask[wi] = (k.l.hmask[wi] & ~sw) | nzw;
+                k.l.smask[wi] = 0u;
+            }
         }
     }
     if (merge_q) {
@@ -999,15 +1047,12 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_v(KArgs k, uint32_t step,
         const uint32_t dt = k.p.time_step;
         const float season = k.clock->season;
         const uint32_t V = k.m.n_variants;
-        // PER consecutive locations lie in one mask word (PER divides 32)
+        // PER consecutive locations lie in one mask word (PER divides 32);
+        // only the dirty ones are read (see k_scan)
         const uint32_t wi = l0 >> 5;
         const uint32_t sw = k.l.smask[wi];
         const uint32_t mine = (sw >> (l0 & 31u)) & ((PER == 32) ? 0xFFFFFFFFu : ((1u << PER) - 1u));
-        __syncwarp();
-        if ((l0 & 31u) == 0u) {
-            k.l.hmask[wi] = sw;
-            if (sw) k.l.smask[wi] = 0u;
-        }
+        uint32_t nzb = 0;  // my dirty locations whose sum is nonzero, as bits of the word
         if (mine) {
 #pragma unroll
             for (int e = 0; e < PER; ++e) {
@@ -1025,12 +1070,19 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_v(KArgs k, uint32_t step,
                     float h = 0.0f, xx = 0.0f;
                     if (fix != 0) {
                         h = psim_hazard_x(fix, n_l, k_f, w_l, season, dt, &xx);
-                        k.l.sfix[idx] = 0ull;
+                        nzb |= 1u << ((l0 & 31u) + e);
                     }
                     k.l.hazard[idx] = h;
                     if (k.adj.on) k.l.hazard_x[idx] = xx;
                 }
             }
+        }
+        // the word's bits from the 32 / PER consecutive threads that share it
+#pragma unroll
+        for (int o = 1; o < 32 / PER; o <<= 1) nzb |= __shfl_xor_sync(0xffffffffu, nzb, o);
+        if ((l0 & 31u) == 0u && sw) {
+            k.l.hmask[wi] = (k.l.hmask[wi] & ~sw) | nzb;
+            k.l.smask[wi] = 0u;
         }
     }
     if (merge_q) {
@@ -1095,6 +1147,8 @@ __global__ void __launch_bounds__(256, MINB) k_step_fused(KArgs k, uint32_t step
         const uint32_t loc0 = act ? k.a.location[i] : NONE;
         const uint32_t s = act ? k.a.steps_until_move[i] : 0u;
         float inf = act ? k.a.infectious[i] : 0.0f;
+        const float inf0 = inf;
+        const uint32_t var0 = inf0 > 0.0f ? k.a.variant[i] : 0u;
         const bool ok = act && loc0 < L;
         bool hz = false;
         const float h0 = ok ? hazard_at(k, loc0, &hz) : 0.0f;
@@ -1114,7 +1168,7 @@ __global__ void __launch_bounds__(256, MINB) k_step_fused(KArgs k, uint32_t step
             if (inf > 0.0f) var = k.a.variant[i];
         }
         if (k.track_expected) add_expected(k, act, i, term);
-        moved |= count_agent(k, act, loc0, loc, inf, var);
+        moved |= count_agent_delta(k, act, loc0, loc, inf0, var0, inf, var);
     }
     publish_moved(k, moved, c.t);
     grad_end(k, s_grad);
@@ -1168,6 +1222,7 @@ __global__ void __launch_bounds__(256) k_step_ilp(KArgs k, uint32_t step) {
             double term = 0.0;
             uint32_t loc = NONE, var = 0;
             float fi = inf[u];
+            const uint32_t var0 = inf[u] > 0.0f ? k.a.variant[i] : 0u;
             if (act && loc0[u] < L && hz[u]) {
                 term = draw_agent(k, i, loc0[u], t, h0[u], s_grad);
                 fi = k.a.infectious[i];
@@ -1178,7 +1233,7 @@ __global__ void __launch_bounds__(256) k_step_ilp(KArgs k, uint32_t step) {
                 if (fi > 0.0f) var = k.a.variant[i];
             }
             if (k.track_expected) add_expected(k, act, i, term);
-            moved |= count_agent(k, act, loc0[u], loc, fi, var);
+            moved |= count_agent_delta(k, act, loc0[u], loc, inf[u], var0, fi, var);
         }
     }
     publish_moved(k, moved, c.t);
@@ -1320,14 +1375,16 @@ __global__ void __launch_bounds__(256, 8) k_step_hot_ilp(KArgs k, uint32_t step,
 __device__ __forceinline__ bool cold_agent(const KArgs& k, bool act, uint32_t i, uint32_t w, uint32_t t,
                                            const StepClock& c, double* s_grad) {
     double term = 0.0;
-    uint32_t loc = NONE, loc0 = NONE, var = 0;
-    float inf = 0.0f;
+    uint32_t loc = NONE, loc0 = NONE, var0 = 0, var = 0;
+    float inf0 = 0.0f, inf = 0.0f;
     if (act) {
         loc0 = (w & WORK_LOC_MASK) == WORK_LOC_MASK ? NONE : (w & WORK_LOC_MASK);
-        inf = k.a.infectious[i];
+        inf0 = inf = k.a.infectious[i];
+        if (inf0 > 0.0f) var0 = var = k.a.variant[i];
         if (w & WORK_HZ) {
             term = draw_agent(k, i, loc0, t, k.l.hazard[loc0], s_grad);
             inf = k.a.infectious[i];
+            var = inf > 0.0f ? k.a.variant[i] : 0u;
         }
         if (w & WORK_MOVE) {
             // the countdown is at zero (or the curfew step reloads it)
@@ -1336,10 +1393,9 @@ __device__ __forceinline__ bool cold_agent(const KArgs& k, bool act, uint32_t i,
         } else {
             loc = loc0;
         }
-        if (inf > 0.0f) var = k.a.variant[i];
     }
     if (k.track_expected) add_expected(k, act, i, term);
-    return count_agent(k, act, loc0, loc, inf, var);
+    return count_agent_delta(k, act, loc0, loc, inf0, var0, inf, var);
 }
 
 // The cold half, one segment per block: block b runs the agents that hot
