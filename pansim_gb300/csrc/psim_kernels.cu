@@ -261,7 +261,10 @@ __device__ void move_decide(const KArgs& k, uint32_t i, uint32_t t, uint32_t min
         }
         uint32_t new_loc = fl(new_type, num_pot == 1);
         bool too_old = (new_type == p.school_type || new_type == p.classroom_type) && age >= p.school_age_restriction;
-        if (too_old || ((loc_open(k, new_loc) == 0 || loc_closed_until(k, new_loc) > t) && new_type != p.work_type) ||
+        // both flags of the new location load together
+        const uint8_t nl_open = loc_open(k, new_loc);
+        const uint32_t nl_closed = loc_closed_until(k, new_loc);
+        if (too_old || ((nl_open == 0 || nl_closed > t) && new_type != p.work_type) ||
             (p.lockdown_nonvacc && k.a.st_immunization_ts[i] == 0)) {
             if (num_pot > 1) {
                 double rnd = psim_u01(rng) * 1.0;
