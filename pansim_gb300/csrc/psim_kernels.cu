@@ -434,13 +434,11 @@ __device__ __forceinline__ void move_agent(const KArgs& k, uint32_t i, const Ste
 // choice); the masks hold one 32-bit word per warp and item.
 constexpr int SCAN_THREADS = 256;
 
-// The per-location agent counts are kept up to date incrementally: an agent
-// whose location changed from loc0 to loc moves one count (two fire-and-
-// forget reductions); agents that stay do not touch the histogram.  The
-// fixed-point infectiousness sums are rebuilt every step: every infectious
-// agent adds its term at its (new) location, and the scan consumes them.
-// Returns whether the agent took a new location (its kernel then publishes
-// the timestamp of the new locations, publish_moved).
+// The full pass of a day's first step (k_movement, after a reset of the
+// sums): an agent whose location changed from loc0 to loc moves one count
+// (two fire-and-forget reductions), and every infectious agent adds its term
+// at its (new) location.  Returns whether the agent took a new location (its
+// kernel then publishes the timestamp of the new locations, publish_moved).
 __device__ __forceinline__ bool count_agent(const KArgs& k, bool act, uint32_t loc0, uint32_t loc, float inf,
                                             uint32_t variant) {
     const uint32_t L = k.l.n;
@@ -1244,15 +1242,15 @@ __global__ void __launch_bounds__(256) k_step_ilp(KArgs k, uint32_t step) {
 }
 
 // Hot/cold form of k_step_fused.  The hot kernel does, for every agent, the
-// CSR slot of step `step`; agents that neither draw (no infectious agent at
-// their location, so they are not infectious themselves) nor move at step + 1
-// (countdown > 0, no curfew transition) also count down here and need no
-// histogram work (they stay, with nothing to add to the sums).  The others -- a few percent per step, each with a long
-// chain of dependent loads in the movement decision -- are queued in the
-// block's own segment of the work list (shared-memory counter, no global
-// contention), and k_step_cold runs them densely, a block per segment, with
-// the full register budget.  Per agent the operations and their order are
-// those of k_step_fused.
+// CSR slot of step `step` (when the step rebuilds the agent list) and the
+// countdown of every agent that does not move at step + 1.  Movers (countdown
+// at zero, curfew) and agents at a location with an infectious agent (they
+// draw) -- a few percent per step, the movers each with a long chain of
+// dependent loads in the movement decision -- are queued in the block's own
+// segment of the work list (shared-memory counter, no global contention)
+// with their location and flags, and k_step_cold runs them densely, a block
+// per segment.  Per agent the operations and their order are those of
+// k_step_fused.
 __global__ void __launch_bounds__(256, 8) k_step_hot(KArgs k, uint32_t step, uint32_t cap) {
     __shared__ uint32_t s_cnt;
     if (threadIdx.x == 0) s_cnt = 0u;
