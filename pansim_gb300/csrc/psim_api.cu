@@ -211,8 +211,9 @@ int initial_regroup(psim_ctx* c) {
     launch_count(c->k, c->stream);
     launch_scan(c->k, 0, 1, 0, c->stream);
     launch_scatter_draw(c->k, 0, 1, 0, c->stream);
-    launch_stats(c->k, 0, c->stream);
-    c->launches += 4 + (uint64_t)scan_kernels(c->k);
+    // the variant gating of the first steps (the statistics come at midnight)
+    launch_variant_flags(c->k, c->stream);
+    c->launches += 3 + (uint64_t)scan_kernels(c->k);
     int rc = launch_check(c);
     if (rc) return rc;
     c->csr_fresh = true;

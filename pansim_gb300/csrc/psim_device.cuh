@@ -284,6 +284,7 @@ void launch_canonical_csr(const KArgs& k, cudaStream_t s);
 void launch_progress(const KArgs& k, uint32_t t, cudaStream_t s);
 void launch_test(const KArgs& k, uint32_t t, cudaStream_t s);
 void launch_stats(const KArgs& k, uint32_t t, cudaStream_t s);
+void launch_variant_flags(const KArgs& k, cudaStream_t s);
 void launch_plan(const KArgs& k, uint32_t t, cudaStream_t s);
 void launch_flag_hcw(const KArgs& k, cudaStream_t s);
 void launch_bounded_wait_probe(const KArgs& k, uint32_t iters, cudaStream_t s);

@@ -1851,6 +1851,17 @@ __global__ void __launch_bounds__(256) k_stats(KArgs k, uint32_t t, int with_tes
     stats_flush(k, cur, c, imm, V);
 }
 
+// The variant gating alone, without the statistics (after an upload): a
+// variant is active in a replica when one of its agents is infected with it.
+__global__ void __launch_bounds__(256) k_variant_flags(KArgs k) {
+    const uint32_t N = k.a.n, V = k.m.n_variants;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+        if (!k.m.state_infected[(uint8_t)k.a.state[i]]) continue;
+        uint8_t* f = &k.r.variant_active[(size_t)k.a.rep[i] * V + k.a.variant[i]];
+        if (*f == 0) *f = 1;
+    }
+}
+
 // variant gating of the next day (countVariantCases, simulation.h:768-777)
 __global__ void k_variant_active(KArgs k) {
     const uint32_t R = k.r.n, V = k.m.n_variants;
@@ -2253,6 +2264,10 @@ void launch_stats(const KArgs& k, uint32_t t, cudaStream_t s) {
     unsigned blocks = std::min(g, (unsigned)((k.a.n + 255) / 256));
     k_stats<<<blocks ? blocks : 1, 256, 0, s>>>(k, t, 1);
     k_variant_active<<<1, 256, 0, s>>>(k);
+}
+void launch_variant_flags(const KArgs& k, cudaStream_t s) {
+    cudaMemsetAsync(k.r.variant_active, 0, (size_t)k.r.n * k.m.n_variants, s);
+    k_variant_flags<<<grid_for(k.a.n, 8), 256, 0, s>>>(k);
 }
 void launch_plan(const KArgs& k, uint32_t t, cudaStream_t s) {
     if (k.p.quarantine_policy > 3 && k.l.n_schools) k_plan_schools<<<grid_for(k.l.n_schools, 4), 256, 0, s>>>(k, t);
