@@ -203,7 +203,8 @@ def run_reference(args, ws, rank):
     dt = time.perf_counter() - t0
     value = snap.n_agents * spd * args.steps / dt
     cores = ob.threads()
-    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0, "steps": args.steps,
+    # n_gpus: the job's, as in the GB300 arm's line (the work runs on rank 0's host cores)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dt * 1000 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": "2M agents, 500k non-home locations (+homes), dt 10 min, 1 day per step",
