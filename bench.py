@@ -40,8 +40,17 @@ STEP_BYTES = (32, 20)
 # replica = 30 B/location
 KERNEL_BYTES = {"movement": (20, 4), "scan": (0, 30), "step_fused": (38, 0), "step_hot": (16, 8),
                 "step_cold": None}
-KERNEL_LABELS = {"scan": "k_tile_sums + k_scan", "step_fused": "k_step_fused", "step_hot": "k_step_hot",
-                 "step_cold": "k_step_cold"}
+KERNEL_LABELS = {"step_fused": "k_step_fused", "step_hot": "k_step_hot", "step_cold": "k_step_cold"}
+
+
+def scan_label(tuning):
+    """The scan kernels of a tuning (scan_mode 0/3 one pass with look-back,
+    1/2 tile sums then scan; 2/3 over consecutive locations unless scan_items 2)."""
+    mode, items = tuning.get("scan_mode", 3), tuning.get("scan_items", 4)
+    vec = mode in (2, 3) and items in (4, 8)
+    if mode in (0, 3):
+        return "k_scan_v" if vec else "k_scan"
+    return "k_tile_sums_v + k_scan_v" if vec else "k_tile_sums + k_scan"
 
 
 def dist_env():
@@ -508,7 +517,8 @@ def main():
             "config": {"workload": "2M agents, 500k non-home locations (+homes), dt 10 min, 1 day per step",
                        "agents": N, "locations": L, "timesteps_per_step": 144,
                        "l2": "flushed between timed steps (256 MiB write)", "parallelism": "replicas" if ws > 1 else "1 gpu"},
-            "roofline": {"bound": "hbm", "kernel": "one timestep: " + " + ".join(KERNEL_LABELS[n] for n in step_names),
+            "roofline": {"bound": "hbm", "kernel": "one timestep: " + " + ".join(
+                             scan_label(best) if n == "scan" else KERNEL_LABELS[n] for n in step_names),
                          "achieved": ach, "peak": peak,
                          "unit": "GB/s", "frac": ach / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "alg_bytes_per_launch": step_bytes, "launch_ms": step_ms, "dominant": dom,
