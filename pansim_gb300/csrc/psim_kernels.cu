@@ -1741,114 +1741,165 @@ __global__ void __launch_bounds__(256) k_test(KArgs k, uint32_t t) {
 // the host.
 constexpr int STAT_FIELDS = 48;
 
-// reduce the per-thread counters of a warp whose lanes all hold replica
-// `rep` (else per-lane) into the replica's accumulator
-__device__ __forceinline__ void stats_flush(const KArgs& k, uint32_t rep, unsigned* c, double* imm, uint32_t V) {
-    const uint32_t rep0 = __shfl_sync(0xffffffffu, rep, 0);
-    const bool uniform = __all_sync(0xffffffffu, rep == rep0);
-    const bool lead = (threadIdx.x & 31) == 0;
-    if (uniform) {
+// A warp's counters live in its lanes: field f in word f / 32 of lane f % 32.
+// Each agent sets one bit per counted flag in two words (bit f of word w is
+// field 32 w + f); a 32 x 32 bit transpose across the warp hands lane f the
+// column of bit f, whose population count is the warp's count of field f.
+__device__ __forceinline__ uint32_t warp_transpose32(uint32_t x, int lane) {
 #pragma unroll
-        for (int f = 0; f < STAT_FIELDS; ++f) {
-            unsigned x = c[f];
+    for (int j = 16; j > 0; j >>= 1) {
+        const uint32_t m = j == 16 ? 0x0000FFFFu : j == 8 ? 0x00FF00FFu : j == 4 ? 0x0F0F0F0Fu : j == 2 ? 0x33333333u : 0x55555555u;
+        const uint32_t y = __shfl_xor_sync(0xffffffffu, x, j);
+        x = (lane & j) ? ((x & ~m) | ((y & ~m) >> j)) : ((x & m) | ((y & m) << j));
+    }
+    return x;
+}
+
+// adds a warp's counters (lane-distributed), its lanes' sums of the two
+// counted values (reinfections, boosters) and its lanes' immunity sums to
+// replica `rep`: into the block's shared row when `rep` is the block's
+// replica, else into the global row; then clears them
+template <int VM>
+__device__ __forceinline__ void stats_flush_warp(const KArgs& k, uint32_t rep, uint32_t block_rep, unsigned* acc,
+                                                 unsigned* val, double* imm, uint32_t V, unsigned* s_c, double* s_imm) {
+    const int lane = threadIdx.x & 31;
+    const bool shared_row = rep == block_rep;
+    const unsigned reinf = __reduce_add_sync(0xffffffffu, val[0]);
+    const unsigned bstr = __reduce_add_sync(0xffffffffu, val[1]);
+    if (lane == SC_REINF) acc[0] += reinf;
+    if (lane == SC_BSTR) acc[0] += bstr;
+    val[0] = val[1] = 0u;
+#pragma unroll
+    for (int w = 0; w < 2; ++w) {
+        const int f = w * 32 + lane;
+        if (f < STAT_FIELDS && rep != NONE && acc[w]) {
+            if (shared_row)
+                atomicAdd(&s_c[f], acc[w]);
+            else
+                atomicAdd(&k.stats[rep].c[f], acc[w]);
+        }
+        acc[w] = 0;
+    }
+#pragma unroll
+    for (int v = 0; v < VM; ++v) {
+        if ((uint32_t)v < V) {
+            double x = imm[v];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-            if (lead && rep0 != NONE && x) atomicAdd(&k.stats[rep0].c[f], x);
-            c[f] = 0;
-        }
-#pragma unroll
-        for (int v = 0; v < PSIM_MAX_STRAINS; ++v) {
-            if ((uint32_t)v < V) {
-                double x = imm[v];
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-                if (lead && rep0 != NONE && x != 0.0) atomicAdd(&k.stats[rep0].imm[v], x);
+            if (lane == 0 && rep != NONE && x != 0.0) {
+                if (shared_row)
+                    atomicAdd(&s_imm[v], x);
+                else
+                    atomicAdd(&k.stats[rep].imm[v], x);
             }
-            imm[v] = 0.0;
         }
-    } else {
-#pragma unroll
-        for (int f = 0; f < STAT_FIELDS; ++f) {
-            if (rep != NONE && c[f]) atomicAdd(&k.stats[rep].c[f], c[f]);
-            c[f] = 0;
-        }
-#pragma unroll
-        for (int v = 0; v < PSIM_MAX_STRAINS; ++v) {
-            if ((uint32_t)v < V && rep != NONE && imm[v] != 0.0) atomicAdd(&k.stats[rep].imm[v], imm[v]);
-            imm[v] = 0.0;
-        }
+        imm[v] = 0.0;
     }
 }
 
 // The statistics row (Simulation::refreshAndPrintStatistics, simulation.h:473-665)
-// in one pass: each block walks a contiguous range of agents, every thread
-// accumulates its agents' counters in registers and flushes them (one
-// reduction per warp) when its replica changes and at the end.
-__global__ void __launch_bounds__(256) k_stats(KArgs k, uint32_t t, int with_tests) {
+// in one pass: each block walks a contiguous range of agents; a warp counts
+// its 32 agents' flags per field by a bit transpose, keeps the counts in its
+// lanes, and adds them to the block's shared row (or, for another replica
+// than the block's last one, to the global row) when its replica changes and
+// at the end.  A warp whose agents span two replicas counts them one replica
+// at a time.
+// VM: the largest number of variants the kernel accumulates immunity for
+// (at least the context's); the per-lane sums take registers.
+template <int VM>
+__global__ void __launch_bounds__(256, VM > 2 ? 4 : 5) k_stats(KArgs k, uint32_t t, int with_tests) {
+    static_assert(SC_P2 < 17 && SC_HIST == 17 && SC_VAR == 33 && SC_INFV == 40 && PSIM_MAX_STRAINS <= 7,
+                  "the flag words hold fields 0-31 and 32-46");
+    __shared__ unsigned s_c[STAT_FIELDS];
+    __shared__ double s_imm[PSIM_MAX_STRAINS];
     const uint32_t N = k.a.n, V = k.m.n_variants;
     const uint32_t day_steps = 24u * 60u / k.p.time_step;
-    unsigned c[STAT_FIELDS];
-#pragma unroll
-    for (int f = 0; f < STAT_FIELDS; ++f) c[f] = 0;
-    double imm[PSIM_MAX_STRAINS];
-#pragma unroll
-    for (int v = 0; v < PSIM_MAX_STRAINS; ++v) imm[v] = 0.0;
+    const uint32_t vmask = (1u << V) - 1u;
+    const int lane = threadIdx.x & 31;
     const uint32_t per = ((N + gridDim.x - 1) / gridDim.x + 255u) & ~255u;
     const uint32_t begin = blockIdx.x * per, end = min(N, begin + per);
+    if (threadIdx.x < STAT_FIELDS) s_c[threadIdx.x] = 0u;
+    if (threadIdx.x < PSIM_MAX_STRAINS) s_imm[threadIdx.x] = 0.0;
+    // the replica of the block's last agent takes the shared row
+    const uint32_t block_rep = begin < end ? (uint32_t)k.a.rep[end - 1] : NONE;
+    __syncthreads();
+    unsigned acc[2] = {0u, 0u}, val[2] = {0u, 0u};
+    double imm[VM];
+#pragma unroll
+    for (int v = 0; v < VM; ++v) imm[v] = 0.0;
     uint32_t cur = NONE;
     for (uint32_t base = begin; base < end; base += 256u) {
         const uint32_t i = base + threadIdx.x;
         const bool act = i < end;
-        const uint32_t rep = act ? (uint32_t)k.a.rep[i] : cur;
-        // a replica boundary inside the warp: flush what was gathered so far
-        if (__any_sync(0xffffffffu, rep != cur)) {
-            stats_flush(k, cur, c, imm, V);
-            cur = rep;
-        }
-        if (!act) continue;
-        const uint8_t st = (uint8_t)k.a.state[i];
-        const uint32_t wb = k.m.state_wb[st];
-        const bool inf = k.m.state_infected[st] != 0;
-        c[SC_HOSP] += (wb != WB_D && wb != WB_S && t < k.a.st_hospitalized_until[i]);
-        const bool isq = k.a.st_quarantined_ts[i] <= t && k.a.st_quarantined_until[i] > t;
-        c[SC_Q] += isq;
-        c[SC_QT] += isq && inf;
-        c[SC_NQ] += !isq && inf;
-        c[SC_STAYED] += k.a.stayed_home[i] != 0;
-        const bool new_inf = k.a.st_infected_ts[i] > t - day_steps && k.a.st_infected_ts[i] <= t;
-        c[SC_NI] += new_inf;
-        const uint32_t ic = k.a.st_infected_count[i], mc = k.a.st_immunization_count[i];
-        c[SC_INF_ONCE] += ic > 0;
-        c[SC_REINF] += ic > 1 ? ic - 1 : 0;
-        c[SC_BSTR] += mc > 1 ? mc - 1 : 0;
-        c[SC_ALL_INF] += inf;
-        if (k.a.hcw[i]) {
-            c[SC_HCI] += (inf || k.a.quarantined[i]) ? 1u : 0u;
-            c[SC_HCE] += new_inf;
-        }
-        c[SC_INFH] += inf && loc_type(k, k.a.location[i]) == k.p.hospital_type;
-        c[SC_VNI] += ic == 0 && mc > 0;
-        if (with_tests) {
-            c[SC_TESTS] += k.a.last_test[i] == t;
-            const uint32_t d = k.a.st_diagnosed_ts[i];
-            c[SC_P1] += d == t;
-            c[SC_P2] += d < t && d > t - day_steps;
-        }
+        // every field is loaded at once, for idle lanes from a valid agent:
+        // no load waits for the value of another
+        const uint32_t j = act ? i : begin;
+        const uint32_t rep = act ? (uint32_t)k.a.rep[j] : NONE;
+        const uint8_t st = (uint8_t)k.a.state[j];
+        const uint32_t h_until = k.a.st_hospitalized_until[j];
+        const uint32_t q_ts = k.a.st_quarantined_ts[j], q_until = k.a.st_quarantined_until[j];
+        const uint32_t its = k.a.st_infected_ts[j];
+        const uint32_t ic = k.a.st_infected_count[j], mc = k.a.st_immunization_count[j];
+        const bool stayed = k.a.stayed_home[j] != 0, hcw = k.a.hcw[j] != 0, quar = k.a.quarantined[j] != 0;
+        const uint32_t var = k.a.variant[j], vmask_i = k.a.st_variant_mask[j];
+        const uint32_t ltype = loc_type(k, k.a.location[j]);
+        const uint32_t tested = with_tests ? k.a.last_test[j] : NONE;
+        const uint32_t d = with_tests ? k.a.st_diagnosed_ts[j] : NONE;
+        float sus[VM];
 #pragma unroll
-        for (int q = 0; q < 16; ++q) c[SC_HIST + q] += st == (uint8_t)q;
-        const uint32_t var = k.a.variant[i];
+        for (int v = 0; v < VM; ++v) sus[v] = (uint32_t)v < V ? k.a.susceptible[(size_t)v * N + j] : 1.0f;
+        uint32_t wa = 0u, wb = 0u, reinf = 0u, bstr = 0u;
+        if (act) {
+            const uint32_t wbs = k.m.state_wb[st];
+            const bool inf = k.m.state_infected[st] != 0;
+            const bool hosp = wbs != WB_D && wbs != WB_S && t < h_until;
+            const bool isq = q_ts <= t && q_until > t;
+            const bool new_inf = its > t - day_steps && its <= t;
+            wa = (uint32_t)hosp << SC_HOSP | (uint32_t)isq << SC_Q | (uint32_t)(isq && inf) << SC_QT |
+                 (uint32_t)(!isq && inf) << SC_NQ | (uint32_t)stayed << SC_STAYED | (uint32_t)new_inf << SC_NI |
+                 (uint32_t)(ic > 0) << SC_INF_ONCE | (uint32_t)inf << SC_ALL_INF |
+                 (uint32_t)(hcw && (inf || quar)) << SC_HCI | (uint32_t)(hcw && new_inf) << SC_HCE |
+                 (uint32_t)(inf && ltype == k.p.hospital_type) << SC_INFH | (uint32_t)(ic == 0 && mc > 0) << SC_VNI;
+            if (with_tests)
+                wa |= (uint32_t)(tested == t) << SC_TESTS | (uint32_t)(d == t) << SC_P1 |
+                      (uint32_t)(d < t && d > t - day_steps) << SC_P2;
+            // the state histogram: states 0-14 in the first word, 15 in the second
+            if (st < 15)
+                wa |= 1u << (SC_HIST + st);
+            else if (st == 15)
+                wb |= 1u;
+            if (inf && var < (uint32_t)PSIM_MAX_STRAINS) wb |= 1u << (SC_VAR - 32 + var);
+            wb |= (vmask_i & vmask) << (SC_INFV - 32);
+            reinf = ic > 1 ? ic - 1 : 0u;
+            bstr = mc > 1 ? mc - 1 : 0u;
+        }
+        // one replica of the warp at a time (almost always one)
+        unsigned todo = __ballot_sync(0xffffffffu, act);
+        while (todo) {
+            const uint32_t r = __shfl_sync(0xffffffffu, rep, __ffs(todo) - 1);
+            const bool sel = act && rep == r;
+            todo &= ~__ballot_sync(0xffffffffu, sel);
+            if (r != cur) {
+                stats_flush_warp<VM>(k, cur, block_rep, acc, val, imm, V, s_c, s_imm);
+                cur = r;
+            }
+            acc[0] += (unsigned)__popc(warp_transpose32(sel ? wa : 0u, lane));
+            acc[1] += (unsigned)__popc(warp_transpose32(sel ? wb : 0u, lane));
+            if (sel) {
+                val[0] += reinf;
+                val[1] += bstr;
 #pragma unroll
-        for (int v = 0; v < PSIM_MAX_STRAINS; ++v) c[SC_VAR + v] += inf && var == (uint32_t)v;
-        const uint32_t mask = k.a.st_variant_mask[i];
-#pragma unroll
-        for (int v = 0; v < PSIM_MAX_STRAINS; ++v) {
-            if ((uint32_t)v < V) {
-                c[SC_INFV + v] += (mask >> v) & 1u;
-                imm[v] += 1.0 - (double)k.a.susceptible[(size_t)v * N + i];
+                for (int v = 0; v < VM; ++v)
+                    if ((uint32_t)v < V) imm[v] += 1.0 - (double)sus[v];
             }
         }
     }
-    stats_flush(k, cur, c, imm, V);
+    stats_flush_warp<VM>(k, cur, block_rep, acc, val, imm, V, s_c, s_imm);
+    __syncthreads();
+    if (block_rep != NONE) {
+        if (threadIdx.x < STAT_FIELDS && s_c[threadIdx.x]) atomicAdd(&k.stats[block_rep].c[threadIdx.x], s_c[threadIdx.x]);
+        if (threadIdx.x < V && s_imm[threadIdx.x] != 0.0) atomicAdd(&k.stats[block_rep].imm[threadIdx.x], s_imm[threadIdx.x]);
+    }
 }
 
 // The variant gating alone, without the statistics (after an upload): a
@@ -2259,10 +2310,21 @@ void launch_test(const KArgs& k, uint32_t t, cudaStream_t s) {
 }
 void launch_stats(const KArgs& k, uint32_t t, cudaStream_t s) {
     cudaMemsetAsync(k.stats, 0, sizeof(DevStatsAcc) * k.r.n, s);
-    static unsigned g = 0;
-    if (!g) g = wave_grid(k_stats, 1u << 30);
-    unsigned blocks = std::min(g, (unsigned)((k.a.n + 255) / 256));
-    k_stats<<<blocks ? blocks : 1, 256, 0, s>>>(k, t, 1);
+    static unsigned g[3] = {0, 0, 0};
+    if (!g[0]) {
+        g[0] = wave_grid(k_stats<1>, 1u << 30);
+        g[1] = wave_grid(k_stats<2>, 1u << 30);
+        g[2] = wave_grid(k_stats<PSIM_MAX_STRAINS>, 1u << 30);
+    }
+    const int vi = k.m.n_variants <= 1 ? 0 : k.m.n_variants <= 2 ? 1 : 2;
+    unsigned blocks = std::min(g[vi], (unsigned)((k.a.n + 255) / 256));
+    if (!blocks) blocks = 1;
+    if (vi == 0)
+        k_stats<1><<<blocks, 256, 0, s>>>(k, t, 1);
+    else if (vi == 1)
+        k_stats<2><<<blocks, 256, 0, s>>>(k, t, 1);
+    else
+        k_stats<PSIM_MAX_STRAINS><<<blocks, 256, 0, s>>>(k, t, 1);
     k_variant_active<<<1, 256, 0, s>>>(k);
 }
 void launch_variant_flags(const KArgs& k, cudaStream_t s) {
