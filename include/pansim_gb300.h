@@ -311,6 +311,14 @@ int psim_closures_midnight(psim_ctx* ctx, uint32_t t, const psim_day_stats* row)
  * locations/switch are open (previousOpenState); either pointer may be NULL. */
 int psim_closures_status(psim_ctx* ctx, uint8_t* cond_active /* [n_rules] */, uint8_t* rule_open /* [n_rules] */,
                          uint32_t* n_rules);
+/* The policy switches of Simulation::processFlags (simulation.h:779-897) that
+ * act on the locations, for the runForDay binding (matlab/mexPanSim.cpp:92-126):
+ * the non-essential locations of the listed types (at most 10) become open
+ * or closed ("PLNONE" / "PL0"), and the weight of every non-home location is
+ * divided (divide != 0) or multiplied by coef in double precision ("MA1.0" /
+ * "MA0.8"). */
+int psim_set_types_open(psim_ctx* ctx, const uint32_t* types, uint32_t n_types, int open);
+int psim_scale_location_weights(psim_ctx* ctx, double coef, int divide);
 /* Immunization (include/immunization.h:24-900): categories, first doses in
  * category order, booster rounds by age group, and the daily waning of
  * susceptibility and symptom scaling of susceptible agents.  The location

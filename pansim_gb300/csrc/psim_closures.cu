@@ -516,6 +516,35 @@ int psim_closures_midnight(psim_ctx* c, uint32_t t, const psim_day_stats* row) {
     return closures_apply(c, t, row);
 }
 
+// processFlags' location closures (simulation.h:794-828): the non-essential
+// locations of the listed types open or closed
+int psim_set_types_open(psim_ctx* c, const uint32_t* types, uint32_t n_types, int open) {
+    if (!c || (n_types && !types)) return PSIM_ERR_ARG;
+    if (!c->uploaded) return PSIM_ERR_STATE;
+    ClosureTypes ty{};
+    if (n_types > sizeof(ty.v) / sizeof(ty.v[0])) return fail(c, PSIM_ERR_ARG, "too many location types");
+    ty.n = n_types;
+    for (uint32_t q = 0; q < n_types; ++q) ty.v[q] = types[q];
+    launch_close_types(c->k, ty, open ? 1 : 0, c->stream);
+    c->launches += 1;
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(c, PSIM_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+    return check_device_err(c);
+}
+
+// processFlags' masks (simulation.h:846-891): the weight of every non-home
+// location divided (divide != 0) or multiplied by coef, in double precision
+int psim_scale_location_weights(psim_ctx* c, double coef, int divide) {
+    if (!c) return PSIM_ERR_ARG;
+    if (!c->uploaded) return PSIM_ERR_STATE;
+    if (!(coef > 0.0)) return fail(c, PSIM_ERR_ARG, "coef must be positive");
+    launch_masks(c->k, c->params.home_type, coef, divide ? 1 : 0, c->stream);
+    c->launches += 1;
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(c, PSIM_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+    return check_device_err(c);
+}
+
 int psim_closures_status(psim_ctx* c, uint8_t* cond_active, uint8_t* rule_open, uint32_t* n_rules) {
     if (!c) return PSIM_ERR_ARG;
     const ClosureEngine* E = c->closures;

@@ -60,6 +60,8 @@ def lib(auto_build=True):
         L.psim_closures_init.argtypes = [P, P, U32, C.c_char_p, I]
         L.psim_closures_midnight.argtypes = [P, U32, P]
         L.psim_closures_status.argtypes = [P, P, P, P]
+        L.psim_set_types_open.argtypes = [P, P, U32, I]
+        L.psim_scale_location_weights.argtypes = [P, C.c_double, I]
         L.psim_get_params.argtypes = [P, P]
         L.psim_immunization_init.argtypes = [P, P]
         L.psim_immunize_day.argtypes = [P, U32, P]
@@ -222,6 +224,17 @@ class GpuSim:
         self._rules = arr
         self._ck(lib().psim_closures_init(self.h, arr, len(arr), header.encode(), 1 if enable_closures else 0),
                  "closures_init")
+
+    def closures_midnight(self, t, row):
+        """The closure rules on a statistics row (a psim_day_stats)."""
+        self._ck(lib().psim_closures_midnight(self.h, t, C.byref(row)), "closures_midnight")
+
+    def set_types_open(self, types, open_):
+        ty = np.ascontiguousarray(types, dtype=np.uint32)
+        self._ck(lib().psim_set_types_open(self.h, _p(ty), len(ty), 1 if open_ else 0), "set_types_open")
+
+    def scale_location_weights(self, coef, divide):
+        self._ck(lib().psim_scale_location_weights(self.h, float(coef), 1 if divide else 0), "scale_location_weights")
 
     def closures_status(self):
         n = C.c_uint32(0)
