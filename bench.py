@@ -40,7 +40,7 @@ STEP_BYTES = (32, 20)
 # replica = 30 B/location
 KERNEL_BYTES = {"movement": (20, 4), "scan": (0, 30), "step_fused": (38, 0), "step_hot": (16, 8),
                 "step_cold": None}
-KERNEL_LABELS = {"step_fused": "k_step_fused", "step_hot": "k_step_hot", "step_cold": "k_step_cold"}
+KERNEL_LABELS = {"step_fused": "k_step_fused", "step_hot": "k_slots + k_step_hot", "step_cold": "k_step_cold"}
 
 
 def scan_label(tuning):

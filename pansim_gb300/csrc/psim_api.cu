@@ -262,7 +262,24 @@ int capture_day_graph(psim_ctx* c) {
         me = cudaMemsetAsync(c->k.l.smask, 0xFF, sizeof(uint32_t) * (((size_t)c->L + 2047) / 2048 * 64 + 64), c->stream);
     launch_movement(c->k, 0, c->stream);
     mark();
+    // the hot/cold variants outside profiling: the hot kernel reads only the
+    // hazard mask of the scan's outputs, and the mask holds a superset of the
+    // infectious locations before the scan (every added term marks its
+    // location), so the hot kernel runs on a second branch beside the scan
+    // and the agent list's slots; the cold kernel joins them
+    const bool fork = !c->profile && step_fused_kernels(c->k) == 3;
     for (uint32_t s = 0; s < c->spd; ++s) {
+        if (fork && s + 1 < c->spd) {
+            if (me == cudaSuccess) me = cudaEventRecord(c->fork_ev, c->stream);
+            if (me == cudaSuccess) me = cudaStreamWaitEvent(c->stream2, c->fork_ev, 0);
+            launch_step_fused(c->k, s, c->stream2, 2);
+            launch_scan(c->k, s, 1, merge_q, c->stream);
+            launch_step_fused(c->k, s, c->stream, 3);
+            if (me == cudaSuccess) me = cudaEventRecord(c->join_ev, c->stream2);
+            if (me == cudaSuccess) me = cudaStreamWaitEvent(c->stream, c->join_ev, 0);
+            launch_step_fused(c->k, s, c->stream, 1);
+            continue;
+        }
         launch_scan(c->k, s, 1, merge_q, c->stream);
         mark();
         if (s + 1 < c->spd)
@@ -418,6 +435,10 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     if (e != cudaSuccess) return bail(fail(c, PSIM_ERR_CUDA, std::string("stream: ") + cudaGetErrorString(e)));
     cudaEventCreate(&c->ev0);
     cudaEventCreate(&c->ev1);
+    e = cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming);
+    if (e != cudaSuccess) return bail(fail(c, PSIM_ERR_CUDA, std::string("stream: ") + cudaGetErrorString(e)));
     const size_t N = c->N, L = c->L, V = c->V, R = c->R;
     KArgs& k = c->k;
     // model tables
@@ -618,6 +639,9 @@ int psim_destroy(psim_ctx* c) {
     for (void* p : c->allocs) cudaFree(p);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->fork_ev) cudaEventDestroy(c->fork_ev);
+    if (c->join_ev) cudaEventDestroy(c->join_ev);
+    if (c->stream2) cudaStreamDestroy(c->stream2);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return 0;

@@ -30,6 +30,10 @@ struct psim_ctx {
     psim::OtherDiseaseEngine* other_disease = nullptr;
     int device = 0;
     cudaStream_t stream = nullptr;
+    // the day graph's second branch (the hot kernel beside the scan) and its
+    // fork / join events
+    cudaStream_t stream2 = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     std::string err;
     KArgs k{};
     std::vector<void*> allocs;

@@ -434,6 +434,15 @@ __device__ __forceinline__ void move_agent(const KArgs& k, uint32_t i, const Ste
 // choice); the masks hold one 32-bit word per warp and item.
 constexpr int SCAN_THREADS = 256;
 
+// A location that receives an infectious term sets its hazard-mask bit at
+// once; the next scan recomputes the bit from the sums.  Between the two the
+// mask is a superset of the infectious locations, which is what the hot
+// kernel reads while the scan runs beside it (a location whose sum is zero
+// has hazard 0 after the scan, so an agent queued there draws nothing).
+__device__ __forceinline__ void mark_hazardous(const KArgs& k, uint32_t loc) {
+    atomicOr(&k.l.hmask[loc >> 5], 1u << (loc & 31u));
+}
+
 // The full pass of a day's first step (k_movement, after a reset of the
 // sums): an agent whose location changed from loc0 to loc moves one count
 // (two fire-and-forget reductions), and every infectious agent adds its term
@@ -455,6 +464,7 @@ __device__ __forceinline__ bool count_agent(const KArgs& k, bool act, uint32_t l
         const long long q = __float2ll_rn(inf * PSIM_FIX_SCALE_F);
         atomicAdd(&k.l.sfix[(size_t)variant * L + loc], (unsigned long long)q);
         atomicOr(&k.l.smask[loc >> 5], 1u << (loc & 31u));
+        mark_hazardous(k, loc);
     }
     return mv;
 }
@@ -501,6 +511,7 @@ __device__ __forceinline__ bool count_agent_delta(const KArgs& k, bool act, uint
             if (q1) {
                 atomicAdd(&k.l.sfix[(size_t)var * L + loc], (unsigned long long)q1);
                 mark_dirty(k, loc);
+                mark_hazardous(k, loc);
             }
         }
     }
@@ -520,6 +531,7 @@ __device__ __forceinline__ void count_full(const KArgs& k, bool act, uint32_t lo
         const long long q = __float2ll_rn(inf * PSIM_FIX_SCALE_F);
         atomicAdd(&k.l.sfix[(size_t)variant * L + loc], (unsigned long long)q);
         atomicOr(&k.l.smask[loc >> 5], 1u << (loc & 31u));
+        mark_hazardous(k, loc);
     }
 }
 
@@ -1259,7 +1271,6 @@ __global__ void __launch_bounds__(256, 8) k_step_hot(KArgs k, uint32_t step, uin
     const uint32_t dt = k.p.time_step;
     const uint32_t minutes = (step + 1) * dt;
     const bool curfew_now = k.p.enable_curfew && k.p.curfew_begin == minutes / dt;
-    const bool rebuild = csr_rebuild(k, k.clock->t0 + step);
     const uint32_t stride = gridDim.x * blockDim.x;
     uint32_t* seg = k.a.worklist + (size_t)blockIdx.x * cap;
     uint32_t* segl = k.a.worklist_loc + (size_t)blockIdx.x * cap;
@@ -1284,8 +1295,6 @@ __global__ void __launch_bounds__(256, 8) k_step_hot(KArgs k, uint32_t step, uin
         const bool ok = act && loc0 < L;
         bool hz = false;
         if (ok) hazard_at(k, loc0, &hz);
-        const uint32_t pos = take_slot(k, ok, loc0, rebuild);
-        if (ok) store_slot(k, pos, i);
         // movers (countdown at zero, curfew) go to the cold kernel whole;
         // the others count down here and go there only to draw (or to
         // report an invalid location)
@@ -1306,6 +1315,23 @@ __global__ void __launch_bounds__(256, 8) k_step_hot(KArgs k, uint32_t step, uin
     }
     __syncthreads();
     if (threadIdx.x == 0) k.a.seg_count[blockIdx.x] = s_cnt;
+}
+
+// The agent list of a step whose agents took new locations (k_step_hot's
+// variants): every agent takes a slot at its location, whose cursor the
+// scan set to the location's first slot.  Returns at once when the step
+// keeps the agent list of the step before.
+__global__ void __launch_bounds__(256, 8) k_slots(KArgs k, uint32_t step) {
+    if (!csr_rebuild(k, k.clock->t0 + step)) return;
+    const uint32_t N = k.a.n, L = k.l.n;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < N; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        const bool act = i < N;
+        const uint32_t loc = act ? k.a.location[i] : NONE;
+        const bool ok = act && loc < L;
+        const uint32_t pos = take_slot(k, ok, loc, true);
+        if (ok) store_slot(k, pos, i);
+    }
 }
 
 // k_step_hot with U agents per thread in flight: the loads, mask reads and
@@ -2175,8 +2201,11 @@ void launch_movement(const KArgs& k, uint32_t step, cudaStream_t s) {
 // register-capped instantiations of the fused step kernel: a tighter cap
 // raises occupancy for the hot path and spills on the rare cold path; the
 // autotuner picks one (DevTune::variant)
-// part: -1 both kernels of the step; 0 the first (the fused kernel, or the hot
-// kernel of variant 3); 1 the second (the cold kernel of variant 3, else nothing)
+// part: -1 every kernel of the step; 0 the first (the fused kernel; for the
+// hot/cold variants 3, 7-9 the agent list's slots, then the hot kernel);
+// 1 the cold kernel of a hot/cold variant (else nothing); 2 the hot kernel
+// of variants 3, 7-9 alone; 3 their slots alone (2 and 3 let the day graph
+// run the hot kernel beside the scan)
 void launch_step_fused(const KArgs& k, uint32_t step, cudaStream_t s, int part) {
     static unsigned g[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     const uint32_t v = k.tune.variant < 10 ? k.tune.variant : 0;
@@ -2208,10 +2237,11 @@ void launch_step_fused(const KArgs& k, uint32_t step, cudaStream_t s, int part) 
         // one work-list segment per hot block, as many as the block visits
         const unsigned grid = std::min(agent_grid(k, g[3]), (unsigned)WORK_MAX_BLOCKS);
         const uint32_t cap = (uint32_t)((((size_t)k.a.n + (size_t)grid * 256 - 1) / ((size_t)grid * 256)) * 256);
-        if (part != 1) k_step_hot<<<grid, 256, 0, s>>>(k, step, cap);
+        if (part == -1 || part == 0 || part == 3) k_slots<<<grid, 256, 0, s>>>(k, step);
+        if (part == -1 || part == 0 || part == 2) k_step_hot<<<grid, 256, 0, s>>>(k, step, cap);
         // the cold agents are a few percent: at most one wave of cold blocks,
         // each taking segments in turn
-        if (part != 0) {
+        if (part == -1 || part == 1) {
             const size_t sh = (grid + 1) * sizeof(uint32_t);
             if (v == 7)
                 k_step_cold_spread<4><<<g[8], 256, sh, s>>>(k, step, cap, grid);
@@ -2244,7 +2274,8 @@ void launch_step_fused(const KArgs& k, uint32_t step, cudaStream_t s, int part) 
         k_step_fused<8><<<grid, 256, 0, s>>>(k, step);
 }
 int step_fused_kernels(const KArgs& k) {
-    return k.tune.variant == 3 || (k.tune.variant >= 6 && k.tune.variant <= 9) ? 2 : 1;
+    const uint32_t v = k.tune.variant;
+    return v == 3 || (v >= 7 && v <= 9) ? 3 : v == 6 ? 2 : 1;
 }
 void launch_count(const KArgs& k, cudaStream_t s) { k_count<<<grid_for(k.a.n, 8), 256, 0, s>>>(k); }
 // the scan of the histogram with 256 x tune.scan_items locations per tile:
