@@ -102,7 +102,9 @@ double seasonality(const psim_params& p, uint32_t t, uint32_t spd) {
 }
 
 // set the device clock for the day containing t
-int set_clock(psim_ctx* c, uint32_t t) {
+// sync = false: the copy is left in the stream; the caller synchronises
+// before the next set_clock (the copy reads the pinned clock when it runs)
+int set_clock(psim_ctx* c, uint32_t t, bool sync = true) {
     uint32_t t0 = t - t % c->spd;
     DevClock nc = c->h_clock;
     nc.t0 = t0;
@@ -112,9 +114,10 @@ int set_clock(psim_ctx* c, uint32_t t) {
         nc.season == c->h_clock.season)
         return 0;
     c->h_clock = nc;
+    *c->h_clock_pin = nc;
     // only the first three fields; the scan bookkeeping stays on the device
-    CK(cudaMemcpyAsync(c->k.clock, &c->h_clock, 3 * sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpyAsync(c->k.clock, c->h_clock_pin, 3 * sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream));
+    if (sync) CK(cudaStreamSynchronize(c->stream));
     c->clock_valid = true;
     return 0;
 }
@@ -603,8 +606,20 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     k.tune.agg_slot = 0;
     k.tune.blocks_per_sm = 4;
     k.tune.variant = 3;
-    c->h_stats.resize(R);
-    c->h_expected.assign(R, 0.0);
+    {
+        const size_t b_stats = sizeof(DevStatsAcc) * R, b_exp = sizeof(double) * R;
+        const size_t bytes = b_stats + b_exp + sizeof(DevClock) + 64;
+        if (cudaMallocHost(&c->pinned, bytes) != cudaSuccess) {
+            c->pinned = nullptr;
+            return bail(fail(c, PSIM_ERR_ALLOC, "pinned host buffers"));
+        }
+        std::memset(c->pinned, 0, bytes);
+        char* p = (char*)c->pinned;
+        c->h_stats = (DevStatsAcc*)p;
+        c->h_expected = (double*)(p + b_stats);
+        c->h_clock_pin = (DevClock*)(p + b_stats + b_exp);
+        c->h_err_pin = (uint32_t*)(p + b_stats + b_exp + sizeof(DevClock) + 32);
+    }
     // healthcare workers per replica (Simulation::flagHealthcareWorkers, simulation.h:670-693)
     c->hcw_count.assign(R, 0u);
     for (uint32_t q = 0; q < c->R; ++q)
@@ -639,6 +654,7 @@ int psim_destroy(psim_ctx* c) {
     for (void* p : c->allocs) cudaFree(p);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->pinned) cudaFreeHost(c->pinned);
     if (c->fork_ev) cudaEventDestroy(c->fork_ev);
     if (c->join_ev) cudaEventDestroy(c->join_ev);
     if (c->stream2) cudaStreamDestroy(c->stream2);
@@ -926,7 +942,7 @@ int psim_test_day(psim_ctx* c, uint32_t t, uint32_t* tpp) {
     if (tpp) {
         launch_stats(c->k, t, c->stream);
         c->launches += 2;
-        CK(cudaMemcpyAsync(c->h_stats.data(), c->k.stats, sizeof(DevStatsAcc) * c->R, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaMemcpyAsync(c->h_stats, c->k.stats, sizeof(DevStatsAcc) * c->R, cudaMemcpyDeviceToHost, c->stream));
         CK(cudaStreamSynchronize(c->stream));
         for (uint32_t q = 0; q < c->R; ++q) {
             tpp[3 * q + 0] = c->h_stats[q].c[SC_TESTS];
@@ -952,8 +968,8 @@ int psim_stats_day(psim_ctx* c, uint32_t t, psim_day_stats* out) {
     c->launches += 2;
     int rc = launch_check(c);
     if (rc) return rc;
-    CK(cudaMemcpyAsync(c->h_stats.data(), c->k.stats, sizeof(DevStatsAcc) * c->R, cudaMemcpyDeviceToHost, c->stream));
-    CK(cudaMemcpyAsync(c->h_expected.data(), c->k.r.expected, sizeof(double) * c->R, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(c->h_stats, c->k.stats, sizeof(DevStatsAcc) * c->R, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(c->h_expected, c->k.r.expected, sizeof(double) * c->R, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemsetAsync(c->k.r.expected, 0, sizeof(double) * c->R, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     if (out) assemble_stats(c, t, out);
@@ -1013,9 +1029,52 @@ int psim_run_steps(psim_ctx* c, uint32_t day) {
 }
 
 int psim_run_day(psim_ctx* c, uint32_t day, psim_day_stats* out) {
-    int rc = psim_midnight(c, day * (c ? c->spd : 144), out);
-    if (rc) return rc;
-    return psim_run_steps(c, day);
+    if (!c) return PSIM_ERR_ARG;
+    if (!c->uploaded) return PSIM_ERR_STATE;
+    const uint32_t t = day * c->spd;
+    if (c->closures || c->immunization || c->other_disease) {
+        // host logic between the midnight phases (rules on the statistics
+        // row, dose budgets): phase by phase
+        int rc = psim_midnight(c, t, out);
+        if (rc) return rc;
+        return psim_run_steps(c, day);
+    }
+    // The midnight phases, the clock and the day graph in stream order with
+    // one synchronisation at the end: the statistics and the error flags come
+    // back through pinned buffers.
+    int rc = 0;
+    if (c->graph_dirty || !c->day_graph) {
+        if ((rc = capture_day_graph(c))) return rc;
+    }
+    if (t > 0 && c->params.testing_enabled) {
+        launch_test(c->k, t, c->stream);
+        c->launches += 2;
+    }
+    if (t > 0) {
+        launch_progress(c->k, t, c->stream);
+        c->launches += 1;
+    }
+    launch_stats(c->k, t, c->stream);
+    c->launches += 2;
+    CK(cudaMemcpyAsync(c->h_stats, c->k.stats, sizeof(DevStatsAcc) * c->R, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(c->h_expected, c->k.r.expected, sizeof(double) * c->R, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemsetAsync(c->k.r.expected, 0, sizeof(double) * c->R, c->stream));
+    launch_plan(c->k, t, c->stream);
+    c->launches += 5 + (c->params.quarantine_policy > 3 && c->k.l.n_schools ? 1 : 0);
+    if ((rc = launch_check(c))) return rc;
+    if ((rc = set_clock(c, t, false))) return rc;
+    CK(cudaEventRecord(c->ev0, c->stream));
+    CK(cudaGraphLaunch(c->day_graph, c->stream));
+    CK(cudaEventRecord(c->ev1, c->stream));
+    CK(cudaMemcpyAsync(c->h_err_pin, c->k.err, sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaEventElapsedTime(&c->last_ms, c->ev0, c->ev1));
+    c->launches += c->graph_kernels;
+    c->prof_valid = c->profile;
+    c->csr_fresh = false;
+    if (*c->h_err_pin) return check_device_err(c);
+    if (out) assemble_stats(c, t, out);
+    return 0;
 }
 
 int psim_get_csr(psim_ctx* c, int canonical, uint32_t* offsets, uint32_t* agents) {

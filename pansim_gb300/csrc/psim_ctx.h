@@ -55,8 +55,14 @@ struct psim_ctx {
     uint64_t launches = 0;
     bool uploaded = false;
     bool csr_fresh = false;      // counts of the current positions are built
-    std::vector<DevStatsAcc> h_stats;
-    std::vector<double> h_expected;
+    // pinned host memory (one block): the statistics accumulators and the
+    // expected-infection sums copied back, the clock copied in, the error
+    // flags copied back, so that a day needs no synchronisation in between
+    void* pinned = nullptr;
+    DevStatsAcc* h_stats = nullptr;   // [R]
+    double* h_expected = nullptr;     // [R]
+    DevClock* h_clock_pin = nullptr;
+    uint32_t* h_err_pin = nullptr;
     // adjoint
     double* d_adj_weight = nullptr;
     double* d_grad = nullptr;
