@@ -1321,16 +1321,37 @@ __global__ void __launch_bounds__(256, 8) k_step_hot(KArgs k, uint32_t step, uin
 // variants): every agent takes a slot at its location, whose cursor the
 // scan set to the location's first slot.  Returns at once when the step
 // keeps the agent list of the step before.
+// With plain slot atomics each thread has SLOT_ILP agents' atomics in flight
+// (their returns are what the pass waits for); the warp-aggregated form
+// (tune.agg_slot) takes one agent per thread and trip.
+constexpr int SLOT_ILP = 4;
 __global__ void __launch_bounds__(256, 8) k_slots(KArgs k, uint32_t step) {
     if (!csr_rebuild(k, k.clock->t0 + step)) return;
     const uint32_t N = k.a.n, L = k.l.n;
-    for (uint32_t base = blockIdx.x * blockDim.x; base < N; base += gridDim.x * blockDim.x) {
-        const uint32_t i = base + threadIdx.x;
-        const bool act = i < N;
-        const uint32_t loc = act ? k.a.location[i] : NONE;
-        const bool ok = act && loc < L;
-        const uint32_t pos = take_slot(k, ok, loc, true);
-        if (ok) store_slot(k, pos, i);
+    if (k.tune.agg_slot) {
+        for (uint32_t base = blockIdx.x * blockDim.x; base < N; base += gridDim.x * blockDim.x) {
+            const uint32_t i = base + threadIdx.x;
+            const bool act = i < N;
+            const uint32_t loc = act ? k.a.location[i] : NONE;
+            const bool ok = act && loc < L;
+            const uint32_t pos = take_slot(k, ok, loc, true);
+            if (ok) store_slot(k, pos, i);
+        }
+        return;
+    }
+    const uint32_t tile = blockDim.x * SLOT_ILP;
+    for (uint32_t base = blockIdx.x * tile; base < N; base += gridDim.x * tile) {
+        uint32_t loc[SLOT_ILP], pos[SLOT_ILP];
+#pragma unroll
+        for (int u = 0; u < SLOT_ILP; ++u) {
+            const uint32_t i = base + u * blockDim.x + threadIdx.x;
+            loc[u] = i < N ? k.a.location[i] : NONE;
+        }
+#pragma unroll
+        for (int u = 0; u < SLOT_ILP; ++u) pos[u] = loc[u] < L ? atomicAdd(&k.l.cursor[loc[u]], 1u) : NONE;
+#pragma unroll
+        for (int u = 0; u < SLOT_ILP; ++u)
+            if (loc[u] < L) store_slot(k, pos[u], base + u * blockDim.x + threadIdx.x);
     }
 }
 
