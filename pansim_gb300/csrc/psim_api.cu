@@ -268,18 +268,27 @@ int capture_day_graph(psim_ctx* c) {
     // the hot/cold variants outside profiling: the hot kernel reads only the
     // hazard mask of the scan's outputs, and the mask holds a superset of the
     // infectious locations before the scan (every added term marks its
-    // location), so the hot kernel runs on a second branch beside the scan
-    // and the agent list's slots; the cold kernel joins them
+    // location), so the hot kernel runs on a second branch beside the scan;
+    // the cold kernel joins them.  On a step that rebuilds the agent list the hot kernel records the
+    // agents' locations, and the slots run after the scan and the hot kernel,
+    // beside the cold kernel; the next step starts after both.
     const bool fork = !c->profile && step_fused_kernels(c->k) == 3;
+    bool slots_pending = false;
     for (uint32_t s = 0; s < c->spd; ++s) {
+        if (slots_pending && me == cudaSuccess) me = cudaStreamWaitEvent(c->stream, c->slots_ev, 0);
+        slots_pending = false;
         if (fork && s + 1 < c->spd) {
             if (me == cudaSuccess) me = cudaEventRecord(c->fork_ev, c->stream);
             if (me == cudaSuccess) me = cudaStreamWaitEvent(c->stream2, c->fork_ev, 0);
             launch_step_fused(c->k, s, c->stream2, 2);
             launch_scan(c->k, s, 1, merge_q, c->stream);
-            launch_step_fused(c->k, s, c->stream, 3);
             if (me == cudaSuccess) me = cudaEventRecord(c->join_ev, c->stream2);
             if (me == cudaSuccess) me = cudaStreamWaitEvent(c->stream, c->join_ev, 0);
+            if (me == cudaSuccess) me = cudaEventRecord(c->both_ev, c->stream);
+            if (me == cudaSuccess) me = cudaStreamWaitEvent(c->stream2, c->both_ev, 0);
+            launch_step_fused(c->k, s, c->stream2, 3);
+            if (me == cudaSuccess) me = cudaEventRecord(c->slots_ev, c->stream2);
+            slots_pending = true;
             launch_step_fused(c->k, s, c->stream, 1);
             continue;
         }
@@ -441,6 +450,8 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     e = cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->both_ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->slots_ev, cudaEventDisableTiming);
     if (e != cudaSuccess) return bail(fail(c, PSIM_ERR_CUDA, std::string("stream: ") + cudaGetErrorString(e)));
     const size_t N = c->N, L = c->L, V = c->V, R = c->R;
     KArgs& k = c->k;
@@ -515,7 +526,7 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     AL(st_hospitalized_until, N) AL(st_immunization_ts, N) AL(st_recovered_ts, N) AL(st_variant_mask, N)
     AL(st_immunization_count, N) AL(st_infected_count, N) AL(st_worst_state, N) AL(hcw, N) AL(rank, N)
     AL(worklist, (size_t)N + (size_t)WORK_MAX_BLOCKS * 256) AL(worklist_loc, (size_t)N + (size_t)WORK_MAX_BLOCKS * 256)
-    AL(seg_count, WORK_MAX_BLOCKS)
+    AL(seg_count, WORK_MAX_BLOCKS) AL(slot_loc, N)
     AL(imm_round, N) AL(scaling_v, (size_t)N * V)
 #undef AL
     // locations
@@ -657,6 +668,8 @@ int psim_destroy(psim_ctx* c) {
     if (c->pinned) cudaFreeHost(c->pinned);
     if (c->fork_ev) cudaEventDestroy(c->fork_ev);
     if (c->join_ev) cudaEventDestroy(c->join_ev);
+    if (c->both_ev) cudaEventDestroy(c->both_ev);
+    if (c->slots_ev) cudaEventDestroy(c->slots_ev);
     if (c->stream2) cudaStreamDestroy(c->stream2);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;

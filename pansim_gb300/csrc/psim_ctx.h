@@ -33,7 +33,7 @@ struct psim_ctx {
     // the day graph's second branch (the hot kernel beside the scan) and its
     // fork / join events
     cudaStream_t stream2 = nullptr;
-    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr, both_ev = nullptr, slots_ev = nullptr;
     std::string err;
     KArgs k{};
     std::vector<void*> allocs;

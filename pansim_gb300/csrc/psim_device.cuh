@@ -97,6 +97,9 @@ struct DevAgents {
     uint32_t* worklist_loc;       // beside each: its location (low 30 bits, WORK_LOC_MASK for an
                                   // invalid one) | WORK_HZ | WORK_MOVE
     uint32_t* seg_count;          // queued agents per segment
+    uint32_t* slot_loc;           // [N] the agents' locations at a step that rebuilds the agent
+                                  // list, recorded by the hot kernel for k_slots (which runs
+                                  // beside the cold kernel, whose movers rewrite `location`)
 };
 
 struct DevLocs {
@@ -239,6 +242,13 @@ __device__ __forceinline__ bool csr_decide(const KArgs& k, uint32_t t) {
 }
 // the decision, in the later kernels of the step at t
 __device__ __forceinline__ bool csr_rebuild(const KArgs& k, uint32_t t) { return k.l.build[2] == t; }
+// the same decision from the words csr_decide reads, for a kernel that runs
+// beside the first scan kernel (block 0's turning BUILD_PENDING into t leaves
+// it unchanged)
+__device__ __forceinline__ bool csr_peek(const KArgs& k, uint32_t t) {
+    const uint32_t moved = k.l.build[0], force = k.l.build[1];
+    return moved == t || force == t || force == BUILD_PENDING;
+}
 // movers of a block publish the timestamp of their new locations (one store
 // per block; every thread of the block calls this)
 __device__ __forceinline__ void publish_moved(const KArgs& k, bool any, uint32_t t_new) {

@@ -1271,6 +1271,8 @@ __global__ void __launch_bounds__(256, 8) k_step_hot(KArgs k, uint32_t step, uin
     const uint32_t dt = k.p.time_step;
     const uint32_t minutes = (step + 1) * dt;
     const bool curfew_now = k.p.enable_curfew && k.p.curfew_begin == minutes / dt;
+    // a step that rebuilds the agent list: the locations for k_slots
+    const bool rebuild = csr_peek(k, k.clock->t0 + step);
     const uint32_t stride = gridDim.x * blockDim.x;
     uint32_t* seg = k.a.worklist + (size_t)blockIdx.x * cap;
     uint32_t* segl = k.a.worklist_loc + (size_t)blockIdx.x * cap;
@@ -1295,6 +1297,7 @@ __global__ void __launch_bounds__(256, 8) k_step_hot(KArgs k, uint32_t step, uin
         const bool ok = act && loc0 < L;
         bool hz = false;
         if (ok) hazard_at(k, loc0, &hz);
+        if (rebuild && act) k.a.slot_loc[i] = loc0;
         // movers (countdown at zero, curfew) go to the cold kernel whole;
         // the others count down here and go there only to draw (or to
         // report an invalid location)
@@ -1318,8 +1321,9 @@ __global__ void __launch_bounds__(256, 8) k_step_hot(KArgs k, uint32_t step, uin
 }
 
 // The agent list of a step whose agents took new locations (k_step_hot's
-// variants): every agent takes a slot at its location, whose cursor the
-// scan set to the location's first slot.  Returns at once when the step
+// variants): every agent takes a slot at the location k_step_hot recorded
+// for it, whose cursor the scan set to the location's first slot.  It runs
+// after both and beside the cold kernel.  Returns at once when the step
 // keeps the agent list of the step before.
 // With plain slot atomics each thread has SLOT_ILP agents' atomics in flight
 // (their returns are what the pass waits for); the warp-aggregated form
@@ -1332,7 +1336,7 @@ __global__ void __launch_bounds__(256, 8) k_slots(KArgs k, uint32_t step) {
         for (uint32_t base = blockIdx.x * blockDim.x; base < N; base += gridDim.x * blockDim.x) {
             const uint32_t i = base + threadIdx.x;
             const bool act = i < N;
-            const uint32_t loc = act ? k.a.location[i] : NONE;
+            const uint32_t loc = act ? k.a.slot_loc[i] : NONE;
             const bool ok = act && loc < L;
             const uint32_t pos = take_slot(k, ok, loc, true);
             if (ok) store_slot(k, pos, i);
@@ -1345,7 +1349,7 @@ __global__ void __launch_bounds__(256, 8) k_slots(KArgs k, uint32_t step) {
 #pragma unroll
         for (int u = 0; u < SLOT_ILP; ++u) {
             const uint32_t i = base + u * blockDim.x + threadIdx.x;
-            loc[u] = i < N ? k.a.location[i] : NONE;
+            loc[u] = i < N ? k.a.slot_loc[i] : NONE;
         }
 #pragma unroll
         for (int u = 0; u < SLOT_ILP; ++u) pos[u] = loc[u] < L ? atomicAdd(&k.l.cursor[loc[u]], 1u) : NONE;
@@ -2223,10 +2227,10 @@ void launch_movement(const KArgs& k, uint32_t step, cudaStream_t s) {
 // raises occupancy for the hot path and spills on the rare cold path; the
 // autotuner picks one (DevTune::variant)
 // part: -1 every kernel of the step; 0 the first (the fused kernel; for the
-// hot/cold variants 3, 7-9 the agent list's slots, then the hot kernel);
+// hot/cold variants 3, 7-9 the hot kernel, then the agent list's slots);
 // 1 the cold kernel of a hot/cold variant (else nothing); 2 the hot kernel
 // of variants 3, 7-9 alone; 3 their slots alone (2 and 3 let the day graph
-// run the hot kernel beside the scan)
+// run the hot kernel beside the scan and the slots beside the cold kernel)
 void launch_step_fused(const KArgs& k, uint32_t step, cudaStream_t s, int part) {
     static unsigned g[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     const uint32_t v = k.tune.variant < 10 ? k.tune.variant : 0;
@@ -2258,8 +2262,8 @@ void launch_step_fused(const KArgs& k, uint32_t step, cudaStream_t s, int part) 
         // one work-list segment per hot block, as many as the block visits
         const unsigned grid = std::min(agent_grid(k, g[3]), (unsigned)WORK_MAX_BLOCKS);
         const uint32_t cap = (uint32_t)((((size_t)k.a.n + (size_t)grid * 256 - 1) / ((size_t)grid * 256)) * 256);
-        if (part == -1 || part == 0 || part == 3) k_slots<<<grid, 256, 0, s>>>(k, step);
         if (part == -1 || part == 0 || part == 2) k_step_hot<<<grid, 256, 0, s>>>(k, step, cap);
+        if (part == -1 || part == 0 || part == 3) k_slots<<<grid, 256, 0, s>>>(k, step);
         // the cold agents are a few percent: at most one wave of cold blocks,
         // each taking segments in turn
         if (part == -1 || part == 1) {
