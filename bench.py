@@ -30,7 +30,9 @@ N_OTHER_LOCS = 500_000
 METRIC = "agent-steps/s at 2M agents"
 UNIT = "agent-steps/s"
 # algorithmic bytes per step (per agent, per location) of the whole step,
-# 32*N + 20*L, and of each kernel of the step
+# 32*N + 20*L: the reference's step touches, per agent, the countdown (read and
+# write, 8), the agent list (12) and the infection inputs (12); per location the
+# offsets (8) and the reduction's inputs and output (12).  Then each kernel's.
 STEP_BYTES = (32, 20)
 # k_step_fused: location, rank, steps (r+w), infectiousness, replica, CSR offset
 # and hazard gathers, CSR and rank writes = 38 B/agent; k_step_hot: location,

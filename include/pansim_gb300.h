@@ -190,7 +190,7 @@ typedef struct psim_params {
     float sigma_band[PSIM_MAX_BANDS]; /* age-band susceptibility, 1 = reference */
 } psim_params;
 
-/* Replicas batched in one context (BASELINE-style ensembles).  Agents and
+/* Replicas batched in one context (ensembles of uneven populations).  Agents and
  * locations of replica r occupy [agent_offset[r], agent_offset[r+1]) and
  * [loc_offset[r], loc_offset[r+1]); location indices in the snapshot are
  * global.  Each replica has its own Philox key and infection coefficient;
@@ -401,8 +401,9 @@ int psim_run_day(psim_ctx* ctx, uint32_t day, psim_day_stats* out /* [replicas] 
 int psim_set_tuning(psim_ctx* ctx, const psim_tuning* tuning);
 int psim_get_tuning(psim_ctx* ctx, psim_tuning* tuning);
 
-/* Differentiable calibration (no counterpart in the reference; SURVEY
- * config 5).  theta = (k, location-type weights, age-band susceptibilities).
+/* Differentiable calibration (no counterpart in the reference: the gradient of
+ * expected daily new infections over replicas and days).
+ * theta = (k, location-type weights, age-band susceptibilities).
  * w_l = w_by_type[type_l]; slot_of_type[type] = weight slot 0..7 of that type
  * in the gradient (-1: not a parameter; NULL keeps the current table). */
 int psim_set_type_weights(psim_ctx* ctx, const float* w_by_type /*[256]*/, const int8_t* slot_of_type /*[256]*/);
