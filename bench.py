@@ -145,24 +145,25 @@ def make_snapshot(rank):
 
 
 def pinned_copy(snap):
-    """Snapshot whose mutable arrays live in pinned host memory (torch.pin_memory)."""
+    """Snapshot whose mutable arrays live in one block of pinned host memory
+    (torch.pin_memory), laid out as the library's device state
+    (native.state_layout), so that an upload or a download is one copy."""
     import torch
+    from pansim_gb300 import native
     from pansim_gb300.snapshot import AGENT_MUTABLE, LOC_MUTABLE
     s = snap.copy()
-    pins = []
-
-    def pin(a):
-        t = torch.empty(max(a.nbytes, 1), dtype=torch.uint8, pin_memory=True)
-        v = t.numpy()[: a.nbytes].view(a.dtype).reshape(a.shape)
+    fields = [(s.agents, k) for k in AGENT_MUTABLE] + [(s.locs, k) for k in LOC_MUTABLE]
+    off = native.state_layout(s.n_agents, s.n_locations, int(s.model["n_variants"]))
+    assert len(off) == len(fields) + 1
+    t = torch.empty(max(int(off[-1]), 1), dtype=torch.uint8, pin_memory=True)
+    buf = t.numpy()
+    for j, (part, k) in enumerate(fields):
+        a = part[k]
+        assert a.nbytes <= int(off[j + 1] - off[j]), k
+        v = buf[int(off[j]): int(off[j]) + a.nbytes].view(a.dtype).reshape(a.shape)
         v[...] = a
-        pins.append(t)
-        return v
-
-    for k in AGENT_MUTABLE:
-        s.agents[k] = pin(s.agents[k])
-    for k in LOC_MUTABLE:
-        s.locs[k] = pin(s.locs[k])
-    s._pins = pins
+        part[k] = v
+    s._pins = [t]
     return s
 
 

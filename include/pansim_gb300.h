@@ -256,6 +256,21 @@ const char* psim_last_error(const psim_ctx* ctx);
 
 /* State transfer: host SoA <-> device SoA (all mutable arrays). */
 int psim_upload(psim_ctx* ctx, const psim_agents* agents, const psim_locations* locs);
+/* The byte offsets (offsets[n_fields] = the total) of the mutable state that
+ * psim_upload and psim_download move, for n agents, locations and variants,
+ * in this order: the agents' location, steps_until_move, state, days,
+ * variant, infectious, susceptible, diagnosed, quarantined, stayed_home,
+ * no_work, last_test, st_infected_ts, st_infected_loc, st_worst_ts,
+ * st_worst_end_ts, st_diagnosed_ts, st_quarantined_ts, st_quarantined_until,
+ * st_days_in_quarantine, st_hospitalized_ts, st_hospitalized_until,
+ * st_immunization_ts, st_recovered_ts, st_variant_mask,
+ * st_immunization_count, st_infected_count, st_worst_state, imm_round,
+ * symptom_scaling_v, then the locations' infectiousness, open, closed_until,
+ * quarantine_until (34 fields, each at a 256-byte aligned offset).  Host
+ * arrays laid out this way from agents->location on (pinned memory: one
+ * block) move in one copy each way. */
+int psim_state_layout(uint32_t n_agents, uint32_t n_locations, uint32_t n_variants, uint64_t* offsets,
+                      uint32_t* n_fields);
 int psim_download(psim_ctx* ctx, psim_agents* agents, psim_locations* locs);
 int psim_set_params(psim_ctx* ctx, const psim_params* params);
 

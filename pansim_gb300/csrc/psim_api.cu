@@ -48,6 +48,47 @@ int dalloc(psim_ctx* c, T** p, size_t count) {
     return 0;
 }
 
+// The mutable state (what psim_upload / psim_download move) lives in one
+// device allocation: these fields in this order, each at a 256-byte aligned
+// offset (psim_state_layout).  A caller whose host arrays follow the same
+// layout from agents->location on moves the whole state in one copy.
+#define PSIM_AGENT_STATE(X)                                                                                         \
+    X(location, location, N) X(steps_until_move, steps_until_move, N) X(state, state, N) X(days, days, N)          \
+    X(variant, variant, N) X(infectious, infectious, N) X(susceptible, susceptible, N* V)                          \
+    X(diagnosed, diagnosed, N) X(quarantined, quarantined, N) X(stayed_home, stayed_home, N)                       \
+    X(no_work, no_work, N) X(last_test, last_test, N) X(st_infected_ts, st_infected_ts, N)                         \
+    X(st_infected_loc, st_infected_loc, N) X(st_worst_ts, st_worst_ts, N) X(st_worst_end_ts, st_worst_end_ts, N)   \
+    X(st_diagnosed_ts, st_diagnosed_ts, N) X(st_quarantined_ts, st_quarantined_ts, N)                              \
+    X(st_quarantined_until, st_quarantined_until, N) X(st_days_in_quarantine, st_days_in_quarantine, N)            \
+    X(st_hospitalized_ts, st_hospitalized_ts, N) X(st_hospitalized_until, st_hospitalized_until, N)                \
+    X(st_immunization_ts, st_immunization_ts, N) X(st_recovered_ts, st_recovered_ts, N)                            \
+    X(st_variant_mask, st_variant_mask, N) X(st_immunization_count, st_immunization_count, N)                      \
+    X(st_infected_count, st_infected_count, N) X(st_worst_state, st_worst_state, N) X(imm_round, imm_round, N)     \
+    X(scaling_v, symptom_scaling_v, N* V)
+#define PSIM_LOC_STATE(X) \
+    X(infectiousness, infectiousness, L) X(open, open, L) X(closed_until, closed_until, L) X(quarantine_until, quarantine_until, L)
+
+constexpr uint32_t STATE_FIELDS = 34;
+
+// offsets of the state fields for N agents, L locations and V variants
+// (off[STATE_FIELDS] = the total); returns the total
+size_t state_layout(size_t N, size_t L, size_t V, uint64_t* off) {
+    size_t o = 0;
+    uint32_t f = 0;
+    auto put = [&](size_t bytes) {
+        if (off) off[f] = o;
+        ++f;
+        o += (bytes + 255) & ~(size_t)255;
+    };
+#define XA(dev, host, cnt) put(sizeof(*DevAgents{}.dev) * (size_t)(cnt));
+#define XL(dev, host, cnt) put(sizeof(*DevLocs{}.dev) * (size_t)(cnt));
+    PSIM_AGENT_STATE(XA) PSIM_LOC_STATE(XL)
+#undef XA
+#undef XL
+    if (off) off[f] = o;
+    return o;
+}
+
 template <typename T>
 int dcopy_in(psim_ctx* c, const T* dptr, const T* host, size_t count) {
     if (count == 0) return 0;
@@ -157,10 +198,29 @@ int validate(psim_ctx* c, const psim_model* m, const psim_agents* a, const psim_
     return 0;
 }
 
+// whether the host arrays follow the state layout from a->location on
+bool state_packed(const psim_ctx* c, const psim_agents* a, const psim_locations* l) {
+    uint64_t off[STATE_FIELDS + 1];
+    state_layout(c->N, c->L, c->V, off);
+    const char* base = (const char*)a->location;
+    bool ok = base != nullptr;
+    uint32_t f = 0;
+#define XA(dev, host, cnt) ok = ok && (const char*)a->host == base + off[f++];
+#define XL(dev, host, cnt) ok = ok && (const char*)l->host == base + off[f++];
+    PSIM_AGENT_STATE(XA) PSIM_LOC_STATE(XL)
+#undef XA
+#undef XL
+    return ok;
+}
+
 int upload_mutable(psim_ctx* c, const psim_agents* a, const psim_locations* l) {
     const size_t N = c->N, L = c->L;
     DevAgents& d = c->k.a;
     int rc = 0;
+    if (state_packed(c, a, l)) {
+        CK(cudaMemcpyAsync(c->state_slab, a->location, c->state_bytes, cudaMemcpyHostToDevice, c->stream));
+        return 0;
+    }
 #define UP(field, cnt) \
     if ((rc = dcopy_in(c, d.field, a->field, cnt))) return rc;
     UP(location, N) UP(steps_until_move, N) UP(state, N) UP(days, N) UP(variant, N) UP(infectious, N)
@@ -517,17 +577,25 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
         da.sex = z;
     }
     if ((rc = dupload(c, &da.rep, arep.data(), N))) return bail(rc);
+    // the mutable state: one allocation (state_layout)
+    {
+        uint64_t off[STATE_FIELDS + 1];
+        uint8_t* slab = nullptr;
+        if ((rc = dalloc(c, &slab, state_layout(N, L, V, off)))) return bail(rc);
+        c->state_slab = slab;
+        c->state_bytes = off[STATE_FIELDS];
+        uint32_t f = 0;
+#define XA(dev, host, cnt) da.dev = (decltype(da.dev))(slab + off[f++]);
+#define XL(dev, host, cnt) k.l.dev = (decltype(k.l.dev))(slab + off[f++]);
+        PSIM_AGENT_STATE(XA) PSIM_LOC_STATE(XL)
+#undef XA
+#undef XL
+    }
 #define AL(field, cnt) \
     if ((rc = dalloc(c, &da.field, cnt))) return bail(rc);
-    AL(location, N) AL(steps_until_move, N) AL(state, N) AL(days, N) AL(variant, N) AL(infectious, N)
-    AL(susceptible, N * V) AL(diagnosed, N) AL(quarantined, N) AL(stayed_home, N) AL(no_work, N) AL(last_test, N)
-    AL(st_infected_ts, N) AL(st_infected_loc, N) AL(st_worst_ts, N) AL(st_worst_end_ts, N) AL(st_diagnosed_ts, N)
-    AL(st_quarantined_ts, N) AL(st_quarantined_until, N) AL(st_days_in_quarantine, N) AL(st_hospitalized_ts, N)
-    AL(st_hospitalized_until, N) AL(st_immunization_ts, N) AL(st_recovered_ts, N) AL(st_variant_mask, N)
-    AL(st_immunization_count, N) AL(st_infected_count, N) AL(st_worst_state, N) AL(hcw, N) AL(rank, N)
+    AL(hcw, N) AL(rank, N)
     AL(worklist, (size_t)N + (size_t)WORK_MAX_BLOCKS * 256) AL(worklist_loc, (size_t)N + (size_t)WORK_MAX_BLOCKS * 256)
     AL(seg_count, WORK_MAX_BLOCKS) AL(slot_loc, N)
-    AL(imm_round, N) AL(scaling_v, (size_t)N * V)
 #undef AL
     // locations
     DevLocs& dl = k.l;
@@ -540,10 +608,6 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     if ((rc = dupload(c, &dl.classroom_offsets, l->classroom_offsets, l->n_schools ? l->n_schools + 1 : 0)))
         return bail(rc);
     if ((rc = dupload(c, &dl.rep, lrep.data(), L))) return bail(rc);
-    if ((rc = dalloc(c, &dl.infectiousness, L))) return bail(rc);
-    if ((rc = dalloc(c, &dl.open, L))) return bail(rc);
-    if ((rc = dalloc(c, &dl.closed_until, L))) return bail(rc);
-    if ((rc = dalloc(c, &dl.quarantine_until, L))) return bail(rc);
     if ((rc = dalloc(c, &dl.counts, L))) return bail(rc);
     if ((rc = dalloc(c, &dl.csr_off, L + 1))) return bail(rc);
     if ((rc = dalloc(c, &dl.cursor, L))) return bail(rc);
@@ -693,6 +757,11 @@ int psim_download(psim_ctx* c, psim_agents* a, psim_locations* l) {
     if (!a || !l || a->n != c->N || l->n != c->L) return fail(c, PSIM_ERR_ARG, "snapshot size mismatch");
     const size_t N = c->N, L = c->L;
     const DevAgents& d = c->k.a;
+    if (state_packed(c, a, l)) {
+        CK(cudaMemcpyAsync(a->location, c->state_slab, c->state_bytes, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        return check_device_err(c);
+    }
 #define DN(field, cnt) \
     if (a->field) CK(cudaMemcpyAsync(a->field, d.field, (cnt) * sizeof(*a->field), cudaMemcpyDeviceToHost, c->stream));
     DN(location, N) DN(steps_until_move, N) DN(state, N) DN(days, N) DN(variant, N) DN(infectious, N)
@@ -712,6 +781,13 @@ int psim_download(psim_ctx* c, psim_agents* a, psim_locations* l) {
         CK(cudaMemcpyAsync(l->quarantine_until, dl.quarantine_until, L * 4, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     return check_device_err(c);
+}
+
+int psim_state_layout(uint32_t n_agents, uint32_t n_locations, uint32_t n_variants, uint64_t* offsets,
+                      uint32_t* n_fields) {
+    if (n_fields) *n_fields = STATE_FIELDS;
+    if (offsets) state_layout(n_agents, n_locations, n_variants, offsets);
+    return 0;
 }
 
 int psim_get_params(psim_ctx* c, psim_params* out) {

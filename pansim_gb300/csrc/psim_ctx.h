@@ -37,6 +37,9 @@ struct psim_ctx {
     std::string err;
     KArgs k{};
     std::vector<void*> allocs;
+    // the mutable state's one device allocation and its size
+    void* state_slab = nullptr;
+    size_t state_bytes = 0;
     uint32_t N = 0, L = 0, V = 0, R = 0, S = 0, spd = 144;
     uint64_t n_poss = 0;
     psim_params params{};

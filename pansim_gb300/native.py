@@ -86,6 +86,7 @@ def lib(auto_build=True):
         L.psim_checkpoint_bytes.argtypes = [P, C.POINTER(C.c_uint64)]
         L.psim_noalloc_last_error.restype = C.c_char_p
         L.psim_get_tuning.argtypes = [P, P]
+        L.psim_state_layout.argtypes = [U32, U32, U32, P, P]
         _lib = L
     return _lib
 
@@ -94,6 +95,17 @@ def abi_sizes():
     out = np.zeros(6, np.uint64)
     lib().psim_abi_sizes(out.ctypes.data_as(C.c_void_p), 6)
     return [int(x) for x in out]
+
+
+def state_layout(n_agents, n_locations, n_variants):
+    """Byte offsets of the mutable state fields (snapshot.AGENT_MUTABLE then
+    LOC_MUTABLE; the last entry is the total) as the library lays them out in
+    one device allocation: host arrays in this layout move in one copy."""
+    n = C.c_uint32(0)
+    lib().psim_state_layout(n_agents, n_locations, n_variants, None, C.byref(n))
+    off = np.zeros(n.value + 1, np.uint64)
+    lib().psim_state_layout(n_agents, n_locations, n_variants, _p(off), None)
+    return off
 
 
 def device_count():
