@@ -257,3 +257,26 @@ def test_restored_day_rebuilds_the_agent_list(gpu_lib):
     off_g, ag_g = g.csr(canonical=True)
     assert np.array_equal(off_o, off_g) and np.array_equal(ag_o, ag_g)
     g.checkpoint_drop(7)
+
+
+def test_timestep_timing_leaves_a_consistent_agent_list(gpu_lib):
+    """psim_time_step_kernels (two timesteps, the step kernels timed) runs the
+    hot, slot and cold kernels in sequence; afterwards the agent list is the
+    stable grouping of the agents' current locations, for every hot/cold
+    variant."""
+    for variant in (3, 7):
+        s_gpu = small_snapshot(n=12000, locs=3000, initial_infected_frac=0.02)
+        g = GpuSim(s_gpu)
+        g.set_tuning(agg_count=0, agg_slot=0, blocks_per_sm=4, variant=variant, scan_items=4, scan_mode=3)
+        g.run_day(0)
+        spd = s_gpu.steps_per_day
+        for step in (40, 47, 48):
+            ms = g.time_step_kernels(spd + step)
+            assert (np.asarray(ms) > 0).all(), ms
+            g.download()
+            loc = s_gpu.agents["location"]
+            off, ag = g.csr(canonical=True)
+            order = np.argsort(loc, kind="stable").astype(np.uint32)
+            counts = np.bincount(loc, minlength=s_gpu.n_locations)
+            assert np.array_equal(off, np.concatenate([[0], np.cumsum(counts)]).astype(np.uint32))
+            assert np.array_equal(ag, order)
