@@ -593,7 +593,7 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     }
 #define AL(field, cnt) \
     if ((rc = dalloc(c, &da.field, cnt))) return bail(rc);
-    AL(hcw, N) AL(rank, N)
+    AL(hcw, N) AL(rank, N) AL(home, N)
     AL(worklist, (size_t)N + (size_t)WORK_MAX_BLOCKS * 256) AL(worklist_loc, (size_t)N + (size_t)WORK_MAX_BLOCKS * 256)
     AL(seg_count, WORK_MAX_BLOCKS) AL(slot_loc, N)
 #undef AL
@@ -709,7 +709,9 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     if ((rc = upload_mutable(c, a, l))) return bail(rc);
     if ((rc = set_clock(c, 0))) return bail(rc);
     launch_flag_hcw(k, c->stream);
-    c->launches += 1;
+    launch_homes(k, c->stream);
+    c->home_type_done = c->params.home_type;
+    c->launches += 2;
     if ((rc = initial_regroup(c))) return bail(rc);
     c->uploaded = true;
     *out = c;
@@ -818,6 +820,13 @@ int psim_set_params(psim_ctx* c, const psim_params* p) {
     c->k.p = *p;
     c->graph_dirty = true;
     c->clock_valid = false;
+    if (c->uploaded && p->home_type != c->home_type_done) {
+        launch_homes(c->k, c->stream);
+        c->launches += 1;
+        c->home_type_done = p->home_type;
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return fail(c, PSIM_ERR_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e));
+    }
     return 0;
 }
 

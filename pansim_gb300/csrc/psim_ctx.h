@@ -40,6 +40,8 @@ struct psim_ctx {
     // the mutable state's one device allocation and its size
     void* state_slab = nullptr;
     size_t state_bytes = 0;
+    // the home type the agents' home column was computed for
+    uint32_t home_type_done = 0xFFFFFFFFu;
     uint32_t N = 0, L = 0, V = 0, R = 0, S = 0, spd = 144;
     uint64_t n_poss = 0;
     psim_params params{};

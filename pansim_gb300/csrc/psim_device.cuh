@@ -97,6 +97,9 @@ struct DevAgents {
     uint32_t* worklist_loc;       // beside each: its location (low 30 bits, WORK_LOC_MASK for an
                                   // invalid one) | WORK_HZ | WORK_MOVE
     uint32_t* seg_count;          // queued agents per segment
+    uint32_t* home;               // [N] the agent's home: the first home-type entry of its location
+                                  // list (findActualLocationForType's first match, no draw),
+                                  // computed when the context is made or the home type changes
     uint32_t* slot_loc;           // [N] the agents' locations at a step that rebuilds the agent
                                   // list, recorded by the hot kernel for k_slots (which runs
                                   // beside the cold kernel, whose movers rewrite `location`)
@@ -295,6 +298,7 @@ void launch_progress(const KArgs& k, uint32_t t, cudaStream_t s);
 void launch_test(const KArgs& k, uint32_t t, cudaStream_t s);
 void launch_stats(const KArgs& k, uint32_t t, cudaStream_t s);
 void launch_variant_flags(const KArgs& k, cudaStream_t s);
+void launch_homes(const KArgs& k, cudaStream_t s);
 void launch_plan(const KArgs& k, uint32_t t, cudaStream_t s);
 void launch_flag_hcw(const KArgs& k, cudaStream_t s);
 void launch_bounded_wait_probe(const KArgs& k, uint32_t iters, cudaStream_t s);

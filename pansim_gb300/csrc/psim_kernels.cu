@@ -1716,7 +1716,7 @@ __global__ void __launch_bounds__(256) k_test_flag(KArgs k, uint32_t t) {
         const uint32_t rep = k.a.rep[i];
         psim_stream rng;
         psim_stream_init(&rng, k.r.seed[rep], i - k.r.agent_off[rep], t, PSIM_PHASE_TEST_FLAG);
-        uint32_t home = find_location(k, i, p.home_type, 0, &rng);
+        uint32_t home = k.a.home[i];
         if (home != NONE && home < k.l.n) k.l.flags[home] = 1;
         uint32_t work = find_location(k, i, p.work_type, 0, &rng);
         if (work != NONE && work < k.l.n && quarantine_window_ok(k.l.quarantine_until[work], t, ql_steps, day_steps))
@@ -1744,7 +1744,7 @@ __global__ void __launch_bounds__(256) k_test(KArgs k, uint32_t t) {
         const uint32_t rep = k.a.rep[i];
         psim_stream rng;
         psim_stream_init(&rng, k.r.seed[rep], i - k.r.agent_off[rep], t, PSIM_PHASE_TEST);
-        uint32_t home = find_location(k, i, p.home_type, 0, &rng);
+        uint32_t home = k.a.home[i];
         int home_flag = (home != NONE && home < k.l.n) ? k.l.flags[home] : 0;
         uint32_t work = find_location(k, i, p.work_type, 0, &rng);
         int work_flag = (work != NONE && work < k.l.n) ? k.l.flags[work] : 0;
@@ -2056,7 +2056,7 @@ __global__ void __launch_bounds__(256) k_plan_underage(KArgs k, uint32_t t) {
         const uint32_t rep = k.a.rep[i];
         psim_stream rng;
         psim_stream_init(&rng, k.r.seed[rep], i - k.r.agent_off[rep], t, PSIM_PHASE_PLAN_UNDERAGE);
-        const uint32_t home = find_location3(k, i, p.home_type, 0, &rng, p.home_type, p.school_type, p.classroom_type);
+        const uint32_t home = k.a.home[i];
         bool flag = false;
         if (k.a.quarantined[i]) {
             flag = true;
@@ -2072,30 +2072,38 @@ __global__ void __launch_bounds__(256) k_plan_underage(KArgs k, uint32_t t) {
 }
 
 // setNoWorkToday, :1137-1158: the lowest-id eligible adult of a flagged home
+// (the home is a first match: the agent's stream is not drawn from)
 __global__ void __launch_bounds__(256) k_plan_nowork_min(KArgs k, uint32_t t) {
-    const psim_params& p = k.p;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < k.a.n; i += gridDim.x * blockDim.x) {
         const uint8_t age = k.a.age[i];
         if (!(age > 26 && age < 65)) continue;
-        const uint32_t rep = k.a.rep[i];
-        psim_stream rng;
-        psim_stream_init(&rng, k.r.seed[rep], i - k.r.agent_off[rep], t, PSIM_PHASE_PLAN_NOWORK);
-        const uint32_t home = find_location3(k, i, p.home_type, 0, &rng, p.home_type, p.home_type, p.home_type);
+        const uint32_t home = k.a.home[i];
         // 0 = home not flagged, NONE = flagged, else 1 + the lowest claiming id
         if (home < k.l.n && k.l.no_work_loc[home] != 0u) atomicMin(&k.l.no_work_loc[home], i + 1u);
     }
 }
 
 __global__ void __launch_bounds__(256) k_plan_nowork_set(KArgs k, uint32_t t) {
-    const psim_params& p = k.p;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < k.a.n; i += gridDim.x * blockDim.x) {
         const uint8_t age = k.a.age[i];
         if (!(age > 26 && age < 65)) continue;
-        const uint32_t rep = k.a.rep[i];
-        psim_stream rng;
-        psim_stream_init(&rng, k.r.seed[rep], i - k.r.agent_off[rep], t, PSIM_PHASE_PLAN_NOWORK);
-        const uint32_t home = find_location3(k, i, p.home_type, 0, &rng, p.home_type, p.home_type, p.home_type);
+        const uint32_t home = k.a.home[i];
         if (home < k.l.n && k.l.no_work_loc[home] == i + 1u) k.a.no_work[i] = 1;
+    }
+}
+
+// The agents' homes (findActualLocationForType for the home type,
+// movementPolicies.h:69-122: the first entry of that type, no draw).
+__global__ void k_homes(KArgs k) {
+    const uint32_t ht = k.p.home_type;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < k.a.n; i += gridDim.x * blockDim.x) {
+        uint32_t h = NONE;
+        for (uint32_t j = k.a.loc_offset[i]; j < k.a.loc_offset[i + 1]; ++j)
+            if (k.a.poss_type[j] == ht) {
+                h = k.a.poss_loc[j];
+                break;
+            }
+        k.a.home[i] = h;
     }
 }
 
@@ -2396,6 +2404,7 @@ void launch_plan(const KArgs& k, uint32_t t, cudaStream_t s) {
     k_plan_nowork_set<<<grid_for(k.a.n, 8), 256, 0, s>>>(k, t);
 }
 void launch_flag_hcw(const KArgs& k, cudaStream_t s) { k_flag_hcw<<<grid_for(k.a.n, 8), 256, 0, s>>>(k); }
+void launch_homes(const KArgs& k, cudaStream_t s) { k_homes<<<grid_for(k.a.n, 8), 256, 0, s>>>(k); }
 void launch_type_weights(const KArgs& k, const float* w_by_type, cudaStream_t s) {
     k_type_weights<<<grid_for(k.l.n, 8), 256, 0, s>>>(k, w_by_type);
 }
