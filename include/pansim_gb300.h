@@ -486,12 +486,17 @@ int psim_bounded_wait_selftest(psim_ctx* ctx, uint32_t iters);
  * nothing.  Its scratch is one file-scope __device__ array sized for
  * PSIM_NOALLOC_MAX_LOCATIONS locations (about 16.8 MB, held by every GPU that
  * loads the library until the process exits); larger sizes are rejected with
- * PSIM_ERR_ARG and a message in psim_noalloc_last_error().  The first call on
- * a device looks up the array's device address (cudaGetSymbolAddress): make
- * that first call before any stream capture.  All calls share the array and
- * it keeps the last call's contents (the histogram is cleared at the start of
- * each call); calls that overlap on the GPU race.  The order of the agents
- * within a location is unspecified; locations >= n_locations are left out. */
+ * PSIM_ERR_ARG and a message in psim_noalloc_last_error() (cleared at the
+ * start of every call, so it describes the last call only).  The first call
+ * on a device, and the first after that device's context changed (a device
+ * reset, another context made current), looks up the array's device address
+ * (cudaGetSymbolAddress, keyed by the context's unique id): make that first
+ * call before any stream capture.  All calls share the array and it keeps
+ * the last call's contents (the histogram is cleared at the start of each
+ * call); calls that overlap on the GPU race.  The order of the agents within
+ * a location is unspecified; locations >= n_locations are left out (then
+ * d_offsets[n_locations] < n_agents and only that prefix of d_agents is
+ * written). */
 #define PSIM_NOALLOC_MAX_LOCATIONS (1u << 21)
 #define PSIM_NOALLOC_MAX_AGENTS 0xFFFFFFF0u
 int psim_csr_build_noalloc(const uint32_t* d_location, uint32_t n_agents, uint32_t n_locations,

@@ -381,10 +381,11 @@ __device__ __forceinline__ unsigned lanemask_lt() {
 
 // Hazard of variant 0 at `loc` and whether an infectious agent is there (the
 // scan computed the location's hazards this step; elsewhere every hazard is
-// 0): the bit mask written by the scan is read through L1, so the hazard
-// itself is gathered only at infectious locations.
+// 0): the hazard itself is gathered only at infectious locations.  The mask
+// is read with a plain load, not the read-only path: in the day graph the
+// scan rewrites it while the hot kernel runs beside it.
 __device__ __forceinline__ float hazard_at(const KArgs& k, uint32_t loc, bool* any) {
-    const uint32_t w = __ldg(&k.l.hmask[loc >> 5]);
+    const uint32_t w = k.l.hmask[loc >> 5];
     *any = ((w >> (loc & 31u)) & 1u) != 0;
     return *any ? k.l.hazard[loc] : 0.0f;
 }

@@ -14,6 +14,12 @@
 // Every call shares the scratch array and leaves its contents behind: the
 // histogram is cleared at the start of each call; calls that overlap on the
 // GPU (for example on two streams of the same device) race on it.
+//
+// The array's device address is looked up once per CUDA context (keyed by
+// the context's process-unique id, cuCtxGetId): a device reset or another
+// context made current on the same device loads the module again, possibly
+// at another address, and the next call looks the address up afresh.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -34,20 +40,33 @@ __device__ __align__(256) uint32_t g_noalloc_scratch[NA_WORDS];
 
 constexpr int NA_MAX_DEVICES = 64;
 std::mutex g_setup_mutex;
+// per device: the id of the context whose module the address belongs to
 uint32_t* g_scratch_ptr[NA_MAX_DEVICES] = {};
+unsigned long long g_scratch_ctx[NA_MAX_DEVICES] = {};
 thread_local std::string g_noalloc_error;
+
+// driver entry points taken through the runtime (the library does not link
+// libcuda itself)
+typedef CUresult (*ctx_get_current_fn)(CUcontext*);
+typedef CUresult (*ctx_get_id_fn)(CUcontext, unsigned long long*);
+ctx_get_current_fn g_ctx_get_current = nullptr;
+ctx_get_id_fn g_ctx_get_id = nullptr;
 
 int na_fail(int code, const std::string& msg) {
     g_noalloc_error = msg;
     return code;
 }
 
+// grid-stride loops count in 64 bits: with 32-bit indices an n_agents near
+// 2^32 would wrap the index past the end and visit agents twice
 __global__ void na_zero(uint32_t* counts, uint32_t L) {
-    for (uint32_t l = blockIdx.x * blockDim.x + threadIdx.x; l < L; l += gridDim.x * blockDim.x) counts[l] = 0u;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t l = (size_t)blockIdx.x * blockDim.x + threadIdx.x; l < L; l += stride) counts[l] = 0u;
 }
 
 __global__ void na_count(const uint32_t* loc, uint32_t N, uint32_t L, uint32_t* counts) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += stride) {
         const uint32_t l = loc[i];
         if (l < L) atomicAdd(&counts[l], 1u);
     }
@@ -118,29 +137,59 @@ __global__ void __launch_bounds__(NA_THREADS) na_scan(const uint32_t* counts, ui
 }
 
 __global__ void na_scatter(const uint32_t* loc, uint32_t N, uint32_t L, uint32_t* cursor, uint32_t* agents) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < N; i += stride) {
         const uint32_t l = loc[i];
         if (l < L) {
             const uint32_t p = atomicAdd(&cursor[l], 1u);
-            if (p < N) agents[p] = i;
+            if (p < N) agents[p] = (uint32_t)i;
         }
     }
 }
 
-// once per device, with that device current: the device address of the
-// scratch array (its host-side name is only a stand-in)
+// The id of the current thread's CUDA context (0 and no error when the
+// thread has none yet).
+int current_context_id(unsigned long long* id) {
+    *id = 0;
+    if (!g_ctx_get_current || !g_ctx_get_id) {
+        cudaDriverEntryPointQueryResult q1, q2;
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        cudaError_t e1 = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1);
+        cudaError_t e2 = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2);
+        if (e1 != cudaSuccess || e2 != cudaSuccess || q1 != cudaDriverEntryPointSuccess ||
+            q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+            return na_fail(PSIM_ERR_CUDA, "cudaGetDriverEntryPointByVersion: cuCtxGetCurrent/cuCtxGetId unavailable");
+        g_ctx_get_current = (ctx_get_current_fn)f1;
+        g_ctx_get_id = (ctx_get_id_fn)f2;
+    }
+    CUcontext ctx = nullptr;
+    if (g_ctx_get_current(&ctx) != CUDA_SUCCESS) return na_fail(PSIM_ERR_CUDA, "cuCtxGetCurrent failed");
+    if (ctx && g_ctx_get_id(ctx, id) != CUDA_SUCCESS) return na_fail(PSIM_ERR_CUDA, "cuCtxGetId failed");
+    return 0;
+}
+
+// Set-up, once per device and context, with that device current: the device
+// address of the scratch array (its host-side name is only a stand-in).
 int scratch_for_current_device(uint32_t** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return na_fail(PSIM_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
     if (dev < 0 || dev >= NA_MAX_DEVICES) return na_fail(PSIM_ERR_ARG, "device index out of range");
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_ptr[dev]) {
+    unsigned long long ctx_id = 0;
+    int rc = current_context_id(&ctx_id);
+    if (rc) return rc;
+    if (!g_scratch_ptr[dev] || ctx_id == 0 || ctx_id != g_scratch_ctx[dev]) {
         void* p = nullptr;
+        // makes the device's primary context current if the thread had none
         e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p)
             return na_fail(PSIM_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        rc = current_context_id(&ctx_id);
+        if (rc) return rc;
         g_scratch_ptr[dev] = (uint32_t*)p;
+        g_scratch_ctx[dev] = ctx_id;
     }
     *out = g_scratch_ptr[dev];
     return 0;
@@ -156,6 +205,7 @@ unsigned grid(uint32_t n) {
 
 extern "C" int psim_csr_build_noalloc(const uint32_t* d_location, uint32_t n_agents, uint32_t n_locations,
                                       uint32_t* d_offsets, uint32_t* d_agents, void* stream) {
+    g_noalloc_error.clear();
     if (n_locations == 0 || n_locations > PSIM_NOALLOC_MAX_LOCATIONS)
         return na_fail(PSIM_ERR_ARG, "psim_csr_build_noalloc: n_locations must be 1.." +
                                          std::to_string(PSIM_NOALLOC_MAX_LOCATIONS) + ", got " +

@@ -90,3 +90,18 @@ def test_create_rejects_empty_population_and_shared_replica_locations():
     batch.agents["location"][5] = batch.reps["loc_offset"][1] + 3  # an agent of replica 0 placed in replica 1
     rc, msg = _create(batch)
     assert rc == -4 and "outside its replica" in msg
+
+
+def test_noalloc_limit_checks_on_host():
+    """psim_csr_build_noalloc rejects sizes beyond its fixed scratch before any CUDA call,
+    and its message describes the last call only."""
+    L = native.lib()
+    rc = L.psim_csr_build_noalloc(None, 0, (1 << 21) + 1, None, None, None)
+    assert rc == -1
+    assert b"n_locations must be" in L.psim_noalloc_last_error()
+    rc = L.psim_csr_build_noalloc(None, 0, 0, None, None, None)
+    assert rc == -1
+    rc = L.psim_csr_build_noalloc(None, 0xFFFFFFFF, 16, None, None, None)
+    assert rc == -1 and b"n_agents must be" in L.psim_noalloc_last_error()
+    rc = L.psim_csr_build_noalloc(None, 10, 16, None, None, None)
+    assert rc == -1 and b"null device pointer" in L.psim_noalloc_last_error()

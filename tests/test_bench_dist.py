@@ -52,3 +52,43 @@ def test_single_rank_needs_no_collective():
     import bench
     t_max, value = bench.whole_job(50.0, 2_000_000, 144, 4, 1)
     assert t_max == 50.0 and value == pytest.approx(2e6 * 144 * 4 / 0.05)
+
+
+RANK_SCRIPT = r'''
+import json, os, sys
+sys.path.insert(0, {root!r})
+import torch.distributed as dist
+import bench
+ws, rank, local = bench.dist_env()
+dist.init_process_group("gloo")
+t_max, value = bench.whole_job(100.0 * (rank + 1), 1000, 144, 10, ws, dist, "cpu")
+if rank == 0:
+    print(json.dumps({{"n_gpus": ws, "value": value, "ms": t_max, "local_ranks": ws}}))
+with open(os.path.join({out!r}, "rank%d.json" % rank), "w") as f:
+    json.dump({{"rank": rank, "local": local, "ws": ws}}, f)
+dist.barrier()
+dist.destroy_process_group()
+'''
+
+
+def test_launcher_starts_one_rank_per_gpu(tmp_path, capfd):
+    """bench.launch_ranks (what `bench.py --gpus N` does outside torchrun) starts N
+    ranks with RANK / LOCAL_RANK / WORLD_SIZE set; rank 0 prints the whole-job line."""
+    import json
+    import bench
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    script = tmp_path / "rank.py"
+    script.write_text(RANK_SCRIPT.format(root=root, out=str(tmp_path)))
+    env_ws = os.environ.pop("WORLD_SIZE", None)
+    try:
+        rc = bench.launch_ranks(2, [], script=str(script))
+    finally:
+        if env_ws is not None:
+            os.environ["WORLD_SIZE"] = env_ws
+    assert rc == 0
+    ranks = sorted(json.loads((tmp_path / ("rank%d.json" % r)).read_text())["local"] for r in range(2))
+    assert ranks == [0, 1]
+    out = capfd.readouterr().out
+    line = json.loads([x for x in out.splitlines() if x.startswith("{")][-1])
+    assert line["n_gpus"] == 2 and line["ms"] == 200.0
+    assert line["value"] == pytest.approx(1000 * 2 * 144 * 10 / 0.2)

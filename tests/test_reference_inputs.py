@@ -20,7 +20,9 @@ from pansim_gb300 import reference_inputs as ri
 from pansim_gb300 import snapshot as sn
 from tests.helpers import diff_state, stats_rows
 
-REF = "/root/reference"
+# the reference tree, where present (its example inputs); the same variable
+# the reference build recipe reads
+REF = os.environ.get("PANSIM_REFERENCE", os.path.join(os.sep, "root", "reference"))
 
 
 def test_time_day_notation():

@@ -20,7 +20,7 @@ pytestmark = pytest.mark.gpu
 
 def _noalloc(lib, loc_host, n_locations, torch):
     dev = torch.device("cuda", 0)
-    d_loc = torch.from_numpy(loc_host.astype(np.int32).view(np.int32)).to(dev)
+    d_loc = torch.from_numpy(loc_host.astype(np.uint32).view(np.int32)).to(dev)
     d_off = torch.zeros(n_locations + 1, dtype=torch.int32, device=dev)
     d_ag = torch.full((len(loc_host),), -1, dtype=torch.int32, device=dev)
     stream = torch.cuda.current_stream(dev)
@@ -66,9 +66,43 @@ def test_noalloc_csr_matches_context_path_on_two_calls(gpu_lib):
     assert np.array_equal(_segments_sorted(off2, ag2), ag_ref2)
 
 
-def test_noalloc_rejects_oversize(gpu_lib):
+def _numpy_csr(loc, L):
+    """Offsets and agents (ascending id inside a location) of the in-range entries."""
+    loc = loc.astype(np.int64)
+    keep = np.nonzero(loc < L)[0]
+    counts = np.bincount(loc[keep], minlength=L)
+    off = np.zeros(L + 1, np.uint64)
+    off[1:] = np.cumsum(counts)
+    order = keep[np.argsort(loc[keep], kind="stable")]
+    return off.astype(np.uint32), order.astype(np.uint32)
+
+
+def test_noalloc_edge_cases(gpu_lib):
+    """Maximum location count, out-of-range locations left out, and no agents."""
+    torch = pytest.importorskip("torch")
     from pansim_gb300 import native
     lib = native.lib()
-    rc = lib.psim_csr_build_noalloc(None, 0, (1 << 21) + 1, None, None, None)
-    assert rc == -1
-    assert b"n_locations must be" in lib.psim_noalloc_last_error()
+    rng = np.random.default_rng(11)
+    Lmax = 1 << 21
+    # the largest location count: the per-tile prefix loop of the scan is longest
+    loc = rng.integers(0, Lmax, 5000).astype(np.uint32)
+    loc[:3] = [0, Lmax - 1, Lmax - 1]
+    off, ag = _noalloc(lib, loc, Lmax, torch)
+    off_ref, ag_ref = _numpy_csr(loc, Lmax)
+    assert np.array_equal(off, off_ref)
+    assert np.array_equal(_segments_sorted(off, ag), ag_ref)
+    # some agents at locations >= n_locations: left out, offsets[L] < n_agents,
+    # only the prefix of the agent list is written
+    L = 3000
+    loc = rng.integers(0, L, 20000).astype(np.uint32)
+    loc[rng.random(20000) < 0.1] = L + 7
+    loc[5] = 0xFFFFFFFF
+    off, ag = _noalloc(lib, loc, L, torch)
+    off_ref, ag_ref = _numpy_csr(loc, L)
+    assert off[L] == int(np.sum(loc < L)) < len(loc)
+    assert np.array_equal(off, off_ref)
+    assert np.array_equal(_segments_sorted(off, ag)[: off[L]], ag_ref)
+    assert np.all(ag[off[L]:] == 0xFFFFFFFF)  # untouched: the buffer's fill value
+    # no agents: every offset is 0
+    off, ag = _noalloc(lib, np.zeros(0, np.uint32), 1000, torch)
+    assert off.shape == (1001,) and not off.any()
