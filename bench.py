@@ -30,20 +30,43 @@ N_AGENTS = 2_000_000
 N_OTHER_LOCS = 500_000
 METRIC = "agent-steps/s at 2M agents"
 UNIT = "agent-steps/s"
-# algorithmic bytes per step (per agent, per location) of the whole step,
-# 32*N + 20*L: the reference's step touches, per agent, the countdown (read and
-# write, 8), the agent list (12) and the infection inputs (12); per location the
-# offsets (8) and the reduction's inputs and output (12).  Then each kernel's.
+# The reference's step: per agent the countdown (read and write, 8), the
+# agent list (12) and the infection inputs (12); per location the offsets (8)
+# and the reduction's inputs and output (12): 32*N + 20*L bytes per timestep.
+# Our step touches much less (most timesteps move nobody); this figure over
+# our timestep time is the step-rate fraction, a rate and not a bandwidth.
 STEP_BYTES = (32, 20)
-# k_step_fused: location, rank, steps (r+w), infectiousness, replica, CSR offset
-# and hazard gathers, CSR and rank writes = 38 B/agent; k_step_hot: location,
-# steps (r+w), CSR write = 16 B/agent, cursor (r+w) = 8 B/location; k_step_cold
-# works on the queued agents only (their number is not known here, so no
-# bytes); k_scan: counts (r+w), offsets, fixed-point sums, hazard, w_l,
-# replica = 30 B/location
-KERNEL_BYTES = {"movement": (20, 4), "scan": (0, 30), "step_fused": (38, 0), "step_hot": (16, 8),
-                "step_cold": None}
-KERNEL_LABELS = {"step_fused": "k_step_fused", "step_hot": "k_slots + k_step_hot", "step_cold": "k_step_cold"}
+
+
+def kernel_bytes(N, L, V, spd, counts):
+    """Algorithmic bytes per simulated day of each step kernel, from the
+    profiled day's counters (entries E, visited locations H, queued agents M,
+    queue passes Q, rebuilds R):
+      draw      per step the two mask words per 32 locations (L/4); at the
+                day's first step every location's sums, count, weight and
+                replica read and its hazard written (22 L); per visited
+                location count, cursor, hazard, replica (14); per entry the
+                agent id and the susceptibility products (4 + 4 V)
+      queue     per pass the decision timestamps (4 N); per queued agent its
+                work-list entry (4)
+      decide    per decision 72: the agent's location, decision timestamp,
+                state, type, age, flags and timestamps (38), its location-list
+                entries (12), the new location's flags (5), the location and
+                timestamp written (8), the histogram deltas (8), its work-list
+                entry (4)
+      rebuild   per rebuild the scan's counts read and first slots written
+                (8 L) and per agent its location, age band and
+                susceptibilities read, its slot's atomic, id and
+                susceptibility products written (17 + 8 V)
+    """
+    E, H, M, Q, R = (float(x) for x in counts)
+    return {"draw": spd * L / 4.0 + 22.0 * L + 14.0 * H + (4 + 4 * V) * E,
+            "queue": 4.0 * N * Q + 4.0 * M,
+            "decide": 72.0 * M,
+            "rebuild": R * (8.0 * L + (17 + 8 * V) * N)}
+
+
+KERNEL_LABELS = {"rebuild": "scan + k_rebuild_slots", "draw": "k_draw", "queue": "k_queue", "decide": "k_decide"}
 
 
 def scan_label(tuning):
@@ -511,31 +534,27 @@ def main():
     clocks = sampler.stop()
     spd = snap.steps_per_day
     t_max, value = whole_job(total_ms, snap.n_agents, spd, args.steps, ws, dist, "cuda")
-    # per-kernel launch durations (roofline): the same days again with
-    # event-record nodes around every kernel group of the day graph, on the
-    # library's stream.  The nodes add gaps between kernels, so this pass is
-    # kept out of the timed region above.
+    # per-kernel durations (roofline): the same days again with event-record
+    # nodes around every kernel group of the day graph, on the library's
+    # stream, and the day's counters (entries drawn, decisions, rebuilds).
+    # The nodes serialise the graph and add gaps, so this pass is kept out of
+    # the timed region above.
     g.set_profiling(True)
     g.run_day(day)  # captures the profiled graph
     day += 1
     n_prof = min(args.steps, 10)
     kms_sum = np.zeros(5)
+    cnt_sum = np.zeros(5)
     prof_day_ms = 0.0
     for _ in range(n_prof):
         flush.fill_(1.0)
         torch.cuda.synchronize()
         g.run_day(day)
         kms_sum += g.day_kernel_ms()
+        cnt_sum += g.day_counts().astype(np.float64)
         prof_day_ms += g.last_day_ms()
         day += 1
     g.set_profiling(False)
-    # average launch durations: movement(0) once a day, scan every step, the
-    # step kernels (fused, or hot + cold) on all steps but the last
-    split = best.get("variant") == 3
-    names = ["movement", "scan"] + (["step_hot", "step_cold"] if split else ["step_fused"])
-    kms = [kms_sum[0] / n_prof, kms_sum[1] / (n_prof * spd), kms_sum[2] / (n_prof * (spd - 1))]
-    if split:
-        kms.append(kms_sum[4] / (n_prof * (spd - 1)))
 
     # end to end through the C ABI with pinned host buffers: per step, the
     # full mutable state host->device, one day, the full state device->host
@@ -565,40 +584,54 @@ def main():
     if rank == 0:
         peak, peak_kind = peaks()
         N, L = snap.n_agents, snap.n_locations
-        kern = {}
-        for name, ms in zip(names, kms):
-            if KERNEL_BYTES[name] is None:
-                kern[name] = {"ms": float(ms), "alg_bytes": None, "gbs": None}
-                continue
-            bn, bl = KERNEL_BYTES[name]
-            b = bn * N + bl * L
-            kern[name] = {"ms": float(ms), "alg_bytes": b, "gbs": b / (ms * 1e-3) / 1e9}
-        # the roofline unit is one timestep of the day graph (tile sums + scan +
-        # fused scatter/draw/movement), its duration the graph time of the timed
-        # days over their timesteps; per-kernel durations come from the
-        # event-timed pass and serve as shares
+        V = int(snap.model["n_variants"])
+        counts = cnt_sum / n_prof
+        kb = kernel_bytes(N, L, V, spd, counts)
+        kms_day = kms_sum / n_prof  # per simulated day: movement(0), rebuild, draw, queue, decide
+        launches_per_day = {"rebuild": max(counts[4], 1.0), "draw": float(spd), "queue": max(counts[3], 1.0),
+                            "decide": max(counts[3], 1.0)}
+        kern = {"movement": {"ms_per_day": float(kms_day[0])}}
+        for j, name in enumerate(["rebuild", "draw", "queue", "decide"]):
+            ms = float(kms_day[1 + j])
+            kern[name] = {"ms_per_day": ms, "alg_bytes_per_day": kb[name],
+                          "launches_with_work_per_day": launches_per_day[name],
+                          "gbs": kb[name] / (ms * 1e-3) / 1e9 if ms > 0 else None,
+                          "frac": kb[name] / (ms * 1e-3) / 1e9 / peak if ms > 0 else None}
+        tot_k = sum(kern[n]["ms_per_day"] for n in KERNEL_LABELS) or 1.0
+        for name in KERNEL_LABELS:
+            kern[name]["share_of_steps"] = kern[name]["ms_per_day"] / tot_k
+        dom = max(KERNEL_LABELS, key=lambda k: kern[k]["ms_per_day"])
+        # the dominant kernel per launch: its bytes and time over the launches
+        # that did work (the others return at their first loads)
+        nl = launches_per_day[dom]
+        dom_ms = kern[dom]["ms_per_day"] / nl
+        dom_bytes = kb[dom] / nl
+        ach = dom_bytes / (dom_ms * 1e-3) / 1e9
+        tr = committed_traffic()
+        traffic = tr.get(dom) if tr else None
+        # the step-rate figure: the reference's per-step bytes over our
+        # average timestep time
         step_ms = graph_ms / (args.steps * spd)
         step_bytes = STEP_BYTES[0] * N + STEP_BYTES[1] * L
-        step_names = names[1:]
-        tot_k = sum(kern[n]["ms"] for n in step_names) or 1.0
-        for name in step_names:
-            kern[name]["share_of_step"] = kern[name]["ms"] / tot_k
-        dom = max(step_names, key=lambda k: kern[k]["ms"])
-        tr = committed_traffic()
-        traffic = tr.get("step") if tr else None
-        ach = step_bytes / (step_ms * 1e-3) / 1e9
+        counts_d = {"draw_entries": counts[0], "draw_locations": counts[1], "decisions": counts[2],
+                    "queue_passes": counts[3], "rebuilds": counts[4]}
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
             "config": workload_config(snap, ws),
-            "roofline": {"bound": "hbm", "kernel": "one timestep: " + " + ".join(
-                             scan_label(best) if n == "scan" else KERNEL_LABELS[n] for n in step_names),
-                         "achieved": ach, "peak": peak,
-                         "unit": "GB/s", "frac": ach / peak, "traffic": traffic, "peak_kind": peak_kind,
-                         "alg_bytes_per_launch": step_bytes, "launch_ms": step_ms, "dominant": dom,
-                         "launch_ms_source": "day-graph CUDA events over the timed days / timesteps",
-                         "per_kernel": kern},
+            "roofline": {"bound": "hbm",
+                         "kernel": (scan_label(best) + " + k_rebuild_slots") if dom == "rebuild" else KERNEL_LABELS[dom],
+                         "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak, "traffic": traffic,
+                         "peak_kind": peak_kind, "alg_bytes_per_launch": dom_bytes, "launch_ms": dom_ms,
+                         "launch_ms_source": "event-record nodes in the profiled day graph, over the launches "
+                                             "that did work",
+                         "dominant": dom, "per_kernel": kern, "day_counts": counts_d,
+                         "step_rate": {"reference_bytes_per_timestep": step_bytes, "timestep_ms": step_ms,
+                                       "gbs": step_bytes / (step_ms * 1e-3) / 1e9,
+                                       "frac": step_bytes / (step_ms * 1e-3) / 1e9 / peak,
+                                       "note": "the reference's step bytes (32 N + 20 L) over our timestep "
+                                               "time: a rate, not a bandwidth"}},
             "clocks": clocks, "gpu_launches": int(launches), "e2e": e2e,
             "kernel_timing": {"days": n_prof, "graph_ms_per_day_with_event_nodes": prof_day_ms / n_prof,
                               "note": "per-kernel durations from event-record nodes in a separate pass"},

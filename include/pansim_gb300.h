@@ -219,17 +219,15 @@ typedef struct psim_day_stats {
 
 /* Launch and algorithm choices of the per-step kernels, picked per device
  * and workload by the autotuner (pansim_gb300/autotune.py).  A new context
- * starts with variant 3, agg_slot 0, blocks_per_sm 4, scan_items 4,
- * scan_mode 3 (the fastest measured on GB300 at 2M agents). */
+ * starts with agg_slot 0, blocks_per_sm 4, scan_items 4, scan_mode 3. */
 typedef struct psim_tuning {
     uint32_t agg_count;      /* no effect (the histogram is updated by movers only) */
-    uint32_t agg_slot;       /* warp-aggregated CSR slot atomics */
+    uint32_t agg_slot;       /* warp-aggregated agent-list slot atomics */
     uint32_t blocks_per_sm;  /* 256-thread blocks per SM of the per-agent kernels; 0 = occupancy */
-    uint32_t variant;        /* fused step kernel: 0/1/2 = one kernel capped at 64/40/32
-                                registers, 3 = hot/cold split, 4/5 = 2/4 agents per
-                                thread in flight (plain slot atomics), 6 = hot/cold
-                                split with 2 agents per hot thread in flight, 7 = hot/cold
-                                split with the cold agents spread evenly over the grid */
+    uint32_t variant;        /* must be 3: the location-ordered step (agent list rebuilt at the
+                                steps where agents took new locations, draws over the
+                                locations with an infectious agent, decisions of the agents
+                                whose decision step it is) */
     uint32_t scan_items;     /* locations per thread of the scan: 2, 4 or 8 (0 = 8) */
     uint32_t scan_mode;      /* 0 = single pass with decoupled look-back, 1 = tile sums + scan,
                                 2 = tile sums + scan with each thread owning consecutive
@@ -450,21 +448,24 @@ int psim_get_csr(psim_ctx* ctx, int canonical, uint32_t* offsets /*[L+1]*/, uint
 /* Per-location hazard r_l of the last psim_infect call (infectionRatios). */
 int psim_get_hazard(psim_ctx* ctx, float* out /*[L]*/, int64_t* fixed_sum /*[L] or NULL*/);
 
-/* Steps t and t+1 (same day) as the day graph runs them, with CUDA events
- * around movement(t), scan(t) and the fused scatter+draw(t)/movement(t+1)
- * kernel; ms[3] receives those three durations. */
+/* Step t as the day graph runs it, after movement(t) with the sums afresh and
+ * the agent list rebuilt, with CUDA events around the rebuild (scan + slots),
+ * the draws of t and the queue + decisions of t + 1; ms[3] receives those
+ * three durations.  t and t + 1 must lie in the same day. */
 int psim_time_step_kernels(psim_ctx* ctx, uint32_t t, float* ms /* [3] */);
 /* Timing of the last psim_run_steps graph launch, milliseconds. */
 int psim_last_day_ms(psim_ctx* ctx, float* ms);
-/* With on != 0 the day graph is captured with event-record nodes around
- * each of its kernel groups; psim_day_kernel_ms then gives, for the last
- * psim_run_steps, the summed durations ms[5] = {movement of step 0, the
- * scans of all steps (tile sums + scan), the first step kernel of steps
- * 0..spd-2 (the fused scatter/draw/movement kernel, or the hot kernel of the
- * hot/cold form), the scatter/draw of the last step, the cold kernel of steps
- * 0..spd-2 (0 for the fused forms)}. */
+/* With on != 0 the day graph is captured on one branch with event-record
+ * nodes around each of its kernel groups; psim_day_kernel_ms then gives, for
+ * the last psim_run_steps, the summed durations ms[5] = {movement of step 0,
+ * the rebuilds of all steps (scan + slots), the draws, the queues, the
+ * decisions}, and psim_day_counts out[5] = {agent-list entries the draws
+ * expanded, locations with a set hazard-mask bit they visited, agents queued
+ * for a decision, steps whose queue passed over the agents, steps that
+ * rebuilt the agent list}, summed over the day's steps. */
 int psim_set_profiling(psim_ctx* ctx, int on);
 int psim_day_kernel_ms(psim_ctx* ctx, float* ms /* [5] */);
+int psim_day_counts(psim_ctx* ctx, uint64_t* out /* [5] */);
 /* Counts of kernel launches issued by the library since creation. */
 int psim_launch_count(psim_ctx* ctx, uint64_t* out);
 /* The context's cudaStream_t (as void*), for callers that order their own work after it. */

@@ -1,40 +1,33 @@
 """Autotuner of the per-step kernels.
 
-Times each candidate tuning (fused-kernel variant, warp aggregation of the
-CSR slot atomics, blocks per SM of the per-agent kernels, scan tile size and
-single-pass or two-pass scan) on the live workload: every candidate runs the same whole day (the
-day graph, all its steps) from the same checkpoint taken after that day's
-midnight phases, timed with CUDA events, and the fastest is kept.  Steps at
-different times of day differ several-fold in cost (movers, infectious
-locations), so candidates are never compared on different steps.  The
-choice depends on the device and on the population (location sizes,
+Times each candidate tuning (warp aggregation of the agent-list slot
+atomics, blocks per SM of the per-agent kernels, scan tile size and
+single-pass or two-pass scan) on the live workload: every candidate runs the
+same whole day (the day graph, all its steps) from the same checkpoint taken
+after that day's midnight phases, timed with CUDA events, and the fastest is
+kept.  Steps at different times of day differ several-fold in cost (movers,
+infectious locations), so candidates are never compared on different steps.
+The choice depends on the device and on the population (location sizes,
 household structure), so it is made per context.
 """
 import itertools
 
-import numpy as np
-
 DEFAULT_GRID = [0, 4, 8, 16]
-DEFAULT_VARIANTS = [0, 3]
 LARGE_AGENTS = 8_000_000
 
 
-def candidates(grid=None, variants=None):
-    """variant: register cap of the fused kernel (64 / 40 / 32 registers),
-    3 = hot/cold split, 4 / 5 = 2 / 4 agents per thread in flight;
-    blocks_per_sm 0 = one occupancy wave of that variant; scan_mode 2 / 3 =
-    two passes / one pass with look-back over consecutive locations per
-    thread."""
-    for variant, agg_slot, bps, items, mode in itertools.product(variants or DEFAULT_VARIANTS, [1, 0],
-                                                                 grid or DEFAULT_GRID, [8, 4, 2], [2, 3]):
-        yield dict(agg_count=0, agg_slot=agg_slot, blocks_per_sm=bps, variant=variant, scan_items=items,
-                   scan_mode=mode)
+def candidates(grid=None):
+    """blocks_per_sm 0 = one occupancy wave of each per-agent kernel;
+    scan_mode 2 / 3 = two passes / one pass with look-back over consecutive
+    locations per thread."""
+    for agg_slot, bps, items, mode in itertools.product([1, 0], grid or DEFAULT_GRID, [8, 4, 2], [2, 3]):
+        yield dict(agg_count=0, agg_slot=agg_slot, blocks_per_sm=bps, variant=3, scan_items=items, scan_mode=mode)
 
 
 TUNE_SLOT = 1 << 16
 
 
-def autotune(sim, day, reps=2, grid=None, variants=None, verbose=False):
+def autotune(sim, day, reps=2, grid=None, verbose=False):
     """Tries the candidates on the steps of `day` (the simulation must be at
     the start of that day); returns (best tuning, table of (tuning, day ms)).
     The simulation state is saved first and restored afterwards, so tuning
@@ -42,7 +35,6 @@ def autotune(sim, day, reps=2, grid=None, variants=None, verbose=False):
     set and one repetition (a day there takes a good fraction of a second)."""
     if sim.snap.n_agents > LARGE_AGENTS:
         grid = grid or [0, 16]
-        variants = variants or [0, 3]
         reps = 1
     spd = sim.snap.steps_per_day
     sim.checkpoint_save(TUNE_SLOT)
@@ -57,7 +49,7 @@ def autotune(sim, day, reps=2, grid=None, variants=None, verbose=False):
     sim.plan(t)
     sim.checkpoint_save(TUNE_SLOT + 1)
     table = []
-    for cand in candidates(grid, variants):
+    for cand in candidates(grid):
         sim.set_tuning(**cand)
         ms = []
         for _ in range(reps):

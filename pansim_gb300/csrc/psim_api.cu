@@ -26,6 +26,7 @@ int check_device_err(psim_ctx* c) {
         if (e & ERR_LOCATION) m += " agent on an invalid location;";
         if (e & ERR_TEST_WAIT) m += " bounded wait expired;";
         if (e & ERR_SCAN_WAIT) m += " scan tile wait expired;";
+        if (e & ERR_AGENT_LIST) m += " agent list inconsistent;";
         return fail(c, PSIM_ERR_DEVICE, m);
     }
     return 0;
@@ -53,7 +54,7 @@ int dalloc(psim_ctx* c, T** p, size_t count) {
 // offset (psim_state_layout).  A caller whose host arrays follow the same
 // layout from agents->location on moves the whole state in one copy.
 #define PSIM_AGENT_STATE(X)                                                                                         \
-    X(location, location, N) X(steps_until_move, steps_until_move, N) X(state, state, N) X(days, days, N)          \
+    X(location, location, N) X(move_at, steps_until_move, N) X(state, state, N) X(days, days, N)          \
     X(variant, variant, N) X(infectious, infectious, N) X(susceptible, susceptible, N* V)                          \
     X(diagnosed, diagnosed, N) X(quarantined, quarantined, N) X(stayed_home, stayed_home, N)                       \
     X(no_work, no_work, N) X(last_test, last_test, N) X(st_infected_ts, st_infected_ts, N)                         \
@@ -219,11 +220,15 @@ int upload_mutable(psim_ctx* c, const psim_agents* a, const psim_locations* l) {
     int rc = 0;
     if (state_packed(c, a, l)) {
         CK(cudaMemcpyAsync(c->state_slab, a->location, c->state_bytes, cudaMemcpyHostToDevice, c->stream));
-        return 0;
+        // countdowns -> absolute decision timestamps
+        launch_time_shift(d.move_at, c->N, c->t_next, c->stream);
+        return launch_check(c);
     }
 #define UP(field, cnt) \
     if ((rc = dcopy_in(c, d.field, a->field, cnt))) return rc;
-    UP(location, N) UP(steps_until_move, N) UP(state, N) UP(days, N) UP(variant, N) UP(infectious, N)
+    if ((rc = dcopy_in(c, d.move_at, a->steps_until_move, N))) return rc;
+    launch_time_shift(d.move_at, c->N, c->t_next, c->stream);
+    UP(location, N) UP(state, N) UP(days, N) UP(variant, N) UP(infectious, N)
     UP(susceptible, N * c->V) UP(diagnosed, N) UP(quarantined, N) UP(stayed_home, N) UP(no_work, N) UP(last_test, N)
     UP(st_infected_ts, N) UP(st_infected_loc, N) UP(st_worst_ts, N) UP(st_worst_end_ts, N) UP(st_diagnosed_ts, N)
     UP(st_quarantined_ts, N) UP(st_quarantined_until, N) UP(st_days_in_quarantine, N) UP(st_hospitalized_ts, N)
@@ -284,7 +289,7 @@ int initial_regroup(psim_ctx* c) {
 }
 
 int do_step(psim_ctx* c, uint32_t step, bool draw, bool movement) {
-    const int merge_q = c->params.quarantine_policy > 1;
+    const int merge_q = c->params.quarantine_policy > 1 ? 2 : 0;
     if (movement) {
         int rc = reset_sums(c);
         if (rc) return rc;
@@ -302,64 +307,67 @@ int capture_day_graph(psim_ctx* c) {
         c->day_graph = nullptr;
     }
     cudaGraph_t g = nullptr;
-    // 3 * spd + 2 events: [0] before movement(0), then one after every kernel
-    // group (movement; per step the scan, the first and the second step kernel)
-    const size_t n_ev = c->profile ? 3ull * c->spd + 2 : 0;
+    // 4 * spd + 2 events: [0] before movement(0), [1] after it, then per step
+    // one after the rebuild (scan + slots), the draws, the queue and the
+    // decisions
+    const size_t n_ev = c->profile ? 4ull * c->spd + 2 : 0;
     while (c->prof_ev.size() < n_ev) {
         cudaEvent_t ev = nullptr;
         CK(cudaEventCreate(&ev));
         c->prof_ev.push_back(ev);
     }
+    c->k.prof = c->profile ? c->d_prof : nullptr;
     size_t ev_i = 0;
     auto mark = [&]() {
         if (c->profile) cudaEventRecordWithFlags(c->prof_ev[ev_i++], c->stream, cudaEventRecordExternal);
     };
     CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    const int merge_q = c->params.quarantine_policy > 1;
-    // movement(0) with the sums afresh; then per step: scan(s), scatter+draw(s)
-    // fused with movement(s+1), which update the sums
+    const int merge_q = c->params.quarantine_policy > 1 ? 1 : 0;
     mark();
     // (the capture stays open until EndCapture: errors are checked after it)
+    // The day's first step: the sums afresh (every location dirty), the
+    // agent list rebuilt (its slots take the susceptibilities the midnight
+    // phases left), the mask of decision steps recomputed from every agent.
     cudaError_t me = cudaMemsetAsync(c->k.l.sfix, 0, sizeof(unsigned long long) * c->L * c->V, c->stream);
     if (me == cudaSuccess)
         me = cudaMemsetAsync(c->k.l.smask, 0xFF, sizeof(uint32_t) * (((size_t)c->L + 2047) / 2048 * 64 + 64), c->stream);
+    if (me == cudaSuccess) me = cudaMemsetAsync(c->k.a.move_mask, 0, sizeof(uint32_t) * MOVE_MASK_WORDS, c->stream);
+    if (me == cudaSuccess) me = cudaMemsetAsync(c->k.l.build + 1, 0xFF, sizeof(uint32_t), c->stream);
+    if (me == cudaSuccess && c->profile) me = cudaMemsetAsync(c->d_prof, 0, sizeof(unsigned long long) * PROF_N, c->stream);
     launch_movement(c->k, 0, c->stream);
     mark();
-    // the hot/cold variants outside profiling: the hot kernel reads only the
-    // hazard mask of the scan's outputs, and the mask holds a superset of the
-    // infectious locations before the scan (every added term marks its
-    // location), so the hot kernel runs on a second branch beside the scan;
-    // the cold kernel joins them.  On a step that rebuilds the agent list the hot kernel records the
-    // agents' locations, and the slots run after the scan and the hot kernel,
-    // beside the cold kernel; the next step starts after both.
-    const bool fork = !c->profile && step_fused_kernels(c->k) == 3;
-    bool slots_pending = false;
+    // Per step s: the rebuild (scan, slots) and the draws on the first
+    // branch; the queue of the agents deciding at s + 1 on the second (it
+    // reads only their decision timestamps, which nothing on the first branch
+    // writes); the decisions after both (they read the draws' outcomes).
+    // The profiled graph runs them in that order on one branch with an event
+    // between each.
     for (uint32_t s = 0; s < c->spd; ++s) {
-        if (slots_pending && me == cudaSuccess) me = cudaStreamWaitEvent(c->stream, c->slots_ev, 0);
-        slots_pending = false;
-        if (fork && s + 1 < c->spd) {
-            if (me == cudaSuccess) me = cudaEventRecord(c->fork_ev, c->stream);
-            if (me == cudaSuccess) me = cudaStreamWaitEvent(c->stream2, c->fork_ev, 0);
-            launch_step_fused(c->k, s, c->stream2, 2);
-            launch_scan(c->k, s, 1, merge_q, c->stream);
-            if (me == cudaSuccess) me = cudaEventRecord(c->join_ev, c->stream2);
-            if (me == cudaSuccess) me = cudaStreamWaitEvent(c->stream, c->join_ev, 0);
-            if (me == cudaSuccess) me = cudaEventRecord(c->both_ev, c->stream);
-            if (me == cudaSuccess) me = cudaStreamWaitEvent(c->stream2, c->both_ev, 0);
-            launch_step_fused(c->k, s, c->stream2, 3);
-            if (me == cudaSuccess) me = cudaEventRecord(c->slots_ev, c->stream2);
-            slots_pending = true;
-            launch_step_fused(c->k, s, c->stream, 1);
+        const bool next = s + 1 < c->spd;
+        if (!c->profile) {
+            if (next) {
+                if (me == cudaSuccess) me = cudaEventRecord(c->fork_ev, c->stream);
+                if (me == cudaSuccess) me = cudaStreamWaitEvent(c->stream2, c->fork_ev, 0);
+                launch_queue(c->k, s, c->stream2);
+                if (me == cudaSuccess) me = cudaEventRecord(c->join_ev, c->stream2);
+            }
+            launch_scan(c->k, s, 0, merge_q, c->stream);
+            launch_rebuild_slots(c->k, s, c->stream);
+            launch_draw(c->k, s, c->stream);
+            if (next) {
+                if (me == cudaSuccess) me = cudaStreamWaitEvent(c->stream, c->join_ev, 0);
+                launch_decide(c->k, s, c->stream);
+            }
             continue;
         }
-        launch_scan(c->k, s, 1, merge_q, c->stream);
+        launch_scan(c->k, s, 0, merge_q, c->stream);
+        launch_rebuild_slots(c->k, s, c->stream);
         mark();
-        if (s + 1 < c->spd)
-            launch_step_fused(c->k, s, c->stream, 0);
-        else
-            launch_scatter_draw(c->k, s, 1, 1, c->stream);
+        launch_draw(c->k, s, c->stream);
         mark();
-        if (s + 1 < c->spd) launch_step_fused(c->k, s, c->stream, 1);
+        if (next) launch_queue(c->k, s, c->stream);
+        mark();
+        if (next) launch_decide(c->k, s, c->stream);
         mark();
     }
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
@@ -371,8 +379,9 @@ int capture_day_graph(psim_ctx* c) {
     e = cudaGraphInstantiate(&c->day_graph, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(c, PSIM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
-    // movement(0), the scans, the step kernels of all steps but the last, the last scatter/draw
-    c->graph_kernels = 2 + (uint64_t)scan_kernels(c->k) * c->spd + (uint64_t)step_fused_kernels(c->k) * (c->spd - 1);
+    // movement(0); per step the scan kernels, the slots and the draws; the
+    // queue and the decisions of all steps but the last
+    c->graph_kernels = 1 + (uint64_t)(scan_kernels(c->k) + 2) * c->spd + 2ull * (c->spd - 1);
     c->graph_dirty = false;
     c->prof_valid = false;
     return 0;
@@ -456,8 +465,7 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     int rc = validate(c, m, a, l);
     if (rc) return bail(rc);
     if (p->time_step == 0 || 1440 % p->time_step) return bail(fail(c, PSIM_ERR_ARG, "time_step must divide 1440"));
-    // the hot/cold step hands a queued agent's location on in 30 bits
-    if (l->n >= WORK_LOC_MASK) return bail(fail(c, PSIM_ERR_ARG, "more than 2^30 - 2 locations"));
+    if (l->n >= 0x3FFFFFFFu) return bail(fail(c, PSIM_ERR_ARG, "more than 2^30 - 2 locations"));
     c->N = a->n;
     c->L = l->n;
     c->V = m->n_variants;
@@ -594,8 +602,8 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
 #define AL(field, cnt) \
     if ((rc = dalloc(c, &da.field, cnt))) return bail(rc);
     AL(hcw, N) AL(rank, N) AL(home, N)
-    AL(worklist, (size_t)N + (size_t)WORK_MAX_BLOCKS * 256) AL(worklist_loc, (size_t)N + (size_t)WORK_MAX_BLOCKS * 256)
-    AL(seg_count, WORK_MAX_BLOCKS) AL(slot_loc, N)
+    AL(worklist, (size_t)N + (size_t)WORK_MAX_BLOCKS * 256) AL(seg_count, WORK_MAX_BLOCKS)
+    AL(move_mask, MOVE_MASK_WORDS)
 #undef AL
     // locations
     DevLocs& dl = k.l;
@@ -612,6 +620,7 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     if ((rc = dalloc(c, &dl.csr_off, L + 1))) return bail(rc);
     if ((rc = dalloc(c, &dl.cursor, L))) return bail(rc);
     if ((rc = dalloc(c, &dl.csr_agents, N))) return bail(rc);
+    if ((rc = dalloc(c, &dl.slot_su, N * V))) return bail(rc);
     if ((rc = dalloc(c, &dl.qu_pending, L))) return bail(rc);
     if ((rc = dalloc(c, &dl.sfix, L * V))) return bail(rc);
     if ((rc = dalloc(c, &dl.hazard, L * V))) return bail(rc);
@@ -624,7 +633,8 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     if ((rc = dalloc(c, &dl.tile_sums, tiles))) return bail(rc);
     if ((rc = dalloc(c, &dl.scan_status, tiles))) return bail(rc);
     if ((rc = dalloc(c, &dl.scan_state, 2))) return bail(rc);
-    if ((rc = dalloc(c, &dl.build, 3))) return bail(rc);
+    if ((rc = dalloc(c, &dl.build, 8))) return bail(rc);
+    if ((rc = dalloc(c, &c->d_prof, PROF_N))) return bail(rc);
     // replicas
     DevReps& dr = k.r;
     dr.n = c->R;
@@ -656,7 +666,7 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     {
         auto add = [&](void* ptr, size_t bytes) { c->regions.push_back({ptr, bytes}); c->checkpoint_bytes += bytes; };
         DevAgents& a2 = k.a;
-        add(a2.location, 4 * N); add(a2.steps_until_move, 4 * N); add(a2.state, N); add(a2.days, 2 * N);
+        add(a2.location, 4 * N); add(a2.move_at, 4 * N); add(a2.state, N); add(a2.days, 2 * N);
         add(a2.variant, N); add(a2.infectious, 4 * N); add(a2.susceptible, 4 * N * V); add(a2.diagnosed, N);
         add(a2.quarantined, N); add(a2.stayed_home, N); add(a2.no_work, N); add(a2.last_test, 4 * N);
         add(a2.st_infected_ts, 4 * N); add(a2.st_infected_loc, 4 * N); add(a2.st_worst_ts, 4 * N);
@@ -759,14 +769,22 @@ int psim_download(psim_ctx* c, psim_agents* a, psim_locations* l) {
     if (!a || !l || a->n != c->N || l->n != c->L) return fail(c, PSIM_ERR_ARG, "snapshot size mismatch");
     const size_t N = c->N, L = c->L;
     const DevAgents& d = c->k.a;
+    // absolute decision timestamps -> countdowns for the copy, and back
+    launch_time_shift(d.move_at, c->N, 0u - c->t_next, c->stream);
     if (state_packed(c, a, l)) {
         CK(cudaMemcpyAsync(a->location, c->state_slab, c->state_bytes, cudaMemcpyDeviceToHost, c->stream));
+        launch_time_shift(d.move_at, c->N, c->t_next, c->stream);
         CK(cudaStreamSynchronize(c->stream));
+        int rc = launch_check(c);
+        if (rc) return rc;
         return check_device_err(c);
     }
 #define DN(field, cnt) \
     if (a->field) CK(cudaMemcpyAsync(a->field, d.field, (cnt) * sizeof(*a->field), cudaMemcpyDeviceToHost, c->stream));
-    DN(location, N) DN(steps_until_move, N) DN(state, N) DN(days, N) DN(variant, N) DN(infectious, N)
+    if (a->steps_until_move)
+        CK(cudaMemcpyAsync(a->steps_until_move, d.move_at, N * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream));
+    launch_time_shift(d.move_at, c->N, c->t_next, c->stream);
+    DN(location, N) DN(state, N) DN(days, N) DN(variant, N) DN(infectious, N)
     DN(susceptible, N * c->V) DN(diagnosed, N) DN(quarantined, N) DN(stayed_home, N) DN(no_work, N) DN(last_test, N)
     DN(st_infected_ts, N) DN(st_infected_loc, N) DN(st_worst_ts, N) DN(st_worst_end_ts, N) DN(st_diagnosed_ts, N)
     DN(st_quarantined_ts, N) DN(st_quarantined_until, N) DN(st_days_in_quarantine, N) DN(st_hospitalized_ts, N)
@@ -782,6 +800,8 @@ int psim_download(psim_ctx* c, psim_agents* a, psim_locations* l) {
     if (l->quarantine_until)
         CK(cudaMemcpyAsync(l->quarantine_until, dl.quarantine_until, L * 4, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    int rc = launch_check(c);
+    if (rc) return rc;
     return check_device_err(c);
 }
 
@@ -836,7 +856,7 @@ int psim_set_tuning(psim_ctx* c, const psim_tuning* t) {
     c->k.tune.agg_count = t->agg_count ? 1u : 0u;
     c->k.tune.agg_slot = t->agg_slot ? 1u : 0u;
     c->k.tune.blocks_per_sm = t->blocks_per_sm;
-    if (t->variant > 9) return fail(c, PSIM_ERR_ARG, "variant out of range");
+    if (t->variant != 3) return fail(c, PSIM_ERR_ARG, "variant must be 3 (the location-ordered step)");
     c->k.tune.variant = t->variant;
     if (t->scan_items != 0 && t->scan_items != 2 && t->scan_items != 4 && t->scan_items != 8)
         return fail(c, PSIM_ERR_ARG, "scan_items must be 2, 4 or 8");
@@ -915,6 +935,7 @@ int psim_checkpoint_save(psim_ctx* c, uint32_t slot) {
         if (e != cudaSuccess) return fail(c, PSIM_ERR_ALLOC, std::string("checkpoint: ") + cudaGetErrorString(e));
         c->checkpoints[slot] = p;
     }
+    c->checkpoint_t_next[slot] = c->t_next;
     char* dst = (char*)c->checkpoints[slot];
     for (auto& r : c->regions) {
         CK(cudaMemcpyAsync(dst, r.first, r.second, cudaMemcpyDeviceToDevice, c->stream));
@@ -933,6 +954,7 @@ int psim_checkpoint_restore(psim_ctx* c, uint32_t slot) {
         CK(cudaMemcpyAsync(r.first, src, r.second, cudaMemcpyDeviceToDevice, c->stream));
         src += r.second;
     }
+    c->t_next = c->checkpoint_t_next[slot];
     // the restored locations need not match the agent list of the last step
     int rc = force_rebuild(c);
     if (rc) return rc;
@@ -981,6 +1003,7 @@ int psim_movement(psim_ctx* c, uint32_t t) {
     launch_movement(c->k, t % c->spd, c->stream);
     c->launches += 1;
     c->csr_fresh = true;
+    c->t_next = t + 1;
     rc = launch_check(c);
     if (rc) return rc;
     return check_device_err(c);
@@ -996,7 +1019,7 @@ int psim_regroup(psim_ctx* c) {
         launch_count(c->k, c->stream);
         c->launches += 1;
     }
-    launch_scan(c->k, 0, 1, c->params.quarantine_policy > 1, c->stream);
+    launch_scan(c->k, 0, 1, c->params.quarantine_policy > 1 ? 2 : 0, c->stream);
     launch_scatter_draw(c->k, 0, 1, 0, c->stream);
     c->launches += 1 + (uint64_t)scan_kernels(c->k);
     c->csr_fresh = false;
@@ -1028,6 +1051,7 @@ int psim_step(psim_ctx* c, uint32_t t) {
     rc = do_step(c, t % c->spd, true, true);
     if (rc) return rc;
     c->csr_fresh = false;
+    c->t_next = t + 1;
     return check_device_err(c);
 }
 
@@ -1078,6 +1102,7 @@ int psim_plan_day(psim_ctx* c, uint32_t t) {
     if (!c || !c->uploaded) return PSIM_ERR_STATE;
     launch_plan(c->k, t, c->stream);
     c->launches += 5 + (c->params.quarantine_policy > 3 && c->k.l.n_schools ? 1 : 0);
+    c->t_next = t;  // the plan sets every countdown relative to midnight t
     int rc = launch_check(c);
     if (rc) return rc;
     return check_device_err(c);
@@ -1123,6 +1148,7 @@ int psim_run_steps(psim_ctx* c, uint32_t day) {
     c->launches += c->graph_kernels;
     c->prof_valid = c->profile;
     c->csr_fresh = false;
+    c->t_next = (day + 1) * c->spd;
     return check_device_err(c);
 }
 
@@ -1159,6 +1185,7 @@ int psim_run_day(psim_ctx* c, uint32_t day, psim_day_stats* out) {
     CK(cudaMemsetAsync(c->k.r.expected, 0, sizeof(double) * c->R, c->stream));
     launch_plan(c->k, t, c->stream);
     c->launches += 5 + (c->params.quarantine_policy > 3 && c->k.l.n_schools ? 1 : 0);
+    c->t_next = t;
     if ((rc = launch_check(c))) return rc;
     if ((rc = set_clock(c, t, false))) return rc;
     CK(cudaEventRecord(c->ev0, c->stream));
@@ -1170,6 +1197,7 @@ int psim_run_day(psim_ctx* c, uint32_t day, psim_day_stats* out) {
     c->launches += c->graph_kernels;
     c->prof_valid = c->profile;
     c->csr_fresh = false;
+    c->t_next = (day + 1) * c->spd;
     if (*c->h_err_pin) return check_device_err(c);
     if (out) assemble_stats(c, t, out);
     return 0;
@@ -1230,14 +1258,26 @@ int psim_day_kernel_ms(psim_ctx* c, float* ms) {
     ms[0] = t;
     ms[1] = ms[2] = ms[3] = ms[4] = 0.f;
     for (uint32_t s = 0; s < c->spd; ++s) {
-        const size_t e = 1 + 3 * (size_t)s;
-        CK(cudaEventElapsedTime(&t, c->prof_ev[e], c->prof_ev[e + 1]));
-        ms[1] += t;
-        CK(cudaEventElapsedTime(&t, c->prof_ev[e + 1], c->prof_ev[e + 2]));
-        ms[s + 1 < c->spd ? 2 : 3] += t;
-        CK(cudaEventElapsedTime(&t, c->prof_ev[e + 2], c->prof_ev[e + 3]));
-        ms[4] += t;
+        const size_t e = 1 + 4 * (size_t)s;
+        for (int j = 0; j < 4; ++j) {
+            CK(cudaEventElapsedTime(&t, c->prof_ev[e + j], c->prof_ev[e + j + 1]));
+            ms[1 + j] += t;
+        }
     }
+    return 0;
+}
+
+int psim_day_counts(psim_ctx* c, uint64_t* out) {
+    if (!c || !out) return PSIM_ERR_ARG;
+    if (!c->prof_valid) return fail(c, PSIM_ERR_STATE, "no profiled day: psim_set_profiling(1), then psim_run_steps");
+    unsigned long long h[PROF_N];
+    CK(cudaMemcpyAsync(h, c->d_prof, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    out[0] = h[PROF_DRAW_ENTRIES];
+    out[1] = h[PROF_DRAW_LOCATIONS];
+    out[2] = h[PROF_MOVERS];
+    out[3] = h[PROF_QUEUE_STEPS];
+    out[4] = h[PROF_REBUILDS];
     return 0;
 }
 
@@ -1261,24 +1301,33 @@ int psim_time_step_kernels(psim_ctx* c, uint32_t t, float* ms) {
     cudaEvent_t ev[4];
     for (int j = 0; j < 4; ++j) CK(cudaEventCreate(&ev[j]));
     const uint32_t step = t % c->spd;
-    const int merge_q = c->params.quarantine_policy > 1;
-    // steps t and t+1 as in the day graph: movement(t) | scan(t) | scatter+draw(t) fused with
-    // movement(t+1); then scan(t+1) and scatter+draw(t+1) untimed
-    CK(cudaEventRecord(ev[0], c->stream));
+    const int merge_q = c->params.quarantine_policy > 1 ? 1 : 0;
+    // step t as the day graph runs it, from movement(t) with the sums afresh
+    // and the agent list rebuilt: the rebuild (scan + slots), the draws, and
+    // the queue + decisions of t + 1; then the rebuild and draws of t + 1
+    // untimed
     if ((rc = reset_sums(c))) return rc;
+    CK(cudaMemsetAsync(c->k.a.move_mask, 0, sizeof(uint32_t) * MOVE_MASK_WORDS, c->stream));
+    if ((rc = force_rebuild(c))) return rc;
     launch_movement(c->k, step, c->stream);
+    CK(cudaEventRecord(ev[0], c->stream));
+    launch_scan(c->k, step, 0, merge_q, c->stream);
+    launch_rebuild_slots(c->k, step, c->stream);
     CK(cudaEventRecord(ev[1], c->stream));
-    launch_scan(c->k, step, 1, merge_q, c->stream);
+    launch_draw(c->k, step, c->stream);
     CK(cudaEventRecord(ev[2], c->stream));
-    launch_step_fused(c->k, step, c->stream);
+    launch_queue(c->k, step, c->stream);
+    launch_decide(c->k, step, c->stream);
     CK(cudaEventRecord(ev[3], c->stream));
-    launch_scan(c->k, step + 1, 1, merge_q, c->stream);
-    launch_scatter_draw(c->k, step + 1, 1, 1, c->stream);
-    c->launches += 2 + 2 * (uint64_t)scan_kernels(c->k) + (uint64_t)step_fused_kernels(c->k);
+    launch_scan(c->k, step + 1, 0, merge_q, c->stream);
+    launch_rebuild_slots(c->k, step + 1, c->stream);
+    launch_draw(c->k, step + 1, c->stream);
+    c->launches += 7 + 2 * (uint64_t)scan_kernels(c->k);
     CK(cudaStreamSynchronize(c->stream));
     for (int j = 0; j < 3; ++j) CK(cudaEventElapsedTime(&ms[j], ev[j], ev[j + 1]));
     for (int j = 0; j < 4; ++j) cudaEventDestroy(ev[j]);
     c->csr_fresh = false;
+    c->t_next = t + 2;
     rc = launch_check(c);
     if (rc) return rc;
     return check_device_err(c);

@@ -30,10 +30,16 @@ struct psim_ctx {
     psim::OtherDiseaseEngine* other_disease = nullptr;
     int device = 0;
     cudaStream_t stream = nullptr;
-    // the day graph's second branch (the hot kernel beside the scan) and its
-    // fork / join events
+    // the day graph's second branch (the queue kernel beside the rebuild and
+    // the draws) and its fork / join events
     cudaStream_t stream2 = nullptr;
     cudaEvent_t fork_ev = nullptr, join_ev = nullptr, both_ev = nullptr, slots_ev = nullptr;
+    // Time base of the agents' decision timestamps: the next step that
+    // movement will process.  The device keeps move_at (absolute); a host
+    // countdown S (stepsUntilMove) is move_at - t_next.
+    uint32_t t_next = 0;
+    // counters of the profiled day graph (KArgs::prof when profiling)
+    unsigned long long* d_prof = nullptr;
     std::string err;
     KArgs k{};
     std::vector<void*> allocs;
@@ -77,8 +83,9 @@ struct psim_ctx {
     std::vector<std::pair<void*, size_t>> regions;
     size_t checkpoint_bytes = 0;
     std::map<uint32_t, void*> checkpoints;
+    std::map<uint32_t, uint32_t> checkpoint_t_next;
     // per-kernel timing inside the day graph: event-record nodes around the
-    // movement of step 0, every scan, every fused step and the last scatter
+    // movement of step 0 and every kernel group of every step
     bool profile = false;
     std::vector<cudaEvent_t> prof_ev;
     bool prof_valid = false;

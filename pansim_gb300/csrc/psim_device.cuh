@@ -16,6 +16,7 @@ constexpr int WB_W = 0, WB_N = 1, WB_M = 2, WB_S = 3, WB_D = 4;
 constexpr uint32_t ERR_LOCATION = 2u;      // an agent ended on an invalid location
 constexpr uint32_t ERR_TEST_WAIT = 4u;     // bounded-wait self test expired (expected in tests)
 constexpr uint32_t ERR_SCAN_WAIT = 1u;     // a scan tile gave up waiting for its predecessors
+constexpr uint32_t ERR_AGENT_LIST = 8u;    // the agent list disagrees with the histogram or work list
 
 struct DevModel {
     uint32_t n_states, n_variants, n_prog, n_agent_types;
@@ -59,7 +60,9 @@ struct DevAgents {
     const uint8_t* poss_type;
     const uint16_t* rep;          // replica of each agent
     uint32_t* location;
-    uint32_t* steps_until_move;
+    uint32_t* move_at;            // absolute timestamp of the agent's next decision: the
+                                  // reference's countdown stepsUntilMove after step t is
+                                  // move_at - t - 1 (u32 arithmetic)
     int8_t* state;
     int16_t* days;
     uint8_t* variant;
@@ -92,17 +95,14 @@ struct DevAgents {
     float* scaling_v;             // [V*N] symptom scaling of the states up to 6, per variant
     uint8_t* hcw;                 // healthcare worker flag
     uint32_t* rank;               // scratch of the canonical CSR ordering
-    uint32_t* worklist;           // agents queued for the cold half of a step (hot/cold variant),
-                                  // one segment per hot block
-    uint32_t* worklist_loc;       // beside each: its location (low 30 bits, WORK_LOC_MASK for an
-                                  // invalid one) | WORK_HZ | WORK_MOVE
+    uint32_t* worklist;           // agents that decide at the next step (k_queue), one segment
+                                  // per queue block
     uint32_t* seg_count;          // queued agents per segment
     uint32_t* home;               // [N] the agent's home: the first home-type entry of its location
                                   // list (findActualLocationForType's first match, no draw),
                                   // computed when the context is made or the home type changes
-    uint32_t* slot_loc;           // [N] the agents' locations at a step that rebuilds the agent
-                                  // list, recorded by the hot kernel for k_slots (which runs
-                                  // beside the cold kernel, whose movers rewrite `location`)
+    uint32_t* move_mask;          // [MOVE_MASK_WORDS] bit s: some agent decides at step s of the
+                                  // running day (a superset; rebuilt by the day's first step)
 };
 
 struct DevLocs {
@@ -122,6 +122,8 @@ struct DevLocs {
     uint32_t* cursor;             // [n] next free CSR slot of each location (scan: first slot)
     uint32_t* csr_off;            // [n+1] CSR offsets, derived from the cursors on demand
     uint32_t* csr_agents;         // [N]
+    float* slot_su;               // [V][N] beside each agent-list slot: the agent's susceptibility
+                                  // to the variant times its age band's factor
     uint32_t* qu_pending;         // quarantine writes of the running step
     unsigned long long* sfix;     // [V][n] fixed-point infectiousness sums
     float* hazard;                // [V][n] infection ratio of the last step
@@ -137,7 +139,9 @@ struct DevLocs {
                                   // [1] BUILD_PENDING (rebuild at the next scan) or the timestamp
                                   //     of the scan that took the pending rebuild,
                                   // [2] the timestamp of the last step that rebuilt (decided by
-                                  //     the step's first scan kernel, read by its later kernels)
+                                  //     the step's first scan kernel, read by its later kernels),
+                                  // [3] the timestamp of the last step whose decisions wrote a
+                                  //     location quarantine (merged by that step's scan)
 };
 
 // Incremental CSR: at most steps of a day no agent moves, and then the
@@ -177,9 +181,7 @@ struct DevTune {
     uint32_t agg_count;      // no effect: the histogram is updated by movers only
     uint32_t agg_slot;       // warp-aggregate the CSR slot atomics
     uint32_t blocks_per_sm;  // grid of the per-agent kernels (0 = one occupancy wave)
-    uint32_t variant;        // fused step kernel: 0/1/2 = one kernel capped at 64/40/32 registers,
-                             // 3 = hot/cold split (lean kernel + queued cold agents),
-                             // 4/5 = 2/4 agents per thread in flight
+    uint32_t variant;        // 3: the location-ordered step (the only form)
     uint32_t scan_items;     // locations per scan thread: 2, 4 or 8 (tile = 256 x items)
     uint32_t scan_mode;      // 0 = single pass with decoupled look-back, 1 = tile sums + scan,
                              // 2 = tile sums + scan with thread-contiguous locations (items 4, 8)
@@ -199,6 +201,17 @@ struct DevAdjoint {
     const int8_t* type_slot;      // [256] location type -> weight slot (-1: none)
 };
 
+// counters of the profiled day graph (KArgs::prof, null otherwise), summed
+// over the day's steps
+enum {
+    PROF_DRAW_ENTRIES = 0,   // agent-list entries the draw kernel expanded
+    PROF_DRAW_LOCATIONS = 1, // locations with their hazard-mask bit set it visited
+    PROF_MOVERS = 2,         // agents queued for a decision
+    PROF_QUEUE_STEPS = 3,    // steps whose queue kernel passed over the agents
+    PROF_REBUILDS = 4,       // steps that rebuilt the agent list
+    PROF_N = 8
+};
+
 struct KArgs {
     DevModel m;
     DevAgents a;
@@ -212,6 +225,7 @@ struct KArgs {
     uint32_t track_expected;
     DevTune tune;
     DevAdjoint adj;
+    unsigned long long* prof;  // [PROF_N] or null
 };
 
 // raw counter slots of DevStatsAcc::c
@@ -270,19 +284,22 @@ __device__ __forceinline__ void update_meta(const KArgs& k, uint32_t i) {
 // launchers (psim_kernels.cu)
 void launch_movement(const KArgs& k, uint32_t step_in_day, cudaStream_t s);
 void launch_count(const KArgs& k, cudaStream_t s);
+// merge_quarantine: 0 no, 1 at the steps whose decisions wrote location
+// quarantines, 2 always
 void launch_scan(const KArgs& k, uint32_t step_in_day, int with_hazard, int merge_quarantine, cudaStream_t s);
 void launch_scatter_draw(const KArgs& k, uint32_t step_in_day, int scatter, int draw, cudaStream_t s);
 void launch_offsets(const KArgs& k, cudaStream_t s);
-void launch_step_fused(const KArgs& k, uint32_t step_in_day, cudaStream_t s, int part = -1);
 int scan_kernels(const KArgs& k);
-// work-list segments of the hot/cold step (blocks of the hot kernel at most)
+// the day graph's step kernels (psim_kernels.cu, k_draw and around)
+void launch_rebuild_slots(const KArgs& k, uint32_t step_in_day, cudaStream_t s);
+void launch_draw(const KArgs& k, uint32_t step_in_day, cudaStream_t s);
+void launch_queue(const KArgs& k, uint32_t step_in_day, cudaStream_t s);
+void launch_decide(const KArgs& k, uint32_t step_in_day, cudaStream_t s);
+void launch_time_shift(uint32_t* a, uint32_t n, uint32_t delta, cudaStream_t s);
+// work-list segments of the decisions (blocks of the queue kernel at most)
 constexpr uint32_t WORK_MAX_BLOCKS = 152u * 64u;
-// the second word of a work-list entry: the agent draws (an infectious
-// agent is at its location), the agent moves at the next step (countdown at
-// zero or curfew; hazard-only agents have counted down in the hot kernel)
-constexpr uint32_t WORK_LOC_MASK = 0x3FFFFFFFu;
-constexpr uint32_t WORK_HZ = 0x80000000u;
-constexpr uint32_t WORK_MOVE = 0x40000000u;
+// words of the per-day mask of decision steps (1440 steps of one minute at most)
+constexpr uint32_t MOVE_MASK_WORDS = 48;
 
 // closure rules
 struct ClosureTypes {
@@ -292,7 +309,6 @@ struct ClosureTypes {
 void launch_masks(const KArgs& k, uint32_t home_type, double coef, int open, cudaStream_t s);
 void launch_close_types(const KArgs& k, const ClosureTypes& ty, int open, cudaStream_t s);
 void launch_expose(const KArgs& k, uint32_t t, uint32_t variant, double fraction, cudaStream_t s);
-int step_fused_kernels(const KArgs& k);
 void launch_canonical_csr(const KArgs& k, cudaStream_t s);
 void launch_progress(const KArgs& k, uint32_t t, cudaStream_t s);
 void launch_test(const KArgs& k, uint32_t t, cudaStream_t s);
@@ -303,6 +319,5 @@ void launch_plan(const KArgs& k, uint32_t t, cudaStream_t s);
 void launch_flag_hcw(const KArgs& k, cudaStream_t s);
 void launch_bounded_wait_probe(const KArgs& k, uint32_t iters, cudaStream_t s);
 void launch_type_weights(const KArgs& k, const float* w_by_type, cudaStream_t s);
-uint64_t launches_per_step(int quarantine);
 
 }  // namespace psim

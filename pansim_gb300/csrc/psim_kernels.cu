@@ -57,7 +57,9 @@ __device__ uint32_t find_location_range(const KArgs& k, uint32_t b, uint32_t e, 
     if (counter == 1) return k.a.poss_loc[pos];
     if (counter > 1) {
         uint32_t counter2 = counter, rand_idx = counter2;
-        for (;;) {
+        // the reference loops until the pick is open or its one retry is
+        // spent: a second pass always ends (retry is 0 by then)
+        for (int pass = 0; pass < 2; ++pass) {
             while (rand_idx == counter2) rand_idx = psim_below(rng, counter);
             counter2 = 0;
             for (uint32_t j = pos; j < e; ++j) {
@@ -86,8 +88,14 @@ __device__ __forceinline__ uint32_t find_location(const KArgs& k, uint32_t i, ui
     return find_location3(k, i, lt, retry, rng, k.p.home_type, k.p.school_type, k.p.work_type);
 }
 
-__device__ __forceinline__ void qu_write(const KArgs& k, uint32_t loc, uint32_t until) {
-    if (loc < k.l.n) atomicMax(&k.l.qu_pending[loc], until);
+// A location quarantine written by a decision at step t: merged into
+// quarantine_until by the scan of step t (build[3] = the step whose decisions
+// wrote; every writer of a step stores the same value).
+__device__ __forceinline__ void qu_write(const KArgs& k, uint32_t loc, uint32_t until, uint32_t t) {
+    if (loc < k.l.n) {
+        atomicMax(&k.l.qu_pending[loc], until);
+        k.l.build[3] = t;
+    }
 }
 
 // RealMovementOps::quarantineAgent, movementPolicies.h:176-245
@@ -103,7 +111,7 @@ __device__ void quarantine_agent(const KArgs& k, uint32_t i, uint32_t t, uint32_
     k.a.st_days_in_quarantine[i] += (until - t) / (24u * 60u / p.time_step);
     if (k.a.diagnosed[i]) {
         uint32_t my_home = find_location(k, i, p.home_type, 0, rng);
-        if (p.quarantine_policy > 1) qu_write(k, my_home, until);
+        if (p.quarantine_policy > 1) qu_write(k, my_home, until, t);
         if (p.quarantine_policy > 2 && prev_until < t) {
             uint32_t classroom = find_location(k, i, p.classroom_type, 0, rng);
             uint32_t work = find_location(k, i, p.work_type, 0, rng);
@@ -112,7 +120,7 @@ __device__ void quarantine_agent(const KArgs& k, uint32_t i, uint32_t t, uint32_
                 uint32_t loc = to_close[c];
                 if (loc != NONE && (loc_type(k, loc) == p.work_type || loc_type(k, loc) == p.classroom_type) &&
                     loc_qu(k, loc) < t && loc_open(k, loc) && loc_closed_until(k, loc) < t)
-                    qu_write(k, loc, until);
+                    qu_write(k, loc, until, t);
             }
         }
     }
@@ -135,19 +143,20 @@ __device__ void diagnose_and_quarantine(const KArgs& k, uint32_t i, uint32_t t, 
     quarantine_agent(k, i, t, t + k.p.quarantine_length * 24u * 60u / dt, rng);
 }
 
-__device__ __forceinline__ void stayed_home_check(const KArgs& k, uint32_t i, uint32_t agent_home) {
-    if (agent_home != NONE && k.a.location[i] != agent_home && k.a.steps_until_move[i] > 60u / k.p.time_step)
-        k.a.stayed_home[i] = 0;
+// S: the agent's countdown (stepsUntilMove) as the decision just set it
+__device__ __forceinline__ void stayed_home_check(const KArgs& k, uint32_t i, uint32_t agent_home, uint32_t S) {
+    if (agent_home != NONE && k.a.location[i] != agent_home && S > 60u / k.p.time_step) k.a.stayed_home[i] = 0;
 }
 
 // The full per-agent decision of doMovement once the countdown reached zero
 // (movementPolicies.h:333-1040).  The curfew and countdown prologue is in
-// k_movement.
+// move_agent.  S receives the agent's new countdown (stepsUntilMove after
+// the step); the caller turns it into the absolute timestamp of the next
+// decision.
 __device__ void move_decide(const KArgs& k, uint32_t i, uint32_t t, uint32_t minutes, uint32_t day, uint32_t sum,
-                            psim_stream* rng) {
+                            psim_stream* rng, uint32_t& S) {
     const psim_params& p = k.p;
     const uint32_t dt = p.time_step;
-    uint32_t* sum_ptr = &k.a.steps_until_move[i];
     // The agent's fields that the decision reads, loaded together: read where
     // they are needed, behind branches and stores, each costs a round trip
     // of its own.  None of them is written before that point.
@@ -168,7 +177,7 @@ __device__ void move_decide(const KArgs& k, uint32_t i, uint32_t t, uint32_t min
 
     uint32_t wb = k.m.state_wb[state_i];
     if (wb == WB_D) {
-        *sum_ptr = NONE;
+        S = NONE;
         k.a.location[i] = k.r.cemetery[k.a.rep[i]];
         return;
     }
@@ -176,13 +185,13 @@ __device__ void move_decide(const KArgs& k, uint32_t i, uint32_t t, uint32_t min
 
     if (h_ts <= t && h_until > t && wb != WB_S && wb != WB_D) {
         uint32_t x = h_until - t - 1;
-        *sum_ptr = x < sum ? x : sum;
+        S = x < sum ? x : sum;
         k.a.location[i] = fl(p.hospital_type, 0);
         if (!diag && k.a.infectious[i] != 0.0f) diagnose_and_quarantine(k, i, t, sum, rng);
         return;
     }
     if (wb == WB_S) {
-        *sum_ptr = sum;
+        S = sum;
         k.a.location[i] = fl(p.hospital_type, 0);
         if (!diag && k.a.infectious[i] != 0.0f) diagnose_and_quarantine(k, i, t, sum, rng);
         return;
@@ -193,10 +202,10 @@ __device__ void move_decide(const KArgs& k, uint32_t i, uint32_t t, uint32_t min
             if (k.a.quarantined[i] == 0) quarantine_agent(k, i, t, loc_qu(k, loc), rng);
             if (k.a.quarantined[i]) {
                 uint32_t x = loc_qu(k, k.a.location[i]) - t - 1;
-                *sum_ptr = x < sum ? x : sum;
+                S = x < sum ? x : sum;
                 uint32_t home_location = fl(p.home_type, 0);
                 if (home_location != k.a.location[i]) k.a.location[i] = home_location;
-                stayed_home_check(k, i, agent_home);
+                stayed_home_check(k, i, agent_home, S);
                 return;
             }
         }
@@ -209,8 +218,8 @@ __device__ void move_decide(const KArgs& k, uint32_t i, uint32_t t, uint32_t min
             quarantine_agent(k, i, t, t + p.quarantine_length * 24u * 60u / dt, rng);
         if (k.a.quarantined[i]) {
             k.a.location[i] = fl(p.home_type, 0);
-            *sum_ptr = sum;
-            stayed_home_check(k, i, agent_home);
+            S = sum;
+            stayed_home_check(k, i, agent_home, S);
             return;
         }
     }
@@ -233,7 +242,7 @@ __device__ void move_decide(const KArgs& k, uint32_t i, uint32_t t, uint32_t min
     if (act_b == -1 && act_e == -1) {  // Case 1
         new_type = wb == WB_S ? p.hospital_type : p.home_type;
         k.a.location[i] = fl(new_type, 0);
-        *sum_ptr = sum;
+        S = sum;
     }
     if (act_b != -1) {  // Case 2 and 4
         uint32_t num_pot = (uint32_t)((act_e == -1 ? act_b + 1 : act_e) - act_b);
@@ -292,21 +301,21 @@ __device__ void move_decide(const KArgs& k, uint32_t i, uint32_t t, uint32_t min
         }
         k.a.location[i] = new_loc;
         if (dur / 60u > 24u) {
-            *sum_ptr = sum;
+            S = sum;
         } else if (act_e == -1) {
-            *sum_ptr = (minutes + dur >= 1440u) ? sum : dur / dt;
+            S = (minutes + dur >= 1440u) ? sum : dur / dt;
         } else {
             // a read past the last event yields a 24:00 window
             const bool in = (uint32_t)act_e < k.m.n_events;
             uint32_t nstart = in ? k.m.ev_start[act_e] : 1440u, nend = in ? k.m.ev_end[act_e] : 1440u;
             if (minutes + dur < nstart) {
-                *sum_ptr = dur / dt;
+                S = dur / dt;
             } else if (minutes + dur > nend) {
-                *sum_ptr = td_minutes(nend - minutes) / dt - 1u;
+                S = td_minutes(nend - minutes) / dt - 1u;
             } else {
                 uint32_t st = td_minutes(nend - (minutes + dur)) / dt;
                 uint32_t extra = psim_below(rng, st);
-                *sum_ptr = dur / dt + extra;
+                S = dur / dt + extra;
             }
         }
         if (agent_type + 1 == 7 && p.enable_curfew && (p.curfew_begin <= minutes / dt || p.curfew_end > minutes / dt)) {
@@ -317,8 +326,8 @@ __device__ void move_decide(const KArgs& k, uint32_t i, uint32_t t, uint32_t min
     if (act_b == -1 && act_e != -1) {  // Case 3
         uint32_t length_steps = td_minutes((uint32_t)k.m.ev_end[act_e] - (uint32_t)k.m.ev_start[act_e]) / dt;
         uint32_t delay = psim_below(rng, length_steps);
-        *sum_ptr = td_minutes((uint32_t)k.m.ev_start[act_e] - minutes) / dt + delay;
-        uint32_t left = *sum_ptr;
+        S = td_minutes((uint32_t)k.m.ev_start[act_e] - minutes) / dt + delay;
+        uint32_t left = S;
         if (left < 30u / dt) {
         } else if (left < 60u / dt) {
             new_type = p.public_type;
@@ -334,10 +343,10 @@ __device__ void move_decide(const KArgs& k, uint32_t i, uint32_t t, uint32_t min
             if (!k.a.quarantined[i]) quarantine_agent(k, i, t, loc_qu(k, loc), rng);
             if (k.a.quarantined[i]) {
                 uint32_t x = loc_qu(k, k.a.location[i]) - t - 1;
-                *sum_ptr = x < sum ? x : sum;
+                S = x < sum ? x : sum;
                 uint32_t home_location = fl(p.home_type, 0);
                 if (home_location != k.a.location[i]) k.a.location[i] = home_location;
-                stayed_home_check(k, i, agent_home);
+                stayed_home_check(k, i, agent_home, S);
                 return;
             }
         }
@@ -345,13 +354,13 @@ __device__ void move_decide(const KArgs& k, uint32_t i, uint32_t t, uint32_t min
     if (new_type == p.hospital_type || (new_type == p.doctor_type && psim_u01(rng) * 1.0 < 0.7)) {
         if (!diag && k.a.infectious[i] != 0.0f) diagnose_and_quarantine(k, i, t, sum, rng);
     }
-    stayed_home_check(k, i, agent_home);
-    *sum_ptr = *sum_ptr - 1u;
+    stayed_home_check(k, i, agent_home, S);
+    S = S - 1u;
 }
 
 // curfew prologue of doMovement (movementPolicies.h:267-326); returns true if
-// the agent's step is finished.
-__device__ bool curfew_prologue(const KArgs& k, uint32_t i, uint32_t t, uint32_t sum, psim_stream* rng) {
+// the agent's step is finished (S, the countdown, then holds `sum`).
+__device__ bool curfew_prologue(const KArgs& k, uint32_t i, uint32_t t, uint32_t sum, psim_stream* rng, uint32_t& S) {
     const psim_params& p = k.p;
     uint32_t wb = wb_of(k, i);
     bool dead_or_hosp = (wb == WB_D || wb == WB_S);
@@ -362,13 +371,13 @@ __device__ bool curfew_prologue(const KArgs& k, uint32_t i, uint32_t t, uint32_t
         if (k.a.location[i] != workplace || workplace == NONE || loc_open(k, workplace) == 0) {
             k.a.location[i] = find_location(k, i, p.home_type, 0, rng);
             if (workplace == NONE || loc_open(k, workplace) == 0) {
-                k.a.steps_until_move[i] = sum;
+                S = sum;
                 return true;
             }
         }
         return false;
     }
-    k.a.steps_until_move[i] = sum;
+    S = sum;
     k.a.location[i] = find_location(k, i, p.home_type, 0, rng);
     return true;
 }
@@ -409,26 +418,56 @@ __device__ __forceinline__ StepClock step_clock(const KArgs& k, uint32_t step) {
     return c;
 }
 
-// doMovement for agent i (s = its steps_until_move, already loaded).
-__device__ __forceinline__ void move_agent(const KArgs& k, uint32_t i, const StepClock& c, uint32_t s) {
-    if (c.curfew_now || s == 0) {
-        const uint32_t rep = k.a.rep[i];
-        psim_stream rng;
-        psim_stream_init(&rng, k.r.seed[rep], i - k.r.agent_off[rep], c.t, PSIM_PHASE_MOVE);
-        bool done = false;
-        if (c.curfew_now) {
-            done = curfew_prologue(k, i, c.t, c.sum, &rng);
-            s = k.a.steps_until_move[i];
-        }
-        if (!done) {
-            if (s > 0)
-                k.a.steps_until_move[i] = s - 1;
-            else
-                move_decide(k, i, c.t, c.minutes, c.day, c.sum, &rng);
-        }
-    } else {
-        k.a.steps_until_move[i] = s - 1;
+// The countdown of the reference (stepsUntilMove: decremented every step,
+// a decision when it reaches zero) is kept as the absolute timestamp of the
+// agent's next decision, move_at = t + 1 + stepsUntilMove after step t (u32
+// arithmetic: the dead agents' NONE countdown wraps like the reference's).
+// Before step t the countdown is move_at - t; only a decision or the curfew
+// prologue writes move_at, so the steps in between touch nothing.  The
+// library converts to and from countdowns at upload and download (time base
+// t_next, psim_api.cu).
+//
+// Steps of the running day at which some agent decides: one bit per step in
+// move_mask, set by whoever writes such a move_at (through a block-shared
+// copy, one global atomic per word and block).  The day graph's kernels read
+// it to skip the steps nobody decides at.
+__device__ __forceinline__ void mask_clear_shared(uint32_t* s_mm) {
+    for (uint32_t w = threadIdx.x; w < MOVE_MASK_WORDS; w += blockDim.x) s_mm[w] = 0u;
+    __syncthreads();
+}
+__device__ __forceinline__ void mask_note(const KArgs& k, uint32_t* s_mm, uint32_t m) {
+    const uint32_t s = m - k.clock->t0;
+    if (s < k.spd) atomicOr(&s_mm[s >> 5], 1u << (s & 31u));
+}
+__device__ __forceinline__ void mask_flush(const KArgs& k, uint32_t* s_mm) {
+    __syncthreads();
+    for (uint32_t w = threadIdx.x; w < MOVE_MASK_WORDS; w += blockDim.x)
+        if (s_mm[w]) atomicOr(&k.a.move_mask[w], s_mm[w]);
+}
+__device__ __forceinline__ bool mask_has(const KArgs& k, uint32_t s) {
+    return s < k.spd && ((k.a.move_mask[s >> 5] >> (s & 31u)) & 1u) != 0;
+}
+
+// doMovement for agent i at step c.t; s = its countdown before the step
+// (move_at - c.t).  Writes move_at when the agent decides or the curfew
+// prologue resets its countdown.
+__device__ __forceinline__ void move_agent(const KArgs& k, uint32_t i, const StepClock& c, uint32_t s, uint32_t* s_mm) {
+    if (!(c.curfew_now || s == 0)) return;  // counts down: move_at stays
+    const uint32_t rep = k.a.rep[i];
+    psim_stream rng;
+    psim_stream_init(&rng, k.r.seed[rep], i - k.r.agent_off[rep], c.t, PSIM_PHASE_MOVE);
+    bool done = false;
+    uint32_t S = s;
+    if (c.curfew_now) done = curfew_prologue(k, i, c.t, c.sum, &rng, S);
+    if (!done) {
+        if (S > 0)
+            S = S - 1u;
+        else
+            move_decide(k, i, c.t, c.minutes, c.day, c.sum, &rng, S);
     }
+    const uint32_t m = c.t + 1u + S;
+    k.a.move_at[i] = m;
+    mask_note(k, s_mm, m);
 }
 
 // Scan tiles: 256 threads x ITEMS locations (ITEMS = 2, 4 or 8, a tuning
@@ -653,8 +692,12 @@ __device__ __forceinline__ void add_expected(const KArgs& k, bool act, uint32_t 
     if ((int)(threadIdx.x & 31) == leader) atomicAdd(&k.r.expected[rep], tot);
 }
 
-// Movement of every agent + histogram + fixed-point infectiousness sums.
+// Movement of every agent + histogram + fixed-point infectiousness sums (the
+// day's first step, after a reset of the sums, and the per-phase entry
+// points).  Records the steps of the day at which agents decide next.
 __global__ void __launch_bounds__(256) k_movement(KArgs k, uint32_t step) {
+    __shared__ uint32_t s_mm[MOVE_MASK_WORDS];
+    mask_clear_shared(s_mm);
     const uint32_t N = k.a.n;
     const StepClock c = step_clock(k, step);
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -665,16 +708,23 @@ __global__ void __launch_bounds__(256) k_movement(KArgs k, uint32_t step) {
         uint32_t loc = NONE, loc0 = NONE, var = 0;
         float inf = 0.0f;
         if (act) {
-            const uint32_t s = k.a.steps_until_move[i];
+            const uint32_t m0 = k.a.move_at[i];
+            const uint32_t s = m0 - c.t;
             loc0 = k.a.location[i];
             inf = k.a.infectious[i];
-            move_agent(k, i, c, s);
-            loc = (c.curfew_now || s == 0) ? k.a.location[i] : loc0;
+            move_agent(k, i, c, s, s_mm);
+            if (c.curfew_now || s == 0) {
+                loc = k.a.location[i];
+            } else {
+                loc = loc0;
+                mask_note(k, s_mm, m0);  // an agent counting down decides later today
+            }
             if (inf > 0.0f) var = k.a.variant[i];
         }
         moved |= count_agent(k, act, loc0, loc, inf, var);
     }
     publish_moved(k, moved, c.t);
+    mask_flush(k, s_mm);
 }
 
 // Histogram + fixed-point sums without movement (regroup after an upload).
@@ -829,6 +879,10 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan(KArgs k, uint32_t step, i
     // before (no prefix, no cursor writes).
     const uint32_t t_step = k.clock->t0 + step;
     const bool rebuild = LOOKBACK ? csr_decide(k, t_step) : csr_rebuild(k, t_step);
+    // merge_q 1: the location quarantines are merged at the steps whose
+    // decisions wrote some (the day graph); 2: at every call
+    merge_q = merge_q == 2 || (merge_q == 1 && k.l.build[3] == t_step);
+    if (!rebuild && !with_hazard && !merge_q) return;
     uint32_t tile = blockIdx.x;
     if (LOOKBACK && rebuild) {
         scan_take_ticket(k, &s_tile, &s_epoch);
@@ -999,6 +1053,8 @@ __global__ void __launch_bounds__(SCAN_THREADS) k_scan_v(KArgs k, uint32_t step,
     // the counts are read at the flagged locations only
     const uint32_t t_step = k.clock->t0 + step;
     const bool rebuild = LOOKBACK ? csr_decide(k, t_step) : csr_rebuild(k, t_step);
+    merge_q = merge_q == 2 || (merge_q == 1 && k.l.build[3] == t_step);
+    if (!rebuild && !with_hazard && !merge_q) return;
     uint32_t tile = blockIdx.x;
     if (LOOKBACK && rebuild) {
         scan_take_ticket(k, &s_tile, &s_epoch);
@@ -1140,410 +1196,429 @@ __global__ void __launch_bounds__(256) k_scatter_draw(KArgs k, uint32_t step, in
     grad_end(k, s_grad);
 }
 
-// Scatter + draw of step `step` fused with the movement and histogram of
-// step + 1.  Both halves touch only agent i's own state and per-location
-// counters that the scan of `step` has already reset, so per agent they run
-// back to back in one pass; used inside the day graph.
-template <int MINB>
-__global__ void __launch_bounds__(256, MINB) k_step_fused(KArgs k, uint32_t step) {
-    __shared__ double s_grad[GRAD_N];
-    grad_begin(k, s_grad);
-    const uint32_t N = k.a.n, L = k.l.n;
-    const uint32_t t = k.clock->t0 + step;
-    const bool rebuild = csr_rebuild(k, t);
-    const StepClock c = step_clock(k, step + 1);
-    const uint32_t stride = gridDim.x * blockDim.x;
-    bool moved = false;
-    for (uint32_t base = blockIdx.x * blockDim.x; base < N; base += stride) {
-        const uint32_t i = base + threadIdx.x;
-        const bool act = i < N;
-        // independent loads first
-        const uint32_t loc0 = act ? k.a.location[i] : NONE;
-        const uint32_t s = act ? k.a.steps_until_move[i] : 0u;
-        float inf = act ? k.a.infectious[i] : 0.0f;
-        const float inf0 = inf;
-        const uint32_t var0 = inf0 > 0.0f ? k.a.variant[i] : 0u;
-        const bool ok = act && loc0 < L;
-        bool hz = false;
-        const float h0 = ok ? hazard_at(k, loc0, &hz) : 0.0f;
-        const uint32_t pos = take_slot(k, ok, loc0, rebuild);
-        double term = 0.0;
-        uint32_t loc = NONE, var = 0;
-        if (ok) {
-            store_slot(k, pos, i);
-            if (hz) {
-                term = draw_agent(k, i, loc0, t, h0, s_grad);
-                inf = k.a.infectious[i];
-            }
-        }
-        if (act) {
-            move_agent(k, i, c, s);
-            loc = (c.curfew_now || s == 0) ? k.a.location[i] : loc0;
-            if (inf > 0.0f) var = k.a.variant[i];
-        }
-        if (k.track_expected) add_expected(k, act, i, term);
-        moved |= count_agent_delta(k, act, loc0, loc, inf0, var0, inf, var);
+// ---------------------------------------------------------------------------
+// The day graph's step kernels.  Per timestep t of the day (step s):
+//   k_scan_v / k_tile_sums_v  only when agents took new locations for t (or a
+//                  rebuild is pending): the prefix of the histogram into the
+//                  locations' first slots; also the merge of the step's
+//                  location quarantine writes when there were any
+//   k_rebuild_slots           the agent list of such a step: every agent takes
+//                  a slot at its location, and the slot keeps the agent's
+//                  susceptibility x age-band factor of every variant
+//   k_draw         the per-location infection ratio and the infection draws,
+//                  location by location over the locations with an infectious
+//                  agent, from the agent list (LocationsList::infectAgents,
+//                  locationList.h:233-310, with the ratio of
+//                  BasicInfection::infectionsAtLocations,
+//                  infectionPolicies.h:520-546)
+//   k_queue        beside the three above: the agents that decide at step
+//                  s + 1 (move_at == t + 1, or everyone at the curfew step),
+//                  queued in per-block work-list segments
+//   k_decide       after k_draw and k_queue: doMovement of the queued agents
+//                  for step s + 1 and the histogram/sum deltas of their moves
+// A step at which nobody takes a new location and nobody decides at the next
+// step runs only k_draw (the others return at their first loads): its cost
+// is the agents at the infectious locations, not the whole population.
+
+// Slot data of the agent list: csr_agents[pos] = agent, slot_su[v][pos] =
+// its susceptibility to variant v times its age band's factor (the product
+// the draw compares with), written when the list is rebuilt and by the draw
+// that infects the agent.
+__device__ __forceinline__ void slot_fill(const KArgs& k, uint32_t pos, uint32_t i) {
+    const uint32_t N = k.a.n;
+    if (pos >= N) {
+        atomicOr(k.err, ERR_LOCATION);
+        return;
     }
-    publish_moved(k, moved, c.t);
-    grad_end(k, s_grad);
+    k.l.csr_agents[pos] = i;
+    const float sigma = k.p.sigma_band[k.a.band[i]];
+    for (uint32_t v = 0; v < k.m.n_variants; ++v)
+        k.l.slot_su[(size_t)v * N + pos] = k.a.susceptible[(size_t)v * N + i] * sigma;
 }
 
-// k_step_fused with U agents per thread in flight: the location, countdown
-// and infectiousness loads of all U agents are issued first, then their
-// hazard gathers and CSR slot atomics (plain returning atomics), then the
-// slot stores; the draw / movement / histogram of each agent follows as in
-// k_step_fused.  The per-agent chain load -> gather/atomic -> store is what
-// bounds the single-agent form, so U independent chains per thread multiply
-// the memory-level parallelism at the same occupancy.
-template <int U>
-__global__ void __launch_bounds__(256) k_step_ilp(KArgs k, uint32_t step) {
-    __shared__ double s_grad[GRAD_N];
-    grad_begin(k, s_grad);
-    const uint32_t N = k.a.n, L = k.l.n;
-    const uint32_t t = k.clock->t0 + step;
-    const StepClock c = step_clock(k, step + 1);
-    const bool rebuild = csr_rebuild(k, t);
-    const uint32_t chunk = 256u * U;
-    bool moved = false;
-    for (uint32_t base = blockIdx.x * chunk; base < N; base += gridDim.x * chunk) {
-        uint32_t loc0[U], s[U], pos[U];
-        float inf[U], h0[U];
-        bool hz[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const uint32_t i = base + u * 256u + threadIdx.x;
-            const bool act = i < N;
-            loc0[u] = act ? k.a.location[i] : NONE;
-            s[u] = act ? k.a.steps_until_move[i] : 0u;
-            inf[u] = act ? k.a.infectious[i] : 0.0f;
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const bool ok = loc0[u] < L;
-            hz[u] = false;
-            h0[u] = ok ? hazard_at(k, loc0[u], &hz[u]) : 0.0f;
-            pos[u] = !rebuild ? SLOT_KEEP : ok ? atomicAdd(&k.l.cursor[loc0[u]], 1u) : NONE;
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const uint32_t i = base + u * 256u + threadIdx.x;
-            if (loc0[u] < L) store_slot(k, pos[u], i);
-        }
-#pragma unroll 1
-        for (int u = 0; u < U; ++u) {
-            const uint32_t i = base + u * 256u + threadIdx.x;
-            const bool act = i < N;
-            double term = 0.0;
-            uint32_t loc = NONE, var = 0;
-            float fi = inf[u];
-            const uint32_t var0 = inf[u] > 0.0f ? k.a.variant[i] : 0u;
-            if (act && loc0[u] < L && hz[u]) {
-                term = draw_agent(k, i, loc0[u], t, h0[u], s_grad);
-                fi = k.a.infectious[i];
-            }
-            if (act) {
-                move_agent(k, i, c, s[u]);
-                loc = (c.curfew_now || s[u] == 0) ? k.a.location[i] : loc0[u];
-                if (fi > 0.0f) var = k.a.variant[i];
-            }
-            if (k.track_expected) add_expected(k, act, i, term);
-            moved |= count_agent_delta(k, act, loc0[u], loc, inf[u], var0, fi, var);
-        }
-    }
-    publish_moved(k, moved, c.t);
-    grad_end(k, s_grad);
-}
-
-// Hot/cold form of k_step_fused.  The hot kernel does, for every agent, the
-// CSR slot of step `step` (when the step rebuilds the agent list) and the
-// countdown of every agent that does not move at step + 1.  Movers (countdown
-// at zero, curfew) and agents at a location with an infectious agent (they
-// draw) -- a few percent per step, the movers each with a long chain of
-// dependent loads in the movement decision -- are queued in the block's own
-// segment of the work list (shared-memory counter, no global contention)
-// with their location and flags, and k_step_cold runs them densely, a block
-// per segment.  Per agent the operations and their order are those of
-// k_step_fused.
-__global__ void __launch_bounds__(256, 8) k_step_hot(KArgs k, uint32_t step, uint32_t cap) {
-    __shared__ uint32_t s_cnt;
-    if (threadIdx.x == 0) s_cnt = 0u;
-    __syncthreads();
-    const uint32_t N = k.a.n, L = k.l.n;
-    const uint32_t dt = k.p.time_step;
-    const uint32_t minutes = (step + 1) * dt;
-    const bool curfew_now = k.p.enable_curfew && k.p.curfew_begin == minutes / dt;
-    // a step that rebuilds the agent list: the locations for k_slots
-    const bool rebuild = csr_peek(k, k.clock->t0 + step);
-    const uint32_t stride = gridDim.x * blockDim.x;
-    uint32_t* seg = k.a.worklist + (size_t)blockIdx.x * cap;
-    uint32_t* segl = k.a.worklist_loc + (size_t)blockIdx.x * cap;
-    const int lane = threadIdx.x & 31;
-    // the next iteration's agent columns are loaded one iteration ahead
-    uint32_t base = blockIdx.x * blockDim.x;
-    uint32_t n_loc = NONE, n_s = 0u;
-    if (base + threadIdx.x < N) {
-        n_loc = k.a.location[base + threadIdx.x];
-        n_s = k.a.steps_until_move[base + threadIdx.x];
-    }
-    for (; base < N; base += stride) {
-        const uint32_t i = base + threadIdx.x;
-        const bool act = i < N;
-        const uint32_t loc0 = n_loc;
-        const uint32_t s = n_s;
-        const uint32_t j = i + stride;
-        if (j < N) {
-            n_loc = k.a.location[j];
-            n_s = k.a.steps_until_move[j];
-        }
-        const bool ok = act && loc0 < L;
-        bool hz = false;
-        if (ok) hazard_at(k, loc0, &hz);
-        if (rebuild && act) k.a.slot_loc[i] = loc0;
-        // movers (countdown at zero, curfew) go to the cold kernel whole;
-        // the others count down here and go there only to draw (or to
-        // report an invalid location)
-        const bool mover = act && (curfew_now || s == 0);
-        const bool cold = mover || (act && (hz || !ok));
-        if (act && !mover) k.a.steps_until_move[i] = s - 1;
-        const unsigned cm = __ballot_sync(0xffffffffu, cold);
-        if (cm) {
-            uint32_t basew = 0;
-            if (lane == __ffs(cm) - 1) basew = atomicAdd(&s_cnt, (uint32_t)__popc(cm));
-            basew = __shfl_sync(0xffffffffu, basew, __ffs(cm) - 1);
-            if (cold) {
-                const uint32_t q = basew + __popc(cm & lanemask_lt());
-                seg[q] = i;
-                segl[q] = (ok ? loc0 : WORK_LOC_MASK) | (hz ? WORK_HZ : 0u) | (mover ? WORK_MOVE : 0u);
-            }
-        }
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) k.a.seg_count[blockIdx.x] = s_cnt;
-}
-
-// The agent list of a step whose agents took new locations (k_step_hot's
-// variants): every agent takes a slot at the location k_step_hot recorded
-// for it, whose cursor the scan set to the location's first slot.  It runs
-// after both and beside the cold kernel.  Returns at once when the step
-// keeps the agent list of the step before.
-// With plain slot atomics each thread has SLOT_ILP agents' atomics in flight
-// (their returns are what the pass waits for); the warp-aggregated form
-// (tune.agg_slot) takes one agent per thread and trip.
 constexpr int SLOT_ILP = 4;
-__global__ void __launch_bounds__(256, 8) k_slots(KArgs k, uint32_t step) {
+__global__ void __launch_bounds__(256, 8) k_rebuild_slots(KArgs k, uint32_t step) {
     if (!csr_rebuild(k, k.clock->t0 + step)) return;
+    if (k.prof && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&k.prof[PROF_REBUILDS], 1ull);
     const uint32_t N = k.a.n, L = k.l.n;
     if (k.tune.agg_slot) {
         for (uint32_t base = blockIdx.x * blockDim.x; base < N; base += gridDim.x * blockDim.x) {
             const uint32_t i = base + threadIdx.x;
             const bool act = i < N;
-            const uint32_t loc = act ? k.a.slot_loc[i] : NONE;
+            const uint32_t loc = act ? k.a.location[i] : NONE;
             const bool ok = act && loc < L;
             const uint32_t pos = take_slot(k, ok, loc, true);
-            if (ok) store_slot(k, pos, i);
+            if (ok) slot_fill(k, pos, i);
         }
         return;
     }
+    // SLOT_ILP agents' returning atomics in flight per thread
     const uint32_t tile = blockDim.x * SLOT_ILP;
     for (uint32_t base = blockIdx.x * tile; base < N; base += gridDim.x * tile) {
         uint32_t loc[SLOT_ILP], pos[SLOT_ILP];
 #pragma unroll
         for (int u = 0; u < SLOT_ILP; ++u) {
             const uint32_t i = base + u * blockDim.x + threadIdx.x;
-            loc[u] = i < N ? k.a.slot_loc[i] : NONE;
+            loc[u] = i < N ? k.a.location[i] : NONE;
         }
 #pragma unroll
         for (int u = 0; u < SLOT_ILP; ++u) pos[u] = loc[u] < L ? atomicAdd(&k.l.cursor[loc[u]], 1u) : NONE;
 #pragma unroll
         for (int u = 0; u < SLOT_ILP; ++u)
-            if (loc[u] < L) store_slot(k, pos[u], base + u * blockDim.x + threadIdx.x);
+            if (loc[u] < L) slot_fill(k, pos[u], base + u * blockDim.x + threadIdx.x);
     }
 }
 
-// k_step_hot with U agents per thread in flight: the loads, mask reads and
-// slot atomics of all U agents are issued before any of them is needed.  A
-// block visits U * 256 consecutive agents per trip; its work-list segment
-// holds `cap` entries (a multiple of U * 256).
-template <int U>
-__global__ void __launch_bounds__(256, 8) k_step_hot_ilp(KArgs k, uint32_t step, uint32_t cap) {
+// expected-infection accumulation of the draw kernel: one atomic per replica
+// present in the warp (warp-collective; rep given, not looked up)
+__device__ __forceinline__ void add_expected_rep(const KArgs& k, bool act, uint32_t rep, double term) {
+    const unsigned am = __ballot_sync(0xffffffffu, act && term != 0.0);
+    if (!(act && term != 0.0)) return;
+    const unsigned peers = __match_any_sync(am, rep);
+    const int leader = __ffs(peers) - 1;
+    unsigned rest = peers;
+    double tot = 0.0;
+    while (rest) {
+        const int src = __ffs(rest) - 1;
+        tot += __shfl_sync(peers, term, src);
+        rest &= rest - 1;
+    }
+    if ((int)(threadIdx.x & 31) == leader) atomicAdd(&k.r.expected[rep], tot);
+}
+
+// DynamicPPState::gotInfected (dynamicPPState.cpp:235-244) and the agent's
+// statistics (locationList.h:283-304)
+__device__ __forceinline__ void infect_agent(const KArgs& k, uint32_t i, uint32_t v, uint32_t loc, uint32_t t) {
+    k.a.state[i] = (int8_t)k.m.first_infected;
+    k.a.variant[i] = (uint8_t)v;
+    k.a.days[i] = -2;
+    update_meta(k, i);
+    k.a.st_infected_ts[i] = t;
+    k.a.st_infected_count[i] = k.a.st_infected_count[i] + 1;
+    k.a.st_infected_loc[i] = loc;
+    k.a.st_worst_state[i] = (int8_t)k.m.first_infected;
+    k.a.st_worst_ts[i] = t;
+    k.a.st_variant_mask[i] |= 1u << v;
+}
+
+// Hazards of every variant at location l from its fixed-point sums and count
+// (the scan's formula); returns whether some variant's sum is nonzero.
+__device__ __forceinline__ bool location_hazards(const KArgs& k, uint32_t l, uint32_t n_l, float season, uint32_t dt) {
+    const uint32_t L = k.l.n, V = k.m.n_variants;
+    const uint32_t rep = k.l.rep[l];
+    const float w_l = k.l.infectiousness[l];
+    const float k_f = k.r.k_f[rep];
+    bool nz = false;
+    for (uint32_t v = 0; v < V; ++v) {
+        const size_t idx = (size_t)v * L + l;
+        const long long fix = (long long)k.l.sfix[idx];
+        float h = 0.0f, x = 0.0f;
+        if (fix != 0) {
+            h = psim_hazard_x(fix, n_l, k_f, w_l, season, dt, &x);
+            nz = true;
+        }
+        k.l.hazard[idx] = h;
+        if (k.adj.on) k.l.hazard_x[idx] = x;
+    }
+    return nz;
+}
+
+// Position of the n-th (0-based) set bit of w, n < popc(w): five halvings,
+// each keeping the half that holds it.
+__device__ __forceinline__ uint32_t nth_set_bit(uint32_t w, uint32_t n) {
+    uint32_t pos = 0;
+#pragma unroll
+    for (int width = 16; width > 0; width >>= 1) {
+        const uint32_t c = __popc(w & ((1u << width) - 1u));
+        if (n >= c) {
+            n -= c;
+            w >>= width;
+            pos += (uint32_t)width;
+        }
+    }
+    return pos;
+}
+
+// The r-th set bit (0-based) of the chunk's words held by lanes 0..DRAW_WPW-1,
+// given each lane's inclusive prefix of the set-bit counts: the word index
+// within the chunk and the bit (meaningful for r below the chunk's total
+// only).  Every lane of the warp calls it, and every shuffle runs on all
+// lanes.
+constexpr int DRAW_WPW = 8;  // mask words per warp chunk (256 locations)
+__device__ __forceinline__ void chunk_bit(uint32_t r, uint32_t words, uint32_t inc, uint32_t* wo, uint32_t* bit) {
+    uint32_t o = 0;
+#pragma unroll
+    for (int q = 0; q < DRAW_WPW - 1; ++q) o += r >= __shfl_sync(0xffffffffu, inc, q) ? 1u : 0u;
+    const uint32_t w = __shfl_sync(0xffffffffu, words, (int)o);
+    const uint32_t before = __shfl_sync(0xffffffffu, inc, o > 0 ? (int)o - 1 : 0);
+    const uint32_t exc = o > 0 ? before : 0u;
+    *wo = o;
+    *bit = nth_set_bit(w, r - exc) & 31u;
+}
+
+// Location-ordered infection of step `step`.  A warp takes a chunk of
+// DRAW_WPW mask words (32 locations each).  Pass 1: the dirty locations
+// (sum or count changed since their last evaluation) get their hazards
+// recomputed and their hazard-mask bits rewritten.  Pass 2: every location
+// whose bit is set has its agent-list segment expanded over the lanes (a warp
+// scan of the segment lengths, each lane finds its entry's location by a
+// binary search) and each agent draws from its Philox stream (seed, agent,
+// t); the slot holds the susceptibility product, so an agent that is not
+// infected costs two coalesced loads of its slot.  An agent that is infected
+// changes its own location's sum (a delta for the next step: only this warp
+// reads that location's sum in this step).
+__global__ void __launch_bounds__(256, 4) k_draw(KArgs k, uint32_t step) {
+    __shared__ double s_grad[GRAD_N];
+    __shared__ uint32_t s_nz[8][DRAW_WPW];
+    grad_begin(k, s_grad);
+    const uint32_t L = k.l.n, N = k.a.n, V = k.m.n_variants;
+    const uint32_t t = k.clock->t0 + step;
+    const float season = k.clock->season;
+    const uint32_t dt = k.p.time_step;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t n_words = (L + 31) >> 5;
+    const uint32_t n_chunks = (n_words + DRAW_WPW - 1) / DRAW_WPW;
+    const uint32_t nw = gridDim.x * (blockDim.x >> 5);
+    uint32_t entries = 0, visited = 0;  // counted for the profiling figures
+    for (uint32_t ch = blockIdx.x * (blockDim.x >> 5) + warp; ch < n_chunks; ch += nw) {
+        const uint32_t w0 = ch * DRAW_WPW;
+        const bool own = lane < DRAW_WPW && w0 + lane < n_words;
+        uint32_t hm = own ? k.l.hmask[w0 + lane] : 0u;
+        const uint32_t sm = own ? k.l.smask[w0 + lane] : 0u;
+        if (!__any_sync(0xffffffffu, (hm | sm) != 0u)) continue;
+        // pass 1: the dirty locations
+        if (__any_sync(0xffffffffu, sm != 0u)) {
+            if (lane < DRAW_WPW) s_nz[warp][lane] = 0u;
+            __syncwarp();
+            uint32_t inc = __popc(sm);
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += y;
+            }
+            const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
+            for (uint32_t b0 = 0; b0 < total; b0 += 32) {
+                const uint32_t r = b0 + lane;
+                uint32_t wo, bit;
+                chunk_bit(r, sm, inc, &wo, &bit);
+                const uint32_t l = (w0 + wo) * 32u + bit;
+                if (r < total && l < L) {
+                    if (location_hazards(k, l, k.l.counts[l], season, dt)) atomicOr(&s_nz[warp][wo], 1u << bit);
+                }
+            }
+            __syncwarp();
+            if (own && sm) {
+                hm = (hm & ~sm) | s_nz[warp][lane];
+                k.l.hmask[w0 + lane] = hm;
+                k.l.smask[w0 + lane] = 0u;
+            }
+            // the mask stores and hazards above come before this warp's
+            // infections mark their locations for the next step
+            __syncwarp();
+            __threadfence_block();
+        }
+        // pass 2: the agents of the locations whose hazard-mask bit is set
+        uint32_t inc = __popc(hm);
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += y;
+        }
+        const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
+        visited += total;
+        for (uint32_t b0 = 0; b0 < total; b0 += 32) {
+            const uint32_t r = b0 + lane;
+            uint32_t wo, bit;
+            chunk_bit(r, hm, inc, &wo, &bit);
+            const uint32_t l = (w0 + wo) * 32u + bit;
+            uint32_t len = 0, beg = 0, rep = 0;
+            float h0 = 0.0f;
+            if (r < total && l < L) {
+                len = k.l.counts[l];
+                const uint32_t end = k.l.cursor[l];
+                h0 = k.l.hazard[l];
+                rep = k.l.rep[l];
+                // a histogram that disagrees with the agent list is reported
+                // and the location skipped, never expanded
+                if (len > end || end > N) {
+                    atomicOr(k.err, ERR_AGENT_LIST);
+                    len = 0;
+                }
+                beg = end - len;
+            }
+            // the segments of these (up to 32) locations over the lanes
+            uint32_t einc = len;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, einc, o);
+                if (lane >= o) einc += y;
+            }
+            const uint32_t etotal = __shfl_sync(0xffffffffu, einc, 31);
+            entries += lane == 0 ? etotal : 0u;
+            for (uint32_t e0 = 0; e0 < etotal; e0 += 32) {
+                const uint32_t e = e0 + lane;
+                // owner lane: the number of lanes whose inclusive end is <= e
+                uint32_t q = 0;
+#pragma unroll
+                for (int st = 16; st > 0; st >>= 1) {
+                    const uint32_t v = __shfl_sync(0xffffffffu, einc, (int)(q + st - 1));
+                    if (e >= v) q += st;
+                }
+                q &= 31u;
+                const uint32_t q_inc = __shfl_sync(0xffffffffu, einc, (int)q);
+                const uint32_t q_len = __shfl_sync(0xffffffffu, len, (int)q);
+                const uint32_t q_beg = __shfl_sync(0xffffffffu, beg, (int)q);
+                const uint32_t q_loc = __shfl_sync(0xffffffffu, l, (int)q);
+                const uint32_t q_rep = __shfl_sync(0xffffffffu, rep, (int)q);
+                const float q_h0 = __shfl_sync(0xffffffffu, h0, (int)q);
+                bool act = e < etotal;
+                double term = 0.0;
+                const uint32_t pos = q_beg + (e - (q_inc - q_len));
+                uint32_t i = NONE;
+                if (act) {
+                    // an agent list that disagrees with the histogram is
+                    // reported, never read out of bounds
+                    if (pos < N) i = k.l.csr_agents[pos];
+                    if (i >= N) {
+                        atomicOr(k.err, ERR_AGENT_LIST);
+                        act = false;
+                    }
+                }
+                if (act) {
+                    const float su0 = k.l.slot_su[pos];
+                    const unsigned long long seed = k.r.seed[q_rep];
+                    const uint32_t li = i - k.r.agent_off[q_rep];
+                    bool infected = false;
+                    float inf0 = 0.0f, sigma = 0.0f;
+                    uint32_t var0 = 0;
+                    for (uint32_t v = 0; v < V; ++v) {
+                        const float h = v == 0 ? q_h0 : k.l.hazard[(size_t)v * L + q_loc];
+                        if (!(h > 0.0f)) continue;
+                        if (!k.r.variant_active[q_rep * V + v]) continue;
+                        // after an infection the later variants read the
+                        // agent's new susceptibility (what the slot then gets)
+                        float s_eff;
+                        if (!infected)
+                            s_eff = v == 0 ? su0 : k.l.slot_su[(size_t)v * N + pos];
+                        else
+                            s_eff = k.a.susceptible[(size_t)v * N + i] * sigma;
+                        if (!(s_eff > 0.0f)) continue;
+                        const float pf = h * s_eff;
+                        term += pf < 1.0f ? (double)pf : 1.0;
+                        if (k.adj.on && pf < 1.0f)
+                            adjoint_terms(k, i, q_loc, v, q_rep, h, k.a.susceptible[(size_t)v * N + i], s_eff, s_grad);
+                        const double U = psim_u01_once(seed, li, t, PSIM_PHASE_INFECT + v);
+                        if (U < (double)pf) {
+                            if (!infected) {
+                                inf0 = k.a.infectious[i];
+                                var0 = inf0 > 0.0f ? k.a.variant[i] : 0u;
+                                sigma = k.p.sigma_band[k.a.band[i]];
+                                infected = true;
+                            }
+                            infect_agent(k, i, v, q_loc, t);
+                        }
+                    }
+                    if (infected) {
+                        for (uint32_t v = 0; v < V; ++v)
+                            k.l.slot_su[(size_t)v * N + pos] = k.a.susceptible[(size_t)v * N + i] * sigma;
+                        const float inf = k.a.infectious[i];
+                        const uint32_t var = inf > 0.0f ? k.a.variant[i] : 0u;
+                        count_agent_delta(k, true, q_loc, q_loc, inf0, var0, inf, var);
+                    }
+                }
+                if (k.track_expected) add_expected_rep(k, act, q_rep, term);
+            }
+        }
+    }
+    if (k.prof && lane == 0 && (entries | visited)) {
+        atomicAdd(&k.prof[PROF_DRAW_ENTRIES], (unsigned long long)entries);
+        atomicAdd(&k.prof[PROF_DRAW_LOCATIONS], (unsigned long long)visited);
+    }
+    grad_end(k, s_grad);
+}
+
+// whether any agent decides at step s1 of the day (or it is the curfew step)
+__device__ __forceinline__ bool decides_at(const KArgs& k, uint32_t s1) {
+    const bool curfew_now = k.p.enable_curfew && k.p.curfew_begin == s1;
+    return curfew_now || mask_has(k, s1);
+}
+
+// The agents that decide at step + 1, in the block's own segment of the work
+// list (shared-memory counter: no global contention).  Reads one word per
+// agent, and nothing at a step nobody decides at.
+__global__ void __launch_bounds__(256, 8) k_queue(KArgs k, uint32_t step, uint32_t cap) {
+    const uint32_t s1 = step + 1;
+    if (!decides_at(k, s1)) return;
+    if (k.prof && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&k.prof[PROF_QUEUE_STEPS], 1ull);
     __shared__ uint32_t s_cnt;
     if (threadIdx.x == 0) s_cnt = 0u;
     __syncthreads();
-    const uint32_t N = k.a.n, L = k.l.n;
-    const uint32_t dt = k.p.time_step;
-    const uint32_t minutes = (step + 1) * dt;
-    const bool curfew_now = k.p.enable_curfew && k.p.curfew_begin == minutes / dt;
-    const bool rebuild = csr_rebuild(k, k.clock->t0 + step);
+    const uint32_t N = k.a.n;
+    const bool curfew_now = k.p.enable_curfew && k.p.curfew_begin == s1;
+    const uint32_t t1 = k.clock->t0 + s1;
+    const uint32_t stride = gridDim.x * blockDim.x;
     uint32_t* seg = k.a.worklist + (size_t)blockIdx.x * cap;
-    uint32_t* segl = k.a.worklist_loc + (size_t)blockIdx.x * cap;
     const int lane = threadIdx.x & 31;
-    for (uint32_t base = blockIdx.x * (256u * U); base < N; base += gridDim.x * (256u * U)) {
-        uint32_t loc[U], sv[U], pos[U];
-        bool hz[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const uint32_t i = base + u * 256u + threadIdx.x;
-            loc[u] = NONE;
-            sv[u] = 0u;
-            if (i < N) {
-                loc[u] = k.a.location[i];
-                sv[u] = k.a.steps_until_move[i];
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            hz[u] = false;
-            if (loc[u] < L) hazard_at(k, loc[u], &hz[u]);
-            pos[u] = take_slot(k, loc[u] < L, loc[u], rebuild);
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const uint32_t i = base + u * 256u + threadIdx.x;
-            const bool act = i < N;
-            const bool ok = act && loc[u] < L;
-            if (ok) store_slot(k, pos[u], i);
-            const bool mover = act && (curfew_now || sv[u] == 0);
-            const bool cold = mover || (act && (hz[u] || !ok));
-            if (act && !mover) k.a.steps_until_move[i] = sv[u] - 1;
-            const unsigned cm = __ballot_sync(0xffffffffu, cold);
-            if (cm) {
-                uint32_t basew = 0;
-                if (lane == __ffs(cm) - 1) basew = atomicAdd(&s_cnt, (uint32_t)__popc(cm));
-                basew = __shfl_sync(0xffffffffu, basew, __ffs(cm) - 1);
-                if (cold) {
-                    const uint32_t q = basew + __popc(cm & lanemask_lt());
-                    seg[q] = i;
-                    segl[q] = (ok ? loc[u] : WORK_LOC_MASK) | (hz[u] ? WORK_HZ : 0u) | (mover ? WORK_MOVE : 0u);
-                }
-            }
+    for (uint32_t base = blockIdx.x * blockDim.x; base < N; base += stride) {
+        const uint32_t i = base + threadIdx.x;
+        const bool mover = i < N && (curfew_now || k.a.move_at[i] == t1);
+        const unsigned cm = __ballot_sync(0xffffffffu, mover);
+        if (cm) {
+            uint32_t basew = 0;
+            if (lane == __ffs(cm) - 1) basew = atomicAdd(&s_cnt, (uint32_t)__popc(cm));
+            basew = __shfl_sync(0xffffffffu, basew, __ffs(cm) - 1);
+            if (mover) seg[basew + __popc(cm & lanemask_lt())] = i;
         }
     }
     __syncthreads();
-    if (threadIdx.x == 0) k.a.seg_count[blockIdx.x] = s_cnt;
-}
-
-// The cold agents of one step, one per thread: queued agent i with the hot
-// kernel's word w (its location, whether it draws, whether it moves) draws
-// at its location, then moves; the histogram and the sums follow.
-__device__ __forceinline__ bool cold_agent(const KArgs& k, bool act, uint32_t i, uint32_t w, uint32_t t,
-                                           const StepClock& c, double* s_grad) {
-    double term = 0.0;
-    uint32_t loc = NONE, loc0 = NONE, var0 = 0, var = 0;
-    float inf0 = 0.0f, inf = 0.0f;
-    if (act) {
-        loc0 = (w & WORK_LOC_MASK) == WORK_LOC_MASK ? NONE : (w & WORK_LOC_MASK);
-        inf0 = inf = k.a.infectious[i];
-        if (inf0 > 0.0f) var0 = var = k.a.variant[i];
-        if (w & WORK_HZ) {
-            term = draw_agent(k, i, loc0, t, k.l.hazard[loc0], s_grad);
-            inf = k.a.infectious[i];
-            var = inf > 0.0f ? k.a.variant[i] : 0u;
-        }
-        if (w & WORK_MOVE) {
-            // the countdown is at zero (or the curfew step reloads it)
-            move_agent(k, i, c, 0u);
-            loc = k.a.location[i];
-        } else {
-            loc = loc0;
-        }
+    if (threadIdx.x == 0) {
+        k.a.seg_count[blockIdx.x] = s_cnt;
+        if (k.prof && s_cnt) atomicAdd(&k.prof[PROF_MOVERS], (unsigned long long)s_cnt);
     }
-    if (k.track_expected) add_expected(k, act, i, term);
-    return count_agent_delta(k, act, loc0, loc, inf0, var0, inf, var);
 }
 
-// The cold half, one segment per block: block b runs the agents that hot
-// block b queued (and segments b + gridDim.x, ...).
-// four blocks per SM: the movers' decision chains are latency bound, and
-// fewer resident warps (the registers the compiler would otherwise take)
-// measured slower than the few spills
-__global__ void __launch_bounds__(256, 4) k_step_cold(KArgs k, uint32_t step, uint32_t cap, uint32_t n_seg) {
-    __shared__ double s_grad[GRAD_N];
-    grad_begin(k, s_grad);
-    const uint32_t t = k.clock->t0 + step;
-    const StepClock c = step_clock(k, step + 1);
+// doMovement of the queued agents for step + 1, one segment per block in
+// turn; then the histogram and sum deltas of the agents that took a new
+// location.  Four blocks per SM: the decisions are chains of dependent
+// loads, and fewer resident warps (the registers the compiler would take
+// otherwise) measured slower than a few spills.
+__global__ void __launch_bounds__(256, 4) k_decide(KArgs k, uint32_t step, uint32_t cap, uint32_t n_seg) {
+    const uint32_t s1 = step + 1;
+    if (!decides_at(k, s1)) return;
+    __shared__ uint32_t s_mm[MOVE_MASK_WORDS];
+    mask_clear_shared(s_mm);
+    const StepClock c = step_clock(k, s1);
     bool moved = false;
     for (uint32_t sg = blockIdx.x; sg < n_seg; sg += gridDim.x) {
-        const uint32_t n = k.a.seg_count[sg];
+        uint32_t n = k.a.seg_count[sg];
+        if (n > cap) {
+            if (threadIdx.x == 0) atomicOr(k.err, ERR_AGENT_LIST);
+            n = 0;
+        }
         const uint32_t* seg = k.a.worklist + (size_t)sg * cap;
-        const uint32_t* segl = k.a.worklist_loc + (size_t)sg * cap;
         const uint32_t trips = (n + blockDim.x - 1) / blockDim.x;  // uniform per block
         for (uint32_t it = 0; it < trips; ++it) {
             const uint32_t j = it * blockDim.x + threadIdx.x;
-            const bool act = j < n;
-            moved |= cold_agent(k, act, act ? seg[j] : 0u, act ? segl[j] : 0u, t, c, s_grad);
-        }
-    }
-    publish_moved(k, moved, c.t);
-    grad_end(k, s_grad);
-}
-
-// The cold half with the queued agents of all segments spread evenly over the
-// grid: the movers of a step cluster in a few hot blocks (agents of one type
-// leave for the same event together), and one block per segment then makes
-// several trips through the movement decision's long chain of dependent
-// loads while the other SMs idle.  Every block scans the segment counts into
-// shared memory (dynamic, n_seg + 1 words); work index w lies in segment
-// sg with pre[sg] <= w < pre[sg + 1].
-template <int MINB>
-__global__ void __launch_bounds__(256, MINB) k_step_cold_spread(KArgs k, uint32_t step, uint32_t cap, uint32_t n_seg) {
-    extern __shared__ uint32_t s_pre[];  // [n_seg + 1]
-    __shared__ double s_grad[GRAD_N];
-    __shared__ uint32_t s_warp[8];
-    grad_begin(k, s_grad);
-    const uint32_t t = k.clock->t0 + step;
-    const StepClock c = step_clock(k, step + 1);
-    // exclusive prefix of seg_count: each thread sums a run of consecutive
-    // segments, then a block scan of the run totals
-    const uint32_t per = (n_seg + blockDim.x - 1) / blockDim.x;
-    const uint32_t b0 = threadIdx.x * per;
-    uint32_t run = 0;
-    for (uint32_t q = 0; q < per; ++q)
-        if (b0 + q < n_seg) run += k.a.seg_count[b0 + q];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t x = run;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-    }
-    if (lane == 31) s_warp[warp] = x;
-    __syncthreads();
-    uint32_t woff = 0;
-    for (int q = 0; q < warp; ++q) woff += s_warp[q];
-    uint32_t acc = woff + x - run;
-    for (uint32_t q = 0; q < per; ++q)
-        if (b0 + q < n_seg) {
-            s_pre[b0 + q] = acc;
-            acc += k.a.seg_count[b0 + q];
-        }
-    if (threadIdx.x == blockDim.x - 1) s_pre[n_seg] = woff + x;
-    __syncthreads();
-    const uint32_t total = s_pre[n_seg];
-    const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t trips = (total + stride - 1) / stride;  // uniform over the grid
-    bool moved = false;
-    for (uint32_t it = 0; it < trips; ++it) {
-        const uint32_t w = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
-        const bool act = w < total;
-        uint32_t i = 0u, lw = 0u;
-        if (act) {
-            // the last segment whose start is <= w
-            uint32_t lo = 0, hi = n_seg - 1;
-            while (lo < hi) {
-                const uint32_t mid = (lo + hi + 1) >> 1;
-                if (s_pre[mid] <= w)
-                    lo = mid;
-                else
-                    hi = mid - 1;
+            bool act = j < n;
+            uint32_t loc0 = NONE, loc = NONE, var = 0;
+            float inf = 0.0f;
+            const uint32_t i = act ? seg[j] : NONE;
+            if (act && i >= k.a.n) {
+                atomicOr(k.err, ERR_AGENT_LIST);
+                act = false;
             }
-            const size_t q = (size_t)lo * cap + (w - s_pre[lo]);
-            i = k.a.worklist[q];
-            lw = k.a.worklist_loc[q];
+            if (act) {
+                loc0 = k.a.location[i];
+                inf = k.a.infectious[i];
+                if (inf > 0.0f) var = k.a.variant[i];
+                move_agent(k, i, c, k.a.move_at[i] - c.t, s_mm);
+                loc = k.a.location[i];
+            }
+            moved |= count_agent_delta(k, act, loc0, loc, inf, var, inf, var);
         }
-        moved |= cold_agent(k, act, i, lw, t, c, s_grad);
     }
     publish_moved(k, moved, c.t);
-    grad_end(k, s_grad);
+    mask_flush(k, s_mm);
 }
 
 // Canonical CSR order (ascending agent id inside a location, the output of
@@ -2002,7 +2077,7 @@ __global__ void k_plan_schools(KArgs k, uint32_t t) {
 __global__ void __launch_bounds__(256) k_plan_agents(KArgs k, uint32_t t) {
     const psim_params& p = k.p;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < k.a.n; i += gridDim.x * blockDim.x) {
-        k.a.steps_until_move[i] = p.curfew_end;
+        k.a.move_at[i] = t + p.curfew_end;  // stepsUntilMove = curfewEnd before step t
         k.a.stayed_home[i] = 1;
         k.a.no_work[i] = 0;
         if (p.quarantine_policy > 2) {
@@ -2232,84 +2307,47 @@ void launch_movement(const KArgs& k, uint32_t step, cudaStream_t s) {
     if (!g) g = wave_grid(k_movement, 1u << 30);
     k_movement<<<agent_grid(k, g), 256, 0, s>>>(k, step);
 }
-// register-capped instantiations of the fused step kernel: a tighter cap
-// raises occupancy for the hot path and spills on the rare cold path; the
-// autotuner picks one (DevTune::variant)
-// part: -1 every kernel of the step; 0 the first (the fused kernel; for the
-// hot/cold variants 3, 7-9 the hot kernel, then the agent list's slots);
-// 1 the cold kernel of a hot/cold variant (else nothing); 2 the hot kernel
-// of variants 3, 7-9 alone; 3 their slots alone (2 and 3 let the day graph
-// run the hot kernel beside the scan and the slots beside the cold kernel)
-void launch_step_fused(const KArgs& k, uint32_t step, cudaStream_t s, int part) {
-    static unsigned g[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-    const uint32_t v = k.tune.variant < 10 ? k.tune.variant : 0;
-    if (!g[0]) {
-        g[0] = wave_grid(k_step_fused<4>, 1u << 30);
-        g[1] = wave_grid(k_step_fused<6>, 1u << 30);
-        g[2] = wave_grid(k_step_fused<8>, 1u << 30);
-        g[3] = wave_grid(k_step_hot, 1u << 30);
-        g[4] = wave_grid(k_step_cold, 1u << 30);
-        g[5] = wave_grid(k_step_ilp<2>, 1u << 30);
-        g[6] = wave_grid(k_step_ilp<4>, 1u << 30);
-        g[7] = wave_grid(k_step_hot_ilp<2>, 1u << 30);
-        g[8] = wave_grid(k_step_cold_spread<4>, 1u << 30);
-        g[9] = wave_grid(k_step_cold_spread<6>, 1u << 30);
-        g[10] = wave_grid(k_step_cold_spread<8>, 1u << 30);
+// The day graph's step kernels (see k_draw): the work-list segments are one
+// per queue block, each as large as the agents the block visits.
+struct StepGrid {
+    unsigned queue, decide, draw, slots;
+    uint32_t cap;
+};
+static StepGrid step_grid(const KArgs& k) {
+    static unsigned wq = 0, wd = 0, wr = 0, ws = 0;
+    if (!wq) {
+        wq = wave_grid(k_queue, 1u << 30);
+        wd = wave_grid(k_decide, 1u << 30);
+        wr = wave_grid(k_draw, 1u << 30);
+        ws = wave_grid(k_rebuild_slots, 1u << 30);
     }
-    if (v == 6) {
-        // hot/cold with two agents per hot thread in flight
-        const uint32_t tile = 512;
-        unsigned grid = k.tune.blocks_per_sm ? (unsigned)(sm_count() * k.tune.blocks_per_sm) : g[7];
-        // grid * cap < N + grid * 512 <= N + WORK_MAX_BLOCKS * 256 (the work list's size)
-        grid = std::min(std::min(grid, grid_for((k.a.n + 1) / 2, 1 << 20)), (unsigned)WORK_MAX_BLOCKS / 2);
-        const uint32_t cap = (uint32_t)((((size_t)k.a.n + (size_t)grid * tile - 1) / ((size_t)grid * tile)) * tile);
-        if (part != 1) k_step_hot_ilp<2><<<grid, 256, 0, s>>>(k, step, cap);
-        if (part != 0) k_step_cold<<<std::min(grid, g[4]), 256, 0, s>>>(k, step, cap, grid);
-        return;
-    }
-    if (v == 3 || v >= 7) {
-        // one work-list segment per hot block, as many as the block visits
-        const unsigned grid = std::min(agent_grid(k, g[3]), (unsigned)WORK_MAX_BLOCKS);
-        const uint32_t cap = (uint32_t)((((size_t)k.a.n + (size_t)grid * 256 - 1) / ((size_t)grid * 256)) * 256);
-        if (part == -1 || part == 0 || part == 2) k_step_hot<<<grid, 256, 0, s>>>(k, step, cap);
-        if (part == -1 || part == 0 || part == 3) k_slots<<<grid, 256, 0, s>>>(k, step);
-        // the cold agents are a few percent: at most one wave of cold blocks,
-        // each taking segments in turn
-        if (part == -1 || part == 1) {
-            const size_t sh = (grid + 1) * sizeof(uint32_t);
-            if (v == 7)
-                k_step_cold_spread<4><<<g[8], 256, sh, s>>>(k, step, cap, grid);
-            else if (v == 8)
-                k_step_cold_spread<6><<<g[9], 256, sh, s>>>(k, step, cap, grid);
-            else if (v == 9)
-                k_step_cold_spread<8><<<g[10], 256, sh, s>>>(k, step, cap, grid);
-            else
-                k_step_cold<<<std::min(grid, g[4]), 256, 0, s>>>(k, step, cap, grid);
-        }
-        return;
-    }
-    if (part == 1) return;
-    if (v == 4 || v == 5) {
-        const int U = v == 4 ? 2 : 4;
-        unsigned grid = k.tune.blocks_per_sm ? (unsigned)(sm_count() * k.tune.blocks_per_sm) : g[v == 4 ? 5 : 6];
-        grid = std::min(grid, grid_for((k.a.n + U - 1) / U, 1 << 20));
-        if (v == 4)
-            k_step_ilp<2><<<grid, 256, 0, s>>>(k, step);
-        else
-            k_step_ilp<4><<<grid, 256, 0, s>>>(k, step);
-        return;
-    }
-    const unsigned grid = agent_grid(k, g[v]);
-    if (v == 0)
-        k_step_fused<4><<<grid, 256, 0, s>>>(k, step);
-    else if (v == 1)
-        k_step_fused<6><<<grid, 256, 0, s>>>(k, step);
-    else
-        k_step_fused<8><<<grid, 256, 0, s>>>(k, step);
+    StepGrid g;
+    g.queue = std::min(agent_grid(k, wq), (unsigned)WORK_MAX_BLOCKS);
+    g.cap = (uint32_t)((((size_t)k.a.n + (size_t)g.queue * 256 - 1) / ((size_t)g.queue * 256)) * 256);
+    // the decisions are a few percent of the agents: at most one wave of
+    // blocks, each taking segments in turn
+    g.decide = std::min(g.queue, wd);
+    // one warp per chunk of DRAW_WPW mask words, at most one wave
+    const size_t chunks = (((size_t)k.l.n + 31) / 32 + DRAW_WPW - 1) / DRAW_WPW;
+    g.draw = (unsigned)std::max<size_t>(1, std::min<size_t>((chunks + 7) / 8, wr));
+    g.slots = agent_grid(k, ws);
+    return g;
 }
-int step_fused_kernels(const KArgs& k) {
-    const uint32_t v = k.tune.variant;
-    return v == 3 || (v >= 7 && v <= 9) ? 3 : v == 6 ? 2 : 1;
+void launch_rebuild_slots(const KArgs& k, uint32_t step, cudaStream_t s) {
+    const StepGrid g = step_grid(k);
+    k_rebuild_slots<<<g.slots, 256, 0, s>>>(k, step);
+}
+void launch_draw(const KArgs& k, uint32_t step, cudaStream_t s) {
+    const StepGrid g = step_grid(k);
+    k_draw<<<g.draw, 256, 0, s>>>(k, step);
+}
+void launch_queue(const KArgs& k, uint32_t step, cudaStream_t s) {
+    const StepGrid g = step_grid(k);
+    k_queue<<<g.queue, 256, 0, s>>>(k, step, g.cap);
+}
+void launch_decide(const KArgs& k, uint32_t step, cudaStream_t s) {
+    const StepGrid g = step_grid(k);
+    k_decide<<<g.decide, 256, 0, s>>>(k, step, g.cap, g.queue);
 }
 void launch_count(const KArgs& k, cudaStream_t s) { k_count<<<grid_for(k.a.n, 8), 256, 0, s>>>(k); }
 // the scan of the histogram with 256 x tune.scan_items locations per tile:
@@ -2421,6 +2459,12 @@ void launch_expose(const KArgs& k, uint32_t t, uint32_t variant, double fraction
 void launch_bounded_wait_probe(const KArgs& k, uint32_t iters, cudaStream_t s) {
     k_bounded_wait_probe<<<1, 32, 0, s>>>(k, iters);
 }
-uint64_t launches_per_step(int) { return 2; }
+// countdowns <-> absolute decision timestamps (upload, download)
+__global__ void k_time_shift(uint32_t* a, uint32_t n, uint32_t delta) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) a[i] += delta;
+}
+void launch_time_shift(uint32_t* a, uint32_t n, uint32_t delta, cudaStream_t s) {
+    if (n && delta) k_time_shift<<<grid_for(n, 8), 256, 0, s>>>(a, n, delta);
+}
 
 }  // namespace psim

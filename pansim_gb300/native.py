@@ -69,6 +69,7 @@ def lib(auto_build=True):
         L.psim_other_disease_day.argtypes = [P, U32]
         L.psim_get_events.argtypes = [P, P, P, P, P, P, P, U32, P]
         L.psim_day_kernel_ms.argtypes = [P, C.c_void_p]
+        L.psim_day_counts.argtypes = [P, C.c_void_p]
         L.psim_launch_count.argtypes = [P, C.POINTER(C.c_uint64)]
         L.psim_stream_handle.argtypes = [P, C.POINTER(P)]
         L.psim_bounded_wait_selftest.argtypes = [P, U32]
@@ -298,11 +299,20 @@ class GpuSim:
         self._ck(lib().psim_set_profiling(self.h, 1 if on else 0), "set_profiling")
 
     def day_kernel_ms(self):
-        """Summed kernel durations of the last profiled day: movement(0), scans,
-        fused (or hot) step kernels, last scatter/draw, cold step kernels."""
+        """Summed kernel durations of the last profiled day: movement(0), the
+        rebuilds (scan + slots), the draws, the queues, the decisions."""
         ms = np.zeros(5, np.float32)
         self._ck(lib().psim_day_kernel_ms(self.h, _p(ms)), "day_kernel_ms")
         return ms
+
+    def day_counts(self):
+        """Of the last profiled day: agent-list entries the draws expanded,
+        locations with a set hazard-mask bit they visited, agents queued for a
+        decision, steps whose queue passed over the agents, steps that rebuilt
+        the agent list."""
+        out = np.zeros(5, np.uint64)
+        self._ck(lib().psim_day_counts(self.h, _p(out)), "day_counts")
+        return out
 
     def launch_count(self):
         n = C.c_uint64(0)

@@ -26,18 +26,17 @@ def main(argv=None):
     ap.add_argument("--quarantine-policy", type=int, default=0)
     ap.add_argument("--testing", action="store_true")
     ap.add_argument("--quiet", action="store_true")
-    ap.add_argument("--variant", type=int, default=None, help="fused step kernel variant (0-3)")
-    ap.add_argument("--agg-count", type=int, default=1)
-    ap.add_argument("--agg-slot", type=int, default=1)
-    ap.add_argument("--blocks-per-sm", type=int, default=0)
+    ap.add_argument("--tune", action="store_true", help="set the tuning below (else the context's default)")
+    ap.add_argument("--agg-slot", type=int, default=0)
+    ap.add_argument("--blocks-per-sm", type=int, default=4)
     ap.add_argument("--scan-items", type=int, default=4)
     ap.add_argument("--scan-mode", type=int, default=3)
     a = ap.parse_args(argv)
     snap = synth.make_snapshot(a.agents, a.locs, seed=a.seed, pop_seed=a.pop_seed,
                                quarantine_policy=a.quarantine_policy, testing=a.testing)
     g = native.GpuSim(snap)
-    if a.variant is not None:
-        g.set_tuning(agg_count=a.agg_count, agg_slot=a.agg_slot, blocks_per_sm=a.blocks_per_sm, variant=a.variant,
+    if a.tune:
+        g.set_tuning(agg_count=0, agg_slot=a.agg_slot, blocks_per_sm=a.blocks_per_sm, variant=3,
                      scan_items=a.scan_items, scan_mode=a.scan_mode)
     t0 = time.perf_counter()
     for d in range(a.days):

@@ -148,39 +148,20 @@ def test_bounded_wait_reports_error_and_context_survives(gpu_lib):
     g.run_day(0)  # still usable
 
 
-@pytest.mark.parametrize("tuning", [dict(agg_count=0, agg_slot=0, blocks_per_sm=0, variant=2),
-                                    dict(agg_count=1, agg_slot=0, blocks_per_sm=3, variant=1),
-                                    dict(agg_count=0, agg_slot=1, blocks_per_sm=16, variant=0),
-                                    dict(agg_count=1, agg_slot=1, blocks_per_sm=0, variant=3),
-                                    dict(agg_count=0, agg_slot=0, blocks_per_sm=5, variant=3),
-                                    dict(agg_count=1, agg_slot=0, blocks_per_sm=0, variant=4, scan_items=2),
-                                    dict(agg_count=0, agg_slot=1, blocks_per_sm=3, variant=5, scan_items=4),
-                                    dict(agg_count=0, agg_slot=0, blocks_per_sm=4, variant=3, scan_items=2,
-                                         scan_mode=1),
-                                    dict(agg_count=0, agg_slot=0, blocks_per_sm=0, variant=0, scan_items=8,
-                                         scan_mode=1),
-                                    dict(agg_count=0, agg_slot=0, blocks_per_sm=4, variant=3, scan_items=4,
-                                         scan_mode=2),
-                                    dict(agg_count=0, agg_slot=1, blocks_per_sm=0, variant=0, scan_items=8,
-                                         scan_mode=2),
-                                    dict(agg_count=0, agg_slot=0, blocks_per_sm=4, variant=3, scan_items=8,
-                                         scan_mode=0),
-                                    dict(agg_count=0, agg_slot=0, blocks_per_sm=8, variant=6, scan_items=4,
-                                         scan_mode=2),
-                                    dict(agg_count=0, agg_slot=1, blocks_per_sm=0, variant=6, scan_items=2,
-                                         scan_mode=1),
-                                    dict(agg_count=0, agg_slot=0, blocks_per_sm=4, variant=7, scan_items=4,
-                                         scan_mode=2),
-                                    dict(agg_count=0, agg_slot=1, blocks_per_sm=8, variant=8, scan_items=8,
-                                         scan_mode=2),
-                                    dict(agg_count=0, agg_slot=0, blocks_per_sm=0, variant=9, scan_items=4,
-                                         scan_mode=1),
-                                    dict(agg_count=0, agg_slot=0, blocks_per_sm=4, variant=3, scan_items=4,
-                                         scan_mode=3),
-                                    dict(agg_count=0, agg_slot=1, blocks_per_sm=0, variant=0, scan_items=8,
-                                         scan_mode=3),
-                                    dict(agg_count=0, agg_slot=0, blocks_per_sm=8, variant=6, scan_items=2,
-                                         scan_mode=3)])
+@pytest.mark.parametrize("tuning", [dict(agg_count=0, agg_slot=0, blocks_per_sm=0),
+                                    dict(agg_count=1, agg_slot=1, blocks_per_sm=3),
+                                    dict(agg_count=0, agg_slot=1, blocks_per_sm=16),
+                                    dict(agg_count=0, agg_slot=0, blocks_per_sm=5),
+                                    dict(agg_count=0, agg_slot=0, blocks_per_sm=0, scan_items=2, scan_mode=1),
+                                    dict(agg_count=0, agg_slot=1, blocks_per_sm=3, scan_items=4, scan_mode=0),
+                                    dict(agg_count=0, agg_slot=0, blocks_per_sm=4, scan_items=2, scan_mode=1),
+                                    dict(agg_count=0, agg_slot=0, blocks_per_sm=0, scan_items=8, scan_mode=1),
+                                    dict(agg_count=0, agg_slot=0, blocks_per_sm=4, scan_items=4, scan_mode=2),
+                                    dict(agg_count=0, agg_slot=1, blocks_per_sm=0, scan_items=8, scan_mode=2),
+                                    dict(agg_count=0, agg_slot=0, blocks_per_sm=4, scan_items=8, scan_mode=0),
+                                    dict(agg_count=0, agg_slot=0, blocks_per_sm=8, scan_items=4, scan_mode=3),
+                                    dict(agg_count=0, agg_slot=1, blocks_per_sm=0, scan_items=8, scan_mode=3),
+                                    dict(agg_count=0, agg_slot=0, blocks_per_sm=8, scan_items=2, scan_mode=3)])
 def test_tuning_choices_do_not_change_results(gpu_lib, tuning):
     """Every tuning against the oracle over three days: statistics, state and
     the agent list at the end of each day.  Most steps of a day move nobody
@@ -203,8 +184,10 @@ def test_profiled_graph_same_results_and_kernel_times(gpu_lib):
     for d in range(2):
         assert stats_rows(o.run_day(d)) == stats_rows(g.run_day(d)), d
         ms = g.day_kernel_ms()
-        assert (ms > 0).all(), ms  # the default tuning is the hot/cold form
+        assert (ms > 0).all(), ms
         assert ms.sum() <= g.last_day_ms() * 1.001
+        entries, visited, movers, queues, rebuilds = g.day_counts()
+        assert entries > 0 and visited > 0 and movers > 0 and 0 < queues < 143 and 0 < rebuilds <= 144
     g.set_profiling(False)
     assert stats_rows(o.run_day(2)) == stats_rows(g.run_day(2))
     g.download()
@@ -260,14 +243,14 @@ def test_restored_day_rebuilds_the_agent_list(gpu_lib):
 
 
 def test_timestep_timing_leaves_a_consistent_agent_list(gpu_lib):
-    """psim_time_step_kernels (two timesteps, the step kernels timed) runs the
-    hot, slot and cold kernels in sequence; afterwards the agent list is the
-    stable grouping of the agents' current locations, for every hot/cold
-    variant."""
-    for variant in (3, 7):
+    """psim_time_step_kernels (one timestep and the decisions of the next, the
+    step kernels timed) runs the rebuild, draw, queue and decision kernels in
+    sequence; afterwards the agent list is the stable grouping of the agents'
+    current locations."""
+    for agg in (0, 1):
         s_gpu = small_snapshot(n=12000, locs=3000, initial_infected_frac=0.02)
         g = GpuSim(s_gpu)
-        g.set_tuning(agg_count=0, agg_slot=0, blocks_per_sm=4, variant=variant, scan_items=4, scan_mode=3)
+        g.set_tuning(agg_count=0, agg_slot=agg, blocks_per_sm=4, variant=3, scan_items=4, scan_mode=3)
         g.run_day(0)
         spd = s_gpu.steps_per_day
         for step in (40, 47, 48):
