@@ -39,44 +39,32 @@ STEP_BYTES = (32, 20)
 
 
 def kernel_bytes(N, L, V, spd, counts):
-    """Algorithmic bytes per simulated day of each step kernel, from the
-    profiled day's counters (entries E, visited locations H, queued agents M,
-    queue passes Q, rebuilds R):
+    """Algorithmic bytes per simulated day of each phase of the step kernel,
+    from the profiled day's counters (entries E, visited locations H, queued
+    agents M, queue passes Q, rebuilds R):
+      rebuild   per rebuild the histogram read twice and the first slots
+                written (12 L), and per agent its location, age band and
+                susceptibilities read, its slot's atomic, id and
+                susceptibility products written (17 + 8 V)
       draw      per step the two mask words per 32 locations (L/4); at the
                 day's first step every location's sums, count, weight and
                 replica read and its hazard written (22 L); per visited
                 location count, cursor, hazard, replica (14); per entry the
                 agent id and the susceptibility products (4 + 4 V)
-      queue     per pass the decision timestamps (4 N); per queued agent its
-                work-list entry (4)
-      decide    per decision 72: the agent's location, decision timestamp,
-                state, type, age, flags and timestamps (38), its location-list
-                entries (12), the new location's flags (5), the location and
-                timestamp written (8), the histogram deltas (8), its work-list
-                entry (4)
-      rebuild   per rebuild the scan's counts read and first slots written
-                (8 L) and per agent its location, age band and
-                susceptibilities read, its slot's atomic, id and
-                susceptibility products written (17 + 8 V)
+      decide    per queue pass the decision timestamps (4 N); per decision
+                76: its work-list entry written and read (8), the agent's
+                location, decision timestamp, state, type, age, flags and
+                timestamps (38), its location-list entries (12), the new
+                location's flags (5), the location and timestamp written (8),
+                the histogram deltas (8)
     """
     E, H, M, Q, R = (float(x) for x in counts)
-    return {"draw": spd * L / 4.0 + 22.0 * L + 14.0 * H + (4 + 4 * V) * E,
-            "queue": 4.0 * N * Q + 4.0 * M,
-            "decide": 72.0 * M,
-            "rebuild": R * (8.0 * L + (17 + 8 * V) * N)}
+    return {"rebuild": R * (12.0 * L + (17 + 8 * V) * N),
+            "draw": spd * L / 4.0 + 22.0 * L + 14.0 * H + (4 + 4 * V) * E,
+            "decide": 4.0 * N * Q + 76.0 * M}
 
 
-KERNEL_LABELS = {"rebuild": "scan + k_rebuild_slots", "draw": "k_draw", "queue": "k_queue", "decide": "k_decide"}
-
-
-def scan_label(tuning):
-    """The scan kernels of a tuning (scan_mode 0/3 one pass with look-back,
-    1/2 tile sums then scan; 2/3 over consecutive locations unless scan_items 2)."""
-    mode, items = tuning.get("scan_mode", 3), tuning.get("scan_items", 4)
-    vec = mode in (2, 3) and items in (4, 8)
-    if mode in (0, 3):
-        return "k_scan_v" if vec else "k_scan"
-    return "k_tile_sums_v + k_scan_v" if vec else "k_tile_sums + k_scan"
+KERNEL_LABELS = {"rebuild": "k_step rebuild phase", "draw": "k_step draw phase", "decide": "k_step queue + decide phase"}
 
 
 def dist_env():
@@ -588,10 +576,9 @@ def main():
         counts = cnt_sum / n_prof
         kb = kernel_bytes(N, L, V, spd, counts)
         kms_day = kms_sum / n_prof  # per simulated day: movement(0), rebuild, draw, queue, decide
-        launches_per_day = {"rebuild": max(counts[4], 1.0), "draw": float(spd), "queue": max(counts[3], 1.0),
-                            "decide": max(counts[3], 1.0)}
+        launches_per_day = {"rebuild": max(counts[4], 1.0), "draw": float(spd), "decide": max(counts[3], 1.0)}
         kern = {"movement": {"ms_per_day": float(kms_day[0])}}
-        for j, name in enumerate(["rebuild", "draw", "queue", "decide"]):
+        for j, name in enumerate(["rebuild", "draw", "decide"]):
             ms = float(kms_day[1 + j])
             kern[name] = {"ms_per_day": ms, "alg_bytes_per_day": kb[name],
                           "launches_with_work_per_day": launches_per_day[name],
@@ -620,12 +607,11 @@ def main():
             "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
             "config": workload_config(snap, ws),
-            "roofline": {"bound": "hbm",
-                         "kernel": (scan_label(best) + " + k_rebuild_slots") if dom == "rebuild" else KERNEL_LABELS[dom],
+            "roofline": {"bound": "hbm", "kernel": KERNEL_LABELS[dom],
                          "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak, "traffic": traffic,
                          "peak_kind": peak_kind, "alg_bytes_per_launch": dom_bytes, "launch_ms": dom_ms,
-                         "launch_ms_source": "event-record nodes in the profiled day graph, over the launches "
-                                             "that did work",
+                         "launch_ms_source": "the phase launched alone in the profiled day graph, event-record "
+                                             "nodes, over the steps at which it did work",
                          "dominant": dom, "per_kernel": kern, "day_counts": counts_d,
                          "step_rate": {"reference_bytes_per_timestep": step_bytes, "timestep_ms": step_ms,
                                        "gbs": step_bytes / (step_ms * 1e-3) / 1e9,

@@ -449,20 +449,22 @@ int psim_get_csr(psim_ctx* ctx, int canonical, uint32_t* offsets /*[L+1]*/, uint
 int psim_get_hazard(psim_ctx* ctx, float* out /*[L]*/, int64_t* fixed_sum /*[L] or NULL*/);
 
 /* Step t as the day graph runs it, after movement(t) with the sums afresh and
- * the agent list rebuilt, with CUDA events around the rebuild (scan + slots),
- * the draws of t and the queue + decisions of t + 1; ms[3] receives those
- * three durations.  t and t + 1 must lie in the same day. */
+ * a rebuild of the agent list pending, with CUDA events around the step
+ * kernel's three phases launched apart: the rebuild, the draws of t and the
+ * queue + decisions of t + 1; ms[3] receives those three durations.  t and
+ * t + 1 must lie in the same day. */
 int psim_time_step_kernels(psim_ctx* ctx, uint32_t t, float* ms /* [3] */);
 /* Timing of the last psim_run_steps graph launch, milliseconds. */
 int psim_last_day_ms(psim_ctx* ctx, float* ms);
-/* With on != 0 the day graph is captured on one branch with event-record
- * nodes around each of its kernel groups; psim_day_kernel_ms then gives, for
- * the last psim_run_steps, the summed durations ms[5] = {movement of step 0,
- * the rebuilds of all steps (scan + slots), the draws, the queues, the
- * decisions}, and psim_day_counts out[5] = {agent-list entries the draws
- * expanded, locations with a set hazard-mask bit they visited, agents queued
- * for a decision, steps whose queue passed over the agents, steps that
- * rebuilt the agent list}, summed over the day's steps. */
+/* With on != 0 the day graph is captured with the step kernel's three phases
+ * as separate launches and an event-record node after each; psim_day_kernel_ms
+ * then gives, for the last psim_run_steps, the summed durations ms[5] =
+ * {movement of step 0, the rebuilds (histogram prefix + agent-list slots) of
+ * all steps, the draws, the queues + decisions, 0}, and psim_day_counts
+ * out[5] = {agent-list entries the draws expanded, locations with a set
+ * hazard-mask bit they visited, agents queued for a decision, steps at which
+ * agents were queued, steps that rebuilt the agent list}, summed over the
+ * day's steps. */
 int psim_set_profiling(psim_ctx* ctx, int on);
 int psim_day_kernel_ms(psim_ctx* ctx, float* ms /* [5] */);
 int psim_day_counts(psim_ctx* ctx, uint64_t* out /* [5] */);

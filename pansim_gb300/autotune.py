@@ -1,27 +1,26 @@
-"""Autotuner of the per-step kernels.
+"""Autotuner of the step kernel.
 
 Times each candidate tuning (warp aggregation of the agent-list slot
-atomics, blocks per SM of the per-agent kernels, scan tile size and
-single-pass or two-pass scan) on the live workload: every candidate runs the
-same whole day (the day graph, all its steps) from the same checkpoint taken
-after that day's midnight phases, timed with CUDA events, and the fastest is
-kept.  Steps at different times of day differ several-fold in cost (movers,
-infectious locations), so candidates are never compared on different steps.
-The choice depends on the device and on the population (location sizes,
-household structure), so it is made per context.
+atomics, resident blocks per SM of the persistent step kernel) on the live
+workload: every candidate runs the same whole day (the day graph, all its
+steps) from the same checkpoint taken after that day's midnight phases,
+timed with CUDA events, and the fastest is kept.  Steps at different times
+of day differ several-fold in cost (movers, infectious locations), so
+candidates are never compared on different steps.  The choice depends on the
+device and on the population, so it is made per context.
 """
 import itertools
 
-DEFAULT_GRID = [0, 4, 8, 16]
+DEFAULT_GRID = [0, 2, 3]
 LARGE_AGENTS = 8_000_000
 
 
 def candidates(grid=None):
-    """blocks_per_sm 0 = one occupancy wave of each per-agent kernel;
-    scan_mode 2 / 3 = two passes / one pass with look-back over consecutive
-    locations per thread."""
-    for agg_slot, bps, items, mode in itertools.product([1, 0], grid or DEFAULT_GRID, [8, 4, 2], [2, 3]):
-        yield dict(agg_count=0, agg_slot=agg_slot, blocks_per_sm=bps, variant=3, scan_items=items, scan_mode=mode)
+    """blocks_per_sm 0 = as many as the step kernel's occupancy allows (the
+    library caps every value there: its grid barriers need every block
+    resident)."""
+    for agg_slot, bps in itertools.product([1, 0], grid or DEFAULT_GRID):
+        yield dict(agg_count=0, agg_slot=agg_slot, blocks_per_sm=bps, variant=3, scan_items=4, scan_mode=3)
 
 
 TUNE_SLOT = 1 << 16
@@ -34,7 +33,7 @@ def autotune(sim, day, reps=2, grid=None, verbose=False):
     leaves no trace.  Populations above LARGE_AGENTS get a reduced candidate
     set and one repetition (a day there takes a good fraction of a second)."""
     if sim.snap.n_agents > LARGE_AGENTS:
-        grid = grid or [0, 16]
+        grid = grid or [0, 2]
         reps = 1
     spd = sim.snap.steps_per_day
     sim.checkpoint_save(TUNE_SLOT)

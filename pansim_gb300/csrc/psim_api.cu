@@ -27,6 +27,7 @@ int check_device_err(psim_ctx* c) {
         if (e & ERR_TEST_WAIT) m += " bounded wait expired;";
         if (e & ERR_SCAN_WAIT) m += " scan tile wait expired;";
         if (e & ERR_AGENT_LIST) m += " agent list inconsistent;";
+        if (e & ERR_BARRIER) m += " step kernel grid barrier expired;";
         return fail(c, PSIM_ERR_DEVICE, m);
     }
     return 0;
@@ -307,10 +308,9 @@ int capture_day_graph(psim_ctx* c) {
         c->day_graph = nullptr;
     }
     cudaGraph_t g = nullptr;
-    // 4 * spd + 2 events: [0] before movement(0), [1] after it, then per step
-    // one after the rebuild (scan + slots), the draws, the queue and the
-    // decisions
-    const size_t n_ev = c->profile ? 4ull * c->spd + 2 : 0;
+    // 3 * spd + 2 events: [0] before movement(0), [1] after it, then per step
+    // one after the rebuild, the draws and the queue + decisions
+    const size_t n_ev = c->profile ? 3ull * c->spd + 2 : 0;
     while (c->prof_ev.size() < n_ev) {
         cudaEvent_t ev = nullptr;
         CK(cudaEventCreate(&ev));
@@ -322,7 +322,6 @@ int capture_day_graph(psim_ctx* c) {
         if (c->profile) cudaEventRecordWithFlags(c->prof_ev[ev_i++], c->stream, cudaEventRecordExternal);
     };
     CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    const int merge_q = c->params.quarantine_policy > 1 ? 1 : 0;
     mark();
     // (the capture stays open until EndCapture: errors are checked after it)
     // The day's first step: the sums afresh (every location dirty), the
@@ -336,38 +335,20 @@ int capture_day_graph(psim_ctx* c) {
     if (me == cudaSuccess && c->profile) me = cudaMemsetAsync(c->d_prof, 0, sizeof(unsigned long long) * PROF_N, c->stream);
     launch_movement(c->k, 0, c->stream);
     mark();
-    // Per step s: the rebuild (scan, slots) and the draws on the first
-    // branch; the queue of the agents deciding at s + 1 on the second (it
-    // reads only their decision timestamps, which nothing on the first branch
-    // writes); the decisions after both (they read the draws' outcomes).
-    // The profiled graph runs them in that order on one branch with an event
-    // between each.
+    // Per step: one launch of the step kernel (rebuild, draws, decisions for
+    // the next step, with grid barriers inside).  The profiled graph
+    // launches the three phases separately with an event after each.
+    if (me == cudaSuccess) me = cudaMemsetAsync(c->k.l.bar, 0, sizeof(uint32_t) * BAR_WORDS, c->stream);
     for (uint32_t s = 0; s < c->spd; ++s) {
-        const bool next = s + 1 < c->spd;
         if (!c->profile) {
-            if (next) {
-                if (me == cudaSuccess) me = cudaEventRecord(c->fork_ev, c->stream);
-                if (me == cudaSuccess) me = cudaStreamWaitEvent(c->stream2, c->fork_ev, 0);
-                launch_queue(c->k, s, c->stream2);
-                if (me == cudaSuccess) me = cudaEventRecord(c->join_ev, c->stream2);
-            }
-            launch_scan(c->k, s, 0, merge_q, c->stream);
-            launch_rebuild_slots(c->k, s, c->stream);
-            launch_draw(c->k, s, c->stream);
-            if (next) {
-                if (me == cudaSuccess) me = cudaStreamWaitEvent(c->stream, c->join_ev, 0);
-                launch_decide(c->k, s, c->stream);
-            }
+            launch_step(c->k, s, PH_ALL, c->stream);
             continue;
         }
-        launch_scan(c->k, s, 0, merge_q, c->stream);
-        launch_rebuild_slots(c->k, s, c->stream);
+        launch_step(c->k, s, PH_REBUILD, c->stream);
         mark();
-        launch_draw(c->k, s, c->stream);
+        launch_step(c->k, s, PH_DRAW, c->stream);
         mark();
-        if (next) launch_queue(c->k, s, c->stream);
-        mark();
-        if (next) launch_decide(c->k, s, c->stream);
+        launch_step(c->k, s, PH_DECIDE, c->stream);
         mark();
     }
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
@@ -379,9 +360,8 @@ int capture_day_graph(psim_ctx* c) {
     e = cudaGraphInstantiate(&c->day_graph, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(c, PSIM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
-    // movement(0); per step the scan kernels, the slots and the draws; the
-    // queue and the decisions of all steps but the last
-    c->graph_kernels = 1 + (uint64_t)(scan_kernels(c->k) + 2) * c->spd + 2ull * (c->spd - 1);
+    // movement(0) and one step kernel per step (three when profiled)
+    c->graph_kernels = 1 + (c->profile ? 3ull : 1ull) * c->spd;
     c->graph_dirty = false;
     c->prof_valid = false;
     return 0;
@@ -630,7 +610,8 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     if ((rc = dalloc(c, &dl.no_work_loc, L))) return bail(rc);
     if ((rc = dalloc(c, &dl.flags, L))) return bail(rc);
     const size_t tiles = (L + 511) / 512 + 1;
-    if ((rc = dalloc(c, &dl.tile_sums, tiles))) return bail(rc);
+    if ((rc = dalloc(c, &dl.tile_sums, tiles + WORK_MAX_BLOCKS))) return bail(rc);
+    if ((rc = dalloc(c, &dl.bar, BAR_WORDS))) return bail(rc);
     if ((rc = dalloc(c, &dl.scan_status, tiles))) return bail(rc);
     if ((rc = dalloc(c, &dl.scan_state, 2))) return bail(rc);
     if ((rc = dalloc(c, &dl.build, 8))) return bail(rc);
@@ -1258,8 +1239,8 @@ int psim_day_kernel_ms(psim_ctx* c, float* ms) {
     ms[0] = t;
     ms[1] = ms[2] = ms[3] = ms[4] = 0.f;
     for (uint32_t s = 0; s < c->spd; ++s) {
-        const size_t e = 1 + 4 * (size_t)s;
-        for (int j = 0; j < 4; ++j) {
+        const size_t e = 1 + 3 * (size_t)s;
+        for (int j = 0; j < 3; ++j) {
             CK(cudaEventElapsedTime(&t, c->prof_ev[e + j], c->prof_ev[e + j + 1]));
             ms[1 + j] += t;
         }
@@ -1301,28 +1282,24 @@ int psim_time_step_kernels(psim_ctx* c, uint32_t t, float* ms) {
     cudaEvent_t ev[4];
     for (int j = 0; j < 4; ++j) CK(cudaEventCreate(&ev[j]));
     const uint32_t step = t % c->spd;
-    const int merge_q = c->params.quarantine_policy > 1 ? 1 : 0;
     // step t as the day graph runs it, from movement(t) with the sums afresh
-    // and the agent list rebuilt: the rebuild (scan + slots), the draws, and
-    // the queue + decisions of t + 1; then the rebuild and draws of t + 1
-    // untimed
+    // and the agent list rebuilt: the rebuild, the draws, the queue +
+    // decisions of t + 1 (the step kernel's phases as separate launches);
+    // then step t + 1 untimed
     if ((rc = reset_sums(c))) return rc;
     CK(cudaMemsetAsync(c->k.a.move_mask, 0, sizeof(uint32_t) * MOVE_MASK_WORDS, c->stream));
+    CK(cudaMemsetAsync(c->k.l.bar, 0, sizeof(uint32_t) * BAR_WORDS, c->stream));
     if ((rc = force_rebuild(c))) return rc;
     launch_movement(c->k, step, c->stream);
     CK(cudaEventRecord(ev[0], c->stream));
-    launch_scan(c->k, step, 0, merge_q, c->stream);
-    launch_rebuild_slots(c->k, step, c->stream);
+    launch_step(c->k, step, PH_REBUILD, c->stream);
     CK(cudaEventRecord(ev[1], c->stream));
-    launch_draw(c->k, step, c->stream);
+    launch_step(c->k, step, PH_DRAW, c->stream);
     CK(cudaEventRecord(ev[2], c->stream));
-    launch_queue(c->k, step, c->stream);
-    launch_decide(c->k, step, c->stream);
+    launch_step(c->k, step, PH_DECIDE, c->stream);
     CK(cudaEventRecord(ev[3], c->stream));
-    launch_scan(c->k, step + 1, 0, merge_q, c->stream);
-    launch_rebuild_slots(c->k, step + 1, c->stream);
-    launch_draw(c->k, step + 1, c->stream);
-    c->launches += 7 + 2 * (uint64_t)scan_kernels(c->k);
+    launch_step(c->k, step + 1, PH_REBUILD | PH_DRAW, c->stream);
+    c->launches += 5;
     CK(cudaStreamSynchronize(c->stream));
     for (int j = 0; j < 3; ++j) CK(cudaEventElapsedTime(&ms[j], ev[j], ev[j + 1]));
     for (int j = 0; j < 4; ++j) cudaEventDestroy(ev[j]);

@@ -17,6 +17,7 @@ constexpr uint32_t ERR_LOCATION = 2u;      // an agent ended on an invalid locat
 constexpr uint32_t ERR_TEST_WAIT = 4u;     // bounded-wait self test expired (expected in tests)
 constexpr uint32_t ERR_SCAN_WAIT = 1u;     // a scan tile gave up waiting for its predecessors
 constexpr uint32_t ERR_AGENT_LIST = 8u;    // the agent list disagrees with the histogram or work list
+constexpr uint32_t ERR_BARRIER = 16u;      // a grid barrier of the step kernel gave up waiting
 
 struct DevModel {
     uint32_t n_states, n_variants, n_prog, n_agent_types;
@@ -132,7 +133,10 @@ struct DevLocs {
     float* hazard_x;              // [V][n] its argument x = k*S/n*w*season*dt (adjoint mode)
     uint32_t* no_work_loc;
     uint8_t* flags;               // testing flags
-    uint32_t* tile_sums;          // per-tile sums of the histogram (two-pass scan)
+    uint32_t* tile_sums;          // per-tile sums of the histogram (two-pass scan), per-block sums
+                                  // of the step kernel's rebuild
+    uint32_t* bar;                // the step kernel's grid barrier ([0] arrivals, [1] generation)
+                                  // and per-step decision tickets ([BAR_TICKETS + step])
     uint64_t* scan_status;        // per-tile status words of the single-pass scan (epoch | flag | value)
     uint32_t* scan_state;         // [0] epoch of the next single-pass scan, [1] its tile ticket
     uint32_t* build;              // [0] timestamp at which agents last took new locations,
@@ -290,12 +294,14 @@ void launch_scan(const KArgs& k, uint32_t step_in_day, int with_hazard, int merg
 void launch_scatter_draw(const KArgs& k, uint32_t step_in_day, int scatter, int draw, cudaStream_t s);
 void launch_offsets(const KArgs& k, cudaStream_t s);
 int scan_kernels(const KArgs& k);
-// the day graph's step kernels (psim_kernels.cu, k_draw and around)
-void launch_rebuild_slots(const KArgs& k, uint32_t step_in_day, cudaStream_t s);
-void launch_draw(const KArgs& k, uint32_t step_in_day, cudaStream_t s);
-void launch_queue(const KArgs& k, uint32_t step_in_day, cudaStream_t s);
-void launch_decide(const KArgs& k, uint32_t step_in_day, cudaStream_t s);
+// the day graph's step kernel (psim_kernels.cu, k_step): the phases of one
+// launch (the profiled day graph launches them separately)
+constexpr uint32_t PH_REBUILD = 1u, PH_DRAW = 2u, PH_DECIDE = 4u, PH_ALL = 7u;
+void launch_step(const KArgs& k, uint32_t step_in_day, uint32_t phases, cudaStream_t s);
 void launch_time_shift(uint32_t* a, uint32_t n, uint32_t delta, cudaStream_t s);
+// words of the barrier array: two for the barrier, one ticket per step
+constexpr uint32_t BAR_TICKETS = 2;
+constexpr uint32_t BAR_WORDS = BAR_TICKETS + 1440;
 // work-list segments of the decisions (blocks of the queue kernel at most)
 constexpr uint32_t WORK_MAX_BLOCKS = 152u * 64u;
 // words of the per-day mask of decision steps (1440 steps of one minute at most)

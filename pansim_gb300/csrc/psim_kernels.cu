@@ -1197,28 +1197,68 @@ __global__ void __launch_bounds__(256) k_scatter_draw(KArgs k, uint32_t step, in
 }
 
 // ---------------------------------------------------------------------------
-// The day graph's step kernels.  Per timestep t of the day (step s):
-//   k_scan_v / k_tile_sums_v  only when agents took new locations for t (or a
-//                  rebuild is pending): the prefix of the histogram into the
-//                  locations' first slots; also the merge of the step's
-//                  location quarantine writes when there were any
-//   k_rebuild_slots           the agent list of such a step: every agent takes
-//                  a slot at its location, and the slot keeps the agent's
-//                  susceptibility x age-band factor of every variant
-//   k_draw         the per-location infection ratio and the infection draws,
-//                  location by location over the locations with an infectious
-//                  agent, from the agent list (LocationsList::infectAgents,
-//                  locationList.h:233-310, with the ratio of
-//                  BasicInfection::infectionsAtLocations,
-//                  infectionPolicies.h:520-546)
-//   k_queue        beside the three above: the agents that decide at step
-//                  s + 1 (move_at == t + 1, or everyone at the curfew step),
-//                  queued in per-block work-list segments
-//   k_decide       after k_draw and k_queue: doMovement of the queued agents
-//                  for step s + 1 and the histogram/sum deltas of their moves
-// A step at which nobody takes a new location and nobody decides at the next
-// step runs only k_draw (the others return at their first loads): its cost
-// is the agents at the infectious locations, not the whole population.
+// The day graph's step kernel.  One launch per timestep t (step s of the day),
+// a persistent grid (every block resident; see launch_step) whose phases are
+// separated by grid barriers only where one phase needs another's results:
+//   rebuild   only when agents took new locations for t (or a rebuild is
+//             pending): per-block sums of the histogram | the prefix into
+//             the locations' first slots | every agent takes a slot at its
+//             location, and the slot keeps the agent's susceptibility x
+//             age-band factor of every variant.  The step's location
+//             quarantine writes are merged here too (or alone when there were
+//             some but no rebuild).
+//   draw      the per-location infection ratio and the infection draws,
+//             location by location over the locations with an infectious
+//             agent, from the agent list (LocationsList::infectAgents,
+//             locationList.h:233-310, with the ratio of
+//             BasicInfection::infectionsAtLocations,
+//             infectionPolicies.h:520-546)
+//   decide    only when some agent decides at s + 1 (move_at == t + 1, or
+//             everyone at the curfew step): the block queues its own agents
+//             that decide | doMovement of the queued agents for s + 1 (work
+//             segments taken in turn) and the histogram and sum deltas of
+//             their moves
+// A step at which nobody takes a new location and nobody decides next runs
+// the draw alone, without a barrier: its cost is the agents at the
+// infectious locations, not the whole population.
+
+// Grid barrier of the persistent step kernel: the last block to arrive
+// resets the count and advances the generation the others wait on.  Every
+// wait is bounded: on expiry the block records ERR_BARRIER and returns false,
+// and every later barrier and step kernel returns at once, so a failure ends
+// in an error report, never a hang.
+constexpr uint32_t BARRIER_SPIN_LIMIT = 1u << 24;
+__device__ __forceinline__ bool grid_barrier(const KArgs& k, bool* s_ok) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        bool ok = (*((volatile uint32_t*)k.err) & ERR_BARRIER) == 0;
+        if (ok) {
+            volatile uint32_t* gen_p = (volatile uint32_t*)&k.l.bar[1];
+            const uint32_t gen = *gen_p;
+            __threadfence();
+            const uint32_t arrived = atomicAdd(&k.l.bar[0], 1u) + 1u;
+            if (arrived == gridDim.x) {
+                k.l.bar[0] = 0u;
+                __threadfence();
+                atomicAdd(&k.l.bar[1], 1u);
+            } else {
+                uint32_t spins = 0;
+                while (*gen_p == gen) {
+                    if (++spins > BARRIER_SPIN_LIMIT) {
+                        atomicOr(k.err, ERR_BARRIER);
+                        ok = false;
+                        break;
+                    }
+                    __nanosleep(64);
+                }
+            }
+            __threadfence();
+        }
+        *s_ok = ok;
+    }
+    __syncthreads();
+    return *s_ok;
+}
 
 // Slot data of the agent list: csr_agents[pos] = agent, slot_su[v][pos] =
 // its susceptibility to variant v times its age band's factor (the product
@@ -1236,11 +1276,96 @@ __device__ __forceinline__ void slot_fill(const KArgs& k, uint32_t pos, uint32_t
         k.l.slot_su[(size_t)v * N + pos] = k.a.susceptible[(size_t)v * N + i] * sigma;
 }
 
+// The locations of block b for the rebuild: a contiguous range of `per`
+// locations (a multiple of 4), each thread owning consecutive quads.
+__device__ __forceinline__ uint32_t rebuild_per_block(uint32_t L) {
+    const uint32_t per = (L + gridDim.x - 1) / gridDim.x;
+    return (per + 3u) & ~3u;
+}
+
+__device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t* s_red) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) s_red[warp] = v;
+    __syncthreads();
+    uint32_t tot = 0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) tot += s_red[q];
+    __syncthreads();
+    return tot;
+}
+
+// the step's location quarantine writes into quarantine_until (grid-stride)
+__device__ __forceinline__ void merge_quarantine(const KArgs& k) {
+    const uint32_t L = k.l.n;
+    for (uint32_t l = blockIdx.x * blockDim.x + threadIdx.x; l < L; l += gridDim.x * blockDim.x) {
+        const uint32_t qq = k.l.qu_pending[l];
+        if (qq) {
+            if (qq > k.l.quarantine_until[l]) k.l.quarantine_until[l] = qq;
+            k.l.qu_pending[l] = 0u;
+        }
+    }
+}
+
+// Rebuild of the agent list: returns false when a barrier expired.
 constexpr int SLOT_ILP = 4;
-__global__ void __launch_bounds__(256, 8) k_rebuild_slots(KArgs k, uint32_t step) {
-    if (!csr_rebuild(k, k.clock->t0 + step)) return;
-    if (k.prof && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&k.prof[PROF_REBUILDS], 1ull);
-    const uint32_t N = k.a.n, L = k.l.n;
+__device__ bool phase_rebuild(const KArgs& k, uint32_t* s_red, bool* s_ok) {
+    const uint32_t L = k.l.n, N = k.a.n;
+    const uint32_t per = rebuild_per_block(L);
+    const uint32_t lb = blockIdx.x * per;
+    const uint32_t le = min(L, lb + per);
+    const uint32_t quads = (per / 4 + blockDim.x - 1) / blockDim.x;  // per thread
+    const uint32_t q0 = lb + threadIdx.x * quads * 4u;
+    // 1: the block's total
+    uint32_t mine = 0;
+    for (uint32_t q = 0; q < quads; ++q) {
+        const uint32_t l = q0 + 4u * q;
+        if (l + 3u < le) {
+            const uint4 c = *reinterpret_cast<const uint4*>(k.l.counts + l);
+            mine += c.x + c.y + c.z + c.w;
+        } else {
+            for (uint32_t e = 0; e < 4; ++e)
+                if (l + e < le) mine += k.l.counts[l + e];
+        }
+    }
+    const uint32_t tot = block_sum(mine, s_red);
+    if (threadIdx.x == 0) k.l.tile_sums[blockIdx.x] = tot;
+    if (!grid_barrier(k, s_ok)) return false;
+    // 2: the sums of the blocks before this one, the thread's offset, the
+    // first slot of every location (the cursor the slots advance)
+    uint32_t pre = 0;
+    for (uint32_t b = threadIdx.x; b < blockIdx.x; b += blockDim.x) pre += k.l.tile_sums[b];
+    const uint32_t prefix = block_sum(pre, s_red);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = mine;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_red[warp] = x;
+    __syncthreads();
+    uint32_t woff = 0;
+    for (int q = 0; q < warp; ++q) woff += s_red[q];
+    __syncthreads();
+    uint32_t run = prefix + woff + x - mine;
+    for (uint32_t q = 0; q < quads; ++q) {
+        const uint32_t l = q0 + 4u * q;
+        if (l + 3u < le) {
+            const uint4 c = *reinterpret_cast<const uint4*>(k.l.counts + l);
+            *reinterpret_cast<uint4*>(k.l.cursor + l) = make_uint4(run, run + c.x, run + c.x + c.y, run + c.x + c.y + c.z);
+            run += c.x + c.y + c.z + c.w;
+        } else {
+            for (uint32_t e = 0; e < 4; ++e)
+                if (l + e < le) {
+                    k.l.cursor[l + e] = run;
+                    run += k.l.counts[l + e];
+                }
+        }
+    }
+    if (!grid_barrier(k, s_ok)) return false;
+    // 3: the slots, SLOT_ILP agents' returning atomics in flight per thread
+    // (or one warp-aggregated atomic per location and warp)
     if (k.tune.agg_slot) {
         for (uint32_t base = blockIdx.x * blockDim.x; base < N; base += gridDim.x * blockDim.x) {
             const uint32_t i = base + threadIdx.x;
@@ -1250,26 +1375,26 @@ __global__ void __launch_bounds__(256, 8) k_rebuild_slots(KArgs k, uint32_t step
             const uint32_t pos = take_slot(k, ok, loc, true);
             if (ok) slot_fill(k, pos, i);
         }
-        return;
-    }
-    // SLOT_ILP agents' returning atomics in flight per thread
-    const uint32_t tile = blockDim.x * SLOT_ILP;
-    for (uint32_t base = blockIdx.x * tile; base < N; base += gridDim.x * tile) {
-        uint32_t loc[SLOT_ILP], pos[SLOT_ILP];
+    } else {
+        const uint32_t tile = blockDim.x * SLOT_ILP;
+        for (uint32_t base = blockIdx.x * tile; base < N; base += gridDim.x * tile) {
+            uint32_t loc[SLOT_ILP], pos[SLOT_ILP];
 #pragma unroll
-        for (int u = 0; u < SLOT_ILP; ++u) {
-            const uint32_t i = base + u * blockDim.x + threadIdx.x;
-            loc[u] = i < N ? k.a.location[i] : NONE;
+            for (int u = 0; u < SLOT_ILP; ++u) {
+                const uint32_t i = base + u * blockDim.x + threadIdx.x;
+                loc[u] = i < N ? k.a.location[i] : NONE;
+            }
+#pragma unroll
+            for (int u = 0; u < SLOT_ILP; ++u) pos[u] = loc[u] < L ? atomicAdd(&k.l.cursor[loc[u]], 1u) : NONE;
+#pragma unroll
+            for (int u = 0; u < SLOT_ILP; ++u)
+                if (loc[u] < L) slot_fill(k, pos[u], base + u * blockDim.x + threadIdx.x);
         }
-#pragma unroll
-        for (int u = 0; u < SLOT_ILP; ++u) pos[u] = loc[u] < L ? atomicAdd(&k.l.cursor[loc[u]], 1u) : NONE;
-#pragma unroll
-        for (int u = 0; u < SLOT_ILP; ++u)
-            if (loc[u] < L) slot_fill(k, pos[u], base + u * blockDim.x + threadIdx.x);
     }
+    return grid_barrier(k, s_ok);
 }
 
-// expected-infection accumulation of the draw kernel: one atomic per replica
+// expected-infection accumulation of the draws: one atomic per replica
 // present in the warp (warp-collective; rep given, not looked up)
 __device__ __forceinline__ void add_expected_rep(const KArgs& k, bool act, uint32_t rep, double term) {
     const unsigned am = __ballot_sync(0xffffffffu, act && term != 0.0);
@@ -1299,28 +1424,6 @@ __device__ __forceinline__ void infect_agent(const KArgs& k, uint32_t i, uint32_
     k.a.st_worst_state[i] = (int8_t)k.m.first_infected;
     k.a.st_worst_ts[i] = t;
     k.a.st_variant_mask[i] |= 1u << v;
-}
-
-// Hazards of every variant at location l from its fixed-point sums and count
-// (the scan's formula); returns whether some variant's sum is nonzero.
-__device__ __forceinline__ bool location_hazards(const KArgs& k, uint32_t l, uint32_t n_l, float season, uint32_t dt) {
-    const uint32_t L = k.l.n, V = k.m.n_variants;
-    const uint32_t rep = k.l.rep[l];
-    const float w_l = k.l.infectiousness[l];
-    const float k_f = k.r.k_f[rep];
-    bool nz = false;
-    for (uint32_t v = 0; v < V; ++v) {
-        const size_t idx = (size_t)v * L + l;
-        const long long fix = (long long)k.l.sfix[idx];
-        float h = 0.0f, x = 0.0f;
-        if (fix != 0) {
-            h = psim_hazard_x(fix, n_l, k_f, w_l, season, dt, &x);
-            nz = true;
-        }
-        k.l.hazard[idx] = h;
-        if (k.adj.on) k.l.hazard_x[idx] = x;
-    }
-    return nz;
 }
 
 // Position of the n-th (0-based) set bit of w, n < popc(w): five halvings,
@@ -1356,59 +1459,138 @@ __device__ __forceinline__ void chunk_bit(uint32_t r, uint32_t words, uint32_t i
     *bit = nth_set_bit(w, r - exc) & 31u;
 }
 
-// Location-ordered infection of step `step`.  A warp takes a chunk of
-// DRAW_WPW mask words (32 locations each).  Pass 1: the dirty locations
-// (sum or count changed since their last evaluation) get their hazards
-// recomputed and their hazard-mask bits rewritten.  Pass 2: every location
-// whose bit is set has its agent-list segment expanded over the lanes (a warp
-// scan of the segment lengths, each lane finds its entry's location by a
-// binary search) and each agent draws from its Philox stream (seed, agent,
-// t); the slot holds the susceptibility product, so an agent that is not
-// infected costs two coalesced loads of its slot.  An agent that is infected
-// changes its own location's sum (a delta for the next step: only this warp
-// reads that location's sum in this step).
-__global__ void __launch_bounds__(256, 4) k_draw(KArgs k, uint32_t step) {
-    __shared__ double s_grad[GRAD_N];
-    __shared__ uint32_t s_nz[8][DRAW_WPW];
-    grad_begin(k, s_grad);
+// Pass 1 of a chunk: the dirty locations (sum or count changed since their
+// last evaluation) get their hazards recomputed from the fixed-point sums
+// (the scan's formula) and their hazard-mask bits rewritten.  Lane j takes
+// bit j of every word, four words at a time with their loads issued together.
+// Returns the chunk's new hazard-mask word of lane q < DRAW_WPW.
+__device__ __forceinline__ uint32_t draw_dirty(const KArgs& k, uint32_t w0, uint32_t sm, float season, uint32_t dt) {
+    const uint32_t L = k.l.n, V = k.m.n_variants;
+    const int lane = threadIdx.x & 31;
+    uint32_t my_nz = 0;
+#pragma unroll
+    for (int g = 0; g < DRAW_WPW; g += 4) {
+        bool dy[4];
+        uint32_t cnt[4], rp[4];
+        float wl[4];
+        long long fx[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const uint32_t smq = __shfl_sync(0xffffffffu, sm, g + u);
+            const uint32_t l = (w0 + g + u) * 32u + (uint32_t)lane;
+            dy[u] = ((smq >> lane) & 1u) && l < L;
+            cnt[u] = 0;
+            rp[u] = 0;
+            wl[u] = 0.0f;
+            fx[u] = 0;
+            if (dy[u]) {
+                cnt[u] = k.l.counts[l];
+                rp[u] = k.l.rep[l];
+                wl[u] = k.l.infectiousness[l];
+                fx[u] = (long long)k.l.sfix[l];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            bool nz = false;
+            if (dy[u]) {
+                const uint32_t l = (w0 + g + u) * 32u + (uint32_t)lane;
+                const float k_f = k.r.k_f[rp[u]];
+                for (uint32_t v = 0; v < V; ++v) {
+                    const size_t idx = (size_t)v * L + l;
+                    const long long fix = v == 0 ? fx[u] : (long long)k.l.sfix[idx];
+                    float h = 0.0f, x = 0.0f;
+                    if (fix != 0) {
+                        h = psim_hazard_x(fix, cnt[u], k_f, wl[u], season, dt, &x);
+                        nz = true;
+                    }
+                    k.l.hazard[idx] = h;
+                    if (k.adj.on) k.l.hazard_x[idx] = x;
+                }
+            }
+            const uint32_t nzw = __ballot_sync(0xffffffffu, nz);
+            if (lane == g + u) my_nz = nzw;
+        }
+    }
+    return my_nz;
+}
+
+// The draws of one agent-list entry (the agent in slot pos at location loc of
+// replica rep, variant-0 hazard h0); returns the sum of min(1, p) over its
+// draws.  An agent that is infected updates its slot's susceptibility
+// products and its location's sum (a delta for the next step: only the warp
+// handling this location reads its sum in this step).
+__device__ __forceinline__ double draw_entry(const KArgs& k, uint32_t pos, uint32_t i, uint32_t loc, uint32_t rep,
+                                             float h0, uint32_t t, double* s_grad) {
     const uint32_t L = k.l.n, N = k.a.n, V = k.m.n_variants;
-    const uint32_t t = k.clock->t0 + step;
+    const float su0 = k.l.slot_su[pos];
+    const unsigned long long seed = k.r.seed[rep];
+    const uint32_t li = i - k.r.agent_off[rep];
+    double term = 0.0;
+    bool infected = false;
+    float inf0 = 0.0f, sigma = 0.0f;
+    uint32_t var0 = 0;
+    for (uint32_t v = 0; v < V; ++v) {
+        const float h = v == 0 ? h0 : k.l.hazard[(size_t)v * L + loc];
+        if (!(h > 0.0f)) continue;
+        if (!k.r.variant_active[rep * V + v]) continue;
+        // after an infection the later variants read the agent's new
+        // susceptibility (what the slot then gets)
+        float s_eff;
+        if (!infected)
+            s_eff = v == 0 ? su0 : k.l.slot_su[(size_t)v * N + pos];
+        else
+            s_eff = k.a.susceptible[(size_t)v * N + i] * sigma;
+        if (!(s_eff > 0.0f)) continue;
+        const float pf = h * s_eff;
+        term += pf < 1.0f ? (double)pf : 1.0;
+        if (k.adj.on && pf < 1.0f) adjoint_terms(k, i, loc, v, rep, h, k.a.susceptible[(size_t)v * N + i], s_eff, s_grad);
+        const double U = psim_u01_once(seed, li, t, PSIM_PHASE_INFECT + v);
+        if (U < (double)pf) {
+            if (!infected) {
+                inf0 = k.a.infectious[i];
+                var0 = inf0 > 0.0f ? k.a.variant[i] : 0u;
+                sigma = k.p.sigma_band[k.a.band[i]];
+                infected = true;
+            }
+            infect_agent(k, i, v, loc, t);
+        }
+    }
+    if (infected) {
+        for (uint32_t v = 0; v < V; ++v) k.l.slot_su[(size_t)v * N + pos] = k.a.susceptible[(size_t)v * N + i] * sigma;
+        const float inf = k.a.infectious[i];
+        const uint32_t var = inf > 0.0f ? k.a.variant[i] : 0u;
+        count_agent_delta(k, true, loc, loc, inf0, var0, inf, var);
+    }
+    return term;
+}
+
+// The draw phase: a warp takes a chunk of DRAW_WPW mask words (32 locations
+// each): pass 1 (draw_dirty) for the dirty locations, then every location
+// whose hazard-mask bit is set has its agent-list segment expanded over the
+// lanes (a warp scan of the segment lengths, each lane finds its entry's
+// location by a binary search) and each agent draws from its Philox stream
+// (seed, agent, t).  The slot holds the susceptibility product, so an agent
+// that is not infected costs two coalesced loads of its slot.
+__device__ void phase_draw(const KArgs& k, uint32_t t, double* s_grad, uint32_t* n_entries, uint32_t* n_visited) {
+    const uint32_t L = k.l.n, N = k.a.n;
     const float season = k.clock->season;
     const uint32_t dt = k.p.time_step;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t n_words = (L + 31) >> 5;
     const uint32_t n_chunks = (n_words + DRAW_WPW - 1) / DRAW_WPW;
     const uint32_t nw = gridDim.x * (blockDim.x >> 5);
-    uint32_t entries = 0, visited = 0;  // counted for the profiling figures
+    uint32_t entries = 0, visited = 0;
     for (uint32_t ch = blockIdx.x * (blockDim.x >> 5) + warp; ch < n_chunks; ch += nw) {
         const uint32_t w0 = ch * DRAW_WPW;
         const bool own = lane < DRAW_WPW && w0 + lane < n_words;
         uint32_t hm = own ? k.l.hmask[w0 + lane] : 0u;
         const uint32_t sm = own ? k.l.smask[w0 + lane] : 0u;
         if (!__any_sync(0xffffffffu, (hm | sm) != 0u)) continue;
-        // pass 1: the dirty locations
         if (__any_sync(0xffffffffu, sm != 0u)) {
-            if (lane < DRAW_WPW) s_nz[warp][lane] = 0u;
-            __syncwarp();
-            uint32_t inc = __popc(sm);
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
-                if (lane >= o) inc += y;
-            }
-            const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
-            for (uint32_t b0 = 0; b0 < total; b0 += 32) {
-                const uint32_t r = b0 + lane;
-                uint32_t wo, bit;
-                chunk_bit(r, sm, inc, &wo, &bit);
-                const uint32_t l = (w0 + wo) * 32u + bit;
-                if (r < total && l < L) {
-                    if (location_hazards(k, l, k.l.counts[l], season, dt)) atomicOr(&s_nz[warp][wo], 1u << bit);
-                }
-            }
-            __syncwarp();
+            const uint32_t nzw = draw_dirty(k, w0, sm, season, dt);
             if (own && sm) {
-                hm = (hm & ~sm) | s_nz[warp][lane];
+                hm = (hm & ~sm) | nzw;
                 k.l.hmask[w0 + lane] = hm;
                 k.l.smask[w0 + lane] = 0u;
             }
@@ -1446,7 +1628,6 @@ __global__ void __launch_bounds__(256, 4) k_draw(KArgs k, uint32_t step) {
                 }
                 beg = end - len;
             }
-            // the segments of these (up to 32) locations over the lanes
             uint32_t einc = len;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
@@ -1454,7 +1635,7 @@ __global__ void __launch_bounds__(256, 4) k_draw(KArgs k, uint32_t step) {
                 if (lane >= o) einc += y;
             }
             const uint32_t etotal = __shfl_sync(0xffffffffu, einc, 31);
-            entries += lane == 0 ? etotal : 0u;
+            entries += etotal;
             for (uint32_t e0 = 0; e0 < etotal; e0 += 32) {
                 const uint32_t e = e0 + lane;
                 // owner lane: the number of lanes whose inclusive end is <= e
@@ -1472,69 +1653,22 @@ __global__ void __launch_bounds__(256, 4) k_draw(KArgs k, uint32_t step) {
                 const uint32_t q_rep = __shfl_sync(0xffffffffu, rep, (int)q);
                 const float q_h0 = __shfl_sync(0xffffffffu, h0, (int)q);
                 bool act = e < etotal;
-                double term = 0.0;
                 const uint32_t pos = q_beg + (e - (q_inc - q_len));
                 uint32_t i = NONE;
                 if (act) {
-                    // an agent list that disagrees with the histogram is
-                    // reported, never read out of bounds
                     if (pos < N) i = k.l.csr_agents[pos];
                     if (i >= N) {
                         atomicOr(k.err, ERR_AGENT_LIST);
                         act = false;
                     }
                 }
-                if (act) {
-                    const float su0 = k.l.slot_su[pos];
-                    const unsigned long long seed = k.r.seed[q_rep];
-                    const uint32_t li = i - k.r.agent_off[q_rep];
-                    bool infected = false;
-                    float inf0 = 0.0f, sigma = 0.0f;
-                    uint32_t var0 = 0;
-                    for (uint32_t v = 0; v < V; ++v) {
-                        const float h = v == 0 ? q_h0 : k.l.hazard[(size_t)v * L + q_loc];
-                        if (!(h > 0.0f)) continue;
-                        if (!k.r.variant_active[q_rep * V + v]) continue;
-                        // after an infection the later variants read the
-                        // agent's new susceptibility (what the slot then gets)
-                        float s_eff;
-                        if (!infected)
-                            s_eff = v == 0 ? su0 : k.l.slot_su[(size_t)v * N + pos];
-                        else
-                            s_eff = k.a.susceptible[(size_t)v * N + i] * sigma;
-                        if (!(s_eff > 0.0f)) continue;
-                        const float pf = h * s_eff;
-                        term += pf < 1.0f ? (double)pf : 1.0;
-                        if (k.adj.on && pf < 1.0f)
-                            adjoint_terms(k, i, q_loc, v, q_rep, h, k.a.susceptible[(size_t)v * N + i], s_eff, s_grad);
-                        const double U = psim_u01_once(seed, li, t, PSIM_PHASE_INFECT + v);
-                        if (U < (double)pf) {
-                            if (!infected) {
-                                inf0 = k.a.infectious[i];
-                                var0 = inf0 > 0.0f ? k.a.variant[i] : 0u;
-                                sigma = k.p.sigma_band[k.a.band[i]];
-                                infected = true;
-                            }
-                            infect_agent(k, i, v, q_loc, t);
-                        }
-                    }
-                    if (infected) {
-                        for (uint32_t v = 0; v < V; ++v)
-                            k.l.slot_su[(size_t)v * N + pos] = k.a.susceptible[(size_t)v * N + i] * sigma;
-                        const float inf = k.a.infectious[i];
-                        const uint32_t var = inf > 0.0f ? k.a.variant[i] : 0u;
-                        count_agent_delta(k, true, q_loc, q_loc, inf0, var0, inf, var);
-                    }
-                }
+                const double term = act ? draw_entry(k, pos, i, q_loc, q_rep, q_h0, t, s_grad) : 0.0;
                 if (k.track_expected) add_expected_rep(k, act, q_rep, term);
             }
         }
     }
-    if (k.prof && lane == 0 && (entries | visited)) {
-        atomicAdd(&k.prof[PROF_DRAW_ENTRIES], (unsigned long long)entries);
-        atomicAdd(&k.prof[PROF_DRAW_LOCATIONS], (unsigned long long)visited);
-    }
-    grad_end(k, s_grad);
+    *n_entries += entries;
+    *n_visited += visited;
 }
 
 // whether any agent decides at step s1 of the day (or it is the curfew step)
@@ -1543,15 +1677,10 @@ __device__ __forceinline__ bool decides_at(const KArgs& k, uint32_t s1) {
     return curfew_now || mask_has(k, s1);
 }
 
-// The agents that decide at step + 1, in the block's own segment of the work
-// list (shared-memory counter: no global contention).  Reads one word per
-// agent, and nothing at a step nobody decides at.
-__global__ void __launch_bounds__(256, 8) k_queue(KArgs k, uint32_t step, uint32_t cap) {
-    const uint32_t s1 = step + 1;
-    if (!decides_at(k, s1)) return;
-    if (k.prof && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&k.prof[PROF_QUEUE_STEPS], 1ull);
-    __shared__ uint32_t s_cnt;
-    if (threadIdx.x == 0) s_cnt = 0u;
+// The block's agents that decide at s1, in its own segment of the work list
+// (shared-memory counter: no global contention).  Reads one word per agent.
+__device__ __forceinline__ uint32_t phase_queue(const KArgs& k, uint32_t s1, uint32_t cap, uint32_t* s_cnt) {
+    if (threadIdx.x == 0) *s_cnt = 0u;
     __syncthreads();
     const uint32_t N = k.a.n;
     const bool curfew_now = k.p.enable_curfew && k.p.curfew_begin == s1;
@@ -1565,31 +1694,31 @@ __global__ void __launch_bounds__(256, 8) k_queue(KArgs k, uint32_t step, uint32
         const unsigned cm = __ballot_sync(0xffffffffu, mover);
         if (cm) {
             uint32_t basew = 0;
-            if (lane == __ffs(cm) - 1) basew = atomicAdd(&s_cnt, (uint32_t)__popc(cm));
+            if (lane == __ffs(cm) - 1) basew = atomicAdd(s_cnt, (uint32_t)__popc(cm));
             basew = __shfl_sync(0xffffffffu, basew, __ffs(cm) - 1);
             if (mover) seg[basew + __popc(cm & lanemask_lt())] = i;
         }
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        k.a.seg_count[blockIdx.x] = s_cnt;
-        if (k.prof && s_cnt) atomicAdd(&k.prof[PROF_MOVERS], (unsigned long long)s_cnt);
-    }
+    const uint32_t n = *s_cnt;
+    if (threadIdx.x == 0) k.a.seg_count[blockIdx.x] = n;
+    return n;
 }
 
-// doMovement of the queued agents for step + 1, one segment per block in
-// turn; then the histogram and sum deltas of the agents that took a new
-// location.  Four blocks per SM: the decisions are chains of dependent
-// loads, and fewer resident warps (the registers the compiler would take
-// otherwise) measured slower than a few spills.
-__global__ void __launch_bounds__(256, 4) k_decide(KArgs k, uint32_t step, uint32_t cap, uint32_t n_seg) {
+// doMovement of the queued agents for s1: the segments are taken in turn
+// from the step's ticket counter (zeroed at the start of the day graph),
+// then the histogram and sum deltas of the agents that took a new location.
+__device__ void phase_decide(const KArgs& k, uint32_t step, uint32_t cap, uint32_t* s_mm, uint32_t* s_seg) {
     const uint32_t s1 = step + 1;
-    if (!decides_at(k, s1)) return;
-    __shared__ uint32_t s_mm[MOVE_MASK_WORDS];
-    mask_clear_shared(s_mm);
     const StepClock c = step_clock(k, s1);
+    uint32_t* ticket = &k.l.bar[BAR_TICKETS + step];
     bool moved = false;
-    for (uint32_t sg = blockIdx.x; sg < n_seg; sg += gridDim.x) {
+    for (;;) {
+        if (threadIdx.x == 0) *s_seg = atomicAdd(ticket, 1u);
+        __syncthreads();
+        const uint32_t sg = *s_seg;
+        __syncthreads();
+        if (sg >= gridDim.x) break;
         uint32_t n = k.a.seg_count[sg];
         if (n > cap) {
             if (threadIdx.x == 0) atomicOr(k.err, ERR_AGENT_LIST);
@@ -1618,7 +1747,49 @@ __global__ void __launch_bounds__(256, 4) k_decide(KArgs k, uint32_t step, uint3
         }
     }
     publish_moved(k, moved, c.t);
-    mask_flush(k, s_mm);
+}
+
+// The step kernel: see the section comment.  cap = the work-list segment
+// size of a block.
+__global__ void __launch_bounds__(256, 4) k_step(KArgs k, uint32_t step, uint32_t phases, uint32_t cap) {
+    __shared__ double s_grad[GRAD_N];
+    __shared__ uint32_t s_mm[MOVE_MASK_WORDS];
+    __shared__ uint32_t s_red[32];
+    __shared__ uint32_t s_cnt, s_seg;
+    __shared__ bool s_ok;
+    if (*((volatile uint32_t*)k.err) & ERR_BARRIER) return;  // an earlier barrier expired
+    const uint32_t t = k.clock->t0 + step;
+    if (phases & PH_REBUILD) {
+        const bool rebuild = csr_decide(k, t);
+        if (rebuild) {
+            if (k.prof && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&k.prof[PROF_REBUILDS], 1ull);
+            if (!phase_rebuild(k, s_red, &s_ok)) return;
+        }
+        // the step's location quarantine writes (decisions of step t)
+        if (k.p.quarantine_policy > 1 && k.l.build[3] == t) merge_quarantine(k);
+    }
+    if (phases & PH_DRAW) {
+        grad_begin(k, s_grad);
+        uint32_t entries = 0, visited = 0;
+        phase_draw(k, t, s_grad, &entries, &visited);
+        if (k.prof && (threadIdx.x & 31) == 0 && (entries | visited)) {
+            atomicAdd(&k.prof[PROF_DRAW_ENTRIES], (unsigned long long)entries);
+            atomicAdd(&k.prof[PROF_DRAW_LOCATIONS], (unsigned long long)visited);
+        }
+        grad_end(k, s_grad);
+    }
+    if ((phases & PH_DECIDE) && step + 1 < k.spd && decides_at(k, step + 1)) {
+        mask_clear_shared(s_mm);
+        const uint32_t n = phase_queue(k, step + 1, cap, &s_cnt);
+        if (k.prof && threadIdx.x == 0) {
+            if (n) atomicAdd(&k.prof[PROF_MOVERS], (unsigned long long)n);
+            if (blockIdx.x == 0) atomicAdd(&k.prof[PROF_QUEUE_STEPS], 1ull);
+        }
+        // every draw and every block's queue before any decision
+        if (!grid_barrier(k, &s_ok)) return;
+        phase_decide(k, step, cap, s_mm, &s_seg);
+        mask_flush(k, s_mm);
+    }
 }
 
 // Canonical CSR order (ascending agent id inside a location, the output of
@@ -2307,47 +2478,31 @@ void launch_movement(const KArgs& k, uint32_t step, cudaStream_t s) {
     if (!g) g = wave_grid(k_movement, 1u << 30);
     k_movement<<<agent_grid(k, g), 256, 0, s>>>(k, step);
 }
-// The day graph's step kernels (see k_draw): the work-list segments are one
-// per queue block, each as large as the agents the block visits.
-struct StepGrid {
-    unsigned queue, decide, draw, slots;
-    uint32_t cap;
-};
-static StepGrid step_grid(const KArgs& k) {
-    static unsigned wq = 0, wd = 0, wr = 0, ws = 0;
-    if (!wq) {
-        wq = wave_grid(k_queue, 1u << 30);
-        wd = wave_grid(k_decide, 1u << 30);
-        wr = wave_grid(k_draw, 1u << 30);
-        ws = wave_grid(k_rebuild_slots, 1u << 30);
+// The step kernel's grid: every block resident at once (its grid barriers
+// need that), tune.blocks_per_sm capped at the kernel's occupancy, and no
+// more blocks than the population and locations give work to.  Each block's
+// work-list segment holds the agents its queue pass visits.
+static unsigned step_blocks_per_sm() {
+    static int occ = 0;
+    if (!occ) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_step, 256, 0) != cudaSuccess || occ < 1) occ = 1;
     }
-    StepGrid g;
-    g.queue = std::min(agent_grid(k, wq), (unsigned)WORK_MAX_BLOCKS);
-    g.cap = (uint32_t)((((size_t)k.a.n + (size_t)g.queue * 256 - 1) / ((size_t)g.queue * 256)) * 256);
-    // the decisions are a few percent of the agents: at most one wave of
-    // blocks, each taking segments in turn
-    g.decide = std::min(g.queue, wd);
-    // one warp per chunk of DRAW_WPW mask words, at most one wave
-    const size_t chunks = (((size_t)k.l.n + 31) / 32 + DRAW_WPW - 1) / DRAW_WPW;
-    g.draw = (unsigned)std::max<size_t>(1, std::min<size_t>((chunks + 7) / 8, wr));
-    g.slots = agent_grid(k, ws);
-    return g;
+    return (unsigned)occ;
 }
-void launch_rebuild_slots(const KArgs& k, uint32_t step, cudaStream_t s) {
-    const StepGrid g = step_grid(k);
-    k_rebuild_slots<<<g.slots, 256, 0, s>>>(k, step);
+static void step_geometry(const KArgs& k, unsigned* grid, uint32_t* cap) {
+    const unsigned occ = step_blocks_per_sm();
+    const unsigned bps = k.tune.blocks_per_sm ? std::min<unsigned>(k.tune.blocks_per_sm, occ) : occ;
+    const size_t want = std::max<size_t>(((size_t)k.a.n + 255) / 256, (((size_t)k.l.n + 31) / 32 + 7) / 8);
+    unsigned g = (unsigned)std::min<size_t>((size_t)sm_count() * bps, std::max<size_t>(want, 1));
+    g = std::min(g, (unsigned)WORK_MAX_BLOCKS);
+    *grid = g;
+    *cap = (uint32_t)((((size_t)k.a.n + (size_t)g * 256 - 1) / ((size_t)g * 256)) * 256);
 }
-void launch_draw(const KArgs& k, uint32_t step, cudaStream_t s) {
-    const StepGrid g = step_grid(k);
-    k_draw<<<g.draw, 256, 0, s>>>(k, step);
-}
-void launch_queue(const KArgs& k, uint32_t step, cudaStream_t s) {
-    const StepGrid g = step_grid(k);
-    k_queue<<<g.queue, 256, 0, s>>>(k, step, g.cap);
-}
-void launch_decide(const KArgs& k, uint32_t step, cudaStream_t s) {
-    const StepGrid g = step_grid(k);
-    k_decide<<<g.decide, 256, 0, s>>>(k, step, g.cap, g.queue);
+void launch_step(const KArgs& k, uint32_t step, uint32_t phases, cudaStream_t s) {
+    unsigned g;
+    uint32_t cap;
+    step_geometry(k, &g, &cap);
+    k_step<<<g, 256, 0, s>>>(k, step, phases, cap);
 }
 void launch_count(const KArgs& k, cudaStream_t s) { k_count<<<grid_for(k.a.n, 8), 256, 0, s>>>(k); }
 // the scan of the histogram with 256 x tune.scan_items locations per tile:

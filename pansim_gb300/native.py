@@ -299,8 +299,8 @@ class GpuSim:
         self._ck(lib().psim_set_profiling(self.h, 1 if on else 0), "set_profiling")
 
     def day_kernel_ms(self):
-        """Summed kernel durations of the last profiled day: movement(0), the
-        rebuilds (scan + slots), the draws, the queues, the decisions."""
+        """Summed durations of the last profiled day: movement(0), the step
+        kernel's rebuilds, draws, queues + decisions, and 0."""
         ms = np.zeros(5, np.float32)
         self._ck(lib().psim_day_kernel_ms(self.h, _p(ms)), "day_kernel_ms")
         return ms

@@ -184,7 +184,7 @@ def test_profiled_graph_same_results_and_kernel_times(gpu_lib):
     for d in range(2):
         assert stats_rows(o.run_day(d)) == stats_rows(g.run_day(d)), d
         ms = g.day_kernel_ms()
-        assert (ms > 0).all(), ms
+        assert (ms[:4] > 0).all() and ms[4] == 0, ms
         assert ms.sum() <= g.last_day_ms() * 1.001
         entries, visited, movers, queues, rebuilds = g.day_counts()
         assert entries > 0 and visited > 0 and movers > 0 and 0 < queues < 143 and 0 < rebuilds <= 144
