@@ -1442,43 +1442,62 @@ __device__ __forceinline__ uint32_t nth_set_bit(uint32_t w, uint32_t n) {
     return pos;
 }
 
-// The r-th set bit (0-based) of the chunk's words held by lanes 0..DRAW_WPW-1,
-// given each lane's inclusive prefix of the set-bit counts: the word index
-// within the chunk and the bit (meaningful for r below the chunk's total
-// only).  Every lane of the warp calls it, and every shuffle runs on all
-// lanes.
-constexpr int DRAW_WPW = 8;  // mask words per warp chunk (256 locations)
-__device__ __forceinline__ void chunk_bit(uint32_t r, uint32_t words, uint32_t inc, uint32_t* wo, uint32_t* bit) {
-    uint32_t o = 0;
+// Owner lane of item r among lanes holding inclusive prefix counts `inc`
+// (non-decreasing over the lanes): the number of lanes whose inclusive end is
+// <= r, by a five-step binary search.  Every lane calls it.
+__device__ __forceinline__ uint32_t owner_lane(uint32_t r, uint32_t inc) {
+    uint32_t q = 0;
 #pragma unroll
-    for (int q = 0; q < DRAW_WPW - 1; ++q) o += r >= __shfl_sync(0xffffffffu, inc, q) ? 1u : 0u;
-    const uint32_t w = __shfl_sync(0xffffffffu, words, (int)o);
-    const uint32_t before = __shfl_sync(0xffffffffu, inc, o > 0 ? (int)o - 1 : 0);
-    const uint32_t exc = o > 0 ? before : 0u;
-    *wo = o;
-    *bit = nth_set_bit(w, r - exc) & 31u;
+    for (int st = 16; st > 0; st >>= 1) {
+        const uint32_t v = __shfl_sync(0xffffffffu, inc, (int)(q + st - 1));
+        if (r >= v) q += st;
+    }
+    return q & 31u;
 }
 
-// Pass 1 of a chunk: the dirty locations (sum or count changed since their
-// last evaluation) get their hazards recomputed from the fixed-point sums
-// (the scan's formula) and their hazard-mask bits rewritten.  Lane j takes
-// bit j of every word, four words at a time with their loads issued together.
-// Returns the chunk's new hazard-mask word of lane q < DRAW_WPW.
-__device__ __forceinline__ uint32_t draw_dirty(const KArgs& k, uint32_t w0, uint32_t sm, float season, uint32_t dt) {
+// The r-th set bit (0-based) of the words held by the lanes (lane j: word
+// word_id, bits `words`, inclusive prefix `inc` of the set-bit counts): the
+// location (meaningful for r below the total only).  Every lane calls it, and
+// every shuffle runs on all lanes.
+__device__ __forceinline__ uint32_t set_bit_location(uint32_t r, uint32_t words, uint32_t word_id, uint32_t inc) {
+    const uint32_t o = owner_lane(r, inc);
+    const uint32_t w = __shfl_sync(0xffffffffu, words, (int)o);
+    const uint32_t wid = __shfl_sync(0xffffffffu, word_id, (int)o);
+    const uint32_t before = __shfl_sync(0xffffffffu, inc, o > 0 ? (int)o - 1 : 0);
+    const uint32_t exc = o > 0 ? before : 0u;
+    return wid * 32u + (nth_set_bit(w, r - exc) & 31u);
+}
+
+// Dirty pass of the draw: the dirty locations (sum or count changed since
+// their last evaluation) of the lanes' words get their hazards recomputed from
+// the fixed-point sums (the scan's formula).  Lane j takes bit j of each dirty
+// word, four words at a time with their loads issued together.  Returns, in
+// each lane, the new hazard bits of its own word.
+__device__ __forceinline__ uint32_t draw_dirty(const KArgs& k, uint32_t word_id, uint32_t sm, float season,
+                                               uint32_t dt) {
     const uint32_t L = k.l.n, V = k.m.n_variants;
     const int lane = threadIdx.x & 31;
     uint32_t my_nz = 0;
+    unsigned pending = __ballot_sync(0xffffffffu, sm != 0u);
+    while (pending) {  // warp-uniform
+        int qs[4];
 #pragma unroll
-    for (int g = 0; g < DRAW_WPW; g += 4) {
+        for (int u = 0; u < 4; ++u) {
+            qs[u] = pending ? __ffs(pending) - 1 : -1;
+            if (pending) pending &= pending - 1;
+        }
         bool dy[4];
-        uint32_t cnt[4], rp[4];
+        uint32_t cnt[4], rp[4], lid[4];
         float wl[4];
         long long fx[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-            const uint32_t smq = __shfl_sync(0xffffffffu, sm, g + u);
-            const uint32_t l = (w0 + g + u) * 32u + (uint32_t)lane;
-            dy[u] = ((smq >> lane) & 1u) && l < L;
+            const int src = qs[u] >= 0 ? qs[u] : 0;
+            const uint32_t smq = __shfl_sync(0xffffffffu, sm, src);
+            const uint32_t wid = __shfl_sync(0xffffffffu, word_id, src);
+            const uint32_t l = wid * 32u + (uint32_t)lane;
+            lid[u] = l;
+            dy[u] = qs[u] >= 0 && ((smq >> lane) & 1u) && l < L;
             cnt[u] = 0;
             rp[u] = 0;
             wl[u] = 0.0f;
@@ -1494,7 +1513,7 @@ __device__ __forceinline__ uint32_t draw_dirty(const KArgs& k, uint32_t w0, uint
         for (int u = 0; u < 4; ++u) {
             bool nz = false;
             if (dy[u]) {
-                const uint32_t l = (w0 + g + u) * 32u + (uint32_t)lane;
+                const uint32_t l = lid[u];
                 const float k_f = k.r.k_f[rp[u]];
                 for (uint32_t v = 0; v < V; ++v) {
                     const size_t idx = (size_t)v * L + l;
@@ -1509,17 +1528,28 @@ __device__ __forceinline__ uint32_t draw_dirty(const KArgs& k, uint32_t w0, uint
                 }
             }
             const uint32_t nzw = __ballot_sync(0xffffffffu, nz);
-            if (lane == g + u) my_nz = nzw;
+            if (lane == qs[u]) my_nz = nzw;
         }
     }
     return my_nz;
 }
 
+// U < p for the 53-bit uniform U = K * 2^-53 of the words (a, b)
+// (psim_u01_from) and a float probability p > 0, in integers: p * 2^53 is
+// exact in float (a power-of-two scaling of a normal or subnormal p), and
+// K < p * 2^53 holds exactly when K < ceil(p * 2^53).
+__device__ __forceinline__ bool u01_below(uint32_t a, uint32_t b, float p) {
+    if (p >= 1.0f) return true;
+    const unsigned long long K = ((unsigned long long)(a >> 5) << 26) | (unsigned long long)(b >> 6);
+    return K < __float2ull_ru(p * 9007199254740992.0f);
+}
+
 // The draws of one agent-list entry (the agent in slot pos at location loc of
 // replica rep, variant-0 hazard h0); returns the sum of min(1, p) over its
-// draws.  An agent that is infected updates its slot's susceptibility
-// products and its location's sum (a delta for the next step: only the warp
-// handling this location reads its sum in this step).
+// draws when expected infections are tracked (else 0).  An agent that is
+// infected updates its slot's susceptibility products and its location's sum
+// (a delta for the next step: only the warp handling this location reads its
+// sum in this step).
 __device__ __forceinline__ double draw_entry(const KArgs& k, uint32_t pos, uint32_t i, uint32_t loc, uint32_t rep,
                                              float h0, uint32_t t, double* s_grad) {
     const uint32_t L = k.l.n, N = k.a.n, V = k.m.n_variants;
@@ -1543,10 +1573,17 @@ __device__ __forceinline__ double draw_entry(const KArgs& k, uint32_t pos, uint3
             s_eff = k.a.susceptible[(size_t)v * N + i] * sigma;
         if (!(s_eff > 0.0f)) continue;
         const float pf = h * s_eff;
-        term += pf < 1.0f ? (double)pf : 1.0;
+        if (k.track_expected) term += pf < 1.0f ? (double)pf : 1.0;
         if (k.adj.on && pf < 1.0f) adjoint_terms(k, i, loc, v, rep, h, k.a.susceptible[(size_t)v * N + i], s_eff, s_grad);
-        const double U = psim_u01_once(seed, li, t, PSIM_PHASE_INFECT + v);
-        if (U < (double)pf) {
+        // the uniform of the stream (seed, agent, t, infection + v), as
+        // psim_u01_once draws it
+        psim_ctr4 c;
+        c.v[0] = li;
+        c.v[1] = t;
+        c.v[2] = PSIM_PHASE_INFECT + v;
+        c.v[3] = 0u;
+        const psim_ctr4 o = psim_philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+        if (u01_below(o.v[0], o.v[1], pf)) {
             if (!infected) {
                 inf0 = k.a.infectious[i];
                 var0 = inf0 > 0.0f ? k.a.variant[i] : 0u;
@@ -1565,41 +1602,44 @@ __device__ __forceinline__ double draw_entry(const KArgs& k, uint32_t pos, uint3
     return term;
 }
 
-// The draw phase: a warp takes a chunk of DRAW_WPW mask words (32 locations
-// each): pass 1 (draw_dirty) for the dirty locations, then every location
-// whose hazard-mask bit is set has its agent-list segment expanded over the
-// lanes (a warp scan of the segment lengths, each lane finds its entry's
-// location by a binary search) and each agent draws from its Philox stream
-// (seed, agent, t).  The slot holds the susceptibility product, so an agent
-// that is not infected costs two coalesced loads of its slot.
+// The draw phase.  Warp g takes, 32 at a time (one per lane), the mask words
+// g, g + G, g + 2G, ... (G warps in the grid): words strided over the whole
+// location range, so that the locations of one type, which lie together (and
+// at a time of day are infectious together), spread over all warps.  The dirty
+// locations of its words get their hazards and mask bits first
+// (draw_dirty); then every location whose hazard-mask bit is set has its
+// agent-list segment expanded over the lanes (warp scans of the set bits and
+// of the segment lengths, each lane finding its item by a binary search) and
+// each agent draws from its Philox stream (seed, agent, t).  The slot holds
+// the susceptibility product, so an agent that is not infected costs two
+// coalesced loads of its slot.
 __device__ void phase_draw(const KArgs& k, uint32_t t, double* s_grad, uint32_t* n_entries, uint32_t* n_visited) {
     const uint32_t L = k.l.n, N = k.a.n;
     const float season = k.clock->season;
     const uint32_t dt = k.p.time_step;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
     const uint32_t n_words = (L + 31) >> 5;
-    const uint32_t n_chunks = (n_words + DRAW_WPW - 1) / DRAW_WPW;
     const uint32_t nw = gridDim.x * (blockDim.x >> 5);
+    const uint32_t gw = (threadIdx.x >> 5) * gridDim.x + blockIdx.x;  // neighbouring blocks, neighbouring words
     uint32_t entries = 0, visited = 0;
-    for (uint32_t ch = blockIdx.x * (blockDim.x >> 5) + warp; ch < n_chunks; ch += nw) {
-        const uint32_t w0 = ch * DRAW_WPW;
-        const bool own = lane < DRAW_WPW && w0 + lane < n_words;
-        uint32_t hm = own ? k.l.hmask[w0 + lane] : 0u;
-        const uint32_t sm = own ? k.l.smask[w0 + lane] : 0u;
+    for (uint32_t base = gw; base < n_words; base += 32u * nw) {
+        const uint32_t wid = base + (uint32_t)lane * nw;
+        const bool own = wid < n_words;
+        uint32_t hm = own ? k.l.hmask[wid] : 0u;
+        const uint32_t sm = own ? k.l.smask[wid] : 0u;
         if (!__any_sync(0xffffffffu, (hm | sm) != 0u)) continue;
         if (__any_sync(0xffffffffu, sm != 0u)) {
-            const uint32_t nzw = draw_dirty(k, w0, sm, season, dt);
+            const uint32_t nzw = draw_dirty(k, wid, sm, season, dt);
             if (own && sm) {
                 hm = (hm & ~sm) | nzw;
-                k.l.hmask[w0 + lane] = hm;
-                k.l.smask[w0 + lane] = 0u;
+                k.l.hmask[wid] = hm;
+                k.l.smask[wid] = 0u;
             }
             // the mask stores and hazards above come before this warp's
             // infections mark their locations for the next step
             __syncwarp();
             __threadfence_block();
         }
-        // pass 2: the agents of the locations whose hazard-mask bit is set
         uint32_t inc = __popc(hm);
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -1610,9 +1650,7 @@ __device__ void phase_draw(const KArgs& k, uint32_t t, double* s_grad, uint32_t*
         visited += total;
         for (uint32_t b0 = 0; b0 < total; b0 += 32) {
             const uint32_t r = b0 + lane;
-            uint32_t wo, bit;
-            chunk_bit(r, hm, inc, &wo, &bit);
-            const uint32_t l = (w0 + wo) * 32u + bit;
+            const uint32_t l = set_bit_location(r, hm, wid, inc);
             uint32_t len = 0, beg = 0, rep = 0;
             float h0 = 0.0f;
             if (r < total && l < L) {
@@ -1638,14 +1676,7 @@ __device__ void phase_draw(const KArgs& k, uint32_t t, double* s_grad, uint32_t*
             entries += etotal;
             for (uint32_t e0 = 0; e0 < etotal; e0 += 32) {
                 const uint32_t e = e0 + lane;
-                // owner lane: the number of lanes whose inclusive end is <= e
-                uint32_t q = 0;
-#pragma unroll
-                for (int st = 16; st > 0; st >>= 1) {
-                    const uint32_t v = __shfl_sync(0xffffffffu, einc, (int)(q + st - 1));
-                    if (e >= v) q += st;
-                }
-                q &= 31u;
+                const uint32_t q = owner_lane(e, einc);
                 const uint32_t q_inc = __shfl_sync(0xffffffffu, einc, (int)q);
                 const uint32_t q_len = __shfl_sync(0xffffffffu, len, (int)q);
                 const uint32_t q_beg = __shfl_sync(0xffffffffu, beg, (int)q);
