@@ -1,17 +1,18 @@
 // Hand-written sm_103a kernels of the PanSim per-timestep agent loop.
 //
-// Per step (Simulation::runSimulation, simulation.h:918-922):
-//   k_movement      RealMovementOps::doMovement (movementPolicies.h:263-1041) for every
-//                   agent, fused with the per-location histogram (warp-aggregated
-//                   atomics, the rank of each agent inside its location) and with the
-//                   per-location infectiousness reduction (Util::reduce_by_location,
-//                   util.h:48-101) as exact 2^-40 fixed-point int64 sums.
-//   k_scan          exclusive scan of the histogram into CSR offsets (single pass,
-//                   decoupled look-back), infection ratio of every location
-//                   (infectionPolicies.h:520-546), reset of the per-step counters.
-//   k_scatter_draw  CSR scatter (replaces thrust::stable_sort_by_key, util.cpp:69) fused
-//                   with the per-agent infection draw (LocationsList::infectAgents,
-//                   locationList.h:233-310).
+// The day graph (psim_api.cu): k_movement (RealMovementOps::doMovement,
+// movementPolicies.h:263-1041, for every agent at the day's first step, with
+// the per-location histogram and the per-location infectiousness sums of
+// Util::reduce_by_location, util.h:48-101, as exact 2^-40 fixed-point int64
+// sums), then one k_step per timestep: the agent list rebuilt where agents
+// took new locations (replaces thrust::stable_sort_by_key, util.cpp:69), the
+// infection ratio and draws over the locations with an infectious agent
+// (infectionPolicies.h:520-546, LocationsList::infectAgents,
+// locationList.h:233-310), and the decisions of the agents whose decision
+// step comes next.
+// The per-phase entry points (psim_movement, psim_regroup, psim_infect) use
+// k_movement, the scans (k_scan / k_scan_v: prefix of the histogram, ratio
+// of every dirty location) and k_scatter_draw (slots and agent-ordered draws).
 // Per day: k_progress (DynamicPPState::update), k_test_flag/k_test (DetailedTesting),
 // k_stats (refreshAndPrintStatistics), k_plan_* (RealMovement::planLocations).
 //
