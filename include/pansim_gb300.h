@@ -477,6 +477,14 @@ int psim_stream_handle(psim_ctx* ctx, void** out);
  * does) and leaves the context usable.  Exercises the error path of every
  * bounded wait in the library without faulting the GPU. */
 int psim_bounded_wait_selftest(psim_ctx* ctx, uint32_t iters);
+/* Test hook of the allocation-failure paths (no counterpart in the
+ * reference, which checks allocations only at initialization,
+ * simulation.h:762-765): the next `allowed` device allocations of the
+ * library succeed and the one after fails as if the device were out of
+ * memory (PSIM_ERR_ALLOC); allowed < 0 switches the hook off.  Process-wide.
+ * A context whose creation failed is returned for psim_last_error and frees
+ * everything it took in psim_destroy. */
+int psim_set_alloc_fault(long long allowed);
 
 /* psim_csr_build_noalloc — no counterpart in the reference.
  * For callers that cannot call cudaMalloc (their device memory belongs to

@@ -82,5 +82,18 @@ def build(force=False, verbose=False):
     return LIB
 
 
+def check_adapters():
+    """Compiles (syntax only) oracle/ref_harness/adapter_check.cpp: the
+    reference's own Simulation instantiated with the GB300 policies of
+    include/gb300_policies.h.  Returns (ok, compiler output), or None when
+    the reference tree is absent."""
+    if not available():
+        return None
+    src = os.path.join(HERE, "ref_harness", "adapter_check.cpp")
+    cmd = flags() + ["-I", os.path.join(HERE, "..", "include"), "-fsyntax-only", src]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    return r.returncode == 0, r.stderr[-8000:]
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))

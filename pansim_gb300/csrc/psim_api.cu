@@ -4,6 +4,7 @@
 // cudaDeviceSynchronize after every launch (simulation.h:899-926).
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -33,6 +34,22 @@ int check_device_err(psim_ctx* c) {
     return 0;
 }
 
+// Allocation-failure hook: the device allocations still allowed before one
+// fails (negative: off).  Process-wide, for tests of the error paths.
+static std::atomic<long long> g_alloc_budget{-1};
+
+cudaError_t psim_device_malloc(void** p, size_t bytes) {
+    long long b = g_alloc_budget.load();
+    while (b >= 0) {
+        if (b == 0) {
+            *p = nullptr;
+            return cudaErrorMemoryAllocation;
+        }
+        if (g_alloc_budget.compare_exchange_weak(b, b - 1)) break;
+    }
+    return cudaMalloc(p, bytes);
+}
+
 namespace {
 
 const char* kVersion = "pansim_gb300 0.1.0 (sm_103a)";
@@ -42,7 +59,7 @@ int dalloc(psim_ctx* c, T** p, size_t count) {
     size_t bytes = count * sizeof(T);
     if (bytes == 0) bytes = 16;
     void* q = nullptr;
-    cudaError_t e = cudaMalloc(&q, bytes);
+    cudaError_t e = psim_device_malloc(&q, bytes);
     if (e != cudaSuccess) return fail(c, PSIM_ERR_ALLOC, std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
     cudaMemsetAsync(q, 0, bytes, c->stream);
     c->allocs.push_back(q);
@@ -495,12 +512,6 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     if (e != cudaSuccess) return bail(fail(c, PSIM_ERR_CUDA, std::string("stream: ") + cudaGetErrorString(e)));
     cudaEventCreate(&c->ev0);
     cudaEventCreate(&c->ev1);
-    e = cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->both_ev, cudaEventDisableTiming);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->slots_ev, cudaEventDisableTiming);
-    if (e != cudaSuccess) return bail(fail(c, PSIM_ERR_CUDA, std::string("stream: ") + cudaGetErrorString(e)));
     const size_t N = c->N, L = c->L, V = c->V, R = c->R;
     KArgs& k = c->k;
     // model tables
@@ -723,11 +734,6 @@ int psim_destroy(psim_ctx* c) {
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->pinned) cudaFreeHost(c->pinned);
-    if (c->fork_ev) cudaEventDestroy(c->fork_ev);
-    if (c->join_ev) cudaEventDestroy(c->join_ev);
-    if (c->both_ev) cudaEventDestroy(c->both_ev);
-    if (c->slots_ev) cudaEventDestroy(c->slots_ev);
-    if (c->stream2) cudaStreamDestroy(c->stream2);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return 0;
@@ -912,7 +918,7 @@ int psim_checkpoint_save(psim_ctx* c, uint32_t slot) {
     if (!c || !c->uploaded) return PSIM_ERR_STATE;
     if (!c->checkpoints.count(slot) || !c->checkpoints[slot]) {
         void* p = nullptr;
-        cudaError_t e = cudaMalloc(&p, c->checkpoint_bytes);
+        cudaError_t e = psim_device_malloc(&p, c->checkpoint_bytes);
         if (e != cudaSuccess) return fail(c, PSIM_ERR_ALLOC, std::string("checkpoint: ") + cudaGetErrorString(e));
         c->checkpoints[slot] = p;
     }
@@ -1308,6 +1314,11 @@ int psim_time_step_kernels(psim_ctx* c, uint32_t t, float* ms) {
     rc = launch_check(c);
     if (rc) return rc;
     return check_device_err(c);
+}
+
+int psim_set_alloc_fault(long long allowed) {
+    g_alloc_budget.store(allowed < 0 ? -1 : allowed);
+    return 0;
 }
 
 int psim_bounded_wait_selftest(psim_ctx* c, uint32_t iters) {

@@ -148,7 +148,7 @@ int upload_events(psim_ctx* c) {
     auto put = [&](const void* host, size_t bytes, void** dst) -> int {
         void* d = nullptr;
         const size_t b = bytes ? bytes : 16;
-        cudaError_t e = cudaMalloc(&d, b);
+        cudaError_t e = psim_device_malloc((void**)&d, b);
         if (e != cudaSuccess) return fail(c, PSIM_ERR_ALLOC, std::string("schedule table: ") + cudaGetErrorString(e));
         c->allocs.push_back(d);
         if (bytes) {

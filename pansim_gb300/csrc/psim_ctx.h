@@ -30,10 +30,6 @@ struct psim_ctx {
     psim::OtherDiseaseEngine* other_disease = nullptr;
     int device = 0;
     cudaStream_t stream = nullptr;
-    // the day graph's second branch (the queue kernel beside the rebuild and
-    // the draws) and its fork / join events
-    cudaStream_t stream2 = nullptr;
-    cudaEvent_t fork_ev = nullptr, join_ev = nullptr, both_ev = nullptr, slots_ev = nullptr;
     // Time base of the agents' decision timestamps: the next step that
     // movement will process.  The device keeps move_at (absolute); a host
     // countdown S (stepsUntilMove) is move_at - t_next.
@@ -106,6 +102,10 @@ inline int fail(psim_ctx* c, int code, const std::string& msg) {
 
 // device error flags of the kernels since the last check (psim_api.cu)
 int check_device_err(psim_ctx* c);
+
+// cudaMalloc through the allocation-failure test hook (psim_set_alloc_fault):
+// when the hook's count runs out the allocation fails without calling CUDA
+cudaError_t psim_device_malloc(void** p, size_t bytes);
 
 // non-COVID hospitalization and death (psim_other_disease.cu)
 void other_disease_free(psim_ctx* c);

@@ -337,7 +337,7 @@ int psim_immunization_init(psim_ctx* c, const psim_immunization* imm) {
                          imm->protection_symptomatic, imm->protection_symptomatic_waning,
                          imm->protection_hospitalization, imm->protection_hospitalization_waning,
                          imm->variant_similarity, imm->variant_similar_multiplier);
-    cudaError_t e = cudaMalloc(&E->d_counts, sizeof(uint32_t) * 16);
+    cudaError_t e = psim_device_malloc((void**)&E->d_counts, sizeof(uint32_t) * 16);
     if (e != cudaSuccess) {
         delete E;
         return fail(c, PSIM_ERR_ALLOC, std::string("immunization: ") + cudaGetErrorString(e));

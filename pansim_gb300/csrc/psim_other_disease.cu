@@ -142,8 +142,8 @@ int psim_other_disease_init(psim_ctx* c, const psim_other_disease* od) {
     OtherDiseaseEngine* E = new OtherDiseaseEngine();
     E->due_with_covid = od->due_with_covid;
     E->targets.assign(od->total_hospitalizations, od->total_hospitalizations + od->n_targets);
-    if (cudaMalloc(&E->d_counts, sizeof(uint32_t) * c->R) != cudaSuccess ||
-        cudaMalloc(&E->d_mul, sizeof(float) * c->R) != cudaSuccess) {
+    if (psim_device_malloc((void**)&E->d_counts, sizeof(uint32_t) * c->R) != cudaSuccess ||
+        psim_device_malloc((void**)&E->d_mul, sizeof(float) * c->R) != cudaSuccess) {
         if (E->d_counts) cudaFree(E->d_counts);
         delete E;
         return fail(c, PSIM_ERR_ALLOC, "other disease: cudaMalloc failed");

@@ -70,6 +70,7 @@ def lib(auto_build=True):
         L.psim_get_events.argtypes = [P, P, P, P, P, P, P, U32, P]
         L.psim_day_kernel_ms.argtypes = [P, C.c_void_p]
         L.psim_day_counts.argtypes = [P, C.c_void_p]
+        L.psim_set_alloc_fault.argtypes = [C.c_longlong]
         L.psim_launch_count.argtypes = [P, C.POINTER(C.c_uint64)]
         L.psim_stream_handle.argtypes = [P, C.POINTER(P)]
         L.psim_bounded_wait_selftest.argtypes = [P, U32]

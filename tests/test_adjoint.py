@@ -4,7 +4,8 @@ The GPU gradient (checkpoint replay, FP64 accumulation in the draw kernels)
 is checked against an FP64 torch autograd evaluation of the same expected
 curve along the same sampled trajectory (recorded with the oracle), and
 against central finite differences (h = 1e-3 relative) of that FP64
-function: within 1e-4 relative.
+function: within 1e-4 relative per component, with an absolute floor of 1e-9
+of the largest component for components that are zero.
 """
 import math
 
@@ -84,8 +85,15 @@ def test_adjoint_matches_fp64_autograd_and_finite_differences(gpu_lib):
     L.backward()
     g_ref = th.grad.numpy()
     g_gpu = runner.backward((2.0 * (E_gpu - target.numpy()))[None, :])
+    # per component: within 1e-4 relative of the FP64 reference, with an
+    # absolute floor of 1e-9 of the largest component for components that
+    # are (nearly) zero; those are named
     scale = np.abs(g_ref).max()
-    assert np.abs(g_gpu - g_ref).max() <= 1e-4 * scale, (g_gpu, g_ref)
+    floor = 1e-9 * scale
+    tol = 1e-4 * np.abs(g_ref) + floor
+    assert (np.abs(g_gpu - g_ref) <= tol).all(), (g_gpu, g_ref)
+    below = [j for j in range(len(g_ref)) if abs(g_ref[j]) < 1e-4 * scale]
+    assert len(below) <= 2, below  # at most the sparsest age bands
 
     def loss(theta):
         with torch.no_grad():
@@ -99,7 +107,7 @@ def test_adjoint_matches_fp64_autograd_and_finite_differences(gpu_lib):
         tp[j] += h
         tm[j] -= h
         fd[j] = (loss(tp) - loss(tm)) / (2 * h)
-    assert np.abs(g_gpu - fd).max() <= 1e-4 * scale, (g_gpu, fd)
+    assert (np.abs(g_gpu - fd) <= 1e-4 * np.abs(fd) + floor).all(), (g_gpu, fd)
 
 
 def test_autograd_function_and_replica_sum(gpu_lib):
