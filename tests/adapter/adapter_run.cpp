@@ -83,6 +83,11 @@ public:
     unsigned timeStep;
     pansim_gb300::Bridge scratch;   // the oracle's copy for updateAgents
     psim_oracle* oracle = nullptr;
+    // the one replica of the oracle's copy
+    uint32_t rep_agents[2] = {0, 0}, rep_locs[2] = {0, 0}, rep_cemetery = 0;
+    uint64_t rep_seed = 0;
+    double rep_k = 0.0;
+    psim_replicas reps{};
 
     StandInSim(AgentsStandIn* a, LocsStandIn* l, unsigned dt) : agents(a), locs(l), timeStep(dt) {}
     ~StandInSim() {
@@ -96,7 +101,19 @@ public:
         if (!oracle) {
             scratch.gather(this, true);
             scratch.bind();
-            oracle = psim_oracle_create(pansim_gb300::model_slot(), &scratch.a, &scratch.l, p, nullptr);
+            rep_agents[1] = scratch.N;
+            rep_locs[1] = scratch.L;
+            rep_cemetery = p->cemetery_loc;
+            rep_seed = p->seed;
+            rep_k = p->k;
+            reps.n = 1;
+            reps.agent_offset = rep_agents;
+            reps.loc_offset = rep_locs;
+            reps.seed = &rep_seed;
+            reps.k = &rep_k;
+            reps.cemetery = &rep_cemetery;
+            oracle = psim_oracle_create(pansim_gb300::model_slot(), &scratch.a, &scratch.l, p, &reps);
+            if (!oracle) throw pansim_gb300::Error("psim_oracle_create failed");
         }
         scratch.gather(this, false);
         psim_oracle_progress(oracle, t);
