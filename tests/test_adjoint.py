@@ -87,13 +87,13 @@ def test_adjoint_matches_fp64_autograd_and_finite_differences(gpu_lib):
     g_gpu = runner.backward((2.0 * (E_gpu - target.numpy()))[None, :])
     # per component: within 1e-4 relative of the FP64 reference, with an
     # absolute floor of 1e-9 of the largest component for components that
-    # are (nearly) zero; those are named
+    # are zero (the parameters differ in scale by orders of magnitude, so a
+    # bound relative to the largest component would not test the others)
     scale = np.abs(g_ref).max()
     floor = 1e-9 * scale
     tol = 1e-4 * np.abs(g_ref) + floor
     assert (np.abs(g_gpu - g_ref) <= tol).all(), (g_gpu, g_ref)
-    below = [j for j in range(len(g_ref)) if abs(g_ref[j]) < 1e-4 * scale]
-    assert len(below) <= 2, below  # at most the sparsest age bands
+    assert (np.abs(g_ref) > floor).sum() >= 12  # k, the weights and the populated bands
 
     def loss(theta):
         with torch.no_grad():
