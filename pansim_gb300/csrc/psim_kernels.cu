@@ -1228,32 +1228,44 @@ __global__ void __launch_bounds__(256) k_scatter_draw(KArgs k, uint32_t step, in
 // wait is bounded: on expiry the block records ERR_BARRIER and returns false,
 // and every later barrier and step kernel returns at once, so a failure ends
 // in an error report, never a hang.
+// The block's writes reach the other blocks through the arrival (release:
+// the block's threads' writes are ordered before it by the __syncthreads
+// before) and the generation read (acquire).
 constexpr uint32_t BARRIER_SPIN_LIMIT = 1u << 24;
+__device__ __forceinline__ uint32_t ld_acquire_gpu(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ uint32_t atom_add_acq_rel_gpu(uint32_t* p, uint32_t x) {
+    uint32_t old;
+    asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(x) : "memory");
+    return old;
+}
+__device__ __forceinline__ void st_relaxed_gpu(uint32_t* p, uint32_t x) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(x) : "memory");
+}
 __device__ __forceinline__ bool grid_barrier(const KArgs& k, bool* s_ok) {
     __syncthreads();
     if (threadIdx.x == 0) {
-        bool ok = (*((volatile uint32_t*)k.err) & ERR_BARRIER) == 0;
+        bool ok = (ld_acquire_gpu(k.err) & ERR_BARRIER) == 0;
         if (ok) {
-            volatile uint32_t* gen_p = (volatile uint32_t*)&k.l.bar[1];
-            const uint32_t gen = *gen_p;
-            __threadfence();
-            const uint32_t arrived = atomicAdd(&k.l.bar[0], 1u) + 1u;
+            const uint32_t gen = ld_acquire_gpu(&k.l.bar[1]);
+            const uint32_t arrived = atom_add_acq_rel_gpu(&k.l.bar[0], 1u) + 1u;
             if (arrived == gridDim.x) {
-                k.l.bar[0] = 0u;
-                __threadfence();
-                atomicAdd(&k.l.bar[1], 1u);
+                st_relaxed_gpu(&k.l.bar[0], 0u);
+                atom_add_acq_rel_gpu(&k.l.bar[1], 1u);
             } else {
                 uint32_t spins = 0;
-                while (*gen_p == gen) {
+                while (ld_acquire_gpu(&k.l.bar[1]) == gen) {
                     if (++spins > BARRIER_SPIN_LIMIT) {
                         atomicOr(k.err, ERR_BARRIER);
                         ok = false;
                         break;
                     }
-                    __nanosleep(64);
+                    __nanosleep(32);
                 }
             }
-            __threadfence();
         }
         *s_ok = ok;
     }
@@ -1377,19 +1389,34 @@ __device__ bool phase_rebuild(const KArgs& k, uint32_t* s_red, bool* s_ok) {
             if (ok) slot_fill(k, pos, i);
         }
     } else {
+        // one variant (the common case): the slot's product is computed
+        // before the returning atomic, whose latency then covers the loads
+        const bool one = k.m.n_variants == 1;
         const uint32_t tile = blockDim.x * SLOT_ILP;
         for (uint32_t base = blockIdx.x * tile; base < N; base += gridDim.x * tile) {
             uint32_t loc[SLOT_ILP], pos[SLOT_ILP];
+            float su[SLOT_ILP];
 #pragma unroll
             for (int u = 0; u < SLOT_ILP; ++u) {
                 const uint32_t i = base + u * blockDim.x + threadIdx.x;
                 loc[u] = i < N ? k.a.location[i] : NONE;
+                su[u] = (one && i < N) ? k.a.susceptible[i] * k.p.sigma_band[k.a.band[i]] : 0.0f;
             }
 #pragma unroll
             for (int u = 0; u < SLOT_ILP; ++u) pos[u] = loc[u] < L ? atomicAdd(&k.l.cursor[loc[u]], 1u) : NONE;
 #pragma unroll
-            for (int u = 0; u < SLOT_ILP; ++u)
-                if (loc[u] < L) slot_fill(k, pos[u], base + u * blockDim.x + threadIdx.x);
+            for (int u = 0; u < SLOT_ILP; ++u) {
+                if (loc[u] >= L) continue;
+                const uint32_t i = base + u * blockDim.x + threadIdx.x;
+                if (!one) {
+                    slot_fill(k, pos[u], i);
+                } else if (pos[u] < N) {
+                    k.l.csr_agents[pos[u]] = i;
+                    k.l.slot_su[pos[u]] = su[u];
+                } else {
+                    atomicOr(k.err, ERR_LOCATION);
+                }
+            }
         }
     }
     return grid_barrier(k, s_ok);
