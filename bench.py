@@ -41,11 +41,13 @@ STEP_BYTES = (32, 20)
 def kernel_bytes(N, L, V, spd, counts):
     """Algorithmic bytes per simulated day of each phase of the step kernel,
     from the profiled day's counters (entries E, visited locations H, queued
-    agents M, queue passes Q, rebuilds R):
-      rebuild   per rebuild the histogram read twice and the first slots
-                written (12 L), and per agent its location, age band and
-                susceptibilities read, its slot's atomic, id and
-                susceptibility products written (17 + 8 V)
+    agents M, queue passes Q, rebuilds R, listed locations LL and agents LA,
+    summed over the rebuilds):
+      rebuild   per rebuild the hazard mask read twice (L / 4) and every
+                agent's location (4 N); per listed location its count read
+                twice, its first slot and epoch written (16); per listed
+                agent its age band and susceptibilities read, its slot's
+                atomic, id and susceptibility products written (13 + 8 V)
       draw      per step the two mask words per 32 locations (L/4); at the
                 day's first step every location's sums, count, weight and
                 replica read and its hazard written (22 L); per visited
@@ -58,13 +60,32 @@ def kernel_bytes(N, L, V, spd, counts):
                 location's flags (5), the location and timestamp written (8),
                 the histogram deltas (8)
     """
-    E, H, M, Q, R = (float(x) for x in counts)
-    return {"rebuild": R * (12.0 * L + (17 + 8 * V) * N),
+    E, H, M, Q, R, LL, LA = (float(x) for x in counts)
+    return {"rebuild": R * (L / 4.0 + 4.0 * N) + 16.0 * LL + (13 + 8 * V) * LA,
             "draw": spd * L / 4.0 + 22.0 * L + 14.0 * H + (4 + 4 * V) * E,
             "decide": 4.0 * N * Q + 76.0 * M}
 
 
 KERNEL_LABELS = {"rebuild": "k_step rebuild phase", "draw": "k_step draw phase", "decide": "k_step queue + decide phase"}
+
+
+def step_kinds(tl):
+    """The profiled day's steps by kind (tl: per step the kernel span, the
+    rebuild's totals, prefix and slots, the draws, the queue, the decisions,
+    the time since the previous kernel, us): count and mean span, gap and
+    phase times of the draw-only steps, the steps with a rebuild and no
+    decisions, with decisions and no rebuild, with both."""
+    reb, dec = tl[:, 1:4].sum(axis=1) > 0, tl[:, 6] > 0
+    out = {}
+    cols = ["span_us", "rebuild_totals_us", "rebuild_prefix_us", "rebuild_slots_us", "draw_us", "queue_us",
+            "decide_us", "gap_us"]
+    for name, sel in [("draw_only", ~reb & ~dec), ("rebuild", reb & ~dec), ("decide", ~reb & dec),
+                      ("rebuild_and_decide", reb & dec)]:
+        n = int(sel.sum())
+        out[name] = {"steps": n}
+        for j, c in enumerate(cols):
+            out[name][c] = float(tl[sel, j].mean()) if n else None
+    return out
 
 
 def dist_env():
@@ -522,17 +543,17 @@ def main():
     clocks = sampler.stop()
     spd = snap.steps_per_day
     t_max, value = whole_job(total_ms, snap.n_agents, spd, args.steps, ws, dist, "cuda")
-    # per-kernel durations (roofline): the same days again with event-record
-    # nodes around every kernel group of the day graph, on the library's
-    # stream, and the day's counters (entries drawn, decisions, rebuilds).
-    # The nodes serialise the graph and add gaps, so this pass is kept out of
-    # the timed region above.
+    # per-phase durations (roofline): the same days again with the kernels'
+    # timeline stamps (global timer at every block's entry, phase ends and
+    # exit, one atomic per block and stamp) and the day's counters (entries
+    # drawn, decisions, rebuilds).  Kept out of the timed region above.
     g.set_profiling(True)
     g.run_day(day)  # captures the profiled graph
     day += 1
     n_prof = min(args.steps, 10)
     kms_sum = np.zeros(5)
-    cnt_sum = np.zeros(5)
+    cnt_sum = np.zeros(7)
+    tl_sum = None
     prof_day_ms = 0.0
     for _ in range(n_prof):
         flush.fill_(1.0)
@@ -540,6 +561,8 @@ def main():
         g.run_day(day)
         kms_sum += g.day_kernel_ms()
         cnt_sum += g.day_counts().astype(np.float64)
+        tl = g.day_timeline().astype(np.float64)
+        tl_sum = tl if tl_sum is None else tl_sum + tl
         prof_day_ms += g.last_day_ms()
         day += 1
     g.set_profiling(False)
@@ -575,7 +598,7 @@ def main():
         V = int(snap.model["n_variants"])
         counts = cnt_sum / n_prof
         kb = kernel_bytes(N, L, V, spd, counts)
-        kms_day = kms_sum / n_prof  # per simulated day: movement(0), rebuild, draw, queue + decide, 0
+        kms_day = kms_sum / n_prof  # per simulated day: movement(0), rebuild, draw, queue + decide, between kernels
         launches_per_day = {"rebuild": max(counts[4], 1.0), "draw": float(spd), "decide": max(counts[3], 1.0)}
         kern = {"movement": {"ms_per_day": float(kms_day[0])}}
         for j, name in enumerate(["rebuild", "draw", "decide"]):
@@ -584,9 +607,11 @@ def main():
                           "launches_with_work_per_day": launches_per_day[name],
                           "gbs": kb[name] / (ms * 1e-3) / 1e9 if ms > 0 else None,
                           "frac": kb[name] / (ms * 1e-3) / 1e9 / peak if ms > 0 else None}
+        kern["between_kernels"] = {"ms_per_day": float(kms_day[4])}
         tot_k = sum(kern[n]["ms_per_day"] for n in KERNEL_LABELS) or 1.0
         for name in KERNEL_LABELS:
             kern[name]["share_of_steps"] = kern[name]["ms_per_day"] / tot_k
+        steps_by_kind = step_kinds(tl_sum / n_prof)
         # The step kernel (one launch per timestep, its phases fused with
         # grid barriers) is the kernel of the day graph: its algorithmic
         # bytes per launch are the phases' bytes of a day over the day's
@@ -601,7 +626,8 @@ def main():
         # average timestep time
         step_bytes = STEP_BYTES[0] * N + STEP_BYTES[1] * L
         counts_d = {"draw_entries": counts[0], "draw_locations": counts[1], "decisions": counts[2],
-                    "queue_passes": counts[3], "rebuilds": counts[4]}
+                    "queue_passes": counts[3], "rebuilds": counts[4], "listed_locations": counts[5],
+                    "listed_agents": counts[6]}
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -613,15 +639,15 @@ def main():
                          "launch_ms_source": "day-graph CUDA events over the timed days, less the first movement "
                                              "pass, over their timesteps",
                          "dominant": "k_step", "dominant_phase": max(KERNEL_LABELS, key=lambda n: kern[n]["ms_per_day"]),
-                         "per_phase": kern, "day_counts": counts_d,
+                         "per_phase": kern, "day_counts": counts_d, "steps_by_kind": steps_by_kind,
                          "step_rate": {"reference_bytes_per_timestep": step_bytes, "timestep_ms": step_ms,
                                        "gbs": step_bytes / (step_ms * 1e-3) / 1e9,
                                        "frac": step_bytes / (step_ms * 1e-3) / 1e9 / peak,
                                        "note": "the reference's step bytes (32 N + 20 L) over our timestep "
                                                "time: a rate, not a bandwidth"}},
             "clocks": clocks, "gpu_launches": int(launches), "e2e": e2e,
-            "kernel_timing": {"days": n_prof, "graph_ms_per_day_with_event_nodes": prof_day_ms / n_prof,
-                              "note": "per-kernel durations from event-record nodes in a separate pass"},
+            "kernel_timing": {"days": n_prof, "graph_ms_per_day_with_stamps": prof_day_ms / n_prof,
+                              "note": "per-phase durations from the kernels' timeline stamps in a separate pass"},
             "tuning": {"best": best, "candidates": len(table),
                        "worst_step_ms": max(x[1] for x in table), "best_step_ms": min(x[1] for x in table)},
         }

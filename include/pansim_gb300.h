@@ -441,9 +441,11 @@ int psim_checkpoint_bytes(psim_ctx* ctx, uint64_t* out);
  * susceptible agents, reported in psim_day_stats) during the steps. */
 int psim_set_tracking(psim_ctx* ctx, int expected);
 
-/* Location CSR (LocationsList::locationListOffsets / locationAgentList).
- * With canonical != 0 each location's agents are sorted by id, which equals
- * thrust::stable_sort_by_key's output (util.cpp:69). */
+/* Location CSR (LocationsList::locationListOffsets / locationAgentList) of
+ * the current positions.  With canonical != 0 each location's agents are
+ * sorted by id, which equals thrust::stable_sort_by_key's output
+ * (util.cpp:69).  After day graphs (whose step kernel keeps agent lists only
+ * for the locations its draws visit) the full list is built first. */
 int psim_get_csr(psim_ctx* ctx, int canonical, uint32_t* offsets /*[L+1]*/, uint32_t* agents /*[N]*/);
 /* Per-location hazard r_l of the last psim_infect call (infectionRatios). */
 int psim_get_hazard(psim_ctx* ctx, float* out /*[L]*/, int64_t* fixed_sum /*[L] or NULL*/);
@@ -456,18 +458,26 @@ int psim_get_hazard(psim_ctx* ctx, float* out /*[L]*/, int64_t* fixed_sum /*[L] 
 int psim_time_step_kernels(psim_ctx* ctx, uint32_t t, float* ms /* [3] */);
 /* Timing of the last psim_run_steps graph launch, milliseconds. */
 int psim_last_day_ms(psim_ctx* ctx, float* ms);
-/* With on != 0 the day graph is captured with the step kernel's three phases
- * as separate launches and an event-record node after each; psim_day_kernel_ms
- * then gives, for the last psim_run_steps, the summed durations ms[5] =
- * {movement of step 0, the rebuilds (histogram prefix + agent-list slots) of
- * all steps, the draws, the queues + decisions, 0}, and psim_day_counts
- * out[5] = {agent-list entries the draws expanded, locations with a set
- * hazard-mask bit they visited, agents queued for a decision, steps at which
- * agents were queued, steps that rebuilt the agent list}, summed over the
- * day's steps. */
+/* With on != 0 the day graph is captured with timeline stamps in its kernels
+ * (the global nanosecond timer at every block's entry, at the end of each
+ * phase of the step kernel and at its exit; one atomic per block and stamp)
+ * and counters.  For the last psim_run_steps: psim_day_kernel_ms gives ms[5]
+ * = {the day's first movement kernel, the step kernel's rebuilds (histogram
+ * prefix + agent-list slots), its draws, its queues + decisions, and the time
+ * between the kernels}, summed over the day; psim_day_timeline gives per step
+ * s, at us[8*s .. 8*s+7], {the kernel's span from its first block's entry to
+ * its last block's exit, the rebuild's totals, its prefix and cursors, its
+ * slots, the draws, the queue, the decisions (0 when the phase did not run),
+ * the time since the previous kernel's last exit}, microseconds;
+ * psim_day_counts gives out[7] = {agent-list entries the draws expanded,
+ * locations with a set hazard-mask bit they visited, agents queued for a
+ * decision, steps at which agents were queued, steps that rebuilt the agent
+ * list, locations and agents those rebuilds listed}, summed over the day's
+ * steps. */
 int psim_set_profiling(psim_ctx* ctx, int on);
 int psim_day_kernel_ms(psim_ctx* ctx, float* ms /* [5] */);
-int psim_day_counts(psim_ctx* ctx, uint64_t* out /* [5] */);
+int psim_day_timeline(psim_ctx* ctx, float* us /* [8 * steps_per_day] */);
+int psim_day_counts(psim_ctx* ctx, uint64_t* out /* [7] */);
 /* Counts of kernel launches issued by the library since creation. */
 int psim_launch_count(psim_ctx* ctx, uint64_t* out);
 /* The context's cudaStream_t (as void*), for callers that order their own work after it. */

@@ -297,6 +297,7 @@ int initial_regroup(psim_ctx* c) {
     launch_count(c->k, c->stream);
     launch_scan(c->k, 0, 1, 0, c->stream);
     launch_scatter_draw(c->k, 0, 1, 0, c->stream);
+    c->list_sparse = false;
     // the variant gating of the first steps (the statistics come at midnight)
     launch_variant_flags(c->k, c->stream);
     c->launches += 3 + (uint64_t)scan_kernels(c->k);
@@ -316,6 +317,7 @@ int do_step(psim_ctx* c, uint32_t step, bool draw, bool movement) {
     launch_scan(c->k, step, 1, merge_q, c->stream);
     launch_scatter_draw(c->k, step, 1, draw ? 1 : 0, c->stream);
     c->launches += (movement ? 2 : 1) + (uint64_t)scan_kernels(c->k);
+    c->list_sparse = false;
     return launch_check(c);
 }
 
@@ -325,21 +327,9 @@ int capture_day_graph(psim_ctx* c) {
         c->day_graph = nullptr;
     }
     cudaGraph_t g = nullptr;
-    // 3 * spd + 2 events: [0] before movement(0), [1] after it, then per step
-    // one after the rebuild, the draws and the queue + decisions
-    const size_t n_ev = c->profile ? 3ull * c->spd + 2 : 0;
-    while (c->prof_ev.size() < n_ev) {
-        cudaEvent_t ev = nullptr;
-        CK(cudaEventCreate(&ev));
-        c->prof_ev.push_back(ev);
-    }
+    // profiled: the step kernel's counters and timeline stamps (KArgs::prof)
     c->k.prof = c->profile ? c->d_prof : nullptr;
-    size_t ev_i = 0;
-    auto mark = [&]() {
-        if (c->profile) cudaEventRecordWithFlags(c->prof_ev[ev_i++], c->stream, cudaEventRecordExternal);
-    };
     CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    mark();
     // (the capture stays open until EndCapture: errors are checked after it)
     // The day's first step: the sums afresh (every location dirty), the
     // agent list rebuilt (its slots take the susceptibilities the midnight
@@ -349,25 +339,13 @@ int capture_day_graph(psim_ctx* c) {
         me = cudaMemsetAsync(c->k.l.smask, 0xFF, sizeof(uint32_t) * (((size_t)c->L + 2047) / 2048 * 64 + 64), c->stream);
     if (me == cudaSuccess) me = cudaMemsetAsync(c->k.a.move_mask, 0, sizeof(uint32_t) * MOVE_MASK_WORDS, c->stream);
     if (me == cudaSuccess) me = cudaMemsetAsync(c->k.l.build + 1, 0xFF, sizeof(uint32_t), c->stream);
-    if (me == cudaSuccess && c->profile) me = cudaMemsetAsync(c->d_prof, 0, sizeof(unsigned long long) * PROF_N, c->stream);
-    launch_movement(c->k, 0, c->stream);
-    mark();
-    // Per step: one launch of the step kernel (rebuild, draws, decisions for
-    // the next step, with grid barriers inside).  The profiled graph
-    // launches the three phases separately with an event after each.
     if (me == cudaSuccess) me = cudaMemsetAsync(c->k.l.bar, 0, sizeof(uint32_t) * BAR_WORDS, c->stream);
-    for (uint32_t s = 0; s < c->spd; ++s) {
-        if (!c->profile) {
-            launch_step(c->k, s, PH_ALL, c->stream);
-            continue;
-        }
-        launch_step(c->k, s, PH_REBUILD, c->stream);
-        mark();
-        launch_step(c->k, s, PH_DRAW, c->stream);
-        mark();
-        launch_step(c->k, s, PH_DECIDE, c->stream);
-        mark();
-    }
+    if (me == cudaSuccess && c->profile) me = cudaMemsetAsync(c->d_prof, 0, sizeof(unsigned long long) * PROF_WORDS, c->stream);
+    launch_movement(c->k, 0, c->stream);
+    // Per step: one launch of the step kernel (rebuild, draws, decisions for
+    // the next step, with grid barriers inside); the profiled graph is the
+    // same launches with the kernels' timeline stamps.
+    for (uint32_t s = 0; s < c->spd; ++s) launch_step(c->k, s, PH_ALL, c->stream);
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     if (e == cudaSuccess && me != cudaSuccess) {
         cudaGraphDestroy(g);
@@ -377,8 +355,8 @@ int capture_day_graph(psim_ctx* c) {
     e = cudaGraphInstantiate(&c->day_graph, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(c, PSIM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
-    // movement(0) and one step kernel per step (three when profiled)
-    c->graph_kernels = 1 + (c->profile ? 3ull : 1ull) * c->spd;
+    // movement(0) and one step kernel per step
+    c->graph_kernels = 1 + (uint64_t)c->spd;
     c->graph_dirty = false;
     c->prof_valid = false;
     return 0;
@@ -561,6 +539,11 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     UPA(type, N) UPA(age, N) UPA(band, N) UPA(prog_id, N) UPA(symptom_scaling, N) UPA(loc_offset, N + 1)
     UPA(poss_loc, c->n_poss) UPA(poss_type, c->n_poss)
 #undef UPA
+    {
+        std::vector<uint2> packed(c->n_poss);
+        for (size_t j = 0; j < c->n_poss; ++j) packed[j] = make_uint2(a->poss_loc[j], a->poss_type[j]);
+        if ((rc = dupload(c, &da.poss, packed.data(), c->n_poss))) return bail(rc);
+    }
     if (a->precond) {
         if ((rc = dupload(c, &da.precond, a->precond, N))) return bail(rc);
     } else {
@@ -593,7 +576,7 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
 #define AL(field, cnt) \
     if ((rc = dalloc(c, &da.field, cnt))) return bail(rc);
     AL(hcw, N) AL(rank, N) AL(home, N)
-    AL(worklist, (size_t)N + (size_t)WORK_MAX_BLOCKS * 256) AL(seg_count, WORK_MAX_BLOCKS)
+    AL(worklist, (size_t)N + (size_t)WORK_MAX_BLOCKS * 1024 + 4) AL(seg_count, WORK_MAX_BLOCKS)
     AL(move_mask, MOVE_MASK_WORDS)
 #undef AL
     // locations
@@ -611,6 +594,7 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     if ((rc = dalloc(c, &dl.csr_off, L + 1))) return bail(rc);
     if ((rc = dalloc(c, &dl.cursor, L))) return bail(rc);
     if ((rc = dalloc(c, &dl.csr_agents, N))) return bail(rc);
+    if ((rc = dalloc(c, &dl.list_at, L))) return bail(rc);
     if ((rc = dalloc(c, &dl.slot_su, N * V))) return bail(rc);
     if ((rc = dalloc(c, &dl.qu_pending, L))) return bail(rc);
     if ((rc = dalloc(c, &dl.sfix, L * V))) return bail(rc);
@@ -626,7 +610,7 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     if ((rc = dalloc(c, &dl.scan_status, tiles))) return bail(rc);
     if ((rc = dalloc(c, &dl.scan_state, 2))) return bail(rc);
     if ((rc = dalloc(c, &dl.build, 8))) return bail(rc);
-    if ((rc = dalloc(c, &c->d_prof, PROF_N))) return bail(rc);
+    if ((rc = dalloc(c, &c->d_prof, PROF_WORDS))) return bail(rc);
     // replicas
     DevReps& dr = k.r;
     dr.n = c->R;
@@ -729,7 +713,6 @@ int psim_destroy(psim_ctx* c) {
     for (auto& kv : c->checkpoints)
         if (kv.second) cudaFree(kv.second);
     if (c->day_graph) cudaGraphExecDestroy(c->day_graph);
-    for (cudaEvent_t ev : c->prof_ev) cudaEventDestroy(ev);
     for (void* p : c->allocs) cudaFree(p);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
@@ -1010,6 +993,7 @@ int psim_regroup(psim_ctx* c) {
     launch_scatter_draw(c->k, 0, 1, 0, c->stream);
     c->launches += 1 + (uint64_t)scan_kernels(c->k);
     c->csr_fresh = false;
+    c->list_sparse = false;
     int rc = launch_check(c);
     if (rc) return rc;
     return check_device_err(c);
@@ -1135,6 +1119,7 @@ int psim_run_steps(psim_ctx* c, uint32_t day) {
     c->launches += c->graph_kernels;
     c->prof_valid = c->profile;
     c->csr_fresh = false;
+    c->list_sparse = true;
     c->t_next = (day + 1) * c->spd;
     return check_device_err(c);
 }
@@ -1184,6 +1169,7 @@ int psim_run_day(psim_ctx* c, uint32_t day, psim_day_stats* out) {
     c->launches += c->graph_kernels;
     c->prof_valid = c->profile;
     c->csr_fresh = false;
+    c->list_sparse = true;
     c->t_next = (day + 1) * c->spd;
     if (*c->h_err_pin) return check_device_err(c);
     if (out) assemble_stats(c, t, out);
@@ -1192,6 +1178,18 @@ int psim_run_day(psim_ctx* c, uint32_t day, psim_day_stats* out) {
 
 int psim_get_csr(psim_ctx* c, int canonical, uint32_t* offsets, uint32_t* agents) {
     if (!c || !c->uploaded) return PSIM_ERR_STATE;
+    if (c->list_sparse) {
+        // the step kernel lists only the locations its draws visit: the full
+        // agent list of the current positions (prefix of the histogram,
+        // slots), which no later step reads (the day graph's and the step
+        // kernel's first step rebuild)
+        int rc = force_rebuild(c);
+        if (rc) return rc;
+        launch_scan(c->k, 0, 0, 0, c->stream);
+        launch_scatter_draw(c->k, 0, 1, 0, c->stream);
+        c->launches += 1 + (uint64_t)scan_kernels(c->k);
+        c->list_sparse = false;
+    }
     launch_offsets(c->k, c->stream);
     c->launches += 1;
     if (canonical) {
@@ -1237,20 +1235,61 @@ int psim_set_profiling(psim_ctx* c, int on) {
     return 0;
 }
 
+// the profiled day's timeline, copied back (stamps in ns; first entries
+// stored as complements, see PROF_T)
+static int read_timeline(psim_ctx* c, std::vector<unsigned long long>& h) {
+    if (!c->prof_valid) return fail(c, PSIM_ERR_STATE, "no profiled day: psim_set_profiling(1), then psim_run_steps");
+    h.assign(PROF_WORDS, 0ull);
+    CK(cudaMemcpyAsync(h.data(), c->d_prof, sizeof(unsigned long long) * PROF_WORDS, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+// Per step of the profiled day, in microseconds (TL_COLS values): the
+// kernel's span (first block entry to last block exit), the rebuild's
+// totals, its prefix and cursors, its slots, the draws, the queue, the
+// decisions (0 where the phase did not run), and the time from the previous
+// kernel's last exit to this kernel's first entry.
+constexpr int TL_COLS = 8;
+static void step_times(psim_ctx* c, const std::vector<unsigned long long>& h, uint32_t s, float* o) {
+    const unsigned long long* T = &h[PROF_T + PROF_TW * (size_t)s];
+    const unsigned long long t0 = ~T[0], r1 = T[1], r2 = T[2], r3 = T[3], drw = T[4], que = T[5], end = T[6];
+    const unsigned long long prev = s == 0 ? h[PROF_N + 1] : h[PROF_T + PROF_TW * (size_t)(s - 1) + 6];
+    auto us = [](unsigned long long a, unsigned long long b) { return b > a ? (float)((double)(b - a) * 1e-3) : 0.0f; };
+    o[0] = us(t0, end);
+    o[1] = r1 ? us(t0, r1) : 0.0f;
+    o[2] = r2 ? us(r1, r2) : 0.0f;
+    o[3] = r3 ? us(r2, r3) : 0.0f;
+    o[4] = us(r3 ? r3 : t0, drw);
+    o[5] = que ? us(drw, que) : 0.0f;
+    o[6] = que ? us(que, end) : 0.0f;
+    o[7] = us(prev, t0);
+}
+
 int psim_day_kernel_ms(psim_ctx* c, float* ms) {
     if (!c || !ms) return PSIM_ERR_ARG;
-    if (!c->prof_valid) return fail(c, PSIM_ERR_STATE, "no profiled day: psim_set_profiling(1), then psim_run_steps");
-    float t = 0.f;
-    CK(cudaEventElapsedTime(&t, c->prof_ev[0], c->prof_ev[1]));
-    ms[0] = t;
+    std::vector<unsigned long long> h;
+    int rc = read_timeline(c, h);
+    if (rc) return rc;
+    ms[0] = h[PROF_N + 1] > ~h[PROF_N] ? (float)((double)(h[PROF_N + 1] - ~h[PROF_N]) * 1e-6) : 0.0f;
     ms[1] = ms[2] = ms[3] = ms[4] = 0.f;
     for (uint32_t s = 0; s < c->spd; ++s) {
-        const size_t e = 1 + 3 * (size_t)s;
-        for (int j = 0; j < 3; ++j) {
-            CK(cudaEventElapsedTime(&t, c->prof_ev[e + j], c->prof_ev[e + j + 1]));
-            ms[1 + j] += t;
-        }
+        float o[TL_COLS];
+        step_times(c, h, s, o);
+        ms[1] += (o[1] + o[2] + o[3]) * 1e-3f;
+        ms[2] += o[4] * 1e-3f;
+        ms[3] += (o[5] + o[6]) * 1e-3f;
+        ms[4] += o[7] * 1e-3f;
     }
+    return 0;
+}
+
+int psim_day_timeline(psim_ctx* c, float* us) {
+    if (!c || !us) return PSIM_ERR_ARG;
+    std::vector<unsigned long long> h;
+    int rc = read_timeline(c, h);
+    if (rc) return rc;
+    for (uint32_t s = 0; s < c->spd; ++s) step_times(c, h, s, us + TL_COLS * (size_t)s);
     return 0;
 }
 
@@ -1265,6 +1304,8 @@ int psim_day_counts(psim_ctx* c, uint64_t* out) {
     out[2] = h[PROF_MOVERS];
     out[3] = h[PROF_QUEUE_STEPS];
     out[4] = h[PROF_REBUILDS];
+    out[5] = h[PROF_LISTED_LOCATIONS];
+    out[6] = h[PROF_LISTED_AGENTS];
     return 0;
 }
 
@@ -1310,6 +1351,7 @@ int psim_time_step_kernels(psim_ctx* c, uint32_t t, float* ms) {
     for (int j = 0; j < 3; ++j) CK(cudaEventElapsedTime(&ms[j], ev[j], ev[j + 1]));
     for (int j = 0; j < 4; ++j) cudaEventDestroy(ev[j]);
     c->csr_fresh = false;
+    c->list_sparse = true;
     c->t_next = t + 2;
     rc = launch_check(c);
     if (rc) return rc;

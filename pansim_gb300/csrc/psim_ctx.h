@@ -62,6 +62,8 @@ struct psim_ctx {
     uint64_t launches = 0;
     bool uploaded = false;
     bool csr_fresh = false;      // counts of the current positions are built
+    bool list_sparse = false;    // the agent list holds only the locations the step kernel's
+                                 // last rebuild listed (psim_get_csr builds the full one)
     // pinned host memory (one block): the statistics accumulators and the
     // expected-infection sums copied back, the clock copied in, the error
     // flags copied back, so that a day needs no synchronisation in between
@@ -83,7 +85,6 @@ struct psim_ctx {
     // per-kernel timing inside the day graph: event-record nodes around the
     // movement of step 0 and every kernel group of every step
     bool profile = false;
-    std::vector<cudaEvent_t> prof_ev;
     bool prof_valid = false;
 };
 

@@ -59,6 +59,8 @@ struct DevAgents {
     const uint32_t* loc_offset;
     const uint32_t* poss_loc;
     const uint8_t* poss_type;
+    const uint2* poss;            // the same entries packed: x = location, y = its type (one
+                                  // 8-byte load per entry for the decisions)
     const uint16_t* rep;          // replica of each agent
     uint32_t* location;
     uint32_t* move_at;            // absolute timestamp of the agent's next decision: the
@@ -123,6 +125,8 @@ struct DevLocs {
     uint32_t* cursor;             // [n] next free CSR slot of each location (scan: first slot)
     uint32_t* csr_off;            // [n+1] CSR offsets, derived from the cursors on demand
     uint32_t* csr_agents;         // [N]
+    uint32_t* list_at;            // [n] epoch of the step kernel's rebuild that last listed the
+                                  // location (build[4])
     float* slot_su;               // [V][N] beside each agent-list slot: the agent's susceptibility
                                   // to the variant times its age band's factor
     uint32_t* qu_pending;         // quarantine writes of the running step
@@ -145,7 +149,9 @@ struct DevLocs {
                                   // [2] the timestamp of the last step that rebuilt (decided by
                                   //     the step's first scan kernel, read by its later kernels),
                                   // [3] the timestamp of the last step whose decisions wrote a
-                                  //     location quarantine (merged by that step's scan)
+                                  //     location quarantine (merged by that step's scan),
+                                  // [4] the epoch of the step kernel's last rebuild (one more per
+                                  //     rebuild; its listed locations carry it in list_at)
 };
 
 // Incremental CSR: at most steps of a day no agent moves, and then the
@@ -213,7 +219,19 @@ enum {
     PROF_MOVERS = 2,         // agents queued for a decision
     PROF_QUEUE_STEPS = 3,    // steps whose queue kernel passed over the agents
     PROF_REBUILDS = 4,       // steps that rebuilt the agent list
-    PROF_N = 8
+    PROF_LISTED_LOCATIONS = 5,  // locations the rebuilds listed
+    PROF_LISTED_AGENTS = 6,     // agents the rebuilds listed
+    PROF_N = 8,
+    // Then the day's timeline (globaltimer, ns; a first entry is kept as the
+    // maximum of complements, so one zero fill starts every slot):
+    // [PROF_N] ~first block entry of the day's first movement, [PROF_N + 1]
+    // its last block exit; per step s at PROF_T + PROF_TW * s: ~first block
+    // entry, the last block past the rebuild's totals, its prefix and
+    // cursors, its slots, past the draws, past the queue, last block exit
+    // (the rebuild and queue slots stay 0 at steps without that phase).
+    PROF_T = PROF_N + 2,
+    PROF_TW = 7,
+    PROF_WORDS = PROF_T + PROF_TW * 1440
 };
 
 struct KArgs {
@@ -229,7 +247,7 @@ struct KArgs {
     uint32_t track_expected;
     DevTune tune;
     DevAdjoint adj;
-    unsigned long long* prof;  // [PROF_N] or null
+    unsigned long long* prof;  // [PROF_WORDS] or null
 };
 
 // raw counter slots of DevStatsAcc::c

@@ -44,18 +44,24 @@ __device__ __forceinline__ uint32_t loc_type(const KArgs& k, uint32_t l) { retur
 __device__ uint32_t find_location_range(const KArgs& k, uint32_t b, uint32_t e, uint32_t lt, int retry,
                                         psim_stream* rng, uint32_t f0, uint32_t f1, uint32_t f2) {
     if (lt == f0 || lt == f1 || lt == f2) {
-        for (uint32_t j = b; j < e; ++j)
-            if (lt == k.a.poss_type[j]) return k.a.poss_loc[j];
+        for (uint32_t j = b; j < e; ++j) {
+            const uint2 en = k.a.poss[j];
+            if (lt == en.y) return en.x;
+        }
         return NONE;
     }
-    uint32_t counter = 0, pos = 0;
+    uint32_t counter = 0, pos = 0, first = NONE;
     for (uint32_t j = b; j < e; ++j) {
-        if (lt == k.a.poss_type[j]) {
-            if (counter == 0) pos = j;
+        const uint2 en = k.a.poss[j];
+        if (lt == en.y) {
+            if (counter == 0) {
+                pos = j;
+                first = en.x;
+            }
             counter++;
         }
     }
-    if (counter == 1) return k.a.poss_loc[pos];
+    if (counter == 1) return first;
     if (counter > 1) {
         uint32_t counter2 = counter, rand_idx = counter2;
         // the reference loops until the pick is open or its one retry is
@@ -64,13 +70,14 @@ __device__ uint32_t find_location_range(const KArgs& k, uint32_t b, uint32_t e, 
             while (rand_idx == counter2) rand_idx = psim_below(rng, counter);
             counter2 = 0;
             for (uint32_t j = pos; j < e; ++j) {
-                if (lt == k.a.poss_type[j]) {
+                const uint2 en = k.a.poss[j];
+                if (lt == en.y) {
                     if (counter2 == rand_idx) {
-                        if (retry && loc_open(k, k.a.poss_loc[j]) == 0) {
+                        if (retry && loc_open(k, en.x) == 0) {
                             retry = 0;
                             break;
                         }
-                        return k.a.poss_loc[j];
+                        return en.x;
                     }
                     counter2++;
                 }
@@ -100,11 +107,12 @@ __device__ __forceinline__ void qu_write(const KArgs& k, uint32_t loc, uint32_t 
 }
 
 // RealMovementOps::quarantineAgent, movementPolicies.h:176-245
-__device__ void quarantine_agent(const KArgs& k, uint32_t i, uint32_t t, uint32_t until, psim_stream* rng) {
+// Returns whether the agent was quarantined (its flag set).
+__device__ bool quarantine_agent(const KArgs& k, uint32_t i, uint32_t t, uint32_t until, psim_stream* rng) {
     const psim_params& p = k.p;
-    if (p.quarantine_policy == 0) return;
-    if (k.a.st_diagnosed_ts[i] > 0 && !infected_of(k, i) && !p.quarantine_immune) return;
-    if (!k.a.diagnosed[i] && k.a.st_immunization_ts[i] > 0 && !p.quarantine_immune) return;
+    if (p.quarantine_policy == 0) return false;
+    if (k.a.st_diagnosed_ts[i] > 0 && !infected_of(k, i) && !p.quarantine_immune) return false;
+    if (!k.a.diagnosed[i] && k.a.st_immunization_ts[i] > 0 && !p.quarantine_immune) return false;
     k.a.quarantined[i] = 1;
     k.a.st_quarantined_ts[i] = t;
     uint32_t prev_until = k.a.st_quarantined_until[i];
@@ -125,6 +133,7 @@ __device__ void quarantine_agent(const KArgs& k, uint32_t i, uint32_t t, uint32_
             }
         }
     }
+    return true;
 }
 
 // minutes of TimeDayDuration(unsigned mins) (timeDay.cpp:64): the hours are
@@ -141,91 +150,133 @@ __device__ void diagnose_and_quarantine(const KArgs& k, uint32_t i, uint32_t t, 
     k.a.diagnosed[i] = 1;
     k.a.st_diagnosed_ts[i] = t;
     if (sum == 24u * 60u / dt) k.a.st_diagnosed_ts[i]++;
-    quarantine_agent(k, i, t, t + k.p.quarantine_length * 24u * 60u / dt, rng);
+    (void)quarantine_agent(k, i, t, t + k.p.quarantine_length * 24u * 60u / dt, rng);
 }
 
-// S: the agent's countdown (stepsUntilMove) as the decision just set it
-__device__ __forceinline__ void stayed_home_check(const KArgs& k, uint32_t i, uint32_t agent_home, uint32_t S) {
-    if (agent_home != NONE && k.a.location[i] != agent_home && S > 60u / k.p.time_step) k.a.stayed_home[i] = 0;
+// S: the agent's countdown (stepsUntilMove) as the decision just set it;
+// cur: the agent's location as the decision left it
+__device__ __forceinline__ void stayed_home_check(const KArgs& k, uint32_t i, uint32_t agent_home, uint32_t cur,
+                                                  uint32_t S) {
+    if (agent_home != NONE && cur != agent_home && S > 60u / k.p.time_step) k.a.stayed_home[i] = 0;
+}
+
+// The agent's fields that a decision reads, loaded together before it
+// starts: read where they are needed, behind branches and stores, each would
+// cost a round trip of its own.  The decision keeps its own copies of the two
+// it writes (location, quarantined flag).
+struct DecisionIn {
+    uint32_t loc, q_until, h_ts, h_until, lb, le, diag_ts, rep;
+    float inf;
+    uint8_t state, type, diag, no_work, age, quarantined;
+};
+__device__ __forceinline__ void decision_in(const KArgs& k, uint32_t i, DecisionIn& d) {
+    d.loc = k.a.location[i];
+    d.q_until = k.a.st_quarantined_until[i];
+    d.h_ts = k.a.st_hospitalized_ts[i];
+    d.h_until = k.a.st_hospitalized_until[i];
+    d.lb = k.a.loc_offset[i];
+    d.le = k.a.loc_offset[i + 1];
+    d.diag_ts = k.a.st_diagnosed_ts[i];
+    d.rep = k.a.rep[i];
+    d.inf = k.a.infectious[i];
+    d.state = (uint8_t)k.a.state[i];
+    d.type = k.a.type[i];
+    d.diag = k.a.diagnosed[i];
+    d.no_work = k.a.no_work[i];
+    d.age = k.a.age[i];
+    d.quarantined = k.a.quarantined[i];
+}
+
+// Quarantine end and type of a location (the quarantine rule's inputs);
+// neither changes during a step's decisions.
+struct LocQ {
+    uint32_t qu, ty;
+};
+__device__ __forceinline__ LocQ loc_q(const KArgs& k, uint32_t loc) {
+    LocQ q;
+    q.qu = loc_qu(k, loc);
+    q.ty = loc_type(k, loc);
+    return q;
+}
+__device__ __forceinline__ bool quarantine_type(const KArgs& k, uint32_t ty) {
+    return ty == k.p.home_type || ty == k.p.school_type || ty == k.p.classroom_type || ty == k.p.work_type;
 }
 
 // The full per-agent decision of doMovement once the countdown reached zero
 // (movementPolicies.h:333-1040).  The curfew and countdown prologue is in
 // move_agent.  S receives the agent's new countdown (stepsUntilMove after
 // the step); the caller turns it into the absolute timestamp of the next
-// decision.
+// decision, cur the agent's location after it (d.loc before).  The
+// location-dependent inputs (the quarantine rule's at the current and at the
+// chosen location, the chosen location's flags) load together as soon as the
+// location is known.
 __device__ void move_decide(const KArgs& k, uint32_t i, uint32_t t, uint32_t minutes, uint32_t day, uint32_t sum,
-                            psim_stream* rng, uint32_t& S) {
+                            psim_stream* rng, uint32_t& S, const DecisionIn& d, uint32_t& cur) {
     const psim_params& p = k.p;
     const uint32_t dt = p.time_step;
-    // The agent's fields that the decision reads, loaded together: read where
-    // they are needed, behind branches and stores, each costs a round trip
-    // of its own.  None of them is written before that point.
-    const uint32_t q_until = k.a.st_quarantined_until[i];
-    const uint8_t state_i = (uint8_t)k.a.state[i];
-    const uint32_t h_ts = k.a.st_hospitalized_ts[i];
-    const uint32_t h_until = k.a.st_hospitalized_until[i];
-    const uint32_t lb = k.a.loc_offset[i], le = k.a.loc_offset[i + 1];
-    const uint32_t agent_type = k.a.type[i];
-    const uint32_t loc_now = k.a.location[i];
-    const uint8_t diag = k.a.diagnosed[i];
-    const uint8_t no_work = k.a.no_work[i];
-    const uint8_t age = k.a.age[i];
+    const bool qrule = p.quarantine_policy > 1;
+    const LocQ q_now = qrule ? loc_q(k, d.loc) : LocQ{0u, NONE};
     auto fl = [&](uint32_t lt, int retry) {
-        return find_location_range(k, lb, le, lt, retry, rng, p.home_type, p.school_type, p.work_type);
+        return find_location_range(k, d.lb, d.le, lt, retry, rng, p.home_type, p.school_type, p.work_type);
     };
-    if (q_until <= t) k.a.quarantined[i] = 0;
+    cur = d.loc;
+    auto set_loc = [&](uint32_t l) {
+        cur = l;
+        k.a.location[i] = l;
+    };
+    bool quar = d.quarantined != 0;
+    if (d.q_until <= t) {
+        quar = false;
+        k.a.quarantined[i] = 0;
+    }
 
-    uint32_t wb = k.m.state_wb[state_i];
+    const uint32_t wb = k.m.state_wb[d.state];
     if (wb == WB_D) {
         S = NONE;
-        k.a.location[i] = k.r.cemetery[k.a.rep[i]];
+        set_loc(k.r.cemetery[d.rep]);
         return;
     }
-    uint32_t agent_home = fl(p.home_type, 0);
+    const uint32_t agent_home = fl(p.home_type, 0);
 
-    if (h_ts <= t && h_until > t && wb != WB_S && wb != WB_D) {
-        uint32_t x = h_until - t - 1;
+    if (d.h_ts <= t && d.h_until > t && wb != WB_S && wb != WB_D) {
+        uint32_t x = d.h_until - t - 1;
         S = x < sum ? x : sum;
-        k.a.location[i] = fl(p.hospital_type, 0);
-        if (!diag && k.a.infectious[i] != 0.0f) diagnose_and_quarantine(k, i, t, sum, rng);
+        set_loc(fl(p.hospital_type, 0));
+        if (!d.diag && d.inf != 0.0f) diagnose_and_quarantine(k, i, t, sum, rng);
         return;
     }
     if (wb == WB_S) {
         S = sum;
-        k.a.location[i] = fl(p.hospital_type, 0);
-        if (!diag && k.a.infectious[i] != 0.0f) diagnose_and_quarantine(k, i, t, sum, rng);
+        set_loc(fl(p.hospital_type, 0));
+        if (!d.diag && d.inf != 0.0f) diagnose_and_quarantine(k, i, t, sum, rng);
         return;
     }
-    {
-        uint32_t loc = loc_now;
-        if (p.quarantine_policy > 1 && t < loc_qu(k, loc) && is_quarantine_type(k, loc)) {
-            if (k.a.quarantined[i] == 0) quarantine_agent(k, i, t, loc_qu(k, loc), rng);
-            if (k.a.quarantined[i]) {
-                uint32_t x = loc_qu(k, k.a.location[i]) - t - 1;
-                S = x < sum ? x : sum;
-                uint32_t home_location = fl(p.home_type, 0);
-                if (home_location != k.a.location[i]) k.a.location[i] = home_location;
-                stayed_home_check(k, i, agent_home, S);
-                return;
-            }
+    if (qrule && t < q_now.qu && quarantine_type(k, q_now.ty)) {
+        if (!quar) quar = quarantine_agent(k, i, t, q_now.qu, rng);
+        if (quar) {
+            // the location is still the current one
+            uint32_t x = q_now.qu - t - 1;
+            S = x < sum ? x : sum;
+            uint32_t home_location = fl(p.home_type, 0);
+            if (home_location != cur) set_loc(home_location);
+            stayed_home_check(k, i, agent_home, cur, S);
+            return;
         }
     }
     if ((p.quarantine_policy > 0 &&
-         (diag ||
-          (k.a.st_diagnosed_ts[i] > 0 && (t - k.a.st_diagnosed_ts[i]) < p.quarantine_length * 24u * 60u / dt))) ||
-        (p.quarantine_policy > 0 && k.a.quarantined[i])) {
-        if (p.quarantine_policy > 0 && !k.a.quarantined[i])
-            quarantine_agent(k, i, t, t + p.quarantine_length * 24u * 60u / dt, rng);
-        if (k.a.quarantined[i]) {
-            k.a.location[i] = fl(p.home_type, 0);
+         (d.diag || (d.diag_ts > 0 && (t - d.diag_ts) < p.quarantine_length * 24u * 60u / dt))) ||
+        (p.quarantine_policy > 0 && quar)) {
+        if (p.quarantine_policy > 0 && !quar) quar = quarantine_agent(k, i, t, t + p.quarantine_length * 24u * 60u / dt, rng);
+        if (quar) {
+            set_loc(fl(p.home_type, 0));
             S = sum;
-            stayed_home_check(k, i, agent_home, S);
+            stayed_home_check(k, i, agent_home, cur, S);
             return;
         }
     }
 
     // schedule window (AgentTypeList::getOffsetIndex, agentType.cpp:13-15)
+    const uint32_t agent_type = d.type;
     const uint32_t off_idx = 7u * wb + day + agent_type * 28u;
     const uint32_t ev_b = k.m.event_offset[off_idx], ev_e = k.m.event_offset[off_idx + 1];
     int act_b = -1, act_e = -1;
@@ -240,9 +291,12 @@ __device__ void move_decide(const KArgs& k, uint32_t i, uint32_t t, uint32_t min
     }
 
     uint32_t new_type = NONE;
+    // the quarantine rule's inputs at a location loaded with its flags
+    uint32_t spec_loc = NONE;
+    LocQ spec_q{0u, NONE};
     if (act_b == -1 && act_e == -1) {  // Case 1
         new_type = wb == WB_S ? p.hospital_type : p.home_type;
-        k.a.location[i] = fl(new_type, 0);
+        set_loc(fl(new_type, 0));
         S = sum;
     }
     if (act_b != -1) {  // Case 2 and 4
@@ -264,16 +318,20 @@ __device__ void move_decide(const KArgs& k, uint32_t i, uint32_t t, uint32_t min
             new_type = k.m.ev_loc_type[act_b + idx];
             dur = k.m.ev_duration[act_b + idx];
         }
-        if (no_work != 0 && new_type == p.work_type) {
+        if (d.no_work != 0 && new_type == p.work_type) {
             new_type = p.home_type;
             num_pot = 1;
-            if (k.a.quarantined[i] == 0) k.a.st_days_in_quarantine[i]++;
+            if (!quar) k.a.st_days_in_quarantine[i]++;
         }
         uint32_t new_loc = fl(new_type, num_pot == 1);
-        bool too_old = (new_type == p.school_type || new_type == p.classroom_type) && age >= p.school_age_restriction;
-        // both flags of the new location load together
+        bool too_old = (new_type == p.school_type || new_type == p.classroom_type) && d.age >= p.school_age_restriction;
+        // the new location's flags and quarantine inputs load together
         const uint8_t nl_open = loc_open(k, new_loc);
         const uint32_t nl_closed = loc_closed_until(k, new_loc);
+        if (qrule) {
+            spec_loc = new_loc;
+            spec_q = loc_q(k, new_loc);
+        }
         if (too_old || ((nl_open == 0 || nl_closed > t) && new_type != p.work_type) ||
             (p.lockdown_nonvacc && k.a.st_immunization_ts[i] == 0)) {
             if (num_pot > 1) {
@@ -300,7 +358,7 @@ __device__ void move_decide(const KArgs& k, uint32_t i, uint32_t t, uint32_t min
             uint32_t my_class = fl(p.classroom_type, 0);
             if (my_class != NONE && loc_closed_until(k, my_class) > t) new_loc = fl(p.home_type, 0);
         }
-        k.a.location[i] = new_loc;
+        set_loc(new_loc);
         if (dur / 60u > 24u) {
             S = sum;
         } else if (act_e == -1) {
@@ -321,7 +379,7 @@ __device__ void move_decide(const KArgs& k, uint32_t i, uint32_t t, uint32_t min
         }
         if (agent_type + 1 == 7 && p.enable_curfew && (p.curfew_begin <= minutes / dt || p.curfew_end > minutes / dt)) {
             bool work_closed = new_type == p.work_type && (loc_open(k, new_loc) == 0 || loc_closed_until(k, new_loc) > t);
-            if (work_closed || (new_type != p.work_type && new_type != p.home_type)) k.a.location[i] = agent_home;
+            if (work_closed || (new_type != p.work_type && new_type != p.home_type)) set_loc(agent_home);
         }
     }
     if (act_b == -1 && act_e != -1) {  // Case 3
@@ -332,30 +390,30 @@ __device__ void move_decide(const KArgs& k, uint32_t i, uint32_t t, uint32_t min
         if (left < 30u / dt) {
         } else if (left < 60u / dt) {
             new_type = p.public_type;
-            k.a.location[i] = fl(p.public_type, 0);
+            set_loc(fl(p.public_type, 0));
         } else {
             new_type = p.home_type;
-            k.a.location[i] = fl(p.home_type, 0);
+            set_loc(fl(p.home_type, 0));
         }
     }
-    {
-        uint32_t loc = k.a.location[i];
-        if (p.quarantine_policy > 1 && t < loc_qu(k, loc) && is_quarantine_type(k, loc)) {
-            if (!k.a.quarantined[i]) quarantine_agent(k, i, t, loc_qu(k, loc), rng);
-            if (k.a.quarantined[i]) {
-                uint32_t x = loc_qu(k, k.a.location[i]) - t - 1;
+    if (qrule) {
+        const LocQ q = cur == spec_loc ? spec_q : cur == d.loc ? q_now : loc_q(k, cur);
+        if (t < q.qu && quarantine_type(k, q.ty)) {
+            if (!quar) quar = quarantine_agent(k, i, t, q.qu, rng);
+            if (quar) {
+                uint32_t x = q.qu - t - 1;
                 S = x < sum ? x : sum;
                 uint32_t home_location = fl(p.home_type, 0);
-                if (home_location != k.a.location[i]) k.a.location[i] = home_location;
-                stayed_home_check(k, i, agent_home, S);
+                if (home_location != cur) set_loc(home_location);
+                stayed_home_check(k, i, agent_home, cur, S);
                 return;
             }
         }
     }
     if (new_type == p.hospital_type || (new_type == p.doctor_type && psim_u01(rng) * 1.0 < 0.7)) {
-        if (!diag && k.a.infectious[i] != 0.0f) diagnose_and_quarantine(k, i, t, sum, rng);
+        if (!d.diag && d.inf != 0.0f) diagnose_and_quarantine(k, i, t, sum, rng);
     }
-    stayed_home_check(k, i, agent_home, S);
+    stayed_home_check(k, i, agent_home, cur, S);
     S = S - 1u;
 }
 
@@ -451,24 +509,36 @@ __device__ __forceinline__ bool mask_has(const KArgs& k, uint32_t s) {
 
 // doMovement for agent i at step c.t; s = its countdown before the step
 // (move_at - c.t).  Writes move_at when the agent decides or the curfew
-// prologue resets its countdown.
-__device__ __forceinline__ void move_agent(const KArgs& k, uint32_t i, const StepClock& c, uint32_t s, uint32_t* s_mm) {
-    if (!(c.curfew_now || s == 0)) return;  // counts down: move_at stays
-    const uint32_t rep = k.a.rep[i];
+// prologue resets its countdown.  pre: the decision's inputs when the caller
+// loaded them (its agents all decide), else null (loaded here if needed).
+// Returns the agent's location after the step (loc0: before it).
+__device__ __forceinline__ uint32_t move_agent(const KArgs& k, uint32_t i, const StepClock& c, uint32_t s,
+                                               uint32_t* s_mm, const DecisionIn* pre, uint32_t loc0) {
+    if (!(c.curfew_now || s == 0)) return loc0;  // counts down: move_at stays
+    DecisionIn d;
+    if (pre)
+        d = *pre;
+    else
+        decision_in(k, i, d);
     psim_stream rng;
-    psim_stream_init(&rng, k.r.seed[rep], i - k.r.agent_off[rep], c.t, PSIM_PHASE_MOVE);
+    psim_stream_init(&rng, k.r.seed[d.rep], i - k.r.agent_off[d.rep], c.t, PSIM_PHASE_MOVE);
     bool done = false;
     uint32_t S = s;
-    if (c.curfew_now) done = curfew_prologue(k, i, c.t, c.sum, &rng, S);
+    if (c.curfew_now) {
+        done = curfew_prologue(k, i, c.t, c.sum, &rng, S);
+        d.loc = k.a.location[i];  // the prologue may have sent the agent home
+    }
+    uint32_t cur = d.loc;
     if (!done) {
         if (S > 0)
             S = S - 1u;
         else
-            move_decide(k, i, c.t, c.minutes, c.day, c.sum, &rng, S);
+            move_decide(k, i, c.t, c.minutes, c.day, c.sum, &rng, S, d, cur);
     }
     const uint32_t m = c.t + 1u + S;
     k.a.move_at[i] = m;
     mask_note(k, s_mm, m);
+    return cur;
 }
 
 // Scan tiles: 256 threads x ITEMS locations (ITEMS = 2, 4 or 8, a tuning
@@ -693,11 +763,30 @@ __device__ __forceinline__ void add_expected(const KArgs& k, bool act, uint32_t 
     if ((int)(threadIdx.x & 31) == leader) atomicAdd(&k.r.expected[rep], tot);
 }
 
+// Timeline stamps of the profiled day graph (KArgs::prof): one atomic per
+// block, from thread 0, on the global nanosecond timer.
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// the block's entry (no wait for the other threads)
+__device__ __forceinline__ void prof_enter(const KArgs& k, uint32_t slot) {
+    if (k.prof && threadIdx.x == 0) atomicMax(&k.prof[slot], ~global_ns());
+}
+// the block's threads are past this point (every thread calls it)
+__device__ __forceinline__ void prof_mark(const KArgs& k, uint32_t slot) {
+    if (!k.prof) return;
+    __syncthreads();
+    if (threadIdx.x == 0) atomicMax(&k.prof[slot], global_ns());
+}
+
 // Movement of every agent + histogram + fixed-point infectiousness sums (the
 // day's first step, after a reset of the sums, and the per-phase entry
 // points).  Records the steps of the day at which agents decide next.
 __global__ void __launch_bounds__(256) k_movement(KArgs k, uint32_t step) {
     __shared__ uint32_t s_mm[MOVE_MASK_WORDS];
+    if (step == 0) prof_enter(k, PROF_N);
     mask_clear_shared(s_mm);
     const uint32_t N = k.a.n;
     const StepClock c = step_clock(k, step);
@@ -713,19 +802,15 @@ __global__ void __launch_bounds__(256) k_movement(KArgs k, uint32_t step) {
             const uint32_t s = m0 - c.t;
             loc0 = k.a.location[i];
             inf = k.a.infectious[i];
-            move_agent(k, i, c, s, s_mm);
-            if (c.curfew_now || s == 0) {
-                loc = k.a.location[i];
-            } else {
-                loc = loc0;
-                mask_note(k, s_mm, m0);  // an agent counting down decides later today
-            }
+            loc = move_agent(k, i, c, s, s_mm, nullptr, loc0);
+            if (!(c.curfew_now || s == 0)) mask_note(k, s_mm, m0);  // an agent counting down decides later today
             if (inf > 0.0f) var = k.a.variant[i];
         }
         moved |= count_agent(k, act, loc0, loc, inf, var);
     }
     publish_moved(k, moved, c.t);
     mask_flush(k, s_mm);
+    if (step == 0) prof_mark(k, PROF_N + 1);
 }
 
 // Histogram + fixed-point sums without movement (regroup after an upload).
@@ -1289,13 +1374,6 @@ __device__ __forceinline__ void slot_fill(const KArgs& k, uint32_t pos, uint32_t
         k.l.slot_su[(size_t)v * N + pos] = k.a.susceptible[(size_t)v * N + i] * sigma;
 }
 
-// The locations of block b for the rebuild: a contiguous range of `per`
-// locations (a multiple of 4), each thread owning consecutive quads.
-__device__ __forceinline__ uint32_t rebuild_per_block(uint32_t L) {
-    const uint32_t per = (L + gridDim.x - 1) / gridDim.x;
-    return (per + 3u) & ~3u;
-}
-
 __device__ __forceinline__ uint32_t block_sum(uint32_t v, uint32_t* s_red) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
@@ -1320,37 +1398,11 @@ __device__ __forceinline__ void merge_quarantine(const KArgs& k) {
     }
 }
 
-// Rebuild of the agent list: returns false when a barrier expired.
-constexpr int SLOT_ILP = 4;
-__device__ bool phase_rebuild(const KArgs& k, uint32_t* s_red, bool* s_ok) {
-    const uint32_t L = k.l.n, N = k.a.n;
-    const uint32_t per = rebuild_per_block(L);
-    const uint32_t lb = blockIdx.x * per;
-    const uint32_t le = min(L, lb + per);
-    const uint32_t quads = (per / 4 + blockDim.x - 1) / blockDim.x;  // per thread
-    const uint32_t q0 = lb + threadIdx.x * quads * 4u;
-    // 1: the block's total
-    uint32_t mine = 0;
-    for (uint32_t q = 0; q < quads; ++q) {
-        const uint32_t l = q0 + 4u * q;
-        if (l + 3u < le) {
-            const uint4 c = *reinterpret_cast<const uint4*>(k.l.counts + l);
-            mine += c.x + c.y + c.z + c.w;
-        } else {
-            for (uint32_t e = 0; e < 4; ++e)
-                if (l + e < le) mine += k.l.counts[l + e];
-        }
-    }
-    const uint32_t tot = block_sum(mine, s_red);
-    if (threadIdx.x == 0) k.l.tile_sums[blockIdx.x] = tot;
-    if (!grid_barrier(k, s_ok)) return false;
-    // 2: the sums of the blocks before this one, the thread's offset, the
-    // first slot of every location (the cursor the slots advance)
-    uint32_t pre = 0;
-    for (uint32_t b = threadIdx.x; b < blockIdx.x; b += blockDim.x) pre += k.l.tile_sums[b];
-    const uint32_t prefix = block_sum(pre, s_red);
+// Exclusive prefix of v over the block's threads in thread order; *total
+// receives the block's sum.  Every thread calls it.
+__device__ __forceinline__ uint32_t block_scan_excl(uint32_t v, uint32_t* s_red, uint32_t* total) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t x = mine;
+    uint32_t x = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
         const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
@@ -1358,64 +1410,135 @@ __device__ bool phase_rebuild(const KArgs& k, uint32_t* s_red, bool* s_ok) {
     }
     if (lane == 31) s_red[warp] = x;
     __syncthreads();
-    uint32_t woff = 0;
-    for (int q = 0; q < warp; ++q) woff += s_red[q];
+    uint32_t woff = 0, tot = 0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) {
+        const uint32_t wq = s_red[q];
+        if (q < warp) woff += wq;
+        tot += wq;
+    }
     __syncthreads();
-    uint32_t run = prefix + woff + x - mine;
-    for (uint32_t q = 0; q < quads; ++q) {
-        const uint32_t l = q0 + 4u * q;
-        if (l + 3u < le) {
-            const uint4 c = *reinterpret_cast<const uint4*>(k.l.counts + l);
-            *reinterpret_cast<uint4*>(k.l.cursor + l) = make_uint4(run, run + c.x, run + c.x + c.y, run + c.x + c.y + c.z);
-            run += c.x + c.y + c.z + c.w;
-        } else {
-            for (uint32_t e = 0; e < 4; ++e)
-                if (l + e < le) {
-                    k.l.cursor[l + e] = run;
-                    run += k.l.counts[l + e];
-                }
+    *total = tot;
+    return woff + x - v;
+}
+
+// the agents at the listed locations of mask word w (its set bits)
+__device__ __forceinline__ uint32_t listed_word_count(const KArgs& k, uint32_t hm, uint32_t w) {
+    uint32_t c = 0;
+    while (hm) {
+        const uint32_t l = w * 32u + (uint32_t)(__ffs(hm) - 1);
+        hm &= hm - 1u;
+        if (l < k.l.n) c += k.l.counts[l];
+    }
+    return c;
+}
+
+// Rebuild of the agent list.  Only the locations whose hazard-mask bit is set
+// are listed, because the draws of every step until the next rebuild visit no
+// other location: the mask is a superset of the locations with a nonzero sum
+// (every kernel that adds an infectious term sets the bit at once), and until
+// the next rebuild no other location gains a nonzero sum (nobody moves, since
+// a move makes the next step rebuild, and a draw infects only agents at a
+// location it visits).  A listed location gets its first slot (cursor, which
+// the slots advance to the segment's end) and the rebuild's epoch (list_at =
+// build[4]), which the draw checks.  In three parts between grid barriers:
+// 1: per block the agents at its listed locations (its range of mask words);
+// 2: the blocks before it, then the cursors and epochs of its locations;
+// 3: every agent at a listed location takes a slot (one returning atomic on
+// the location's cursor, or one per location and warp with agg_slot), its id
+// and susceptibility products written there.
+// Returns false when a barrier expired.
+__device__ bool phase_rebuild(const KArgs& k, uint32_t* s_red, bool* s_ok, uint32_t tl) {
+    const uint32_t L = k.l.n, N = k.a.n;
+    const uint32_t n_words = (L + 31u) >> 5;
+    const uint32_t per = (n_words + gridDim.x - 1) / gridDim.x;
+    const uint32_t wb = min(n_words, blockIdx.x * per), we = min(n_words, wb + per);
+    // 1
+    uint32_t mine = 0, locs = 0;
+    for (uint32_t w = wb + threadIdx.x; w < we; w += blockDim.x) {
+        const uint32_t hm = k.l.hmask[w];
+        if (hm) {
+            mine += listed_word_count(k, hm, w);
+            locs += __popc(hm);
+        }
+    }
+    const uint32_t tot = block_sum(mine, s_red);
+    if (threadIdx.x == 0) {
+        k.l.tile_sums[blockIdx.x] = tot;
+        if (blockIdx.x == 0) k.l.build[4] = k.l.build[4] + 1u;  // read after the barrier
+    }
+    if (k.prof) {
+        const uint32_t nl = block_sum(locs, s_red);
+        if (threadIdx.x == 0 && (nl | tot)) {
+            atomicAdd(&k.prof[PROF_LISTED_LOCATIONS], (unsigned long long)nl);
+            atomicAdd(&k.prof[PROF_LISTED_AGENTS], (unsigned long long)tot);
         }
     }
     if (!grid_barrier(k, s_ok)) return false;
-    // 3: the slots, SLOT_ILP agents' returning atomics in flight per thread
-    // (or one warp-aggregated atomic per location and warp)
-    if (k.tune.agg_slot) {
-        for (uint32_t base = blockIdx.x * blockDim.x; base < N; base += gridDim.x * blockDim.x) {
-            const uint32_t i = base + threadIdx.x;
-            const bool act = i < N;
-            const uint32_t loc = act ? k.a.location[i] : NONE;
-            const bool ok = act && loc < L;
-            const uint32_t pos = take_slot(k, ok, loc, true);
-            if (ok) slot_fill(k, pos, i);
-        }
-    } else {
-        // one variant (the common case): the slot's product is computed
-        // before the returning atomic, whose latency then covers the loads
-        const bool one = k.m.n_variants == 1;
-        const uint32_t tile = blockDim.x * SLOT_ILP;
-        for (uint32_t base = blockIdx.x * tile; base < N; base += gridDim.x * tile) {
-            uint32_t loc[SLOT_ILP], pos[SLOT_ILP];
-            float su[SLOT_ILP];
-#pragma unroll
-            for (int u = 0; u < SLOT_ILP; ++u) {
-                const uint32_t i = base + u * blockDim.x + threadIdx.x;
-                loc[u] = i < N ? k.a.location[i] : NONE;
-                su[u] = (one && i < N) ? k.a.susceptible[i] * k.p.sigma_band[k.a.band[i]] : 0.0f;
+    prof_mark(k, tl + 1);
+    // 2
+    const uint32_t epoch = k.l.build[4];
+    uint32_t pre = 0;
+    for (uint32_t b = threadIdx.x; b < blockIdx.x; b += blockDim.x) pre += k.l.tile_sums[b];
+    uint32_t base = block_sum(pre, s_red);
+    for (uint32_t c0 = wb; c0 < we; c0 += blockDim.x) {  // block-uniform trips
+        const uint32_t w = c0 + threadIdx.x;
+        uint32_t hm = w < we ? k.l.hmask[w] : 0u;
+        const uint32_t wc = hm ? listed_word_count(k, hm, w) : 0u;
+        uint32_t chunk = 0;
+        uint32_t run = base + block_scan_excl(wc, s_red, &chunk);
+        while (hm) {
+            const uint32_t l = w * 32u + (uint32_t)(__ffs(hm) - 1);
+            hm &= hm - 1u;
+            if (l < L) {
+                k.l.cursor[l] = run;
+                k.l.list_at[l] = epoch;
+                run += k.l.counts[l];
             }
+        }
+        base += chunk;
+    }
+    if (!grid_barrier(k, s_ok)) return false;
+    prof_mark(k, tl + 2);
+    // 3: four consecutive agents per thread (one 16-byte load of their
+    // locations), two quads in flight
+    const bool one = k.m.n_variants == 1;
+    const uint32_t quads = (N + 3u) >> 2;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t q0 = blockIdx.x * blockDim.x; q0 < quads; q0 += 2u * stride) {  // warp-uniform trips
+        uint32_t loc[8];
 #pragma unroll
-            for (int u = 0; u < SLOT_ILP; ++u) pos[u] = loc[u] < L ? atomicAdd(&k.l.cursor[loc[u]], 1u) : NONE;
+        for (int h = 0; h < 2; ++h) {
+            const uint32_t q = q0 + (uint32_t)h * stride + threadIdx.x;
+            const uint32_t i0 = q * 4u;
+            if (i0 + 3u < N) {
+                const uint4 v = *reinterpret_cast<const uint4*>(k.a.location + i0);
+                loc[4 * h + 0] = v.x;
+                loc[4 * h + 1] = v.y;
+                loc[4 * h + 2] = v.z;
+                loc[4 * h + 3] = v.w;
+            } else {
 #pragma unroll
-            for (int u = 0; u < SLOT_ILP; ++u) {
-                if (loc[u] >= L) continue;
-                const uint32_t i = base + u * blockDim.x + threadIdx.x;
-                if (!one) {
-                    slot_fill(k, pos[u], i);
-                } else if (pos[u] < N) {
-                    k.l.csr_agents[pos[u]] = i;
-                    k.l.slot_su[pos[u]] = su[u];
-                } else {
-                    atomicOr(k.err, ERR_LOCATION);
-                }
+                for (int u = 0; u < 4; ++u) loc[4 * h + u] = i0 + u < N ? k.a.location[i0 + u] : NONE;
+            }
+        }
+        uint32_t lw[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) lw[u] = loc[u] < L ? k.l.hmask[loc[u] >> 5] : 0u;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const uint32_t i = (q0 + (uint32_t)(u >> 2) * stride + threadIdx.x) * 4u + (uint32_t)(u & 3);
+            const bool ok = loc[u] < L && ((lw[u] >> (loc[u] & 31u)) & 1u);
+            float su = 0.0f;
+            if (ok && one) su = k.a.susceptible[i] * k.p.sigma_band[k.a.band[i]];
+            const uint32_t pos = take_slot(k, ok, loc[u], true);
+            if (!ok) continue;
+            if (!one) {
+                slot_fill(k, pos, i);
+            } else if (pos < N) {
+                k.l.csr_agents[pos] = i;
+                k.l.slot_su[pos] = su;
+            } else {
+                atomicOr(k.err, ERR_LOCATION);
             }
         }
     }
@@ -1649,6 +1772,7 @@ __device__ void phase_draw(const KArgs& k, uint32_t t, double* s_grad, uint32_t*
     const uint32_t n_words = (L + 31) >> 5;
     const uint32_t nw = gridDim.x * (blockDim.x >> 5);
     const uint32_t gw = (threadIdx.x >> 5) * gridDim.x + blockIdx.x;  // neighbouring blocks, neighbouring words
+    const uint32_t epoch = k.l.build[4];  // the last rebuild's: every visited location carries it
     uint32_t entries = 0, visited = 0;
     for (uint32_t base = gw; base < n_words; base += 32u * nw) {
         const uint32_t wid = base + (uint32_t)lane * nw;
@@ -1684,11 +1808,13 @@ __device__ void phase_draw(const KArgs& k, uint32_t t, double* s_grad, uint32_t*
             if (r < total && l < L) {
                 len = k.l.counts[l];
                 const uint32_t end = k.l.cursor[l];
+                const uint32_t listed = k.l.list_at[l];
                 h0 = k.l.hazard[l];
                 rep = k.l.rep[l];
-                // a histogram that disagrees with the agent list is reported
-                // and the location skipped, never expanded
-                if (len > end || end > N) {
+                // a location the last rebuild did not list, or a histogram
+                // that disagrees with the agent list, is reported and the
+                // location skipped, never expanded
+                if (listed != epoch || len > end || end > N) {
                     atomicOr(k.err, ERR_AGENT_LIST);
                     len = 0;
                 }
@@ -1737,25 +1863,61 @@ __device__ __forceinline__ bool decides_at(const KArgs& k, uint32_t s1) {
 }
 
 // The block's agents that decide at s1, in its own segment of the work list
-// (shared-memory counter: no global contention).  Reads one word per agent.
+// (shared-memory counter: no global contention).  Reads one word per agent:
+// four consecutive agents per thread (one 16-byte load), two quads in flight.
 __device__ __forceinline__ uint32_t phase_queue(const KArgs& k, uint32_t s1, uint32_t cap, uint32_t* s_cnt) {
     if (threadIdx.x == 0) *s_cnt = 0u;
     __syncthreads();
     const uint32_t N = k.a.n;
     const bool curfew_now = k.p.enable_curfew && k.p.curfew_begin == s1;
     const uint32_t t1 = k.clock->t0 + s1;
+    const uint32_t quads = (N + 3u) >> 2;
     const uint32_t stride = gridDim.x * blockDim.x;
     uint32_t* seg = k.a.worklist + (size_t)blockIdx.x * cap;
     const int lane = threadIdx.x & 31;
-    for (uint32_t base = blockIdx.x * blockDim.x; base < N; base += stride) {
-        const uint32_t i = base + threadIdx.x;
-        const bool mover = i < N && (curfew_now || k.a.move_at[i] == t1);
-        const unsigned cm = __ballot_sync(0xffffffffu, mover);
-        if (cm) {
-            uint32_t basew = 0;
-            if (lane == __ffs(cm) - 1) basew = atomicAdd(s_cnt, (uint32_t)__popc(cm));
-            basew = __shfl_sync(0xffffffffu, basew, __ffs(cm) - 1);
-            if (mover) seg[basew + __popc(cm & lanemask_lt())] = i;
+    for (uint32_t q0 = blockIdx.x * blockDim.x; q0 < quads; q0 += 2u * stride) {  // warp-uniform trips
+        uint32_t m[8];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const uint32_t i0 = (q0 + (uint32_t)h * stride + threadIdx.x) * 4u;
+            if (i0 + 3u < N) {
+                const uint4 v = *reinterpret_cast<const uint4*>(k.a.move_at + i0);
+                m[4 * h + 0] = v.x;
+                m[4 * h + 1] = v.y;
+                m[4 * h + 2] = v.z;
+                m[4 * h + 3] = v.w;
+            } else {
+#pragma unroll
+                for (int u = 0; u < 4; ++u) m[4 * h + u] = i0 + u < N ? k.a.move_at[i0 + u] : t1 + 1u;
+            }
+        }
+        // each quad's deciders in agent order: the warp's 128 agents of the
+        // first quad, then those of the second
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const uint32_t i0 = (q0 + (uint32_t)h * stride + threadIdx.x) * 4u;
+            uint32_t flags = 0;
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (i0 + u < N && (curfew_now || m[4 * h + u] == t1)) flags |= 1u << u;
+            const uint32_t mine = __popc(flags);
+            uint32_t inc = mine;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
+                if (lane >= o) inc += y;
+            }
+            const uint32_t wtot = __shfl_sync(0xffffffffu, inc, 31);
+            if (wtot) {
+                uint32_t basew = 0;
+                if (lane == 31) basew = atomicAdd(s_cnt, wtot);
+                uint32_t pos = __shfl_sync(0xffffffffu, basew, 31) + inc - mine;
+                while (flags) {
+                    const int u = __ffs(flags) - 1;
+                    flags &= flags - 1u;
+                    seg[pos++] = i0 + (uint32_t)u;
+                }
+            }
         }
     }
     __syncthreads();
@@ -1796,11 +1958,15 @@ __device__ void phase_decide(const KArgs& k, uint32_t step, uint32_t cap, uint32
                 act = false;
             }
             if (act) {
-                loc0 = k.a.location[i];
-                inf = k.a.infectious[i];
-                if (inf > 0.0f) var = k.a.variant[i];
-                move_agent(k, i, c, k.a.move_at[i] - c.t, s_mm);
-                loc = k.a.location[i];
+                // every queued agent decides: its inputs load at once
+                DecisionIn d;
+                decision_in(k, i, d);
+                const uint32_t m0 = k.a.move_at[i];
+                const uint32_t vr = k.a.variant[i];
+                loc0 = d.loc;
+                inf = d.inf;
+                if (inf > 0.0f) var = vr;
+                loc = move_agent(k, i, c, m0 - c.t, s_mm, &d, loc0);
             }
             moved |= count_agent_delta(k, act, loc0, loc, inf, var, inf, var);
         }
@@ -1816,13 +1982,16 @@ __global__ void __launch_bounds__(256, 4) k_step(KArgs k, uint32_t step, uint32_
     __shared__ uint32_t s_red[32];
     __shared__ uint32_t s_cnt, s_seg;
     __shared__ bool s_ok;
+    const uint32_t tl = PROF_T + PROF_TW * step;  // the step's timeline slots (profiled graph)
+    prof_enter(k, tl);
     if (*((volatile uint32_t*)k.err) & ERR_BARRIER) return;  // an earlier barrier expired
     const uint32_t t = k.clock->t0 + step;
     if (phases & PH_REBUILD) {
         const bool rebuild = csr_decide(k, t);
         if (rebuild) {
             if (k.prof && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&k.prof[PROF_REBUILDS], 1ull);
-            if (!phase_rebuild(k, s_red, &s_ok)) return;
+            if (!phase_rebuild(k, s_red, &s_ok, tl)) return;
+            prof_mark(k, tl + 3);
         }
         // the step's location quarantine writes (decisions of step t)
         if (k.p.quarantine_policy > 1 && k.l.build[3] == t) merge_quarantine(k);
@@ -1836,6 +2005,7 @@ __global__ void __launch_bounds__(256, 4) k_step(KArgs k, uint32_t step, uint32_
             atomicAdd(&k.prof[PROF_DRAW_LOCATIONS], (unsigned long long)visited);
         }
         grad_end(k, s_grad);
+        prof_mark(k, tl + 4);
     }
     if ((phases & PH_DECIDE) && step + 1 < k.spd && decides_at(k, step + 1)) {
         mask_clear_shared(s_mm);
@@ -1844,11 +2014,13 @@ __global__ void __launch_bounds__(256, 4) k_step(KArgs k, uint32_t step, uint32_
             if (n) atomicAdd(&k.prof[PROF_MOVERS], (unsigned long long)n);
             if (blockIdx.x == 0) atomicAdd(&k.prof[PROF_QUEUE_STEPS], 1ull);
         }
+        prof_mark(k, tl + 5);
         // every draw and every block's queue before any decision
         if (!grid_barrier(k, &s_ok)) return;
         phase_decide(k, step, cap, s_mm, &s_seg);
         mask_flush(k, s_mm);
     }
+    prof_mark(k, tl + 6);
 }
 
 // Canonical CSR order (ascending agent id inside a location, the output of
@@ -2555,7 +2727,9 @@ static void step_geometry(const KArgs& k, unsigned* grid, uint32_t* cap) {
     unsigned g = (unsigned)std::min<size_t>((size_t)sm_count() * bps, std::max<size_t>(want, 1));
     g = std::min(g, (unsigned)WORK_MAX_BLOCKS);
     *grid = g;
-    *cap = (uint32_t)((((size_t)k.a.n + (size_t)g * 256 - 1) / ((size_t)g * 256)) * 256);
+    // the queue's quads: ceil(quads / (g * 256)) per thread, 4 agents each
+    const size_t quads = ((size_t)k.a.n + 3) / 4;
+    *cap = (uint32_t)(((quads + (size_t)g * 256 - 1) / ((size_t)g * 256)) * 1024);
 }
 void launch_step(const KArgs& k, uint32_t step, uint32_t phases, cudaStream_t s) {
     unsigned g;

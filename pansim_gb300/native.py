@@ -69,6 +69,7 @@ def lib(auto_build=True):
         L.psim_other_disease_day.argtypes = [P, U32]
         L.psim_get_events.argtypes = [P, P, P, P, P, P, P, U32, P]
         L.psim_day_kernel_ms.argtypes = [P, C.c_void_p]
+        L.psim_day_timeline.argtypes = [P, C.c_void_p]
         L.psim_day_counts.argtypes = [P, C.c_void_p]
         L.psim_set_alloc_fault.argtypes = [C.c_longlong]
         L.psim_launch_count.argtypes = [P, C.POINTER(C.c_uint64)]
@@ -300,18 +301,28 @@ class GpuSim:
         self._ck(lib().psim_set_profiling(self.h, 1 if on else 0), "set_profiling")
 
     def day_kernel_ms(self):
-        """Summed durations of the last profiled day: movement(0), the step
-        kernel's rebuilds, draws, queues + decisions, and 0."""
+        """Of the last profiled day, from the kernels' timeline stamps: the
+        first movement kernel, the step kernel's rebuilds, draws, queues +
+        decisions, and the time between the kernels (ms, summed)."""
         ms = np.zeros(5, np.float32)
         self._ck(lib().psim_day_kernel_ms(self.h, _p(ms)), "day_kernel_ms")
         return ms
+
+    def day_timeline(self):
+        """Per step of the last profiled day (rows), microseconds: the step
+        kernel's span, its rebuild's totals, prefix and cursors, slots, the
+        draws, the queue, the decisions (0 where the phase did not run), the
+        time since the previous kernel ended."""
+        us = np.zeros((self.snap.steps_per_day, 8), np.float32)
+        self._ck(lib().psim_day_timeline(self.h, _p(us)), "day_timeline")
+        return us
 
     def day_counts(self):
         """Of the last profiled day: agent-list entries the draws expanded,
         locations with a set hazard-mask bit they visited, agents queued for a
         decision, steps whose queue passed over the agents, steps that rebuilt
-        the agent list."""
-        out = np.zeros(5, np.uint64)
+        the agent list, locations and agents those rebuilds listed."""
+        out = np.zeros(7, np.uint64)
         self._ck(lib().psim_day_counts(self.h, _p(out)), "day_counts")
         return out
 

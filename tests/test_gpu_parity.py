@@ -184,10 +184,19 @@ def test_profiled_graph_same_results_and_kernel_times(gpu_lib):
     for d in range(2):
         assert stats_rows(o.run_day(d)) == stats_rows(g.run_day(d)), d
         ms = g.day_kernel_ms()
-        assert (ms[:4] > 0).all() and ms[4] == 0, ms
-        assert ms.sum() <= g.last_day_ms() * 1.001
-        entries, visited, movers, queues, rebuilds = g.day_counts()
+        assert (ms[:4] > 0).all() and ms[4] >= 0, ms
+        assert ms.sum() <= g.last_day_ms() * 1.01, (ms, g.last_day_ms())
+        entries, visited, movers, queues, rebuilds, listed_locs, listed_agents = g.day_counts()
         assert entries > 0 and visited > 0 and movers > 0 and 0 < queues < 143 and 0 < rebuilds <= 144
+        # the rebuilds list the visited locations' agents, a small part of all
+        assert 0 < listed_agents < rebuilds * 12000 and listed_locs * 144 >= visited * rebuilds // 2
+        # per step: spans, the steps that rebuilt and queued, the gaps
+        tl = g.day_timeline()
+        assert tl.shape == (144, 8) and (tl >= 0).all()
+        assert (tl[:, 0] > 0).all()
+        assert rebuilds - 2 <= (tl[:, 1:4].sum(axis=1) > 0).sum() <= rebuilds
+        assert queues - 2 <= (tl[:, 6] > 0).sum() <= queues
+        assert (tl[:, 0].sum() + tl[:, 7].sum()) * 1e-3 <= g.last_day_ms() * 1.01
     g.set_profiling(False)
     assert stats_rows(o.run_day(2)) == stats_rows(g.run_day(2))
     g.download()
