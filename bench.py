@@ -40,19 +40,18 @@ STEP_BYTES = (32, 20)
 
 def kernel_bytes(N, L, V, spd, counts):
     """Algorithmic bytes per simulated day of each phase of the step kernel,
-    from the profiled day's counters (entries E, visited locations H, queued
-    agents M, queue passes Q, rebuilds R, listed locations LL and agents LA,
-    summed over the rebuilds):
+    from the profiled day's counters (entries E, entries at a location with a
+    nonzero ratio EH, queued agents M, queue passes Q, rebuilds R, listed
+    locations LL and agents LA, summed over the rebuilds and steps):
       rebuild   per rebuild the hazard mask read twice (L / 4) and every
-                agent's location (4 N); per listed location its count read
-                twice, its first slot and epoch written (16); per listed
-                agent its age band and susceptibilities read, its slot's
-                atomic, id and susceptibility products written (13 + 8 V)
-      draw      per step the two mask words per 32 locations (L/4); at the
-                day's first step every location's sums, count, weight and
-                replica read and its hazard written (22 L); per visited
-                location count, cursor, hazard, replica (14); per entry the
-                agent id and the susceptibility products (4 + 4 V)
+                agent's location (4 N); per listed location its sums read
+                (8 V), its count read twice and its first slot written (12);
+                per listed agent its age band and susceptibilities read, its
+                slot's atomic, id, location and susceptibility products
+                written (17 + 8 V)
+      draw      per entry its slot's location, agent and susceptibility
+                products (8 + 4 V) and its location's count, weight, replica
+                and sums (10 + 8 V)
       decide    per queue pass the decision timestamps (4 N); per decision
                 76: its work-list entry written and read (8), the agent's
                 location, decision timestamp, state, type, age, flags and
@@ -60,9 +59,9 @@ def kernel_bytes(N, L, V, spd, counts):
                 location's flags (5), the location and timestamp written (8),
                 the histogram deltas (8)
     """
-    E, H, M, Q, R, LL, LA = (float(x) for x in counts)
-    return {"rebuild": R * (L / 4.0 + 4.0 * N) + 16.0 * LL + (13 + 8 * V) * LA,
-            "draw": spd * L / 4.0 + 22.0 * L + 14.0 * H + (4 + 4 * V) * E,
+    E, EH, M, Q, R, LL, LA = (float(x) for x in counts)
+    return {"rebuild": R * (L / 4.0 + 4.0 * N) + (12 + 8 * V) * LL + (17 + 8 * V) * LA,
+            "draw": (18 + 12 * V) * E,
             "decide": 4.0 * N * Q + 76.0 * M}
 
 
@@ -625,7 +624,7 @@ def main():
         # the step-rate figure: the reference's per-step bytes over our
         # average timestep time
         step_bytes = STEP_BYTES[0] * N + STEP_BYTES[1] * L
-        counts_d = {"draw_entries": counts[0], "draw_locations": counts[1], "decisions": counts[2],
+        counts_d = {"draw_entries": counts[0], "draw_entries_with_hazard": counts[1], "decisions": counts[2],
                     "queue_passes": counts[3], "rebuilds": counts[4], "listed_locations": counts[5],
                     "listed_agents": counts[6]}
         line = {

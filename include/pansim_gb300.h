@@ -470,9 +470,9 @@ int psim_last_day_ms(psim_ctx* ctx, float* ms);
  * slots, the draws, the queue, the decisions (0 when the phase did not run),
  * the time since the previous kernel's last exit}, microseconds;
  * psim_day_counts gives out[7] = {agent-list entries the draws expanded,
- * locations with a set hazard-mask bit they visited, agents queued for a
- * decision, steps at which agents were queued, steps that rebuilt the agent
- * list, locations and agents those rebuilds listed}, summed over the day's
+ * those at a location with a nonzero ratio, agents queued for a decision,
+ * steps at which agents were queued, steps that rebuilt the agent list,
+ * locations and agents those rebuilds listed}, summed over the day's
  * steps. */
 int psim_set_profiling(psim_ctx* ctx, int on);
 int psim_day_kernel_ms(psim_ctx* ctx, float* ms /* [5] */);

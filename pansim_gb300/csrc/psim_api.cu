@@ -594,7 +594,8 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     if ((rc = dalloc(c, &dl.csr_off, L + 1))) return bail(rc);
     if ((rc = dalloc(c, &dl.cursor, L))) return bail(rc);
     if ((rc = dalloc(c, &dl.csr_agents, N))) return bail(rc);
-    if ((rc = dalloc(c, &dl.list_at, L))) return bail(rc);
+    if ((rc = dalloc(c, &dl.slot_loc, N))) return bail(rc);
+    if ((rc = dalloc(c, &dl.inf_pending, N))) return bail(rc);
     if ((rc = dalloc(c, &dl.slot_su, N * V))) return bail(rc);
     if ((rc = dalloc(c, &dl.qu_pending, L))) return bail(rc);
     if ((rc = dalloc(c, &dl.sfix, L * V))) return bail(rc);
@@ -1300,7 +1301,7 @@ int psim_day_counts(psim_ctx* c, uint64_t* out) {
     CK(cudaMemcpyAsync(h, c->d_prof, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     out[0] = h[PROF_DRAW_ENTRIES];
-    out[1] = h[PROF_DRAW_LOCATIONS];
+    out[1] = h[PROF_DRAW_HAZARD];
     out[2] = h[PROF_MOVERS];
     out[3] = h[PROF_QUEUE_STEPS];
     out[4] = h[PROF_REBUILDS];

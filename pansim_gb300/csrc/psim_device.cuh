@@ -125,8 +125,6 @@ struct DevLocs {
     uint32_t* cursor;             // [n] next free CSR slot of each location (scan: first slot)
     uint32_t* csr_off;            // [n+1] CSR offsets, derived from the cursors on demand
     uint32_t* csr_agents;         // [N]
-    uint32_t* list_at;            // [n] epoch of the step kernel's rebuild that last listed the
-                                  // location (build[4])
     float* slot_su;               // [V][N] beside each agent-list slot: the agent's susceptibility
                                   // to the variant times its age band's factor
     uint32_t* qu_pending;         // quarantine writes of the running step
@@ -139,8 +137,12 @@ struct DevLocs {
     uint8_t* flags;               // testing flags
     uint32_t* tile_sums;          // per-tile sums of the histogram (two-pass scan), per-block sums
                                   // of the step kernel's rebuild
-    uint32_t* bar;                // the step kernel's grid barrier ([0] arrivals, [1] generation)
-                                  // and per-step decision tickets ([BAR_TICKETS + step])
+    uint32_t* bar;                // the step kernel's grid barrier ([0] arrivals, [1] generation),
+                                  // per-step decision tickets ([BAR_TICKETS + step]), the
+                                  // deferred infections and the blocks past the draws
+    uint32_t* slot_loc;           // [N] the location of each agent-list slot the step kernel listed
+    uint4* inf_pending;           // [N] the step's deferred infections (location, infectiousness
+                                  // before and after, variants)
     uint64_t* scan_status;        // per-tile status words of the single-pass scan (epoch | flag | value)
     uint32_t* scan_state;         // [0] epoch of the next single-pass scan, [1] its tile ticket
     uint32_t* build;              // [0] timestamp at which agents last took new locations,
@@ -150,8 +152,8 @@ struct DevLocs {
                                   //     the step's first scan kernel, read by its later kernels),
                                   // [3] the timestamp of the last step whose decisions wrote a
                                   //     location quarantine (merged by that step's scan),
-                                  // [4] the epoch of the step kernel's last rebuild (one more per
-                                  //     rebuild; its listed locations carry it in list_at)
+                                  // [5] the agent-list entries the step kernel's last rebuild
+                                  //     listed
 };
 
 // Incremental CSR: at most steps of a day no agent moves, and then the
@@ -215,7 +217,7 @@ struct DevAdjoint {
 // over the day's steps
 enum {
     PROF_DRAW_ENTRIES = 0,   // agent-list entries the draw kernel expanded
-    PROF_DRAW_LOCATIONS = 1, // locations with their hazard-mask bit set it visited
+    PROF_DRAW_HAZARD = 1,    // entries at a location with a nonzero ratio
     PROF_MOVERS = 2,         // agents queued for a decision
     PROF_QUEUE_STEPS = 3,    // steps whose queue kernel passed over the agents
     PROF_REBUILDS = 4,       // steps that rebuilt the agent list
@@ -269,15 +271,16 @@ enum {
 // The words are written by earlier kernels (or by block 0 here, which leaves
 // the decision unchanged): plain loads, so that the warps of an SM share one
 // L1 line instead of queueing on one L2 address.
-__device__ __forceinline__ bool csr_decide(const KArgs& k, uint32_t t) {
-    const uint32_t moved = k.l.build[0];
-    const uint32_t force = k.l.build[1];
+__device__ __forceinline__ bool csr_decide_from(const KArgs& k, uint32_t t, uint32_t moved, uint32_t force) {
     const bool r = moved == t || force == t || force == BUILD_PENDING;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         if (force == BUILD_PENDING) k.l.build[1] = t;
         k.l.build[2] = r ? t : NONE;
     }
     return r;
+}
+__device__ __forceinline__ bool csr_decide(const KArgs& k, uint32_t t) {
+    return csr_decide_from(k, t, k.l.build[0], k.l.build[1]);
 }
 // the decision, in the later kernels of the step at t
 __device__ __forceinline__ bool csr_rebuild(const KArgs& k, uint32_t t) { return k.l.build[2] == t; }
@@ -319,7 +322,11 @@ void launch_step(const KArgs& k, uint32_t step_in_day, uint32_t phases, cudaStre
 void launch_time_shift(uint32_t* a, uint32_t n, uint32_t delta, cudaStream_t s);
 // words of the barrier array: two for the barrier, one ticket per step
 constexpr uint32_t BAR_TICKETS = 2;
-constexpr uint32_t BAR_WORDS = BAR_TICKETS + 1440;
+// after the tickets: the step's deferred infections and the blocks that
+// finished its draws
+constexpr uint32_t BAR_INFECTIONS = BAR_TICKETS + 1440;
+constexpr uint32_t BAR_DRAWN = BAR_INFECTIONS + 1;
+constexpr uint32_t BAR_WORDS = BAR_DRAWN + 1;
 // work-list segments of the decisions (blocks of the queue kernel at most)
 constexpr uint32_t WORK_MAX_BLOCKS = 152u * 64u;
 // words of the per-day mask of decision steps (1440 steps of one minute at most)

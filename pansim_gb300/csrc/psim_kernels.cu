@@ -681,11 +681,12 @@ __device__ __forceinline__ void store_slot(const KArgs& k, uint32_t pos, uint32_
 // d p / d theta of one draw (p = r * s * sigma_band, r = 1 - exp(-x),
 // x = k * S/n * w * season * dt), weighted by the replica's dL/dE, added to the
 // block's FP64 accumulators
+// x: the location's hazard argument k*S/n*w*season*dt for variant v
 __device__ __noinline__ void adjoint_terms(const KArgs& k, uint32_t i, uint32_t loc, uint32_t v, uint32_t rep, float r,
-                                           float su, float s_eff, double* s_grad) {
+                                           float su, float s_eff, double* s_grad, float x_f) {
     const double g = k.adj.weight[rep];
     if (g == 0.0) return;
-    const double x = (double)k.l.hazard_x[(size_t)v * k.l.n + loc];
+    const double x = (double)x_f;
     const double dpdx = (double)s_eff * (1.0 - (double)r);
     const double kf = (double)k.r.k_f[rep];
     if (kf != 0.0) atomicAdd(&s_grad[GRAD_K], g * dpdx * x / kf);
@@ -715,7 +716,8 @@ __device__ __forceinline__ double draw_agent(const KArgs& k, uint32_t i, uint32_
         if (!(s_eff > 0.0f)) continue;
         const float pf = h * s_eff;
         term_sum += pf < 1.0f ? (double)pf : 1.0;
-        if (k.adj.on && pf < 1.0f) adjoint_terms(k, i, loc, v, rep, h, su, s_eff, s_grad);
+        if (k.adj.on && pf < 1.0f)
+            adjoint_terms(k, i, loc, v, rep, h, su, s_eff, s_grad, k.l.hazard_x[(size_t)v * L + loc]);
         const double U = psim_u01_once(seed, li, t, PSIM_PHASE_INFECT + v);
         if (U < (double)pf) {
             k.a.state[i] = (int8_t)k.m.first_infected;
@@ -1421,6 +1423,22 @@ __device__ __forceinline__ uint32_t block_scan_excl(uint32_t v, uint32_t* s_red,
     return woff + x - v;
 }
 
+// the set bits of mask word w whose location has a nonzero sum of some variant
+__device__ __forceinline__ uint32_t nonzero_sum_bits(const KArgs& k, uint32_t hm, uint32_t w) {
+    const uint32_t L = k.l.n, V = k.m.n_variants;
+    uint32_t keep = 0, rest = hm;
+    while (rest) {
+        const uint32_t b = (uint32_t)(__ffs(rest) - 1);
+        rest &= rest - 1u;
+        const uint32_t l = w * 32u + b;
+        if (l >= L) continue;
+        bool nz = false;
+        for (uint32_t v = 0; v < V && !nz; ++v) nz = k.l.sfix[(size_t)v * L + l] != 0ull;
+        if (nz) keep |= 1u << b;
+    }
+    return keep;
+}
+
 // the agents at the listed locations of mask word w (its set bits)
 __device__ __forceinline__ uint32_t listed_word_count(const KArgs& k, uint32_t hm, uint32_t w) {
     uint32_t c = 0;
@@ -1432,40 +1450,39 @@ __device__ __forceinline__ uint32_t listed_word_count(const KArgs& k, uint32_t h
     return c;
 }
 
-// Rebuild of the agent list.  Only the locations whose hazard-mask bit is set
-// are listed, because the draws of every step until the next rebuild visit no
-// other location: the mask is a superset of the locations with a nonzero sum
-// (every kernel that adds an infectious term sets the bit at once), and until
-// the next rebuild no other location gains a nonzero sum (nobody moves, since
-// a move makes the next step rebuild, and a draw infects only agents at a
-// location it visits).  A listed location gets its first slot (cursor, which
-// the slots advance to the segment's end) and the rebuild's epoch (list_at =
-// build[4]), which the draw checks.  In three parts between grid barriers:
-// 1: per block the agents at its listed locations (its range of mask words);
-// 2: the blocks before it, then the cursors and epochs of its locations;
-// 3: every agent at a listed location takes a slot (one returning atomic on
-// the location's cursor, or one per location and warp with agg_slot), its id
-// and susceptibility products written there.
-// Returns false when a barrier expired.
+// Rebuild of the agent list.  Only the locations with a nonzero sum are
+// listed, because the draws of every step until the next rebuild need no
+// other location: until then no other location gains a nonzero sum (nobody
+// moves, since a move makes the next step rebuild, and a draw infects only
+// agents at a location with a nonzero sum).  The hazard mask is a superset of
+// those locations (every kernel that adds an infectious term sets the bit at
+// once); part 1 clears the bits of the locations whose sums are zero again.
+// The listed locations' agents fill the first build[5] slots, each slot with
+// its agent, susceptibility products and location.  In three parts between
+// grid barriers: 1: per block the agents at its listed locations (its range
+// of mask words); 2: the blocks before it, then the first slot (cursor) of
+// each of its locations; 3: every agent at a listed location takes a slot
+// (one returning atomic on the location's cursor, or one per location and
+// warp with agg_slot).  Returns false when a barrier expired.
 __device__ bool phase_rebuild(const KArgs& k, uint32_t* s_red, bool* s_ok, uint32_t tl) {
     const uint32_t L = k.l.n, N = k.a.n;
     const uint32_t n_words = (L + 31u) >> 5;
     const uint32_t per = (n_words + gridDim.x - 1) / gridDim.x;
     const uint32_t wb = min(n_words, blockIdx.x * per), we = min(n_words, wb + per);
-    // 1
+    // 1 (the bits of locations whose sums are all zero again are cleared:
+    // the mask is then exactly the locations with a nonzero sum)
     uint32_t mine = 0, locs = 0;
     for (uint32_t w = wb + threadIdx.x; w < we; w += blockDim.x) {
         const uint32_t hm = k.l.hmask[w];
         if (hm) {
-            mine += listed_word_count(k, hm, w);
-            locs += __popc(hm);
+            const uint32_t keep = nonzero_sum_bits(k, hm, w);
+            if (keep != hm) k.l.hmask[w] = keep;
+            mine += listed_word_count(k, keep, w);
+            locs += __popc(keep);
         }
     }
     const uint32_t tot = block_sum(mine, s_red);
-    if (threadIdx.x == 0) {
-        k.l.tile_sums[blockIdx.x] = tot;
-        if (blockIdx.x == 0) k.l.build[4] = k.l.build[4] + 1u;  // read after the barrier
-    }
+    if (threadIdx.x == 0) k.l.tile_sums[blockIdx.x] = tot;
     if (k.prof) {
         const uint32_t nl = block_sum(locs, s_red);
         if (threadIdx.x == 0 && (nl | tot)) {
@@ -1476,7 +1493,6 @@ __device__ bool phase_rebuild(const KArgs& k, uint32_t* s_red, bool* s_ok, uint3
     if (!grid_barrier(k, s_ok)) return false;
     prof_mark(k, tl + 1);
     // 2
-    const uint32_t epoch = k.l.build[4];
     uint32_t pre = 0;
     for (uint32_t b = threadIdx.x; b < blockIdx.x; b += blockDim.x) pre += k.l.tile_sums[b];
     uint32_t base = block_sum(pre, s_red);
@@ -1491,12 +1507,12 @@ __device__ bool phase_rebuild(const KArgs& k, uint32_t* s_red, bool* s_ok, uint3
             hm &= hm - 1u;
             if (l < L) {
                 k.l.cursor[l] = run;
-                k.l.list_at[l] = epoch;
                 run += k.l.counts[l];
             }
         }
         base += chunk;
     }
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) k.l.build[5] = base;  // all blocks' entries
     if (!grid_barrier(k, s_ok)) return false;
     prof_mark(k, tl + 2);
     // 3: four consecutive agents per thread (one 16-byte load of their
@@ -1540,6 +1556,7 @@ __device__ bool phase_rebuild(const KArgs& k, uint32_t* s_red, bool* s_ok, uint3
             } else {
                 atomicOr(k.err, ERR_LOCATION);
             }
+            if (pos < N) k.l.slot_loc[pos] = loc[u];
         }
     }
     return grid_barrier(k, s_ok);
@@ -1577,114 +1594,6 @@ __device__ __forceinline__ void infect_agent(const KArgs& k, uint32_t i, uint32_
     k.a.st_variant_mask[i] |= 1u << v;
 }
 
-// Position of the n-th (0-based) set bit of w, n < popc(w): five halvings,
-// each keeping the half that holds it.
-__device__ __forceinline__ uint32_t nth_set_bit(uint32_t w, uint32_t n) {
-    uint32_t pos = 0;
-#pragma unroll
-    for (int width = 16; width > 0; width >>= 1) {
-        const uint32_t c = __popc(w & ((1u << width) - 1u));
-        if (n >= c) {
-            n -= c;
-            w >>= width;
-            pos += (uint32_t)width;
-        }
-    }
-    return pos;
-}
-
-// Owner lane of item r among lanes holding inclusive prefix counts `inc`
-// (non-decreasing over the lanes): the number of lanes whose inclusive end is
-// <= r, by a five-step binary search.  Every lane calls it.
-__device__ __forceinline__ uint32_t owner_lane(uint32_t r, uint32_t inc) {
-    uint32_t q = 0;
-#pragma unroll
-    for (int st = 16; st > 0; st >>= 1) {
-        const uint32_t v = __shfl_sync(0xffffffffu, inc, (int)(q + st - 1));
-        if (r >= v) q += st;
-    }
-    return q & 31u;
-}
-
-// The r-th set bit (0-based) of the words held by the lanes (lane j: word
-// word_id, bits `words`, inclusive prefix `inc` of the set-bit counts): the
-// location (meaningful for r below the total only).  Every lane calls it, and
-// every shuffle runs on all lanes.
-__device__ __forceinline__ uint32_t set_bit_location(uint32_t r, uint32_t words, uint32_t word_id, uint32_t inc) {
-    const uint32_t o = owner_lane(r, inc);
-    const uint32_t w = __shfl_sync(0xffffffffu, words, (int)o);
-    const uint32_t wid = __shfl_sync(0xffffffffu, word_id, (int)o);
-    const uint32_t before = __shfl_sync(0xffffffffu, inc, o > 0 ? (int)o - 1 : 0);
-    const uint32_t exc = o > 0 ? before : 0u;
-    return wid * 32u + (nth_set_bit(w, r - exc) & 31u);
-}
-
-// Dirty pass of the draw: the dirty locations (sum or count changed since
-// their last evaluation) of the lanes' words get their hazards recomputed from
-// the fixed-point sums (the scan's formula).  Lane j takes bit j of each dirty
-// word, four words at a time with their loads issued together.  Returns, in
-// each lane, the new hazard bits of its own word.
-__device__ __forceinline__ uint32_t draw_dirty(const KArgs& k, uint32_t word_id, uint32_t sm, float season,
-                                               uint32_t dt) {
-    const uint32_t L = k.l.n, V = k.m.n_variants;
-    const int lane = threadIdx.x & 31;
-    uint32_t my_nz = 0;
-    unsigned pending = __ballot_sync(0xffffffffu, sm != 0u);
-    while (pending) {  // warp-uniform
-        int qs[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            qs[u] = pending ? __ffs(pending) - 1 : -1;
-            if (pending) pending &= pending - 1;
-        }
-        bool dy[4];
-        uint32_t cnt[4], rp[4], lid[4];
-        float wl[4];
-        long long fx[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const int src = qs[u] >= 0 ? qs[u] : 0;
-            const uint32_t smq = __shfl_sync(0xffffffffu, sm, src);
-            const uint32_t wid = __shfl_sync(0xffffffffu, word_id, src);
-            const uint32_t l = wid * 32u + (uint32_t)lane;
-            lid[u] = l;
-            dy[u] = qs[u] >= 0 && ((smq >> lane) & 1u) && l < L;
-            cnt[u] = 0;
-            rp[u] = 0;
-            wl[u] = 0.0f;
-            fx[u] = 0;
-            if (dy[u]) {
-                cnt[u] = k.l.counts[l];
-                rp[u] = k.l.rep[l];
-                wl[u] = k.l.infectiousness[l];
-                fx[u] = (long long)k.l.sfix[l];
-            }
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            bool nz = false;
-            if (dy[u]) {
-                const uint32_t l = lid[u];
-                const float k_f = k.r.k_f[rp[u]];
-                for (uint32_t v = 0; v < V; ++v) {
-                    const size_t idx = (size_t)v * L + l;
-                    const long long fix = v == 0 ? fx[u] : (long long)k.l.sfix[idx];
-                    float h = 0.0f, x = 0.0f;
-                    if (fix != 0) {
-                        h = psim_hazard_x(fix, cnt[u], k_f, wl[u], season, dt, &x);
-                        nz = true;
-                    }
-                    k.l.hazard[idx] = h;
-                    if (k.adj.on) k.l.hazard_x[idx] = x;
-                }
-            }
-            const uint32_t nzw = __ballot_sync(0xffffffffu, nz);
-            if (lane == qs[u]) my_nz = nzw;
-        }
-    }
-    return my_nz;
-}
-
 // U < p for the 53-bit uniform U = K * 2^-53 of the words (a, b)
 // (psim_u01_from) and a float probability p > 0, in integers: p * 2^53 is
 // exact in float (a power-of-two scaling of a normal or subnormal p), and
@@ -1695,15 +1604,39 @@ __device__ __forceinline__ bool u01_below(uint32_t a, uint32_t b, float p) {
     return K < __float2ull_ru(p * 9007199254740992.0f);
 }
 
-// The draws of one agent-list entry (the agent in slot pos at location loc of
-// replica rep, variant-0 hazard h0); returns the sum of min(1, p) over its
-// draws when expected infections are tracked (else 0).  An agent that is
-// infected updates its slot's susceptibility products and its location's sum
-// (a delta for the next step: only the warp handling this location reads its
-// sum in this step).
+// Infection ratio of variant v at location loc (count cnt, weight wl,
+// replica coefficient kf) from the location's fixed-point sum as the step
+// started: the formula the scans evaluate (psim_hazard_x), so every entry of
+// a location computes the same value.  x receives its argument.
+__device__ __forceinline__ float entry_hazard(const KArgs& k, uint32_t loc, uint32_t v, uint32_t cnt, float wl,
+                                              float kf, float season, uint32_t dt, float* x) {
+    const long long fix = (long long)k.l.sfix[(size_t)v * k.l.n + loc];
+    *x = 0.0f;
+    return fix != 0 ? psim_hazard_x(fix, cnt, kf, wl, season, dt, x) : 0.0f;
+}
+
+// An infection's change of its location's sum, applied after every draw of
+// the step (the ratios of a step come from the sums as the step started):
+// location, infectiousness before and after, variants before and after.
+__device__ __forceinline__ void defer_infection(const KArgs& k, uint32_t loc, float inf0, uint32_t var0, float inf,
+                                                uint32_t var) {
+    const uint32_t j = atomicAdd(&k.l.bar[BAR_INFECTIONS], 1u);
+    if (j < k.a.n)
+        k.l.inf_pending[j] = make_uint4(loc, __float_as_uint(inf0), __float_as_uint(inf), var0 | (var << 8));
+    else
+        atomicOr(k.err, ERR_AGENT_LIST);
+}
+
+// The draws of one agent-list entry: the agent in slot pos at location loc
+// of replica rep (count cnt, weight wl).  Returns the sum of min(1, p) over
+// its draws when expected infections are tracked (else 0).  An agent that is
+// infected updates its slot's susceptibility products (read by no other
+// entry) and defers its location's sum change.
 __device__ __forceinline__ double draw_entry(const KArgs& k, uint32_t pos, uint32_t i, uint32_t loc, uint32_t rep,
-                                             float h0, uint32_t t, double* s_grad) {
-    const uint32_t L = k.l.n, N = k.a.n, V = k.m.n_variants;
+                                             uint32_t cnt, float wl, float season, uint32_t t, double* s_grad,
+                                             bool* any_h) {
+    const uint32_t N = k.a.n, V = k.m.n_variants, dt = k.p.time_step;
+    const float kf = k.r.k_f[rep];
     const float su0 = k.l.slot_su[pos];
     const unsigned long long seed = k.r.seed[rep];
     const uint32_t li = i - k.r.agent_off[rep];
@@ -1712,8 +1645,10 @@ __device__ __forceinline__ double draw_entry(const KArgs& k, uint32_t pos, uint3
     float inf0 = 0.0f, sigma = 0.0f;
     uint32_t var0 = 0;
     for (uint32_t v = 0; v < V; ++v) {
-        const float h = v == 0 ? h0 : k.l.hazard[(size_t)v * L + loc];
+        float x;
+        const float h = entry_hazard(k, loc, v, cnt, wl, kf, season, dt, &x);
         if (!(h > 0.0f)) continue;
+        *any_h = true;
         if (!k.r.variant_active[rep * V + v]) continue;
         // after an infection the later variants read the agent's new
         // susceptibility (what the slot then gets)
@@ -1725,7 +1660,8 @@ __device__ __forceinline__ double draw_entry(const KArgs& k, uint32_t pos, uint3
         if (!(s_eff > 0.0f)) continue;
         const float pf = h * s_eff;
         if (k.track_expected) term += pf < 1.0f ? (double)pf : 1.0;
-        if (k.adj.on && pf < 1.0f) adjoint_terms(k, i, loc, v, rep, h, k.a.susceptible[(size_t)v * N + i], s_eff, s_grad);
+        if (k.adj.on && pf < 1.0f)
+            adjoint_terms(k, i, loc, v, rep, h, k.a.susceptible[(size_t)v * N + i], s_eff, s_grad, x);
         // the uniform of the stream (seed, agent, t, infection + v), as
         // psim_u01_once draws it
         psim_ctr4 c;
@@ -1748,118 +1684,95 @@ __device__ __forceinline__ double draw_entry(const KArgs& k, uint32_t pos, uint3
         for (uint32_t v = 0; v < V; ++v) k.l.slot_su[(size_t)v * N + pos] = k.a.susceptible[(size_t)v * N + i] * sigma;
         const float inf = k.a.infectious[i];
         const uint32_t var = inf > 0.0f ? k.a.variant[i] : 0u;
-        count_agent_delta(k, true, loc, loc, inf0, var0, inf, var);
+        const long long q0 = inf0 > 0.0f ? __float2ll_rn(inf0 * PSIM_FIX_SCALE_F) : 0ll;
+        const long long q1 = inf > 0.0f ? __float2ll_rn(inf * PSIM_FIX_SCALE_F) : 0ll;
+        if (q0 != q1 || var0 != var) defer_infection(k, loc, inf0, var0, inf, var);
     }
     return term;
 }
 
-// The draw phase.  Warp g takes, 32 at a time (one per lane), the mask words
-// g, g + G, g + 2G, ... (G warps in the grid): words strided over the whole
-// location range, so that the locations of one type, which lie together (and
-// at a time of day are infectious together), spread over all warps.  The dirty
-// locations of its words get their hazards and mask bits first
-// (draw_dirty); then every location whose hazard-mask bit is set has its
-// agent-list segment expanded over the lanes (warp scans of the set bits and
-// of the segment lengths, each lane finding its item by a binary search) and
-// each agent draws from its Philox stream (seed, agent, t).  The slot holds
-// the susceptibility product, so an agent that is not infected costs two
-// coalesced loads of its slot.
-__device__ void phase_draw(const KArgs& k, uint32_t t, double* s_grad, uint32_t* n_entries, uint32_t* n_visited) {
+// The draw phase: every entry of the agent list (the agents at the locations
+// the last rebuild listed, build[5] of them), one per thread, slots in order
+// (coalesced loads of the slot's location, agent and susceptibility
+// products).  Each entry evaluates its location's ratio from the location's
+// sum, count and weight (the same inputs give the same value at every entry)
+// and draws from the agent's Philox stream (seed, agent, t).  The work is the
+// listed entries, spread evenly over the grid, whatever the number of
+// locations.
+__device__ void phase_draw(const KArgs& k, uint32_t t, float season, double* s_grad, uint32_t* n_entries,
+                           uint32_t* n_hazard) {
     const uint32_t L = k.l.n, N = k.a.n;
-    const float season = k.clock->season;
-    const uint32_t dt = k.p.time_step;
-    const int lane = threadIdx.x & 31;
-    const uint32_t n_words = (L + 31) >> 5;
-    const uint32_t nw = gridDim.x * (blockDim.x >> 5);
-    const uint32_t gw = (threadIdx.x >> 5) * gridDim.x + blockIdx.x;  // neighbouring blocks, neighbouring words
-    const uint32_t epoch = k.l.build[4];  // the last rebuild's: every visited location carries it
-    uint32_t entries = 0, visited = 0;
-    for (uint32_t base = gw; base < n_words; base += 32u * nw) {
-        const uint32_t wid = base + (uint32_t)lane * nw;
-        const bool own = wid < n_words;
-        uint32_t hm = own ? k.l.hmask[wid] : 0u;
-        const uint32_t sm = own ? k.l.smask[wid] : 0u;
-        if (!__any_sync(0xffffffffu, (hm | sm) != 0u)) continue;
-        if (__any_sync(0xffffffffu, sm != 0u)) {
-            const uint32_t nzw = draw_dirty(k, wid, sm, season, dt);
-            if (own && sm) {
-                hm = (hm & ~sm) | nzw;
-                k.l.hmask[wid] = hm;
-                k.l.smask[wid] = 0u;
-            }
-            // the mask stores and hazards above come before this warp's
-            // infections mark their locations for the next step
-            __syncwarp();
-            __threadfence_block();
-        }
-        uint32_t inc = __popc(hm);
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(0xffffffffu, inc, o);
-            if (lane >= o) inc += y;
-        }
-        const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
-        visited += total;
-        for (uint32_t b0 = 0; b0 < total; b0 += 32) {
-            const uint32_t r = b0 + lane;
-            const uint32_t l = set_bit_location(r, hm, wid, inc);
-            uint32_t len = 0, beg = 0, rep = 0;
-            float h0 = 0.0f;
-            if (r < total && l < L) {
-                len = k.l.counts[l];
-                const uint32_t end = k.l.cursor[l];
-                const uint32_t listed = k.l.list_at[l];
-                h0 = k.l.hazard[l];
-                rep = k.l.rep[l];
-                // a location the last rebuild did not list, or a histogram
-                // that disagrees with the agent list, is reported and the
-                // location skipped, never expanded
-                if (listed != epoch || len > end || end > N) {
-                    atomicOr(k.err, ERR_AGENT_LIST);
-                    len = 0;
-                }
-                beg = end - len;
-            }
-            uint32_t einc = len;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t y = __shfl_up_sync(0xffffffffu, einc, o);
-                if (lane >= o) einc += y;
-            }
-            const uint32_t etotal = __shfl_sync(0xffffffffu, einc, 31);
-            entries += etotal;
-            for (uint32_t e0 = 0; e0 < etotal; e0 += 32) {
-                const uint32_t e = e0 + lane;
-                const uint32_t q = owner_lane(e, einc);
-                const uint32_t q_inc = __shfl_sync(0xffffffffu, einc, (int)q);
-                const uint32_t q_len = __shfl_sync(0xffffffffu, len, (int)q);
-                const uint32_t q_beg = __shfl_sync(0xffffffffu, beg, (int)q);
-                const uint32_t q_loc = __shfl_sync(0xffffffffu, l, (int)q);
-                const uint32_t q_rep = __shfl_sync(0xffffffffu, rep, (int)q);
-                const float q_h0 = __shfl_sync(0xffffffffu, h0, (int)q);
-                bool act = e < etotal;
-                const uint32_t pos = q_beg + (e - (q_inc - q_len));
-                uint32_t i = NONE;
-                if (act) {
-                    if (pos < N) i = k.l.csr_agents[pos];
-                    if (i >= N) {
-                        atomicOr(k.err, ERR_AGENT_LIST);
-                        act = false;
-                    }
-                }
-                const double term = act ? draw_entry(k, pos, i, q_loc, q_rep, q_h0, t, s_grad) : 0.0;
-                if (k.track_expected) add_expected_rep(k, act, q_rep, term);
+    const uint32_t n_listed = k.l.build[5];
+    const uint32_t stride = gridDim.x * blockDim.x;
+    uint32_t entries = 0, hazard = 0;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n_listed; base += stride) {  // block-uniform trips
+        const uint32_t pos = base + threadIdx.x;
+        bool act = pos < n_listed && pos < N;
+        uint32_t loc = NONE, i = NONE, rep = 0, cnt = 0;
+        float wl = 0.0f;
+        if (act) {
+            loc = k.l.slot_loc[pos];
+            i = k.l.csr_agents[pos];
+            if (loc >= L || i >= N) {
+                atomicOr(k.err, ERR_AGENT_LIST);
+                act = false;
+            } else {
+                cnt = k.l.counts[loc];
+                wl = k.l.infectiousness[loc];
+                rep = k.l.rep[loc];
             }
         }
+        bool any_h = false;
+        const double term = act ? draw_entry(k, pos, i, loc, rep, cnt, wl, season, t, s_grad, &any_h) : 0.0;
+        entries += act ? 1u : 0u;
+        hazard += any_h ? 1u : 0u;
+        if (k.track_expected) add_expected_rep(k, act, rep, term);
     }
     *n_entries += entries;
-    *n_visited += visited;
+    *n_hazard += hazard;
 }
 
-// whether any agent decides at step s1 of the day (or it is the curfew step)
-__device__ __forceinline__ bool decides_at(const KArgs& k, uint32_t s1) {
-    const bool curfew_now = k.p.enable_curfew && k.p.curfew_begin == s1;
-    return curfew_now || mask_has(k, s1);
+// After every draw of the step: the deferred sum changes of the infected
+// agents (called by the last block to finish its draws; the counters start
+// at 0 again for the next step).
+__device__ void apply_infections(const KArgs& k) {
+    const uint32_t L = k.l.n;
+    const uint32_t n = min(k.l.bar[BAR_INFECTIONS], k.a.n);
+    for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
+        const uint4 e = k.l.inf_pending[j];
+        const uint32_t loc = e.x;
+        const float inf0 = __uint_as_float(e.y), inf = __uint_as_float(e.z);
+        const uint32_t var0 = e.w & 0xFFu, var = (e.w >> 8) & 0xFFu;
+        const long long q0 = inf0 > 0.0f ? __float2ll_rn(inf0 * PSIM_FIX_SCALE_F) : 0ll;
+        const long long q1 = inf > 0.0f ? __float2ll_rn(inf * PSIM_FIX_SCALE_F) : 0ll;
+        if (q0) {
+            atomicAdd(&k.l.sfix[(size_t)var0 * L + loc], (unsigned long long)(-q0));
+            mark_dirty(k, loc);
+        }
+        if (q1) {
+            atomicAdd(&k.l.sfix[(size_t)var * L + loc], (unsigned long long)q1);
+            mark_dirty(k, loc);
+            mark_hazardous(k, loc);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        k.l.bar[BAR_INFECTIONS] = 0u;
+        k.l.bar[BAR_DRAWN] = 0u;
+    }
+}
+
+// Whether this block is the last to finish the step's draws (every thread
+// calls it; the block's draws are ordered before its arrival).
+__device__ __forceinline__ bool last_to_draw(const KArgs& k, bool* s_flag) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        *s_flag = atomicAdd(&k.l.bar[BAR_DRAWN], 1u) == gridDim.x - 1u;
+        if (*s_flag) __threadfence();
+    }
+    __syncthreads();
+    return *s_flag;
 }
 
 // The block's agents that decide at s1, in its own segment of the work list
@@ -1981,33 +1894,51 @@ __global__ void __launch_bounds__(256, 4) k_step(KArgs k, uint32_t step, uint32_
     __shared__ uint32_t s_mm[MOVE_MASK_WORDS];
     __shared__ uint32_t s_red[32];
     __shared__ uint32_t s_cnt, s_seg;
-    __shared__ bool s_ok;
+    __shared__ bool s_ok, s_last;
     const uint32_t tl = PROF_T + PROF_TW * step;  // the step's timeline slots (profiled graph)
     prof_enter(k, tl);
-    if (*((volatile uint32_t*)k.err) & ERR_BARRIER) return;  // an earlier barrier expired
-    const uint32_t t = k.clock->t0 + step;
+    // the words the step's phases start from, loaded together: the error
+    // flags, the clock, the rebuild words (a block that starts after block 0
+    // turned BUILD_PENDING into t decides the same), the step of the last
+    // quarantine writes, the decision-mask word of the next step (the
+    // decisions of this launch mark later steps only)
+    const uint32_t err0 = *((volatile uint32_t*)k.err);
+    const uint32_t t0 = k.clock->t0;
+    const float season = k.clock->season;
+    const uint32_t moved = k.l.build[0], force = k.l.build[1], q_step = k.l.build[3];
+    const uint32_t s1 = step + 1;
+    const uint32_t mm_word = s1 < k.spd ? k.a.move_mask[s1 >> 5] : 0u;
+    if (err0 & ERR_BARRIER) return;  // an earlier barrier expired
+    const uint32_t t = t0 + step;
     if (phases & PH_REBUILD) {
-        const bool rebuild = csr_decide(k, t);
+        const bool rebuild = csr_decide_from(k, t, moved, force);
         if (rebuild) {
             if (k.prof && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&k.prof[PROF_REBUILDS], 1ull);
             if (!phase_rebuild(k, s_red, &s_ok, tl)) return;
             prof_mark(k, tl + 3);
         }
         // the step's location quarantine writes (decisions of step t)
-        if (k.p.quarantine_policy > 1 && k.l.build[3] == t) merge_quarantine(k);
+        if (k.p.quarantine_policy > 1 && q_step == t) merge_quarantine(k);
     }
     if (phases & PH_DRAW) {
         grad_begin(k, s_grad);
-        uint32_t entries = 0, visited = 0;
-        phase_draw(k, t, s_grad, &entries, &visited);
-        if (k.prof && (threadIdx.x & 31) == 0 && (entries | visited)) {
-            atomicAdd(&k.prof[PROF_DRAW_ENTRIES], (unsigned long long)entries);
-            atomicAdd(&k.prof[PROF_DRAW_LOCATIONS], (unsigned long long)visited);
+        uint32_t entries = 0, hazard = 0;
+        phase_draw(k, t, season, s_grad, &entries, &hazard);
+        if (k.prof) {
+            entries = __reduce_add_sync(0xffffffffu, entries);
+            hazard = __reduce_add_sync(0xffffffffu, hazard);
+            if ((threadIdx.x & 31) == 0 && (entries | hazard)) {
+                atomicAdd(&k.prof[PROF_DRAW_ENTRIES], (unsigned long long)entries);
+                atomicAdd(&k.prof[PROF_DRAW_HAZARD], (unsigned long long)hazard);
+            }
         }
         grad_end(k, s_grad);
+        // the infections' sum changes, once every draw of the step is done
+        if (last_to_draw(k, &s_last)) apply_infections(k);
         prof_mark(k, tl + 4);
     }
-    if ((phases & PH_DECIDE) && step + 1 < k.spd && decides_at(k, step + 1)) {
+    const bool decides = (k.p.enable_curfew && k.p.curfew_begin == s1) || ((mm_word >> (s1 & 31u)) & 1u) != 0;
+    if ((phases & PH_DECIDE) && s1 < k.spd && decides) {
         mask_clear_shared(s_mm);
         const uint32_t n = phase_queue(k, step + 1, cap, &s_cnt);
         if (k.prof && threadIdx.x == 0) {

@@ -319,7 +319,7 @@ class GpuSim:
 
     def day_counts(self):
         """Of the last profiled day: agent-list entries the draws expanded,
-        locations with a set hazard-mask bit they visited, agents queued for a
+        those at a location with a nonzero ratio, agents queued for a
         decision, steps whose queue passed over the agents, steps that rebuilt
         the agent list, locations and agents those rebuilds listed."""
         out = np.zeros(7, np.uint64)

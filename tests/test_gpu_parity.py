@@ -186,10 +186,11 @@ def test_profiled_graph_same_results_and_kernel_times(gpu_lib):
         ms = g.day_kernel_ms()
         assert (ms[:4] > 0).all() and ms[4] >= 0, ms
         assert ms.sum() <= g.last_day_ms() * 1.01, (ms, g.last_day_ms())
-        entries, visited, movers, queues, rebuilds, listed_locs, listed_agents = g.day_counts()
-        assert entries > 0 and visited > 0 and movers > 0 and 0 < queues < 143 and 0 < rebuilds <= 144
-        # the rebuilds list the visited locations' agents, a small part of all
-        assert 0 < listed_agents < rebuilds * 12000 and listed_locs * 144 >= visited * rebuilds // 2
+        entries, hazard, movers, queues, rebuilds, listed_locs, listed_agents = g.day_counts()
+        assert entries > 0 and 0 < hazard <= entries and movers > 0 and 0 < queues < 143 and 0 < rebuilds <= 144
+        # the rebuilds list the agents at locations with a nonzero sum, a
+        # part of all; every step draws the entries of the last rebuild
+        assert 0 < listed_locs <= listed_agents < rebuilds * 12000 and entries >= listed_agents
         # per step: spans, the steps that rebuilt and queued, the gaps
         tl = g.day_timeline()
         assert tl.shape == (144, 8) and (tl >= 0).all()
