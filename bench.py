@@ -70,14 +70,13 @@ KERNEL_LABELS = {"rebuild": "k_step rebuild phase", "draw": "k_step draw phase",
 
 def step_kinds(tl):
     """The profiled day's steps by kind (tl: per step the kernel span, the
-    rebuild's totals, prefix and slots, the draws, the queue, the decisions,
-    the time since the previous kernel, us): count and mean span, gap and
-    phase times of the draw-only steps, the steps with a rebuild and no
-    decisions, with decisions and no rebuild, with both."""
-    reb, dec = tl[:, 1:4].sum(axis=1) > 0, tl[:, 6] > 0
+    rebuild's listing and slots, the draws, the queue, the decisions, the
+    time since the previous kernel, us): count and mean span, gap and phase
+    times of the draw-only steps, the steps with a rebuild and no decisions,
+    with decisions and no rebuild, with both."""
+    reb, dec = tl[:, 1:3].sum(axis=1) > 0, tl[:, 5] > 0
     out = {}
-    cols = ["span_us", "rebuild_totals_us", "rebuild_prefix_us", "rebuild_slots_us", "draw_us", "queue_us",
-            "decide_us", "gap_us"]
+    cols = ["span_us", "rebuild_listing_us", "rebuild_slots_us", "draw_us", "queue_us", "decide_us", "gap_us"]
     for name, sel in [("draw_only", ~reb & ~dec), ("rebuild", reb & ~dec), ("decide", ~reb & dec),
                       ("rebuild_and_decide", reb & dec)]:
         n = int(sel.sum())

@@ -462,13 +462,13 @@ int psim_last_day_ms(psim_ctx* ctx, float* ms);
  * (the global nanosecond timer at every block's entry, at the end of each
  * phase of the step kernel and at its exit; one atomic per block and stamp)
  * and counters.  For the last psim_run_steps: psim_day_kernel_ms gives ms[5]
- * = {the day's first movement kernel, the step kernel's rebuilds (histogram
- * prefix + agent-list slots), its draws, its queues + decisions, and the time
- * between the kernels}, summed over the day; psim_day_timeline gives per step
- * s, at us[8*s .. 8*s+7], {the kernel's span from its first block's entry to
- * its last block's exit, the rebuild's totals, its prefix and cursors, its
- * slots, the draws, the queue, the decisions (0 when the phase did not run),
- * the time since the previous kernel's last exit}, microseconds;
+ * = {the day's first movement kernel, the step kernel's rebuilds (listing +
+ * agent-list slots), its draws, its queues + decisions, and the time between
+ * the kernels}, summed over the day; psim_day_timeline gives per step
+ * s, at us[7*s .. 7*s+6], {the kernel's span from its first block's entry to
+ * its last block's exit, the rebuild's listing, its slots, the draws, the
+ * queue, the decisions (0 when the phase did not run), the time since the
+ * previous kernel's last exit}, microseconds;
  * psim_day_counts gives out[7] = {agent-list entries the draws expanded,
  * those at a location with a nonzero ratio, agents queued for a decision,
  * steps at which agents were queued, steps that rebuilt the agent list,
@@ -476,7 +476,7 @@ int psim_last_day_ms(psim_ctx* ctx, float* ms);
  * steps. */
 int psim_set_profiling(psim_ctx* ctx, int on);
 int psim_day_kernel_ms(psim_ctx* ctx, float* ms /* [5] */);
-int psim_day_timeline(psim_ctx* ctx, float* us /* [8 * steps_per_day] */);
+int psim_day_timeline(psim_ctx* ctx, float* us /* [7 * steps_per_day] */);
 int psim_day_counts(psim_ctx* ctx, uint64_t* out /* [7] */);
 /* Counts of kernel launches issued by the library since creation. */
 int psim_launch_count(psim_ctx* ctx, uint64_t* out);

@@ -406,6 +406,45 @@ void assemble_stats(psim_ctx* c, uint32_t t, psim_day_stats* out) {
 
 }  // namespace
 
+// The schedule window of doMovement (movementPolicies.h:585-603) for every
+// schedule slot and step of the day: act_b = the first event of the slot
+// active at the step's minute, act_e = the first event starting after it (or
+// the slot's end when its last event is the active one), -1 where none.
+int upload_window_table(psim_ctx* c) {
+    const std::vector<uint32_t>& off = c->h_event_offset;
+    const std::vector<uint16_t>&st = c->h_ev_start, &en = c->h_ev_end;
+    const size_t n_slots = off.empty() ? 0 : off.size() - 1;
+    const uint32_t spd = c->spd, dt = 1440u / spd;
+    std::vector<int2> win(n_slots * spd);
+    for (size_t q = 0; q < n_slots; ++q) {
+        const uint32_t ev_b = off[q], ev_e = off[q + 1];
+        for (uint32_t s = 0; s < spd; ++s) {
+            const uint32_t minutes = s * dt;
+            int act_b = -1, act_e = -1;
+            for (uint32_t j = ev_b; j < ev_e; ++j) {
+                const uint32_t a = st[j], b = en[j];
+                if (minutes >= a && minutes < b && act_b == -1) act_b = (int)j;
+                if (minutes < a) {
+                    act_e = (int)j;
+                    break;
+                }
+                if (j == ev_e - 1 && minutes >= a && minutes < b) act_e = (int)ev_e;
+            }
+            win[q * spd + s] = make_int2(act_b, act_e);
+        }
+    }
+    int2* d = nullptr;
+    const size_t bytes = std::max<size_t>(win.size() * sizeof(int2), 16);
+    cudaError_t e = psim_device_malloc((void**)&d, bytes);
+    if (e != cudaSuccess) return fail(c, PSIM_ERR_ALLOC, std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
+    c->allocs.push_back(d);
+    if (!win.empty()) CK(cudaMemcpyAsync(d, win.data(), win.size() * sizeof(int2), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    c->k.m.window = d;
+    return 0;
+}
+
+
 extern "C" {
 
 const char* psim_version(void) { return kVersion; }
@@ -525,6 +564,7 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
         c->h_ev_end.assign(m->ev_end, m->ev_end + ne);
         c->h_ev_duration.assign(m->ev_duration, m->ev_duration + ne);
     }
+    if ((rc = upload_window_table(c))) return bail(rc);
     if ((rc = dupload(c, &dm.len_thr, thr.data(), thr.size()))) return bail(rc);
     // agents: immutable
     DevAgents& da = k.a;
@@ -1248,23 +1288,22 @@ static int read_timeline(psim_ctx* c, std::vector<unsigned long long>& h) {
 
 // Per step of the profiled day, in microseconds (TL_COLS values): the
 // kernel's span (first block entry to last block exit), the rebuild's
-// totals, its prefix and cursors, its slots, the draws, the queue, the
-// decisions (0 where the phase did not run), and the time from the previous
-// kernel's last exit to this kernel's first entry.
-constexpr int TL_COLS = 8;
+// listing, its slots, the draws, the queue, the decisions (0 where the phase
+// did not run), and the time from the previous kernel's last exit to this
+// kernel's first entry.
+constexpr int TL_COLS = 7;
 static void step_times(psim_ctx* c, const std::vector<unsigned long long>& h, uint32_t s, float* o) {
     const unsigned long long* T = &h[PROF_T + PROF_TW * (size_t)s];
-    const unsigned long long t0 = ~T[0], r1 = T[1], r2 = T[2], r3 = T[3], drw = T[4], que = T[5], end = T[6];
-    const unsigned long long prev = s == 0 ? h[PROF_N + 1] : h[PROF_T + PROF_TW * (size_t)(s - 1) + 6];
+    const unsigned long long t0 = ~T[0], r1 = T[1], r2 = T[2], drw = T[3], que = T[4], end = T[5];
+    const unsigned long long prev = s == 0 ? h[PROF_N + 1] : h[PROF_T + PROF_TW * (size_t)(s - 1) + 5];
     auto us = [](unsigned long long a, unsigned long long b) { return b > a ? (float)((double)(b - a) * 1e-3) : 0.0f; };
     o[0] = us(t0, end);
     o[1] = r1 ? us(t0, r1) : 0.0f;
     o[2] = r2 ? us(r1, r2) : 0.0f;
-    o[3] = r3 ? us(r2, r3) : 0.0f;
-    o[4] = us(r3 ? r3 : t0, drw);
-    o[5] = que ? us(drw, que) : 0.0f;
-    o[6] = que ? us(que, end) : 0.0f;
-    o[7] = us(prev, t0);
+    o[3] = us(r2 ? r2 : t0, drw);
+    o[4] = que ? us(drw, que) : 0.0f;
+    o[5] = que ? us(que, end) : 0.0f;
+    o[6] = us(prev, t0);
 }
 
 int psim_day_kernel_ms(psim_ctx* c, float* ms) {
@@ -1277,10 +1316,10 @@ int psim_day_kernel_ms(psim_ctx* c, float* ms) {
     for (uint32_t s = 0; s < c->spd; ++s) {
         float o[TL_COLS];
         step_times(c, h, s, o);
-        ms[1] += (o[1] + o[2] + o[3]) * 1e-3f;
-        ms[2] += o[4] * 1e-3f;
-        ms[3] += (o[5] + o[6]) * 1e-3f;
-        ms[4] += o[7] * 1e-3f;
+        ms[1] += (o[1] + o[2]) * 1e-3f;
+        ms[2] += o[3] * 1e-3f;
+        ms[3] += (o[4] + o[5]) * 1e-3f;
+        ms[4] += o[6] * 1e-3f;
     }
     return 0;
 }

@@ -174,6 +174,7 @@ int upload_events(psim_ctx* c) {
     dm.ev_duration = (const uint16_t*)p;
     dm.n_events = (uint32_t)ne;
     CK(cudaStreamSynchronize(c->stream));
+    if ((rc = upload_window_table(c))) return rc;
     c->graph_dirty = true;
     return 0;
 }

@@ -107,6 +107,9 @@ int check_device_err(psim_ctx* c);
 // cudaMalloc through the allocation-failure test hook (psim_set_alloc_fault):
 // when the hook's count runs out the allocation fails without calling CUDA
 cudaError_t psim_device_malloc(void** p, size_t bytes);
+// the decisions' event windows of the current host schedule table, uploaded
+// into a new device table (DevModel::window)
+int upload_window_table(psim_ctx* c);
 
 // non-COVID hospitalization and death (psim_other_disease.cu)
 void other_disease_free(psim_ctx* c);

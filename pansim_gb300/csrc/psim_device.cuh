@@ -47,6 +47,10 @@ struct DevModel {
     const uint16_t* ev_start;
     const uint16_t* ev_end;
     const uint16_t* ev_duration;
+    // per schedule slot and step of the day, the decision's active event
+    // window (first event active at the step, first event starting after it;
+    // -1 for none), computed on the host from the schedule table
+    const int2* window;        // [n_agent_types * 28 * steps_per_day]
 };
 
 struct DevAgents {
@@ -228,11 +232,11 @@ enum {
     // maximum of complements, so one zero fill starts every slot):
     // [PROF_N] ~first block entry of the day's first movement, [PROF_N + 1]
     // its last block exit; per step s at PROF_T + PROF_TW * s: ~first block
-    // entry, the last block past the rebuild's totals, its prefix and
-    // cursors, its slots, past the draws, past the queue, last block exit
-    // (the rebuild and queue slots stay 0 at steps without that phase).
+    // entry, the last block past the rebuild's listing, past its slots, past
+    // the draws, past the queue, last block exit (the rebuild and queue
+    // slots stay 0 at steps without that phase).
     PROF_T = PROF_N + 2,
-    PROF_TW = 7,
+    PROF_TW = 6,
     PROF_WORDS = PROF_T + PROF_TW * 1440
 };
 
@@ -326,7 +330,9 @@ constexpr uint32_t BAR_TICKETS = 2;
 // finished its draws
 constexpr uint32_t BAR_INFECTIONS = BAR_TICKETS + 1440;
 constexpr uint32_t BAR_DRAWN = BAR_INFECTIONS + 1;
-constexpr uint32_t BAR_WORDS = BAR_DRAWN + 1;
+// the rebuild's listing counter (slots reserved so far)
+constexpr uint32_t BAR_LISTED = BAR_DRAWN + 1;
+constexpr uint32_t BAR_WORDS = BAR_LISTED + 1;
 // work-list segments of the decisions (blocks of the queue kernel at most)
 constexpr uint32_t WORK_MAX_BLOCKS = 152u * 64u;
 // words of the per-day mask of decision steps (1440 steps of one minute at most)

@@ -275,20 +275,13 @@ __device__ void move_decide(const KArgs& k, uint32_t i, uint32_t t, uint32_t min
         }
     }
 
-    // schedule window (AgentTypeList::getOffsetIndex, agentType.cpp:13-15)
+    // schedule window (AgentTypeList::getOffsetIndex, agentType.cpp:13-15;
+    // the window of the slot at this step, movementPolicies.h:585-603, from
+    // the table the host computed)
     const uint32_t agent_type = d.type;
     const uint32_t off_idx = 7u * wb + day + agent_type * 28u;
-    const uint32_t ev_b = k.m.event_offset[off_idx], ev_e = k.m.event_offset[off_idx + 1];
-    int act_b = -1, act_e = -1;
-    for (uint32_t j = ev_b; j < ev_e; ++j) {
-        uint32_t st = k.m.ev_start[j], en = k.m.ev_end[j];
-        if (minutes >= st && minutes < en && act_b == -1) act_b = (int)j;
-        if (minutes < st) {
-            act_e = (int)j;
-            break;
-        }
-        if (j == ev_e - 1 && minutes >= st && minutes < en) act_e = (int)ev_e;
-    }
+    const int2 win = k.m.window[(size_t)off_idx * k.spd + minutes / dt];
+    const int act_b = win.x, act_e = win.y;
 
     uint32_t new_type = NONE;
     // the quarantine rule's inputs at a location loaded with its flags
@@ -496,7 +489,12 @@ __device__ __forceinline__ void mask_clear_shared(uint32_t* s_mm) {
 }
 __device__ __forceinline__ void mask_note(const KArgs& k, uint32_t* s_mm, uint32_t m) {
     const uint32_t s = m - k.clock->t0;
-    if (s < k.spd) atomicOr(&s_mm[s >> 5], 1u << (s & 31u));
+    if (s < k.spd) {
+        // most deciders of a step land on a few steps: read before the
+        // atomic, whose lanes on one word would queue
+        const uint32_t bit = 1u << (s & 31u);
+        if (!(s_mm[s >> 5] & bit)) atomicOr(&s_mm[s >> 5], bit);
+    }
 }
 __device__ __forceinline__ void mask_flush(const KArgs& k, uint32_t* s_mm) {
     __syncthreads();
@@ -1456,52 +1454,43 @@ __device__ __forceinline__ uint32_t listed_word_count(const KArgs& k, uint32_t h
 // moves, since a move makes the next step rebuild, and a draw infects only
 // agents at a location with a nonzero sum).  The hazard mask is a superset of
 // those locations (every kernel that adds an infectious term sets the bit at
-// once); part 1 clears the bits of the locations whose sums are zero again.
-// The listed locations' agents fill the first build[5] slots, each slot with
-// its agent, susceptibility products and location.  In three parts between
-// grid barriers: 1: per block the agents at its listed locations (its range
-// of mask words); 2: the blocks before it, then the first slot (cursor) of
-// each of its locations; 3: every agent at a listed location takes a slot
-// (one returning atomic on the location's cursor, or one per location and
-// warp with agg_slot).  Returns false when a barrier expired.
-__device__ bool phase_rebuild(const KArgs& k, uint32_t* s_red, bool* s_ok, uint32_t tl) {
+// once); the listing clears the bits of the locations whose sums are zero
+// again.  The listed locations' agents fill the first *n_listed slots, each
+// slot with its agent, susceptibility products and location; the order of
+// the locations' segments is the order in which their chunks reserved them
+// (the draws do not depend on it).  In two parts between grid barriers:
+// 1 (listing): per chunk of 256 mask words of the block's range, the listed
+// locations, one atomic on the listing counter reserving the chunk's slots,
+// each location's first slot (cursor); 2 (slots): every agent at a listed
+// location takes a slot (one returning atomic on the location's cursor, or
+// one per location and warp with agg_slot).  Returns false when a barrier
+// expired.
+__device__ bool phase_rebuild(const KArgs& k, uint32_t* s_red, bool* s_ok, uint32_t tl, uint32_t* s_base,
+                              uint32_t* n_listed) {
     const uint32_t L = k.l.n, N = k.a.n;
     const uint32_t n_words = (L + 31u) >> 5;
     const uint32_t per = (n_words + gridDim.x - 1) / gridDim.x;
     const uint32_t wb = min(n_words, blockIdx.x * per), we = min(n_words, wb + per);
-    // 1 (the bits of locations whose sums are all zero again are cleared:
-    // the mask is then exactly the locations with a nonzero sum)
-    uint32_t mine = 0, locs = 0;
-    for (uint32_t w = wb + threadIdx.x; w < we; w += blockDim.x) {
-        const uint32_t hm = k.l.hmask[w];
-        if (hm) {
-            const uint32_t keep = nonzero_sum_bits(k, hm, w);
-            if (keep != hm) k.l.hmask[w] = keep;
-            mine += listed_word_count(k, keep, w);
-            locs += __popc(keep);
-        }
-    }
-    const uint32_t tot = block_sum(mine, s_red);
-    if (threadIdx.x == 0) k.l.tile_sums[blockIdx.x] = tot;
-    if (k.prof) {
-        const uint32_t nl = block_sum(locs, s_red);
-        if (threadIdx.x == 0 && (nl | tot)) {
-            atomicAdd(&k.prof[PROF_LISTED_LOCATIONS], (unsigned long long)nl);
-            atomicAdd(&k.prof[PROF_LISTED_AGENTS], (unsigned long long)tot);
-        }
-    }
-    if (!grid_barrier(k, s_ok)) return false;
-    prof_mark(k, tl + 1);
-    // 2
-    uint32_t pre = 0;
-    for (uint32_t b = threadIdx.x; b < blockIdx.x; b += blockDim.x) pre += k.l.tile_sums[b];
-    uint32_t base = block_sum(pre, s_red);
+    // 1
+    uint32_t locs = 0, agents = 0;
     for (uint32_t c0 = wb; c0 < we; c0 += blockDim.x) {  // block-uniform trips
         const uint32_t w = c0 + threadIdx.x;
         uint32_t hm = w < we ? k.l.hmask[w] : 0u;
+        if (hm) {
+            const uint32_t keep = nonzero_sum_bits(k, hm, w);
+            if (keep != hm) k.l.hmask[w] = keep;
+            hm = keep;
+        }
         const uint32_t wc = hm ? listed_word_count(k, hm, w) : 0u;
         uint32_t chunk = 0;
-        uint32_t run = base + block_scan_excl(wc, s_red, &chunk);
+        const uint32_t ex = block_scan_excl(wc, s_red, &chunk);
+        if (chunk == 0) continue;  // block-uniform
+        if (threadIdx.x == 0) *s_base = atomicAdd(&k.l.bar[BAR_LISTED], chunk);
+        __syncthreads();
+        uint32_t run = *s_base + ex;
+        __syncthreads();
+        locs += __popc(hm);
+        agents += chunk;
         while (hm) {
             const uint32_t l = w * 32u + (uint32_t)(__ffs(hm) - 1);
             hm &= hm - 1u;
@@ -1510,11 +1499,17 @@ __device__ bool phase_rebuild(const KArgs& k, uint32_t* s_red, bool* s_ok, uint3
                 run += k.l.counts[l];
             }
         }
-        base += chunk;
     }
-    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) k.l.build[5] = base;  // all blocks' entries
+    if (k.prof) {
+        const uint32_t nl = block_sum(locs, s_red);
+        if (threadIdx.x == 0 && (nl | agents)) {
+            atomicAdd(&k.prof[PROF_LISTED_LOCATIONS], (unsigned long long)nl);
+            atomicAdd(&k.prof[PROF_LISTED_AGENTS], (unsigned long long)agents);
+        }
+    }
     if (!grid_barrier(k, s_ok)) return false;
-    prof_mark(k, tl + 2);
+    prof_mark(k, tl + 1);
+    *n_listed = k.l.bar[BAR_LISTED];  // every block's reservation is in
     // 3: four consecutive agents per thread (one 16-byte load of their
     // locations), two quads in flight
     const bool one = k.m.n_variants == 1;
@@ -1559,7 +1554,14 @@ __device__ bool phase_rebuild(const KArgs& k, uint32_t* s_red, bool* s_ok, uint3
             if (pos < N) k.l.slot_loc[pos] = loc[u];
         }
     }
-    return grid_barrier(k, s_ok);
+    if (!grid_barrier(k, s_ok)) return false;
+    // every block has read the listing counter: block 0 keeps the count for
+    // the steps until the next rebuild and starts the counter at 0 for it
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        k.l.build[5] = *n_listed;
+        k.l.bar[BAR_LISTED] = 0u;
+    }
+    return true;
 }
 
 // expected-infection accumulation of the draws: one atomic per replica
@@ -1699,11 +1701,11 @@ __device__ __forceinline__ double draw_entry(const KArgs& k, uint32_t pos, uint3
 // and draws from the agent's Philox stream (seed, agent, t).  The work is the
 // listed entries, spread evenly over the grid, whatever the number of
 // locations.
-__device__ void phase_draw(const KArgs& k, uint32_t t, float season, double* s_grad, uint32_t* n_entries,
-                           uint32_t* n_hazard) {
+__device__ void phase_draw(const KArgs& k, uint32_t t, uint32_t n_listed, float season, double* s_grad,
+                           uint32_t* n_entries, uint32_t* n_hazard) {
     const uint32_t L = k.l.n, N = k.a.n;
-    const uint32_t n_listed = k.l.build[5];
     const uint32_t stride = gridDim.x * blockDim.x;
+    const bool one_rep = k.r.n == 1;
     uint32_t entries = 0, hazard = 0;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n_listed; base += stride) {  // block-uniform trips
         const uint32_t pos = base + threadIdx.x;
@@ -1719,7 +1721,7 @@ __device__ void phase_draw(const KArgs& k, uint32_t t, float season, double* s_g
             } else {
                 cnt = k.l.counts[loc];
                 wl = k.l.infectiousness[loc];
-                rep = k.l.rep[loc];
+                rep = one_rep ? 0u : k.l.rep[loc];
             }
         }
         bool any_h = false;
@@ -1762,13 +1764,17 @@ __device__ void apply_infections(const KArgs& k) {
     }
 }
 
-// Whether this block is the last to finish the step's draws (every thread
-// calls it; the block's draws are ordered before its arrival).
-__device__ __forceinline__ bool last_to_draw(const KArgs& k, bool* s_flag) {
+// Whether this block is the last to finish the step's draws among the blocks
+// that drew entries (the first ceil(n_listed / 256) of the grid; the others
+// infect nobody).  Every thread of the block calls it; the block's draws are
+// ordered before its arrival.
+__device__ __forceinline__ bool last_to_draw(const KArgs& k, uint32_t n_listed, bool* s_flag) {
+    const uint32_t drawing = (uint32_t)min((size_t)gridDim.x, ((size_t)n_listed + blockDim.x - 1) / blockDim.x);
+    if (blockIdx.x >= drawing) return false;  // block-uniform
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
-        *s_flag = atomicAdd(&k.l.bar[BAR_DRAWN], 1u) == gridDim.x - 1u;
+        *s_flag = atomicAdd(&k.l.bar[BAR_DRAWN], 1u) == drawing - 1u;
         if (*s_flag) __threadfence();
     }
     __syncthreads();
@@ -1893,7 +1899,7 @@ __global__ void __launch_bounds__(256, 4) k_step(KArgs k, uint32_t step, uint32_
     __shared__ double s_grad[GRAD_N];
     __shared__ uint32_t s_mm[MOVE_MASK_WORDS];
     __shared__ uint32_t s_red[32];
-    __shared__ uint32_t s_cnt, s_seg;
+    __shared__ uint32_t s_cnt, s_seg, s_base;
     __shared__ bool s_ok, s_last;
     const uint32_t tl = PROF_T + PROF_TW * step;  // the step's timeline slots (profiled graph)
     prof_enter(k, tl);
@@ -1906,6 +1912,7 @@ __global__ void __launch_bounds__(256, 4) k_step(KArgs k, uint32_t step, uint32_
     const uint32_t t0 = k.clock->t0;
     const float season = k.clock->season;
     const uint32_t moved = k.l.build[0], force = k.l.build[1], q_step = k.l.build[3];
+    uint32_t n_listed = k.l.build[5];  // the last rebuild's entries (this step's if it rebuilds)
     const uint32_t s1 = step + 1;
     const uint32_t mm_word = s1 < k.spd ? k.a.move_mask[s1 >> 5] : 0u;
     if (err0 & ERR_BARRIER) return;  // an earlier barrier expired
@@ -1914,8 +1921,8 @@ __global__ void __launch_bounds__(256, 4) k_step(KArgs k, uint32_t step, uint32_
         const bool rebuild = csr_decide_from(k, t, moved, force);
         if (rebuild) {
             if (k.prof && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&k.prof[PROF_REBUILDS], 1ull);
-            if (!phase_rebuild(k, s_red, &s_ok, tl)) return;
-            prof_mark(k, tl + 3);
+            if (!phase_rebuild(k, s_red, &s_ok, tl, &s_base, &n_listed)) return;
+            prof_mark(k, tl + 2);
         }
         // the step's location quarantine writes (decisions of step t)
         if (k.p.quarantine_policy > 1 && q_step == t) merge_quarantine(k);
@@ -1923,7 +1930,7 @@ __global__ void __launch_bounds__(256, 4) k_step(KArgs k, uint32_t step, uint32_
     if (phases & PH_DRAW) {
         grad_begin(k, s_grad);
         uint32_t entries = 0, hazard = 0;
-        phase_draw(k, t, season, s_grad, &entries, &hazard);
+        phase_draw(k, t, n_listed, season, s_grad, &entries, &hazard);
         if (k.prof) {
             entries = __reduce_add_sync(0xffffffffu, entries);
             hazard = __reduce_add_sync(0xffffffffu, hazard);
@@ -1934,8 +1941,8 @@ __global__ void __launch_bounds__(256, 4) k_step(KArgs k, uint32_t step, uint32_
         }
         grad_end(k, s_grad);
         // the infections' sum changes, once every draw of the step is done
-        if (last_to_draw(k, &s_last)) apply_infections(k);
-        prof_mark(k, tl + 4);
+        if (last_to_draw(k, n_listed, &s_last)) apply_infections(k);
+        prof_mark(k, tl + 3);
     }
     const bool decides = (k.p.enable_curfew && k.p.curfew_begin == s1) || ((mm_word >> (s1 & 31u)) & 1u) != 0;
     if ((phases & PH_DECIDE) && s1 < k.spd && decides) {
@@ -1945,13 +1952,13 @@ __global__ void __launch_bounds__(256, 4) k_step(KArgs k, uint32_t step, uint32_
             if (n) atomicAdd(&k.prof[PROF_MOVERS], (unsigned long long)n);
             if (blockIdx.x == 0) atomicAdd(&k.prof[PROF_QUEUE_STEPS], 1ull);
         }
-        prof_mark(k, tl + 5);
+        prof_mark(k, tl + 4);
         // every draw and every block's queue before any decision
         if (!grid_barrier(k, &s_ok)) return;
         phase_decide(k, step, cap, s_mm, &s_seg);
         mask_flush(k, s_mm);
     }
-    prof_mark(k, tl + 6);
+    prof_mark(k, tl + 5);
 }
 
 // Canonical CSR order (ascending agent id inside a location, the output of

@@ -310,10 +310,10 @@ class GpuSim:
 
     def day_timeline(self):
         """Per step of the last profiled day (rows), microseconds: the step
-        kernel's span, its rebuild's totals, prefix and cursors, slots, the
-        draws, the queue, the decisions (0 where the phase did not run), the
-        time since the previous kernel ended."""
-        us = np.zeros((self.snap.steps_per_day, 8), np.float32)
+        kernel's span, its rebuild's listing and slots, the draws, the queue,
+        the decisions (0 where the phase did not run), the time since the
+        previous kernel ended."""
+        us = np.zeros((self.snap.steps_per_day, 7), np.float32)
         self._ck(lib().psim_day_timeline(self.h, _p(us)), "day_timeline")
         return us
 

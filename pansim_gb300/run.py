@@ -7,8 +7,8 @@ Prints the daily statistics row (the reference's TSV columns,
 simulation.h:754) and the wall time.  --steps runs the timesteps of day 0
 one psim_step call at a time (no graph), which is the form used for kernel
 profiles.  --timeline FILE runs the days with the kernels' timeline stamps
-and writes, per day and step, the step kernel's span, the rebuild's totals,
-prefix and slots, the draws, the queue, the decisions and the time since the
+and writes, per day and step, the step kernel's span, the rebuild's listing
+and slots, the draws, the queue, the decisions and the time since the
 previous kernel (us, tab-separated), with the day's counters.
 """
 import argparse
@@ -45,8 +45,7 @@ def main(argv=None):
     tl_out = open(a.timeline, "w") if a.timeline else None
     if tl_out:
         g.set_profiling(True)
-        tl_out.write("day\tstep\tspan_us\treb_totals_us\treb_prefix_us\treb_slots_us\tdraw_us\tqueue_us\t"
-                     "decide_us\tgap_us\n")
+        tl_out.write("day\tstep\tspan_us\treb_listing_us\treb_slots_us\tdraw_us\tqueue_us\tdecide_us\tgap_us\n")
     t0 = time.perf_counter()
     for d in range(a.days):
         st = g.run_day(d)

@@ -193,11 +193,11 @@ def test_profiled_graph_same_results_and_kernel_times(gpu_lib):
         assert 0 < listed_locs <= listed_agents < rebuilds * 12000 and entries >= listed_agents
         # per step: spans, the steps that rebuilt and queued, the gaps
         tl = g.day_timeline()
-        assert tl.shape == (144, 8) and (tl >= 0).all()
+        assert tl.shape == (144, 7) and (tl >= 0).all()
         assert (tl[:, 0] > 0).all()
-        assert rebuilds - 2 <= (tl[:, 1:4].sum(axis=1) > 0).sum() <= rebuilds
-        assert queues - 2 <= (tl[:, 6] > 0).sum() <= queues
-        assert (tl[:, 0].sum() + tl[:, 7].sum()) * 1e-3 <= g.last_day_ms() * 1.01
+        assert rebuilds - 2 <= (tl[:, 1:3].sum(axis=1) > 0).sum() <= rebuilds
+        assert queues - 2 <= (tl[:, 5] > 0).sum() <= queues
+        assert (tl[:, 0].sum() + tl[:, 6].sum()) * 1e-3 <= g.last_day_ms() * 1.01
     g.set_profiling(False)
     assert stats_rows(o.run_day(2)) == stats_rows(g.run_day(2))
     g.download()
