@@ -579,18 +579,15 @@ __device__ __forceinline__ bool count_agent(const KArgs& k, bool act, uint32_t l
 }
 
 // Within a day the per-location sums persist: an agent changes them only
-// when it moves or its infectiousness changes (a draw that infects), and the
-// scan recomputes the hazards of the locations marked dirty (the sum mask)
-// only.  The first step of a day (k_movement after a reset of the sums and
-// a mark on every location) adds every agent's term afresh.
-__device__ __forceinline__ void mark_dirty(const KArgs& k, uint32_t loc) {
-    atomicOr(&k.l.smask[loc >> 5], 1u << (loc & 31u));
-}
-
-// The agent went from (loc0, inf0, var0) to (loc, inf, var): its count moves,
-// its fixed-point term leaves (loc0, var0) and joins (loc, var).  A count
-// change alone marks a location only if its sum is nonzero (else its hazard
-// is 0 whatever the count).  Returns whether the agent took a new location.
+// when it moves or its infectiousness changes (a draw that infects).  The
+// first step of a day (k_movement after a reset of the sums) adds every
+// agent's term afresh.
+// The agent went from (loc0, inf0, var0) to (loc, inf, var) in a step
+// kernel's decision: its count moves, its fixed-point term leaves (loc0,
+// var0) and joins (loc, var).  The step kernel computes every ratio from the
+// sums, so it keeps no dirty marks (the day graph marks every location dirty
+// at its start: a scan after it recomputes every ratio).  Returns whether the
+// agent took a new location.
 __device__ __forceinline__ bool count_agent_delta(const KArgs& k, bool act, uint32_t loc0, uint32_t loc, float inf0,
                                                   uint32_t var0, float inf, uint32_t var) {
     const uint32_t L = k.l.n;
@@ -600,26 +597,16 @@ __device__ __forceinline__ bool count_agent_delta(const KArgs& k, bool act, uint
     }
     const bool mv = act && loc != loc0;
     if (mv) {
-        if (loc0 < L) {
-            atomicSub(&k.l.counts[loc0], 1u);
-            if ((k.l.hmask[loc0 >> 5] >> (loc0 & 31u)) & 1u) mark_dirty(k, loc0);
-        }
-        if (loc != NONE) {
-            atomicAdd(&k.l.counts[loc], 1u);
-            if ((k.l.hmask[loc >> 5] >> (loc & 31u)) & 1u) mark_dirty(k, loc);
-        }
+        if (loc0 < L) atomicSub(&k.l.counts[loc0], 1u);
+        if (loc != NONE) atomicAdd(&k.l.counts[loc], 1u);
     }
     if (act) {
         const long long q0 = (loc0 < L && inf0 > 0.0f) ? __float2ll_rn(inf0 * PSIM_FIX_SCALE_F) : 0ll;
         const long long q1 = (loc != NONE && inf > 0.0f) ? __float2ll_rn(inf * PSIM_FIX_SCALE_F) : 0ll;
         if (mv || q0 != q1 || var0 != var) {
-            if (q0) {
-                atomicAdd(&k.l.sfix[(size_t)var0 * L + loc0], (unsigned long long)(-q0));
-                mark_dirty(k, loc0);
-            }
+            if (q0) atomicAdd(&k.l.sfix[(size_t)var0 * L + loc0], (unsigned long long)(-q0));
             if (q1) {
                 atomicAdd(&k.l.sfix[(size_t)var * L + loc], (unsigned long long)q1);
-                mark_dirty(k, loc);
                 mark_hazardous(k, loc);
             }
         }
@@ -1747,13 +1734,9 @@ __device__ void apply_infections(const KArgs& k) {
         const uint32_t var0 = e.w & 0xFFu, var = (e.w >> 8) & 0xFFu;
         const long long q0 = inf0 > 0.0f ? __float2ll_rn(inf0 * PSIM_FIX_SCALE_F) : 0ll;
         const long long q1 = inf > 0.0f ? __float2ll_rn(inf * PSIM_FIX_SCALE_F) : 0ll;
-        if (q0) {
-            atomicAdd(&k.l.sfix[(size_t)var0 * L + loc], (unsigned long long)(-q0));
-            mark_dirty(k, loc);
-        }
+        if (q0) atomicAdd(&k.l.sfix[(size_t)var0 * L + loc], (unsigned long long)(-q0));
         if (q1) {
             atomicAdd(&k.l.sfix[(size_t)var * L + loc], (unsigned long long)q1);
-            mark_dirty(k, loc);
             mark_hazardous(k, loc);
         }
     }
