@@ -342,9 +342,12 @@ int capture_day_graph(psim_ctx* c) {
     if (me == cudaSuccess) me = cudaMemsetAsync(c->k.l.bar, 0, sizeof(uint32_t) * BAR_WORDS, c->stream);
     if (me == cudaSuccess && c->profile) me = cudaMemsetAsync(c->d_prof, 0, sizeof(unsigned long long) * PROF_WORDS, c->stream);
     launch_movement(c->k, 0, c->stream);
-    // Per step: one launch of the step kernel (rebuild, draws, decisions for
-    // the next step, with grid barriers inside); the profiled graph is the
-    // same launches with the kernels' timeline stamps.
+    // Per timestep one launch of the step kernel (rebuild, draws, decisions
+    // for the next timestep, grid barriers between its phases); the profiled
+    // graph is the same launches with the kernel's timeline stamps.  (One
+    // launch for the whole day, grid barriers between the timesteps,
+    // measured slower: a barrier takes longer than the gap between two
+    // kernel nodes of the graph.)
     for (uint32_t s = 0; s < c->spd; ++s) launch_step(c->k, s, PH_ALL, c->stream);
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     if (e == cudaSuccess && me != cudaSuccess) {
@@ -355,7 +358,7 @@ int capture_day_graph(psim_ctx* c) {
     e = cudaGraphInstantiate(&c->day_graph, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(c, PSIM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
-    // movement(0) and one step kernel per step
+    // movement(0) and one step kernel per timestep
     c->graph_kernels = 1 + (uint64_t)c->spd;
     c->graph_dirty = false;
     c->prof_valid = false;

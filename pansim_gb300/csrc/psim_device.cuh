@@ -319,10 +319,11 @@ void launch_scan(const KArgs& k, uint32_t step_in_day, int with_hazard, int merg
 void launch_scatter_draw(const KArgs& k, uint32_t step_in_day, int scatter, int draw, cudaStream_t s);
 void launch_offsets(const KArgs& k, cudaStream_t s);
 int scan_kernels(const KArgs& k);
-// the day graph's step kernel (psim_kernels.cu, k_step): the phases of one
-// launch (the profiled day graph launches them separately)
+// the step kernel (psim_kernels.cu, k_step): the phases a launch runs, and
+// launches of one timestep or of a range of timesteps (grid barriers between)
 constexpr uint32_t PH_REBUILD = 1u, PH_DRAW = 2u, PH_DECIDE = 4u, PH_ALL = 7u;
 void launch_step(const KArgs& k, uint32_t step_in_day, uint32_t phases, cudaStream_t s);
+void launch_steps(const KArgs& k, uint32_t step0, uint32_t nsteps, uint32_t phases, cudaStream_t s);
 void launch_time_shift(uint32_t* a, uint32_t n, uint32_t delta, cudaStream_t s);
 // words of the barrier array: two for the barrier, one ticket per step
 constexpr uint32_t BAR_TICKETS = 2;

@@ -1274,35 +1274,34 @@ __global__ void __launch_bounds__(256) k_scatter_draw(KArgs k, uint32_t step, in
 // a persistent grid (every block resident; see launch_step) whose phases are
 // separated by grid barriers only where one phase needs another's results:
 //   rebuild   only when agents took new locations for t (or a rebuild is
-//             pending): per-block sums of the histogram | the prefix into
-//             the locations' first slots | every agent takes a slot at its
-//             location, and the slot keeps the agent's susceptibility x
-//             age-band factor of every variant.  The step's location
+//             pending): the locations with a nonzero sum listed and their
+//             segments reserved | every agent at a listed location takes a
+//             slot, which keeps its id, its susceptibility x age-band factor
+//             of every variant and its location.  The step's location
 //             quarantine writes are merged here too (or alone when there were
 //             some but no rebuild).
-//   draw      the per-location infection ratio and the infection draws,
-//             location by location over the locations with an infectious
-//             agent, from the agent list (LocationsList::infectAgents,
-//             locationList.h:233-310, with the ratio of
-//             BasicInfection::infectionsAtLocations,
-//             infectionPolicies.h:520-546)
-//   decide    only when some agent decides at s + 1 (move_at == t + 1, or
-//             everyone at the curfew step): the block queues its own agents
-//             that decide | doMovement of the queued agents for s + 1 (work
-//             segments taken in turn) and the histogram and sum deltas of
-//             their moves
+//   draw      every listed entry, one per thread: the location's infection
+//             ratio from its sum and the agent's draws (LocationsList::
+//             infectAgents, locationList.h:233-310); the infections' sum
+//             changes are applied once every draw of t is done
+//   decide    only when some agent decides at s + 1 (or everyone at the
+//             curfew step): the block queues its own agents that decide |
+//             doMovement of the queued agents for s + 1 (work segments taken
+//             in turn) and the histogram and sum deltas of their moves
 // A step at which nobody takes a new location and nobody decides next runs
-// the draw alone, without a barrier: its cost is the agents at the
-// infectious locations, not the whole population.
+// the draw alone, without a barrier: its cost is the listed entries, not the
+// whole population.
 
 // Grid barrier of the persistent step kernel: the last block to arrive
-// resets the count and advances the generation the others wait on.  Every
-// wait is bounded: on expiry the block records ERR_BARRIER and returns false,
-// and every later barrier and step kernel returns at once, so a failure ends
-// in an error report, never a hang.
-// The block's writes reach the other blocks through the arrival (release:
-// the block's threads' writes are ordered before it by the __syncthreads
-// before) and the generation read (acquire).
+// resets the count and advances the generation the others wait on (a
+// two-level arrival, 8 groups then the grid, measured slower: the second
+// atomic round trip costs more than the serialized arrivals it saves).
+// Every wait is bounded: on expiry the block records ERR_BARRIER and returns
+// false, and every later barrier and step kernel returns at once, so a
+// failure ends in an error report, never a hang.  The block's writes reach
+// the other blocks through the arrival (release: the block's threads' writes
+// are ordered before it by the __syncthreads before) and the generation read
+// (acquire).
 constexpr uint32_t BARRIER_SPIN_LIMIT = 1u << 24;
 __device__ __forceinline__ uint32_t ld_acquire_gpu(const uint32_t* p) {
     uint32_t v;
@@ -1876,21 +1875,27 @@ __device__ void phase_decide(const KArgs& k, uint32_t step, uint32_t cap, uint32
     publish_moved(k, moved, c.t);
 }
 
-// The step kernel: see the section comment.  cap = the work-list segment
+// Block-shared scratch of the step kernel.
+struct StepShared {
+    double grad[GRAD_N];
+    uint32_t mm[MOVE_MASK_WORDS];
+    uint32_t red[32];
+    uint32_t cnt, seg, base;
+    bool ok, last;
+};
+
+// One timestep of the step kernel (see the section comment); false when a
+// grid barrier expired (the kernel then ends).  cap = the work-list segment
 // size of a block.
-__global__ void __launch_bounds__(256, 4) k_step(KArgs k, uint32_t step, uint32_t phases, uint32_t cap) {
-    __shared__ double s_grad[GRAD_N];
-    __shared__ uint32_t s_mm[MOVE_MASK_WORDS];
-    __shared__ uint32_t s_red[32];
-    __shared__ uint32_t s_cnt, s_seg, s_base;
-    __shared__ bool s_ok, s_last;
+__device__ __forceinline__ bool step_body(const KArgs& k, uint32_t step, uint32_t phases, uint32_t cap,
+                                          StepShared& sh) {
     const uint32_t tl = PROF_T + PROF_TW * step;  // the step's timeline slots (profiled graph)
     prof_enter(k, tl);
     // the words the step's phases start from, loaded together: the error
     // flags, the clock, the rebuild words (a block that starts after block 0
     // turned BUILD_PENDING into t decides the same), the step of the last
     // quarantine writes, the decision-mask word of the next step (the
-    // decisions of this launch mark later steps only)
+    // decisions of this step mark later steps only)
     const uint32_t err0 = *((volatile uint32_t*)k.err);
     const uint32_t t0 = k.clock->t0;
     const float season = k.clock->season;
@@ -1898,22 +1903,22 @@ __global__ void __launch_bounds__(256, 4) k_step(KArgs k, uint32_t step, uint32_
     uint32_t n_listed = k.l.build[5];  // the last rebuild's entries (this step's if it rebuilds)
     const uint32_t s1 = step + 1;
     const uint32_t mm_word = s1 < k.spd ? k.a.move_mask[s1 >> 5] : 0u;
-    if (err0 & ERR_BARRIER) return;  // an earlier barrier expired
+    if (err0 & ERR_BARRIER) return false;  // an earlier barrier expired
     const uint32_t t = t0 + step;
     if (phases & PH_REBUILD) {
         const bool rebuild = csr_decide_from(k, t, moved, force);
         if (rebuild) {
             if (k.prof && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&k.prof[PROF_REBUILDS], 1ull);
-            if (!phase_rebuild(k, s_red, &s_ok, tl, &s_base, &n_listed)) return;
+            if (!phase_rebuild(k, sh.red, &sh.ok, tl, &sh.base, &n_listed)) return false;
             prof_mark(k, tl + 2);
         }
         // the step's location quarantine writes (decisions of step t)
         if (k.p.quarantine_policy > 1 && q_step == t) merge_quarantine(k);
     }
     if (phases & PH_DRAW) {
-        grad_begin(k, s_grad);
+        grad_begin(k, sh.grad);
         uint32_t entries = 0, hazard = 0;
-        phase_draw(k, t, n_listed, season, s_grad, &entries, &hazard);
+        phase_draw(k, t, n_listed, season, sh.grad, &entries, &hazard);
         if (k.prof) {
             entries = __reduce_add_sync(0xffffffffu, entries);
             hazard = __reduce_add_sync(0xffffffffu, hazard);
@@ -1922,26 +1927,38 @@ __global__ void __launch_bounds__(256, 4) k_step(KArgs k, uint32_t step, uint32_
                 atomicAdd(&k.prof[PROF_DRAW_HAZARD], (unsigned long long)hazard);
             }
         }
-        grad_end(k, s_grad);
+        grad_end(k, sh.grad);
         // the infections' sum changes, once every draw of the step is done
-        if (last_to_draw(k, n_listed, &s_last)) apply_infections(k);
+        if (last_to_draw(k, n_listed, &sh.last)) apply_infections(k);
         prof_mark(k, tl + 3);
     }
     const bool decides = (k.p.enable_curfew && k.p.curfew_begin == s1) || ((mm_word >> (s1 & 31u)) & 1u) != 0;
     if ((phases & PH_DECIDE) && s1 < k.spd && decides) {
-        mask_clear_shared(s_mm);
-        const uint32_t n = phase_queue(k, step + 1, cap, &s_cnt);
+        mask_clear_shared(sh.mm);
+        const uint32_t n = phase_queue(k, step + 1, cap, &sh.cnt);
         if (k.prof && threadIdx.x == 0) {
             if (n) atomicAdd(&k.prof[PROF_MOVERS], (unsigned long long)n);
             if (blockIdx.x == 0) atomicAdd(&k.prof[PROF_QUEUE_STEPS], 1ull);
         }
         prof_mark(k, tl + 4);
         // every draw and every block's queue before any decision
-        if (!grid_barrier(k, &s_ok)) return;
-        phase_decide(k, step, cap, s_mm, &s_seg);
-        mask_flush(k, s_mm);
+        if (!grid_barrier(k, &sh.ok)) return false;
+        phase_decide(k, step, cap, sh.mm, &sh.seg);
+        mask_flush(k, sh.mm);
     }
     prof_mark(k, tl + 5);
+    return true;
+}
+
+// The step kernel: timesteps step0 .. step0 + nsteps - 1, a grid barrier
+// between two (the day graph runs a whole day in one launch).
+__global__ void __launch_bounds__(256, 4) k_step(KArgs k, uint32_t step0, uint32_t nsteps, uint32_t phases,
+                                                 uint32_t cap) {
+    __shared__ StepShared sh;
+    for (uint32_t j = 0; j < nsteps; ++j) {
+        if (!step_body(k, step0 + j, phases, cap, sh)) return;
+        if (j + 1 < nsteps && !grid_barrier(k, &sh.ok)) return;
+    }
 }
 
 // Canonical CSR order (ascending agent id inside a location, the output of
@@ -2652,12 +2669,13 @@ static void step_geometry(const KArgs& k, unsigned* grid, uint32_t* cap) {
     const size_t quads = ((size_t)k.a.n + 3) / 4;
     *cap = (uint32_t)(((quads + (size_t)g * 256 - 1) / ((size_t)g * 256)) * 1024);
 }
-void launch_step(const KArgs& k, uint32_t step, uint32_t phases, cudaStream_t s) {
+void launch_steps(const KArgs& k, uint32_t step0, uint32_t nsteps, uint32_t phases, cudaStream_t s) {
     unsigned g;
     uint32_t cap;
     step_geometry(k, &g, &cap);
-    k_step<<<g, 256, 0, s>>>(k, step, phases, cap);
+    k_step<<<g, 256, 0, s>>>(k, step0, nsteps, phases, cap);
 }
+void launch_step(const KArgs& k, uint32_t step, uint32_t phases, cudaStream_t s) { launch_steps(k, step, 1, phases, s); }
 void launch_count(const KArgs& k, cudaStream_t s) { k_count<<<grid_for(k.a.n, 8), 256, 0, s>>>(k); }
 // the scan of the histogram with 256 x tune.scan_items locations per tile:
 // single pass with decoupled look-back (tune.scan_mode 0) or tile sums, then
