@@ -140,11 +140,6 @@ __device__ bool quarantine_agent(const KArgs& k, uint32_t i, uint32_t t, uint32_
 // an unsigned char, so a difference that went negative folds modulo 256 hours
 __device__ __forceinline__ uint32_t td_minutes(uint32_t mins) { return (uint32_t)(uint8_t)(mins / 60u) * 60u + mins % 60u; }
 
-__device__ __forceinline__ bool is_quarantine_type(const KArgs& k, uint32_t loc) {
-    uint32_t ty = loc_type(k, loc);
-    return ty == k.p.home_type || ty == k.p.school_type || ty == k.p.classroom_type || ty == k.p.work_type;
-}
-
 __device__ void diagnose_and_quarantine(const KArgs& k, uint32_t i, uint32_t t, uint32_t sum, psim_stream* rng) {
     const uint32_t dt = k.p.time_step;
     k.a.diagnosed[i] = 1;
@@ -440,11 +435,10 @@ __device__ __forceinline__ unsigned lanemask_lt() {
     return m;
 }
 
-// Hazard of variant 0 at `loc` and whether an infectious agent is there (the
-// scan computed the location's hazards this step; elsewhere every hazard is
-// 0): the hazard itself is gathered only at infectious locations.  The mask
-// is read with a plain load, not the read-only path: in the day graph the
-// scan rewrites it while the hot kernel runs beside it.
+// Hazard of variant 0 at `loc` and whether an infectious agent is there, for
+// the agent-ordered draws of the per-phase entry points (the scan computed
+// the location's hazards this step; elsewhere every hazard is 0): the hazard
+// itself is gathered only at infectious locations.
 __device__ __forceinline__ float hazard_at(const KArgs& k, uint32_t loc, bool* any) {
     const uint32_t w = k.l.hmask[loc >> 5];
     *any = ((w >> (loc & 31u)) & 1u) != 0;
@@ -501,9 +495,6 @@ __device__ __forceinline__ void mask_flush(const KArgs& k, uint32_t* s_mm) {
     for (uint32_t w = threadIdx.x; w < MOVE_MASK_WORDS; w += blockDim.x)
         if (s_mm[w]) atomicOr(&k.a.move_mask[w], s_mm[w]);
 }
-__device__ __forceinline__ bool mask_has(const KArgs& k, uint32_t s) {
-    return s < k.spd && ((k.a.move_mask[s >> 5] >> (s & 31u)) & 1u) != 0;
-}
 
 // doMovement for agent i at step c.t; s = its countdown before the step
 // (move_at - c.t).  Writes move_at when the agent decides or the curfew
@@ -544,10 +535,9 @@ __device__ __forceinline__ uint32_t move_agent(const KArgs& k, uint32_t i, const
 constexpr int SCAN_THREADS = 256;
 
 // A location that receives an infectious term sets its hazard-mask bit at
-// once; the next scan recomputes the bit from the sums.  Between the two the
-// mask is a superset of the infectious locations, which is what the hot
-// kernel reads while the scan runs beside it (a location whose sum is zero
-// has hazard 0 after the scan, so an agent queued there draws nothing).
+// once, so the mask is always a superset of the locations with a nonzero sum
+// (the step kernel's rebuild lists from it and clears the bits of zero sums;
+// the per-phase scans recompute the bits of their dirty locations).
 __device__ __forceinline__ void mark_hazardous(const KArgs& k, uint32_t loc) {
     atomicOr(&k.l.hmask[loc >> 5], 1u << (loc & 31u));
 }
