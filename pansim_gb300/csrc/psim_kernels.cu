@@ -1397,31 +1397,38 @@ __device__ __forceinline__ uint32_t block_scan_excl(uint32_t v, uint32_t* s_red,
     return woff + x - v;
 }
 
-// the set bits of mask word w whose location has a nonzero sum of some variant
-__device__ __forceinline__ uint32_t nonzero_sum_bits(const KArgs& k, uint32_t hm, uint32_t w) {
+// the set bits of mask word w whose location has a nonzero sum of some
+// variant (returned) and the agents at those locations (*agents); the loads of
+// four set bits at a time are issued together
+__device__ __forceinline__ uint32_t nonzero_sum_bits(const KArgs& k, uint32_t hm, uint32_t w, uint32_t* agents) {
     const uint32_t L = k.l.n, V = k.m.n_variants;
-    uint32_t keep = 0, rest = hm;
+    uint32_t keep = 0, rest = hm, cnt = 0;
     while (rest) {
-        const uint32_t b = (uint32_t)(__ffs(rest) - 1);
-        rest &= rest - 1u;
-        const uint32_t l = w * 32u + b;
-        if (l >= L) continue;
-        bool nz = false;
-        for (uint32_t v = 0; v < V && !nz; ++v) nz = k.l.sfix[(size_t)v * L + l] != 0ull;
-        if (nz) keep |= 1u << b;
+        uint32_t b[4], l[4];
+        unsigned long long f[4];
+        uint32_t c[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            b[u] = rest ? (uint32_t)(__ffs(rest) - 1) : 32u;
+            if (rest) rest &= rest - 1u;
+            l[u] = b[u] < 32u ? w * 32u + b[u] : NONE;
+            const bool in = l[u] < L;
+            f[u] = in ? k.l.sfix[l[u]] : 0ull;
+            c[u] = in ? k.l.counts[l[u]] : 0u;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (l[u] >= L) continue;
+            bool nz = f[u] != 0ull;
+            for (uint32_t v = 1; v < V && !nz; ++v) nz = k.l.sfix[(size_t)v * L + l[u]] != 0ull;
+            if (nz) {
+                keep |= 1u << b[u];
+                cnt += c[u];
+            }
+        }
     }
+    *agents = cnt;
     return keep;
-}
-
-// the agents at the listed locations of mask word w (its set bits)
-__device__ __forceinline__ uint32_t listed_word_count(const KArgs& k, uint32_t hm, uint32_t w) {
-    uint32_t c = 0;
-    while (hm) {
-        const uint32_t l = w * 32u + (uint32_t)(__ffs(hm) - 1);
-        hm &= hm - 1u;
-        if (l < k.l.n) c += k.l.counts[l];
-    }
-    return c;
 }
 
 // Rebuild of the agent list.  Only the locations with a nonzero sum are
@@ -1452,12 +1459,12 @@ __device__ bool phase_rebuild(const KArgs& k, uint32_t* s_red, bool* s_ok, uint3
     for (uint32_t c0 = wb; c0 < we; c0 += blockDim.x) {  // block-uniform trips
         const uint32_t w = c0 + threadIdx.x;
         uint32_t hm = w < we ? k.l.hmask[w] : 0u;
+        uint32_t wc = 0;
         if (hm) {
-            const uint32_t keep = nonzero_sum_bits(k, hm, w);
+            const uint32_t keep = nonzero_sum_bits(k, hm, w, &wc);
             if (keep != hm) k.l.hmask[w] = keep;
             hm = keep;
         }
-        const uint32_t wc = hm ? listed_word_count(k, hm, w) : 0u;
         uint32_t chunk = 0;
         const uint32_t ex = block_scan_excl(wc, s_red, &chunk);
         if (chunk == 0) continue;  // block-uniform
