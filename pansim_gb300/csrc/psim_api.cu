@@ -279,6 +279,7 @@ int upload_mutable(psim_ctx* c, const psim_agents* a, const psim_locations* l) {
 // (k_movement, k_count): the first step of each day and the regroups.
 int reset_sums(psim_ctx* c) {
     CK(cudaMemsetAsync(c->k.l.sfix, 0, sizeof(unsigned long long) * c->L * c->V, c->stream));
+    CK(cudaMemsetAsync(c->k.l.sfix_b, 0, sizeof(unsigned long long) * c->L * c->V, c->stream));
     CK(cudaMemsetAsync(c->k.l.smask, 0xFF, sizeof(uint32_t) * (((size_t)c->L + 2047) / 2048 * 64 + 64), c->stream));
     return 0;
 }
@@ -335,6 +336,7 @@ int capture_day_graph(psim_ctx* c) {
     // agent list rebuilt (its slots take the susceptibilities the midnight
     // phases left), the mask of decision steps recomputed from every agent.
     cudaError_t me = cudaMemsetAsync(c->k.l.sfix, 0, sizeof(unsigned long long) * c->L * c->V, c->stream);
+    if (me == cudaSuccess) me = cudaMemsetAsync(c->k.l.sfix_b, 0, sizeof(unsigned long long) * c->L * c->V, c->stream);
     if (me == cudaSuccess)
         me = cudaMemsetAsync(c->k.l.smask, 0xFF, sizeof(uint32_t) * (((size_t)c->L + 2047) / 2048 * 64 + 64), c->stream);
     if (me == cudaSuccess) me = cudaMemsetAsync(c->k.a.move_mask, 0, sizeof(uint32_t) * MOVE_MASK_WORDS, c->stream);
@@ -349,6 +351,11 @@ int capture_day_graph(psim_ctx* c) {
     // measured slower: a barrier takes longer than the gap between two
     // kernel nodes of the graph.)
     for (uint32_t s = 0; s < c->spd; ++s) launch_step(c->k, s, PH_ALL, c->stream);
+    // the day's final sums are in the copy its next step would read: with an
+    // odd number of steps that is the second one
+    if (me == cudaSuccess && (c->spd & 1u))
+        me = cudaMemcpyAsync(c->k.l.sfix, c->k.l.sfix_b, sizeof(unsigned long long) * c->L * c->V,
+                             cudaMemcpyDeviceToDevice, c->stream);
     cudaError_t e = cudaStreamEndCapture(c->stream, &g);
     if (e == cudaSuccess && me != cudaSuccess) {
         cudaGraphDestroy(g);
@@ -638,10 +645,11 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     if ((rc = dalloc(c, &dl.cursor, L))) return bail(rc);
     if ((rc = dalloc(c, &dl.csr_agents, N))) return bail(rc);
     if ((rc = dalloc(c, &dl.slot_loc, N))) return bail(rc);
-    if ((rc = dalloc(c, &dl.inf_pending, N))) return bail(rc);
+    if ((rc = dalloc(c, &dl.inf_pending, 3 * N))) return bail(rc);
     if ((rc = dalloc(c, &dl.slot_su, N * V))) return bail(rc);
     if ((rc = dalloc(c, &dl.qu_pending, L))) return bail(rc);
     if ((rc = dalloc(c, &dl.sfix, L * V))) return bail(rc);
+    if ((rc = dalloc(c, &dl.sfix_b, L * V))) return bail(rc);
     if ((rc = dalloc(c, &dl.hazard, L * V))) return bail(rc);
     if ((rc = dalloc(c, &dl.hazard_x, L * V))) return bail(rc);
     if ((rc = dalloc(c, &dl.hmask, ((size_t)L + 2047) / 2048 * 64 + 64))) return bail(rc);
@@ -1390,6 +1398,10 @@ int psim_time_step_kernels(psim_ctx* c, uint32_t t, float* ms) {
     CK(cudaEventRecord(ev[3], c->stream));
     launch_step(c->k, step + 1, PH_REBUILD | PH_DRAW, c->stream);
     c->launches += 5;
+    // the sums as the step after them reads them, in the first copy
+    if ((step + 2) & 1u)
+        CK(cudaMemcpyAsync(c->k.l.sfix, c->k.l.sfix_b, sizeof(unsigned long long) * c->L * c->V,
+                           cudaMemcpyDeviceToDevice, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     for (int j = 0; j < 3; ++j) CK(cudaEventElapsedTime(&ms[j], ev[j], ev[j + 1]));
     for (int j = 0; j < 4; ++j) cudaEventDestroy(ev[j]);

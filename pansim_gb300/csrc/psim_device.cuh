@@ -133,6 +133,8 @@ struct DevLocs {
                                   // to the variant times its age band's factor
     uint32_t* qu_pending;         // quarantine writes of the running step
     unsigned long long* sfix;     // [V][n] fixed-point infectiousness sums
+    unsigned long long* sfix_b;   // [V][n] the step kernel's second copy: even steps of the day
+                                  // read sfix, odd steps sfix_b (see k_step)
     float* hazard;                // [V][n] infection ratio of the last step
     uint32_t* hmask;              // bit l: some variant's hazard at location l is > 0
     uint32_t* smask;              // bit l: some variant's fixed-point sum at l received a term this step
@@ -145,8 +147,8 @@ struct DevLocs {
                                   // per-step decision tickets ([BAR_TICKETS + step]), the
                                   // deferred infections and the blocks past the draws
     uint32_t* slot_loc;           // [N] the location of each agent-list slot the step kernel listed
-    uint4* inf_pending;           // [N] the step's deferred infections (location, infectiousness
-                                  // before and after, variants)
+    uint4* inf_pending;           // [3][N] the infections of a step (location, infectiousness
+                                  // before and after, variants), in list step % 3
     uint64_t* scan_status;        // per-tile status words of the single-pass scan (epoch | flag | value)
     uint32_t* scan_state;         // [0] epoch of the next single-pass scan, [1] its tile ticket
     uint32_t* build;              // [0] timestamp at which agents last took new locations,
@@ -327,12 +329,10 @@ void launch_steps(const KArgs& k, uint32_t step0, uint32_t nsteps, uint32_t phas
 void launch_time_shift(uint32_t* a, uint32_t n, uint32_t delta, cudaStream_t s);
 // words of the barrier array: two for the barrier, one ticket per step
 constexpr uint32_t BAR_TICKETS = 2;
-// after the tickets: the step's deferred infections and the blocks that
-// finished its draws
+// after the tickets: the infections of the steps in lists 0-2 (step % 3)
 constexpr uint32_t BAR_INFECTIONS = BAR_TICKETS + 1440;
-constexpr uint32_t BAR_DRAWN = BAR_INFECTIONS + 1;
 // the rebuild's listing counter (slots reserved so far)
-constexpr uint32_t BAR_LISTED = BAR_DRAWN + 1;
+constexpr uint32_t BAR_LISTED = BAR_INFECTIONS + 3;
 constexpr uint32_t BAR_WORDS = BAR_LISTED + 1;
 // work-list segments of the decisions (blocks of the queue kernel at most)
 constexpr uint32_t WORK_MAX_BLOCKS = 152u * 64u;

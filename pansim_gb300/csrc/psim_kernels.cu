@@ -562,6 +562,7 @@ __device__ __forceinline__ bool count_agent(const KArgs& k, bool act, uint32_t l
     if (act && loc != NONE && inf > 0.0f) {
         const long long q = __float2ll_rn(inf * PSIM_FIX_SCALE_F);
         atomicAdd(&k.l.sfix[(size_t)variant * L + loc], (unsigned long long)q);
+        atomicAdd(&k.l.sfix_b[(size_t)variant * L + loc], (unsigned long long)q);
         atomicOr(&k.l.smask[loc >> 5], 1u << (loc & 31u));
         mark_hazardous(k, loc);
     }
@@ -594,9 +595,15 @@ __device__ __forceinline__ bool count_agent_delta(const KArgs& k, bool act, uint
         const long long q0 = (loc0 < L && inf0 > 0.0f) ? __float2ll_rn(inf0 * PSIM_FIX_SCALE_F) : 0ll;
         const long long q1 = (loc != NONE && inf > 0.0f) ? __float2ll_rn(inf * PSIM_FIX_SCALE_F) : 0ll;
         if (mv || q0 != q1 || var0 != var) {
-            if (q0) atomicAdd(&k.l.sfix[(size_t)var0 * L + loc0], (unsigned long long)(-q0));
+            // both copies of the step kernel's sums (the next step reads
+            // the other one)
+            if (q0) {
+                atomicAdd(&k.l.sfix[(size_t)var0 * L + loc0], (unsigned long long)(-q0));
+                atomicAdd(&k.l.sfix_b[(size_t)var0 * L + loc0], (unsigned long long)(-q0));
+            }
             if (q1) {
                 atomicAdd(&k.l.sfix[(size_t)var * L + loc], (unsigned long long)q1);
+                atomicAdd(&k.l.sfix_b[(size_t)var * L + loc], (unsigned long long)q1);
                 mark_hazardous(k, loc);
             }
         }
@@ -616,6 +623,7 @@ __device__ __forceinline__ void count_full(const KArgs& k, bool act, uint32_t lo
     if (inf > 0.0f) {
         const long long q = __float2ll_rn(inf * PSIM_FIX_SCALE_F);
         atomicAdd(&k.l.sfix[(size_t)variant * L + loc], (unsigned long long)q);
+        atomicAdd(&k.l.sfix_b[(size_t)variant * L + loc], (unsigned long long)q);
         atomicOr(&k.l.smask[loc >> 5], 1u << (loc & 31u));
         mark_hazardous(k, loc);
     }
@@ -1400,7 +1408,8 @@ __device__ __forceinline__ uint32_t block_scan_excl(uint32_t v, uint32_t* s_red,
 // the set bits of mask word w whose location has a nonzero sum of some
 // variant (returned) and the agents at those locations (*agents); the loads of
 // four set bits at a time are issued together
-__device__ __forceinline__ uint32_t nonzero_sum_bits(const KArgs& k, uint32_t hm, uint32_t w, uint32_t* agents) {
+__device__ __forceinline__ uint32_t nonzero_sum_bits(const KArgs& k, const unsigned long long* sums, uint32_t hm,
+                                                     uint32_t w, uint32_t* agents) {
     const uint32_t L = k.l.n, V = k.m.n_variants;
     uint32_t keep = 0, rest = hm, cnt = 0;
     while (rest) {
@@ -1413,14 +1422,14 @@ __device__ __forceinline__ uint32_t nonzero_sum_bits(const KArgs& k, uint32_t hm
             if (rest) rest &= rest - 1u;
             l[u] = b[u] < 32u ? w * 32u + b[u] : NONE;
             const bool in = l[u] < L;
-            f[u] = in ? k.l.sfix[l[u]] : 0ull;
+            f[u] = in ? sums[l[u]] : 0ull;
             c[u] = in ? k.l.counts[l[u]] : 0u;
         }
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             if (l[u] >= L) continue;
             bool nz = f[u] != 0ull;
-            for (uint32_t v = 1; v < V && !nz; ++v) nz = k.l.sfix[(size_t)v * L + l[u]] != 0ull;
+            for (uint32_t v = 1; v < V && !nz; ++v) nz = sums[(size_t)v * L + l[u]] != 0ull;
             if (nz) {
                 keep |= 1u << b[u];
                 cnt += c[u];
@@ -1448,8 +1457,8 @@ __device__ __forceinline__ uint32_t nonzero_sum_bits(const KArgs& k, uint32_t hm
 // location takes a slot (one returning atomic on the location's cursor, or
 // one per location and warp with agg_slot).  Returns false when a barrier
 // expired.
-__device__ bool phase_rebuild(const KArgs& k, uint32_t* s_red, bool* s_ok, uint32_t tl, uint32_t* s_base,
-                              uint32_t* n_listed) {
+__device__ bool phase_rebuild(const KArgs& k, const unsigned long long* sums, uint32_t* s_red, bool* s_ok,
+                              uint32_t tl, uint32_t* s_base, uint32_t* n_listed) {
     const uint32_t L = k.l.n, N = k.a.n;
     const uint32_t n_words = (L + 31u) >> 5;
     const uint32_t per = (n_words + gridDim.x - 1) / gridDim.x;
@@ -1461,7 +1470,7 @@ __device__ bool phase_rebuild(const KArgs& k, uint32_t* s_red, bool* s_ok, uint3
         uint32_t hm = w < we ? k.l.hmask[w] : 0u;
         uint32_t wc = 0;
         if (hm) {
-            const uint32_t keep = nonzero_sum_bits(k, hm, w, &wc);
+            const uint32_t keep = nonzero_sum_bits(k, sums, hm, w, &wc);
             if (keep != hm) k.l.hmask[w] = keep;
             hm = keep;
         }
@@ -1593,21 +1602,45 @@ __device__ __forceinline__ bool u01_below(uint32_t a, uint32_t b, float p) {
 // replica coefficient kf) from the location's fixed-point sum as the step
 // started: the formula the scans evaluate (psim_hazard_x), so every entry of
 // a location computes the same value.  x receives its argument.
-__device__ __forceinline__ float entry_hazard(const KArgs& k, uint32_t loc, uint32_t v, uint32_t cnt, float wl,
-                                              float kf, float season, uint32_t dt, float* x) {
-    const long long fix = (long long)k.l.sfix[(size_t)v * k.l.n + loc];
+__device__ __forceinline__ float entry_hazard(const KArgs& k, const unsigned long long* sums, uint32_t loc, uint32_t v,
+                                              uint32_t cnt, float wl, float kf, float season, uint32_t dt, float* x) {
+    const long long fix = (long long)sums[(size_t)v * k.l.n + loc];
     *x = 0.0f;
     return fix != 0 ? psim_hazard_x(fix, cnt, kf, wl, season, dt, x) : 0.0f;
 }
 
-// An infection's change of its location's sum, applied after every draw of
-// the step (the ratios of a step come from the sums as the step started):
-// location, infectiousness before and after, variants before and after.
-__device__ __forceinline__ void defer_infection(const KArgs& k, uint32_t loc, float inf0, uint32_t var0, float inf,
-                                                uint32_t var) {
-    const uint32_t j = atomicAdd(&k.l.bar[BAR_INFECTIONS], 1u);
+// The sums of the step kernel are kept twice: step s of the day reads copy
+// s & 1 (sfix, sfix_b) as the step started, and every change of step s goes
+// to the other copy, which step s + 1 reads.  The decisions change both
+// copies (they come after the step's draws); an infection changes the other
+// copy at once and is listed (list s % 3), and step s + 1 applies the list to
+// the copy it does not read, so that copy is complete when step s + 2 reads it
+// (apply_previous_infections).
+__device__ __forceinline__ unsigned long long* sums_read(const KArgs& k, uint32_t step) {
+    return (step & 1u) ? k.l.sfix_b : k.l.sfix;
+}
+__device__ __forceinline__ unsigned long long* sums_next(const KArgs& k, uint32_t step) {
+    return (step & 1u) ? k.l.sfix : k.l.sfix_b;
+}
+__device__ __forceinline__ void add_infection_change(const KArgs& k, unsigned long long* sums, uint32_t loc,
+                                                     float inf0, uint32_t var0, float inf, uint32_t var) {
+    const uint32_t L = k.l.n;
+    const long long q0 = inf0 > 0.0f ? __float2ll_rn(inf0 * PSIM_FIX_SCALE_F) : 0ll;
+    const long long q1 = inf > 0.0f ? __float2ll_rn(inf * PSIM_FIX_SCALE_F) : 0ll;
+    if (q0) atomicAdd(&sums[(size_t)var0 * L + loc], (unsigned long long)(-q0));
+    if (q1) {
+        atomicAdd(&sums[(size_t)var * L + loc], (unsigned long long)q1);
+        mark_hazardous(k, loc);
+    }
+}
+__device__ __forceinline__ void record_infection(const KArgs& k, uint32_t step, uint32_t loc, float inf0,
+                                                 uint32_t var0, float inf, uint32_t var) {
+    add_infection_change(k, sums_next(k, step), loc, inf0, var0, inf, var);
+    const uint32_t list = step % 3u;
+    const uint32_t j = atomicAdd(&k.l.bar[BAR_INFECTIONS + list], 1u);
     if (j < k.a.n)
-        k.l.inf_pending[j] = make_uint4(loc, __float_as_uint(inf0), __float_as_uint(inf), var0 | (var << 8));
+        k.l.inf_pending[(size_t)list * k.a.n + j] =
+            make_uint4(loc, __float_as_uint(inf0), __float_as_uint(inf), var0 | (var << 8));
     else
         atomicOr(k.err, ERR_AGENT_LIST);
 }
@@ -1616,10 +1649,10 @@ __device__ __forceinline__ void defer_infection(const KArgs& k, uint32_t loc, fl
 // of replica rep (count cnt, weight wl).  Returns the sum of min(1, p) over
 // its draws when expected infections are tracked (else 0).  An agent that is
 // infected updates its slot's susceptibility products (read by no other
-// entry) and defers its location's sum change.
-__device__ __forceinline__ double draw_entry(const KArgs& k, uint32_t pos, uint32_t i, uint32_t loc, uint32_t rep,
-                                             uint32_t cnt, float wl, float season, uint32_t t, double* s_grad,
-                                             bool* any_h) {
+// entry) and records its location's sum change for the next steps.
+__device__ __forceinline__ double draw_entry(const KArgs& k, const unsigned long long* sums, uint32_t step,
+                                             uint32_t pos, uint32_t i, uint32_t loc, uint32_t rep, uint32_t cnt,
+                                             float wl, float season, uint32_t t, double* s_grad, bool* any_h) {
     const uint32_t N = k.a.n, V = k.m.n_variants, dt = k.p.time_step;
     const float kf = k.r.k_f[rep];
     const float su0 = k.l.slot_su[pos];
@@ -1631,7 +1664,7 @@ __device__ __forceinline__ double draw_entry(const KArgs& k, uint32_t pos, uint3
     uint32_t var0 = 0;
     for (uint32_t v = 0; v < V; ++v) {
         float x;
-        const float h = entry_hazard(k, loc, v, cnt, wl, kf, season, dt, &x);
+        const float h = entry_hazard(k, sums, loc, v, cnt, wl, kf, season, dt, &x);
         if (!(h > 0.0f)) continue;
         *any_h = true;
         if (!k.r.variant_active[rep * V + v]) continue;
@@ -1671,7 +1704,7 @@ __device__ __forceinline__ double draw_entry(const KArgs& k, uint32_t pos, uint3
         const uint32_t var = inf > 0.0f ? k.a.variant[i] : 0u;
         const long long q0 = inf0 > 0.0f ? __float2ll_rn(inf0 * PSIM_FIX_SCALE_F) : 0ll;
         const long long q1 = inf > 0.0f ? __float2ll_rn(inf * PSIM_FIX_SCALE_F) : 0ll;
-        if (q0 != q1 || var0 != var) defer_infection(k, loc, inf0, var0, inf, var);
+        if (q0 != q1 || var0 != var) record_infection(k, step, loc, inf0, var0, inf, var);
     }
     return term;
 }
@@ -1684,8 +1717,9 @@ __device__ __forceinline__ double draw_entry(const KArgs& k, uint32_t pos, uint3
 // and draws from the agent's Philox stream (seed, agent, t).  The work is the
 // listed entries, spread evenly over the grid, whatever the number of
 // locations.
-__device__ void phase_draw(const KArgs& k, uint32_t t, uint32_t n_listed, float season, double* s_grad,
+__device__ void phase_draw(const KArgs& k, uint32_t step, uint32_t t, uint32_t n_listed, float season, double* s_grad,
                            uint32_t* n_entries, uint32_t* n_hazard) {
+    const unsigned long long* sums = sums_read(k, step);
     const uint32_t L = k.l.n, N = k.a.n;
     const uint32_t stride = gridDim.x * blockDim.x;
     const bool one_rep = k.r.n == 1;
@@ -1708,7 +1742,7 @@ __device__ void phase_draw(const KArgs& k, uint32_t t, uint32_t n_listed, float 
             }
         }
         bool any_h = false;
-        const double term = act ? draw_entry(k, pos, i, loc, rep, cnt, wl, season, t, s_grad, &any_h) : 0.0;
+        const double term = act ? draw_entry(k, sums, step, pos, i, loc, rep, cnt, wl, season, t, s_grad, &any_h) : 0.0;
         entries += act ? 1u : 0u;
         hazard += any_h ? 1u : 0u;
         if (k.track_expected) add_expected_rep(k, act, rep, term);
@@ -1717,47 +1751,20 @@ __device__ void phase_draw(const KArgs& k, uint32_t t, uint32_t n_listed, float 
     *n_hazard += hazard;
 }
 
-// After every draw of the step: the deferred sum changes of the infected
-// agents (called by the last block to finish its draws; the counters start
-// at 0 again for the next step).
-__device__ void apply_infections(const KArgs& k) {
-    const uint32_t L = k.l.n;
-    const uint32_t n = min(k.l.bar[BAR_INFECTIONS], k.a.n);
-    for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
-        const uint4 e = k.l.inf_pending[j];
-        const uint32_t loc = e.x;
-        const float inf0 = __uint_as_float(e.y), inf = __uint_as_float(e.z);
-        const uint32_t var0 = e.w & 0xFFu, var = (e.w >> 8) & 0xFFu;
-        const long long q0 = inf0 > 0.0f ? __float2ll_rn(inf0 * PSIM_FIX_SCALE_F) : 0ll;
-        const long long q1 = inf > 0.0f ? __float2ll_rn(inf * PSIM_FIX_SCALE_F) : 0ll;
-        if (q0) atomicAdd(&k.l.sfix[(size_t)var0 * L + loc], (unsigned long long)(-q0));
-        if (q1) {
-            atomicAdd(&k.l.sfix[(size_t)var * L + loc], (unsigned long long)q1);
-            mark_hazardous(k, loc);
-        }
+// The infections of step s - 1 into the copy of the sums that step s does not
+// read (every thread of the grid takes a share; list (s - 1) % 3, complete
+// since the kernel of step s - 1 ended).  Block 0 also empties list
+// (s + 1) % 3, applied by step s - 1 and next written by step s + 1.
+__device__ __forceinline__ void apply_previous_infections(const KArgs& k, uint32_t step) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) k.l.bar[BAR_INFECTIONS + (step + 1u) % 3u] = 0u;
+    if (step == 0) return;  // the day's first step: the sums are afresh
+    const uint32_t list = (step + 2u) % 3u;
+    const uint32_t n = min(k.l.bar[BAR_INFECTIONS + list], k.a.n);
+    unsigned long long* sums = sums_next(k, step);
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const uint4 e = k.l.inf_pending[(size_t)list * k.a.n + j];
+        add_infection_change(k, sums, e.x, __uint_as_float(e.y), e.w & 0xFFu, __uint_as_float(e.z), (e.w >> 8) & 0xFFu);
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        k.l.bar[BAR_INFECTIONS] = 0u;
-        k.l.bar[BAR_DRAWN] = 0u;
-    }
-}
-
-// Whether this block is the last to finish the step's draws among the blocks
-// that drew entries (the first ceil(n_listed / 256) of the grid; the others
-// infect nobody).  Every thread of the block calls it; the block's draws are
-// ordered before its arrival.
-__device__ __forceinline__ bool last_to_draw(const KArgs& k, uint32_t n_listed, bool* s_flag) {
-    const uint32_t drawing = (uint32_t)min((size_t)gridDim.x, ((size_t)n_listed + blockDim.x - 1) / blockDim.x);
-    if (blockIdx.x >= drawing) return false;  // block-uniform
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        *s_flag = atomicAdd(&k.l.bar[BAR_DRAWN], 1u) == drawing - 1u;
-        if (*s_flag) __threadfence();
-    }
-    __syncthreads();
-    return *s_flag;
 }
 
 // The block's agents that decide at s1, in its own segment of the work list
@@ -1878,7 +1885,7 @@ struct StepShared {
     uint32_t mm[MOVE_MASK_WORDS];
     uint32_t red[32];
     uint32_t cnt, seg, base;
-    bool ok, last;
+    bool ok;
 };
 
 // One timestep of the step kernel (see the section comment); false when a
@@ -1906,16 +1913,17 @@ __device__ __forceinline__ bool step_body(const KArgs& k, uint32_t step, uint32_
         const bool rebuild = csr_decide_from(k, t, moved, force);
         if (rebuild) {
             if (k.prof && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&k.prof[PROF_REBUILDS], 1ull);
-            if (!phase_rebuild(k, sh.red, &sh.ok, tl, &sh.base, &n_listed)) return false;
+            if (!phase_rebuild(k, sums_read(k, step), sh.red, &sh.ok, tl, &sh.base, &n_listed)) return false;
             prof_mark(k, tl + 2);
         }
         // the step's location quarantine writes (decisions of step t)
         if (k.p.quarantine_policy > 1 && q_step == t) merge_quarantine(k);
     }
     if (phases & PH_DRAW) {
+        apply_previous_infections(k, step);
         grad_begin(k, sh.grad);
         uint32_t entries = 0, hazard = 0;
-        phase_draw(k, t, n_listed, season, sh.grad, &entries, &hazard);
+        phase_draw(k, step, t, n_listed, season, sh.grad, &entries, &hazard);
         if (k.prof) {
             entries = __reduce_add_sync(0xffffffffu, entries);
             hazard = __reduce_add_sync(0xffffffffu, hazard);
@@ -1925,8 +1933,6 @@ __device__ __forceinline__ bool step_body(const KArgs& k, uint32_t step, uint32_
             }
         }
         grad_end(k, sh.grad);
-        // the infections' sum changes, once every draw of the step is done
-        if (last_to_draw(k, n_listed, &sh.last)) apply_infections(k);
         prof_mark(k, tl + 3);
     }
     const bool decides = (k.p.enable_curfew && k.p.curfew_begin == s1) || ((mm_word >> (s1 & 31u)) & 1u) != 0;
