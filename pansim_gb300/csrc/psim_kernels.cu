@@ -1645,6 +1645,20 @@ __device__ __forceinline__ void record_infection(const KArgs& k, uint32_t step, 
         atomicOr(k.err, ERR_AGENT_LIST);
 }
 
+// A replica's infection coefficient, seed and first agent.
+struct RepConst {
+    float kf;
+    uint32_t off;
+    unsigned long long seed;
+};
+__device__ __forceinline__ RepConst rep_const(const KArgs& k, uint32_t rep) {
+    RepConst c;
+    c.kf = k.r.k_f[rep];
+    c.off = k.r.agent_off[rep];
+    c.seed = k.r.seed[rep];
+    return c;
+}
+
 // The draws of one agent-list entry: the agent in slot pos at location loc
 // of replica rep (count cnt, weight wl).  Returns the sum of min(1, p) over
 // its draws when expected infections are tracked (else 0).  An agent that is
@@ -1652,12 +1666,12 @@ __device__ __forceinline__ void record_infection(const KArgs& k, uint32_t step, 
 // entry) and records its location's sum change for the next steps.
 __device__ __forceinline__ double draw_entry(const KArgs& k, const unsigned long long* sums, uint32_t step,
                                              uint32_t pos, uint32_t i, uint32_t loc, uint32_t rep, uint32_t cnt,
-                                             float wl, float season, uint32_t t, double* s_grad, bool* any_h) {
+                                             float wl, float su0, const RepConst& rc, float season, uint32_t t,
+                                             double* s_grad, bool* any_h) {
     const uint32_t N = k.a.n, V = k.m.n_variants, dt = k.p.time_step;
-    const float kf = k.r.k_f[rep];
-    const float su0 = k.l.slot_su[pos];
-    const unsigned long long seed = k.r.seed[rep];
-    const uint32_t li = i - k.r.agent_off[rep];
+    const float kf = rc.kf;
+    const unsigned long long seed = rc.seed;
+    const uint32_t li = i - rc.off;
     double term = 0.0;
     bool infected = false;
     float inf0 = 0.0f, sigma = 0.0f;
@@ -1717,21 +1731,44 @@ __device__ __forceinline__ double draw_entry(const KArgs& k, const unsigned long
 // and draws from the agent's Philox stream (seed, agent, t).  The work is the
 // listed entries, spread evenly over the grid, whatever the number of
 // locations.
-__device__ void phase_draw(const KArgs& k, uint32_t step, uint32_t t, uint32_t n_listed, float season, double* s_grad,
-                           uint32_t* n_entries, uint32_t* n_hazard) {
+// First-trip slot of a thread (its slot, agent and variant-0 product),
+// loaded by the step's prologue with the step's words when the step does not
+// rebuild (its slots are then the last rebuild's).
+struct SlotPre {
+    uint32_t loc, i;
+    float su0;
+    bool ok;
+};
+__device__ __forceinline__ SlotPre slot_pre(const KArgs& k, bool draws) {
+    SlotPre p{NONE, NONE, 0.0f, false};
+    const uint32_t pos = blockIdx.x * blockDim.x + threadIdx.x;
+    if (draws && pos < k.a.n) {  // issued before the step's words arrive
+        p.loc = k.l.slot_loc[pos];
+        p.i = k.l.csr_agents[pos];
+        p.su0 = k.l.slot_su[pos];
+        p.ok = true;
+    }
+    return p;
+}
+
+__device__ void phase_draw(const KArgs& k, uint32_t step, uint32_t t, uint32_t n_listed, float season,
+                           const SlotPre& pre, double* s_grad, uint32_t* n_entries, uint32_t* n_hazard) {
     const unsigned long long* sums = sums_read(k, step);
     const uint32_t L = k.l.n, N = k.a.n;
     const uint32_t stride = gridDim.x * blockDim.x;
     const bool one_rep = k.r.n == 1;
+    const RepConst rc0 = rep_const(k, 0);
     uint32_t entries = 0, hazard = 0;
     for (uint32_t base = blockIdx.x * blockDim.x; base < n_listed; base += stride) {  // block-uniform trips
         const uint32_t pos = base + threadIdx.x;
         bool act = pos < n_listed && pos < N;
         uint32_t loc = NONE, i = NONE, rep = 0, cnt = 0;
-        float wl = 0.0f;
+        float wl = 0.0f, su0 = 0.0f;
         if (act) {
-            loc = k.l.slot_loc[pos];
-            i = k.l.csr_agents[pos];
+            const bool first = base == blockIdx.x * blockDim.x && pre.ok;
+            loc = first ? pre.loc : k.l.slot_loc[pos];
+            i = first ? pre.i : k.l.csr_agents[pos];
+            su0 = first ? pre.su0 : k.l.slot_su[pos];
             if (loc >= L || i >= N) {
                 atomicOr(k.err, ERR_AGENT_LIST);
                 act = false;
@@ -1742,7 +1779,10 @@ __device__ void phase_draw(const KArgs& k, uint32_t step, uint32_t t, uint32_t n
             }
         }
         bool any_h = false;
-        const double term = act ? draw_entry(k, sums, step, pos, i, loc, rep, cnt, wl, season, t, s_grad, &any_h) : 0.0;
+        const double term =
+            act ? draw_entry(k, sums, step, pos, i, loc, rep, cnt, wl, su0, one_rep ? rc0 : rep_const(k, rep), season, t,
+                             s_grad, &any_h)
+                : 0.0;
         entries += act ? 1u : 0u;
         hazard += any_h ? 1u : 0u;
         if (k.track_expected) add_expected_rep(k, act, rep, term);
@@ -1761,7 +1801,9 @@ __device__ __forceinline__ void apply_previous_infections(const KArgs& k, uint32
     const uint32_t list = (step + 2u) % 3u;
     const uint32_t n = min(k.l.bar[BAR_INFECTIONS + list], k.a.n);
     unsigned long long* sums = sums_next(k, step);
-    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    // from the grid's last block down: the draws fill the first blocks
+    const uint32_t g = (gridDim.x - 1u - blockIdx.x) * blockDim.x + threadIdx.x;
+    for (uint32_t j = g; j < n; j += gridDim.x * blockDim.x) {
         const uint4 e = k.l.inf_pending[(size_t)list * k.a.n + j];
         add_infection_change(k, sums, e.x, __uint_as_float(e.y), e.w & 0xFFu, __uint_as_float(e.z), (e.w >> 8) & 0xFFu);
     }
@@ -1907,8 +1949,12 @@ __device__ __forceinline__ bool step_body(const KArgs& k, uint32_t step, uint32_
     uint32_t n_listed = k.l.build[5];  // the last rebuild's entries (this step's if it rebuilds)
     const uint32_t s1 = step + 1;
     const uint32_t mm_word = s1 < k.spd ? k.a.move_mask[s1 >> 5] : 0u;
-    if (err0 & ERR_BARRIER) return false;  // an earlier barrier expired
+    // the first-trip slots of the draws, loaded with the words above; used
+    // only when this launch does not rebuild them (moved / force as read)
+    SlotPre pre = slot_pre(k, (phases & PH_DRAW) != 0);
     const uint32_t t = t0 + step;
+    if ((phases & PH_REBUILD) && (moved == t || force == t || force == BUILD_PENDING)) pre.ok = false;
+    if (err0 & ERR_BARRIER) return false;  // an earlier barrier expired
     if (phases & PH_REBUILD) {
         const bool rebuild = csr_decide_from(k, t, moved, force);
         if (rebuild) {
@@ -1923,7 +1969,7 @@ __device__ __forceinline__ bool step_body(const KArgs& k, uint32_t step, uint32_
         apply_previous_infections(k, step);
         grad_begin(k, sh.grad);
         uint32_t entries = 0, hazard = 0;
-        phase_draw(k, step, t, n_listed, season, sh.grad, &entries, &hazard);
+        phase_draw(k, step, t, n_listed, season, pre, sh.grad, &entries, &hazard);
         if (k.prof) {
             entries = __reduce_add_sync(0xffffffffu, entries);
             hazard = __reduce_add_sync(0xffffffffu, hazard);
