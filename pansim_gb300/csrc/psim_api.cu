@@ -657,7 +657,7 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     if ((rc = dalloc(c, &dl.no_work_loc, L))) return bail(rc);
     if ((rc = dalloc(c, &dl.flags, L))) return bail(rc);
     const size_t tiles = (L + 511) / 512 + 1;
-    if ((rc = dalloc(c, &dl.tile_sums, tiles + WORK_MAX_BLOCKS))) return bail(rc);
+    if ((rc = dalloc(c, &dl.tile_sums, tiles))) return bail(rc);
     if ((rc = dalloc(c, &dl.bar, BAR_WORDS))) return bail(rc);
     if ((rc = dalloc(c, &dl.scan_status, tiles))) return bail(rc);
     if ((rc = dalloc(c, &dl.scan_state, 2))) return bail(rc);

@@ -141,11 +141,10 @@ struct DevLocs {
     float* hazard_x;              // [V][n] its argument x = k*S/n*w*season*dt (adjoint mode)
     uint32_t* no_work_loc;
     uint8_t* flags;               // testing flags
-    uint32_t* tile_sums;          // per-tile sums of the histogram (two-pass scan), per-block sums
-                                  // of the step kernel's rebuild
+    uint32_t* tile_sums;          // per-tile sums of the histogram (two-pass scan)
     uint32_t* bar;                // the step kernel's grid barrier ([0] arrivals, [1] generation),
-                                  // per-step decision tickets ([BAR_TICKETS + step]), the
-                                  // deferred infections and the blocks past the draws
+                                  // per-step decision tickets ([BAR_TICKETS + step]), the counts
+                                  // of the three infection lists, the listing counter
     uint32_t* slot_loc;           // [N] the location of each agent-list slot the step kernel listed
     uint4* inf_pending;           // [3][N] the infections of a step (location, infectiousness
                                   // before and after, variants), in list step % 3
