@@ -626,7 +626,7 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
 #define AL(field, cnt) \
     if ((rc = dalloc(c, &da.field, cnt))) return bail(rc);
     AL(hcw, N) AL(rank, N) AL(home, N)
-    AL(worklist, (size_t)N + (size_t)WORK_MAX_BLOCKS * 1024 + 4) AL(seg_count, WORK_MAX_BLOCKS)
+    AL(worklist, (size_t)N + (size_t)WORK_MAX_BLOCKS * 1024 + 4)
     AL(move_mask, MOVE_MASK_WORDS)
 #undef AL
     // locations

@@ -104,7 +104,6 @@ struct DevAgents {
     uint32_t* rank;               // scratch of the canonical CSR ordering
     uint32_t* worklist;           // agents that decide at the next step (k_queue), one segment
                                   // per queue block
-    uint32_t* seg_count;          // queued agents per segment
     uint32_t* home;               // [N] the agent's home: the first home-type entry of its location
                                   // list (findActualLocationForType's first match, no draw),
                                   // computed when the context is made or the home type changes
@@ -143,8 +142,7 @@ struct DevLocs {
     uint8_t* flags;               // testing flags
     uint32_t* tile_sums;          // per-tile sums of the histogram (two-pass scan)
     uint32_t* bar;                // the step kernel's grid barrier ([0] arrivals, [1] generation),
-                                  // per-step decision tickets ([BAR_TICKETS + step]), the counts
-                                  // of the three infection lists, the listing counter
+                                  // the counts of the three infection lists, the listing counter
     uint32_t* slot_loc;           // [N] the location of each agent-list slot the step kernel listed
     uint4* inf_pending;           // [3][N] the infections of a step (location, infectiousness
                                   // before and after, variants), in list step % 3
@@ -326,11 +324,10 @@ constexpr uint32_t PH_REBUILD = 1u, PH_DRAW = 2u, PH_DECIDE = 4u, PH_ALL = 7u;
 void launch_step(const KArgs& k, uint32_t step_in_day, uint32_t phases, cudaStream_t s);
 void launch_steps(const KArgs& k, uint32_t step0, uint32_t nsteps, uint32_t phases, cudaStream_t s);
 void launch_time_shift(uint32_t* a, uint32_t n, uint32_t delta, cudaStream_t s);
-// words of the barrier array: two for the barrier, one ticket per step
-constexpr uint32_t BAR_TICKETS = 2;
-// after the tickets: the infections of the steps in lists 0-2 (step % 3)
-constexpr uint32_t BAR_INFECTIONS = BAR_TICKETS + 1440;
-// the rebuild's listing counter (slots reserved so far)
+// words of the barrier array: two for the barrier, then the counts of the
+// infections of the steps in lists 0-2 (step % 3), then the rebuild's listing
+// counter (slots reserved so far)
+constexpr uint32_t BAR_INFECTIONS = 2;
 constexpr uint32_t BAR_LISTED = BAR_INFECTIONS + 3;
 constexpr uint32_t BAR_WORDS = BAR_LISTED + 1;
 // work-list segments of the decisions (blocks of the queue kernel at most)

@@ -1868,31 +1868,24 @@ __device__ __forceinline__ uint32_t phase_queue(const KArgs& k, uint32_t s1, uin
         }
     }
     __syncthreads();
-    const uint32_t n = *s_cnt;
-    if (threadIdx.x == 0) k.a.seg_count[blockIdx.x] = n;
-    return n;
+    return *s_cnt;
 }
 
-// doMovement of the queued agents for s1: the segments are taken in turn
-// from the step's ticket counter (zeroed at the start of the day graph),
-// then the histogram and sum deltas of the agents that took a new location.
-__device__ void phase_decide(const KArgs& k, uint32_t step, uint32_t cap, uint32_t* s_mm, uint32_t* s_seg) {
+// doMovement of the agents the block queued for s1 (its own segment, whose
+// count the queue left in shared memory: every block starts its decisions at
+// the same barrier, so handing segments out by ticket balanced nothing), then
+// the histogram and sum deltas of the agents that took a new location.
+__device__ void phase_decide(const KArgs& k, uint32_t step, uint32_t cap, uint32_t* s_mm, const uint32_t* s_cnt) {
     const uint32_t s1 = step + 1;
     const StepClock c = step_clock(k, s1);
-    uint32_t* ticket = &k.l.bar[BAR_TICKETS + step];
     bool moved = false;
-    for (;;) {
-        if (threadIdx.x == 0) *s_seg = atomicAdd(ticket, 1u);
-        __syncthreads();
-        const uint32_t sg = *s_seg;
-        __syncthreads();
-        if (sg >= gridDim.x) break;
-        uint32_t n = k.a.seg_count[sg];
+    {
+        uint32_t n = *s_cnt;
         if (n > cap) {
             if (threadIdx.x == 0) atomicOr(k.err, ERR_AGENT_LIST);
             n = 0;
         }
-        const uint32_t* seg = k.a.worklist + (size_t)sg * cap;
+        const uint32_t* seg = k.a.worklist + (size_t)blockIdx.x * cap;
         const uint32_t trips = (n + blockDim.x - 1) / blockDim.x;  // uniform per block
         for (uint32_t it = 0; it < trips; ++it) {
             const uint32_t j = it * blockDim.x + threadIdx.x;
@@ -1926,7 +1919,7 @@ struct StepShared {
     double grad[GRAD_N];
     uint32_t mm[MOVE_MASK_WORDS];
     uint32_t red[32];
-    uint32_t cnt, seg, base;
+    uint32_t cnt, base;
     bool ok;
 };
 
@@ -1992,7 +1985,7 @@ __device__ __forceinline__ bool step_body(const KArgs& k, uint32_t step, uint32_
         prof_mark(k, tl + 4);
         // every draw and every block's queue before any decision
         if (!grid_barrier(k, &sh.ok)) return false;
-        phase_decide(k, step, cap, sh.mm, &sh.seg);
+        phase_decide(k, step, cap, sh.mm, &sh.cnt);
         mask_flush(k, sh.mm);
     }
     prof_mark(k, tl + 5);
