@@ -223,11 +223,13 @@ typedef struct psim_day_stats {
 typedef struct psim_tuning {
     uint32_t agg_count;      /* no effect (the histogram is updated by movers only) */
     uint32_t agg_slot;       /* warp-aggregated agent-list slot atomics */
-    uint32_t blocks_per_sm;  /* 256-thread blocks per SM of the per-agent kernels; 0 = occupancy */
-    uint32_t variant;        /* must be 3: the location-ordered step (agent list rebuilt at the
-                                steps where agents took new locations, draws over the
+    uint32_t blocks_per_sm;  /* 256-thread blocks per SM of the step kernel; 0 = occupancy */
+    uint32_t variant;        /* the day graph's step kernel (agent list rebuilt at the steps
+                                where agents took new locations, draws over the agents at
                                 locations with an infectious agent, decisions of the agents
-                                whose decision step it is) */
+                                whose decision step it is): 3 = one launch per timestep,
+                                4 = one launch for the whole day with a grid barrier between
+                                timesteps (slower on GB300 at 2M and 20M agents) */
     uint32_t scan_items;     /* locations per thread of the scan: 2, 4 or 8 (0 = 8) */
     uint32_t scan_mode;      /* 0 = single pass with decoupled look-back, 1 = tile sums + scan,
                                 2 = tile sums + scan with each thread owning consecutive

@@ -345,12 +345,15 @@ int capture_day_graph(psim_ctx* c) {
     if (me == cudaSuccess && c->profile) me = cudaMemsetAsync(c->d_prof, 0, sizeof(unsigned long long) * PROF_WORDS, c->stream);
     launch_movement(c->k, 0, c->stream);
     // Per timestep one launch of the step kernel (rebuild, draws, decisions
-    // for the next timestep, grid barriers between its phases); the profiled
-    // graph is the same launches with the kernel's timeline stamps.  (One
-    // launch for the whole day, grid barriers between the timesteps,
-    // measured slower: a barrier takes longer than the gap between two
-    // kernel nodes of the graph.)
-    for (uint32_t s = 0; s < c->spd; ++s) launch_step(c->k, s, PH_ALL, c->stream);
+    // for the next timestep, grid barriers between its phases), or with
+    // tuning variant 4 one launch for the whole day with a grid barrier
+    // between timesteps (measured slower on GB300: a barrier takes longer than
+    // the gap between two kernel nodes of the graph); the profiled graph is
+    // the same launches with the kernel's timeline stamps.
+    if (c->k.tune.variant == 4)
+        launch_steps(c->k, 0, c->spd, PH_ALL, c->stream);
+    else
+        for (uint32_t s = 0; s < c->spd; ++s) launch_step(c->k, s, PH_ALL, c->stream);
     // the day's final sums are in the copy its next step would read: with an
     // odd number of steps that is the second one
     if (me == cudaSuccess && (c->spd & 1u))
@@ -365,8 +368,8 @@ int capture_day_graph(psim_ctx* c) {
     e = cudaGraphInstantiate(&c->day_graph, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) return fail(c, PSIM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
-    // movement(0) and one step kernel per timestep
-    c->graph_kernels = 1 + (uint64_t)c->spd;
+    // movement(0) and the step kernel launches
+    c->graph_kernels = 1 + (c->k.tune.variant == 4 ? 1ull : (uint64_t)c->spd);
     c->graph_dirty = false;
     c->prof_valid = false;
     return 0;
@@ -878,7 +881,8 @@ int psim_set_tuning(psim_ctx* c, const psim_tuning* t) {
     c->k.tune.agg_count = t->agg_count ? 1u : 0u;
     c->k.tune.agg_slot = t->agg_slot ? 1u : 0u;
     c->k.tune.blocks_per_sm = t->blocks_per_sm;
-    if (t->variant != 3) return fail(c, PSIM_ERR_ARG, "variant must be 3 (the location-ordered step)");
+    if (t->variant != 3 && t->variant != 4)
+        return fail(c, PSIM_ERR_ARG, "variant must be 3 (a launch per timestep) or 4 (a launch per day)");
     c->k.tune.variant = t->variant;
     if (t->scan_items != 0 && t->scan_items != 2 && t->scan_items != 4 && t->scan_items != 8)
         return fail(c, PSIM_ERR_ARG, "scan_items must be 2, 4 or 8");

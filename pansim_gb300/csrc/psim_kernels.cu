@@ -1993,7 +1993,8 @@ __device__ __forceinline__ bool step_body(const KArgs& k, uint32_t step, uint32_
 }
 
 // The step kernel: timesteps step0 .. step0 + nsteps - 1, a grid barrier
-// between two (the day graph runs a whole day in one launch).
+// between two (the day graph launches it per timestep, or for the whole day
+// with tuning variant 4).
 __global__ void __launch_bounds__(256, 4) k_step(KArgs k, uint32_t step0, uint32_t nsteps, uint32_t phases,
                                                  uint32_t cap) {
     __shared__ StepShared sh;

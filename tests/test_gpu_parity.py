@@ -161,7 +161,9 @@ def test_bounded_wait_reports_error_and_context_survives(gpu_lib):
                                     dict(agg_count=0, agg_slot=0, blocks_per_sm=4, scan_items=8, scan_mode=0),
                                     dict(agg_count=0, agg_slot=0, blocks_per_sm=8, scan_items=4, scan_mode=3),
                                     dict(agg_count=0, agg_slot=1, blocks_per_sm=0, scan_items=8, scan_mode=3),
-                                    dict(agg_count=0, agg_slot=0, blocks_per_sm=8, scan_items=2, scan_mode=3)])
+                                    dict(agg_count=0, agg_slot=0, blocks_per_sm=8, scan_items=2, scan_mode=3),
+                                    dict(agg_count=0, agg_slot=0, blocks_per_sm=0, variant=4),
+                                    dict(agg_count=0, agg_slot=1, blocks_per_sm=2, variant=4)])
 def test_tuning_choices_do_not_change_results(gpu_lib, tuning):
     """Every tuning against the oracle over three days: statistics, state and
     the agent list at the end of each day.  Most steps of a day move nobody
