@@ -139,3 +139,35 @@ def test_autograd_function_and_replica_sum(gpu_lib):
         (e1 ** 2).sum().backward()
         total += t1.grad.numpy()
     np.testing.assert_allclose(g_batch, total, rtol=1e-9, atol=1e-12 * np.abs(total).max())
+
+
+def test_adjoint_identities_at_16_replicas_of_1m_agents(gpu_lib):
+    """The calibration workload, 16 replicas x 1M agents x 28 days, through
+    two identities that hold at any size.  The ratio's argument is
+    proportional to k times the location's weight, so k dL/dk equals
+    sum_j w_j dL/dw_j (every location type with a nonzero weight has a slot);
+    and p is linear in the band susceptibility, so sum_b sigma_b dL/dsigma_b
+    equals sum_{r,d} dL/dE[r, d] E[r, d] when no probability reaches 1: the
+    backward replay accumulates the forward pass's own expected curve."""
+    from pansim_gb300 import snapshot as snp
+    R, n, D = 16, 1_000_000, 28
+    parts = [synth.make_snapshot(n, n // 4, seed=100 + r, pop_seed=0x5EED0005 + r) for r in range(R)]
+    batch = snp.concat(parts, [100 + r for r in range(R)], [3.74e-4] * R)
+    runner = adjoint.CalibrationRunner(batch, D)
+    theta = adjoint.theta_of(batch)
+    runner.set_theta(theta)
+    E = runner.forward()
+    assert E.shape == (R, D) and (E > 0).all()
+    wE = np.random.default_rng(5).uniform(0.5, 1.5, size=E.shape)
+    g = runner.backward(wE)
+    runner.g.close()
+    th = theta.astype(np.float32).astype(np.float64)  # the values the device holds
+    nw = adjoint.N_W
+    k_term = th[0] * g[0]
+    w_term = float((th[1:1 + nw] * g[1:1 + nw]).sum())
+    # every term is positive, so FP64 accumulation errors stay relative
+    assert k_term > 0 and abs(k_term - w_term) <= 1e-8 * k_term, (k_term, w_term)
+    s_term = float((th[1 + nw:] * g[1 + nw:]).sum())
+    e_term = float((wE * E).sum())
+    # p is rounded to FP32 in the forward pass (two roundings per term)
+    assert abs(s_term - e_term) <= 2.5e-7 * e_term, (s_term, e_term)
