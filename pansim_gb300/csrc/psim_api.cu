@@ -593,9 +593,21 @@ int psim_create(int device, const psim_model* m, const psim_agents* a, const psi
     UPA(poss_loc, c->n_poss) UPA(poss_type, c->n_poss)
 #undef UPA
     {
-        std::vector<uint2> packed(c->n_poss);
-        for (size_t j = 0; j < c->n_poss; ++j) packed[j] = make_uint2(a->poss_loc[j], a->poss_type[j]);
-        if ((rc = dupload(c, &da.poss, packed.data(), c->n_poss))) return bail(rc);
+        // the location lists packed for the decisions: 4 bytes per entry when
+        // every location and type fits, else 8
+        bool fits = L < (1u << 26);
+        for (size_t j = 0; fits && j < c->n_poss; ++j) fits = a->poss_loc[j] < (1u << 26) && a->poss_type[j] < 64u;
+        if (fits) {
+            std::vector<uint32_t> packed(c->n_poss);
+            for (size_t j = 0; j < c->n_poss; ++j) packed[j] = a->poss_loc[j] | (uint32_t)a->poss_type[j] << 26;
+            if ((rc = dupload(c, &da.poss4, packed.data(), c->n_poss))) return bail(rc);
+            da.poss = nullptr;
+        } else {
+            std::vector<uint2> packed(c->n_poss);
+            for (size_t j = 0; j < c->n_poss; ++j) packed[j] = make_uint2(a->poss_loc[j], a->poss_type[j]);
+            if ((rc = dupload(c, &da.poss, packed.data(), c->n_poss))) return bail(rc);
+            da.poss4 = nullptr;
+        }
     }
     if (a->precond) {
         if ((rc = dupload(c, &da.precond, a->precond, N))) return bail(rc);

@@ -64,7 +64,10 @@ struct DevAgents {
     const uint32_t* poss_loc;
     const uint8_t* poss_type;
     const uint2* poss;            // the same entries packed: x = location, y = its type (one
-                                  // 8-byte load per entry for the decisions)
+                                  // 8-byte load per entry for the decisions); null when poss4
+                                  // holds them
+    const uint32_t* poss4;        // the same entries in 4 bytes when they fit (locations below
+                                  // 2^26, types below 64): location | type << 26; else null
     const uint16_t* rep;          // replica of each agent
     uint32_t* location;
     uint32_t* move_at;            // absolute timestamp of the agent's next decision: the

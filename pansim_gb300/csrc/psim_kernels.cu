@@ -37,6 +37,15 @@ __device__ __forceinline__ uint32_t loc_closed_until(const KArgs& k, uint32_t l)
 __device__ __forceinline__ uint32_t loc_qu(const KArgs& k, uint32_t l) { return l < k.l.n ? k.l.quarantine_until[l] : 0u; }
 __device__ __forceinline__ uint32_t loc_type(const KArgs& k, uint32_t l) { return l < k.l.n ? k.l.type[l] : NONE; }
 
+// Entry j of the per-agent location lists: x = location, y = its type.
+__device__ __forceinline__ uint2 poss_entry(const KArgs& k, uint32_t j) {
+    if (k.a.poss4) {
+        const uint32_t v = k.a.poss4[j];
+        return make_uint2(v & 0x3FFFFFFu, v >> 26);
+    }
+    return k.a.poss[j];
+}
+
 // RealMovementOps::findActualLocationForType, movementPolicies.h:69-122.
 // f0, f1, f2: the types resolved by first match (home, school, work except in
 // the plan helpers, movementPolicies.h:1073-1080, :1144, :1209-1214).
@@ -45,14 +54,14 @@ __device__ uint32_t find_location_range(const KArgs& k, uint32_t b, uint32_t e, 
                                         psim_stream* rng, uint32_t f0, uint32_t f1, uint32_t f2) {
     if (lt == f0 || lt == f1 || lt == f2) {
         for (uint32_t j = b; j < e; ++j) {
-            const uint2 en = k.a.poss[j];
+            const uint2 en = poss_entry(k, j);
             if (lt == en.y) return en.x;
         }
         return NONE;
     }
     uint32_t counter = 0, pos = 0, first = NONE;
     for (uint32_t j = b; j < e; ++j) {
-        const uint2 en = k.a.poss[j];
+        const uint2 en = poss_entry(k, j);
         if (lt == en.y) {
             if (counter == 0) {
                 pos = j;
@@ -70,7 +79,7 @@ __device__ uint32_t find_location_range(const KArgs& k, uint32_t b, uint32_t e, 
             while (rand_idx == counter2) rand_idx = psim_below(rng, counter);
             counter2 = 0;
             for (uint32_t j = pos; j < e; ++j) {
-                const uint2 en = k.a.poss[j];
+                const uint2 en = poss_entry(k, j);
                 if (lt == en.y) {
                     if (counter2 == rand_idx) {
                         if (retry && loc_open(k, en.x) == 0) {

@@ -139,6 +139,25 @@ def test_replicas_batch_equals_single(gpu_lib):
         assert stats_rows(ob_.run_day(d)) == stats_rows(gb2.run_day(d))
 
 
+def test_location_type_ids_beyond_the_packed_lists(gpu_lib):
+    """The per-agent location lists go to the device in 4-byte entries when
+    every type id is below 64 and every location below 2^26, else in 8-byte
+    entries: the shop type renumbered 7 -> 100 wherever it appears takes the
+    8-byte form and gives the oracle's days bit for bit."""
+    s_cpu = small_snapshot(n=12000, locs=3000, initial_infected_frac=0.02)
+    shop, new = int(s_cpu.params["public_type"]), 100
+    for arr in (s_cpu.locs["type"], s_cpu.agents["poss_type"], s_cpu.model["ev_loc_type"]):
+        assert (arr == shop).any()
+        arr[arr == shop] = new
+    s_cpu.params["public_type"] = new
+    s_gpu = s_cpu.copy()
+    o, g = ob.Oracle(s_cpu), GpuSim(s_gpu)
+    for d in range(3):
+        assert stats_rows(o.run_day(d)) == stats_rows(g.run_day(d)), d
+    g.download()
+    assert diff_state(s_cpu, s_gpu) == []
+
+
 def test_bounded_wait_reports_error_and_context_survives(gpu_lib):
     s = small_snapshot(n=2000, locs=500)
     g = GpuSim(s)
